@@ -1,0 +1,1246 @@
+// cmdg oracle — TEST INFRASTRUCTURE ONLY.
+//
+// A plain-C++ FP64 restatement of ClimateMachine.jl's DG spectral-element
+// tendency for the dry AtmosModel (DGModel volume/interface kernels, gradient
+// and diffusive passes), its LSRK54CarpenterKennedy integrator, the brick
+// geometry it runs on and the weighted reductions used to report errors.
+//
+// It is the checker for the CUDA library: only tests/, __graft_entry__.smoke()
+// and bench.py's CPU-baseline leg may load it.  Nothing in the product path
+// links, loads or calls this file.
+//
+// Parity status: pinned.  The isentropic-vortex golden errors of
+// test/Numerics/DGMethods/Euler/isentropicvortex.jl:105-106 and the LSRK54
+// convergence order of test/Numerics/ODESolvers/ode_tests_convergence.jl:41
+// are reproduced by tests/test_oracle_pins.py.
+//
+// Every function cites the reference file:line (paths relative to the
+// ClimateMachine.jl project root) whose algorithm it restates.  Third-party
+// arithmetic that lives outside the reference tree is restated from its
+// published definitions:
+//   * Thermodynamics.jl 0.5.1  — PhaseDry T(e_int), p, c_s, h_tot, theta_v
+//   * CLIMAParameters.jl 0.2.0 — R_d, cp_d, cv_d, T_0, grav, MSLP, ... (set by
+//                                 the caller through om_params)
+//   * GaussQuadrature.jl 0.5.5 — Legendre-Gauss-Lobatto nodes and weights
+//   * DoubleFloats.jl 1.1.18   — compensated (double-double) weighted sums
+//
+// Layouts follow the reference exactly (all column-major as in Julia):
+//   Q, dQ   : (Np, nstate, nelem)           MPIStateArrays.jl:98
+//   vgeo    : (Np, 16, nelem)               Grids.jl:76-125
+//   sgeo    : (5, Nfp, 6, nelem)            Grids.jl:129-146
+//   vmap-/+ : (Nfp, 6, nelem), 0-based      Grids.jl:559-638
+// Element ordering is "stacked": the vertical index is fastest, then x, then
+// y (columns contiguous, like StackedBrickTopology, Topologies.jl:632).
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+extern "C" {
+
+// ----------------------------------------------------------------------------
+// Public parameter blocks (mirrored by oracle/oracle.py)
+// ----------------------------------------------------------------------------
+typedef struct {
+    int N;                    // polynomial order (same in all directions)
+    int ne[3];                // elements in x, y, z
+    double lo[3], hi[3];      // domain extents
+    int periodic[3];          // 1 = periodic in that direction
+    int bc_lo[3], bc_hi[3];   // boundary tags for non-periodic faces (>0)
+} om_brick;
+
+typedef struct {
+    // CLIMAParameters.jl 0.2.0 planet / SGS constants
+    double R_d, cp_d, cv_d, T_0, grav, MSLP, inv_Pr_turb;
+    int numflux;        // 0 = Rusanov (NumericalFluxes.jl:219-285), 1 = central (:298-340)
+    int orientation;    // 0 = NoOrientation, 1 = FlatOrientation (Orientations.jl:138-150, 246-258)
+    int gravity;        // 1 = Gravity() source (tendencies_momentum.jl:60-72)
+    int ref_state;      // 0 = NoReferenceState, 1 = HydrostaticState (ref_state.jl:36-60)
+    int subtract_off;   // HydrostaticState.subtract_off
+    int profile;        // 0 = Isothermal, 1 = DryAdiabatic (Thermodynamics.TemperatureProfiles)
+    double T_surface;   // isothermal T_virt or dry-adiabatic T_surface
+    double T_min;       // dry-adiabatic T_min_ref
+    int turbulence;     // 0 = inviscid, 1 = ConstantDynamicViscosity, 2 = SmagorinskyLilly
+    double rho_nu;      // dynamic viscosity for turbulence==1
+    int with_divergence;// WithDivergence for turbulence==1
+    double C_smag;      // Smagorinsky coefficient for turbulence==2
+} om_params;
+
+}  // extern "C"
+
+namespace {
+
+constexpr int NVGEO = 16;
+enum { XI1X1 = 0, XI2X1, XI3X1, XI1X2, XI2X2, XI3X2, XI1X3, XI2X3, XI3X3, VM, VMI, VMH, VX1, VX2, VX3, VJCV };
+constexpr int NSGEO = 5;
+enum { SN1 = 0, SN2, SN3, SSM, SVMI };
+// auxiliary fields per node (own ordering; content as AtmosModel.jl:465-481)
+enum { AX = 0, AY, AZ, APHI, AGPX, AGPY, AGPZ, ARHO_REF, AP_REF, AT_REF, ARHOE_REF, ATHV, AAIRT, ADELTA, NAUX };
+constexpr int NS = 5;   // rho, rhou(3), rhoe
+
+struct Model {
+    om_brick mesh;
+    om_params prm;
+    int N, Nq, Np, Nfp;
+    int64_t nelem;
+    std::vector<double> xi, omega, D;       // D[j + Nq*k] = D[j,k] (column-major)
+    std::vector<double> vgeo, sgeo, aux;
+    std::vector<int64_t> vmapM, vmapP;
+    std::vector<int> elemtobndy;
+    std::vector<int64_t> elemtoelem;
+    int ngf;                                 // gradient-flux words per node
+    std::vector<double> gradflux;            // (Np, ngf, nelem)
+};
+
+// ----------------------------------------------------------------------------
+// Legendre-Gauss-Lobatto points and weights.
+// Elements.jl:11-14 calls GaussQuadrature.legendre(T, N+1, both); restated as
+// Newton iteration on (1-x^2) P_N'(x) with the Legendre three-term recurrence,
+// weights 2 / (N (N+1) P_N(x)^2), nodes ascending from -1 to 1.
+// ----------------------------------------------------------------------------
+void lgl(int N, std::vector<double>& x, std::vector<double>& w) {
+    int Nq = N + 1;
+    x.assign(Nq, 0.0);
+    w.assign(Nq, 0.0);
+    std::vector<long double> xl(Nq), P(Nq * Nq);
+    for (int i = 0; i < Nq; ++i) xl[i] = -cosl(3.14159265358979323846264338327950288L * i / N);
+    for (int it = 0; it < 100; ++it) {
+        long double maxd = 0;
+        for (int i = 0; i < Nq; ++i) {
+            long double p0 = 1, p1 = xl[i], pm = 0;
+            // P_N and P_{N-1} at x
+            long double Pn = p1, Pnm1 = p0;
+            if (N == 1) { Pn = p1; Pnm1 = p0; }
+            for (int k = 2; k <= N; ++k) {
+                pm = ((2 * k - 1) * xl[i] * p1 - (k - 1) * p0) / k;
+                p0 = p1; p1 = pm;
+                Pn = p1; Pnm1 = p0;
+            }
+            long double dx = (xl[i] * Pn - Pnm1) / (Nq * Pn);
+            xl[i] -= dx;
+            maxd = std::max(maxd, fabsl(dx));
+        }
+        if (maxd < 1e-30L) break;
+    }
+    for (int i = 0; i < Nq; ++i) {
+        long double s = 0.5L * (xl[i] - xl[N - i]);
+        long double p0 = 1, p1 = s, Pn = s;
+        for (int k = 2; k <= N; ++k) {
+            long double pm = ((2 * k - 1) * s * p1 - (k - 1) * p0) / k;
+            p0 = p1; p1 = pm; Pn = p1;
+        }
+        x[i] = (double)s;
+        w[i] = (double)(2.0L / ((long double)N * Nq * Pn * Pn));
+    }
+    x[0] = -1.0; x[N] = 1.0;
+    if (N % 2 == 0) x[N / 2] = 0.0;
+}
+
+// Barycentric weights and spectral differentiation matrix, Elements.jl:34-82.
+void spectral_derivative(const std::vector<double>& r, std::vector<double>& D) {
+    int Np = (int)r.size();
+    std::vector<double> wb(Np, 1.0);
+    for (int j = 0; j < Np; ++j) {
+        for (int i = 0; i < Np; ++i)
+            if (i != j) wb[j] = wb[j] * (r[j] - r[i]);
+        wb[j] = 1.0 / wb[j];
+    }
+    D.assign(Np * Np, 0.0);
+    for (int k = 0; k < Np; ++k)
+        for (int j = 0; j < Np; ++j) {
+            if (k == j) {
+                for (int l = 0; l < Np; ++l)
+                    if (l != k) D[j + Np * k] = D[j + Np * k] + 1.0 / (r[k] - r[l]);
+            } else {
+                D[j + Np * k] = (wb[k] / wb[j]) / (r[j] - r[k]);
+            }
+        }
+}
+
+inline double Dm(const Model& m, int j, int k) { return m.D[j + m.Nq * k]; }
+inline double& VG(Model& m, int64_t e, int f, int n) { return m.vgeo[(e * NVGEO + f) * m.Np + n]; }
+inline double VGc(const Model& m, int64_t e, int f, int n) { return m.vgeo[(e * NVGEO + f) * m.Np + n]; }
+inline double& SG(Model& m, int64_t e, int face, int n, int s) { return m.sgeo[((e * 6 + face) * m.Nfp + n) * NSGEO + s]; }
+inline double SGc(const Model& m, int64_t e, int face, int n, int s) { return m.sgeo[((e * 6 + face) * m.Nfp + n) * NSGEO + s]; }
+inline double& AUX(Model& m, int64_t e, int a, int n) { return m.aux[(e * NAUX + a) * m.Np + n]; }
+inline double AUXc(const Model& m, int64_t e, int a, int n) { return m.aux[(e * NAUX + a) * m.Np + n]; }
+
+// Julia-style range(a, stop=b, length=n+1) value i (correctly rounded blend).
+double range_value(double a, double b, int n, int i) {
+    long double v = ((long double)a * (n - i) + (long double)b * i) / n;
+    return (double)v;
+}
+
+// Face node masks, Grids.jl:580-597: fmask[f][n] -> volume node index.
+void face_masks(int Nq, std::vector<std::vector<int>>& fmask) {
+    fmask.assign(6, std::vector<int>(Nq * Nq));
+    for (int b = 0; b < Nq; ++b)
+        for (int a = 0; a < Nq; ++a) {
+            int n = a + Nq * b;
+            fmask[0][n] = 0 + Nq * (a + Nq * b);           // i = 1, (j, k)
+            fmask[1][n] = (Nq - 1) + Nq * (a + Nq * b);    // i = Nq
+            fmask[2][n] = a + Nq * (0 + Nq * b);           // j = 1, (i, k)
+            fmask[3][n] = a + Nq * ((Nq - 1) + Nq * b);    // j = Nq
+            fmask[4][n] = a + Nq * (b + Nq * 0);           // k = 1, (i, j)
+            fmask[5][n] = a + Nq * (b + Nq * (Nq - 1));    // k = Nq
+        }
+}
+
+// ----------------------------------------------------------------------------
+// Brick topology + grid.
+//  * element corners and trilinear blend: Metrics.jl:85-121 (creategrid!)
+//  * connectivity / boundary tags: Topologies.jl:470-545, BrickMesh.jl:827,1096
+//  * vmap-/+ (orientation 1 only on a brick): Grids.jl:559-638
+//  * dx/dxi by D: Metrics.jl:215-270; curl-invariant metric, J, normals,
+//    surface Jacobian: Metrics.jl:431-724; M, MI, sM, vMI: Grids.jl:1068-1096
+// ----------------------------------------------------------------------------
+int64_t elem_index(const om_brick& b, int ix, int iy, int iz) {
+    return (int64_t)iz + (int64_t)b.ne[2] * ((int64_t)ix + (int64_t)b.ne[0] * iy);
+}
+
+void build_geometry(Model& m) {
+    const om_brick& b = m.mesh;
+    int N = m.N, Nq = m.Nq, Np = m.Np, Nfp = m.Nfp;
+    int64_t nelem = m.nelem;
+    m.vgeo.assign((size_t)nelem * NVGEO * Np, 0.0);
+    m.sgeo.assign((size_t)nelem * 6 * Nfp * NSGEO, 0.0);
+    m.vmapM.assign((size_t)nelem * 6 * Nfp, 0);
+    m.vmapP.assign((size_t)nelem * 6 * Nfp, 0);
+    m.elemtobndy.assign((size_t)nelem * 6, 0);
+    m.elemtoelem.assign((size_t)nelem * 6, 0);
+    std::vector<std::vector<int>> fmask;
+    face_masks(Nq, fmask);
+    const std::vector<double>& xi = m.xi;
+
+    // connectivity
+    for (int iy = 0; iy < b.ne[1]; ++iy)
+        for (int ix = 0; ix < b.ne[0]; ++ix)
+            for (int iz = 0; iz < b.ne[2]; ++iz) {
+                int64_t e = elem_index(b, ix, iy, iz);
+                int idx[3] = {ix, iy, iz};
+                for (int f = 0; f < 6; ++f) {
+                    int d = f / 2, side = f % 2;
+                    int nb[3] = {idx[0], idx[1], idx[2]};
+                    nb[d] += side ? 1 : -1;
+                    int64_t e2 = e;
+                    int f2 = f;
+                    int tag = 0;
+                    if (nb[d] < 0 || nb[d] >= b.ne[d]) {
+                        if (b.periodic[d]) {
+                            nb[d] = (nb[d] + b.ne[d]) % b.ne[d];
+                            e2 = elem_index(b, nb[0], nb[1], nb[2]);
+                            f2 = f ^ 1;
+                        } else {
+                            tag = side ? b.bc_hi[d] : b.bc_lo[d];
+                            if (tag <= 0) tag = 1;
+                        }
+                    } else {
+                        e2 = elem_index(b, nb[0], nb[1], nb[2]);
+                        f2 = f ^ 1;
+                    }
+                    m.elemtobndy[e * 6 + f] = tag;
+                    m.elemtoelem[e * 6 + f] = e2;
+                    for (int n = 0; n < Nfp; ++n) {
+                        m.vmapM[(e * 6 + f) * Nfp + n] = e * Np + fmask[f][n];
+                        m.vmapP[(e * 6 + f) * Nfp + n] = e2 * Np + fmask[f2][n];
+                    }
+                }
+            }
+
+    std::vector<double> xg[3];
+    for (int d = 0; d < 3; ++d) {
+        xg[d].resize(b.ne[d] + 1);
+        for (int i = 0; i <= b.ne[d]; ++i) xg[d][i] = range_value(b.lo[d], b.hi[d], b.ne[d], i);
+    }
+
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < nelem; ++e) {
+        int64_t iz = e % b.ne[2];
+        int64_t ix = (e / b.ne[2]) % b.ne[0];
+        int64_t iy = e / ((int64_t)b.ne[2] * b.ne[0]);
+        double c[3][8];
+        for (int v = 0; v < 8; ++v) {
+            int bi = v & 1, bj = (v >> 1) & 1, bk = (v >> 2) & 1;
+            c[0][v] = xg[0][ix + bi];
+            c[1][v] = xg[1][iy + bj];
+            c[2][v] = xg[2][iz + bk];
+        }
+        std::vector<double> X[3], Xr[3][3];
+        for (int d = 0; d < 3; ++d) {
+            X[d].assign(Np, 0.0);
+            for (int q = 0; q < 3; ++q) Xr[d][q].assign(Np, 0.0);
+        }
+        // trilinear blend, Metrics.jl:100-118
+        for (int d = 0; d < 3; ++d)
+            for (int k = 0; k < Nq; ++k)
+                for (int j = 0; j < Nq; ++j)
+                    for (int i = 0; i < Nq; ++i) {
+                        double a1 = 1 - xi[i], b1 = 1 + xi[i];
+                        double a2 = 1 - xi[j], b2 = 1 + xi[j];
+                        double a3 = 1 - xi[k], b3 = 1 + xi[k];
+                        X[d][i + Nq * (j + Nq * k)] =
+                            (a1 * a2 * a3 * c[d][0] + b1 * a2 * a3 * c[d][1] + a1 * b2 * a3 * c[d][2] +
+                             b1 * b2 * a3 * c[d][3] + a1 * a2 * b3 * c[d][4] + b1 * a2 * b3 * c[d][5] +
+                             a1 * b2 * b3 * c[d][6] + b1 * b2 * b3 * c[d][7]) / 8;
+                    }
+        // dx/dxi, Metrics.jl:246-266
+        for (int k = 0; k < Nq; ++k)
+            for (int j = 0; j < Nq; ++j)
+                for (int i = 0; i < Nq; ++i) {
+                    int ijk = i + Nq * (j + Nq * k);
+                    for (int d = 0; d < 3; ++d) {
+                        for (int n = 0; n < Nq; ++n) Xr[d][0][ijk] += Dm(m, i, n) * X[d][n + Nq * (j + Nq * k)];
+                        for (int n = 0; n < Nq; ++n) Xr[d][1][ijk] += Dm(m, j, n) * X[d][i + Nq * (n + Nq * k)];
+                        for (int n = 0; n < Nq; ++n) Xr[d][2][ijk] += Dm(m, k, n) * X[d][i + Nq * (j + Nq * n)];
+                    }
+                }
+        // curl-invariant metric terms, Metrics.jl:490-606
+        std::vector<double> J(Np), yz[3], zx[3], xy[3];
+        for (int q = 0; q < 3; ++q) { yz[q].resize(Np); zx[q].resize(Np); xy[q].resize(Np); }
+        double* x1 = X[0].data(); double* x2 = X[1].data(); double* x3 = X[2].data();
+        for (int n = 0; n < Np; ++n) {
+            double x1r = Xr[0][0][n], x1s = Xr[0][1][n], x1t = Xr[0][2][n];
+            double x2r = Xr[1][0][n], x2s = Xr[1][1][n], x2t = Xr[1][2][n];
+            double x3r = Xr[2][0][n], x3s = Xr[2][1][n], x3t = Xr[2][2][n];
+            VG(m, e, VJCV, n) = std::hypot(std::hypot(x1t, x2t), x3t);
+            J[n] = x1r * (x2s * x3t - x3s * x2t) + x2r * (x3s * x1t - x1s * x3t) + x3r * (x1s * x2t - x2s * x1t);
+            yz[0][n] = x2[n] * x3r - x3[n] * x2r; yz[1][n] = x2[n] * x3s - x3[n] * x2s; yz[2][n] = x2[n] * x3t - x3[n] * x2t;
+            zx[0][n] = x3[n] * x1r - x1[n] * x3r; zx[1][n] = x3[n] * x1s - x1[n] * x3s; zx[2][n] = x3[n] * x1t - x1[n] * x3t;
+            xy[0][n] = x1[n] * x2r - x2[n] * x1r; xy[1][n] = x1[n] * x2s - x2[n] * x1s; xy[2][n] = x1[n] * x2t - x2[n] * x1t;
+        }
+        for (int k = 0; k < Nq; ++k)
+            for (int j = 0; j < Nq; ++j)
+                for (int i = 0; i < Nq; ++i) {
+                    int ijk = i + Nq * (j + Nq * k);
+                    double g[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // xi1x1 xi2x1 xi3x1 xi1x2 ... (vgeo order)
+                    for (int n = 0; n < Nq; ++n) {
+                        int nj = n + Nq * (j + Nq * k);
+                        g[XI2X1] -= Dm(m, i, n) * yz[2][nj];
+                        g[XI3X1] += Dm(m, i, n) * yz[1][nj];
+                        g[XI2X2] -= Dm(m, i, n) * zx[2][nj];
+                        g[XI3X2] += Dm(m, i, n) * zx[1][nj];
+                        g[XI2X3] -= Dm(m, i, n) * xy[2][nj];
+                        g[XI3X3] += Dm(m, i, n) * xy[1][nj];
+                    }
+                    for (int n = 0; n < Nq; ++n) {
+                        int in = i + Nq * (n + Nq * k);
+                        g[XI1X1] += Dm(m, j, n) * yz[2][in];
+                        g[XI3X1] -= Dm(m, j, n) * yz[0][in];
+                        g[XI1X2] += Dm(m, j, n) * zx[2][in];
+                        g[XI3X2] -= Dm(m, j, n) * zx[0][in];
+                        g[XI1X3] += Dm(m, j, n) * xy[2][in];
+                        g[XI3X3] -= Dm(m, j, n) * xy[0][in];
+                    }
+                    for (int n = 0; n < Nq; ++n) {
+                        int ij = i + Nq * (j + Nq * n);
+                        g[XI1X1] -= Dm(m, k, n) * yz[1][ij];
+                        g[XI2X1] += Dm(m, k, n) * yz[0][ij];
+                        g[XI1X2] -= Dm(m, k, n) * zx[1][ij];
+                        g[XI2X2] += Dm(m, k, n) * zx[0][ij];
+                        g[XI1X3] -= Dm(m, k, n) * xy[1][ij];
+                        g[XI2X3] += Dm(m, k, n) * xy[0][ij];
+                    }
+                    double JI2 = 1 / (2 * J[ijk]);
+                    for (int q = 0; q < 9; ++q) VG(m, e, q, ijk) = g[q] * JI2;
+                    VG(m, e, VX1, ijk) = x1[ijk];
+                    VG(m, e, VX2, ijk) = x2[ijk];
+                    VG(m, e, VX3, ijk) = x3[ijk];
+                }
+        // surface terms, Metrics.jl:660-722 (uses J before the omega scaling)
+        for (int f = 0; f < 6; ++f) {
+            int d = f / 2;
+            double sgn = (f % 2) ? 1.0 : -1.0;
+            int c1 = (d == 0) ? XI1X1 : (d == 1) ? XI2X1 : XI3X1;
+            int c2 = (d == 0) ? XI1X2 : (d == 1) ? XI2X2 : XI3X2;
+            int c3 = (d == 0) ? XI1X3 : (d == 1) ? XI2X3 : XI3X3;
+            for (int n = 0; n < Nfp; ++n) {
+                int v = fmask[f][n];
+                double n1 = sgn * J[v] * VG(m, e, c1, v);
+                double n2 = sgn * J[v] * VG(m, e, c2, v);
+                double n3 = sgn * J[v] * VG(m, e, c3, v);
+                double sJ = std::hypot(std::hypot(n1, n2), n3);
+                SG(m, e, f, n, SN1) = n1 / sJ;
+                SG(m, e, f, n, SN2) = n2 / sJ;
+                SG(m, e, f, n, SN3) = n3 / sJ;
+                SG(m, e, f, n, SSM) = sJ;
+            }
+        }
+        // mass matrix and surface mass, Grids.jl:1068-1096
+        for (int k = 0; k < Nq; ++k)
+            for (int j = 0; j < Nq; ++j)
+                for (int i = 0; i < Nq; ++i) {
+                    int ijk = i + Nq * (j + Nq * k);
+                    double Mw = m.omega[k] * m.omega[j] * m.omega[i];
+                    VG(m, e, VM, ijk) = J[ijk] * Mw;
+                    VG(m, e, VMI, ijk) = 1 / VG(m, e, VM, ijk);
+                    VG(m, e, VMH, ijk) = 0;  // diagnostics only
+                }
+        for (int f = 0; f < 6; ++f)
+            for (int bb = 0; bb < Nq; ++bb)
+                for (int a = 0; a < Nq; ++a) {
+                    int n = a + Nq * bb;
+                    SG(m, e, f, n, SVMI) = VG(m, e, VMI, fmask[f][n]);
+                    SG(m, e, f, n, SSM) *= m.omega[a] * m.omega[bb];
+                }
+        (void)N;
+    }
+}
+
+// ----------------------------------------------------------------------------
+// Thermodynamics (Thermodynamics.jl 0.5.1, dry air), as called from
+// Atmos/Model/thermo_states.jl:67-77 and moisture.jl:32-45.
+// ----------------------------------------------------------------------------
+struct Thermo {
+    double e_int, T, p;
+};
+
+// internal energy from the conserved state (moisture.jl:35-45)
+inline double internal_energy(double rho, double rhoe, const double rhou[3], double Phi) {
+    double ke2 = rhou[0] * rhou[0] + rhou[1] * rhou[1] + rhou[2] * rhou[2];
+    return (1 / rho) * (rhoe - ke2 / (2 * rho)) - Phi;
+}
+
+inline Thermo phase_dry(const om_params& p, double rho, double rhoe, const double rhou[3], double Phi) {
+    Thermo t;
+    t.e_int = internal_energy(rho, rhoe, rhou, Phi);
+    t.T = p.T_0 + t.e_int / p.cv_d;
+    t.p = p.R_d * rho * t.T;
+    return t;
+}
+
+inline double soundspeed(const om_params& p, double T) { return std::sqrt(p.cp_d / p.cv_d * p.R_d * T); }
+
+// theta_v for dry air: T / (p / MSLP)^(R_d / cp_d)
+inline double virtual_pottemp(const om_params& p, double T, double pres) {
+    return (p.R_d / p.R_d) * (T / std::pow(pres / p.MSLP, p.R_d / p.cp_d));
+}
+
+// ----------------------------------------------------------------------------
+// Temperature profiles (Thermodynamics.TemperatureProfiles 0.5.1) and the
+// hydrostatic reference state, ref_state.jl:70-141, 143-185, 204-263.
+// ----------------------------------------------------------------------------
+void profile(const om_params& p, double z, double& Tv, double& pres) {
+    if (p.profile == 0) {  // IsothermalProfile
+        Tv = p.T_surface;
+        pres = p.MSLP * std::exp(-z * p.grav / (p.R_d * Tv));
+    } else {               // DryAdiabaticProfile
+        double Gamma = p.grav / p.cp_d;
+        Tv = std::max(p.T_surface - Gamma * z, p.T_min);
+        pres = std::pow(Tv / p.T_surface, p.grav / (p.R_d * Gamma));
+        if (Tv == p.T_min) {
+            double z_top = (p.T_surface - p.T_min) / Gamma;
+            double H_min = p.R_d * p.T_min / p.grav;
+            pres *= std::exp(-(z - z_top) / H_min);
+        }
+        pres *= p.MSLP;
+    }
+}
+
+// Element-local derivative of an aux field, DGModel_kernels.jl:3097-3232
+// (auxiliary_field_gradient!, SpaceDiscretization.jl:391-483): horizontal
+// pass then vertical pass added.
+void aux_field_gradient(Model& m, int ain, int aout) {
+    int Nq = m.Nq;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m.nelem; ++e) {
+        for (int k = 0; k < Nq; ++k)
+            for (int j = 0; j < Nq; ++j)
+                for (int i = 0; i < Nq; ++i) {
+                    int ijk = i + Nq * (j + Nq * k);
+                    double G1 = 0, G2 = 0, G3 = 0;
+                    for (int n = 0; n < Nq; ++n) {
+                        G1 += Dm(m, i, n) * AUX(m, e, ain, n + Nq * (j + Nq * k));
+                        G2 += Dm(m, j, n) * AUX(m, e, ain, i + Nq * (n + Nq * k));
+                    }
+                    for (int n = 0; n < Nq; ++n) G3 += Dm(m, k, n) * AUX(m, e, ain, i + Nq * (j + Nq * n));
+                    double gh[3], gv[3];
+                    gh[0] = VG(m, e, XI1X1, ijk) * G1 + VG(m, e, XI2X1, ijk) * G2;
+                    gh[1] = VG(m, e, XI1X2, ijk) * G1 + VG(m, e, XI2X2, ijk) * G2;
+                    gh[2] = VG(m, e, XI1X3, ijk) * G1 + VG(m, e, XI2X3, ijk) * G2;
+                    gv[0] = VG(m, e, XI3X1, ijk) * G3;
+                    gv[1] = VG(m, e, XI3X2, ijk) * G3;
+                    gv[2] = VG(m, e, XI3X3, ijk) * G3;
+                    for (int q = 0; q < 3; ++q) AUX(m, e, aout + q, ijk) = gh[q] + gv[q];
+                }
+    }
+}
+
+// ∇reference_pressure: DG tendency of PressureGradientModel (flux = -p I,
+// central flux, boundary state = interior), ref_state.jl:204-263, evaluated
+// with the volume/interface kernels of DGModel_kernels.jl:64-548, 588-901.
+void ref_pressure_gradient(Model& m, std::vector<double>& gp /* (Np,3,nelem) */) {
+    int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp;
+    gp.assign((size_t)m.nelem * 3 * Np, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m.nelem; ++e) {
+        std::vector<double> F1(Np * 3), F2(Np * 3), F3(Np * 3);
+        for (int n = 0; n < Np; ++n) {
+            double p = AUX(m, e, AP_REF, n);
+            double M = VG(m, e, VM, n);
+            // flux[:, s] = -p * e_s  -> F[d, s] = -p delta_ds
+            for (int s = 0; s < 3; ++s) {
+                double Fd[3] = {0, 0, 0};
+                Fd[s] = -p;
+                F1[n * 3 + s] = M * (VG(m, e, XI1X1, n) * Fd[0] + VG(m, e, XI1X2, n) * Fd[1] + VG(m, e, XI1X3, n) * Fd[2]);
+                F2[n * 3 + s] = M * (VG(m, e, XI2X1, n) * Fd[0] + VG(m, e, XI2X2, n) * Fd[1] + VG(m, e, XI2X3, n) * Fd[2]);
+                F3[n * 3 + s] = M * (VG(m, e, XI3X1, n) * Fd[0] + VG(m, e, XI3X2, n) * Fd[1] + VG(m, e, XI3X3, n) * Fd[2]);
+            }
+        }
+        for (int k = 0; k < Nq; ++k)
+            for (int j = 0; j < Nq; ++j)
+                for (int i = 0; i < Nq; ++i) {
+                    int ijk = i + Nq * (j + Nq * k);
+                    double MI = VG(m, e, VMI, ijk);
+                    for (int s = 0; s < 3; ++s) {
+                        double th = 0, tv = 0;
+                        for (int n = 0; n < Nq; ++n) {
+                            th += MI * Dm(m, n, i) * F1[(n + Nq * (j + Nq * k)) * 3 + s];
+                            th += MI * Dm(m, n, j) * F2[(i + Nq * (n + Nq * k)) * 3 + s];
+                        }
+                        for (int n = 0; n < Nq; ++n) tv += MI * Dm(m, n, k) * F3[(i + Nq * (j + Nq * n)) * 3 + s];
+                        gp[(e * 3 + s) * Np + ijk] = th + tv;
+                    }
+                }
+        for (int f = 0; f < 6; ++f)
+            for (int n = 0; n < Nfp; ++n) {
+                int64_t idM = m.vmapM[(e * 6 + f) * Nfp + n], idP = m.vmapP[(e * 6 + f) * Nfp + n];
+                int vM = (int)(idM % Np);
+                int64_t eP = idP / Np; int vP = (int)(idP % Np);
+                if (m.elemtobndy[e * 6 + f] != 0) { eP = e; vP = vM; }
+                double nv[3] = {SG(m, e, f, n, SN1), SG(m, e, f, n, SN2), SG(m, e, f, n, SN3)};
+                double pM = AUX(m, e, AP_REF, vM), pP = AUX(m, eP, AP_REF, vP);
+                double sM = SG(m, e, f, n, SSM), vMI = SG(m, e, f, n, SVMI);
+                for (int s = 0; s < 3; ++s) {
+                    // central: (F- + F+)' * (n / 2); F[d, s] = -p delta_ds
+                    double fl = (-pM + -pP) * (nv[s] / 2);
+                    gp[(e * 3 + s) * Np + vM] -= vMI * sM * fl;
+                }
+            }
+    }
+}
+
+void init_aux(Model& m) {
+    const om_params& p = m.prm;
+    int Np = m.Np;
+    m.aux.assign((size_t)m.nelem * NAUX * Np, 0.0);
+    for (int64_t e = 0; e < m.nelem; ++e)
+        for (int n = 0; n < Np; ++n) {
+            AUX(m, e, AX, n) = VG(m, e, VX1, n);
+            AUX(m, e, AY, n) = VG(m, e, VX2, n);
+            AUX(m, e, AZ, n) = VG(m, e, VX3, n);
+        }
+    // Orientation: Phi = g z (Orientations.jl:246-258), grad Phi by DG
+    if (p.orientation == 1) {
+        for (int64_t e = 0; e < m.nelem; ++e)
+            for (int n = 0; n < Np; ++n) AUX(m, e, APHI, n) = p.grav * AUX(m, e, AZ, n);
+        aux_field_gradient(m, APHI, AGPX);
+    }
+    // Hydrostatic reference state (ref_state.jl:143-185)
+    if (p.ref_state == 1) {
+        for (int64_t e = 0; e < m.nelem; ++e)
+            for (int n = 0; n < Np; ++n) {
+                double z = AUX(m, e, APHI, n) / p.grav;  // altitude = Phi / g
+                double Tv, pres;
+                profile(p, z, Tv, pres);
+                AUX(m, e, AP_REF, n) = pres;
+                AUX(m, e, ARHO_REF, n) = pres / (Tv * p.R_d);
+            }
+        std::vector<double> gp;
+        ref_pressure_gradient(m, gp);
+        for (int64_t e = 0; e < m.nelem; ++e)
+            for (int n = 0; n < Np; ++n) {
+                double gP[3] = {AUX(m, e, AGPX, n), AUX(m, e, AGPY, n), AUX(m, e, AGPZ, n)};
+                double k[3] = {gP[0] / p.grav, gP[1] / p.grav, gP[2] / p.grav};
+                double dp[3] = {gp[(e * 3 + 0) * Np + n], gp[(e * 3 + 1) * Np + n], gp[(e * 3 + 2) * Np + n]};
+                double num = k[0] * dp[0] + k[1] * dp[1] + k[2] * dp[2];
+                double den = k[0] * gP[0] + k[1] * gP[1] + k[2] * gP[2];
+                AUX(m, e, ARHO_REF, n) = -num / den;
+            }
+        for (int64_t e = 0; e < m.nelem; ++e)
+            for (int n = 0; n < Np; ++n) {
+                double rho = AUX(m, e, ARHO_REF, n), pres = AUX(m, e, AP_REF, n);
+                double T = pres / (p.R_d * rho);  // PhaseDry_ρp
+                AUX(m, e, AT_REF, n) = T;
+                double e_pot = AUX(m, e, APHI, n);
+                AUX(m, e, ARHOE_REF, n) = rho * ((0.0 + e_pot) + p.cv_d * (T - p.T_0));
+            }
+    }
+    // Smagorinsky length scale, Geometry.jl:121-122 (2 / (cbrt(det(dxi/dx)) N))
+    for (int64_t e = 0; e < m.nelem; ++e)
+        for (int n = 0; n < Np; ++n) {
+            double a = VG(m, e, XI1X1, n), b = VG(m, e, XI1X2, n), c = VG(m, e, XI1X3, n);
+            double d = VG(m, e, XI2X1, n), f = VG(m, e, XI2X2, n), g = VG(m, e, XI2X3, n);
+            double h = VG(m, e, XI3X1, n), i = VG(m, e, XI3X2, n), j = VG(m, e, XI3X3, n);
+            // invJ = [xi1x1 xi1x2 xi1x3; xi2x1 ...; xi3x1 ...]
+            double det = a * (f * j - g * i) - b * (d * j - g * h) + c * (d * i - f * h);
+            AUX(m, e, ADELTA, n) = 2 / (std::cbrt(det) * std::max(1, m.N));
+        }
+}
+
+// ----------------------------------------------------------------------------
+// Model pointwise functions (AtmosModel, dry, TotalEnergy, Compressible).
+// ----------------------------------------------------------------------------
+struct NodeAux {
+    double Phi, gPhi[3], rho_ref, p_ref, thv, Delta;
+};
+
+inline NodeAux node_aux(const Model& m, int64_t e, int n) {
+    NodeAux a;
+    a.Phi = AUXc(m, e, APHI, n);
+    a.gPhi[0] = AUXc(m, e, AGPX, n);
+    a.gPhi[1] = AUXc(m, e, AGPY, n);
+    a.gPhi[2] = AUXc(m, e, AGPZ, n);
+    a.rho_ref = AUXc(m, e, ARHO_REF, n);
+    a.p_ref = AUXc(m, e, AP_REF, n);
+    a.thv = AUXc(m, e, ATHV, n);
+    a.Delta = AUXc(m, e, ADELTA, n);
+    return a;
+}
+
+// First-order flux F[d][s] (atmos_tendencies.jl:9-45; tendencies_mass.jl:7-9,
+// tendencies_momentum.jl:13-29, tendencies_energy.jl:7-21).
+void flux_first_order(const om_params& p, const double q[NS], const NodeAux& a, double F[3][NS]) {
+    double rho = q[0];
+    const double* ru = q + 1;
+    double rhoe = q[4];
+    Thermo t = phase_dry(p, rho, rhoe, ru, a.Phi);
+    double pres = t.p;
+    double pg = (p.ref_state == 1 && p.subtract_off) ? (pres - a.p_ref) : pres;
+    for (int d = 0; d < 3; ++d) {
+        double u_d = ru[d] / rho;
+        F[d][0] = ru[d];
+        for (int c = 0; c < 3; ++c) F[d][1 + c] = ru[d] * (ru[c] / rho) + (c == d ? pg : 0.0);
+        F[d][4] = u_d * rhoe + u_d * pres;
+    }
+}
+
+// Gradient-flux layout per node: [dh_tot(3), S11,S21,S31,S22,S32,S33, (N2)]
+// (AtmosModel.jl:447-461, energy.jl:10-11, TurbulenceClosures.jl:347-362,446-470)
+
+// Second-order flux (tendencies_momentum.jl:37-42, tendencies_energy.jl:27-31,
+// 51-56; turbulence_tensors TurbulenceClosures.jl:199-225, 368-404, 472-505).
+void flux_second_order(const Model& m, const double q[NS], const double* gf, const NodeAux& a, double F[3][NS]) {
+    const om_params& p = m.prm;
+    for (int d = 0; d < 3; ++d)
+        for (int s = 0; s < NS; ++s) F[d][s] = 0;
+    if (p.turbulence == 0) return;
+    double rho = q[0];
+    const double* ru = q + 1;
+    double S[3][3] = {{gf[3], gf[4], gf[5]}, {gf[4], gf[6], gf[7]}, {gf[5], gf[7], gf[8]}};
+    double nu[3], Dt[3];
+    double tau[3][3];
+    if (p.turbulence == 1) {
+        double nu0 = p.rho_nu / rho;
+        double Dt0 = nu0 * p.inv_Pr_turb;
+        for (int c = 0; c < 3; ++c) { nu[c] = nu0; Dt[c] = Dt0; }
+        double trS = S[0][0] + S[1][1] + S[2][2];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                tau[r][c] = (-2 * nu0) * S[r][c];
+                if (p.with_divergence && r == c) tau[r][c] += (2 * nu0 / 3) * trS;
+            }
+    } else {
+        // SmagorinskyLilly
+        double norm2 = S[0][0] * S[0][0] + 2 * (S[1][0] * S[1][0]) + 2 * (S[2][0] * S[2][0]) + S[1][1] * S[1][1] +
+                       2 * (S[2][1] * S[2][1]) + S[2][2] * S[2][2];
+        double normS = std::sqrt(2 * norm2);
+        double khat[3] = {a.gPhi[0] / p.grav, a.gPhi[1] / p.grav, a.gPhi[2] / p.grav};
+        double N2 = gf[9];
+        double epsn = normS == 0 ? 4.9406564584124654e-324 : std::nextafter(normS, INFINITY) - normS;
+        double Ri = N2 / (normS * normS + epsn);
+        double fb2 = std::sqrt(std::min(std::max(1.0 - Ri * p.inv_Pr_turb, 0.0), 1.0));
+        double cd = p.C_smag * a.Delta;
+        double nu0 = normS * (cd * cd) + 1e-5;
+        double dnk = nu0 * khat[0] + nu0 * khat[1] + nu0 * khat[2];
+        for (int c = 0; c < 3; ++c) {
+            double nv = khat[c] * dnk;
+            double nh = nu0 - nv;
+            nu[c] = nh + nv * fb2;
+            Dt[c] = nu[c] * p.inv_Pr_turb;
+        }
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) tau[r][c] = -2 * nu[r] * S[r][c];
+    }
+    // momentum: tau * rho ; energy: tau * rhou + (-D_t .* grad h_tot) * rho
+    for (int d = 0; d < 3; ++d) {
+        for (int c = 0; c < 3; ++c) F[d][1 + c] = tau[d][c] * rho;
+        double tr = tau[d][0] * ru[0] + tau[d][1] * ru[1] + tau[d][2] * ru[2];
+        F[d][4] = tr + (-Dt[d] * gf[d]) * rho;
+    }
+}
+
+// Gravity source (tendencies_momentum.jl:64-72)
+void source(const om_params& p, const double q[NS], const NodeAux& a, double S[NS]) {
+    for (int s = 0; s < NS; ++s) S[s] = 0;
+    if (!p.gravity) return;
+    double r = (p.ref_state == 1 && p.subtract_off) ? (q[0] - a.rho_ref) : q[0];
+    for (int c = 0; c < 3; ++c) S[1 + c] = -r * a.gPhi[c];
+}
+
+// wavespeed (AtmosModel.jl:776-796)
+inline double wavespeed(const om_params& p, const double n[3], const double q[NS], const NodeAux& a) {
+    double rinv = 1 / q[0];
+    double u[3] = {rinv * q[1], rinv * q[2], rinv * q[3]};
+    double uN = std::fabs(n[0] * u[0] + n[1] * u[1] + n[2] * u[2]);
+    Thermo t = phase_dry(p, q[0], q[4], q + 1, a.Phi);
+    return uN + soundspeed(p, t.T);
+}
+
+// Gradient argument (AtmosModel.jl:622-650, energy.jl:20-31,
+// TurbulenceClosures.jl:446-454): u, h_tot, [theta_v]
+int ngrad_args(const om_params& p) { return p.turbulence == 2 ? 5 : 4; }
+void gradient_argument(const om_params& p, const double q[NS], double Phi, double thv, double G[5]) {
+    double rinv = 1 / q[0];
+    G[0] = rinv * q[1]; G[1] = rinv * q[2]; G[2] = rinv * q[3];
+    Thermo t = phase_dry(p, q[0], q[4], q + 1, Phi);
+    double e_tot = q[4] * (1 / q[0]);
+    G[3] = e_tot + p.R_d * t.T;
+    G[4] = thv;
+}
+
+// compute_gradient_flux!: linear map of grad G -> gradient-flux words
+void gradient_flux(const om_params& p, const double gG[3][5], const NodeAux& a, double* gf) {
+    gf[0] = gG[0][3]; gf[1] = gG[1][3]; gf[2] = gG[2][3];
+    // symmetrize(grad u): X[i,j] = d u_j / d x_i (Grad layout (3, ngrad))
+    gf[3] = gG[0][0];
+    gf[4] = (gG[1][0] + gG[0][1]) / 2;
+    gf[5] = (gG[2][0] + gG[0][2]) / 2;
+    gf[6] = gG[1][1];
+    gf[7] = (gG[2][1] + gG[1][2]) / 2;
+    gf[8] = gG[2][2];
+    if (p.turbulence == 2)
+        gf[9] = (gG[0][4] * a.gPhi[0] + gG[1][4] * a.gPhi[1] + gG[2][4] * a.gPhi[2]) / a.thv;
+}
+
+// FreeSlip boundary state for first-order fluxes (bc_momentum.jl:25-34)
+inline void bc_state_first(const double qM[NS], const double n[3], double qP[NS]) {
+    for (int s = 0; s < NS; ++s) qP[s] = qM[s];
+    double dn = qM[1] * n[0] + qM[2] * n[1] + qM[3] * n[2];
+    for (int c = 0; c < 3; ++c) qP[1 + c] -= 2 * dn * n[c];
+}
+// FreeSlip boundary state for the gradient flux (bc_momentum.jl:35-43)
+inline void bc_state_grad(const double qM[NS], const double n[3], double qP[NS]) {
+    for (int s = 0; s < NS; ++s) qP[s] = qM[s];
+    double dn = qM[1] * n[0] + qM[2] * n[1] + qM[3] * n[2];
+    for (int c = 0; c < 3; ++c) qP[1 + c] -= dn * n[c];
+}
+
+inline void load_q(const Model& m, const double* Q, int64_t e, int n, double q[NS]) {
+    for (int s = 0; s < NS; ++s) q[s] = Q[(e * NS + s) * m.Np + n];
+}
+
+// update_auxiliary_state!: DryModel theta_v, air_T (moisture.jl:58-68)
+void update_aux(Model& m, const double* Q) {
+    const om_params& p = m.prm;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m.nelem; ++e)
+        for (int n = 0; n < m.Np; ++n) {
+            double q[NS];
+            load_q(m, Q, e, n, q);
+            Thermo t = phase_dry(p, q[0], q[4], q + 1, AUX(m, e, APHI, n));
+            AUX(m, e, ATHV, n) = virtual_pottemp(p, t.T, t.p);
+            AUX(m, e, AAIRT, n) = t.T;
+        }
+}
+
+// Gradient passes: volume_gradients! (DGModel_kernels.jl:934-1328, H then V
+// incremented) and dgsem_interface_gradients! (:1365-1651, faces 1-4 then 5-6).
+void gradient_pass(Model& m, const double* Q) {
+    const om_params& p = m.prm;
+    int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp, ngf = m.ngf, ng = ngrad_args(p);
+    m.gradflux.assign((size_t)m.nelem * ngf * Np, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m.nelem; ++e) {
+        std::vector<double> G(Np * 5);
+        for (int n = 0; n < Np; ++n) {
+            double q[NS];
+            load_q(m, Q, e, n, q);
+            gradient_argument(p, q, AUXc(m, e, APHI, n), AUXc(m, e, ATHV, n), &G[n * 5]);
+        }
+        for (int k = 0; k < Nq; ++k)
+            for (int j = 0; j < Nq; ++j)
+                for (int i = 0; i < Nq; ++i) {
+                    int ijk = i + Nq * (j + Nq * k);
+                    double gH[3][5], gV[3][5];
+                    for (int s = 0; s < ng; ++s) {
+                        double G1 = 0, G2 = 0, G3 = 0;
+                        for (int n = 0; n < Nq; ++n) {
+                            G1 += Dm(m, i, n) * G[(n + Nq * (j + Nq * k)) * 5 + s];
+                            G2 += Dm(m, j, n) * G[(i + Nq * (n + Nq * k)) * 5 + s];
+                            G3 += Dm(m, k, n) * G[(i + Nq * (j + Nq * n)) * 5 + s];
+                        }
+                        gH[0][s] = VGc(m, e, XI1X1, ijk) * G1 + VGc(m, e, XI2X1, ijk) * G2;
+                        gH[1][s] = VGc(m, e, XI1X2, ijk) * G1 + VGc(m, e, XI2X2, ijk) * G2;
+                        gH[2][s] = VGc(m, e, XI1X3, ijk) * G1 + VGc(m, e, XI2X3, ijk) * G2;
+                        gV[0][s] = VGc(m, e, XI3X1, ijk) * G3;
+                        gV[1][s] = VGc(m, e, XI3X2, ijk) * G3;
+                        gV[2][s] = VGc(m, e, XI3X3, ijk) * G3;
+                    }
+                    NodeAux a = node_aux(m, e, ijk);
+                    double gfH[10], gfV[10];
+                    gradient_flux(p, gH, a, gfH);
+                    gradient_flux(p, gV, a, gfV);
+                    for (int s = 0; s < ngf; ++s) m.gradflux[(e * ngf + s) * Np + ijk] = gfH[s] + gfV[s];
+                }
+        for (int f = 0; f < 6; ++f)
+            for (int n = 0; n < Nfp; ++n) {
+                int64_t idM = m.vmapM[(e * 6 + f) * Nfp + n], idP = m.vmapP[(e * 6 + f) * Nfp + n];
+                int vM = (int)(idM % Np);
+                int64_t eP = idP / Np; int vP = (int)(idP % Np);
+                int tag = m.elemtobndy[e * 6 + f];
+                if (tag != 0) { eP = e; vP = vM; }
+                double nv[3] = {SGc(m, e, f, n, SN1), SGc(m, e, f, n, SN2), SGc(m, e, f, n, SN3)};
+                double sM = SGc(m, e, f, n, SSM), vMI = SGc(m, e, f, n, SVMI);
+                double qM[NS], qP[NS], GM[5], GP[5];
+                load_q(m, Q, e, vM, qM);
+                NodeAux aM = node_aux(m, e, vM);
+                gradient_argument(p, qM, aM.Phi, aM.thv, GM);
+                double Gs[3][5];
+                if (tag == 0) {
+                    load_q(m, Q, eP, vP, qP);
+                    NodeAux aP = node_aux(m, eP, vP);
+                    gradient_argument(p, qP, aP.Phi, aP.thv, GP);
+                    for (int d = 0; d < 3; ++d)
+                        for (int s = 0; s < ng; ++s) Gs[d][s] = nv[d] * (GP[s] + GM[s]) / 2;
+                } else {
+                    bc_state_grad(qM, nv, qP);
+                    // boundary_state! refreshes aux+ (theta_v) from state+
+                    Thermo t = phase_dry(p, qP[0], qP[4], qP + 1, aM.Phi);
+                    double thvP = virtual_pottemp(p, t.T, t.p);
+                    gradient_argument(p, qP, aM.Phi, thvP, GP);
+                    for (int d = 0; d < 3; ++d)
+                        for (int s = 0; s < ng; ++s) Gs[d][s] = nv[d] * GP[s];
+                }
+                double nG[3][5];
+                for (int d = 0; d < 3; ++d)
+                    for (int s = 0; s < ng; ++s) nG[d][s] = nv[d] * GM[s];
+                double gfs[10], gfm[10];
+                gradient_flux(p, Gs, aM, gfs);
+                gradient_flux(p, nG, aM, gfm);
+                for (int s = 0; s < ngf; ++s) m.gradflux[(e * ngf + s) * Np + vM] += vMI * sM * (gfs[s] - gfm[s]);
+            }
+    }
+}
+
+// Numerical flux F*.n at one face node: Rusanov/central first order
+// (NumericalFluxes.jl:219-340, boundary wrapper :163-205) plus central
+// second order (:668-715; zero on FreeSlip/Insulating walls,
+// Atmos/Model/boundaryconditions.jl:113-185).
+void face_flux(const Model& m, const double* Q, int64_t e, int f, int n, double fl[NS]) {
+    const om_params& p = m.prm;
+    int Np = m.Np, Nfp = m.Nfp, ngf = m.ngf;
+    int64_t idM = m.vmapM[(e * 6 + f) * Nfp + n], idP = m.vmapP[(e * 6 + f) * Nfp + n];
+    int vM = (int)(idM % Np);
+    int64_t eP = idP / Np; int vP = (int)(idP % Np);
+    int tag = m.elemtobndy[e * 6 + f];
+    if (tag != 0) { eP = e; vP = vM; }
+    double nv[3] = {SGc(m, e, f, n, SN1), SGc(m, e, f, n, SN2), SGc(m, e, f, n, SN3)};
+    double qM[NS], qP[NS];
+    load_q(m, Q, e, vM, qM);
+    NodeAux aM = node_aux(m, e, vM);
+    NodeAux aP = node_aux(m, eP, vP);
+    if (tag == 0) load_q(m, Q, eP, vP, qP);
+    else bc_state_first(qM, nv, qP);
+    for (int s = 0; s < NS; ++s) fl[s] = 0;
+    double FM[3][NS], FP[3][NS];
+    flux_first_order(p, qM, aM, FM);
+    flux_first_order(p, qP, aP, FP);
+    for (int s = 0; s < NS; ++s) {
+        double acc = 0;
+        for (int d = 0; d < 3; ++d) acc += (FM[d][s] + FP[d][s]) * (nv[d] / 2);
+        fl[s] += acc;
+    }
+    if (p.numflux == 0) {
+        double wM = wavespeed(p, nv, qM, aM), wP = wavespeed(p, nv, qP, aP);
+        double mw = std::max(wM, wP);
+        for (int s = 0; s < NS; ++s) fl[s] += mw * (qM[s] - qP[s]) / 2;
+    }
+    if (p.turbulence != 0 && tag == 0) {
+        const double* gM = &m.gradflux[0];
+        double gfM[10], gfP[10];
+        for (int s = 0; s < ngf; ++s) {
+            gfM[s] = gM[(e * ngf + s) * Np + vM];
+            gfP[s] = gM[(eP * ngf + s) * Np + vP];
+        }
+        flux_second_order(m, qM, gfM, aM, FM);
+        flux_second_order(m, qP, gfP, aP, FP);
+        for (int s = 0; s < NS; ++s) {
+            double acc = 0;
+            for (int d = 0; d < 3; ++d) acc += (FM[d][s] + FP[d][s]) * (nv[d] / 2);
+            fl[s] += acc;
+        }
+    }
+}
+
+// Full tendency, DGModel.jl:85-427: T = alpha * dQ/dt(Q) + beta * T.
+void tendency(Model& m, double* T, const double* Q, double t, double alpha, double beta) {
+    (void)t;
+    const om_params& p = m.prm;
+    int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp, ngf = m.ngf;
+    update_aux(m, Q);
+    if (p.turbulence != 0) gradient_pass(m, Q);
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m.nelem; ++e) {
+        std::vector<double> F1(Np * NS), F2(Np * NS), F3(Np * NS), Src(Np * NS);
+        for (int n = 0; n < Np; ++n) {
+            double q[NS];
+            load_q(m, Q, e, n, q);
+            NodeAux a = node_aux(m, e, n);
+            double F[3][NS], G[3][NS];
+            flux_first_order(p, q, a, F);
+            if (p.turbulence != 0) {
+                double gf[10];
+                for (int s = 0; s < ngf; ++s) gf[s] = m.gradflux[(e * ngf + s) * Np + n];
+                flux_second_order(m, q, gf, a, G);
+                for (int d = 0; d < 3; ++d)
+                    for (int s = 0; s < NS; ++s) F[d][s] += G[d][s];
+            }
+            double M = VGc(m, e, VM, n);
+            for (int s = 0; s < NS; ++s) {
+                F1[n * NS + s] = M * (VGc(m, e, XI1X1, n) * F[0][s] + VGc(m, e, XI1X2, n) * F[1][s] + VGc(m, e, XI1X3, n) * F[2][s]);
+                F2[n * NS + s] = M * (VGc(m, e, XI2X1, n) * F[0][s] + VGc(m, e, XI2X2, n) * F[1][s] + VGc(m, e, XI2X3, n) * F[2][s]);
+                F3[n * NS + s] = M * (VGc(m, e, XI3X1, n) * F[0][s] + VGc(m, e, XI3X2, n) * F[1][s] + VGc(m, e, XI3X3, n) * F[2][s]);
+            }
+            source(p, q, a, &Src[n * NS]);
+        }
+        for (int k = 0; k < Nq; ++k)
+            for (int j = 0; j < Nq; ++j)
+                for (int i = 0; i < Nq; ++i) {
+                    int ijk = i + Nq * (j + Nq * k);
+                    double MI = VGc(m, e, VMI, ijk);
+                    for (int s = 0; s < NS; ++s) {
+                        // horizontal kernel (DGModel_kernels.jl:282-295)
+                        double lh = 0;
+                        for (int n = 0; n < Nq; ++n) {
+                            lh += MI * Dm(m, n, i) * F1[(n + Nq * (j + Nq * k)) * NS + s];
+                            lh += MI * Dm(m, n, j) * F2[(i + Nq * (n + Nq * k)) * NS + s];
+                        }
+                        // vertical kernel (:504-513, 519-524)
+                        double lv = 0;
+                        for (int kk = 0; kk < Nq; ++kk) lv += MI * Dm(m, kk, k) * F3[(i + Nq * (j + Nq * kk)) * NS + s];
+                        lv += Src[ijk * NS + s];
+                        size_t idx = (size_t)(e * NS + s) * Np + ijk;
+                        double Th = (beta != 0) ? alpha * lh + beta * T[idx] : alpha * lh;
+                        T[idx] = alpha * lv + Th;
+                    }
+                }
+        // interface kernel (faces 1-4, then 5-6), DGModel_kernels.jl:893-896
+        for (int f = 0; f < 6; ++f)
+            for (int n = 0; n < Nfp; ++n) {
+                double fl[NS];
+                face_flux(m, Q, e, f, n, fl);
+                int vM = (int)(m.vmapM[(e * 6 + f) * Nfp + n] % Np);
+                double sM = SGc(m, e, f, n, SSM), vMI = SGc(m, e, f, n, SVMI);
+                for (int s = 0; s < NS; ++s) T[(size_t)(e * NS + s) * Np + vM] -= alpha * vMI * sM * fl[s];
+            }
+    }
+}
+
+// LSRK54CarpenterKennedy coefficients, LowStorageRungeKuttaMethod.jl:302-324
+const double RKA[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
+                       -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
+const double RKB[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+                       1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+                       2277821191437.0 / 14882151754819.0};
+const double RKC[5] = {0.0, 1432997174477.0 / 9575080441755.0, 2526269341429.0 / 6820363962896.0,
+                       2006345519317.0 / 3224310063776.0, 2802321613138.0 / 2924317926251.0};
+
+// dostep!, LowStorageRungeKuttaMethod.jl:102-158
+void lsrk_step(Model& m, double* Q, double* dQ, double time, double dt) {
+    size_t len = (size_t)m.nelem * NS * m.Np;
+    for (int s = 0; s < 5; ++s) {
+        tendency(m, dQ, Q, time + RKC[s] * dt, 1.0, 1.0);
+        double a = RKA[(s + 1) % 5], b = RKB[s];
+#pragma omp parallel for schedule(static)
+        for (size_t i = 0; i < len; ++i) {
+            Q[i] += b * dt * dQ[i];
+            dQ[i] *= a;
+        }
+    }
+}
+
+// TwoSum-based double-double accumulate (DoubleFloats.jl semantics)
+struct DD {
+    double hi = 0, lo = 0;
+    void add(double x) {
+        double s = hi + x;
+        double bp = s - hi;
+        double err = (hi - (s - bp)) + (x - bp);
+        lo += err;
+        double s2 = s + lo;
+        lo = lo - (s2 - s);
+        hi = s2;
+    }
+};
+
+// exact product as a double-double then added
+inline void dd_add_prod(DD& acc, double a, double b) {
+    double p = a * b;
+    double e = std::fma(a, b, -p);
+    acc.add(p);
+    acc.add(e);
+}
+
+}  // namespace
+
+extern "C" {
+
+typedef struct Model om_model;
+
+om_model* om_create(const om_brick* b, const om_params* p) {
+    Model* m = new Model();
+    m->mesh = *b;
+    m->prm = *p;
+    m->N = b->N;
+    m->Nq = b->N + 1;
+    m->Np = m->Nq * m->Nq * m->Nq;
+    m->Nfp = m->Nq * m->Nq;
+    m->nelem = (int64_t)b->ne[0] * b->ne[1] * b->ne[2];
+    m->ngf = p->turbulence == 2 ? 10 : 9;
+    lgl(m->N, m->xi, m->omega);
+    spectral_derivative(m->xi, m->D);
+    build_geometry(*m);
+    init_aux(*m);
+    return m;
+}
+
+void om_free(om_model* m) { delete m; }
+
+int64_t om_nelem(const om_model* m) { return m->nelem; }
+int om_Np(const om_model* m) { return m->Np; }
+int om_naux(void) { return NAUX; }
+int om_ngradflux(const om_model* m) { return m->ngf; }
+const double* om_vgeo(const om_model* m) { return m->vgeo.data(); }
+const double* om_sgeo(const om_model* m) { return m->sgeo.data(); }
+const double* om_aux(const om_model* m) { return m->aux.data(); }
+const double* om_gradflux(const om_model* m) { return m->gradflux.data(); }
+const int64_t* om_vmapM(const om_model* m) { return m->vmapM.data(); }
+const int64_t* om_vmapP(const om_model* m) { return m->vmapP.data(); }
+const int* om_elemtobndy(const om_model* m) { return m->elemtobndy.data(); }
+const double* om_D(const om_model* m) { return m->D.data(); }
+const double* om_lgl_nodes(const om_model* m) { return m->xi.data(); }
+const double* om_lgl_weights(const om_model* m) { return m->omega.data(); }
+
+int om_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
+
+void om_tendency(om_model* m, double* dQ, const double* Q, double t, double alpha, double beta) {
+    tendency(*m, dQ, Q, t, alpha, beta);
+}
+
+// Gradient-flux pass only (for parity of the diffusive pass)
+void om_gradient_pass(om_model* m, const double* Q) {
+    update_aux(*m, Q);
+    gradient_pass(*m, Q);
+}
+
+// nsteps LSRK54 steps of size dt from time t0 (dQ is the solver's register)
+void om_lsrk54(om_model* m, double* Q, double* dQ, double t0, double dt, int nsteps) {
+    double time = t0;
+    for (int i = 0; i < nsteps; ++i) {
+        lsrk_step(*m, Q, dQ, time, dt);
+        time += dt;
+    }
+}
+
+// solve!(Q, lsrk; timeend) with adjustfinalstep, ODESolvers.jl:49-158.
+// Returns the number of steps taken.
+int om_solve(om_model* m, double* Q, double t0, double dt, double timeend) {
+    size_t len = (size_t)m->nelem * NS * m->Np;
+    std::vector<double> dQ(len, 0.0);
+    double time = t0;
+    int step = 0;
+    while (time < timeend) {
+        ++step;
+        double h = dt;
+        bool final_step = false;
+        if (time + h > timeend) { h = timeend - time; final_step = true; }
+        lsrk_step(*m, Q, dQ.data(), time, h);
+        time = final_step ? timeend : time + h;
+    }
+    return step;
+}
+
+// Scalar ODE q' = q cos(t) integrated by the same LSRK54 coefficients and
+// solve! loop (test/Numerics/ODESolvers/ode_tests_convergence.jl:15-44).
+double om_lsrk54_scalar(double q0, double dt, double timeend) {
+    double Q = q0, dQ = 0.0, time = 0.0;
+    while (time < timeend) {
+        double h = dt;
+        bool final_step = false;
+        if (time + h > timeend) { h = timeend - time; final_step = true; }
+        for (int s = 0; s < 5; ++s) {
+            dQ += Q * std::cos(time + RKC[s] * h);
+            Q += RKB[s] * h * dQ;
+            dQ *= RKA[(s + 1) % 5];
+        }
+        time = final_step ? timeend : time + h;
+    }
+    return Q;
+}
+
+// Weighted L2 norm sqrt(sum M Q^2), MPIStateArrays.jl:583-606
+double om_norm(const om_model* m, const double* Q) {
+    double acc = 0;
+    for (int64_t e = 0; e < m->nelem; ++e)
+        for (int s = 0; s < NS; ++s)
+            for (int n = 0; n < m->Np; ++n) {
+                double q = Q[(e * NS + s) * m->Np + n];
+                acc += VGc(*m, e, VM, n) * q * q;
+            }
+    return std::sqrt(acc);
+}
+
+// euclidean_distance (MPIStateArrays.jl:628-648)
+double om_euclidean_distance(const om_model* m, const double* A, const double* B) {
+    double acc = 0;
+    for (int64_t e = 0; e < m->nelem; ++e)
+        for (int s = 0; s < NS; ++s)
+            for (int n = 0; n < m->Np; ++n) {
+                size_t i = (size_t)(e * NS + s) * m->Np + n;
+                double d = A[i] - B[i];
+                acc += d * d * VGc(*m, e, VM, n);
+            }
+    return std::sqrt(acc);
+}
+
+// Per-field weighted L2 of A-B and of B (for relative errors)
+void om_field_l2(const om_model* m, const double* A, const double* B, double* err, double* ref) {
+    for (int s = 0; s < NS; ++s) { err[s] = 0; ref[s] = 0; }
+    for (int64_t e = 0; e < m->nelem; ++e)
+        for (int s = 0; s < NS; ++s)
+            for (int n = 0; n < m->Np; ++n) {
+                size_t i = (size_t)(e * NS + s) * m->Np + n;
+                double M = VGc(*m, e, VM, n);
+                double d = A[i] - B[i];
+                err[s] += d * d * M;
+                ref[s] += B[i] * B[i] * M;
+            }
+    for (int s = 0; s < NS; ++s) { err[s] = std::sqrt(err[s]); ref[s] = std::sqrt(ref[s]); }
+}
+
+// weightedsum (compensated), MPIStateArrays.jl:655-675
+double om_weightedsum(const om_model* m, const double* Q, int field) {
+    DD acc;
+    for (int64_t e = 0; e < m->nelem; ++e)
+        for (int n = 0; n < m->Np; ++n) dd_add_prod(acc, Q[(e * NS + field) * m->Np + n], VGc(*m, e, VM, n));
+    return acc.hi + acc.lo;
+}
+
+// Pointwise nondiffusive Courant number max over nodes with dt = 1
+// (SpaceDiscretization.jl:307-365, Atmos/Model/courant.jl, Grids.jl:1228-1334);
+// calculate_dt = CFL / max (DGMethods.jl:79-83).
+double om_courant_dt(const om_model* m, const double* Q, double CFL) {
+    int Nq = m->Nq, Np = m->Np;
+    double cmax = -INFINITY;
+    for (int64_t e = 0; e < m->nelem; ++e)
+        for (int k = 0; k < Nq; ++k)
+            for (int j = 0; j < Nq; ++j)
+                for (int i = 0; i < Nq; ++i) {
+                    int ijk = i + Nq * (j + Nq * k);
+                    double x[3] = {VGc(*m, e, VX1, ijk), VGc(*m, e, VX2, ijk), VGc(*m, e, VX3, ijk)};
+                    double md = INFINITY;
+                    auto nd = [&](int ii, int jj, int kk) {
+                        int o = ii + Nq * (jj + Nq * kk);
+                        double dx = x[0] - VGc(*m, e, VX1, o), dy = x[1] - VGc(*m, e, VX2, o), dz = x[2] - VGc(*m, e, VX3, o);
+                        md = std::min(md, std::sqrt(dx * dx + dy * dy + dz * dz));
+                    };
+                    if (i > 0) nd(i - 1, j, k);
+                    if (i < Nq - 1) nd(i + 1, j, k);
+                    if (j > 0) nd(i, j - 1, k);
+                    if (j < Nq - 1) nd(i, j + 1, k);
+                    if (k > 0) nd(i, j, k - 1);
+                    if (k < Nq - 1) nd(i, j, k + 1);
+                    double q[NS];
+                    load_q(*m, Q, e, ijk, q);
+                    double u[3] = {q[1] / q[0], q[2] / q[0], q[3] / q[0]};
+                    double nu = std::sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+                    Thermo t = phase_dry(m->prm, q[0], q[4], q + 1, AUXc(*m, e, APHI, ijk));
+                    double c = 1.0 * (nu + soundspeed(m->prm, t.T)) / md;
+                    cmax = std::max(cmax, c);
+                }
+    return CFL / cmax;
+}
+
+// Isentropic vortex initial condition,
+// test/Numerics/DGMethods/Euler/isentropicvortex_setup.jl:1-62
+void om_init_vortex(const om_model* m, double* Q, double t, double p_inf, double T_inf, double translation_speed,
+                    double translation_angle, double vortex_speed, double R, double L) {
+    const om_params& p = m->prm;
+    double rho_inf = p_inf / (p.R_d * T_inf);
+    double kappa = p.R_d / p.cp_d;
+    double uinf[3] = {translation_speed * std::cos(translation_angle), translation_speed * std::sin(translation_angle), 0};
+    for (int64_t e = 0; e < m->nelem; ++e)
+        for (int n = 0; n < m->Np; ++n) {
+            double x[3] = {VGc(*m, e, VX1, n), VGc(*m, e, VX2, n), VGc(*m, e, VX3, n)};
+            for (int d = 0; d < 3; ++d) {
+                x[d] -= uinf[d] * t;
+                x[d] -= std::floor((x[d] + L) / (2 * L)) * (2 * L);
+            }
+            double r = std::sqrt(x[0] * x[0] + x[1] * x[1]);
+            double du_x = -vortex_speed * x[1] / R * std::exp(-((r / R) * (r / R)) / 2);
+            double du_y = vortex_speed * x[0] / R * std::exp(-((r / R) * (r / R)) / 2);
+            double u[3] = {uinf[0] + du_x, uinf[1] + du_y, uinf[2] + 0};
+            double T = T_inf * (1 - kappa * (vortex_speed * vortex_speed) / 2 * rho_inf / p_inf * std::exp(-((r / R) * (r / R))));
+            double pres = p_inf * std::pow(T / T_inf, 1.0 / kappa);
+            double rho = pres / (p.R_d * T);
+            double e_kin = (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]) / 2;
+            double* q = Q;
+            q[(e * NS + 0) * m->Np + n] = rho;
+            for (int c = 0; c < 3; ++c) q[(e * NS + 1 + c) * m->Np + n] = rho * u[c];
+            q[(e * NS + 4) * m->Np + n] = rho * ((e_kin + 0.0) + p.cv_d * (T - p.T_0));
+        }
+}
+
+// Rising thermal bubble about a hydrostatic background of potential
+// temperature theta0 (experiments/TestCase/risingbubble.jl:23-91, with a
+// cos^2 bump): theta = theta0 + A cos^2(pi r / (2 rc)) for r <= rc.
+void om_init_bubble(const om_model* m, double* Q, double theta0, double amp, double rc, double xc, double yc,
+                    double zc) {
+    const om_params& p = m->prm;
+    double R = p.R_d, cp = p.cp_d, cv = p.cv_d;
+    for (int64_t e = 0; e < m->nelem; ++e)
+        for (int n = 0; n < m->Np; ++n) {
+            double x = VGc(*m, e, VX1, n), y = VGc(*m, e, VX2, n), z = VGc(*m, e, VX3, n);
+            double r = std::sqrt((x - xc) * (x - xc) + (y - yc) * (y - yc) + (z - zc) * (z - zc));
+            double dth = 0;
+            if (r <= rc) {
+                double c = std::cos(M_PI * r / (2 * rc));
+                dth = amp * c * c;
+            }
+            double th = theta0 + dth;
+            double pi_ex = 1.0 - p.grav / (cp * th) * z;
+            double rho = p.MSLP / (R * th) * std::pow(pi_ex, cv / R);
+            double T = th * pi_ex;
+            double e_pot = AUXc(*m, e, APHI, n);
+            Q[(e * NS + 0) * m->Np + n] = rho;
+            for (int c = 1; c < 4; ++c) Q[(e * NS + c) * m->Np + n] = 0;
+            Q[(e * NS + 4) * m->Np + n] = rho * ((0.0 + e_pot) + cv * (T - p.T_0));
+        }
+}
+
+// Rest state equal to the reference state (discrete_hydrostatic_balance.jl:25-30)
+void om_init_rest(const om_model* m, double* Q) {
+    for (int64_t e = 0; e < m->nelem; ++e)
+        for (int n = 0; n < m->Np; ++n) {
+            Q[(e * NS + 0) * m->Np + n] = AUXc(*m, e, ARHO_REF, n);
+            for (int c = 1; c < 4; ++c) Q[(e * NS + c) * m->Np + n] = 0;
+            Q[(e * NS + 4) * m->Np + n] = AUXc(*m, e, ARHOE_REF, n);
+        }
+}
+
+}  // extern "C"

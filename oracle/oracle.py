@@ -1,0 +1,301 @@
+"""ctypes front end of the C++ oracle — TEST INFRASTRUCTURE ONLY.
+
+The oracle (``oracle/cmdg_oracle.cpp``) is a CPU FP64 restatement of
+ClimateMachine.jl's DGModel tendency, LSRK54 integrator and reductions.  Only
+``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may
+import this module; the product library never does.
+
+Parity status: pinned against the isentropic-vortex golden errors of
+``test/Numerics/DGMethods/Euler/isentropicvortex.jl:105-106`` and the LSRK54
+order of ``test/Numerics/ODESolvers/ode_tests_convergence.jl:41``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+# CLIMAParameters.jl 0.2.0 Earth values (Planet: gas_constant / molmass_dryair,
+# kappa_d = 2/7, T_0, MSLP, grav; SubgridScale: inv_Pr_turb = 3, C_smag = 0.21).
+_R_D = 8.3144598 / 28.97e-3
+_KAPPA_D = 2 / 7
+_CP_D = _R_D / _KAPPA_D
+EARTH = dict(
+    R_d=_R_D,
+    cp_d=_CP_D,
+    cv_d=_CP_D - _R_D,
+    T_0=273.16,
+    grav=9.81,
+    MSLP=1.01325e5,
+    inv_Pr_turb=3.0,
+    C_smag=0.21,
+    planet_radius=6.371e6,
+)
+
+
+class Brick(ctypes.Structure):
+    _fields_ = [
+        ("N", ctypes.c_int),
+        ("ne", ctypes.c_int * 3),
+        ("lo", ctypes.c_double * 3),
+        ("hi", ctypes.c_double * 3),
+        ("periodic", ctypes.c_int * 3),
+        ("bc_lo", ctypes.c_int * 3),
+        ("bc_hi", ctypes.c_int * 3),
+    ]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("R_d", ctypes.c_double),
+        ("cp_d", ctypes.c_double),
+        ("cv_d", ctypes.c_double),
+        ("T_0", ctypes.c_double),
+        ("grav", ctypes.c_double),
+        ("MSLP", ctypes.c_double),
+        ("inv_Pr_turb", ctypes.c_double),
+        ("numflux", ctypes.c_int),
+        ("orientation", ctypes.c_int),
+        ("gravity", ctypes.c_int),
+        ("ref_state", ctypes.c_int),
+        ("subtract_off", ctypes.c_int),
+        ("profile", ctypes.c_int),
+        ("T_surface", ctypes.c_double),
+        ("T_min", ctypes.c_double),
+        ("turbulence", ctypes.c_int),
+        ("rho_nu", ctypes.c_double),
+        ("with_divergence", ctypes.c_int),
+        ("C_smag", ctypes.c_double),
+    ]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (portable flags, any host)."""
+    src = os.path.join(HERE, "cmdg_oracle.cpp")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", HERE, "_build/liboracle.so"], check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.c_void_p
+        D = ctypes.c_double
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.om_create.restype = P
+        L.om_create.argtypes = [ctypes.POINTER(Brick), ctypes.POINTER(Params)]
+        L.om_free.argtypes = [P]
+        L.om_nelem.restype = ctypes.c_int64
+        L.om_nelem.argtypes = [P]
+        L.om_Np.argtypes = [P]
+        L.om_ngradflux.argtypes = [P]
+        for name in ("om_vgeo", "om_sgeo", "om_aux", "om_gradflux", "om_D", "om_lgl_nodes", "om_lgl_weights"):
+            getattr(L, name).restype = dp
+            getattr(L, name).argtypes = [P]
+        for name in ("om_vmapM", "om_vmapP"):
+            getattr(L, name).restype = ctypes.POINTER(ctypes.c_int64)
+            getattr(L, name).argtypes = [P]
+        L.om_elemtobndy.restype = ctypes.POINTER(ctypes.c_int)
+        L.om_elemtobndy.argtypes = [P]
+        L.om_set_threads.argtypes = [ctypes.c_int]
+        L.om_tendency.argtypes = [P, dp, dp, D, D, D]
+        L.om_gradient_pass.argtypes = [P, dp]
+        L.om_lsrk54.argtypes = [P, dp, dp, D, D, ctypes.c_int]
+        L.om_solve.restype = ctypes.c_int
+        L.om_solve.argtypes = [P, dp, D, D, D]
+        L.om_norm.restype = D
+        L.om_norm.argtypes = [P, dp]
+        L.om_euclidean_distance.restype = D
+        L.om_euclidean_distance.argtypes = [P, dp, dp]
+        L.om_field_l2.argtypes = [P, dp, dp, dp, dp]
+        L.om_weightedsum.restype = D
+        L.om_weightedsum.argtypes = [P, dp, ctypes.c_int]
+        L.om_courant_dt.restype = D
+        L.om_courant_dt.argtypes = [P, dp, D]
+        L.om_init_vortex.argtypes = [P, dp, D, D, D, D, D, D, D, D]
+        L.om_init_bubble.argtypes = [P, dp, D, D, D, D, D, D]
+        L.om_init_rest.argtypes = [P, dp]
+        L.om_lsrk54_scalar.restype = D
+        L.om_lsrk54_scalar.argtypes = [D, D, D]
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def set_threads(n: int) -> int:
+    return lib().om_set_threads(n)
+
+
+# Auxiliary field indices of the oracle's (Np, NAUX, nelem) aux array
+AUX = dict(x=0, y=1, z=2, Phi=3, gPhi=4, rho_ref=7, p_ref=8, T_ref=9, rhoe_ref=10, theta_v=11, air_T=12, Delta=13)
+NAUX = 14
+VGEO = dict(xi1x1=0, xi2x1=1, xi3x1=2, xi1x2=3, xi2x2=4, xi3x2=5, xi1x3=6, xi2x3=7, xi3x3=8, M=9, MI=10, MH=11,
+            x1=12, x2=13, x3=14, JcV=15)
+
+
+class OracleModel:
+    """A brick mesh + dry AtmosModel configuration evaluated by the oracle."""
+
+    def __init__(self, N, ne, lo, hi, periodic=(1, 1, 1), bc_lo=(1, 1, 1), bc_hi=(2, 2, 2), **physics):
+        b = Brick()
+        b.N = N
+        for d in range(3):
+            b.ne[d] = ne[d]
+            b.lo[d] = lo[d]
+            b.hi[d] = hi[d]
+            b.periodic[d] = int(periodic[d])
+            b.bc_lo[d] = bc_lo[d]
+            b.bc_hi[d] = bc_hi[d]
+        p = Params()
+        consts = dict(EARTH)
+        consts.update({k: v for k, v in physics.items() if k in EARTH})
+        for k in ("R_d", "cp_d", "cv_d", "T_0", "grav", "MSLP", "inv_Pr_turb"):
+            setattr(p, k, consts[k])
+        p.numflux = {"rusanov": 0, "central": 1}[physics.get("numflux", "rusanov")]
+        p.orientation = {"none": 0, "flat": 1}[physics.get("orientation", "none")]
+        p.gravity = int(physics.get("gravity", False))
+        p.ref_state = int(physics.get("ref_state", False))
+        p.subtract_off = int(physics.get("subtract_off", True))
+        p.profile = {"isothermal": 0, "dry_adiabatic": 1}[physics.get("profile", "dry_adiabatic")]
+        p.T_surface = physics.get("T_surface", 300.0)
+        p.T_min = physics.get("T_min", 0.0)
+        p.turbulence = {"none": 0, "constant": 1, "smagorinsky": 2}[physics.get("turbulence", "none")]
+        p.rho_nu = physics.get("rho_nu", 0.0)
+        p.with_divergence = int(physics.get("with_divergence", False))
+        p.C_smag = physics.get("C_smag", consts["C_smag"])
+        self.brick, self.params, self.consts = b, p, consts
+        self.L = lib()
+        self.h = self.L.om_create(ctypes.byref(b), ctypes.byref(p))
+        self.N = N
+        self.Nq = N + 1
+        self.Np = self.L.om_Np(self.h)
+        self.nelem = self.L.om_nelem(self.h)
+        self.nstate = 5
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.om_free(self.h)
+            self.h = None
+
+    # ------------------------------------------------------------ arrays
+    def _view(self, fn, shape, ctype=np.float64):
+        ptr = fn(self.h)
+        n = int(np.prod(shape))
+        buf = np.ctypeslib.as_array(ptr, shape=(n,))
+        return np.array(buf, dtype=ctype, copy=True).reshape(shape)
+
+    @property
+    def vgeo(self):
+        return self._view(self.L.om_vgeo, (self.nelem, 16, self.Np))
+
+    @property
+    def sgeo(self):
+        return self._view(self.L.om_sgeo, (self.nelem, 6, self.Nq * self.Nq, 5))
+
+    @property
+    def aux(self):
+        return self._view(self.L.om_aux, (self.nelem, NAUX, self.Np))
+
+    @property
+    def gradflux(self):
+        ngf = self.L.om_ngradflux(self.h)
+        return self._view(self.L.om_gradflux, (self.nelem, ngf, self.Np))
+
+    @property
+    def vmapM(self):
+        return self._view(self.L.om_vmapM, (self.nelem, 6, self.Nq * self.Nq), np.int64)
+
+    @property
+    def vmapP(self):
+        return self._view(self.L.om_vmapP, (self.nelem, 6, self.Nq * self.Nq), np.int64)
+
+    @property
+    def elemtobndy(self):
+        return self._view(self.L.om_elemtobndy, (self.nelem, 6), np.int32)
+
+    @property
+    def D(self):
+        # column-major (Julia) D[j, k] stored at j + Nq*k -> numpy [k, j]; return D[j, k]
+        return self._view(self.L.om_D, (self.Nq, self.Nq)).T.copy()
+
+    @property
+    def lgl(self):
+        return self._view(self.L.om_lgl_nodes, (self.Nq,)), self._view(self.L.om_lgl_weights, (self.Nq,))
+
+    def state(self):
+        return np.zeros((self.nelem, self.nstate, self.Np), dtype=np.float64)
+
+    # ------------------------------------------------------------ ops
+    def tendency(self, Q, t=0.0, alpha=1.0, beta=0.0, dQ=None):
+        if dQ is None:
+            dQ = self.state()
+        self.L.om_tendency(self.h, _ptr(dQ), _ptr(Q), t, alpha, beta)
+        return dQ
+
+    def gradient_pass(self, Q):
+        self.L.om_gradient_pass(self.h, _ptr(Q))
+        return self.gradflux
+
+    def lsrk54(self, Q, dt, nsteps, t0=0.0, dQ=None):
+        if dQ is None:
+            dQ = self.state()
+        self.L.om_lsrk54(self.h, _ptr(Q), _ptr(dQ), t0, dt, nsteps)
+        return Q, dQ
+
+    def solve(self, Q, dt, timeend, t0=0.0):
+        return self.L.om_solve(self.h, _ptr(Q), t0, dt, timeend)
+
+    def norm(self, Q):
+        return self.L.om_norm(self.h, _ptr(Q))
+
+    def euclidean_distance(self, A, B):
+        return self.L.om_euclidean_distance(self.h, _ptr(A), _ptr(B))
+
+    def field_l2(self, A, B):
+        err = np.zeros(5)
+        ref = np.zeros(5)
+        self.L.om_field_l2(self.h, _ptr(A), _ptr(B), _ptr(err), _ptr(ref))
+        return err, ref
+
+    def weightedsum(self, Q, field):
+        return self.L.om_weightedsum(self.h, _ptr(Q), field)
+
+    def courant_dt(self, Q, CFL):
+        return self.L.om_courant_dt(self.h, _ptr(Q), CFL)
+
+    def init_vortex(self, t=0.0, p_inf=1e5, T_inf=300.0, translation_speed=150.0, translation_angle=np.pi / 4,
+                    vortex_speed=50.0, R=1 / 200, L=1 / 20):
+        Q = self.state()
+        self.L.om_init_vortex(self.h, _ptr(Q), t, p_inf, T_inf, translation_speed, translation_angle, vortex_speed,
+                              R, L)
+        return Q
+
+    def init_bubble(self, theta0=300.0, amp=2.0, rc=250.0, xc=1250.0, yc=1250.0, zc=350.0):
+        Q = self.state()
+        self.L.om_init_bubble(self.h, _ptr(Q), theta0, amp, rc, xc, yc, zc)
+        return Q
+
+    def init_rest(self):
+        Q = self.state()
+        self.L.om_init_rest(self.h, _ptr(Q))
+        return Q
+
+
+def lsrk54_scalar(q0: float, dt: float, timeend: float) -> float:
+    """q' = q cos t integrated with the oracle's LSRK54 (exact: q0 exp(sin t))."""
+    return lib().om_lsrk54_scalar(q0, dt, timeend)

@@ -1,0 +1,75 @@
+"""The oracle reproduces the reference's own golden values.
+
+Pins (reference paths relative to the ClimateMachine.jl project root):
+  * isentropic vortex, FP64, 3D, Rusanov, N=4, levels 1 and 2 —
+    test/Numerics/DGMethods/Euler/isentropicvortex.jl:105-106 (rtol sqrt(eps)
+    in the reference; held here to 1e-10)
+  * LSRK54CarpenterKennedy order 4 +- 0.17 on q' = q cos t —
+    test/Numerics/ODESolvers/ode_tests_convergence.jl:15-44
+  * discrete hydrostatic balance of a rest state with the central flux —
+    test/Atmos/Model/discrete_hydrostatic_balance.jl (error <= 100 eps)
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+GOLDEN_VORTEX = {1: 3.7918869862613858e00, 2: 6.5816485664822677e-01}
+
+
+def vortex_error(level):
+    L = 1 / 20
+    ne = (5 * 2 ** (level - 1), 5 * 2 ** (level - 1), 1)
+    m = O.OracleModel(4, ne, (-L,) * 3, (L,) * 3, periodic=(1, 1, 1))
+    c = O.EARTH
+    timeend = 2 * L / 10 / 150
+    elementsize = (2 * L) / ne[0]
+    dt = elementsize / math.sqrt(c["cp_d"] / c["cv_d"] * c["R_d"] * 300.0) / 4**2
+    nsteps = math.ceil(timeend / dt)
+    dt = timeend / nsteps
+    Q = m.init_vortex(0.0)
+    m.solve(Q, dt, timeend)
+    return m.euclidean_distance(Q, m.init_vortex(timeend))
+
+
+@pytest.mark.parametrize("level", [1, 2])
+def test_isentropic_vortex_golden(level):
+    err = vortex_error(level)
+    assert err == pytest.approx(GOLDEN_VORTEX[level], rel=1e-10)
+
+
+def test_lsrk54_order():
+    errs = []
+    for k in (6, 7):
+        q = O.lsrk54_scalar(1.0, 2.0**-k, 20.0)
+        errs.append(abs(q - math.exp(math.sin(20.0))))
+    rate = math.log2(errs[0] / errs[1])
+    assert rate == pytest.approx(4.0, abs=0.17)
+
+
+@pytest.mark.parametrize("profile", ["isothermal", "dry_adiabatic"])
+def test_discrete_hydrostatic_balance(profile):
+    # LES box of discrete_hydrostatic_balance.jl: 50 km cube, 3 elements per
+    # direction, N=4, subtract_off=false, central flux, 100 s of LSRK54.
+    # The dry-adiabatic case (the rising-bubble background) uses a 10 km box,
+    # below the height where that profile's temperature reaches zero.
+    H = 50e3 if profile == "isothermal" else 10e3
+    m = O.OracleModel(4, (3, 3, 3), (0, 0, 0), (H, H, H), periodic=(1, 1, 0), numflux="central",
+                      orientation="flat", gravity=True, ref_state=True, subtract_off=False, profile=profile,
+                      T_surface=285.0 if profile == "isothermal" else 300.0, T_min=0.0)
+    Q0 = m.init_rest()
+    Q = Q0.copy()
+    dt = m.courant_dt(Q, 0.1)
+    m.solve(Q, dt, 100.0)
+    err = m.euclidean_distance(Q, Q0) / m.norm(Q0)
+    assert err <= 100 * np.finfo(np.float64).eps
+
+
+def test_weightedsum_is_compensated():
+    m = O.OracleModel(2, (2, 2, 2), (0, 0, 0), (1, 1, 1))
+    Q = m.state()
+    Q[:, 0, :] = 1.0
+    # sum of M over the unit cube is its volume
+    assert m.weightedsum(Q, 0) == pytest.approx(1.0, rel=1e-15)
