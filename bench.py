@@ -1,0 +1,319 @@
+"""Benchmark: DOF-stage updates/s of the DG tendency + LSRK54 hot path.
+
+Workload: the dry rising thermal bubble on a 2500 m cube, 20x20x20 elements,
+N=4 (1,000,000 nodes, 5,000,000 DOF), periodic in x and y, FreeSlip /
+Insulating walls at the bottom and top, FlatOrientation + Gravity,
+HydrostaticState(DryAdiabatic, theta0 = 300 K), +2 K cos^2 bubble of radius
+250 m centred 350 m above the bottom, dt from CFL 0.4.  A step is one
+LSRK54 step (5 fused tendency + stage kernels over the whole mesh).
+
+value      mixed FP32/FP64 path (FP32 perturbation state, FP64 RK register),
+           whole-job DOF-stage/s over all ranks, state resident in HBM; L2 is
+           flushed (256 MiB write) between timed steps and each step is timed
+           with CUDA events on the launching stream.
+fp64       the plain FP64 path, measured the same way.
+e2e        the same metric through the C ABI with the FP64 state in pinned
+           host memory: each step copies the state host->device, runs the
+           step and copies the result back, all inside the timed region.
+roofline   the dominant kernel (the fused mixed stage kernel) against the
+           measured HBM copy bandwidth; algorithmic bytes per node-stage
+           B = 2*5*4 (state r/w, FP32) + 2*5*8 (RK register r/w, FP64) = 120.
+cpu_baseline  the C++ oracle (the CPU restatement of the reference) on the
+           host cores, on a bounded sample of the same workload.
+
+--impl reference times the reference's CPU path (the oracle port, the
+reference itself is Julia and cannot run here) on the same workload.
+
+Multi-GPU: replicas only — each rank advances its own bubble; value is the
+sum over ranks of the work divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "climatemachine.jl_gb300")
+for _p in (REPO, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+NE = (20, 20, 20)
+N = 4
+L = 2500.0
+CFL = 0.4
+NSTAGE = 5
+NFIELD = 5
+BYTES_MIXED = 2 * 5 * 4 + 2 * 5 * 8   # per node-stage
+BYTES_FP64 = 2 * 5 * 8 + 2 * 5 * 8
+WORKLOAD = ("rising bubble: 20x20x20 elements, N=4 (1e6 nodes, 5e6 DOF), [0,2500 m]^3, periodic x/y, "
+            "FreeSlip walls z, dry Euler + gravity, HydrostaticState(DryAdiabatic 300 K), +2 K cos^2 bubble "
+            "r=250 m at z=350 m, Rusanov, LSRK54 at CFL 0.4")
+
+
+def measured_peak():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.proc = None
+        self.index = index
+        self.path = os.path.join(REPO, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}",
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return None
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 7:
+                    try:
+                        rows.append((float(parts[0]), float(parts[1]), parts[3:7]))
+                    except ValueError:
+                        pass
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def run_cpu_reference(steps, threads=None, sample_steps=None):
+    """Times the oracle (CPU restatement of the reference) on the workload."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+
+    threads = threads or os.cpu_count()
+    O.set_threads(threads)
+    om = O.OracleModel(N, NE, (0, 0, 0), (L, L, L), periodic=(1, 1, 0), orientation="flat", gravity=True,
+                       ref_state=True, profile="dry_adiabatic", T_surface=300.0, T_min=0.0)
+    Q = om.init_bubble(theta0=300.0, amp=2.0, rc=250.0, xc=1250.0, yc=1250.0, zc=350.0)
+    dt = om.courant_dt(Q, CFL)
+    dQ = om.state()
+    om.lsrk54(Q, dt, 1, dQ=dQ)  # warm-up
+    nsteps = sample_steps or steps
+    t0 = time.perf_counter()
+    om.lsrk54(Q, dt, nsteps, dQ=dQ)
+    el = time.perf_counter() - t0
+    nodes = om.nelem * om.Np
+    return dict(value=NFIELD * nodes * NSTAGE * nsteps / el, sec=el, steps=nsteps, threads=threads)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="cmdg", choices=["cmdg", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        r = run_cpu_reference(args.steps, sample_steps=max(1, min(args.steps, 3)))
+        line = {"metric": "DOF-stage updates/s", "value": r["value"], "unit": "DOF-stage/s", "n_gpus": args.gpus,
+                "steps": r["steps"], "warmup": 1, "ms_per_step": 1e3 * r["sec"] / r["steps"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "impl": "reference",
+                "config": {"workload": WORKLOAD, "path": "CPU FP64 oracle port of the reference DG + LSRK54"},
+                "cpu_baseline": {"value": r["value"], "unit": "DOF-stage/s", "cores": r["threads"], "kind": "port",
+                                 "sample": f"{r['steps']} LSRK54 steps of the full 1e6-node workload"},
+                "e2e": {"value": r["value"], "unit": "DOF-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as g
+
+    g.build_library()
+    import cmdg
+    from cmdg import workloads
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def build(precision):
+        dg = workloads.bubble_model(ne=NE, N=N, L=L, precision=precision)
+        xyz = dg.grid.coordinates()
+        Q0 = workloads.rising_bubble(xyz, theta0=300.0, amp=2.0, rc=250.0, center=(1250.0, 1250.0, 350.0))
+        return dg, Q0
+
+    def timed_run(dg, Q0, dt):
+        Q = dg.init_ode_state(Q0)
+        lsrk = cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt)
+        for _ in range(args.warmup):
+            cmdg.dostep_(Q, lsrk, None, 0.0)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        barrier()
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            ev[i][0].record(stream)
+            cmdg.dostep_(Q, lsrk, None, 0.0)
+            ev[i][1].record(stream)
+        barrier()
+        ms = [a.elapsed_time(b) for a, b in ev]
+        return Q, sum(ms), ms
+
+    dg64, Q0 = build("fp64")
+    dgmx, _ = build("mixed")
+    dt = dg64.courant_dt(dg64.init_ode_state(Q0), CFL)
+    nodes = dg64.grid.nelem * dg64.grid.Np
+
+    with ClockSampler(local_rank) as clk:
+        Qmx, ms_mx, per_mx = timed_run(dgmx, Q0, dt)
+    Q64, ms_64, per_64 = timed_run(dg64, Q0, dt)
+
+    # accuracy of the mixed path against the FP64 path after warmup+steps
+    a = dgmx.from_perturbation(Qmx).cpu().numpy()
+    b = Q64.cpu().numpy()
+    M = dg64.grid.mass()
+    rel = [math.sqrt(float(np.sum((a[:, s] - b[:, s]) ** 2 * M))) / math.sqrt(float(np.sum(b[:, s] ** 2 * M)))
+           for s in range(5)]
+
+    # e2e: host FP64 state, H2D + step + D2H per step through the C ABI
+    host = torch.from_numpy(np.ascontiguousarray(Q0)).pin_memory()
+    Qd = torch.empty_like(host, device="cuda")
+    Qp = dgmx.new_state(torch.float32)
+    dQ = torch.zeros(host.shape, dtype=torch.float64, device="cuda")
+    def e2e_step():
+        Qd.copy_(host, non_blocking=True)
+        dgmx.to_perturbation(Qd, out=Qp)
+        dgmx.lsrk54_step(Qp, dQ, 0.0, dt, 1)
+        dgmx.from_perturbation(Qp, out=Qd)
+        host.copy_(Qd, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    ms_e2e = e0.elapsed_time(e1)
+
+    # max over ranks
+    def rmax(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    ms_mx, ms_64, ms_e2e = rmax(ms_mx), rmax(ms_64), rmax(ms_e2e)
+    work = world * NFIELD * nodes * NSTAGE * args.steps
+    value = work / (ms_mx * 1e-3)
+    v64 = work / (ms_64 * 1e-3)
+    ve2e = work / (ms_e2e * 1e-3)
+    peak, peak_kind = measured_peak()
+    stage_ms_mx = ms_mx / args.steps / NSTAGE
+    stage_ms_64 = ms_64 / args.steps / NSTAGE
+    ach_mx = BYTES_MIXED * nodes / (stage_ms_mx * 1e-3) / 1e9
+    ach_64 = BYTES_FP64 * nodes / (stage_ms_64 * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(REPO, "profiles", "stage_mixed_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get("bytes_per_launch_full_size")
+        except Exception:
+            traffic = None
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            r = run_cpu_reference(1, sample_steps=2)
+            cpu = {"value": r["value"], "unit": "DOF-stage/s", "cores": r["threads"], "kind": "port",
+                   "sample": f"{r['steps']} LSRK54 steps of the full 1e6-node workload, FP64 oracle"}
+        except Exception as exc:  # the CPU leg must not hide the GPU line
+            cpu = {"value": None, "error": str(exc)[:200]}
+
+    if rank == 0:
+        line = {
+            "metric": "DOF-stage updates/s", "value": value, "unit": "DOF-stage/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mx / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "path": "mixed FP32 perturbation / FP64 RK register",
+                       "l2": "256 MiB buffer written between timed steps (L2 is 129 MB)",
+                       "parallelism": f"replicas x{world}", "dt": dt},
+            "fp64": {"value": v64, "ms_per_step": ms_64 / args.steps,
+                     "roofline": {"bound": "hbm", "achieved": ach_64, "peak": peak, "unit": "GB/s",
+                                  "frac": ach_64 / peak}},
+            "mixed_speedup_vs_fp64": value / v64,
+            "mixed_vs_fp64_rel_l2": rel,
+            "roofline": {"bound": "hbm", "achieved": ach_mx, "peak": peak, "unit": "GB/s", "frac": ach_mx / peak,
+                         "traffic": traffic, "peak_source": peak_kind,
+                         "kernel": "stage_kernel<4,float,mixed,stage>", "bytes_per_node_stage": BYTES_MIXED},
+            "cpu_baseline": cpu,
+            "e2e": {"value": ve2e, "unit": "DOF-stage/s", "h2d_bytes_per_step": int(host.numel() * 8),
+                    "d2h_bytes_per_step": int(host.numel() * 8)},
+            "gpu_launches": args.steps * NSTAGE,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,24 @@
+"""cmdg — GB300-native DG tendency + LSRK54 engine for the dry AtmosModel.
+
+Host-side mirror of ClimateMachine.jl's BalanceLaw / DGModel / ODESolvers API
+for the DG spectral-element hot path, backed by libcmdg.so (hand-written CUDA
+for sm_103a behind a C ABI, include/cmdg.h).  Names follow the reference:
+
+    grid  = BrickGrid(N, ne, lo, hi, periodicity=...)        # BrickTopology + Grid
+    model = AtmosModel(orientation="flat", ref_state=HydrostaticState(...), ...)
+    dg    = DGModel(model, grid, numerical_flux="rusanov", precision="fp64")
+    Q     = dg.init_ode_state(initial_condition)
+    dg(dQ, Q, None, t)                                        # dQ = dQ/dt(Q)
+    lsrk  = LSRK54CarpenterKennedy(dg, Q, dt=dt, t0=0.0)
+    solve_(Q, lsrk, timeend=...)                              # solve!(Q, lsrk; timeend)
+"""
+from .atmos import EARTH, AtmosModel, HydrostaticState, DryAdiabaticProfile, IsothermalProfile
+from .dgmodel import DGModel, BrickGrid, euclidean_distance, weightedsum, norm
+from .odesolvers import LSRK54CarpenterKennedy, solve_, dostep_
+from ._lib import CmdgError, load as load_library
+
+__all__ = [
+    "EARTH", "AtmosModel", "HydrostaticState", "DryAdiabaticProfile", "IsothermalProfile", "DGModel", "BrickGrid",
+    "euclidean_distance", "weightedsum", "norm", "LSRK54CarpenterKennedy", "solve_", "dostep_", "CmdgError",
+    "load_library",
+]

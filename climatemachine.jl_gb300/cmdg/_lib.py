@@ -1,0 +1,109 @@
+"""ctypes binding of libcmdg.so (the C ABI declared in include/cmdg.h).
+
+The library is built in-tree by ``climatemachine.jl_gb300/build.py``.  There
+is no CPU fallback: if the shared library is missing or cannot be loaded,
+every entry point raises ``CmdgError``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG_ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG_ROOT, "_build", "libcmdg.so")
+
+CMDG_OK = 0
+ERRORS = {1: "CMDG_ERR_ARG", 2: "CMDG_ERR_CUDA", 3: "CMDG_ERR_UNSUPPORTED", 4: "CMDG_ERR_NONFINITE",
+          5: "CMDG_ERR_TIMEOUT", 6: "CMDG_ERR_ALLOC", 7: "CMDG_ERR_STATE"}
+CMDG_FP64, CMDG_MIXED = 0, 1
+
+# Every exported symbol of include/cmdg.h (checked by the CPU test suite).
+EXPORTS = (
+    "cmdg_last_error", "cmdg_version", "cmdg_mesh_create_brick", "cmdg_mesh_destroy", "cmdg_mesh_info",
+    "cmdg_mesh_coordinates", "cmdg_mesh_mass", "cmdg_model_create", "cmdg_model_destroy",
+    "cmdg_model_reference_state", "cmdg_tendency", "cmdg_lsrk54_step", "cmdg_to_perturbation",
+    "cmdg_from_perturbation", "cmdg_tendency_mixed", "cmdg_lsrk54_step_mixed", "cmdg_weighted_sums",
+    "cmdg_weighted_sums_mixed", "cmdg_courant_dt", "cmdg_status_word",
+)
+
+
+class CmdgError(RuntimeError):
+    """A libcmdg entry point returned an error code."""
+
+    def __init__(self, fn: str, code: int, msg: str):
+        super().__init__(f"{fn} -> {ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class BrickDesc(ctypes.Structure):
+    _fields_ = [("N", ctypes.c_int), ("ne", ctypes.c_int * 3), ("lo", ctypes.c_double * 3),
+                ("hi", ctypes.c_double * 3), ("periodic", ctypes.c_int * 3), ("bc_lo", ctypes.c_int * 3),
+                ("bc_hi", ctypes.c_int * 3)]
+
+
+class AtmosParams(ctypes.Structure):
+    _fields_ = [("R_d", ctypes.c_double), ("cp_d", ctypes.c_double), ("cv_d", ctypes.c_double),
+                ("T_0", ctypes.c_double), ("grav", ctypes.c_double), ("MSLP", ctypes.c_double),
+                ("inv_Pr_turb", ctypes.c_double), ("numflux", ctypes.c_int), ("orientation", ctypes.c_int),
+                ("gravity", ctypes.c_int), ("ref_state", ctypes.c_int), ("subtract_off", ctypes.c_int),
+                ("profile", ctypes.c_int), ("T_surface", ctypes.c_double), ("T_min", ctypes.c_double),
+                ("turbulence", ctypes.c_int), ("rho_nu", ctypes.c_double), ("with_divergence", ctypes.c_int),
+                ("C_smag", ctypes.c_double)]
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Loads libcmdg.so and declares the prototypes; raises if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise CmdgError("load", 3, f"{path} is missing: build it with climatemachine.jl_gb300/build.py")
+    L = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    D = ctypes.c_double
+    I = ctypes.c_int
+    L.cmdg_last_error.restype = ctypes.c_char_p
+    L.cmdg_version.restype = ctypes.c_char_p
+    proto = {
+        "cmdg_mesh_create_brick": [ctypes.POINTER(BrickDesc), PP],
+        "cmdg_mesh_destroy": [P],
+        "cmdg_mesh_info": [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int)],
+        "cmdg_mesh_coordinates": [P, P],
+        "cmdg_mesh_mass": [P, P],
+        "cmdg_model_create": [P, ctypes.POINTER(AtmosParams), I, PP],
+        "cmdg_model_destroy": [P],
+        "cmdg_model_reference_state": [P, P],
+        "cmdg_tendency": [P, P, P, D, D, D, P],
+        "cmdg_lsrk54_step": [P, P, P, D, D, I, P],
+        "cmdg_to_perturbation": [P, P, P, P],
+        "cmdg_from_perturbation": [P, P, P, P],
+        "cmdg_tendency_mixed": [P, P, P, D, D, D, P],
+        "cmdg_lsrk54_step_mixed": [P, P, P, D, D, I, P],
+        "cmdg_weighted_sums": [P, P, I, P, P, P],
+        "cmdg_weighted_sums_mixed": [P, P, I, P, P, P],
+        "cmdg_courant_dt": [P, P, D, P, P],
+        "cmdg_status_word": [P, P, P],
+    }
+    for name, args in proto.items():
+        fn = getattr(L, name)
+        fn.restype = ctypes.c_int
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(fn_name: str, rc: int):
+    if rc != CMDG_OK:
+        msg = load().cmdg_last_error().decode(errors="replace")
+        raise CmdgError(fn_name, rc, msg)
+
+
+def call(fn_name: str, *args):
+    rc = getattr(load(), fn_name)(*args)
+    check(fn_name, rc)

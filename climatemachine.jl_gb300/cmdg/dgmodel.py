@@ -1,0 +1,202 @@
+"""DGModel and grid objects over libcmdg.so.
+
+``DGModel`` mirrors the SpaceDiscretization functor of the reference:
+``dg(tendency, Q, param, t; increment)`` computes
+``tendency = dQ/dt(Q) + increment * tendency``
+(src/Numerics/DGMethods/SpaceDiscretization.jl:68-77,
+src/Numerics/DGMethods/DGModel.jl:85-427).  State arrays are torch tensors on
+the current CUDA device of shape (nelem, 5, Np) — the same memory as the
+reference's column-major MPIStateArray ``.data[Np, nstate, nelem]``.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import AtmosParams, BrickDesc, call
+
+NSTATE = 5
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _dptr(t: torch.Tensor):
+    if not t.is_cuda or not t.is_contiguous():
+        raise ValueError("state arrays must be contiguous CUDA tensors")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+class BrickGrid:
+    """BrickTopology/StackedBrickTopology + DiscontinuousSpectralElementGrid
+    (src/Numerics/Mesh/Topologies.jl:470-545,632; src/Numerics/Mesh/Grids.jl:267-414).
+
+    Elements are ordered with the vertical index fastest, then x, then y.
+    ``boundary`` gives the tags of the (lower, upper) faces of each
+    non-periodic direction, as in the reference's ``boundary`` keyword.
+    """
+
+    def __init__(self, N, ne, lo, hi, periodicity=(True, True, True), boundary=((1, 2), (1, 2), (1, 2))):
+        _lib.load()
+        d = BrickDesc()
+        d.N = int(N)
+        for k in range(3):
+            d.ne[k] = int(ne[k])
+            d.lo[k] = float(lo[k])
+            d.hi[k] = float(hi[k])
+            d.periodic[k] = int(bool(periodicity[k]))
+            d.bc_lo[k] = int(boundary[k][0])
+            d.bc_hi[k] = int(boundary[k][1])
+        h = ctypes.c_void_p()
+        call("cmdg_mesh_create_brick", ctypes.byref(d), ctypes.byref(h))
+        self.h = h
+        self.desc = d
+        nelem = ctypes.c_int64()
+        Np = ctypes.c_int()
+        call("cmdg_mesh_info", self.h, ctypes.byref(nelem), ctypes.byref(Np))
+        self.N, self.Nq, self.nelem, self.Np = int(N), int(N) + 1, nelem.value, Np.value
+        self.ne = tuple(int(x) for x in ne)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.cmdg_mesh_destroy(self.h)
+            self.h = None
+
+    def coordinates(self) -> np.ndarray:
+        xyz = np.empty((self.nelem, 3, self.Np), dtype=np.float64)
+        call("cmdg_mesh_coordinates", self.h, ctypes.c_void_p(xyz.ctypes.data))
+        return xyz
+
+    def mass(self) -> np.ndarray:
+        M = np.empty((self.nelem, self.Np), dtype=np.float64)
+        call("cmdg_mesh_mass", self.h, ctypes.c_void_p(M.ctypes.data))
+        return M
+
+
+class DGModel:
+    """DGModel(balance_law, grid, numerical_flux_first_order, ...) on the GPU.
+
+    precision="fp64": plain Float64 state.
+    precision="mixed": FP32 state perturbation about the FP64 hydrostatic
+    reference state with an FP64 RK register (see ``to_perturbation``).
+    """
+
+    def __init__(self, balance_law, grid: BrickGrid, numerical_flux: str = "rusanov", precision: str = "fp64"):
+        self.balance_law = balance_law
+        self.grid = grid
+        self.numerical_flux = numerical_flux
+        self.precision = precision
+        self.mixed = precision == "mixed"
+        p: AtmosParams = balance_law.c_params(numerical_flux)
+        self._params = p
+        h = ctypes.c_void_p()
+        call("cmdg_model_create", grid.h, ctypes.byref(p), _lib.CMDG_MIXED if self.mixed else _lib.CMDG_FP64,
+             ctypes.byref(h))
+        self.h = h
+        self.device = torch.device("cuda", torch.cuda.current_device())
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.cmdg_model_destroy(self.h)
+            self.h = None
+
+    # ------------------------------------------------------------------ state
+    @property
+    def state_dtype(self):
+        return torch.float32 if self.mixed else torch.float64
+
+    def new_state(self, dtype=None) -> torch.Tensor:
+        return torch.zeros((self.grid.nelem, NSTATE, self.grid.Np), dtype=dtype or self.state_dtype,
+                           device=self.device)
+
+    def init_ode_state(self, Q_host: np.ndarray) -> torch.Tensor:
+        """Copies a host FP64 state (nelem, 5, Np) to the device in the model's
+        own representation (FP64, or the FP32 perturbation for "mixed")."""
+        Q64 = torch.from_numpy(np.ascontiguousarray(Q_host, dtype=np.float64)).to(self.device)
+        if not self.mixed:
+            return Q64
+        return self.to_perturbation(Q64)
+
+    def reference_state(self) -> np.ndarray:
+        out = np.empty((self.grid.nelem, 3, self.grid.Np), dtype=np.float64)
+        call("cmdg_model_reference_state", self.h, ctypes.c_void_p(out.ctypes.data))
+        return out
+
+    def to_perturbation(self, Q64: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        Qp = self.new_state(torch.float32) if out is None else out
+        call("cmdg_to_perturbation", self.h, _dptr(Qp), _dptr(Q64), _stream())
+        return Qp
+
+    def from_perturbation(self, Qp: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        Q64 = self.new_state(torch.float64) if out is None else out
+        call("cmdg_from_perturbation", self.h, _dptr(Q64), _dptr(Qp), _stream())
+        return Q64
+
+    def full_state(self, Q: torch.Tensor) -> torch.Tensor:
+        """FP64 full state of Q whatever the model's representation."""
+        return self.from_perturbation(Q) if self.mixed else Q
+
+    # ------------------------------------------------------------------ tendency
+    def __call__(self, tendency, Q, param=None, t=0.0, alpha=None, beta=None, increment=False):
+        """tendency = alpha * dQ/dt(Q) + beta * tendency; the 4-argument form
+        is alpha = 1, beta = increment (SpaceDiscretization.jl:68-77)."""
+        a = 1.0 if alpha is None else float(alpha)
+        b = (1.0 if increment else 0.0) if beta is None else float(beta)
+        if tendency.dtype != torch.float64:
+            raise ValueError("the tendency / RK register is FP64 in every precision")
+        fn = "cmdg_tendency_mixed" if self.mixed else "cmdg_tendency"
+        if Q.dtype != self.state_dtype:
+            raise ValueError(f"state dtype {Q.dtype} does not match the model ({self.state_dtype})")
+        call(fn, self.h, _dptr(tendency), _dptr(Q), float(t), a, b, _stream())
+        return tendency
+
+    def lsrk54_step(self, Q, dQ, t, dt, nsteps=1):
+        fn = "cmdg_lsrk54_step_mixed" if self.mixed else "cmdg_lsrk54_step"
+        call(fn, self.h, _dptr(Q), _dptr(dQ), float(t), float(dt), int(nsteps), _stream())
+
+    # ------------------------------------------------------------------ reductions
+    def weighted_sums(self, Q, fields=(0, 4)):
+        fl = (ctypes.c_int * len(fields))(*fields)
+        out = (ctypes.c_double * len(fields))()
+        fn = "cmdg_weighted_sums_mixed" if self.mixed else "cmdg_weighted_sums"
+        call(fn, self.h, _dptr(Q), len(fields), fl, out, _stream())
+        return list(out)
+
+    def courant_dt(self, Q, CFL):
+        dt = ctypes.c_double()
+        call("cmdg_courant_dt", self.h, _dptr(self.full_state(Q)), float(CFL), ctypes.byref(dt), _stream())
+        return dt.value
+
+    def status_word(self) -> int:
+        st = ctypes.c_uint32()
+        call("cmdg_status_word", self.h, ctypes.byref(st), _stream())
+        return st.value
+
+
+def _host(Q: torch.Tensor) -> np.ndarray:
+    return Q.detach().to("cpu", torch.float64).numpy()
+
+
+def norm(dg: DGModel, Q) -> float:
+    """Weighted L2 norm sqrt(sum M q^2) (src/Arrays/MPIStateArrays.jl:583-606)."""
+    q = _host(dg.full_state(Q))
+    M = dg.grid.mass()
+    return math.sqrt(float(np.sum(q * q * M[:, None, :])))
+
+
+def euclidean_distance(dg: DGModel, A, B) -> float:
+    """sqrt(sum M (A-B)^2) (src/Arrays/MPIStateArrays.jl:628-648)."""
+    a = _host(dg.full_state(A))
+    b = _host(dg.full_state(B)) if isinstance(B, torch.Tensor) else np.asarray(B)
+    M = dg.grid.mass()
+    return math.sqrt(float(np.sum((a - b) ** 2 * M[:, None, :])))
+
+
+def weightedsum(dg: DGModel, Q, field: int) -> float:
+    """Compensated sum M q[field] (src/Arrays/MPIStateArrays.jl:655-675)."""
+    return dg.weighted_sums(Q, (field,))[0]

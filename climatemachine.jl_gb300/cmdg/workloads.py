@@ -1,0 +1,78 @@
+"""Synthetic workloads: the configurations the benchmark and tests run.
+
+Initial conditions are evaluated in FP64 on the host from the grid's node
+coordinates (the reference evaluates its ``init_state_prognostic`` on the
+nodes in the same way, src/Numerics/DGMethods/SpaceDiscretization.jl:79-148).
+
+* ``isentropic_vortex``: test/Numerics/DGMethods/Euler/isentropicvortex_setup.jl
+  (translation 150 m/s at pi/4, vortex speed 50, radius L/10, Mach-0.5 style
+  advection), plus optional seeded uniform noise.
+* ``rising_bubble``: dry rising thermal bubble about an isentropic
+  (dry-adiabatic) hydrostatic background of potential temperature theta0,
+  with a cos^2 bump of amplitude A and radius rc centred at (xc, yc, zc)
+  (the structure of experiments/TestCase/risingbubble.jl:23-91).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .atmos import EARTH, AtmosModel, DryAdiabaticProfile, HydrostaticState
+from .dgmodel import BrickGrid, DGModel
+
+
+def isentropic_vortex(xyz: np.ndarray, t: float = 0.0, *, p_inf=1e5, T_inf=300.0, translation_speed=150.0,
+                      translation_angle=math.pi / 4, vortex_speed=50.0, R=1 / 200, L=1 / 20, consts=EARTH,
+                      noise=0.0, seed=0) -> np.ndarray:
+    R_d, cp, cv, T0 = consts["R_d"], consts["cp_d"], consts["cv_d"], consts["T_0"]
+    kappa = R_d / cp
+    rho_inf = p_inf / (R_d * T_inf)
+    uinf = np.array([translation_speed * math.cos(translation_angle), translation_speed * math.sin(translation_angle), 0.0])
+    x = xyz.copy()
+    for d in range(3):
+        x[:, d, :] -= uinf[d] * t
+        x[:, d, :] -= np.floor((x[:, d, :] + L) / (2 * L)) * (2 * L)
+    r = np.sqrt(x[:, 0] ** 2 + x[:, 1] ** 2)
+    g = np.exp(-((r / R) ** 2) / 2)
+    u = np.stack([uinf[0] - vortex_speed * x[:, 1] / R * g, uinf[1] + vortex_speed * x[:, 0] / R * g,
+                  np.zeros_like(r)], axis=1)
+    T = T_inf * (1 - kappa * vortex_speed**2 / 2 * rho_inf / p_inf * np.exp(-((r / R) ** 2)))
+    p = p_inf * (T / T_inf) ** (1 / kappa)
+    rho = p / (R_d * T)
+    Q = np.empty((xyz.shape[0], 5, xyz.shape[2]))
+    Q[:, 0] = rho
+    Q[:, 1:4] = rho[:, None, :] * u
+    Q[:, 4] = rho * (0.5 * np.sum(u * u, axis=1) + cv * (T - T0))
+    if noise:
+        rng = np.random.default_rng(seed)
+        Q += rng.uniform(-noise, noise, size=Q.shape)
+    return Q
+
+
+def rising_bubble(xyz: np.ndarray, *, theta0=300.0, amp=2.0, rc=250.0, center=(1250.0, 1250.0, 350.0),
+                  consts=EARTH) -> np.ndarray:
+    R_d, cp, cv, T0, g, p0 = (consts[k] for k in ("R_d", "cp_d", "cv_d", "T_0", "grav", "MSLP"))
+    x, y, z = xyz[:, 0], xyz[:, 1], xyz[:, 2]
+    xc, yc, zc = center
+    r = np.sqrt((x - xc) ** 2 + (y - yc) ** 2 + (z - zc) ** 2)
+    dth = np.where(r <= rc, amp * np.cos(np.pi * r / (2 * rc)) ** 2, 0.0)
+    th = theta0 + dth
+    pi_ex = 1.0 - g / (cp * th) * z
+    rho = p0 / (R_d * th) * pi_ex ** (cv / R_d)
+    T = th * pi_ex
+    Q = np.zeros((xyz.shape[0], 5, xyz.shape[2]))
+    Q[:, 0] = rho
+    Q[:, 4] = rho * (g * z + cv * (T - T0))
+    return Q
+
+
+def bubble_model(ne=(20, 20, 20), N=4, L=2500.0, precision="fp64", numerical_flux="rusanov"):
+    """The dry rising-bubble configuration: [0, L]^3, periodic in x and y,
+    FreeSlip/Insulating walls at the bottom and top, FlatOrientation + Gravity,
+    HydrostaticState(DryAdiabaticProfile(300 K)), inviscid."""
+    grid = BrickGrid(N, ne, (0.0, 0.0, 0.0), (L, L, L), periodicity=(True, True, False),
+                     boundary=((0, 0), (0, 0), (1, 2)))
+    model = AtmosModel(orientation="flat", gravity=True,
+                       ref_state=HydrostaticState(DryAdiabaticProfile(300.0, 0.0), subtract_off=True))
+    return DGModel(model, grid, numerical_flux=numerical_flux, precision=precision)

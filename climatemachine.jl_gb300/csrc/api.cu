@@ -1,0 +1,375 @@
+// C ABI of libcmdg.so: object lifetime, argument checking, LSRK54 stepping
+// with CUDA-graph capture, and the thin wrappers over the kernels.
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+
+#include "cmdg_internal.h"
+
+namespace cmdg {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+const char* last_error() { return g_err; }
+
+// LSRK54CarpenterKennedy 2N-storage coefficients (Carpenter & Kennedy 1994,
+// NASA TM-109112), exact rationals as in
+// src/Numerics/ODESolvers/LowStorageRungeKuttaMethod.jl:302-324.
+static const double LSRK_A[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
+                                 -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
+static const double LSRK_B[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+                                 1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+                                 2277821191437.0 / 14882151754819.0};
+
+// Two state-sized scratch buffers: the five stages of a step run
+// Q -> S1 -> S2 -> S1 -> S2 -> Q, so every stage reads one buffer and writes
+// another and the step ends in the caller's Q without a copy.
+static int ensure_scratch(Model* md) {
+    const Mesh& m = *md->mesh;
+    const size_t elt = md->precision == CMDG_MIXED ? sizeof(float) : sizeof(double);
+    const size_t need = 2 * (size_t)m.nelem * NSTATE * m.Np * elt;
+    if (md->scratch_bytes >= need) return CMDG_OK;
+    if (md->d_scratch) cudaFree(md->d_scratch);
+    md->d_scratch = nullptr;
+    md->scratch_bytes = 0;
+    cudaError_t e = cudaMalloc(&md->d_scratch, need);
+    if (e != cudaSuccess) {
+        set_error("scratch allocation of %zu bytes failed: %s", need, cudaGetErrorString(e));
+        return CMDG_ERR_ALLOC;
+    }
+    md->scratch_bytes = need;
+    return CMDG_OK;
+}
+
+// Issues 5*nsteps fused stage kernels on stream s (stage buffers
+// Q -> S1 -> S2 -> S1 -> S2 -> Q for every step).
+static int issue_steps(Model* md, void* Q, double* dQ, double dt, int nsteps, cudaStream_t s) {
+    const Mesh& m = *md->mesh;
+    const size_t elt = md->precision == CMDG_MIXED ? sizeof(float) : sizeof(double);
+    const size_t bytes = (size_t)m.nelem * NSTATE * m.Np * elt;
+    char* S1 = static_cast<char*>(md->d_scratch);
+    char* S2 = S1 + bytes;
+    void* const order[6] = {Q, S1, S2, S1, S2, Q};
+    for (int step = 0; step < nsteps; ++step) {
+        for (int st = 0; st < 5; ++st) {
+            LaunchArgs a;
+            a.Qin = order[st];
+            a.Qout = order[st + 1];
+            a.dQ = dQ;
+            a.alpha = 1.0;
+            a.beta = 1.0;
+            a.rka = LSRK_A[(st + 1) % 5];
+            a.rkb_dt = LSRK_B[st] * dt;
+            a.mode = 1;
+            int rc = launch_stage(md, a, s);
+            if (rc) return rc;
+        }
+    }
+    return CMDG_OK;
+}
+
+static int run_steps(Model* md, void* Q, double* dQ, double dt, int nsteps, cudaStream_t s) {
+    int rc = ensure_scratch(md);
+    if (rc) return rc;
+    if (s == nullptr || nsteps > 64) return issue_steps(md, Q, dQ, dt, nsteps, s);
+    // capture once per (Q, dQ, dt, nsteps, stream), replay afterwards
+    GraphKey key{Q, dQ, dt, nsteps, (void*)s};
+    auto it = md->graphs.find(key);
+    if (it == md->graphs.end()) {
+        cudaGraph_t g;
+        CMDG_CUDA_CHECK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        rc = issue_steps(md, Q, dQ, dt, nsteps, s);
+        cudaError_t ce = cudaStreamEndCapture(s, &g);
+        if (rc) return rc;
+        if (ce != cudaSuccess) {
+            set_error("graph capture failed: %s", cudaGetErrorString(ce));
+            return CMDG_ERR_CUDA;
+        }
+        cudaGraphExec_t ex;
+        ce = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            set_error("graph instantiate failed: %s", cudaGetErrorString(ce));
+            return CMDG_ERR_CUDA;
+        }
+        if (md->graphs.size() > 32) {
+            for (auto& kv : md->graphs) cudaGraphExecDestroy(kv.second);
+            md->graphs.clear();
+        }
+        it = md->graphs.emplace(key, ex).first;
+    }
+    CMDG_CUDA_CHECK(cudaGraphLaunch(it->second, s));
+    return CMDG_OK;
+}
+
+static int check_model(const cmdg_model* model) {
+    if (!model) {
+        set_error("model is NULL");
+        return CMDG_ERR_ARG;
+    }
+    return CMDG_OK;
+}
+
+}  // namespace cmdg
+
+using namespace cmdg;
+
+extern "C" {
+
+const char* cmdg_last_error(void) { return cmdg::last_error(); }
+
+const char* cmdg_version(void) { return "cmdg 0.1 (sm_103a)"; }
+
+int cmdg_mesh_create_brick(const cmdg_brick_desc* desc, cmdg_mesh** out) {
+    CMDG_ARG_CHECK(out != nullptr, "output pointer is NULL");
+    *out = nullptr;
+    cmdg_mesh* mh = new cmdg_mesh();
+    int rc = build_brick(desc, &mh->m);
+    if (rc) {
+        if (mh->m.d_emetric) cudaFree(mh->m.d_emetric);
+        if (mh->m.d_nbr) cudaFree(mh->m.d_nbr);
+        delete mh;
+        return rc;
+    }
+    *out = mh;
+    return CMDG_OK;
+}
+
+int cmdg_mesh_destroy(cmdg_mesh* mesh) {
+    if (!mesh) return CMDG_OK;
+    cudaFree(mesh->m.d_emetric);
+    cudaFree(mesh->m.d_nbr);
+    delete mesh;
+    return CMDG_OK;
+}
+
+int cmdg_mesh_info(const cmdg_mesh* mesh, int64_t* nelem, int* Np) {
+    CMDG_ARG_CHECK(mesh != nullptr, "mesh is NULL");
+    if (nelem) *nelem = mesh->m.nelem;
+    if (Np) *Np = mesh->m.Np;
+    return CMDG_OK;
+}
+
+int cmdg_mesh_coordinates(const cmdg_mesh* mesh, double* h_xyz) {
+    CMDG_ARG_CHECK(mesh != nullptr && h_xyz != nullptr, "NULL argument");
+    const Mesh& m = mesh->m;
+    const int Nq = m.Nq, Np = m.Np;
+    for (int64_t e = 0; e < m.nelem; ++e) {
+        const int64_t iz = e % m.nz;
+        const int64_t ix = (e / m.nz) % m.desc.ne[0];
+        const int64_t iy = e / ((int64_t)m.nz * m.desc.ne[0]);
+        const int64_t idx[3] = {ix, iy, iz};
+        for (int d = 0; d < 3; ++d) {
+            const double lo = m.desc.lo[d], hi = m.desc.hi[d];
+            const int n = m.desc.ne[d];
+            const double a = (double)(((long double)lo * (n - idx[d]) + (long double)hi * idx[d]) / n);
+            const double b = (double)(((long double)lo * (n - idx[d] - 1) + (long double)hi * (idx[d] + 1)) / n);
+            for (int node = 0; node < Np; ++node) {
+                const int ijk[3] = {node % Nq, (node / Nq) % Nq, node / (Nq * Nq)};
+                h_xyz[((size_t)e * 3 + d) * Np + node] = a + (m.xi[ijk[d]] + 1) * 0.5 * (b - a);
+            }
+        }
+    }
+    return CMDG_OK;
+}
+
+int cmdg_mesh_mass(const cmdg_mesh* mesh, double* h_M) {
+    CMDG_ARG_CHECK(mesh != nullptr && h_M != nullptr, "NULL argument");
+    const Mesh& m = mesh->m;
+    const int Nq = m.Nq, Np = m.Np;
+    for (int64_t e = 0; e < m.nelem; ++e) {
+        const double J = 8.0 / (m.emetric[3 * e] * m.emetric[3 * e + 1] * m.emetric[3 * e + 2]);
+        for (int node = 0; node < Np; ++node) {
+            const int i = node % Nq, j = (node / Nq) % Nq, k = node / (Nq * Nq);
+            h_M[(size_t)e * Np + node] = J * (m.omega[i] * m.omega[j] * m.omega[k]);
+        }
+    }
+    return CMDG_OK;
+}
+
+int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision, cmdg_model** out) {
+    CMDG_ARG_CHECK(out != nullptr, "output pointer is NULL");
+    *out = nullptr;
+    CMDG_ARG_CHECK(mesh != nullptr && p != nullptr, "NULL argument");
+    CMDG_ARG_CHECK(precision == CMDG_FP64 || precision == CMDG_MIXED, "unknown precision %d", precision);
+    CMDG_ARG_CHECK(p->numflux == CMDG_FLUX_RUSANOV || p->numflux == CMDG_FLUX_CENTRAL, "unknown numerical flux %d",
+                   p->numflux);
+    CMDG_ARG_CHECK(p->orientation == CMDG_ORIENT_NONE || p->orientation == CMDG_ORIENT_FLAT,
+                   "orientation %d is not available on a brick", p->orientation);
+    CMDG_ARG_CHECK(p->R_d > 0 && p->cv_d > 0 && p->cp_d > 0, "gas constants must be positive");
+    if (p->turbulence != CMDG_TURB_NONE) {
+        set_error("turbulence closure %d: the diffusive passes are not built into this library version",
+                  p->turbulence);
+        return CMDG_ERR_UNSUPPORTED;
+    }
+    cmdg_model* mo = new cmdg_model();
+    Model& md = mo->m;
+    md.mesh = &mesh->m;
+    md.prm = *p;
+    md.precision = precision;
+    md.ph.R_d = p->R_d;
+    md.ph.cv_d = p->cv_d;
+    md.ph.gamma = p->cp_d / p->cv_d;
+    md.ph.gm1 = p->R_d / p->cv_d;
+    md.ph.T_0 = p->T_0;
+    md.ph.grav = p->grav;
+    md.ph.inv_cv = 1.0 / p->cv_d;
+    md.ph.numflux = p->numflux;
+    md.ph.gravity = p->gravity;
+    md.ph.ref_state = p->ref_state;
+    md.ph.subtract_off = p->subtract_off;
+    md.ph.turbulence = p->turbulence;
+    int rc = init_model_tables(&md);
+    if (rc == CMDG_OK) {
+        cudaError_t e = cudaMalloc(&md.d_status, sizeof(unsigned));
+        if (e == cudaSuccess) e = cudaMemset(md.d_status, 0, sizeof(unsigned));
+        if (e != cudaSuccess) {
+            set_error("status word allocation failed: %s", cudaGetErrorString(e));
+            rc = CMDG_ERR_CUDA;
+        }
+    }
+    if (rc) {
+        cmdg_model_destroy(mo);
+        return rc;
+    }
+    *out = mo;
+    return CMDG_OK;
+}
+
+int cmdg_model_destroy(cmdg_model* model) {
+    if (!model) return CMDG_OK;
+    Model& md = model->m;
+    for (auto& kv : md.graphs) cudaGraphExecDestroy(kv.second);
+    cudaFree(md.d_lvl64);
+    cudaFree(md.d_lvl32);
+    cudaFree(md.d_jump32);
+    cudaFree(md.d_Dhat64);
+    cudaFree(md.d_Dhat32);
+    cudaFree(md.d_status);
+    cudaFree(md.d_scratch);
+    cudaFree(md.d_red);
+    release_quad(&md);
+    delete model;
+    return CMDG_OK;
+}
+
+int cmdg_model_reference_state(const cmdg_model* model, double* h_ref) {
+    int rc = check_model(model);
+    if (rc) return rc;
+    CMDG_ARG_CHECK(h_ref != nullptr, "NULL output");
+    const Model& md = model->m;
+    const Mesh& m = *md.mesh;
+    for (int64_t e = 0; e < m.nelem; ++e)
+        for (int node = 0; node < m.Np; ++node) {
+            const int lev = (int)(e % m.nz) * m.Nq + node / m.Nfp;
+            const double* L = &md.lvl64[(size_t)lev * LV_NFIELDS];
+            h_ref[((size_t)e * 3 + 0) * m.Np + node] = L[LV_RHO_REF];
+            h_ref[((size_t)e * 3 + 1) * m.Np + node] = L[LV_RHOE_REF];
+            h_ref[((size_t)e * 3 + 2) * m.Np + node] = L[LV_P_REF];
+        }
+    return CMDG_OK;
+}
+
+int cmdg_tendency(cmdg_model* model, double* d_dQ, const double* d_Q, double t, double alpha, double beta,
+                  void* stream) {
+    (void)t;
+    int rc = check_model(model);
+    if (rc) return rc;
+    CMDG_ARG_CHECK(model->m.precision == CMDG_FP64, "cmdg_tendency needs an FP64 model");
+    CMDG_ARG_CHECK(d_dQ != nullptr && d_Q != nullptr, "NULL state");
+    LaunchArgs a{d_Q, nullptr, d_dQ, alpha, beta, 0.0, 0.0, 0};
+    return launch_stage(&model->m, a, (cudaStream_t)stream);
+}
+
+int cmdg_tendency_mixed(cmdg_model* model, double* d_dQ, const float* d_Qp, double t, double alpha, double beta,
+                        void* stream) {
+    (void)t;
+    int rc = check_model(model);
+    if (rc) return rc;
+    CMDG_ARG_CHECK(model->m.precision == CMDG_MIXED, "cmdg_tendency_mixed needs a mixed-precision model");
+    CMDG_ARG_CHECK(d_dQ != nullptr && d_Qp != nullptr, "NULL state");
+    LaunchArgs a{d_Qp, nullptr, d_dQ, alpha, beta, 0.0, 0.0, 0};
+    return launch_stage(&model->m, a, (cudaStream_t)stream);
+}
+
+int cmdg_lsrk54_step(cmdg_model* model, double* d_Q, double* d_dQ, double t, double dt, int nsteps, void* stream) {
+    (void)t;
+    int rc = check_model(model);
+    if (rc) return rc;
+    CMDG_ARG_CHECK(model->m.precision == CMDG_FP64, "cmdg_lsrk54_step needs an FP64 model");
+    CMDG_ARG_CHECK(d_Q != nullptr && d_dQ != nullptr, "NULL state");
+    CMDG_ARG_CHECK(nsteps >= 0, "nsteps must be >= 0");
+    CMDG_ARG_CHECK(std::isfinite(dt) && dt > 0, "dt must be positive and finite");
+    if (nsteps == 0) return CMDG_OK;
+    return run_steps(&model->m, d_Q, d_dQ, dt, nsteps, (cudaStream_t)stream);
+}
+
+int cmdg_lsrk54_step_mixed(cmdg_model* model, float* d_Qp, double* d_dQ, double t, double dt, int nsteps,
+                           void* stream) {
+    (void)t;
+    int rc = check_model(model);
+    if (rc) return rc;
+    CMDG_ARG_CHECK(model->m.precision == CMDG_MIXED, "cmdg_lsrk54_step_mixed needs a mixed-precision model");
+    CMDG_ARG_CHECK(d_Qp != nullptr && d_dQ != nullptr, "NULL state");
+    CMDG_ARG_CHECK(nsteps >= 0, "nsteps must be >= 0");
+    CMDG_ARG_CHECK(std::isfinite(dt) && dt > 0, "dt must be positive and finite");
+    if (nsteps == 0) return CMDG_OK;
+    return run_steps(&model->m, d_Qp, d_dQ, dt, nsteps, (cudaStream_t)stream);
+}
+
+int cmdg_to_perturbation(cmdg_model* model, float* d_Qp, const double* d_Q, void* stream) {
+    int rc = check_model(model);
+    if (rc) return rc;
+    CMDG_ARG_CHECK(d_Qp != nullptr && d_Q != nullptr, "NULL state");
+    return launch_to_perturbation(&model->m, d_Qp, d_Q, (cudaStream_t)stream);
+}
+
+int cmdg_from_perturbation(cmdg_model* model, double* d_Q, const float* d_Qp, void* stream) {
+    int rc = check_model(model);
+    if (rc) return rc;
+    CMDG_ARG_CHECK(d_Qp != nullptr && d_Q != nullptr, "NULL state");
+    return launch_from_perturbation(&model->m, d_Q, d_Qp, (cudaStream_t)stream);
+}
+
+int cmdg_weighted_sums(cmdg_model* model, const double* d_Q, int nfields, const int* h_fields, double* h_out,
+                       void* stream) {
+    int rc = check_model(model);
+    if (rc) return rc;
+    CMDG_ARG_CHECK(d_Q && h_fields && h_out && nfields > 0, "bad arguments");
+    return weighted_sums(&model->m, d_Q, false, nfields, h_fields, h_out, (cudaStream_t)stream);
+}
+
+int cmdg_weighted_sums_mixed(cmdg_model* model, const float* d_Qp, int nfields, const int* h_fields, double* h_out,
+                             void* stream) {
+    int rc = check_model(model);
+    if (rc) return rc;
+    CMDG_ARG_CHECK(d_Qp && h_fields && h_out && nfields > 0, "bad arguments");
+    return weighted_sums(&model->m, d_Qp, true, nfields, h_fields, h_out, (cudaStream_t)stream);
+}
+
+int cmdg_courant_dt(cmdg_model* model, const double* d_Q, double CFL, double* h_dt, void* stream) {
+    int rc = check_model(model);
+    if (rc) return rc;
+    CMDG_ARG_CHECK(d_Q && h_dt && CFL > 0, "bad arguments");
+    return courant_dt(&model->m, d_Q, CFL, h_dt, (cudaStream_t)stream);
+}
+
+int cmdg_status_word(cmdg_model* model, uint32_t* h_status, void* stream) {
+    int rc = check_model(model);
+    if (rc) return rc;
+    CMDG_ARG_CHECK(h_status != nullptr, "NULL output");
+    cudaStream_t s = (cudaStream_t)stream;
+    CMDG_CUDA_CHECK(cudaMemcpyAsync(h_status, model->m.d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CMDG_CUDA_CHECK(cudaMemsetAsync(model->m.d_status, 0, sizeof(unsigned), s));
+    CMDG_CUDA_CHECK(cudaStreamSynchronize(s));
+    return CMDG_OK;
+}
+
+}  // extern "C"

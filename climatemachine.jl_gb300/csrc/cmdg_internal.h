@@ -1,0 +1,142 @@
+// Internal declarations shared by the libcmdg translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/cmdg.h"
+
+namespace cmdg {
+
+// ---------------------------------------------------------------------------
+// error reporting
+// ---------------------------------------------------------------------------
+void set_error(const char* fmt, ...);
+const char* last_error();
+
+#define CMDG_CUDA_CHECK(call)                                                                       \
+    do {                                                                                            \
+        cudaError_t _e = (call);                                                                    \
+        if (_e != cudaSuccess) {                                                                    \
+            ::cmdg::set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__, __LINE__); \
+            return CMDG_ERR_CUDA;                                                                   \
+        }                                                                                           \
+    } while (0)
+
+#define CMDG_ARG_CHECK(cond, ...)           \
+    do {                                    \
+        if (!(cond)) {                      \
+            ::cmdg::set_error(__VA_ARGS__); \
+            return CMDG_ERR_ARG;            \
+        }                                   \
+    } while (0)
+
+constexpr int NSTATE = 5;
+constexpr int MIN_N = 2;
+constexpr int MAX_N = 5;
+
+// per vertical node level ("lvl") table columns (FP64 and FP32 copies)
+enum LevelField {
+    LV_PHI = 0,     // gravitational potential Phi = g z
+    LV_GPHIZ,       // DG derivative dPhi/dz (the only non-zero component on a brick)
+    LV_RHO_REF,     // reference density
+    LV_P_REF,       // reference pressure
+    LV_RHOE_REF,    // reference total energy density
+    LV_CRHO,        // R_d T_0 - (R_d/cv_d) Phi : pressure coefficient of rho
+    LV_HREF,        // rhoe_ref + p_ref : reference total enthalpy density
+    LV_NFIELDS
+};
+
+// Physical constants in the form the kernels use them.
+struct Physics {
+    double R_d, cv_d, gamma, gm1, T_0, grav, inv_cv;
+    int numflux, gravity, ref_state, subtract_off, turbulence;
+};
+
+struct Mesh {
+    cmdg_brick_desc desc;
+    int N = 0, Nq = 0, Np = 0, Nfp = 0;
+    int64_t nelem = 0;
+    int nz = 0;                      // elements per column
+    int nlev = 0;                    // vertical node levels = nz * Nq
+    std::vector<double> xi, omega;   // LGL nodes / weights
+    std::vector<double> D;           // D[j*Nq + k] = d l_k / d xi at xi_j
+    std::vector<double> Dhat;        // Dhat[i*Nq + n] = D[n][i] w_n / w_i (weak-form volume operator)
+    std::vector<double> emetric;     // [nelem][3] dxi_d/dx_d (affine brick)
+    std::vector<int> nbr;            // [nelem][6] neighbour element, or -tag on a boundary face
+    std::vector<double> zlev;        // [nlev] node height of each vertical level
+    std::vector<double> dzlev;       // [nlev] dz/dxi3 derivative helper (xi3x3 per level)
+    // device copies
+    double* d_emetric = nullptr;
+    int* d_nbr = nullptr;
+};
+
+struct GraphKey {
+    const void* Q;
+    const void* dQ;
+    double dt;
+    int nsteps;
+    void* stream;
+    bool operator<(const GraphKey& o) const {
+        return std::tie(Q, dQ, dt, nsteps, stream) < std::tie(o.Q, o.dQ, o.dt, o.nsteps, o.stream);
+    }
+};
+
+struct Model {
+    Mesh* mesh = nullptr;
+    cmdg_atmos_params prm;
+    Physics ph;
+    int precision = CMDG_FP64;
+    std::vector<double> lvl64;       // [nlev][LV_NFIELDS]
+    std::vector<float> lvl32;        // [nlev][LV_NFIELDS]
+    std::vector<float> jump32;       // [nz][2] FP64-computed ref jumps (rho, rhoe) across the bottom face of level ez
+    double* d_lvl64 = nullptr;
+    float* d_lvl32 = nullptr;
+    float* d_jump32 = nullptr;
+    double* d_Dhat64 = nullptr;
+    float* d_Dhat32 = nullptr;
+    unsigned* d_status = nullptr;
+    void* d_scratch = nullptr;       // two state-sized stage buffers (S1, S2) for the fused stage kernels
+    size_t scratch_bytes = 0;
+    double* d_red = nullptr;         // reduction partials
+    size_t red_len = 0;
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+};
+
+// host-side setup (mesh.cpp)
+int build_brick(const cmdg_brick_desc* desc, Mesh* m);
+void lgl_nodes(int N, std::vector<double>& x, std::vector<double>& w);
+int init_model_tables(Model* md);
+
+// kernel launchers (stage.cu)
+struct LaunchArgs {
+    const void* Qin;
+    void* Qout;
+    double* dQ;
+    double alpha, beta;      // tendency mode
+    double rka, rkb_dt;      // stage mode
+    int mode;                // 0 = tendency, 1 = RK stage
+};
+int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
+
+// reductions / conversions (reduce.cu)
+int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s);
+int launch_from_perturbation(Model* md, double* Q, const float* Qp, cudaStream_t s);
+int weighted_sums(Model* md, const void* Q, bool mixed, int nfields, const int* fields, double* out, cudaStream_t s);
+int courant_dt(Model* md, const double* Q, double CFL, double* dt, cudaStream_t s);
+void release_quad(const Model* md);
+
+}  // namespace cmdg
+
+struct cmdg_mesh {
+    cmdg::Mesh m;
+};
+struct cmdg_model {
+    cmdg::Model m;
+};

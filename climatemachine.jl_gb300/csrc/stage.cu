@@ -1,0 +1,381 @@
+// Fused DG tendency + LSRK stage kernels for brick meshes (sm_103a).
+//
+// One CTA owns one element for a whole stage:
+//   phase 1  every node loads its state (coalesced), evaluates the dry
+//            AtmosModel thermodynamics and its first-order flux in the three
+//            directions and stages them in shared memory;
+//   phase 2  every face node (6 (N+1)^2 of them) gathers the neighbour's
+//            state at the matching node, forms the Rusanov (or central)
+//            flux F*.n and stores it lifted, vMI*sM*F*, in shared memory;
+//   phase 3  every node contracts the staged fluxes with the weak-form
+//            derivative Dhat = M^-1 D^T M along xi1, xi2, xi3, subtracts its
+//            face terms, adds gravity and finishes either the tendency
+//            T = alpha*dQ/dt + beta*T or the LSRK 2N stage update
+//            dQ <- dQ/dt + dQ; Q <- Q + B_s dt dQ; dQ <- A_{s+1} dQ.
+// The state is read from one buffer and the stage's new state written to
+// another, so neighbouring elements never see a half-updated state.
+//
+// Algorithm restated from src/Numerics/DGMethods/DGModel_kernels.jl:64-548
+// (volume_tendency!, H and V), :588-901 (dgsem_interface_tendency!),
+// src/Numerics/DGMethods/NumericalFluxes.jl:219-340 (Rusanov / central),
+// src/Atmos/Model/{tendencies_mass.jl:7-9, tendencies_momentum.jl:13-29,60-72,
+// tendencies_energy.jl:7-21, AtmosModel.jl:776-796, bc_momentum.jl:25-34} and
+// src/Numerics/ODESolvers/LowStorageRungeKuttaMethod.jl:102-158.
+//
+// On an affine brick element the contravariant flux M xi_d . F reduces to
+// J w_i w_j w_k (2/dx_d) F_d, so the volume term at node (i,j,k) is
+// (2/dx_1) sum_n Dhat[i][n] F_1(n,j,k) + ... with Dhat[i][n] = D[n][i] w_n / w_i,
+// and the lift vMI*sM on a face normal to xi_d is (2/dx_d) / w_0.
+//
+// Precision: R = double (plain FP64) or R = float (mixed).  In the mixed
+// form the state held in memory is the FP32 perturbation q' = q - q_ref about
+// the FP64 hydrostatic reference state; pressure is formed directly as the
+// perturbation p' = (R/cv)(rhoe' - |rhou|^2/(2 rho)) + rho' (R T0 - (R/cv) Phi),
+// which is exact algebra for dry air (T = T0 + e_int/cv, p = rho R T), the
+// reference-state jump across vertical faces enters the Rusanov penalty
+// from an FP64-computed table, and the RK register dQ stays FP64.
+#include "cmdg_internal.h"
+
+namespace cmdg {
+namespace {
+
+template <int N>
+struct Dims {
+    static constexpr int Nq = N + 1;
+    static constexpr int Nfp = Nq * Nq;
+    static constexpr int Np = Nq * Nq * Nq;
+    static constexpr int NF = 6 * Nfp;
+    static constexpr int NT = (((Np > NF) ? Np : NF) + 31) / 32 * 32;
+};
+
+struct KParams {
+    const void* Qin;
+    void* Qout;
+    double* dQ;
+    const double* emetric;
+    const int* nbr;
+    const double* lvl64;
+    const float* lvl32;
+    const float* jump32;
+    const void* Dhat;
+    unsigned* status;
+    int nelem, nz;
+    double alpha, beta, rka, rkb_dt;
+    double inv_w0;
+    Physics ph;
+};
+
+template <typename R>
+struct Level {
+    R rho_ref, p_ref, href, crho, gphiz;
+};
+
+template <typename R>
+__device__ __forceinline__ Level<R> load_level(const KParams& P, int lev);
+
+template <>
+__device__ __forceinline__ Level<double> load_level<double>(const KParams& P, int lev) {
+    const double* L = P.lvl64 + (size_t)lev * LV_NFIELDS;
+    Level<double> l;
+    l.rho_ref = L[LV_RHO_REF];
+    l.p_ref = L[LV_P_REF];
+    l.href = L[LV_HREF];
+    l.crho = L[LV_CRHO];
+    l.gphiz = L[LV_GPHIZ];
+    return l;
+}
+
+template <>
+__device__ __forceinline__ Level<float> load_level<float>(const KParams& P, int lev) {
+    const float* L = P.lvl32 + (size_t)lev * LV_NFIELDS;
+    Level<float> l;
+    l.rho_ref = L[LV_RHO_REF];
+    l.p_ref = L[LV_P_REF];
+    l.href = L[LV_HREF];
+    l.crho = L[LV_CRHO];
+    l.gphiz = L[LV_GPHIZ];
+    return l;
+}
+
+// Pointwise thermodynamics of dry air (PhaseDry: T = T0 + e_int/cv, p = rho R T,
+// c = sqrt(gamma R T)) for a conserved state q, which is the full state
+// (R = double) or the perturbation about the reference state (MIXED).
+template <typename R, bool MIXED>
+struct Thermo {
+    R rinv;   // 1 / rho
+    R u[3];   // velocity
+    R pflux;  // pressure entering the momentum flux (p - p_ref with subtract_off)
+    R H;      // rhoe + p
+    R c;      // sound speed
+};
+
+template <typename R, bool MIXED>
+__device__ __forceinline__ Thermo<R, MIXED> thermo(const R q[NSTATE], const Level<R>& lv, const Physics& ph) {
+    Thermo<R, MIXED> t;
+    const R gm1 = (R)ph.gm1, gamma = (R)ph.gamma;
+    R rho = MIXED ? (lv.rho_ref + q[0]) : q[0];
+    t.rinv = R(1) / rho;
+    t.u[0] = q[1] * t.rinv;
+    t.u[1] = q[2] * t.rinv;
+    t.u[2] = q[3] * t.rinv;
+    R ke2 = q[1] * t.u[0] + q[2] * t.u[1] + q[3] * t.u[2];
+    R p;
+    if (MIXED) {
+        // p' = gm1 (rhoe' - ke/2) + rho' crho ; p = p_ref + p'
+        R pp = gm1 * (q[4] - R(0.5) * ke2) + q[0] * lv.crho;
+        p = lv.p_ref + pp;
+        t.pflux = (ph.ref_state && ph.subtract_off) ? pp : p;
+        t.H = lv.href + (q[4] + pp);
+    } else {
+        p = gm1 * (q[4] - R(0.5) * ke2) + rho * lv.crho;
+        t.pflux = (ph.ref_state && ph.subtract_off) ? (p - lv.p_ref) : p;
+        t.H = q[4] + p;
+    }
+    t.c = sqrt(gamma * p * t.rinv);
+    return t;
+}
+
+// first-order flux component in direction d for field s
+template <typename R, bool MIXED>
+__device__ __forceinline__ R flux_d(const R q[NSTATE], const Thermo<R, MIXED>& t, int d, int s) {
+    if (s == 0) return q[1 + d];
+    if (s == 4) return t.u[d] * t.H;
+    return q[1 + d] * t.u[s - 1] + ((s - 1 == d) ? t.pflux : R(0));
+}
+
+// component d (0, 1, 2; a run-time value) of a 3-vector without indexing a
+// local array, so the values stay in registers
+template <typename R>
+__device__ __forceinline__ R pick3(int d, R a, R b, R c) {
+    return d == 0 ? a : (d == 1 ? b : c);
+}
+
+// normal first-order flux F_d (all 5 fields) for a face normal to xi_d
+template <typename R, bool MIXED>
+__device__ __forceinline__ void normal_flux(const R q[NSTATE], const Thermo<R, MIXED>& t, int d, R sgn, R F[NSTATE]) {
+    const R mn = pick3(d, q[1], q[2], q[3]);
+    const R un = pick3(d, t.u[0], t.u[1], t.u[2]);
+    F[0] = sgn * mn;
+    F[1] = sgn * (mn * t.u[0] + (d == 0 ? t.pflux : R(0)));
+    F[2] = sgn * (mn * t.u[1] + (d == 1 ? t.pflux : R(0)));
+    F[3] = sgn * (mn * t.u[2] + (d == 2 ? t.pflux : R(0)));
+    F[4] = sgn * (un * t.H);
+}
+
+template <int N>
+__device__ __forceinline__ int face_node(int f, int a, int b) {
+    constexpr int Nq = N + 1;
+    switch (f) {
+        case 0: return 0 + Nq * (a + Nq * b);
+        case 1: return N + Nq * (a + Nq * b);
+        case 2: return a + Nq * (0 + Nq * b);
+        case 3: return a + Nq * (N + Nq * b);
+        case 4: return a + Nq * (b + Nq * 0);
+        default: return a + Nq * (b + Nq * N);
+    }
+}
+
+template <int N, typename R, bool MIXED, int MODE>
+__global__ void __launch_bounds__(Dims<N>::NT) stage_kernel(const KParams P) {
+    using Dm = Dims<N>;
+    constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp;
+    __shared__ R s_q[NSTATE][Np];
+    __shared__ R s_F[3][NSTATE][Np];
+    __shared__ R s_c[Np];
+    __shared__ R s_ri[Np];
+    __shared__ R s_fs[6][NSTATE][Nfp];
+    __shared__ R s_D[Nq * Nq];
+
+    const int e = blockIdx.x;
+    const int t = threadIdx.x;
+    const int ez = e % P.nz;
+    const R* __restrict__ Qin = static_cast<const R*>(P.Qin);
+    const Physics& ph = P.ph;
+
+    if (t < Nq * Nq) s_D[t] = static_cast<const R*>(P.Dhat)[t];
+    const R xi[3] = {(R)P.emetric[3 * e + 0], (R)P.emetric[3 * e + 1], (R)P.emetric[3 * e + 2]};
+
+    // ---------------- phase 1: node state, thermodynamics, volume fluxes
+    R q[NSTATE];
+    R gsrc = 0;
+    if (t < Np) {
+        const int k = t / Nfp;
+        const Level<R> lv = load_level<R>(P, ez * Nq + k);
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) q[s] = Qin[((size_t)e * NSTATE + s) * Np + t];
+        const Thermo<R, MIXED> th = thermo<R, MIXED>(q, lv, ph);
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) {
+            s_q[s][t] = q[s];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) s_F[d][s][t] = flux_d<R, MIXED>(q, th, d, s);
+        }
+        s_c[t] = th.c;
+        s_ri[t] = th.rinv;
+        if (ph.gravity) {
+            R rho_s = MIXED ? ((ph.ref_state && ph.subtract_off) ? q[0] : lv.rho_ref + q[0])
+                            : ((ph.ref_state && ph.subtract_off) ? q[0] - lv.rho_ref : q[0]);
+            gsrc = -rho_s * lv.gphiz;
+        }
+    }
+    __syncthreads();
+
+    // ---------------- phase 2: face fluxes
+    for (int ft = t; ft < 6 * Nfp; ft += Dm::NT) {
+        const int f = ft / Nfp, fn = ft % Nfp;
+        const int a = fn % Nq, b = fn / Nq;
+        const int d = f >> 1;
+        const R sgn = (f & 1) ? R(1) : R(-1);
+        const int vM = face_node<N>(f, a, b);
+        R qm[NSTATE], qp[NSTATE], Fm[NSTATE], Fp[NSTATE], jr[NSTATE] = {0, 0, 0, 0, 0};
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) {
+            qm[s] = s_q[s][vM];
+            Fm[s] = sgn * s_F[d][s][vM];
+        }
+        const R lam_m = fabs(pick3(d, qm[1], qm[2], qm[3]) * s_ri[vM]) + s_c[vM];
+        const int nb = P.nbr[6 * e + f];
+        int levp;
+        if (nb >= 0) {
+            const int vP = face_node<N>(f ^ 1, a, b);
+            const int kP = vP / Nfp;
+            levp = (nb % P.nz) * Nq + kP;
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) qp[s] = Qin[((size_t)nb * NSTATE + s) * Np + vP];
+            if (MIXED && d == 2 && ph.numflux == CMDG_FLUX_RUSANOV) {
+                if (f == 4) {
+                    jr[0] = (R)P.jump32[2 * ez + 0];
+                    jr[4] = (R)P.jump32[2 * ez + 1];
+                } else {
+                    const int ea = (ez + 1) % P.nz;
+                    jr[0] = -(R)P.jump32[2 * ea + 0];
+                    jr[4] = -(R)P.jump32[2 * ea + 1];
+                }
+            }
+        } else {
+            // Impenetrable(FreeSlip) + Insulating wall: rhou+ = rhou- - 2 (rhou-.n) n
+            levp = ez * Nq + vM / Nfp;
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) qp[s] = qm[s];
+            qp[1] = (d == 0) ? -qm[1] : qm[1];
+            qp[2] = (d == 1) ? -qm[2] : qm[2];
+            qp[3] = (d == 2) ? -qm[3] : qm[3];
+        }
+        const Level<R> lvp = load_level<R>(P, levp);
+        const Thermo<R, MIXED> thp = thermo<R, MIXED>(qp, lvp, ph);
+        normal_flux<R, MIXED>(qp, thp, d, sgn, Fp);
+        const R lam_p = fabs(pick3(d, thp.u[0], thp.u[1], thp.u[2])) + thp.c;
+        const R lift = (R)(P.emetric[3 * e + d] * P.inv_w0);
+        const R hmw = (ph.numflux == CMDG_FLUX_RUSANOV) ? R(0.5) * fmax(lam_m, lam_p) : R(0);
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) {
+            R fstar = R(0.5) * (Fm[s] + Fp[s]) + hmw * ((qm[s] - qp[s]) + jr[s]);
+            s_fs[f][s][fn] = lift * fstar;
+        }
+    }
+    __syncthreads();
+
+    // ---------------- phase 3: volume contraction, face terms, source, update
+    int bad = 0;
+    if (t < Np) {
+        const int i = t % Nq, j = (t / Nq) % Nq, k = t / Nfp;
+        R Di[Nq], Dj[Nq], Dk[Nq];
+#pragma unroll
+        for (int n = 0; n < Nq; ++n) {
+            Di[n] = s_D[i * Nq + n];
+            Dj[n] = s_D[j * Nq + n];
+            Dk[n] = s_D[k * Nq + n];
+        }
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) {
+            R c1 = 0, c2 = 0, c3 = 0;
+#pragma unroll
+            for (int n = 0; n < Nq; ++n) {
+                c1 = fma(Di[n], s_F[0][s][n + Nq * (j + Nq * k)], c1);
+                c2 = fma(Dj[n], s_F[1][s][i + Nq * (n + Nq * k)], c2);
+                c3 = fma(Dk[n], s_F[2][s][i + Nq * (j + Nq * n)], c3);
+            }
+            R rhs = xi[0] * c1 + xi[1] * c2 + xi[2] * c3;
+            if (i == 0) rhs -= s_fs[0][s][j + Nq * k];
+            if (i == N) rhs -= s_fs[1][s][j + Nq * k];
+            if (j == 0) rhs -= s_fs[2][s][i + Nq * k];
+            if (j == N) rhs -= s_fs[3][s][i + Nq * k];
+            if (k == 0) rhs -= s_fs[4][s][i + Nq * j];
+            if (k == N) rhs -= s_fs[5][s][i + Nq * j];
+            if (s == 3) rhs += gsrc;
+            if (!isfinite(rhs)) bad = 1;
+            const size_t idx = ((size_t)e * NSTATE + s) * Np + t;
+            if (MODE == 0) {
+                double out = P.alpha * (double)rhs;
+                if (P.beta != 0) out += P.beta * P.dQ[idx];
+                P.dQ[idx] = out;
+            } else {
+                const double dq = (double)rhs + P.dQ[idx];
+                R* Qout = static_cast<R*>(P.Qout);
+                if (MIXED) {
+                    Qout[idx] = q[s] + (R)(P.rkb_dt * dq);
+                } else {
+                    Qout[idx] = (R)((double)q[s] + P.rkb_dt * dq);
+                }
+                P.dQ[idx] = P.rka * dq;
+            }
+        }
+    }
+    if (__syncthreads_or(bad) && t == 0) atomicOr(P.status, 1u);
+}
+
+template <int N, typename R, bool MIXED>
+cudaError_t launch_typed(const KParams& P, int mode, cudaStream_t s) {
+    dim3 grid((unsigned)P.nelem), block(Dims<N>::NT);
+    if (mode == 0)
+        stage_kernel<N, R, MIXED, 0><<<grid, block, 0, s>>>(P);
+    else
+        stage_kernel<N, R, MIXED, 1><<<grid, block, 0, s>>>(P);
+    return cudaGetLastError();
+}
+
+template <int N>
+cudaError_t launch_N(const KParams& P, bool mixed, int mode, cudaStream_t s) {
+    return mixed ? launch_typed<N, float, true>(P, mode, s) : launch_typed<N, double, false>(P, mode, s);
+}
+
+}  // namespace
+
+int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
+    const Mesh& m = *md->mesh;
+    KParams P;
+    P.Qin = a.Qin;
+    P.Qout = a.Qout;
+    P.dQ = a.dQ;
+    P.emetric = m.d_emetric;
+    P.nbr = m.d_nbr;
+    P.lvl64 = md->d_lvl64;
+    P.lvl32 = md->d_lvl32;
+    P.jump32 = md->d_jump32;
+    const bool mixed = md->precision == CMDG_MIXED;
+    P.Dhat = mixed ? (const void*)md->d_Dhat32 : (const void*)md->d_Dhat64;
+    P.status = md->d_status;
+    P.nelem = (int)m.nelem;
+    P.nz = m.nz;
+    P.alpha = a.alpha;
+    P.beta = a.beta;
+    P.rka = a.rka;
+    P.rkb_dt = a.rkb_dt;
+    P.inv_w0 = 1.0 / m.omega[0];
+    P.ph = md->ph;
+    cudaError_t err;
+    switch (m.N) {
+        case 2: err = launch_N<2>(P, mixed, a.mode, s); break;
+        case 3: err = launch_N<3>(P, mixed, a.mode, s); break;
+        case 4: err = launch_N<4>(P, mixed, a.mode, s); break;
+        case 5: err = launch_N<5>(P, mixed, a.mode, s); break;
+        default: set_error("no kernel instantiated for N=%d", m.N); return CMDG_ERR_UNSUPPORTED;
+    }
+    if (err != cudaSuccess) {
+        set_error("stage kernel launch failed: %s", cudaGetErrorString(err));
+        return CMDG_ERR_CUDA;
+    }
+    return CMDG_OK;
+}
+
+}  // namespace cmdg

@@ -1,0 +1,181 @@
+/*
+ * cmdg.h — C ABI of libcmdg.so, a GB300 (sm_103a) implementation of
+ * ClimateMachine.jl's DG spectral-element tendency and LSRK54 stage update
+ * for the dry compressible AtmosModel.
+ *
+ * Conventions
+ *   - Every entry point returns CMDG_OK (0) or a CMDG_ERR_* code and never
+ *     throws; cmdg_last_error() gives a thread-local message for the last
+ *     failure on the calling thread.
+ *   - State arrays use the reference's MPIStateArray layout: column-major
+ *     (Np, nstate, nelem) with nstate = 5 (rho, rhou, rhov, rhow, rhoe),
+ *     Np = (N+1)^3, node index ijk = i + Nq*(j + Nq*k).
+ *   - Pointers named d_* are device pointers (cudaMalloc'd or torch
+ *     tensors); pointers named h_* are host pointers.  `stream` is a
+ *     cudaStream_t passed as void* (NULL = legacy default stream).
+ *   - The caller owns Q, dQ and every buffer it passes.  The library owns
+ *     geometry, reference-state tables, scratch buffers and CUDA graphs.
+ *   - One model is used by one stream at a time; calls on one model are not
+ *     re-entrant.
+ *   - Element ordering of generated brick meshes is "stacked": the vertical
+ *     element index is fastest, then x, then y (columns contiguous, as in
+ *     StackedBrickTopology, src/Numerics/Mesh/Topologies.jl:632).
+ */
+#ifndef CMDG_H
+#define CMDG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    CMDG_OK = 0,
+    CMDG_ERR_ARG = 1,          /* invalid argument or size */
+    CMDG_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+    CMDG_ERR_UNSUPPORTED = 3,  /* configuration not implemented */
+    CMDG_ERR_NONFINITE = 4,    /* a kernel saw a non-finite value */
+    CMDG_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
+    CMDG_ERR_ALLOC = 6,        /* device allocation failed */
+    CMDG_ERR_STATE = 7         /* object used in the wrong state */
+};
+
+/* Arithmetic of a model.
+ *   CMDG_FP64  : plain Float64, the reference's arithmetic.
+ *   CMDG_MIXED : FP32 state perturbation q' = q - q_ref about an FP64
+ *                hydrostatic reference state; FP64 RK register dQ; FP64
+ *                reference subtraction; compensated FP64 sums. */
+enum { CMDG_FP64 = 0, CMDG_MIXED = 1 };
+
+/* Numerical flux for first-order terms */
+enum { CMDG_FLUX_RUSANOV = 0, CMDG_FLUX_CENTRAL = 1 };
+/* Orientation */
+enum { CMDG_ORIENT_NONE = 0, CMDG_ORIENT_FLAT = 1 };
+/* Reference-state temperature profile */
+enum { CMDG_PROFILE_ISOTHERMAL = 0, CMDG_PROFILE_DRY_ADIABATIC = 1 };
+/* Turbulence closure */
+enum { CMDG_TURB_NONE = 0, CMDG_TURB_CONSTANT = 1, CMDG_TURB_SMAGORINSKY = 2 };
+
+/* Brick mesh (BrickTopology / StackedBrickTopology + DiscontinuousSpectralElementGrid,
+ * src/Numerics/Mesh/Topologies.jl:470-545,632; src/Numerics/Mesh/Grids.jl:267-414). */
+typedef struct {
+    int N;              /* polynomial order, 1..7 (kernels instantiated for 2..5) */
+    int ne[3];          /* elements in x, y, z */
+    double lo[3];       /* domain lower corner */
+    double hi[3];       /* domain upper corner */
+    int periodic[3];    /* 1 = periodic */
+    int bc_lo[3];       /* boundary tag of the lower face when not periodic (>0) */
+    int bc_hi[3];       /* boundary tag of the upper face when not periodic (>0) */
+} cmdg_brick_desc;
+
+/* Dry AtmosModel parameters (src/Atmos/Model/AtmosModel.jl:242-375;
+ * planet constants as CLIMAParameters.Planet supplies them). */
+typedef struct {
+    double R_d, cp_d, cv_d, T_0, grav, MSLP, inv_Pr_turb;
+    int numflux;        /* CMDG_FLUX_* */
+    int orientation;    /* CMDG_ORIENT_* */
+    int gravity;        /* 1 = Gravity() source */
+    int ref_state;      /* 1 = HydrostaticState */
+    int subtract_off;   /* HydrostaticState.subtract_off */
+    int profile;        /* CMDG_PROFILE_* */
+    double T_surface;   /* isothermal T_virt, or dry-adiabatic surface temperature */
+    double T_min;       /* dry-adiabatic minimum temperature */
+    int turbulence;     /* CMDG_TURB_* */
+    double rho_nu;      /* ConstantDynamicViscosity rho*nu */
+    int with_divergence;/* ConstantDynamicViscosity WithDivergence */
+    double C_smag;      /* SmagorinskyLilly coefficient */
+} cmdg_atmos_params;
+
+typedef struct cmdg_mesh cmdg_mesh;
+typedef struct cmdg_model cmdg_model;
+
+/* Last error message of the calling thread (never NULL). */
+const char* cmdg_last_error(void);
+
+/* Library version string. */
+const char* cmdg_version(void);
+
+/* Builds a brick mesh and its geometry on the current device.
+ * Replaces BrickTopology/StackedBrickTopology + DiscontinuousSpectralElementGrid
+ * (src/Numerics/Mesh/Topologies.jl:470-545,632; src/Numerics/Mesh/Grids.jl:267-414). */
+int cmdg_mesh_create_brick(const cmdg_brick_desc* desc, cmdg_mesh** out);
+int cmdg_mesh_destroy(cmdg_mesh* mesh);
+/* Sizes of a mesh. */
+int cmdg_mesh_info(const cmdg_mesh* mesh, int64_t* nelem, int* Np);
+/* Node coordinates into host memory, (Np, 3, nelem) column-major
+ * (vgeo x1,x2,x3, src/Numerics/Mesh/Grids.jl:76-125). */
+int cmdg_mesh_coordinates(const cmdg_mesh* mesh, double* h_xyz);
+/* Nodal quadrature weights M = J w_i w_j w_k into host memory, (Np, nelem)
+ * (vgeo M, src/Numerics/Mesh/Grids.jl:96-100). */
+int cmdg_mesh_mass(const cmdg_mesh* mesh, double* h_M);
+
+/* Builds a model (DGModel + AtmosModel) on a mesh; computes the orientation,
+ * reference-state and closure auxiliary data.
+ * Replaces DGModel(bl, grid, nf1, nf2, nfgrad) (src/Numerics/DGMethods/DGModel.jl:22-65)
+ * with the dry AtmosModel auxiliary initialisation (src/Atmos/Model/AtmosModel.jl:908-925,
+ * src/Atmos/Model/ref_state.jl:143-263). */
+int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* params, int precision, cmdg_model** out);
+int cmdg_model_destroy(cmdg_model* model);
+/* Reference state at the nodes into host memory, (Np, 3, nelem):
+ * rho_ref, rhoe_ref, p_ref (aux.ref_state, src/Atmos/Model/ref_state.jl:66-67). */
+int cmdg_model_reference_state(const cmdg_model* model, double* h_ref);
+
+/* One tendency evaluation in FP64:
+ *   d_dQ = alpha * dQ/dt(d_Q) + beta * d_dQ
+ * Replaces (dg::DGModel)(tendency, Q, _, t, alpha, beta)
+ * (src/Numerics/DGMethods/DGModel.jl:85-427). */
+int cmdg_tendency(cmdg_model* model, double* d_dQ, const double* d_Q, double t, double alpha, double beta,
+                  void* stream);
+
+/* nsteps LSRK54CarpenterKennedy steps of size dt in FP64, in place on d_Q;
+ * d_dQ is the solver's RK register (zero before the first step, as the
+ * reference's `fill!(dQ, 0)`).
+ * Replaces dostep!(Q, lsrk::LowStorageRungeKutta2N, p, time)
+ * (src/Numerics/ODESolvers/LowStorageRungeKuttaMethod.jl:102-158, 293-327). */
+int cmdg_lsrk54_step(cmdg_model* model, double* d_Q, double* d_dQ, double t, double dt, int nsteps, void* stream);
+
+/* Mixed precision: converts an FP64 state to the FP32 perturbation
+ * q' = q - q_ref (the subtraction is done in FP64) and back.
+ * No counterpart in the reference (the reference state lives in aux.ref_state,
+ * src/Atmos/Model/ref_state.jl:66-67). */
+int cmdg_to_perturbation(cmdg_model* model, float* d_Qp, const double* d_Q, void* stream);
+int cmdg_from_perturbation(cmdg_model* model, double* d_Q, const float* d_Qp, void* stream);
+
+/* Mixed-precision tendency: d_dQ (FP64) = alpha * dQ/dt(q_ref + d_Qp) + beta * d_dQ.
+ * Same semantics as cmdg_tendency (src/Numerics/DGMethods/DGModel.jl:85-427). */
+int cmdg_tendency_mixed(cmdg_model* model, double* d_dQ, const float* d_Qp, double t, double alpha, double beta,
+                        void* stream);
+
+/* Mixed-precision LSRK54 steps: FP32 perturbation state d_Qp, FP64 RK register d_dQ.
+ * Same semantics as cmdg_lsrk54_step
+ * (src/Numerics/ODESolvers/LowStorageRungeKuttaMethod.jl:102-158). */
+int cmdg_lsrk54_step_mixed(cmdg_model* model, float* d_Qp, double* d_dQ, double t, double dt, int nsteps,
+                           void* stream);
+
+/* Compensated weighted sums sum_nodes M * Q[:, field, :] for nfields fields
+ * (FP64 state), result into host memory; double-double accumulation.
+ * Replaces weightedsum(Q, states) (src/Arrays/MPIStateArrays.jl:655-675). */
+int cmdg_weighted_sums(cmdg_model* model, const double* d_Q, int nfields, const int* h_fields, double* h_out,
+                       void* stream);
+/* The same for a mixed-precision perturbation state: sum M*(q_ref + q'). */
+int cmdg_weighted_sums_mixed(cmdg_model* model, const float* d_Qp, int nfields, const int* h_fields, double* h_out,
+                             void* stream);
+
+/* Time step from the nondiffusive Courant number (host-side evaluation of a
+ * device state): dt = CFL / max_nodes((|u| + c_s) / dx_min).
+ * Replaces calculate_dt (src/Numerics/DGMethods/DGMethods.jl:79-83,
+ * src/Numerics/DGMethods/SpaceDiscretization.jl:307-365). */
+int cmdg_courant_dt(cmdg_model* model, const double* d_Q, double CFL, double* h_dt, void* stream);
+
+/* Device status word accumulated by the kernels since the last call
+ * (bit 0: non-finite tendency seen); reading clears it.
+ * Replaces checked_wait's error flag (src/Arrays/MPIStateArrays.jl:910-936). */
+int cmdg_status_word(cmdg_model* model, uint32_t* h_status, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CMDG_H */

@@ -1,0 +1,195 @@
+"""GPU parity of the fused DG tendency / LSRK54 kernels against the oracle.
+
+Every case feeds the same seeded FP64 state to the oracle (CPU restatement of
+the reference) and to libcmdg.so through the C ABI, and compares:
+
+  * FP64 tendency: max |gpu - oracle| / max |oracle| per field <= 1e-10
+    (reassociated sums of O(1e5)-sized fluxes; the reference's own CPU/GPU
+    check allows sqrt(eps), mms_bc_atmos.jl:152)
+  * FP64 LSRK54 steps: the same bound on the state after K steps
+  * mixed precision: relative L2 per field against the FP64 oracle
+    (<= 1e-5 after the run, the stated target)
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import cmdg
+import oracle as O
+from cmdg import workloads
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-10
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import __graft_entry__ as g
+
+    g.build()
+    torch.cuda.set_device(0)
+
+
+def rel_max(got, ref):
+    out = []
+    for s in range(5):
+        scale = np.abs(ref[:, s]).max()
+        out.append(np.abs(got[:, s] - ref[:, s]).max() / (scale if scale > 0 else 1.0))
+    return np.array(out)
+
+
+def make_pair(kind, N, ne, numflux="rusanov", precision="fp64"):
+    if kind == "vortex":
+        L = 1 / 20
+        om = O.OracleModel(N, ne, (-L,) * 3, (L,) * 3, periodic=(1, 1, 1), numflux=numflux)
+        grid = cmdg.BrickGrid(N, ne, (-L,) * 3, (L,) * 3, periodicity=(True, True, True))
+        model = cmdg.AtmosModel()
+        dg = cmdg.DGModel(model, grid, numerical_flux=numflux, precision=precision)
+        Q0 = om.init_vortex(0.0)
+        rng = np.random.default_rng(7)
+        Q0 += rng.uniform(-1e-6, 1e-6, size=Q0.shape)
+    else:
+        Lb = 2500.0
+        om = O.OracleModel(N, ne, (0, 0, 0), (Lb, Lb, Lb), periodic=(1, 1, 0), numflux=numflux, orientation="flat",
+                           gravity=True, ref_state=True, profile="dry_adiabatic", T_surface=300.0, T_min=0.0)
+        dg = workloads.bubble_model(ne=ne, N=N, L=Lb, precision=precision, numerical_flux=numflux)
+        Q0 = om.init_bubble(rc=900.0, xc=1100.0, yc=1300.0, zc=800.0)
+        rng = np.random.default_rng(11)
+        Q0[:, 1:4] += rng.uniform(-2, 2, size=Q0[:, 1:4].shape)
+    return om, dg, Q0
+
+
+@pytest.mark.parametrize("N", [2, 3, 4, 5])
+@pytest.mark.parametrize("kind", ["vortex", "bubble"])
+def test_fp64_tendency_matches_oracle(kind, N):
+    om, dg, Q0 = make_pair(kind, N, (3, 2, 4))
+    ref = om.tendency(Q0)
+    Q = dg.init_ode_state(Q0)
+    dQ = dg.new_state(torch.float64)
+    dg(dQ, Q, None, 0.0)
+    err = rel_max(dQ.cpu().numpy(), ref)
+    assert (err < TOL64).all(), err
+
+
+def test_fp64_central_flux_and_alpha_beta():
+    om, dg, Q0 = make_pair("bubble", 4, (2, 3, 3), numflux="central")
+    prev = np.random.default_rng(3).standard_normal(Q0.shape)
+    ref = om.tendency(Q0, alpha=0.7, beta=-1.3, dQ=prev.copy())
+    Q = dg.init_ode_state(Q0)
+    dQ = torch.from_numpy(prev.copy()).cuda()
+    dg(dQ, Q, None, 0.0, alpha=0.7, beta=-1.3)
+    err = rel_max(dQ.cpu().numpy(), ref)
+    assert (err < TOL64).all(), err
+
+
+@pytest.mark.parametrize("kind", ["vortex", "bubble"])
+def test_fp64_lsrk54_steps_match_oracle(kind):
+    om, dg, Q0 = make_pair(kind, 4, (3, 3, 3))
+    dt = 0.5 * om.courant_dt(Q0, 0.4)
+    Qo, dQo = om.lsrk54(Q0.copy(), dt, 7)
+    Q = dg.init_ode_state(Q0)
+    lsrk = cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt)
+    cmdg.dostep_(Q, lsrk, None, 0.0, nsteps=7)
+    got = Q.cpu().numpy()
+    err = rel_max(got, Qo)
+    assert (err < TOL64).all(), err
+    # the RK register after the last stage is A_1 * dQ = 0
+    assert float(lsrk.dQ.abs().max()) == 0.0
+
+
+def test_isentropic_vortex_golden_through_gpu():
+    """The reference's golden FP64 error (isentropicvortex.jl:105) via libcmdg."""
+    L = 1 / 20
+    ne = (5, 5, 1)
+    grid = cmdg.BrickGrid(4, ne, (-L,) * 3, (L,) * 3)
+    dg = cmdg.DGModel(cmdg.AtmosModel(), grid)
+    xyz = grid.coordinates()
+    Q = dg.init_ode_state(workloads.isentropic_vortex(xyz, 0.0))
+    c = cmdg.EARTH
+    timeend = 2 * L / 10 / 150
+    dt = (2 * L / 5) / math.sqrt(c["cp_d"] / c["cv_d"] * c["R_d"] * 300.0) / 16
+    dt = timeend / math.ceil(timeend / dt)
+    lsrk = cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt)
+    cmdg.solve_(Q, lsrk, timeend=timeend)
+    err = cmdg.euclidean_distance(dg, Q, workloads.isentropic_vortex(xyz, timeend))
+    assert err == pytest.approx(3.7918869862613858e00, rel=1e-10)
+
+
+def test_mixed_tendency_close_to_oracle():
+    om, dg, Q0 = make_pair("bubble", 4, (3, 3, 4), precision="mixed")
+    ref = om.tendency(Q0)
+    Qp = dg.init_ode_state(Q0)
+    dQ = dg.new_state(torch.float64)
+    dg(dQ, Qp, None, 0.0)
+    got = dQ.cpu().numpy()
+    err = [np.linalg.norm(got[:, s] - ref[:, s]) / np.linalg.norm(ref[:, s]) for s in range(5)]
+    assert max(err) < 1e-4, err
+
+
+def test_mixed_bubble_100_steps_within_1e5_of_fp64_oracle():
+    om, dg, Q0 = make_pair("bubble", 4, (4, 4, 4), precision="mixed")
+    dt = om.courant_dt(Q0, 0.4)
+    Qo, _ = om.lsrk54(Q0.copy(), dt, 100)
+    Qp = dg.init_ode_state(Q0)
+    lsrk = cmdg.LSRK54CarpenterKennedy(dg, Qp, dt=dt)
+    cmdg.dostep_(Qp, lsrk, None, 0.0, nsteps=100)
+    got = dg.from_perturbation(Qp).cpu().numpy()
+    err, ref = om.field_l2(got, Qo)
+    rel = err / ref
+    assert (rel < 1e-5).all(), rel
+    # conservation of mass through the compensated sums
+    m_gpu = dg.weighted_sums(Qp, (0,))[0]
+    assert m_gpu == pytest.approx(om.weightedsum(Qo, 0), rel=1e-9)
+
+
+def test_weighted_sums_and_courant_match_oracle():
+    om, dg, Q0 = make_pair("bubble", 3, (2, 2, 3))
+    Q = dg.init_ode_state(Q0)
+    sums = dg.weighted_sums(Q, (0, 4))
+    assert sums[0] == pytest.approx(om.weightedsum(Q0, 0), rel=1e-14)
+    assert sums[1] == pytest.approx(om.weightedsum(Q0, 4), rel=1e-14)
+    assert dg.courant_dt(Q, 0.4) == pytest.approx(om.courant_dt(Q0, 0.4), rel=1e-12)
+
+
+def test_fp64_discrete_hydrostatic_balance_central():
+    H = 50e3
+    grid = cmdg.BrickGrid(4, (3, 3, 3), (0, 0, 0), (H, H, H), periodicity=(True, True, False),
+                          boundary=((0, 0), (0, 0), (1, 2)))
+    model = cmdg.AtmosModel(orientation="flat", gravity=True,
+                            ref_state=cmdg.HydrostaticState(cmdg.IsothermalProfile(285.0), subtract_off=False))
+    dg = cmdg.DGModel(model, grid, numerical_flux="central")
+    ref = dg.reference_state()
+    Q0 = np.zeros((grid.nelem, 5, grid.Np))
+    Q0[:, 0] = ref[:, 0]
+    Q0[:, 4] = ref[:, 1]
+    Q = dg.init_ode_state(Q0)
+    dt = dg.courant_dt(Q, 0.1)
+    lsrk = cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt)
+    cmdg.solve_(Q, lsrk, timeend=100.0)
+    err = cmdg.euclidean_distance(dg, Q, Q0) / cmdg.norm(dg, torch.from_numpy(Q0).cuda())
+    assert err <= 100 * np.finfo(np.float64).eps
+
+
+def test_nonfinite_state_sets_status_word_without_fault():
+    om, dg, Q0 = make_pair("vortex", 3, (2, 2, 2))
+    Q0[0, 0, 5] = np.nan
+    Q = dg.init_ode_state(Q0)
+    dQ = dg.new_state(torch.float64)
+    dg(dQ, Q, None, 0.0)
+    torch.cuda.synchronize()
+    assert dg.status_word() & 1
+    assert dg.status_word() == 0  # reading clears it
+
+
+def test_fp64_steps_are_bitwise_deterministic():
+    om, dg, Q0 = make_pair("bubble", 4, (3, 3, 3))
+    outs = []
+    for _ in range(2):
+        Q = dg.init_ode_state(Q0)
+        lsrk = cmdg.LSRK54CarpenterKennedy(dg, Q, dt=0.05)
+        cmdg.dostep_(Q, lsrk, None, 0.0, nsteps=3)
+        outs.append(Q.cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
