@@ -65,9 +65,11 @@ static int issue_steps(Model* md, void* Q, double* dQ, double dt, int nsteps, cu
             a.dQ = dQ;
             a.alpha = 1.0;
             a.beta = 1.0;
-            a.rka = LSRK_A[(st + 1) % 5];
+            a.rka = LSRK_A[st];
             a.rkb_dt = LSRK_B[st] * dt;
             a.mode = 1;
+            a.first_stage = (st == 0);
+            a.last_stage = (st == 4);
             int rc = launch_stage(md, a, s);
             if (rc) return rc;
         }
@@ -135,6 +137,7 @@ int cmdg_mesh_create_brick(const cmdg_brick_desc* desc, cmdg_mesh** out) {
     if (rc) {
         if (mh->m.d_emetric) cudaFree(mh->m.d_emetric);
         if (mh->m.d_nbr) cudaFree(mh->m.d_nbr);
+        if (mh->m.d_emetric32) cudaFree(mh->m.d_emetric32);
         delete mh;
         return rc;
     }
@@ -146,6 +149,7 @@ int cmdg_mesh_destroy(cmdg_mesh* mesh) {
     if (!mesh) return CMDG_OK;
     cudaFree(mesh->m.d_emetric);
     cudaFree(mesh->m.d_nbr);
+    cudaFree(mesh->m.d_emetric32);
     delete mesh;
     return CMDG_OK;
 }
@@ -185,7 +189,7 @@ int cmdg_mesh_mass(const cmdg_mesh* mesh, double* h_M) {
     const Mesh& m = mesh->m;
     const int Nq = m.Nq, Np = m.Np;
     for (int64_t e = 0; e < m.nelem; ++e) {
-        const double J = 8.0 / (m.emetric[3 * e] * m.emetric[3 * e + 1] * m.emetric[3 * e + 2]);
+        const double J = 1.0 / (m.emetric[3 * e] * m.emetric[3 * e + 1] * m.emetric[3 * e + 2]);
         for (int node = 0; node < Np; ++node) {
             const int i = node % Nq, j = (node / Nq) % Nq, k = node / (Nq * Nq);
             h_M[(size_t)e * Np + node] = J * (m.omega[i] * m.omega[j] * m.omega[k]);
@@ -284,7 +288,7 @@ int cmdg_tendency(cmdg_model* model, double* d_dQ, const double* d_Q, double t, 
     if (rc) return rc;
     CMDG_ARG_CHECK(model->m.precision == CMDG_FP64, "cmdg_tendency needs an FP64 model");
     CMDG_ARG_CHECK(d_dQ != nullptr && d_Q != nullptr, "NULL state");
-    LaunchArgs a{d_Q, nullptr, d_dQ, alpha, beta, 0.0, 0.0, 0};
+    LaunchArgs a{d_Q, nullptr, d_dQ, alpha, beta, 0.0, 0.0, 0, 0, 0};
     return launch_stage(&model->m, a, (cudaStream_t)stream);
 }
 
@@ -295,7 +299,7 @@ int cmdg_tendency_mixed(cmdg_model* model, double* d_dQ, const float* d_Qp, doub
     if (rc) return rc;
     CMDG_ARG_CHECK(model->m.precision == CMDG_MIXED, "cmdg_tendency_mixed needs a mixed-precision model");
     CMDG_ARG_CHECK(d_dQ != nullptr && d_Qp != nullptr, "NULL state");
-    LaunchArgs a{d_Qp, nullptr, d_dQ, alpha, beta, 0.0, 0.0, 0};
+    LaunchArgs a{d_Qp, nullptr, d_dQ, alpha, beta, 0.0, 0.0, 0, 0, 0};
     return launch_stage(&model->m, a, (cudaStream_t)stream);
 }
 

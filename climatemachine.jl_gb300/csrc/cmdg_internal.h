@@ -74,6 +74,7 @@ struct Mesh {
     std::vector<double> dzlev;       // [nlev] dz/dxi3 derivative helper (xi3x3 per level)
     // device copies
     double* d_emetric = nullptr;
+    float* d_emetric32 = nullptr;
     int* d_nbr = nullptr;
 };
 
@@ -120,8 +121,10 @@ struct LaunchArgs {
     void* Qout;
     double* dQ;
     double alpha, beta;      // tendency mode
-    double rka, rkb_dt;      // stage mode
+    double rka, rkb_dt;      // stage mode: A_s applied to the previous increment, B_s dt
     int mode;                // 0 = tendency, 1 = RK stage
+    int first_stage = 0;     // stage 1: the register is not read (A_1 = 0)
+    int last_stage = 0;      // stage 5: the register is not written
 };
 int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
 

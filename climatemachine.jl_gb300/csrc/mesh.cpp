@@ -149,6 +149,9 @@ int build_brick(const cmdg_brick_desc* d, Mesh* m) {
     CMDG_CUDA_CHECK(cudaMemcpy(m->d_emetric, m->emetric.data(), sizeof(double) * m->emetric.size(),
                                cudaMemcpyHostToDevice));
     CMDG_CUDA_CHECK(cudaMemcpy(m->d_nbr, m->nbr.data(), sizeof(int) * m->nbr.size(), cudaMemcpyHostToDevice));
+    std::vector<float> em32(m->emetric.begin(), m->emetric.end());
+    CMDG_CUDA_CHECK(cudaMalloc(&m->d_emetric32, sizeof(float) * em32.size()));
+    CMDG_CUDA_CHECK(cudaMemcpy(m->d_emetric32, em32.data(), sizeof(float) * em32.size(), cudaMemcpyHostToDevice));
     return CMDG_OK;
 }
 

@@ -68,7 +68,7 @@ __device__ __forceinline__ dd two_prod(double a, double b) {
 }
 
 // Block partial (hi, lo) of sum M * q over all nodes for one field.
-// M = J w_i w_j w_k with J = (dx dy dz)/8 on an affine brick element.
+// M = J w_i w_j w_k with J = (dx/2)(dy/2)(dz/2) = 1/(xi1 xi2 xi3) on an affine brick element.
 template <bool MIXED>
 __global__ void weighted_sum_kernel(const void* Qv, int field, const double* emetric, const double* w, const double* lvl,
                                     int64_t nelem, int Np, int Nq, int nz, double* partial) {
@@ -80,7 +80,7 @@ __global__ void weighted_sum_kernel(const void* Qv, int field, const double* eme
         const int node = (int)(idx % Np);
         const int64_t e = idx / Np;
         const int i = node % Nq, j = (node / Nq) % Nq, k = node / Nfp;
-        const double J = 8.0 / (emetric[3 * e] * emetric[3 * e + 1] * emetric[3 * e + 2]);
+        const double J = 1.0 / (emetric[3 * e] * emetric[3 * e + 1] * emetric[3 * e + 2]);
         const double M = J * (w[i] * w[j] * w[k]);
         const size_t qi = ((size_t)e * NSTATE + field) * Np + node;
         double qv;

@@ -10,8 +10,13 @@
 //   phase 3  every node contracts the staged fluxes with the weak-form
 //            derivative Dhat = M^-1 D^T M along xi1, xi2, xi3, subtracts its
 //            face terms, adds gravity and finishes either the tendency
-//            T = alpha*dQ/dt + beta*T or the LSRK 2N stage update
-//            dQ <- dQ/dt + dQ; Q <- Q + B_s dt dQ; dQ <- A_{s+1} dQ.
+//            T = alpha*dQ/dt + beta*T or the LSRK 2N stage update.  The
+//            register holds the unscaled stage increment:
+//            dq_s = dQ/dt(Q_{s-1}) + A_s dq_{s-1}, Q_s = Q_{s-1} + B_s dt dq_s,
+//            which is the reference's dQ <- dQ/dt + dQ; Q <- Q + B_s dt dQ;
+//            dQ <- A_{s+1} dQ with the A-scaling moved into the next stage
+//            (one FMA per DOF; A_1 = 0, so stage 1 does not read the register
+//            and stage 5 does not write it).
 // The state is read from one buffer and the stage's new state written to
 // another, so neighbouring elements never see a half-updated state.
 //
@@ -46,6 +51,9 @@ struct Dims {
     static constexpr int Np = Nq * Nq * Nq;
     static constexpr int NF = 6 * Nfp;
     static constexpr int NT = (((Np > NF) ? Np : NF) + 31) / 32 * 32;
+    // resident CTAs per SM requested for the FP32 kernels (register budget
+    // 65536 / (NT * MIN_CTAS): 64, 56, 51 and 58 registers for N = 2..5)
+    static constexpr int MIN_CTAS = N == 2 ? 16 : N == 3 ? 12 : N == 4 ? 8 : 5;
 };
 
 struct KParams {
@@ -60,10 +68,71 @@ struct KParams {
     const void* Dhat;
     unsigned* status;
     int nelem, nz;
+    const float* emetric32;
     double alpha, beta, rka, rkb_dt;
     double inv_w0;
+    float rkb_dt32, inv_w032, gm132, gamma32;
+    int first_stage, last_stage;
     Physics ph;
 };
+
+// Constants in the working precision R, read without a run-time FP64->FP32
+// conversion (on this GPU such conversions issue on the FP64 pipe).
+template <typename R>
+struct KConst;
+template <>
+struct KConst<double> {
+    static __device__ __forceinline__ double gm1(const KParams& P) { return P.ph.gm1; }
+    static __device__ __forceinline__ double gamma(const KParams& P) { return P.ph.gamma; }
+    static __device__ __forceinline__ double inv_w0(const KParams& P) { return P.inv_w0; }
+    static __device__ __forceinline__ double rkb_dt(const KParams& P) { return P.rkb_dt; }
+    static __device__ __forceinline__ double metric(const KParams& P, int e, int d) { return P.emetric[3 * e + d]; }
+};
+template <>
+struct KConst<float> {
+    static __device__ __forceinline__ float gm1(const KParams& P) { return P.gm132; }
+    static __device__ __forceinline__ float gamma(const KParams& P) { return P.gamma32; }
+    static __device__ __forceinline__ float inv_w0(const KParams& P) { return P.inv_w032; }
+    static __device__ __forceinline__ float rkb_dt(const KParams& P) { return P.rkb_dt32; }
+    static __device__ __forceinline__ float metric(const KParams& P, int e, int d) { return P.emetric32[3 * e + d]; }
+};
+
+// FP32 -> FP64 by IEEE-754 field arithmetic on the integer pipe: exact for
+// normal numbers; zero and subnormal inputs give a signed zero; infinities and
+// NaNs stay non-finite.
+__device__ __forceinline__ double f32_to_f64_bits(float f) {
+    const unsigned b = __float_as_uint(f);
+    const unsigned sign = b & 0x80000000u;
+    const unsigned mag = b & 0x7FFFFFFFu;
+    unsigned hi = sign | ((mag >> 3) + (896u << 20));
+    unsigned lo = mag << 29;
+    if (mag < 0x00800000u) {
+        hi = sign;
+        lo = 0u;
+    } else if (mag >= 0x7F800000u) {
+        hi = sign | 0x7FF00000u | ((mag >> 3) & 0x000FFFFFu) | ((mag > 0x7F800000u) ? 0x00080000u : 0u);
+    }
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// FP64 -> FP32 by IEEE-754 field arithmetic on the integer pipe, rounding
+// toward zero (error below one FP32 ulp); magnitudes under 2^-126 flush to a
+// signed zero, magnitudes beyond the FP32 range and infinities give an
+// infinity, NaN stays NaN.  Used for the stage increment only, which is small
+// next to the state it is added to.
+__device__ __forceinline__ float f64_to_f32_bits(double d) {
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned sign = hi & 0x80000000u;
+    const unsigned mag = hi & 0x7FFFFFFFu;
+    unsigned bits = sign | (((mag - (896u << 20)) << 3) | (lo >> 29));
+    if (mag < (897u << 20)) {
+        bits = sign;
+    } else if (mag >= (1151u << 20)) {
+        const bool nan = mag > 0x7FF00000u || (mag == 0x7FF00000u && lo != 0u);
+        bits = sign | 0x7F800000u | (nan ? 0x00400000u : 0u);
+    }
+    return __uint_as_float(bits);
+}
 
 template <typename R>
 struct Level {
@@ -110,9 +179,10 @@ struct Thermo {
 };
 
 template <typename R, bool MIXED>
-__device__ __forceinline__ Thermo<R, MIXED> thermo(const R q[NSTATE], const Level<R>& lv, const Physics& ph) {
+__device__ __forceinline__ Thermo<R, MIXED> thermo(const R q[NSTATE], const Level<R>& lv, const KParams& P) {
     Thermo<R, MIXED> t;
-    const R gm1 = (R)ph.gm1, gamma = (R)ph.gamma;
+    const Physics& ph = P.ph;
+    const R gm1 = KConst<R>::gm1(P), gamma = KConst<R>::gamma(P);
     R rho = MIXED ? (lv.rho_ref + q[0]) : q[0];
     t.rinv = R(1) / rho;
     t.u[0] = q[1] * t.rinv;
@@ -176,7 +246,7 @@ __device__ __forceinline__ int face_node(int f, int a, int b) {
 }
 
 template <int N, typename R, bool MIXED, int MODE>
-__global__ void __launch_bounds__(Dims<N>::NT) stage_kernel(const KParams P) {
+__global__ void __launch_bounds__(Dims<N>::NT, MIXED ? Dims<N>::MIN_CTAS : 1) stage_kernel(const KParams P) {
     using Dm = Dims<N>;
     constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp;
     __shared__ R s_q[NSTATE][Np];
@@ -191,24 +261,55 @@ __global__ void __launch_bounds__(Dims<N>::NT) stage_kernel(const KParams P) {
     const int ez = e % P.nz;
     const R* __restrict__ Qin = static_cast<const R*>(P.Qin);
     const Physics& ph = P.ph;
+    const bool node_thread = t < Np;
+    const bool face_thread = t < 6 * Nfp;
+    const bool read_reg = (MODE == 0) ? (P.beta != 0) : !P.first_stage;
 
-    if (t < Nq * Nq) s_D[t] = static_cast<const R*>(P.Dhat)[t];
-    const R xi[3] = {(R)P.emetric[3 * e + 0], (R)P.emetric[3 * e + 1], (R)P.emetric[3 * e + 2]};
-
-    // ---------------- phase 1: node state, thermodynamics, volume fluxes
+    // ---------------- issue every global load of this thread up front:
+    // own node state and RK register, then the neighbour state at this
+    // thread's face node (its latency overlaps the volume work below)
     R q[NSTATE];
-    R gsrc = 0;
-    if (t < Np) {
-        const int k = t / Nfp;
-        const Level<R> lv = load_level<R>(P, ez * Nq + k);
+    double dq_old[NSTATE];
+    if (node_thread) {
 #pragma unroll
         for (int s = 0; s < NSTATE; ++s) q[s] = Qin[((size_t)e * NSTATE + s) * Np + t];
-        const Thermo<R, MIXED> th = thermo<R, MIXED>(q, lv, ph);
+        if (read_reg) {
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) dq_old[s] = P.dQ[((size_t)e * NSTATE + s) * Np + t];
+        }
+    }
+    int f = 0, fn = 0, fa = 0, fb = 0, d = 0, vM = 0, nb = -1, levp = 0;
+    R qp[NSTATE];
+    if (face_thread) {
+        f = t / Nfp;
+        fn = t % Nfp;
+        fa = fn % Nq;
+        fb = fn / Nq;
+        d = f >> 1;
+        vM = face_node<N>(f, fa, fb);
+        nb = P.nbr[6 * e + f];
+        if (nb >= 0) {
+            const int vP = face_node<N>(f ^ 1, fa, fb);
+            levp = (nb % P.nz) * Nq + vP / Nfp;
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) qp[s] = Qin[((size_t)nb * NSTATE + s) * Np + vP];
+        } else {
+            levp = ez * Nq + vM / Nfp;
+        }
+    }
+    if (t < Nq * Nq) s_D[t] = static_cast<const R*>(P.Dhat)[t];
+    const R xi[3] = {KConst<R>::metric(P, e, 0), KConst<R>::metric(P, e, 1), KConst<R>::metric(P, e, 2)};
+
+    // ---------------- phase 1: node thermodynamics and volume fluxes
+    R gsrc = 0;
+    if (node_thread) {
+        const Level<R> lv = load_level<R>(P, ez * Nq + t / Nfp);
+        const Thermo<R, MIXED> th = thermo<R, MIXED>(q, lv, P);
 #pragma unroll
         for (int s = 0; s < NSTATE; ++s) {
             s_q[s][t] = q[s];
 #pragma unroll
-            for (int d = 0; d < 3; ++d) s_F[d][s][t] = flux_d<R, MIXED>(q, th, d, s);
+            for (int dd = 0; dd < 3; ++dd) s_F[dd][s][t] = flux_d<R, MIXED>(q, th, dd, s);
         }
         s_c[t] = th.c;
         s_ri[t] = th.rinv;
@@ -220,29 +321,19 @@ __global__ void __launch_bounds__(Dims<N>::NT) stage_kernel(const KParams P) {
     }
     __syncthreads();
 
-    // ---------------- phase 2: face fluxes
-    for (int ft = t; ft < 6 * Nfp; ft += Dm::NT) {
-        const int f = ft / Nfp, fn = ft % Nfp;
-        const int a = fn % Nq, b = fn / Nq;
-        const int d = f >> 1;
+    // ---------------- phase 2: one numerical flux per face node
+    if (face_thread) {
         const R sgn = (f & 1) ? R(1) : R(-1);
-        const int vM = face_node<N>(f, a, b);
-        R qm[NSTATE], qp[NSTATE], Fm[NSTATE], Fp[NSTATE], jr[NSTATE] = {0, 0, 0, 0, 0};
+        R qm[NSTATE], Fm[NSTATE], Fp[NSTATE], jr[NSTATE] = {0, 0, 0, 0, 0};
 #pragma unroll
         for (int s = 0; s < NSTATE; ++s) {
             qm[s] = s_q[s][vM];
             Fm[s] = sgn * s_F[d][s][vM];
         }
         const R lam_m = fabs(pick3(d, qm[1], qm[2], qm[3]) * s_ri[vM]) + s_c[vM];
-        const int nb = P.nbr[6 * e + f];
-        int levp;
         if (nb >= 0) {
-            const int vP = face_node<N>(f ^ 1, a, b);
-            const int kP = vP / Nfp;
-            levp = (nb % P.nz) * Nq + kP;
-#pragma unroll
-            for (int s = 0; s < NSTATE; ++s) qp[s] = Qin[((size_t)nb * NSTATE + s) * Np + vP];
             if (MIXED && d == 2 && ph.numflux == CMDG_FLUX_RUSANOV) {
+                // reference-state jump q_ref(-) - q_ref(+) across a vertical face
                 if (f == 4) {
                     jr[0] = (R)P.jump32[2 * ez + 0];
                     jr[4] = (R)P.jump32[2 * ez + 1];
@@ -254,7 +345,6 @@ __global__ void __launch_bounds__(Dims<N>::NT) stage_kernel(const KParams P) {
             }
         } else {
             // Impenetrable(FreeSlip) + Insulating wall: rhou+ = rhou- - 2 (rhou-.n) n
-            levp = ez * Nq + vM / Nfp;
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) qp[s] = qm[s];
             qp[1] = (d == 0) ? -qm[1] : qm[1];
@@ -262,10 +352,10 @@ __global__ void __launch_bounds__(Dims<N>::NT) stage_kernel(const KParams P) {
             qp[3] = (d == 2) ? -qm[3] : qm[3];
         }
         const Level<R> lvp = load_level<R>(P, levp);
-        const Thermo<R, MIXED> thp = thermo<R, MIXED>(qp, lvp, ph);
+        const Thermo<R, MIXED> thp = thermo<R, MIXED>(qp, lvp, P);
         normal_flux<R, MIXED>(qp, thp, d, sgn, Fp);
         const R lam_p = fabs(pick3(d, thp.u[0], thp.u[1], thp.u[2])) + thp.c;
-        const R lift = (R)(P.emetric[3 * e + d] * P.inv_w0);
+        const R lift = pick3(d, xi[0], xi[1], xi[2]) * KConst<R>::inv_w0(P);
         const R hmw = (ph.numflux == CMDG_FLUX_RUSANOV) ? R(0.5) * fmax(lam_m, lam_p) : R(0);
 #pragma unroll
         for (int s = 0; s < NSTATE; ++s) {
@@ -277,7 +367,7 @@ __global__ void __launch_bounds__(Dims<N>::NT) stage_kernel(const KParams P) {
 
     // ---------------- phase 3: volume contraction, face terms, source, update
     int bad = 0;
-    if (t < Np) {
+    if (node_thread) {
         const int i = t % Nq, j = (t / Nq) % Nq, k = t / Nfp;
         R Di[Nq], Dj[Nq], Dk[Nq];
 #pragma unroll
@@ -286,6 +376,7 @@ __global__ void __launch_bounds__(Dims<N>::NT) stage_kernel(const KParams P) {
             Dj[n] = s_D[j * Nq + n];
             Dk[n] = s_D[k * Nq + n];
         }
+        const R rkb_dt = KConst<R>::rkb_dt(P);
 #pragma unroll
         for (int s = 0; s < NSTATE; ++s) {
             R c1 = 0, c2 = 0, c3 = 0;
@@ -307,17 +398,27 @@ __global__ void __launch_bounds__(Dims<N>::NT) stage_kernel(const KParams P) {
             const size_t idx = ((size_t)e * NSTATE + s) * Np + t;
             if (MODE == 0) {
                 double out = P.alpha * (double)rhs;
-                if (P.beta != 0) out += P.beta * P.dQ[idx];
+                if (read_reg) out = fma(P.beta, dq_old[s], out);
                 P.dQ[idx] = out;
             } else {
-                const double dq = (double)rhs + P.dQ[idx];
+                // unscaled 2N register: dq_s = rhs_s + A_s dq_{s-1}  (A_1 = 0)
                 R* Qout = static_cast<R*>(P.Qout);
+                double dq;
                 if (MIXED) {
-                    Qout[idx] = q[s] + (R)(P.rkb_dt * dq);
+                    // one FP64 FMA per DOF; the conversions run on the integer pipe
+                    const double r64 = f32_to_f64_bits((float)rhs);
+                    if (read_reg) {
+                        dq = fma(P.rka, dq_old[s], r64);
+                        Qout[idx] = fma(rkb_dt, (R)f64_to_f32_bits(dq), q[s]);
+                    } else {
+                        dq = r64;
+                        Qout[idx] = fma(rkb_dt, rhs, q[s]);
+                    }
                 } else {
-                    Qout[idx] = (R)((double)q[s] + P.rkb_dt * dq);
+                    dq = read_reg ? fma(P.rka, dq_old[s], (double)rhs) : (double)rhs;
+                    Qout[idx] = (R)fma(P.rkb_dt, dq, (double)q[s]);
                 }
-                P.dQ[idx] = P.rka * dq;
+                if (!P.last_stage) P.dQ[idx] = dq;
             }
         }
     }
@@ -361,7 +462,14 @@ int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
     P.beta = a.beta;
     P.rka = a.rka;
     P.rkb_dt = a.rkb_dt;
+    P.first_stage = a.first_stage;
+    P.last_stage = a.last_stage;
     P.inv_w0 = 1.0 / m.omega[0];
+    P.emetric32 = m.d_emetric32;
+    P.rkb_dt32 = (float)a.rkb_dt;
+    P.inv_w032 = (float)P.inv_w0;
+    P.gm132 = (float)md->ph.gm1;
+    P.gamma32 = (float)md->ph.gamma;
     P.ph = md->ph;
     cudaError_t err;
     switch (m.N) {

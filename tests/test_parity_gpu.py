@@ -34,9 +34,14 @@ def _built():
 
 
 def rel_max(got, ref):
+    """max |got - ref| per field, relative to the field's largest magnitude;
+    the three momentum components are scaled together as one vector field
+    (a component that is zero up to noise, like rho*w in the vortex, is a
+    difference of O(p) terms and carries their rounding)."""
     out = []
     for s in range(5):
-        scale = np.abs(ref[:, s]).max()
+        sl = slice(1, 4) if 1 <= s <= 3 else slice(s, s + 1)
+        scale = np.abs(ref[:, sl]).max()
         out.append(np.abs(got[:, s] - ref[:, s]).max() / (scale if scale > 0 else 1.0))
     return np.array(out)
 
@@ -92,12 +97,13 @@ def test_fp64_lsrk54_steps_match_oracle(kind):
     Qo, dQo = om.lsrk54(Q0.copy(), dt, 7)
     Q = dg.init_ode_state(Q0)
     lsrk = cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt)
-    cmdg.dostep_(Q, lsrk, None, 0.0, nsteps=7)
+    cmdg.dostep_(Q, lsrk, None, 0.0, nsteps=4)
+    # A_1 = 0: a step never reads what the register held before it
+    lsrk.dQ.fill_(1.0e30)
+    cmdg.dostep_(Q, lsrk, None, 0.0, nsteps=3)
     got = Q.cpu().numpy()
     err = rel_max(got, Qo)
     assert (err < TOL64).all(), err
-    # the RK register after the last stage is A_1 * dQ = 0
-    assert float(lsrk.dQ.abs().max()) == 0.0
 
 
 def test_isentropic_vortex_golden_through_gpu():
