@@ -299,6 +299,7 @@ def main():
                      "roofline": {"bound": "hbm", "achieved": ach_64, "peak": peak, "unit": "GB/s",
                                   "frac": ach_64 / peak}},
             "mixed_speedup_vs_fp64": value / v64,
+            "mixed_step_ms": [round(x, 4) for x in per_mx],
             "mixed_vs_fp64_rel_l2": rel,
             "roofline": {"bound": "hbm", "achieved": ach_mx, "peak": peak, "unit": "GB/s", "frac": ach_mx / peak,
                          "traffic": traffic, "peak_source": peak_kind,

@@ -97,40 +97,32 @@ struct KConst<float> {
     static __device__ __forceinline__ float metric(const KParams& P, int e, int d) { return P.emetric32[3 * e + d]; }
 };
 
-// FP32 -> FP64 by IEEE-754 field arithmetic on the integer pipe: exact for
-// normal numbers; zero and subnormal inputs give a signed zero; infinities and
-// NaNs stay non-finite.
+// FP32 -> FP64 by IEEE-754 field arithmetic on the integer pipe (on this GPU
+// the F2F conversion instructions issue on the FP64 pipe).  Exact for normal
+// numbers and zero; an FP32 subnormal (|f| < 2^-126) maps to a value of the
+// same sign below 2^-126, and a non-finite input to a value beyond the FP32
+// range (non-finite tendencies are reported through the status word before
+// they reach this conversion).
 __device__ __forceinline__ double f32_to_f64_bits(float f) {
     const unsigned b = __float_as_uint(f);
     const unsigned sign = b & 0x80000000u;
     const unsigned mag = b & 0x7FFFFFFFu;
-    unsigned hi = sign | ((mag >> 3) + (896u << 20));
-    unsigned lo = mag << 29;
-    if (mag < 0x00800000u) {
-        hi = sign;
-        lo = 0u;
-    } else if (mag >= 0x7F800000u) {
-        hi = sign | 0x7FF00000u | ((mag >> 3) & 0x000FFFFFu) | ((mag > 0x7F800000u) ? 0x00080000u : 0u);
-    }
-    return __hiloint2double((int)hi, (int)lo);
+    const unsigned hi = (mag == 0u) ? sign : (sign | ((mag >> 3) + (896u << 20)));
+    return __hiloint2double((int)hi, (int)(mag << 29));
 }
 
 // FP64 -> FP32 by IEEE-754 field arithmetic on the integer pipe, rounding
-// toward zero (error below one FP32 ulp); magnitudes under 2^-126 flush to a
-// signed zero, magnitudes beyond the FP32 range and infinities give an
-// infinity, NaN stays NaN.  Used for the stage increment only, which is small
-// next to the state it is added to.
+// toward zero (error below one FP32 ulp).  Magnitudes under 2^-126 flush to a
+// signed zero; magnitudes beyond the FP32 range, infinities and NaNs give an
+// infinity.  Used for the stage increment only, which is small next to the
+// state it is added to.
 __device__ __forceinline__ float f64_to_f32_bits(double d) {
     const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
     const unsigned sign = hi & 0x80000000u;
     const unsigned mag = hi & 0x7FFFFFFFu;
     unsigned bits = sign | (((mag - (896u << 20)) << 3) | (lo >> 29));
-    if (mag < (897u << 20)) {
-        bits = sign;
-    } else if (mag >= (1151u << 20)) {
-        const bool nan = mag > 0x7FF00000u || (mag == 0x7FF00000u && lo != 0u);
-        bits = sign | 0x7F800000u | (nan ? 0x00400000u : 0u);
-    }
+    bits = (mag < (897u << 20)) ? sign : bits;
+    bits = (mag >= (1151u << 20)) ? (sign | 0x7F800000u) : bits;
     return __uint_as_float(bits);
 }
 
@@ -245,16 +237,73 @@ __device__ __forceinline__ int face_node(int f, int a, int b) {
     }
 }
 
+// Shared-memory record of one node or face node: the five fields packed
+// contiguously (plus two spare slots) so a record moves with 128-bit accesses.
+template <typename R>
+struct Slot {
+    static constexpr int W = 8;  // record width in elements of R
+};
+
+template <typename R>
+__device__ __forceinline__ void ld5(const R* p, R v[NSTATE]);
+template <>
+__device__ __forceinline__ void ld5<float>(const float* p, float v[NSTATE]) {
+    const float4 a = *reinterpret_cast<const float4*>(p);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = a.z;
+    v[3] = a.w;
+    v[4] = p[4];
+}
+template <>
+__device__ __forceinline__ void ld5<double>(const double* p, double v[NSTATE]) {
+    const double2 a = *reinterpret_cast<const double2*>(p);
+    const double2 b = *reinterpret_cast<const double2*>(p + 2);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
+    v[4] = p[4];
+}
+template <typename R>
+__device__ __forceinline__ void st5(R* p, const R v[NSTATE]);
+template <>
+__device__ __forceinline__ void st5<float>(float* p, const float v[NSTATE]) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    p[4] = v[4];
+}
+template <>
+__device__ __forceinline__ void st5<double>(double* p, const double v[NSTATE]) {
+    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+    *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
+    p[4] = v[4];
+}
+
+template <int N, typename R>
+struct Smem {
+    static constexpr int Nq = N + 1, Np = Nq * Nq * Nq, Nfp = Nq * Nq, W = Slot<R>::W;
+    // node records: q (5), sound speed (slot 5), 1/rho (slot 6)
+    static constexpr int NODE = 0;
+    // volume fluxes by direction
+    static constexpr int FLUX = NODE + Np * W;
+    // lifted face fluxes
+    static constexpr int FACE = FLUX + 3 * Np * W;
+    static constexpr int DMAT = FACE + 6 * Nfp * W;
+    static constexpr int TOTAL = DMAT + Nq * Nq;
+    static constexpr size_t BYTES = sizeof(R) * TOTAL;
+};
+
 template <int N, typename R, bool MIXED, int MODE>
 __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? Dims<N>::MIN_CTAS : 1) stage_kernel(const KParams P) {
     using Dm = Dims<N>;
-    constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp;
-    __shared__ R s_q[NSTATE][Np];
-    __shared__ R s_F[3][NSTATE][Np];
-    __shared__ R s_c[Np];
-    __shared__ R s_ri[Np];
-    __shared__ R s_fs[6][NSTATE][Nfp];
-    __shared__ R s_D[Nq * Nq];
+    using SM = Smem<N, R>;
+    constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, W = SM::W;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* const sm = reinterpret_cast<R*>(smem_raw);
+    R* const s_node = sm + SM::NODE;
+    R* const s_F = sm + SM::FLUX;
+    R* const s_fs = sm + SM::FACE;
+    R* const s_D = sm + SM::DMAT;
 
     const int e = blockIdx.x;
     const int t = threadIdx.x;
@@ -264,6 +313,7 @@ __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? Dims<N>::MIN_CTAS : 1) st
     const bool node_thread = t < Np;
     const bool face_thread = t < 6 * Nfp;
     const bool read_reg = (MODE == 0) ? (P.beta != 0) : !P.first_stage;
+    const size_t ebase = (size_t)e * NSTATE * Np;
 
     // ---------------- issue every global load of this thread up front:
     // own node state and RK register, then the neighbour state at this
@@ -272,27 +322,27 @@ __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? Dims<N>::MIN_CTAS : 1) st
     double dq_old[NSTATE];
     if (node_thread) {
 #pragma unroll
-        for (int s = 0; s < NSTATE; ++s) q[s] = Qin[((size_t)e * NSTATE + s) * Np + t];
+        for (int s = 0; s < NSTATE; ++s) q[s] = Qin[ebase + s * Np + t];
         if (read_reg) {
 #pragma unroll
-            for (int s = 0; s < NSTATE; ++s) dq_old[s] = P.dQ[((size_t)e * NSTATE + s) * Np + t];
+            for (int s = 0; s < NSTATE; ++s) dq_old[s] = P.dQ[ebase + s * Np + t];
         }
     }
-    int f = 0, fn = 0, fa = 0, fb = 0, d = 0, vM = 0, nb = -1, levp = 0;
+    int f = 0, fn = 0, d = 0, vM = 0, nb = -1, levp = 0;
     R qp[NSTATE];
     if (face_thread) {
         f = t / Nfp;
-        fn = t % Nfp;
-        fa = fn % Nq;
-        fb = fn / Nq;
+        fn = t - f * Nfp;
+        const int fa = fn % Nq, fb = fn / Nq;
         d = f >> 1;
         vM = face_node<N>(f, fa, fb);
         nb = P.nbr[6 * e + f];
         if (nb >= 0) {
             const int vP = face_node<N>(f ^ 1, fa, fb);
             levp = (nb % P.nz) * Nq + vP / Nfp;
+            const size_t nbase = (size_t)nb * NSTATE * Np + vP;
 #pragma unroll
-            for (int s = 0; s < NSTATE; ++s) qp[s] = Qin[((size_t)nb * NSTATE + s) * Np + vP];
+            for (int s = 0; s < NSTATE; ++s) qp[s] = Qin[nbase + s * Np];
         } else {
             levp = ez * Nq + vM / Nfp;
         }
@@ -305,14 +355,17 @@ __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? Dims<N>::MIN_CTAS : 1) st
     if (node_thread) {
         const Level<R> lv = load_level<R>(P, ez * Nq + t / Nfp);
         const Thermo<R, MIXED> th = thermo<R, MIXED>(q, lv, P);
+        R* rec = s_node + t * W;
+        st5<R>(rec, q);
+        rec[5] = th.c;
+        rec[6] = th.rinv;
 #pragma unroll
-        for (int s = 0; s < NSTATE; ++s) {
-            s_q[s][t] = q[s];
+        for (int dd = 0; dd < 3; ++dd) {
+            R F[NSTATE];
 #pragma unroll
-            for (int dd = 0; dd < 3; ++dd) s_F[dd][s][t] = flux_d<R, MIXED>(q, th, dd, s);
+            for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(q, th, dd, s);
+            st5<R>(s_F + (dd * Np + t) * W, F);
         }
-        s_c[t] = th.c;
-        s_ri[t] = th.rinv;
         if (ph.gravity) {
             R rho_s = MIXED ? ((ph.ref_state && ph.subtract_off) ? q[0] : lv.rho_ref + q[0])
                             : ((ph.ref_state && ph.subtract_off) ? q[0] - lv.rho_ref : q[0]);
@@ -325,12 +378,13 @@ __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? Dims<N>::MIN_CTAS : 1) st
     if (face_thread) {
         const R sgn = (f & 1) ? R(1) : R(-1);
         R qm[NSTATE], Fm[NSTATE], Fp[NSTATE], jr[NSTATE] = {0, 0, 0, 0, 0};
+        const R* rec = s_node + vM * W;
+        ld5<R>(rec, qm);
+        const R c_m = rec[5], ri_m = rec[6];
+        ld5<R>(s_F + (d * Np + vM) * W, Fm);
 #pragma unroll
-        for (int s = 0; s < NSTATE; ++s) {
-            qm[s] = s_q[s][vM];
-            Fm[s] = sgn * s_F[d][s][vM];
-        }
-        const R lam_m = fabs(pick3(d, qm[1], qm[2], qm[3]) * s_ri[vM]) + s_c[vM];
+        for (int s = 0; s < NSTATE; ++s) Fm[s] *= sgn;
+        const R lam_m = fabs(pick3(d, qm[1], qm[2], qm[3]) * ri_m) + c_m;
         if (nb >= 0) {
             if (MIXED && d == 2 && ph.numflux == CMDG_FLUX_RUSANOV) {
                 // reference-state jump q_ref(-) - q_ref(+) across a vertical face
@@ -357,11 +411,11 @@ __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? Dims<N>::MIN_CTAS : 1) st
         const R lam_p = fabs(pick3(d, thp.u[0], thp.u[1], thp.u[2])) + thp.c;
         const R lift = pick3(d, xi[0], xi[1], xi[2]) * KConst<R>::inv_w0(P);
         const R hmw = (ph.numflux == CMDG_FLUX_RUSANOV) ? R(0.5) * fmax(lam_m, lam_p) : R(0);
+        const R hl = R(0.5) * lift, pl = hmw * lift;
+        R fs[NSTATE];
 #pragma unroll
-        for (int s = 0; s < NSTATE; ++s) {
-            R fstar = R(0.5) * (Fm[s] + Fp[s]) + hmw * ((qm[s] - qp[s]) + jr[s]);
-            s_fs[f][s][fn] = lift * fstar;
-        }
+        for (int s = 0; s < NSTATE; ++s) fs[s] = hl * (Fm[s] + Fp[s]) + pl * ((qm[s] - qp[s]) + jr[s]);
+        st5<R>(s_fs + (f * Nfp + fn) * W, fs);
     }
     __syncthreads();
 
@@ -369,53 +423,64 @@ __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? Dims<N>::MIN_CTAS : 1) st
     int bad = 0;
     if (node_thread) {
         const int i = t % Nq, j = (t / Nq) % Nq, k = t / Nfp;
-        R Di[Nq], Dj[Nq], Dk[Nq];
+        R acc1[NSTATE] = {0, 0, 0, 0, 0}, acc2[NSTATE] = {0, 0, 0, 0, 0}, acc3[NSTATE] = {0, 0, 0, 0, 0};
+        const R* F1 = s_F + (0 * Np + Nq * (j + Nq * k)) * W;      // line along xi1
+        const R* F2 = s_F + (1 * Np + i + Nq * Nq * k) * W;        // line along xi2 (stride Nq)
+        const R* F3 = s_F + (2 * Np + i + Nq * j) * W;             // line along xi3 (stride Nfp)
 #pragma unroll
         for (int n = 0; n < Nq; ++n) {
-            Di[n] = s_D[i * Nq + n];
-            Dj[n] = s_D[j * Nq + n];
-            Dk[n] = s_D[k * Nq + n];
+            R v1[NSTATE], v2[NSTATE], v3[NSTATE];
+            ld5<R>(F1 + n * W, v1);
+            ld5<R>(F2 + n * Nq * W, v2);
+            ld5<R>(F3 + n * Nfp * W, v3);
+            const R d1 = s_D[i * Nq + n], d2 = s_D[j * Nq + n], d3 = s_D[k * Nq + n];
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) {
+                acc1[s] = fma(d1, v1[s], acc1[s]);
+                acc2[s] = fma(d2, v2[s], acc2[s]);
+                acc3[s] = fma(d3, v3[s], acc3[s]);
+            }
         }
+        R rhs[NSTATE];
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) rhs[s] = xi[0] * acc1[s] + xi[1] * acc2[s] + xi[2] * acc3[s];
+        // face terms (vMI sM F*, lifted in phase 2), in face order 1..6
+        const int fidx[6] = {j + Nq * k, j + Nq * k, i + Nq * k, i + Nq * k, i + Nq * j, i + Nq * j};
+        const bool on[6] = {i == 0, i == N, j == 0, j == N, k == 0, k == N};
+#pragma unroll
+        for (int ff = 0; ff < 6; ++ff) {
+            if (on[ff]) {
+                R v[NSTATE];
+                ld5<R>(s_fs + (ff * Nfp + fidx[ff]) * W, v);
+#pragma unroll
+                for (int s = 0; s < NSTATE; ++s) rhs[s] -= v[s];
+            }
+        }
+        rhs[3] += gsrc;
         const R rkb_dt = KConst<R>::rkb_dt(P);
+        R* Qout = static_cast<R*>(P.Qout);
 #pragma unroll
         for (int s = 0; s < NSTATE; ++s) {
-            R c1 = 0, c2 = 0, c3 = 0;
-#pragma unroll
-            for (int n = 0; n < Nq; ++n) {
-                c1 = fma(Di[n], s_F[0][s][n + Nq * (j + Nq * k)], c1);
-                c2 = fma(Dj[n], s_F[1][s][i + Nq * (n + Nq * k)], c2);
-                c3 = fma(Dk[n], s_F[2][s][i + Nq * (j + Nq * n)], c3);
-            }
-            R rhs = xi[0] * c1 + xi[1] * c2 + xi[2] * c3;
-            if (i == 0) rhs -= s_fs[0][s][j + Nq * k];
-            if (i == N) rhs -= s_fs[1][s][j + Nq * k];
-            if (j == 0) rhs -= s_fs[2][s][i + Nq * k];
-            if (j == N) rhs -= s_fs[3][s][i + Nq * k];
-            if (k == 0) rhs -= s_fs[4][s][i + Nq * j];
-            if (k == N) rhs -= s_fs[5][s][i + Nq * j];
-            if (s == 3) rhs += gsrc;
-            if (!isfinite(rhs)) bad = 1;
-            const size_t idx = ((size_t)e * NSTATE + s) * Np + t;
+            if (!isfinite(rhs[s])) bad = 1;
+            const size_t idx = ebase + s * Np + t;
             if (MODE == 0) {
-                double out = P.alpha * (double)rhs;
+                double out = P.alpha * (double)rhs[s];
                 if (read_reg) out = fma(P.beta, dq_old[s], out);
                 P.dQ[idx] = out;
             } else {
                 // unscaled 2N register: dq_s = rhs_s + A_s dq_{s-1}  (A_1 = 0)
-                R* Qout = static_cast<R*>(P.Qout);
                 double dq;
                 if (MIXED) {
                     // one FP64 FMA per DOF; the conversions run on the integer pipe
-                    const double r64 = f32_to_f64_bits((float)rhs);
                     if (read_reg) {
-                        dq = fma(P.rka, dq_old[s], r64);
+                        dq = fma(P.rka, dq_old[s], f32_to_f64_bits((float)rhs[s]));
                         Qout[idx] = fma(rkb_dt, (R)f64_to_f32_bits(dq), q[s]);
                     } else {
-                        dq = r64;
-                        Qout[idx] = fma(rkb_dt, rhs, q[s]);
+                        dq = f32_to_f64_bits((float)rhs[s]);
+                        Qout[idx] = fma(rkb_dt, rhs[s], q[s]);
                     }
                 } else {
-                    dq = read_reg ? fma(P.rka, dq_old[s], (double)rhs) : (double)rhs;
+                    dq = read_reg ? fma(P.rka, dq_old[s], (double)rhs[s]) : (double)rhs[s];
                     Qout[idx] = (R)fma(P.rkb_dt, dq, (double)q[s]);
                 }
                 if (!P.last_stage) P.dQ[idx] = dq;
@@ -425,14 +490,29 @@ __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? Dims<N>::MIN_CTAS : 1) st
     if (__syncthreads_or(bad) && t == 0) atomicOr(P.status, 1u);
 }
 
+template <int N, typename R, bool MIXED, int MODE>
+cudaError_t launch_mode(const KParams& P, cudaStream_t s) {
+    constexpr size_t bytes = Smem<N, R>::BYTES;
+    if (bytes > 48 * 1024) {
+        // opt in to more than 48 KB of dynamic shared memory, once per device
+        static unsigned long long configured = 0;
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        if (!(configured & (1ull << (dev & 63)))) {
+            e = cudaFuncSetAttribute(stage_kernel<N, R, MIXED, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)bytes);
+            if (e != cudaSuccess) return e;
+            configured |= 1ull << (dev & 63);
+        }
+    }
+    stage_kernel<N, R, MIXED, MODE><<<(unsigned)P.nelem, Dims<N>::NT, bytes, s>>>(P);
+    return cudaGetLastError();
+}
+
 template <int N, typename R, bool MIXED>
 cudaError_t launch_typed(const KParams& P, int mode, cudaStream_t s) {
-    dim3 grid((unsigned)P.nelem), block(Dims<N>::NT);
-    if (mode == 0)
-        stage_kernel<N, R, MIXED, 0><<<grid, block, 0, s>>>(P);
-    else
-        stage_kernel<N, R, MIXED, 1><<<grid, block, 0, s>>>(P);
-    return cudaGetLastError();
+    return mode == 0 ? launch_mode<N, R, MIXED, 0>(P, s) : launch_mode<N, R, MIXED, 1>(P, s);
 }
 
 template <int N>
