@@ -1,0 +1,120 @@
+"""
+    CMDG
+
+Julia `ccall` shim over libcmdg.so (include/cmdg.h): a `SpaceDiscretization`
+whose functor runs the GPU DG tendency, and a `dostep!` method that runs a
+whole LSRK54CarpenterKennedy step in one fused GPU call.  `solve!`,
+callbacks and `invoke!` of ClimateMachine.jl are used unchanged.
+
+State arrays are the reference's `MPIStateArray.data` (`(Np, nstate,
+nelem)` CuArrays), passed by pointer.  Not exercised in this repository's
+tests (there is no Julia toolchain here); the same ABI is exercised from
+Python.
+"""
+module CMDG
+
+using CUDA
+using ClimateMachine.ODESolvers: LowStorageRungeKutta2N, AbstractODESolver
+import ClimateMachine.ODESolvers: dostep!
+import ClimateMachine.DGMethods: SpaceDiscretization
+
+const libcmdg = get(ENV, "CMDG_LIB", joinpath(@__DIR__, "..", "_build", "libcmdg.so"))
+
+const CMDG_FP64 = Cint(0)
+const CMDG_MIXED = Cint(1)
+
+struct Brick
+    N::Cint
+    ne::NTuple{3, Cint}
+    lo::NTuple{3, Cdouble}
+    hi::NTuple{3, Cdouble}
+    periodic::NTuple{3, Cint}
+    bc_lo::NTuple{3, Cint}
+    bc_hi::NTuple{3, Cint}
+end
+
+struct AtmosParams
+    R_d::Cdouble
+    cp_d::Cdouble
+    cv_d::Cdouble
+    T_0::Cdouble
+    grav::Cdouble
+    MSLP::Cdouble
+    inv_Pr_turb::Cdouble
+    numflux::Cint
+    orientation::Cint
+    gravity::Cint
+    ref_state::Cint
+    subtract_off::Cint
+    profile::Cint
+    T_surface::Cdouble
+    T_min::Cdouble
+    turbulence::Cint
+    rho_nu::Cdouble
+    with_divergence::Cint
+    C_smag::Cdouble
+end
+
+check(rc::Cint) =
+    rc == 0 || error(unsafe_string(ccall((:cmdg_last_error, libcmdg), Cstring, ())))
+
+stream_handle() = CUDA.stream().handle
+
+"""
+    CMDGModel(brick::Brick, params::AtmosParams; precision = CMDG_FP64)
+
+GPU DG model; `grid`, `balance_law` and `state_auxiliary` are kept for the
+reference's callbacks that read them.
+"""
+mutable struct CMDGModel{G, BL, A} <: SpaceDiscretization
+    mesh::Ptr{Cvoid}
+    model::Ptr{Cvoid}
+    grid::G
+    balance_law::BL
+    state_auxiliary::A
+end
+
+function CMDGModel(brick::Brick, params::AtmosParams, grid, balance_law, state_auxiliary;
+                   precision = CMDG_FP64)
+    mesh = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:cmdg_mesh_create_brick, libcmdg), Cint, (Ref{Brick}, Ref{Ptr{Cvoid}}), brick, mesh))
+    model = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:cmdg_model_create, libcmdg), Cint, (Ptr{Cvoid}, Ref{AtmosParams}, Cint, Ref{Ptr{Cvoid}}),
+                mesh[], params, precision, model))
+    dg = CMDGModel(mesh[], model[], grid, balance_law, state_auxiliary)
+    finalizer(dg) do x
+        ccall((:cmdg_model_destroy, libcmdg), Cint, (Ptr{Cvoid},), x.model)
+        ccall((:cmdg_mesh_destroy, libcmdg), Cint, (Ptr{Cvoid},), x.mesh)
+    end
+    return dg
+end
+
+# tendency .= α dQ/dt(Q) + β tendency   (DGModel.jl:85)
+function (dg::CMDGModel)(tendency, Q, _, t, α, β)
+    check(ccall((:cmdg_tendency, libcmdg), Cint,
+                (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, Cdouble, Cdouble, Cdouble, Ptr{Cvoid}),
+                dg.model, pointer(tendency.data), pointer(Q.data), t, α, β, stream_handle()))
+end
+(dg::CMDGModel)(tendency, Q, p, t; increment = false) = dg(tendency, Q, p, t, true, increment)
+
+# one LSRK54 step as one library call (LowStorageRungeKuttaMethod.jl:102)
+function dostep!(Q, lsrk::LowStorageRungeKutta2N{T, RT, AT, 5}, p, time) where {T, RT, AT}
+    dg = lsrk.rhs!
+    if !(dg isa CMDGModel)
+        return invoke(dostep!, Tuple{Any, AbstractODESolver, Any, Any}, Q, lsrk, p, time)
+    end
+    check(ccall((:cmdg_lsrk54_step, libcmdg), Cint,
+                (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, Cdouble, Cdouble, Cint, Ptr{Cvoid}),
+                dg.model, pointer(Q.data), pointer(lsrk.dQ.data), time, lsrk.dt, 1, stream_handle()))
+end
+
+"""Compensated Σ M q over `fields` (weightedsum, MPIStateArrays.jl:655)."""
+function weighted_sums(dg::CMDGModel, Q, fields::Vector{Cint})
+    out = zeros(Cdouble, length(fields))
+    check(ccall((:cmdg_weighted_sums, libcmdg), Cint,
+                (Ptr{Cvoid}, CuPtr{Float64}, Cint, Ptr{Cint}, Ptr{Cdouble}, Ptr{Cvoid}),
+                dg.model, pointer(Q.data), length(fields), fields, out, stream_handle()))
+    return out
+end
+
+end # module
