@@ -24,7 +24,7 @@ EXPORTS = (
     "cmdg_mesh_coordinates", "cmdg_mesh_mass", "cmdg_model_create", "cmdg_model_destroy",
     "cmdg_model_reference_state", "cmdg_tendency", "cmdg_lsrk54_step", "cmdg_to_perturbation",
     "cmdg_from_perturbation", "cmdg_tendency_mixed", "cmdg_lsrk54_step_mixed", "cmdg_weighted_sums",
-    "cmdg_weighted_sums_mixed", "cmdg_courant_dt", "cmdg_status_word",
+    "cmdg_weighted_sums_mixed", "cmdg_courant_dt", "cmdg_status_word", "cmdg_lsrk54_step_noalloc",
 )
 
 
@@ -89,6 +89,7 @@ def load(path: str | None = None):
         "cmdg_weighted_sums_mixed": [P, P, I, P, P, P],
         "cmdg_courant_dt": [P, P, D, P, P],
         "cmdg_status_word": [P, P, P],
+        "cmdg_lsrk54_step_noalloc": [P, P, P, D, D, I, P],
     }
     for name, args in proto.items():
         fn = getattr(L, name)

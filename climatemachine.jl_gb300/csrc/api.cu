@@ -111,6 +111,11 @@ static int run_steps(Model* md, void* Q, double* dQ, double dt, int nsteps, cuda
     return CMDG_OK;
 }
 
+void lsrk54_coefficients(const double** A, const double** B) {
+    *A = LSRK_A;
+    *B = LSRK_B;
+}
+
 static int check_model(const cmdg_model* model) {
     if (!model) {
         set_error("model is NULL");

@@ -127,6 +127,8 @@ struct LaunchArgs {
     int last_stage = 0;      // stage 5: the register is not written
 };
 int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
+// LSRK54CarpenterKennedy A and B coefficient arrays (5 entries each)
+void lsrk54_coefficients(const double** A, const double** B);
 
 // reductions / conversions (reduce.cu)
 int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s);

@@ -136,6 +136,21 @@ int cmdg_tendency(cmdg_model* model, double* d_dQ, const double* d_Q, double t, 
  * (src/Numerics/ODESolvers/LowStorageRungeKuttaMethod.jl:102-158, 293-327). */
 int cmdg_lsrk54_step(cmdg_model* model, double* d_Q, double* d_dQ, double t, double dt, int nsteps, void* stream);
 
+/* Allocation-free form of cmdg_lsrk54_step / cmdg_lsrk54_step_mixed, for
+ * callers that cannot let the library allocate device memory: hosts whose
+ * arena or pool allocator owns all of the device's memory, and hosts that
+ * forbid allocation after start-up.  No counterpart in the reference.
+ *   d_Q: double* for a CMDG_FP64 model, float* (the perturbation) for a
+ *   CMDG_MIXED model; d_dQ: the FP64 RK register.
+ *   The two stage buffers live in a fixed 48 MiB __device__ array held by
+ *   every GPU that loads the library; states larger than 24 MiB are rejected
+ *   with CMDG_ERR_ARG.  The call makes no cudaMalloc / cudaFree.
+ *   The first call on a device looks the array's address up
+ *   (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   Calls share the array: calls whose kernels overlap on the GPU race. */
+int cmdg_lsrk54_step_noalloc(cmdg_model* model, void* d_Q, double* d_dQ, double t, double dt, int nsteps,
+                             void* stream);
+
 /* Mixed precision: converts an FP64 state to the FP32 perturbation
  * q' = q - q_ref (the subtraction is done in FP64) and back.
  * No counterpart in the reference (the reference state lives in aux.ref_state,
