@@ -270,12 +270,14 @@ def main():
     ach_mx = BYTES_MIXED * nodes / (stage_ms_mx * 1e-3) / 1e9
     ach_64 = BYTES_FP64 * nodes / (stage_ms_64 * 1e-3) / 1e9
     traffic = None
-    tpath = os.path.join(REPO, "profiles", "stage_mixed_traffic.json")
+    tpath = os.path.join(REPO, "profiles", "stage_kernel_mixed_bubble20.md")
     if os.path.exists(tpath):
-        try:
-            traffic = json.load(open(tpath)).get("bytes_per_launch_full_size")
-        except Exception:
-            traffic = None
+        for line in open(tpath):
+            if line.startswith("traffic_bytes_per_launch:"):
+                try:
+                    traffic = float(line.split(":", 1)[1].split()[0])
+                except ValueError:
+                    traffic = None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
