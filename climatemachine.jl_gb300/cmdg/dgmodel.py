@@ -159,6 +159,26 @@ class DGModel:
         fn = "cmdg_lsrk54_step_mixed" if self.mixed else "cmdg_lsrk54_step"
         call(fn, self.h, _dptr(Q), _dptr(dQ), float(t), float(dt), int(nsteps), _stream())
 
+    # ------------------------------------------------------------------ launch configuration
+    KERNELS = {"node": 0, "column": 1}
+
+    def set_kernel(self, kind: str = "node", grid_ctas: int = 0):
+        """Stage-kernel family ("node" or "column") and persistent grid size."""
+        call("cmdg_model_set_kernel", self.h, self.KERNELS[kind], int(grid_ctas))
+
+    def get_kernel(self):
+        k, g = ctypes.c_int(), ctypes.c_int()
+        call("cmdg_model_get_kernel", self.h, ctypes.byref(k), ctypes.byref(g))
+        return {v: n for n, v in self.KERNELS.items()}[k.value], g.value
+
+    def autotune(self, reps: int = 20):
+        """Times every launch candidate and keeps the fastest; returns the
+        per-candidate ms/stage and the choice."""
+        ms = (ctypes.c_double * 8)()
+        n = ctypes.c_int()
+        call("cmdg_model_autotune", self.h, int(reps), ms, 8, ctypes.byref(n), _stream())
+        return list(ms)[: n.value], self.get_kernel()
+
     # ------------------------------------------------------------------ reductions
     def weighted_sums(self, Q, fields=(0, 4)):
         fl = (ctypes.c_int * len(fields))(*fields)

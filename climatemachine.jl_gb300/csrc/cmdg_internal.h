@@ -38,6 +38,10 @@ const char* last_error();
     } while (0)
 
 constexpr int NSTATE = 5;
+// neighbour table row per element: 6 face neighbours (or -tag), vertical index, spare
+constexpr int NBR_STRIDE = 8;
+// stage-kernel families: one thread per node, or one thread per vertical line of nodes
+enum { KERNEL_NODE = 0, KERNEL_COLUMN = 1 };
 constexpr int MIN_N = 2;
 constexpr int MAX_N = 5;
 
@@ -50,6 +54,7 @@ enum LevelField {
     LV_RHOE_REF,    // reference total energy density
     LV_CRHO,        // R_d T_0 - (R_d/cv_d) Phi : pressure coefficient of rho
     LV_HREF,        // rhoe_ref + p_ref : reference total enthalpy density
+    LV_PAD,         // unused: rows are 8 wide so a row loads with 128-bit accesses
     LV_NFIELDS
 };
 
@@ -69,7 +74,7 @@ struct Mesh {
     std::vector<double> D;           // D[j*Nq + k] = d l_k / d xi at xi_j
     std::vector<double> Dhat;        // Dhat[i*Nq + n] = D[n][i] w_n / w_i (weak-form volume operator)
     std::vector<double> emetric;     // [nelem][3] dxi_d/dx_d (affine brick)
-    std::vector<int> nbr;            // [nelem][6] neighbour element, or -tag on a boundary face
+    std::vector<int> nbr;            // [nelem][NBR_STRIDE]: 6 neighbours (or -tag), vertical index ez, spare
     std::vector<double> zlev;        // [nlev] node height of each vertical level
     std::vector<double> dzlev;       // [nlev] dz/dxi3 derivative helper (xi3x3 per level)
     // device copies
@@ -108,6 +113,8 @@ struct Model {
     double* d_red = nullptr;         // reduction partials
     size_t red_len = 0;
     std::map<GraphKey, cudaGraphExec_t> graphs;
+    int grid_ctas = 0;               // persistent grid size of the stage kernel (0 = from occupancy)
+    int kernel_kind = 0;             // KERNEL_NODE or KERNEL_COLUMN
 };
 
 // host-side setup (mesh.cpp)

@@ -1,0 +1,401 @@
+// Column-per-thread fused DG tendency + LSRK stage kernel for brick meshes
+// (sm_103a, FP32 mixed-precision path).
+//
+// Work decomposition: a CTA holds EPB elements; the (N+1)^2 threads of an
+// element each own one vertical line of N+1 nodes (i, j, 0..N) — the same
+// (i, j) workgroup shape as the reference's volume_tendency!
+// (src/Numerics/DGMethods/DGModel_kernels.jl:64-309, a thread per (i, j)
+// walking k).  Everything along xi3 stays in registers:
+//   phase A  load the line's state (coalesced across threads), evaluate
+//            thermodynamics and fluxes of its N+1 nodes, stage the xi1/xi2
+//            fluxes in shared memory, contract the xi3 fluxes with Dhat
+//            (compile-time indices: the coefficients come from the parameter
+//            bank), and form the bottom/top face fluxes of the line from the
+//            vertical neighbours' states;
+//   phase B  each thread forms the numerical flux at in-face node c of the
+//            four horizontal faces (balanced: 4 per thread), and contracts the
+//            staged xi1/xi2 fluxes along the two lines through each of its
+//            nodes;
+//   phase C  lines on a horizontal face subtract the lifted face fluxes of
+//            their nodes; gravity; tendency or LSRK 2N stage update.
+// Two barriers per element.  The arithmetic (fluxes, Rusanov flux, lift
+// vMI sM = (2/dx_d)/w_0, Dhat = M^-1 D^T M, unscaled 2N register with one
+// FP64 FMA per DOF) is that of the node-per-thread kernel in stage.cu; only
+// the mapping of work to threads differs.
+#include "dg_common.cuh"
+
+namespace cmdg {
+namespace {
+
+// elements per CTA for each N (threads = EPB (N+1)^2, kept near a multiple of 32)
+template <int N>
+struct ColCfg;
+template <>
+struct ColCfg<3> {
+    static constexpr int EPB = 8;  // 128 threads
+};
+template <>
+struct ColCfg<4> {
+    static constexpr int EPB = 5;  // 125 threads
+};
+template <>
+struct ColCfg<5> {
+    static constexpr int EPB = 4;  // 144 threads
+};
+
+template <int N, typename R>
+struct ColSmem {
+    static constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp, W = 8;
+    // per element: xi1 and xi2 flux records, node records (q, c, 1/rho) of
+    // the horizontal-face nodes, lifted horizontal face fluxes
+    static constexpr int F1 = 0;
+    static constexpr int F2 = F1 + Np * W;
+    static constexpr int NODE = F2 + Np * W;
+    static constexpr int FACE = NODE + 4 * Nfp * W;
+    static constexpr int PER_ELEM = FACE + 4 * Nfp * W;
+    static constexpr int DMAT = ColCfg<N>::EPB * PER_ELEM;
+    static constexpr int TOTAL = DMAT + Nq * Nq;
+    static constexpr size_t BYTES = sizeof(R) * TOTAL;
+};
+
+template <typename R>
+__device__ __forceinline__ R dhat_c(const KParams& P, int idx);
+template <>
+__device__ __forceinline__ float dhat_c<float>(const KParams& P, int idx) {
+    return P.DhatC32[idx];
+}
+template <>
+__device__ __forceinline__ double dhat_c<double>(const KParams& P, int idx) {
+    return P.DhatC64[idx];
+}
+
+// Numerical flux F*.n (Rusanov or central) of one face node, lifted:
+// out = lift * (1/2 (Fm + Fp) + 1/2 max(lam_m, lam_p) ((qm - qp) + jr)).
+template <typename R, bool MIXED>
+__device__ __forceinline__ void face_flux(const KParams& P, const R qm[NSTATE], const R Fm[NSTATE], R lam_m,
+                                          const R qp_in[NSTATE], bool wall, const Level<R>& lvp, int d, R sgn,
+                                          const R jr[NSTATE], R lift, R out[NSTATE]) {
+    R qp[NSTATE];
+    if (wall) {
+        // Impenetrable(FreeSlip) + Insulating wall: rhou+ = rhou- - 2 (rhou-.n) n
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) qp[s] = qm[s];
+        qp[1 + d] = -qm[1 + d];
+    } else {
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) qp[s] = qp_in[s];
+    }
+    const Thermo<R, MIXED> thp = thermo<R, MIXED>(qp, lvp, P);
+    R Fp[NSTATE];
+    normal_flux<R, MIXED>(qp, thp, d, sgn, Fp);
+    const R lam_p = fabs(thp.u[d]) + thp.c;
+    const R hmw = (P.ph.numflux == CMDG_FLUX_RUSANOV) ? R(0.5) * fmax(lam_m, lam_p) : R(0);
+    const R hl = R(0.5) * lift, pl = hmw * lift;
+#pragma unroll
+    for (int s = 0; s < NSTATE; ++s) out[s] = hl * (Fm[s] + Fp[s]) + pl * ((qm[s] - qp[s]) + jr[s]);
+}
+
+template <int N, typename R, bool MIXED, int MODE>
+__global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kernel(const KParams P) {
+    constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp, W = 8, EPB = ColCfg<N>::EPB;
+    constexpr int ESTRIDE = NSTATE * Np;
+    using CS = ColSmem<N, R>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* const sm = reinterpret_cast<R*>(smem_raw);
+
+    const int lt = threadIdx.x;
+    const int el = lt / Nfp;
+    const int c = lt - el * Nfp;
+    const int ci = c % Nq, cj = c / Nq;
+    const int e_raw = blockIdx.x * EPB + el;
+    const bool valid = e_raw < P.nelem;
+    const int e = valid ? e_raw : P.nelem - 1;
+    R* const sF1 = sm + el * CS::PER_ELEM + CS::F1;
+    R* const sF2 = sm + el * CS::PER_ELEM + CS::F2;
+    R* const sNode = sm + el * CS::PER_ELEM + CS::NODE;
+    R* const sFace = sm + el * CS::PER_ELEM + CS::FACE;
+    R* const sD = sm + CS::DMAT;
+    const R* __restrict__ Qin = static_cast<const R*>(P.Qin);
+    const Physics& ph = P.ph;
+    const bool read_reg = (MODE == 0) ? (P.beta != 0) : !P.first_stage;
+    if (lt < Nq * Nq) sD[lt] = dhat_c<R>(P, lt);
+
+    // ---------------- loads: element row, own line, neighbours' face nodes
+    const int4 nb03 = __ldg(reinterpret_cast<const int4*>(P.nbr + NBR_STRIDE * e));
+    const int4 nb45 = __ldg(reinterpret_cast<const int4*>(P.nbr + NBR_STRIDE * e + 4));
+    const int nbf[4] = {nb03.x, nb03.y, nb03.z, nb03.w};
+    const int nbb = nb45.x, nbt = nb45.y, ez = nb45.z;
+    const R xi[3] = {KConst<R>::metric(P, e, 0), KConst<R>::metric(P, e, 1), KConst<R>::metric(P, e, 2)};
+    R q[Nq][NSTATE];
+    {
+        const R* qe = Qin + (size_t)e * ESTRIDE + c;
+#pragma unroll
+        for (int k = 0; k < Nq; ++k)
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) q[k][s] = qe[s * Np + k * Nfp];
+    }
+    R qb[NSTATE], qt[NSTATE], qh[4][NSTATE];
+    if (nbb >= 0) {
+        const R* qn = Qin + (size_t)nbb * ESTRIDE + c + N * Nfp;
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) qb[s] = qn[s * Np];
+    }
+    if (nbt >= 0) {
+        const R* qn = Qin + (size_t)nbt * ESTRIDE + c;
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) qt[s] = qn[s * Np];
+    }
+    // in-face node c = (a, b) of horizontal face f; neighbour node on face f^1
+    const int ca = c % Nq, cb = c / Nq;
+    const int vPh[4] = {N + Nq * c, Nq * c, ca + Nq * (N + Nq * cb), ca + Nq * (Nq * cb)};
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+        if (nbf[f] >= 0) {
+            const R* qn = Qin + (size_t)nbf[f] * ESTRIDE + vPh[f];
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) qh[f][s] = qn[s * Np];
+        }
+    }
+
+    // ---------------- phase A: line thermodynamics, fluxes, xi3 terms
+    R acc[Nq][NSTATE];
+    R gsrc[Nq];
+    {
+        R F3[Nq][NSTATE];
+        R c_end[2], ri_end[2];
+#pragma unroll
+        for (int k = 0; k < Nq; ++k) {
+            const Level<R> lv = load_level<R>(P, ez * Nq + k);
+            const Thermo<R, MIXED> th = thermo<R, MIXED>(q[k], lv, P);
+            const int node = c + k * Nfp;
+            R F[NSTATE];
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(q[k], th, 0, s);
+            st5<R>(sF1 + node * W, F);
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(q[k], th, 1, s);
+            st5<R>(sF2 + node * W, F);
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) F3[k][s] = flux_d<R, MIXED>(q[k], th, 2, s);
+            // node records of horizontal-face nodes, at their in-face index
+            R* rec = nullptr;
+            if (ci == 0) rec = sNode + (0 * Nfp + cj + Nq * k) * W;
+            if (ci == N) rec = sNode + (1 * Nfp + cj + Nq * k) * W;
+            if (rec) {
+                st5<R>(rec, q[k]);
+                rec[5] = th.c;
+                rec[6] = th.rinv;
+            }
+            rec = nullptr;
+            if (cj == 0) rec = sNode + (2 * Nfp + ci + Nq * k) * W;
+            if (cj == N) rec = sNode + (3 * Nfp + ci + Nq * k) * W;
+            if (rec) {
+                st5<R>(rec, q[k]);
+                rec[5] = th.c;
+                rec[6] = th.rinv;
+            }
+            if (k == 0) {
+                c_end[0] = th.c;
+                ri_end[0] = th.rinv;
+            }
+            if (k == N) {
+                c_end[1] = th.c;
+                ri_end[1] = th.rinv;
+            }
+            gsrc[k] = 0;
+            if (ph.gravity) {
+                R rho_s = MIXED ? ((ph.ref_state && ph.subtract_off) ? q[k][0] : lv.rho_ref + q[k][0])
+                                : ((ph.ref_state && ph.subtract_off) ? q[k][0] - lv.rho_ref : q[k][0]);
+                gsrc[k] = -rho_s * lv.gphiz;
+            }
+        }
+        // xi3 contraction in registers: acc[k] = xi3 sum_n Dhat[k][n] F3[n]
+#pragma unroll
+        for (int k = 0; k < Nq; ++k)
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) {
+                R a = 0;
+#pragma unroll
+                for (int n = 0; n < Nq; ++n) a = fma(dhat_c<R>(P, k * Nq + n), F3[n][s], a);
+                acc[k][s] = xi[2] * a;
+            }
+        // bottom (face 5 of the reference, xi3 = -1) and top (face 6) of the line
+        const R lift3 = xi[2] * KConst<R>::inv_w0(P);
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const int k = side ? N : 0;
+            const R sgn = side ? R(1) : R(-1);
+            const int nbv = side ? nbt : nbb;
+            R Fm[NSTATE], jr[NSTATE] = {0, 0, 0, 0, 0};
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) Fm[s] = sgn * F3[k][s];
+            const R lam_m = fabs(q[k][3] * ri_end[side]) + c_end[side];
+            int lev_p = ez * Nq + k;
+            if (nbv >= 0) {
+                int ezp = ez + (side ? 1 : -1);
+                ezp = ezp < 0 ? ezp + P.nz : (ezp >= P.nz ? ezp - P.nz : ezp);
+                lev_p = ezp * Nq + (side ? 0 : N);
+                if (MIXED && ph.numflux == CMDG_FLUX_RUSANOV) {
+                    const int ej = side ? ezp : ez;
+                    const R sj = side ? R(-1) : R(1);
+                    jr[0] = sj * (R)P.jump32[2 * ej + 0];
+                    jr[4] = sj * (R)P.jump32[2 * ej + 1];
+                }
+            }
+            const Level<R> lvp = load_level<R>(P, lev_p);
+            R fs[NSTATE];
+            face_flux<R, MIXED>(P, q[k], Fm, lam_m, side ? qt : qb, nbv < 0, lvp, 2, sgn, jr, lift3, fs);
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) acc[k][s] -= fs[s];
+        }
+    }
+    __syncthreads();
+
+    // ---------------- phase B: horizontal faces (in-face node c of faces 1-4), xi1/xi2 terms
+    double dq_old[Nq][NSTATE];
+    const size_t ebase = (size_t)e * ESTRIDE + c;
+    if (read_reg) {
+#pragma unroll
+        for (int k = 0; k < Nq; ++k)
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) dq_old[k][s] = P.dQ[ebase + s * Np + k * Nfp];
+    }
+    {
+        const int vMh[4] = {Nq * c, N + Nq * c, ca + Nfp * cb, ca + Nq * N + Nfp * cb};
+        const R inv_w0 = KConst<R>::inv_w0(P);
+        const Level<R> lvh = load_level<R>(P, ez * Nq + cb);
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+            const int d = f >> 1;
+            const R sgn = (f & 1) ? R(1) : R(-1);
+            const R* rec = sNode + (f * Nfp + c) * W;
+            R qm[NSTATE], Fm[NSTATE];
+            ld5<R>(rec, qm);
+            const R c_m = rec[5], ri_m = rec[6];
+            ld5<R>((d == 0 ? sF1 : sF2) + vMh[f] * W, Fm);
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) Fm[s] *= sgn;
+            const R lam_m = fabs(qm[1 + d] * ri_m) + c_m;
+            const R jr[NSTATE] = {0, 0, 0, 0, 0};
+            R fs[NSTATE];
+            face_flux<R, MIXED>(P, qm, Fm, lam_m, qh[f], nbf[f] < 0, lvh, d, sgn, jr, xi[d] * inv_w0, fs);
+            st5<R>(sFace + (f * Nfp + c) * W, fs);
+        }
+        R Di[Nq], Dj[Nq];
+#pragma unroll
+        for (int n = 0; n < Nq; ++n) {
+            Di[n] = sD[ci * Nq + n];
+            Dj[n] = sD[cj * Nq + n];
+        }
+#pragma unroll
+        for (int k = 0; k < Nq; ++k) {
+            R c1[NSTATE] = {0, 0, 0, 0, 0}, c2[NSTATE] = {0, 0, 0, 0, 0};
+            const R* L1 = sF1 + (Nq * (cj + Nq * k)) * W;
+            const R* L2 = sF2 + (ci + Nfp * k) * W;
+#pragma unroll
+            for (int n = 0; n < Nq; ++n) {
+                R v1[NSTATE], v2[NSTATE];
+                ld5<R>(L1 + n * W, v1);
+                ld5<R>(L2 + n * Nq * W, v2);
+#pragma unroll
+                for (int s = 0; s < NSTATE; ++s) {
+                    c1[s] = fma(Di[n], v1[s], c1[s]);
+                    c2[s] = fma(Dj[n], v2[s], c2[s]);
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) acc[k][s] += xi[0] * c1[s] + xi[1] * c2[s];
+        }
+    }
+    __syncthreads();
+
+    // ---------------- phase C: horizontal face terms, source, update
+    int bad = 0;
+#pragma unroll
+    for (int k = 0; k < Nq; ++k) {
+        auto sub_face = [&](int f, int idx) {
+            R v[NSTATE];
+            ld5<R>(sFace + (f * Nfp + idx) * W, v);
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) acc[k][s] -= v[s];
+        };
+        if (ci == 0) sub_face(0, cj + Nq * k);
+        if (ci == N) sub_face(1, cj + Nq * k);
+        if (cj == 0) sub_face(2, ci + Nq * k);
+        if (cj == N) sub_face(3, ci + Nq * k);
+        acc[k][3] += gsrc[k];
+    }
+    if (valid) {
+        const R rkb_dt = KConst<R>::rkb_dt(P);
+        R* Qout = static_cast<R*>(P.Qout);
+#pragma unroll
+        for (int k = 0; k < Nq; ++k)
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) {
+                const R rhs = acc[k][s];
+                if (!isfinite(rhs)) bad = 1;
+                const size_t idx = ebase + s * Np + k * Nfp;
+                if (MODE == 0) {
+                    double out = P.alpha * (double)rhs;
+                    if (read_reg) out = fma(P.beta, dq_old[k][s], out);
+                    P.dQ[idx] = out;
+                } else {
+                    double dq;
+                    if (MIXED) {
+                        if (read_reg) {
+                            dq = fma(P.rka, dq_old[k][s], f32_to_f64_bits((float)rhs));
+                            Qout[idx] = fma(rkb_dt, (R)f64_to_f32_bits(dq), q[k][s]);
+                        } else {
+                            dq = f32_to_f64_bits((float)rhs);
+                            Qout[idx] = fma(rkb_dt, rhs, q[k][s]);
+                        }
+                    } else {
+                        dq = read_reg ? fma(P.rka, dq_old[k][s], (double)rhs) : (double)rhs;
+                        Qout[idx] = (R)fma(P.rkb_dt, dq, (double)q[k][s]);
+                    }
+                    if (!P.last_stage) P.dQ[idx] = dq;
+                }
+            }
+    }
+    if (__syncthreads_or(bad) && lt == 0) atomicOr(P.status, 1u);
+}
+
+template <int N, int MODE>
+cudaError_t launch_col(const KParams& P, cudaStream_t s) {
+    using CS = ColSmem<N, float>;
+    constexpr int EPB = ColCfg<N>::EPB;
+    constexpr size_t bytes = CS::BYTES;
+    static unsigned long long configured = 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (bytes > 48 * 1024 && !(configured & (1ull << (dev & 63)))) {
+        e = cudaFuncSetAttribute(column_kernel<N, float, true, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)bytes);
+        if (e != cudaSuccess) return e;
+        configured |= 1ull << (dev & 63);
+    }
+    const unsigned grid = (unsigned)((P.nelem + EPB - 1) / EPB);
+    column_kernel<N, float, true, MODE><<<grid, EPB * (N + 1) * (N + 1), bytes, s>>>(P);
+    return cudaGetLastError();
+}
+
+template <int N>
+cudaError_t launch_col_mode(const KParams& P, int mode, cudaStream_t s) {
+    return mode == 0 ? launch_col<N, 0>(P, s) : launch_col<N, 1>(P, s);
+}
+
+}  // namespace
+
+cudaError_t launch_column(const KParams& P, int N, bool mixed, int mode, int grid, cudaStream_t s) {
+    (void)grid;
+    if (!mixed) return cudaErrorNotSupported;
+    switch (N) {
+        case 3: return launch_col_mode<3>(P, mode, s);
+        case 4: return launch_col_mode<4>(P, mode, s);
+        case 5: return launch_col_mode<5>(P, mode, s);
+        default: return cudaErrorNotSupported;
+    }
+}
+
+}  // namespace cmdg

@@ -1,0 +1,251 @@
+// Device-side building blocks shared by the fused stage kernels: kernel
+// parameters, precision-dependent constants, IEEE-754 conversions on the
+// integer pipe, per-level reference-state rows, dry-air thermodynamics and
+// first-order fluxes of the AtmosModel, and packed shared-memory records.
+#pragma once
+
+#include "cmdg_internal.h"
+
+namespace cmdg {
+
+// Arguments of one stage-kernel launch (passed by value: the parameter bank).
+struct KParams {
+    const void* Qin;
+    void* Qout;
+    double* dQ;
+    const double* emetric;
+    const int* nbr;
+    const double* lvl64;
+    const float* lvl32;
+    const float* jump32;
+    const void* Dhat;
+    unsigned* status;
+    int nelem, nz;
+    const float* emetric32;
+    double alpha, beta, rka, rkb_dt;
+    double inv_w0;
+    float rkb_dt32, inv_w032, gm132, gamma32;
+    int first_stage, last_stage;
+    Physics ph;
+    // weak-form derivative Dhat[i][n] = D[n][i] w_n / w_i (row-major, N <= MAX_N),
+    // in the parameter bank so compile-time indexed reads cost no instruction
+    float DhatC32[(MAX_N + 1) * (MAX_N + 1)];
+    double DhatC64[(MAX_N + 1) * (MAX_N + 1)];
+};
+
+// Builds the launch arguments of a model (stage.cu).
+KParams make_params(Model* md, const LaunchArgs& a);
+// Column-kernel launcher (column.cu); returns cudaErrorNotSupported when no
+// column instantiation exists for the model's N.
+cudaError_t launch_column(const KParams& P, int N, bool mixed, int mode, int grid, cudaStream_t s);
+
+namespace {
+
+
+// Constants in the working precision R, read without a run-time FP64->FP32
+// conversion (on this GPU such conversions issue on the FP64 pipe).
+template <typename R>
+struct KConst;
+template <>
+struct KConst<double> {
+    static __device__ __forceinline__ double gm1(const KParams& P) { return P.ph.gm1; }
+    static __device__ __forceinline__ double gamma(const KParams& P) { return P.ph.gamma; }
+    static __device__ __forceinline__ double inv_w0(const KParams& P) { return P.inv_w0; }
+    static __device__ __forceinline__ double rkb_dt(const KParams& P) { return P.rkb_dt; }
+    static __device__ __forceinline__ double metric(const KParams& P, int e, int d) { return P.emetric[3 * e + d]; }
+};
+template <>
+struct KConst<float> {
+    static __device__ __forceinline__ float gm1(const KParams& P) { return P.gm132; }
+    static __device__ __forceinline__ float gamma(const KParams& P) { return P.gamma32; }
+    static __device__ __forceinline__ float inv_w0(const KParams& P) { return P.inv_w032; }
+    static __device__ __forceinline__ float rkb_dt(const KParams& P) { return P.rkb_dt32; }
+    static __device__ __forceinline__ float metric(const KParams& P, int e, int d) { return P.emetric32[3 * e + d]; }
+};
+
+// FP32 -> FP64 by IEEE-754 field arithmetic on the integer pipe (on this GPU
+// the F2F conversion instructions issue on the FP64 pipe).  Exact for normal
+// numbers and zero; an FP32 subnormal (|f| < 2^-126) maps to a value of the
+// same sign below 2^-126, and a non-finite input to a value beyond the FP32
+// range (non-finite tendencies are reported through the status word before
+// they reach this conversion).
+__device__ __forceinline__ double f32_to_f64_bits(float f) {
+    const unsigned b = __float_as_uint(f);
+    const unsigned sign = b & 0x80000000u;
+    const unsigned mag = b & 0x7FFFFFFFu;
+    const unsigned hi = (mag == 0u) ? sign : (sign | ((mag >> 3) + (896u << 20)));
+    return __hiloint2double((int)hi, (int)(mag << 29));
+}
+
+// FP64 -> FP32 by IEEE-754 field arithmetic on the integer pipe, rounding
+// toward zero (error below one FP32 ulp).  Magnitudes under 2^-126 flush to a
+// signed zero; magnitudes beyond the FP32 range, infinities and NaNs give an
+// infinity.  Used for the stage increment only, which is small next to the
+// state it is added to.
+__device__ __forceinline__ float f64_to_f32_bits(double d) {
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned sign = hi & 0x80000000u;
+    const unsigned mag = hi & 0x7FFFFFFFu;
+    unsigned bits = sign | (((mag - (896u << 20)) << 3) | (lo >> 29));
+    bits = (mag < (897u << 20)) ? sign : bits;
+    bits = (mag >= (1151u << 20)) ? (sign | 0x7F800000u) : bits;
+    return __uint_as_float(bits);
+}
+
+template <typename R>
+struct Level {
+    R rho_ref, p_ref, href, crho, gphiz;
+};
+
+template <typename R>
+__device__ __forceinline__ Level<R> load_level(const KParams& P, int lev);
+
+static_assert(LV_NFIELDS == 8 && LV_GPHIZ == 1 && LV_RHO_REF == 2 && LV_P_REF == 3 && LV_CRHO == 5 && LV_HREF == 6,
+              "level rows are read as vectors");
+
+template <>
+__device__ __forceinline__ Level<double> load_level<double>(const KParams& P, int lev) {
+    const double2* L = reinterpret_cast<const double2*>(P.lvl64 + (size_t)lev * LV_NFIELDS);
+    const double2 a = __ldg(L), b = __ldg(L + 1), c = __ldg(L + 2), d = __ldg(L + 3);
+    Level<double> l;
+    l.gphiz = a.y;
+    l.rho_ref = b.x;
+    l.p_ref = b.y;
+    l.crho = c.y;
+    l.href = d.x;
+    return l;
+}
+
+template <>
+__device__ __forceinline__ Level<float> load_level<float>(const KParams& P, int lev) {
+    const float4* L = reinterpret_cast<const float4*>(P.lvl32 + (size_t)lev * LV_NFIELDS);
+    const float4 a = __ldg(L), b = __ldg(L + 1);
+    Level<float> l;
+    l.gphiz = a.y;
+    l.rho_ref = a.z;
+    l.p_ref = a.w;
+    l.crho = b.y;
+    l.href = b.z;
+    return l;
+}
+
+// Reciprocal and square root in the working precision: correctly rounded in
+// FP64; the hardware approximations (a few ulp) in FP32, where every other
+// operation already carries FP32 rounding.
+__device__ __forceinline__ double rcp_r(double x) { return 1.0 / x; }
+__device__ __forceinline__ float rcp_r(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ double sqrt_r(double x) { return sqrt(x); }
+__device__ __forceinline__ float sqrt_r(float x) { return x * rsqrtf(x); }
+
+// Pointwise thermodynamics of dry air (PhaseDry: T = T0 + e_int/cv, p = rho R T,
+// c = sqrt(gamma R T)) for a conserved state q, which is the full state
+// (R = double) or the perturbation about the reference state (MIXED).
+template <typename R, bool MIXED>
+struct Thermo {
+    R rinv;   // 1 / rho
+    R u[3];   // velocity
+    R pflux;  // pressure entering the momentum flux (p - p_ref with subtract_off)
+    R H;      // rhoe + p
+    R c;      // sound speed
+};
+
+template <typename R, bool MIXED>
+__device__ __forceinline__ Thermo<R, MIXED> thermo(const R q[NSTATE], const Level<R>& lv, const KParams& P) {
+    Thermo<R, MIXED> t;
+    const Physics& ph = P.ph;
+    const R gm1 = KConst<R>::gm1(P), gamma = KConst<R>::gamma(P);
+    R rho = MIXED ? (lv.rho_ref + q[0]) : q[0];
+    t.rinv = rcp_r(rho);
+    t.u[0] = q[1] * t.rinv;
+    t.u[1] = q[2] * t.rinv;
+    t.u[2] = q[3] * t.rinv;
+    R ke2 = q[1] * t.u[0] + q[2] * t.u[1] + q[3] * t.u[2];
+    R p;
+    if (MIXED) {
+        // p' = gm1 (rhoe' - ke/2) + rho' crho ; p = p_ref + p'
+        R pp = gm1 * (q[4] - R(0.5) * ke2) + q[0] * lv.crho;
+        p = lv.p_ref + pp;
+        t.pflux = (ph.ref_state && ph.subtract_off) ? pp : p;
+        t.H = lv.href + (q[4] + pp);
+    } else {
+        p = gm1 * (q[4] - R(0.5) * ke2) + rho * lv.crho;
+        t.pflux = (ph.ref_state && ph.subtract_off) ? (p - lv.p_ref) : p;
+        t.H = q[4] + p;
+    }
+    t.c = sqrt_r(gamma * p * t.rinv);
+    return t;
+}
+
+// first-order flux component in direction d for field s
+template <typename R, bool MIXED>
+__device__ __forceinline__ R flux_d(const R q[NSTATE], const Thermo<R, MIXED>& t, int d, int s) {
+    if (s == 0) return q[1 + d];
+    if (s == 4) return t.u[d] * t.H;
+    return q[1 + d] * t.u[s - 1] + ((s - 1 == d) ? t.pflux : R(0));
+}
+
+// component d (0, 1, 2; a run-time value) of a 3-vector without indexing a
+// local array, so the values stay in registers
+template <typename R>
+__device__ __forceinline__ R pick3(int d, R a, R b, R c) {
+    return d == 0 ? a : (d == 1 ? b : c);
+}
+
+// normal first-order flux F_d (all 5 fields) for a face normal to xi_d
+template <typename R, bool MIXED>
+__device__ __forceinline__ void normal_flux(const R q[NSTATE], const Thermo<R, MIXED>& t, int d, R sgn, R F[NSTATE]) {
+    const R mn = pick3(d, q[1], q[2], q[3]);
+    const R un = pick3(d, t.u[0], t.u[1], t.u[2]);
+    F[0] = sgn * mn;
+    F[1] = sgn * (mn * t.u[0] + (d == 0 ? t.pflux : R(0)));
+    F[2] = sgn * (mn * t.u[1] + (d == 1 ? t.pflux : R(0)));
+    F[3] = sgn * (mn * t.u[2] + (d == 2 ? t.pflux : R(0)));
+    F[4] = sgn * (un * t.H);
+}
+
+
+// Shared-memory record of one node or face node: the five fields packed
+// contiguously (plus two spare slots) so a record moves with 128-bit accesses.
+template <typename R>
+struct Slot {
+    static constexpr int W = 8;  // record width in elements of R
+};
+
+template <typename R>
+__device__ __forceinline__ void ld5(const R* p, R v[NSTATE]);
+template <>
+__device__ __forceinline__ void ld5<float>(const float* p, float v[NSTATE]) {
+    const float4 a = *reinterpret_cast<const float4*>(p);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = a.z;
+    v[3] = a.w;
+    v[4] = p[4];
+}
+template <>
+__device__ __forceinline__ void ld5<double>(const double* p, double v[NSTATE]) {
+    const double2 a = *reinterpret_cast<const double2*>(p);
+    const double2 b = *reinterpret_cast<const double2*>(p + 2);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
+    v[4] = p[4];
+}
+template <typename R>
+__device__ __forceinline__ void st5(R* p, const R v[NSTATE]);
+template <>
+__device__ __forceinline__ void st5<float>(float* p, const float v[NSTATE]) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    p[4] = v[4];
+}
+template <>
+__device__ __forceinline__ void st5<double>(double* p, const double v[NSTATE]) {
+    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+    *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
+    p[4] = v[4];
+}
+
+
+}  // namespace
+}  // namespace cmdg

@@ -104,7 +104,7 @@ int build_brick(const cmdg_brick_desc* d, Mesh* m) {
         for (int n = 0; n < Nq; ++n) m->Dhat[i * Nq + n] = m->D[n * Nq + i] * m->omega[n] / m->omega[i];
 
     m->emetric.assign(nelem * 3, 0.0);
-    m->nbr.assign(nelem * 6, 0);
+    m->nbr.assign(nelem * NBR_STRIDE, 0);
     const int nx = d->ne[0], ny = d->ne[1], nz = d->ne[2];
     auto eid = [&](int ix, int iy, int iz) { return (int64_t)iz + (int64_t)nz * ((int64_t)ix + (int64_t)nx * iy); };
     for (int iy = 0; iy < ny; ++iy)
@@ -132,8 +132,9 @@ int build_brick(const cmdg_brick_desc* d, Mesh* m) {
                     } else {
                         val = (int)eid(nb[0], nb[1], nb[2]);
                     }
-                    m->nbr[e * 6 + f] = val;
+                    m->nbr[e * NBR_STRIDE + f] = val;
                 }
+                m->nbr[e * NBR_STRIDE + 6] = iz;
             }
     m->zlev.assign(m->nlev, 0.0);
     m->dzlev.assign(m->nlev, 0.0);

@@ -39,7 +39,7 @@
 // which is exact algebra for dry air (T = T0 + e_int/cv, p = rho R T), the
 // reference-state jump across vertical faces enters the Rusanov penalty
 // from an FP64-computed table, and the RK register dQ stays FP64.
-#include "cmdg_internal.h"
+#include "dg_common.cuh"
 
 namespace cmdg {
 namespace {
@@ -52,232 +52,16 @@ struct Dims {
     static constexpr int NF = 6 * Nfp;
     static constexpr int NT = (((Np > NF) ? Np : NF) + 31) / 32 * 32;
     // resident CTAs per SM requested for the FP32 kernels (register budget
-    // 65536 / (NT * MIN_CTAS): 64, 56, 51 and 58 registers for N = 2..5)
-    static constexpr int MIN_CTAS = N == 2 ? 16 : N == 3 ? 12 : N == 4 ? 8 : 5;
+    // 65536 / (NT * MIN_CTAS): 85, 85, 68 and 73 registers for N = 2..5)
+#ifndef CMDG_MIN_CTAS_N4
+#define CMDG_MIN_CTAS_N4 6
+#endif
+    static constexpr int MIN_CTAS = N == 2 ? 12 : N == 3 ? 8 : N == 4 ? CMDG_MIN_CTAS_N4 : 4;
+    // the FP64 kernels are FP64-pipe bound; they keep enough CTAs to cover the barriers
+    static constexpr int MIN_CTAS64 = N == 5 ? 2 : 3;
+    // one CTA per element (no look-ahead registers): a tighter register budget
+    static constexpr int MIN_CTAS_DIRECT = N == 2 ? 16 : N == 3 ? 12 : N == 4 ? 7 : 5;
 };
-
-struct KParams {
-    const void* Qin;
-    void* Qout;
-    double* dQ;
-    const double* emetric;
-    const int* nbr;
-    const double* lvl64;
-    const float* lvl32;
-    const float* jump32;
-    const void* Dhat;
-    unsigned* status;
-    int nelem, nz;
-    const float* emetric32;
-    double alpha, beta, rka, rkb_dt;
-    double inv_w0;
-    float rkb_dt32, inv_w032, gm132, gamma32;
-    int first_stage, last_stage;
-    Physics ph;
-};
-
-// Constants in the working precision R, read without a run-time FP64->FP32
-// conversion (on this GPU such conversions issue on the FP64 pipe).
-template <typename R>
-struct KConst;
-template <>
-struct KConst<double> {
-    static __device__ __forceinline__ double gm1(const KParams& P) { return P.ph.gm1; }
-    static __device__ __forceinline__ double gamma(const KParams& P) { return P.ph.gamma; }
-    static __device__ __forceinline__ double inv_w0(const KParams& P) { return P.inv_w0; }
-    static __device__ __forceinline__ double rkb_dt(const KParams& P) { return P.rkb_dt; }
-    static __device__ __forceinline__ double metric(const KParams& P, int e, int d) { return P.emetric[3 * e + d]; }
-};
-template <>
-struct KConst<float> {
-    static __device__ __forceinline__ float gm1(const KParams& P) { return P.gm132; }
-    static __device__ __forceinline__ float gamma(const KParams& P) { return P.gamma32; }
-    static __device__ __forceinline__ float inv_w0(const KParams& P) { return P.inv_w032; }
-    static __device__ __forceinline__ float rkb_dt(const KParams& P) { return P.rkb_dt32; }
-    static __device__ __forceinline__ float metric(const KParams& P, int e, int d) { return P.emetric32[3 * e + d]; }
-};
-
-// FP32 -> FP64 by IEEE-754 field arithmetic on the integer pipe (on this GPU
-// the F2F conversion instructions issue on the FP64 pipe).  Exact for normal
-// numbers and zero; an FP32 subnormal (|f| < 2^-126) maps to a value of the
-// same sign below 2^-126, and a non-finite input to a value beyond the FP32
-// range (non-finite tendencies are reported through the status word before
-// they reach this conversion).
-__device__ __forceinline__ double f32_to_f64_bits(float f) {
-    const unsigned b = __float_as_uint(f);
-    const unsigned sign = b & 0x80000000u;
-    const unsigned mag = b & 0x7FFFFFFFu;
-    const unsigned hi = (mag == 0u) ? sign : (sign | ((mag >> 3) + (896u << 20)));
-    return __hiloint2double((int)hi, (int)(mag << 29));
-}
-
-// FP64 -> FP32 by IEEE-754 field arithmetic on the integer pipe, rounding
-// toward zero (error below one FP32 ulp).  Magnitudes under 2^-126 flush to a
-// signed zero; magnitudes beyond the FP32 range, infinities and NaNs give an
-// infinity.  Used for the stage increment only, which is small next to the
-// state it is added to.
-__device__ __forceinline__ float f64_to_f32_bits(double d) {
-    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
-    const unsigned sign = hi & 0x80000000u;
-    const unsigned mag = hi & 0x7FFFFFFFu;
-    unsigned bits = sign | (((mag - (896u << 20)) << 3) | (lo >> 29));
-    bits = (mag < (897u << 20)) ? sign : bits;
-    bits = (mag >= (1151u << 20)) ? (sign | 0x7F800000u) : bits;
-    return __uint_as_float(bits);
-}
-
-template <typename R>
-struct Level {
-    R rho_ref, p_ref, href, crho, gphiz;
-};
-
-template <typename R>
-__device__ __forceinline__ Level<R> load_level(const KParams& P, int lev);
-
-template <>
-__device__ __forceinline__ Level<double> load_level<double>(const KParams& P, int lev) {
-    const double* L = P.lvl64 + (size_t)lev * LV_NFIELDS;
-    Level<double> l;
-    l.rho_ref = L[LV_RHO_REF];
-    l.p_ref = L[LV_P_REF];
-    l.href = L[LV_HREF];
-    l.crho = L[LV_CRHO];
-    l.gphiz = L[LV_GPHIZ];
-    return l;
-}
-
-template <>
-__device__ __forceinline__ Level<float> load_level<float>(const KParams& P, int lev) {
-    const float* L = P.lvl32 + (size_t)lev * LV_NFIELDS;
-    Level<float> l;
-    l.rho_ref = L[LV_RHO_REF];
-    l.p_ref = L[LV_P_REF];
-    l.href = L[LV_HREF];
-    l.crho = L[LV_CRHO];
-    l.gphiz = L[LV_GPHIZ];
-    return l;
-}
-
-// Pointwise thermodynamics of dry air (PhaseDry: T = T0 + e_int/cv, p = rho R T,
-// c = sqrt(gamma R T)) for a conserved state q, which is the full state
-// (R = double) or the perturbation about the reference state (MIXED).
-template <typename R, bool MIXED>
-struct Thermo {
-    R rinv;   // 1 / rho
-    R u[3];   // velocity
-    R pflux;  // pressure entering the momentum flux (p - p_ref with subtract_off)
-    R H;      // rhoe + p
-    R c;      // sound speed
-};
-
-template <typename R, bool MIXED>
-__device__ __forceinline__ Thermo<R, MIXED> thermo(const R q[NSTATE], const Level<R>& lv, const KParams& P) {
-    Thermo<R, MIXED> t;
-    const Physics& ph = P.ph;
-    const R gm1 = KConst<R>::gm1(P), gamma = KConst<R>::gamma(P);
-    R rho = MIXED ? (lv.rho_ref + q[0]) : q[0];
-    t.rinv = R(1) / rho;
-    t.u[0] = q[1] * t.rinv;
-    t.u[1] = q[2] * t.rinv;
-    t.u[2] = q[3] * t.rinv;
-    R ke2 = q[1] * t.u[0] + q[2] * t.u[1] + q[3] * t.u[2];
-    R p;
-    if (MIXED) {
-        // p' = gm1 (rhoe' - ke/2) + rho' crho ; p = p_ref + p'
-        R pp = gm1 * (q[4] - R(0.5) * ke2) + q[0] * lv.crho;
-        p = lv.p_ref + pp;
-        t.pflux = (ph.ref_state && ph.subtract_off) ? pp : p;
-        t.H = lv.href + (q[4] + pp);
-    } else {
-        p = gm1 * (q[4] - R(0.5) * ke2) + rho * lv.crho;
-        t.pflux = (ph.ref_state && ph.subtract_off) ? (p - lv.p_ref) : p;
-        t.H = q[4] + p;
-    }
-    t.c = sqrt(gamma * p * t.rinv);
-    return t;
-}
-
-// first-order flux component in direction d for field s
-template <typename R, bool MIXED>
-__device__ __forceinline__ R flux_d(const R q[NSTATE], const Thermo<R, MIXED>& t, int d, int s) {
-    if (s == 0) return q[1 + d];
-    if (s == 4) return t.u[d] * t.H;
-    return q[1 + d] * t.u[s - 1] + ((s - 1 == d) ? t.pflux : R(0));
-}
-
-// component d (0, 1, 2; a run-time value) of a 3-vector without indexing a
-// local array, so the values stay in registers
-template <typename R>
-__device__ __forceinline__ R pick3(int d, R a, R b, R c) {
-    return d == 0 ? a : (d == 1 ? b : c);
-}
-
-// normal first-order flux F_d (all 5 fields) for a face normal to xi_d
-template <typename R, bool MIXED>
-__device__ __forceinline__ void normal_flux(const R q[NSTATE], const Thermo<R, MIXED>& t, int d, R sgn, R F[NSTATE]) {
-    const R mn = pick3(d, q[1], q[2], q[3]);
-    const R un = pick3(d, t.u[0], t.u[1], t.u[2]);
-    F[0] = sgn * mn;
-    F[1] = sgn * (mn * t.u[0] + (d == 0 ? t.pflux : R(0)));
-    F[2] = sgn * (mn * t.u[1] + (d == 1 ? t.pflux : R(0)));
-    F[3] = sgn * (mn * t.u[2] + (d == 2 ? t.pflux : R(0)));
-    F[4] = sgn * (un * t.H);
-}
-
-template <int N>
-__device__ __forceinline__ int face_node(int f, int a, int b) {
-    constexpr int Nq = N + 1;
-    switch (f) {
-        case 0: return 0 + Nq * (a + Nq * b);
-        case 1: return N + Nq * (a + Nq * b);
-        case 2: return a + Nq * (0 + Nq * b);
-        case 3: return a + Nq * (N + Nq * b);
-        case 4: return a + Nq * (b + Nq * 0);
-        default: return a + Nq * (b + Nq * N);
-    }
-}
-
-// Shared-memory record of one node or face node: the five fields packed
-// contiguously (plus two spare slots) so a record moves with 128-bit accesses.
-template <typename R>
-struct Slot {
-    static constexpr int W = 8;  // record width in elements of R
-};
-
-template <typename R>
-__device__ __forceinline__ void ld5(const R* p, R v[NSTATE]);
-template <>
-__device__ __forceinline__ void ld5<float>(const float* p, float v[NSTATE]) {
-    const float4 a = *reinterpret_cast<const float4*>(p);
-    v[0] = a.x;
-    v[1] = a.y;
-    v[2] = a.z;
-    v[3] = a.w;
-    v[4] = p[4];
-}
-template <>
-__device__ __forceinline__ void ld5<double>(const double* p, double v[NSTATE]) {
-    const double2 a = *reinterpret_cast<const double2*>(p);
-    const double2 b = *reinterpret_cast<const double2*>(p + 2);
-    v[0] = a.x;
-    v[1] = a.y;
-    v[2] = b.x;
-    v[3] = b.y;
-    v[4] = p[4];
-}
-template <typename R>
-__device__ __forceinline__ void st5(R* p, const R v[NSTATE]);
-template <>
-__device__ __forceinline__ void st5<float>(float* p, const float v[NSTATE]) {
-    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
-    p[4] = v[4];
-}
-template <>
-__device__ __forceinline__ void st5<double>(double* p, const double v[NSTATE]) {
-    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
-    *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
-    p[4] = v[4];
-}
 
 template <int N, typename R>
 struct Smem {
@@ -293,11 +77,25 @@ struct Smem {
     static constexpr size_t BYTES = sizeof(R) * TOTAL;
 };
 
-template <int N, typename R, bool MIXED, int MODE>
-__global__ void __launch_bounds__(Dims<N>::NT, MIXED ? Dims<N>::MIN_CTAS : 1) stage_kernel(const KParams P) {
+// Per-element inputs of one thread, loaded one element ahead (software
+// pipelining across the elements a persistent CTA visits).
+template <typename R>
+struct Ahead {
+    R q[NSTATE];   // own node state (node threads)
+    R qp[NSTATE];  // neighbour state at this thread's face node (face threads)
+    int nb;        // neighbour element across this thread's face, or -tag
+    int ez;        // vertical element index of the element
+};
+
+// PERSIST: a grid of resident CTAs walks the elements with the next element's
+// inputs fetched one element ahead; otherwise one CTA per element.
+template <int N, typename R, bool MIXED, int MODE, bool PERSIST>
+__global__ void __launch_bounds__(Dims<N>::NT, MIXED ? (PERSIST ? Dims<N>::MIN_CTAS : Dims<N>::MIN_CTAS_DIRECT)
+                                                     : Dims<N>::MIN_CTAS64) stage_kernel(const KParams P) {
     using Dm = Dims<N>;
     using SM = Smem<N, R>;
     constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, W = SM::W;
+    constexpr int ESTRIDE = NSTATE * Np;  // elements of R (or double) per element
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* const sm = reinterpret_cast<R*>(smem_raw);
     R* const s_node = sm + SM::NODE;
@@ -305,224 +103,259 @@ __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? Dims<N>::MIN_CTAS : 1) st
     R* const s_fs = sm + SM::FACE;
     R* const s_D = sm + SM::DMAT;
 
-    const int e = blockIdx.x;
     const int t = threadIdx.x;
-    const int ez = e % P.nz;
     const R* __restrict__ Qin = static_cast<const R*>(P.Qin);
+    R* __restrict__ Qout = static_cast<R*>(P.Qout);
     const Physics& ph = P.ph;
     const bool node_thread = t < Np;
     const bool face_thread = t < 6 * Nfp;
     const bool read_reg = (MODE == 0) ? (P.beta != 0) : !P.first_stage;
-    const size_t ebase = (size_t)e * NSTATE * Np;
 
-    // ---------------- issue every global load of this thread up front:
-    // own node state and RK register, then the neighbour state at this
-    // thread's face node (its latency overlaps the volume work below)
-    R q[NSTATE];
-    double dq_old[NSTATE];
-    if (node_thread) {
-#pragma unroll
-        for (int s = 0; s < NSTATE; ++s) q[s] = Qin[ebase + s * Np + t];
-        if (read_reg) {
-#pragma unroll
-            for (int s = 0; s < NSTATE; ++s) dq_old[s] = P.dQ[ebase + s * Np + t];
-        }
-    }
-    int f = 0, fn = 0, d = 0, vM = 0, nb = -1, levp = 0;
-    R qp[NSTATE];
-    if (face_thread) {
-        f = t / Nfp;
-        fn = t - f * Nfp;
-        const int fa = fn % Nq, fb = fn / Nq;
-        d = f >> 1;
-        vM = face_node<N>(f, fa, fb);
-        nb = P.nbr[6 * e + f];
-        if (nb >= 0) {
-            const int vP = face_node<N>(f ^ 1, fa, fb);
-            levp = (nb % P.nz) * Nq + vP / Nfp;
-            const size_t nbase = (size_t)nb * NSTATE * Np + vP;
-#pragma unroll
-            for (int s = 0; s < NSTATE; ++s) qp[s] = Qin[nbase + s * Np];
-        } else {
-            levp = ez * Nq + vM / Nfp;
-        }
-    }
+    // ---------------- element-independent per-thread geometry
+    // node thread: (i, j, k) and its three contraction lines
+    const int nk = node_thread ? t / Nfp : 0;
+    const int nj = node_thread ? (t - nk * Nfp) / Nq : 0;
+    const int ni = node_thread ? t - nk * Nfp - nj * Nq : 0;
+    // face thread: face f (0..5 = xi1-, xi1+, xi2-, xi2+, xi3-, xi3+), in-face node fn
+    const int f = face_thread ? t / Nfp : 0;
+    const int fn = face_thread ? t - f * Nfp : 0;
+    const int fd = f >> 1, fside = f & 1;
+    const int fa = fn % Nq, fb = fn / Nq;
+    // volume node on face f at in-face (a, b), and the matching node of the neighbour on face f^1
+    const int vM = fd == 0 ? fside * N + Nq * fn : (fd == 1 ? fa + Nq * (fside * N + Nq * fb) : fn + Nfp * (fside * N));
+    const int oside = fside ^ 1;
+    const int vP = fd == 0 ? oside * N + Nq * fn : (fd == 1 ? fa + Nq * (oside * N + Nq * fb) : fn + Nfp * (oside * N));
+    const int kM = vM / Nfp, kP = vP / Nfp;
+    const R sgn = fside ? R(1) : R(-1);
+
     if (t < Nq * Nq) s_D[t] = static_cast<const R*>(P.Dhat)[t];
-    const R xi[3] = {KConst<R>::metric(P, e, 0), KConst<R>::metric(P, e, 1), KConst<R>::metric(P, e, 2)};
 
-    // ---------------- phase 1: node thermodynamics and volume fluxes
-    R gsrc = 0;
-    if (node_thread) {
-        const Level<R> lv = load_level<R>(P, ez * Nq + t / Nfp);
-        const Thermo<R, MIXED> th = thermo<R, MIXED>(q, lv, P);
-        R* rec = s_node + t * W;
-        st5<R>(rec, q);
-        rec[5] = th.c;
-        rec[6] = th.rinv;
+    auto fetch = [&](int e, Ahead<R>& a) {
+        const int* nbr = P.nbr + NBR_STRIDE * e;
+        a.ez = __ldg(nbr + 6);
+        if (node_thread) {
+            const R* qe = Qin + (size_t)e * ESTRIDE + t;
 #pragma unroll
-        for (int dd = 0; dd < 3; ++dd) {
-            R F[NSTATE];
+            for (int s = 0; s < NSTATE; ++s) a.q[s] = qe[s * Np];
+        }
+        a.nb = face_thread ? __ldg(nbr + f) : -1;
+        if (a.nb >= 0) {
+            const R* qn = Qin + (size_t)a.nb * ESTRIDE + vP;
 #pragma unroll
-            for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(q, th, dd, s);
-            st5<R>(s_F + (dd * Np + t) * W, F);
+            for (int s = 0; s < NSTATE; ++s) a.qp[s] = qn[s * Np];
         }
-        if (ph.gravity) {
-            R rho_s = MIXED ? ((ph.ref_state && ph.subtract_off) ? q[0] : lv.rho_ref + q[0])
-                            : ((ph.ref_state && ph.subtract_off) ? q[0] - lv.rho_ref : q[0]);
-            gsrc = -rho_s * lv.gphiz;
-        }
-    }
-    __syncthreads();
+    };
 
-    // ---------------- phase 2: one numerical flux per face node
-    if (face_thread) {
-        const R sgn = (f & 1) ? R(1) : R(-1);
-        R qm[NSTATE], Fm[NSTATE], Fp[NSTATE], jr[NSTATE] = {0, 0, 0, 0, 0};
-        const R* rec = s_node + vM * W;
-        ld5<R>(rec, qm);
-        const R c_m = rec[5], ri_m = rec[6];
-        ld5<R>(s_F + (d * Np + vM) * W, Fm);
+    int e = blockIdx.x;
+    Ahead<R> cur;
+    if (e < P.nelem) fetch(e, cur);
+    for (; e < P.nelem; e += gridDim.x) {
+        // RK register of this element (consumed in phase 3), then next element's inputs
+        double dq_old[NSTATE];
+        const size_t ebase = (size_t)e * ESTRIDE + t;
+        if (node_thread && read_reg) {
 #pragma unroll
-        for (int s = 0; s < NSTATE; ++s) Fm[s] *= sgn;
-        const R lam_m = fabs(pick3(d, qm[1], qm[2], qm[3]) * ri_m) + c_m;
-        if (nb >= 0) {
-            if (MIXED && d == 2 && ph.numflux == CMDG_FLUX_RUSANOV) {
-                // reference-state jump q_ref(-) - q_ref(+) across a vertical face
-                if (f == 4) {
-                    jr[0] = (R)P.jump32[2 * ez + 0];
-                    jr[4] = (R)P.jump32[2 * ez + 1];
-                } else {
-                    const int ea = (ez + 1) % P.nz;
-                    jr[0] = -(R)P.jump32[2 * ea + 0];
-                    jr[4] = -(R)P.jump32[2 * ea + 1];
+            for (int s = 0; s < NSTATE; ++s) dq_old[s] = P.dQ[ebase + s * Np];
+        }
+        Ahead<R> nxt;
+        const int en = e + gridDim.x;
+        if (PERSIST && en < P.nelem) fetch(en, nxt);
+
+        const int ez = cur.ez;
+        const R xi[3] = {KConst<R>::metric(P, e, 0), KConst<R>::metric(P, e, 1), KConst<R>::metric(P, e, 2)};
+
+        // ---------------- phase 1: node thermodynamics and volume fluxes
+        R gsrc = 0;
+        if (node_thread) {
+            const Level<R> lv = load_level<R>(P, ez * Nq + nk);
+            const Thermo<R, MIXED> th = thermo<R, MIXED>(cur.q, lv, P);
+            R* rec = s_node + t * W;
+            st5<R>(rec, cur.q);
+            rec[5] = th.c;
+            rec[6] = th.rinv;
+#pragma unroll
+            for (int dd = 0; dd < 3; ++dd) {
+                R F[NSTATE];
+#pragma unroll
+                for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(cur.q, th, dd, s);
+                st5<R>(s_F + (dd * Np + t) * W, F);
+            }
+            if (ph.gravity) {
+                R rho_s = MIXED ? ((ph.ref_state && ph.subtract_off) ? cur.q[0] : lv.rho_ref + cur.q[0])
+                                : ((ph.ref_state && ph.subtract_off) ? cur.q[0] - lv.rho_ref : cur.q[0]);
+                gsrc = -rho_s * lv.gphiz;
+            }
+        }
+        __syncthreads();
+
+        // ---------------- phase 2: one numerical flux per face node
+        if (face_thread) {
+            R qm[NSTATE], Fm[NSTATE], Fp[NSTATE], qp[NSTATE], jr[NSTATE] = {0, 0, 0, 0, 0};
+            const R* rec = s_node + vM * W;
+            ld5<R>(rec, qm);
+            const R c_m = rec[5], ri_m = rec[6];
+            ld5<R>(s_F + (fd * Np + vM) * W, Fm);
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) Fm[s] *= sgn;
+            const R lam_m = fabs(pick3(fd, qm[1], qm[2], qm[3]) * ri_m) + c_m;
+            int ezp = ez;
+            if (cur.nb >= 0) {
+#pragma unroll
+                for (int s = 0; s < NSTATE; ++s) qp[s] = cur.qp[s];
+                if (fd == 2) {
+                    // vertical neighbour: one element below (f = 4) or above (f = 5), periodic wrap
+                    ezp = ez + (fside ? 1 : -1);
+                    ezp = ezp < 0 ? ezp + P.nz : (ezp >= P.nz ? ezp - P.nz : ezp);
+                    if (MIXED && ph.numflux == CMDG_FLUX_RUSANOV) {
+                        // reference-state jump q_ref(-) - q_ref(+) across the face
+                        const int ej = fside ? ezp : ez;
+                        const R sj = fside ? R(-1) : R(1);
+                        jr[0] = sj * (R)P.jump32[2 * ej + 0];
+                        jr[4] = sj * (R)P.jump32[2 * ej + 1];
+                    }
+                }
+            } else {
+                // Impenetrable(FreeSlip) + Insulating wall: rhou+ = rhou- - 2 (rhou-.n) n
+#pragma unroll
+                for (int s = 0; s < NSTATE; ++s) qp[s] = qm[s];
+                qp[1] = (fd == 0) ? -qm[1] : qm[1];
+                qp[2] = (fd == 1) ? -qm[2] : qm[2];
+                qp[3] = (fd == 2) ? -qm[3] : qm[3];
+            }
+            const Level<R> lvp = load_level<R>(P, ezp * Nq + (cur.nb >= 0 ? kP : kM));
+            const Thermo<R, MIXED> thp = thermo<R, MIXED>(qp, lvp, P);
+            normal_flux<R, MIXED>(qp, thp, fd, sgn, Fp);
+            const R lam_p = fabs(pick3(fd, thp.u[0], thp.u[1], thp.u[2])) + thp.c;
+            const R lift = pick3(fd, xi[0], xi[1], xi[2]) * KConst<R>::inv_w0(P);
+            const R hmw = (ph.numflux == CMDG_FLUX_RUSANOV) ? R(0.5) * fmax(lam_m, lam_p) : R(0);
+            const R hl = R(0.5) * lift, pl = hmw * lift;
+            R fs[NSTATE];
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) fs[s] = hl * (Fm[s] + Fp[s]) + pl * ((qm[s] - qp[s]) + jr[s]);
+            st5<R>(s_fs + (f * Nfp + fn) * W, fs);
+        }
+        __syncthreads();
+
+        // ---------------- phase 3: volume contraction, face terms, source, update
+        int bad = 0;
+        if (node_thread) {
+            R acc1[NSTATE] = {0, 0, 0, 0, 0}, acc2[NSTATE] = {0, 0, 0, 0, 0}, acc3[NSTATE] = {0, 0, 0, 0, 0};
+            const R* F1 = s_F + (0 * Np + Nq * (nj + Nq * nk)) * W;  // line along xi1
+            const R* F2 = s_F + (1 * Np + ni + Nfp * nk) * W;        // line along xi2 (stride Nq)
+            const R* F3 = s_F + (2 * Np + ni + Nq * nj) * W;         // line along xi3 (stride Nfp)
+#pragma unroll
+            for (int n = 0; n < Nq; ++n) {
+                R v1[NSTATE], v2[NSTATE], v3[NSTATE];
+                ld5<R>(F1 + n * W, v1);
+                ld5<R>(F2 + n * Nq * W, v2);
+                ld5<R>(F3 + n * Nfp * W, v3);
+                const R d1 = s_D[ni * Nq + n], d2 = s_D[nj * Nq + n], d3 = s_D[nk * Nq + n];
+#pragma unroll
+                for (int s = 0; s < NSTATE; ++s) {
+                    acc1[s] = fma(d1, v1[s], acc1[s]);
+                    acc2[s] = fma(d2, v2[s], acc2[s]);
+                    acc3[s] = fma(d3, v3[s], acc3[s]);
                 }
             }
-        } else {
-            // Impenetrable(FreeSlip) + Insulating wall: rhou+ = rhou- - 2 (rhou-.n) n
+            R rhs[NSTATE];
 #pragma unroll
-            for (int s = 0; s < NSTATE; ++s) qp[s] = qm[s];
-            qp[1] = (d == 0) ? -qm[1] : qm[1];
-            qp[2] = (d == 1) ? -qm[2] : qm[2];
-            qp[3] = (d == 2) ? -qm[3] : qm[3];
-        }
-        const Level<R> lvp = load_level<R>(P, levp);
-        const Thermo<R, MIXED> thp = thermo<R, MIXED>(qp, lvp, P);
-        normal_flux<R, MIXED>(qp, thp, d, sgn, Fp);
-        const R lam_p = fabs(pick3(d, thp.u[0], thp.u[1], thp.u[2])) + thp.c;
-        const R lift = pick3(d, xi[0], xi[1], xi[2]) * KConst<R>::inv_w0(P);
-        const R hmw = (ph.numflux == CMDG_FLUX_RUSANOV) ? R(0.5) * fmax(lam_m, lam_p) : R(0);
-        const R hl = R(0.5) * lift, pl = hmw * lift;
-        R fs[NSTATE];
-#pragma unroll
-        for (int s = 0; s < NSTATE; ++s) fs[s] = hl * (Fm[s] + Fp[s]) + pl * ((qm[s] - qp[s]) + jr[s]);
-        st5<R>(s_fs + (f * Nfp + fn) * W, fs);
-    }
-    __syncthreads();
-
-    // ---------------- phase 3: volume contraction, face terms, source, update
-    int bad = 0;
-    if (node_thread) {
-        const int i = t % Nq, j = (t / Nq) % Nq, k = t / Nfp;
-        R acc1[NSTATE] = {0, 0, 0, 0, 0}, acc2[NSTATE] = {0, 0, 0, 0, 0}, acc3[NSTATE] = {0, 0, 0, 0, 0};
-        const R* F1 = s_F + (0 * Np + Nq * (j + Nq * k)) * W;      // line along xi1
-        const R* F2 = s_F + (1 * Np + i + Nq * Nq * k) * W;        // line along xi2 (stride Nq)
-        const R* F3 = s_F + (2 * Np + i + Nq * j) * W;             // line along xi3 (stride Nfp)
-#pragma unroll
-        for (int n = 0; n < Nq; ++n) {
-            R v1[NSTATE], v2[NSTATE], v3[NSTATE];
-            ld5<R>(F1 + n * W, v1);
-            ld5<R>(F2 + n * Nq * W, v2);
-            ld5<R>(F3 + n * Nfp * W, v3);
-            const R d1 = s_D[i * Nq + n], d2 = s_D[j * Nq + n], d3 = s_D[k * Nq + n];
-#pragma unroll
-            for (int s = 0; s < NSTATE; ++s) {
-                acc1[s] = fma(d1, v1[s], acc1[s]);
-                acc2[s] = fma(d2, v2[s], acc2[s]);
-                acc3[s] = fma(d3, v3[s], acc3[s]);
-            }
-        }
-        R rhs[NSTATE];
-#pragma unroll
-        for (int s = 0; s < NSTATE; ++s) rhs[s] = xi[0] * acc1[s] + xi[1] * acc2[s] + xi[2] * acc3[s];
-        // face terms (vMI sM F*, lifted in phase 2), in face order 1..6
-        const int fidx[6] = {j + Nq * k, j + Nq * k, i + Nq * k, i + Nq * k, i + Nq * j, i + Nq * j};
-        const bool on[6] = {i == 0, i == N, j == 0, j == N, k == 0, k == N};
-#pragma unroll
-        for (int ff = 0; ff < 6; ++ff) {
-            if (on[ff]) {
+            for (int s = 0; s < NSTATE; ++s) rhs[s] = xi[0] * acc1[s] + xi[1] * acc2[s] + xi[2] * acc3[s];
+            // face terms (vMI sM F*, lifted in phase 2), in face order 1..6
+            auto sub_face = [&](int ff, int idx) {
                 R v[NSTATE];
-                ld5<R>(s_fs + (ff * Nfp + fidx[ff]) * W, v);
+                ld5<R>(s_fs + (ff * Nfp + idx) * W, v);
 #pragma unroll
                 for (int s = 0; s < NSTATE; ++s) rhs[s] -= v[s];
-            }
-        }
-        rhs[3] += gsrc;
-        const R rkb_dt = KConst<R>::rkb_dt(P);
-        R* Qout = static_cast<R*>(P.Qout);
+            };
+            if (ni == 0) sub_face(0, nj + Nq * nk);
+            if (ni == N) sub_face(1, nj + Nq * nk);
+            if (nj == 0) sub_face(2, ni + Nq * nk);
+            if (nj == N) sub_face(3, ni + Nq * nk);
+            if (nk == 0) sub_face(4, ni + Nq * nj);
+            if (nk == N) sub_face(5, ni + Nq * nj);
+            rhs[3] += gsrc;
+            const R rkb_dt = KConst<R>::rkb_dt(P);
 #pragma unroll
-        for (int s = 0; s < NSTATE; ++s) {
-            if (!isfinite(rhs[s])) bad = 1;
-            const size_t idx = ebase + s * Np + t;
-            if (MODE == 0) {
-                double out = P.alpha * (double)rhs[s];
-                if (read_reg) out = fma(P.beta, dq_old[s], out);
-                P.dQ[idx] = out;
-            } else {
-                // unscaled 2N register: dq_s = rhs_s + A_s dq_{s-1}  (A_1 = 0)
-                double dq;
-                if (MIXED) {
-                    // one FP64 FMA per DOF; the conversions run on the integer pipe
-                    if (read_reg) {
-                        dq = fma(P.rka, dq_old[s], f32_to_f64_bits((float)rhs[s]));
-                        Qout[idx] = fma(rkb_dt, (R)f64_to_f32_bits(dq), q[s]);
-                    } else {
-                        dq = f32_to_f64_bits((float)rhs[s]);
-                        Qout[idx] = fma(rkb_dt, rhs[s], q[s]);
-                    }
+            for (int s = 0; s < NSTATE; ++s) {
+                if (!isfinite(rhs[s])) bad = 1;
+                const size_t idx = ebase + s * Np;
+                if (MODE == 0) {
+                    double out = P.alpha * (double)rhs[s];
+                    if (read_reg) out = fma(P.beta, dq_old[s], out);
+                    P.dQ[idx] = out;
                 } else {
-                    dq = read_reg ? fma(P.rka, dq_old[s], (double)rhs[s]) : (double)rhs[s];
-                    Qout[idx] = (R)fma(P.rkb_dt, dq, (double)q[s]);
+                    // unscaled 2N register: dq_s = rhs_s + A_s dq_{s-1}  (A_1 = 0)
+                    double dq;
+                    if (MIXED) {
+                        // one FP64 FMA per DOF; the conversions run on the integer pipe
+                        if (read_reg) {
+                            dq = fma(P.rka, dq_old[s], f32_to_f64_bits((float)rhs[s]));
+                            Qout[idx] = fma(rkb_dt, (R)f64_to_f32_bits(dq), cur.q[s]);
+                        } else {
+                            dq = f32_to_f64_bits((float)rhs[s]);
+                            Qout[idx] = fma(rkb_dt, rhs[s], cur.q[s]);
+                        }
+                    } else {
+                        dq = read_reg ? fma(P.rka, dq_old[s], (double)rhs[s]) : (double)rhs[s];
+                        Qout[idx] = (R)fma(P.rkb_dt, dq, (double)cur.q[s]);
+                    }
+                    if (!P.last_stage) P.dQ[idx] = dq;
                 }
-                if (!P.last_stage) P.dQ[idx] = dq;
             }
         }
+        // also separates this element's shared-memory reads from the next one's writes
+        if (__syncthreads_or(bad) && t == 0) atomicOr(P.status, 1u);
+        if (!PERSIST) break;
+        cur = nxt;
     }
-    if (__syncthreads_or(bad) && t == 0) atomicOr(P.status, 1u);
 }
 
-template <int N, typename R, bool MIXED, int MODE>
-cudaError_t launch_mode(const KParams& P, cudaStream_t s) {
+template <int N, typename R, bool MIXED, int MODE, bool PERSIST>
+cudaError_t launch_mode(const KParams& P, int grid_ctas, cudaStream_t s) {
     constexpr size_t bytes = Smem<N, R>::BYTES;
-    if (bytes > 48 * 1024) {
-        // opt in to more than 48 KB of dynamic shared memory, once per device
-        static unsigned long long configured = 0;
-        int dev = 0;
-        cudaError_t e = cudaGetDevice(&dev);
-        if (e != cudaSuccess) return e;
-        if (!(configured & (1ull << (dev & 63)))) {
-            e = cudaFuncSetAttribute(stage_kernel<N, R, MIXED, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)bytes);
+    // per-device set-up: opt in to > 48 KB of dynamic shared memory and size a
+    // persistent grid from the occupancy of this instantiation
+    static int resident[64] = {0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    dev &= 63;
+    if (resident[dev] == 0) {
+        if (bytes > 48 * 1024) {
+            e = cudaFuncSetAttribute(stage_kernel<N, R, MIXED, MODE, PERSIST>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
             if (e != cudaSuccess) return e;
-            configured |= 1ull << (dev & 63);
         }
+        int per_sm = 0, sms = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stage_kernel<N, R, MIXED, MODE, PERSIST>,
+                                                          Dims<N>::NT, bytes);
+        if (e != cudaSuccess) return e;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        resident[dev] = (per_sm > 0 ? per_sm : 1) * sms;
     }
-    stage_kernel<N, R, MIXED, MODE><<<(unsigned)P.nelem, Dims<N>::NT, bytes, s>>>(P);
+    int grid = PERSIST ? (grid_ctas > 0 ? grid_ctas : resident[dev]) : P.nelem;
+    if (grid > P.nelem) grid = P.nelem;
+    stage_kernel<N, R, MIXED, MODE, PERSIST><<<(unsigned)grid, Dims<N>::NT, bytes, s>>>(P);
     return cudaGetLastError();
 }
 
 template <int N, typename R, bool MIXED>
-cudaError_t launch_typed(const KParams& P, int mode, cudaStream_t s) {
-    return mode == 0 ? launch_mode<N, R, MIXED, 0>(P, s) : launch_mode<N, R, MIXED, 1>(P, s);
+cudaError_t launch_typed(const KParams& P, int mode, int grid, cudaStream_t s) {
+    // grid < 0 selects one CTA per element; otherwise the persistent kernel
+    if (grid < 0)
+        return mode == 0 ? launch_mode<N, R, MIXED, 0, false>(P, 0, s) : launch_mode<N, R, MIXED, 1, false>(P, 0, s);
+    return mode == 0 ? launch_mode<N, R, MIXED, 0, true>(P, grid, s) : launch_mode<N, R, MIXED, 1, true>(P, grid, s);
 }
 
 template <int N>
-cudaError_t launch_N(const KParams& P, bool mixed, int mode, cudaStream_t s) {
-    return mixed ? launch_typed<N, float, true>(P, mode, s) : launch_typed<N, double, false>(P, mode, s);
+cudaError_t launch_N(const KParams& P, bool mixed, int mode, int grid, cudaStream_t s) {
+    return mixed ? launch_typed<N, float, true>(P, mode, grid, s) : launch_typed<N, double, false>(P, mode, grid, s);
 }
 
 }  // namespace
 
-int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
+KParams make_params(Model* md, const LaunchArgs& a) {
     const Mesh& m = *md->mesh;
     KParams P;
     P.Qin = a.Qin;
@@ -551,13 +384,27 @@ int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
     P.gm132 = (float)md->ph.gm1;
     P.gamma32 = (float)md->ph.gamma;
     P.ph = md->ph;
-    cudaError_t err;
-    switch (m.N) {
-        case 2: err = launch_N<2>(P, mixed, a.mode, s); break;
-        case 3: err = launch_N<3>(P, mixed, a.mode, s); break;
-        case 4: err = launch_N<4>(P, mixed, a.mode, s); break;
-        case 5: err = launch_N<5>(P, mixed, a.mode, s); break;
-        default: set_error("no kernel instantiated for N=%d", m.N); return CMDG_ERR_UNSUPPORTED;
+    for (int i = 0; i < (MAX_N + 1) * (MAX_N + 1); ++i) {
+        P.DhatC64[i] = i < (int)m.Dhat.size() ? m.Dhat[i] : 0.0;
+        P.DhatC32[i] = (float)P.DhatC64[i];
+    }
+    return P;
+}
+
+int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
+    const Mesh& m = *md->mesh;
+    const KParams P = make_params(md, a);
+    const bool mixed = md->precision == CMDG_MIXED;
+    cudaError_t err = cudaErrorNotSupported;
+    if (md->kernel_kind == KERNEL_COLUMN) err = launch_column(P, m.N, mixed, a.mode, md->grid_ctas, s);
+    if (err == cudaErrorNotSupported) {
+        switch (m.N) {
+            case 2: err = launch_N<2>(P, mixed, a.mode, md->grid_ctas, s); break;
+            case 3: err = launch_N<3>(P, mixed, a.mode, md->grid_ctas, s); break;
+            case 4: err = launch_N<4>(P, mixed, a.mode, md->grid_ctas, s); break;
+            case 5: err = launch_N<5>(P, mixed, a.mode, md->grid_ctas, s); break;
+            default: set_error("no kernel instantiated for N=%d", m.N); return CMDG_ERR_UNSUPPORTED;
+        }
     }
     if (err != cudaSuccess) {
         set_error("stage kernel launch failed: %s", cudaGetErrorString(err));

@@ -1,0 +1,129 @@
+// Launch-configuration selection for the fused stage kernels: explicit
+// setting, and a timing autotuner over the candidates of a model.
+#include <cstring>
+#include <vector>
+
+#include "cmdg_internal.h"
+
+namespace {
+
+struct Candidate {
+    int kind;
+    int grid;  // 0 = one wave of resident CTAs (persistent), n > 0 = n CTAs, -1 = one CTA per element
+};
+
+}  // namespace
+
+extern "C" int cmdg_model_set_kernel(cmdg_model* model, int kernel_kind, int grid_ctas) {
+    using namespace cmdg;
+    CMDG_ARG_CHECK(model != nullptr, "model is NULL");
+    CMDG_ARG_CHECK(kernel_kind == KERNEL_NODE || kernel_kind == KERNEL_COLUMN, "unknown kernel kind %d", kernel_kind);
+    CMDG_ARG_CHECK(grid_ctas >= -1, "grid_ctas must be >= -1");
+    model->m.kernel_kind = kernel_kind;
+    model->m.grid_ctas = grid_ctas;
+    // captured step graphs embed the old launch configuration
+    for (auto& kv : model->m.graphs) cudaGraphExecDestroy(kv.second);
+    model->m.graphs.clear();
+    return CMDG_OK;
+}
+
+extern "C" int cmdg_model_get_kernel(const cmdg_model* model, int* kernel_kind, int* grid_ctas) {
+    using namespace cmdg;
+    CMDG_ARG_CHECK(model != nullptr, "model is NULL");
+    if (kernel_kind) *kernel_kind = model->m.kernel_kind;
+    if (grid_ctas) *grid_ctas = model->m.grid_ctas;
+    return CMDG_OK;
+}
+
+extern "C" int cmdg_model_autotune(cmdg_model* model, int reps, double* h_ms, int h_ms_len, int* n_candidates,
+                                   void* stream) {
+    using namespace cmdg;
+    CMDG_ARG_CHECK(model != nullptr, "model is NULL");
+    CMDG_ARG_CHECK(reps >= 1 && reps <= 10000, "reps must be in [1, 10000]");
+    Model* md = &model->m;
+    const Mesh& m = *md->mesh;
+    const bool mixed = md->precision == CMDG_MIXED;
+    const size_t n = (size_t)m.nelem * NSTATE * m.Np;
+    const size_t elt = mixed ? sizeof(float) : sizeof(double);
+    cudaStream_t s = (cudaStream_t)stream;
+
+    // a physically valid scratch state: the reference state (zero perturbation)
+    std::vector<unsigned char> host(n * elt, 0);
+    if (!mixed) {
+        double* h = reinterpret_cast<double*>(host.data());
+        for (int64_t e = 0; e < m.nelem; ++e)
+            for (int node = 0; node < m.Np; ++node) {
+                const int lev = (int)(e % m.nz) * m.Nq + node / m.Nfp;
+                const double* L = &md->lvl64[(size_t)lev * LV_NFIELDS];
+                const bool ref = md->prm.ref_state != 0;
+                h[((size_t)e * NSTATE + 0) * m.Np + node] = ref ? L[LV_RHO_REF] : 1.0;
+                h[((size_t)e * NSTATE + 4) * m.Np + node] = ref ? L[LV_RHOE_REF] : 2.5e5;
+            }
+    }
+    void *Qa = nullptr, *Qb = nullptr;
+    double* dQ = nullptr;
+    int rc = CMDG_OK;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    const int saved_kind = md->kernel_kind, saved_grid = md->grid_ctas;
+    std::vector<Candidate> cands = {{KERNEL_NODE, 0}, {KERNEL_NODE, -1}};
+    if (mixed && m.N >= 3 && m.N <= 5) cands.push_back({KERNEL_COLUMN, 0});
+    std::vector<double> ms(cands.size(), 0.0);
+    auto fail = [&](cudaError_t e, const char* what) {
+        set_error("autotune: %s: %s", what, cudaGetErrorString(e));
+        rc = CMDG_ERR_CUDA;
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc(&Qa, n * elt)) != cudaSuccess) fail(e, "allocation");
+    if (!rc && (e = cudaMalloc(&Qb, n * elt)) != cudaSuccess) fail(e, "allocation");
+    if (!rc && (e = cudaMalloc((void**)&dQ, n * sizeof(double))) != cudaSuccess) fail(e, "allocation");
+    if (!rc && (e = cudaMemcpy(Qa, host.data(), n * elt, cudaMemcpyHostToDevice)) != cudaSuccess) fail(e, "copy");
+    if (!rc && (e = cudaMemset(dQ, 0, n * sizeof(double))) != cudaSuccess) fail(e, "memset");
+    if (!rc && (e = cudaEventCreate(&t0)) != cudaSuccess) fail(e, "event");
+    if (!rc && (e = cudaEventCreate(&t1)) != cudaSuccess) fail(e, "event");
+    for (size_t ci = 0; ci < cands.size() && !rc; ++ci) {
+        md->kernel_kind = cands[ci].kind;
+        md->grid_ctas = cands[ci].grid;
+        LaunchArgs a;
+        a.dQ = dQ;
+        a.alpha = a.beta = 1.0;
+        a.rka = 0.5;
+        a.rkb_dt = 0.0;  // the scratch state does not change
+        a.mode = 1;
+        a.first_stage = 0;
+        a.last_stage = 0;
+        for (int r = -2; r < reps && !rc; ++r) {
+            if (r == 0 && (e = cudaEventRecord(t0, s)) != cudaSuccess) fail(e, "event record");
+            a.Qin = (r & 1) ? Qb : Qa;
+            a.Qout = (r & 1) ? Qa : Qb;
+            rc = launch_stage(md, a, s);
+        }
+        if (rc) break;
+        if ((e = cudaEventRecord(t1, s)) != cudaSuccess) { fail(e, "event record"); break; }
+        if ((e = cudaEventSynchronize(t1)) != cudaSuccess) { fail(e, "event sync"); break; }
+        float elapsed = 0;
+        cudaEventElapsedTime(&elapsed, t0, t1);
+        ms[ci] = elapsed / reps;
+    }
+    if (t0) cudaEventDestroy(t0);
+    if (t1) cudaEventDestroy(t1);
+    if (Qa) cudaFree(Qa);
+    if (Qb) cudaFree(Qb);
+    if (dQ) cudaFree(dQ);
+    if (rc) {
+        md->kernel_kind = saved_kind;
+        md->grid_ctas = saved_grid;
+        return rc;
+    }
+    size_t best = 0;
+    for (size_t ci = 1; ci < cands.size(); ++ci)
+        if (ms[ci] < ms[best]) best = ci;
+    md->kernel_kind = cands[best].kind;
+    md->grid_ctas = cands[best].grid;
+    for (auto& kv : md->graphs) cudaGraphExecDestroy(kv.second);
+    md->graphs.clear();
+    if (n_candidates) *n_candidates = (int)cands.size();
+    for (int i = 0; h_ms && i < h_ms_len && i < (int)cands.size(); ++i) h_ms[i] = ms[i];
+    // the scratch runs may have flagged nothing; clear the word anyway
+    cudaMemsetAsync(md->d_status, 0, sizeof(unsigned), s);
+    return CMDG_OK;
+}

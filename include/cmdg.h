@@ -122,6 +122,28 @@ int cmdg_model_destroy(cmdg_model* model);
  * rho_ref, rhoe_ref, p_ref (aux.ref_state, src/Atmos/Model/ref_state.jl:66-67). */
 int cmdg_model_reference_state(const cmdg_model* model, double* h_ref);
 
+/* Stage-kernel family of a model: CMDG_KERNEL_NODE (one thread per node,
+ * all precisions) or CMDG_KERNEL_COLUMN (one thread per vertical line of
+ * nodes; mixed precision, N = 3..5; other models fall back to the node
+ * kernel).  For the node kernel, grid_ctas > 0 fixes the size of its
+ * persistent grid, 0 = one wave of resident CTAs, -1 = no persistence (one
+ * CTA per element).  No counterpart in the reference (the
+ * launch configuration of a KernelAbstractions kernel is fixed,
+ * src/Numerics/DGMethods/SpaceDiscretization.jl:1120-1133). */
+enum { CMDG_KERNEL_NODE = 0, CMDG_KERNEL_COLUMN = 1 };
+int cmdg_model_set_kernel(cmdg_model* model, int kernel_kind, int grid_ctas);
+int cmdg_model_get_kernel(const cmdg_model* model, int* kernel_kind, int* grid_ctas);
+
+/* Autotuner: times every (kernel family, grid) candidate of this model on a
+ * scratch copy of the reference state for `reps` stage launches each, keeps
+ * the fastest, and writes the number of candidates and their times (ms per
+ * stage, candidate order: node kernel with a persistent grid of one wave of
+ * resident CTAs, node kernel with one CTA per element, column kernel when the
+ * model has one) to h_ms (capacity h_ms_len).
+ * Allocates and frees two state-sized temporaries.  No counterpart in the
+ * reference. */
+int cmdg_model_autotune(cmdg_model* model, int reps, double* h_ms, int h_ms_len, int* n_candidates, void* stream);
+
 /* One tendency evaluation in FP64:
  *   d_dQ = alpha * dQ/dt(d_Q) + beta * d_dQ
  * Replaces (dg::DGModel)(tendency, Q, _, t, alpha, beta)
