@@ -25,7 +25,7 @@ EXPORTS = (
     "cmdg_model_reference_state", "cmdg_tendency", "cmdg_lsrk54_step", "cmdg_to_perturbation",
     "cmdg_from_perturbation", "cmdg_tendency_mixed", "cmdg_lsrk54_step_mixed", "cmdg_weighted_sums",
     "cmdg_weighted_sums_mixed", "cmdg_courant_dt", "cmdg_status_word", "cmdg_lsrk54_step_noalloc",
-    "cmdg_model_set_kernel", "cmdg_model_get_kernel", "cmdg_model_autotune",
+    "cmdg_model_set_kernel", "cmdg_model_get_kernel", "cmdg_model_autotune", "cmdg_gradient_flux",
 )
 
 
@@ -94,6 +94,7 @@ def load(path: str | None = None):
         "cmdg_model_set_kernel": [P, I, I],
         "cmdg_model_get_kernel": [P, ctypes.POINTER(I), ctypes.POINTER(I)],
         "cmdg_model_autotune": [P, I, P, I, ctypes.POINTER(I), P],
+        "cmdg_gradient_flux": [P, P, P, P],
     }
     for name, args in proto.items():
         fn = getattr(L, name)

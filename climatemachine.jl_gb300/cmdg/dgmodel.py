@@ -192,6 +192,12 @@ class DGModel:
         call("cmdg_courant_dt", self.h, _dptr(self.full_state(Q)), float(CFL), ctypes.byref(dt), _stream())
         return dt.value
 
+    def gradient_flux(self, Q) -> torch.Tensor:
+        """Gradient-flux state (nelem, 10, Np) of Q: grad h_tot, S, N^2."""
+        gf = torch.zeros((self.grid.nelem, 10, self.grid.Np), dtype=self.state_dtype, device=self.device)
+        call("cmdg_gradient_flux", self.h, _dptr(gf), _dptr(Q), _stream())
+        return gf
+
     def status_word(self) -> int:
         st = ctypes.c_uint32()
         call("cmdg_status_word", self.h, ctypes.byref(st), _stream())

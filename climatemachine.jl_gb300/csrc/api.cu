@@ -213,11 +213,11 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
     CMDG_ARG_CHECK(p->orientation == CMDG_ORIENT_NONE || p->orientation == CMDG_ORIENT_FLAT,
                    "orientation %d is not available on a brick", p->orientation);
     CMDG_ARG_CHECK(p->R_d > 0 && p->cv_d > 0 && p->cp_d > 0, "gas constants must be positive");
-    if (p->turbulence != CMDG_TURB_NONE) {
-        set_error("turbulence closure %d: the diffusive passes are not built into this library version",
-                  p->turbulence);
-        return CMDG_ERR_UNSUPPORTED;
-    }
+    CMDG_ARG_CHECK(p->turbulence == CMDG_TURB_NONE || p->turbulence == CMDG_TURB_CONSTANT ||
+                       p->turbulence == CMDG_TURB_SMAGORINSKY,
+                   "unknown turbulence closure %d", p->turbulence);
+    CMDG_ARG_CHECK(p->turbulence != CMDG_TURB_SMAGORINSKY || p->orientation == CMDG_ORIENT_FLAT,
+                   "SmagorinskyLilly needs an orientation (its buoyancy correction uses grad Phi)");
     cmdg_model* mo = new cmdg_model();
     Model& md = mo->m;
     md.mesh = &mesh->m;
@@ -235,7 +235,14 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
     md.ph.ref_state = p->ref_state;
     md.ph.subtract_off = p->subtract_off;
     md.ph.turbulence = p->turbulence;
+    md.ph.rho_nu = p->rho_nu;
+    md.ph.C_smag = p->C_smag;
+    md.ph.inv_Pr_turb = p->inv_Pr_turb;
+    md.ph.kappa = p->R_d / p->cp_d;
+    md.ph.MSLP = p->MSLP;
+    md.ph.with_divergence = p->with_divergence;
     int rc = init_model_tables(&md);
+    if (rc == CMDG_OK && p->turbulence != CMDG_TURB_NONE) rc = init_viscous_tables(&md);
     if (rc == CMDG_OK) {
         cudaError_t e = cudaMalloc(&md.d_status, sizeof(unsigned));
         if (e == cudaSuccess) e = cudaMemset(md.d_status, 0, sizeof(unsigned));
@@ -264,6 +271,9 @@ int cmdg_model_destroy(cmdg_model* model) {
     cudaFree(md.d_status);
     cudaFree(md.d_scratch);
     cudaFree(md.d_red);
+    cudaFree(md.d_lvv64);
+    cudaFree(md.d_lvv32);
+    cudaFree(md.d_gf);
     release_quad(&md);
     delete model;
     return CMDG_OK;
@@ -368,6 +378,14 @@ int cmdg_courant_dt(cmdg_model* model, const double* d_Q, double CFL, double* h_
     if (rc) return rc;
     CMDG_ARG_CHECK(d_Q && h_dt && CFL > 0, "bad arguments");
     return courant_dt(&model->m, d_Q, CFL, h_dt, (cudaStream_t)stream);
+}
+
+int cmdg_gradient_flux(cmdg_model* model, void* d_gf, const void* d_Q, void* stream) {
+    int rc = check_model(model);
+    if (rc) return rc;
+    CMDG_ARG_CHECK(d_gf != nullptr && d_Q != nullptr, "NULL buffer");
+    CMDG_ARG_CHECK(model->m.prm.turbulence != CMDG_TURB_NONE, "the model has no diffusive terms");
+    return launch_gradient(&model->m, d_Q, d_gf, (cudaStream_t)stream);
 }
 
 int cmdg_status_word(cmdg_model* model, uint32_t* h_status, void* stream) {

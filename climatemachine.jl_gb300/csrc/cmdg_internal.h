@@ -58,10 +58,30 @@ enum LevelField {
     LV_NFIELDS
 };
 
+// per vertical node level rows used by the diffusive passes (8 wide)
+enum ViscLevelField {
+    VV_THV_REF = 0,  // reference virtual potential temperature
+    VV_DTHV_REF,     // its DG derivative along z (volume + central face terms)
+    VV_HT_REF,       // reference total specific enthalpy (rhoe_ref + p_ref) / rho_ref
+    VV_DHT_REF,      // its DG derivative along z
+    VV_P_REF,        // reference pressure (duplicate of LV_P_REF, for the same row)
+    VV_RHO_REF,      // reference density
+    VV_PAD0,
+    VV_PAD1,
+    VV_NFIELDS
+};
+
+// gradient-flux words per node: grad h_tot (3), S = sym(grad u) (6), N^2 (Smagorinsky)
+constexpr int NGF = 10;
+
 // Physical constants in the form the kernels use them.
 struct Physics {
     double R_d, cv_d, gamma, gm1, T_0, grav, inv_cv;
     int numflux, gravity, ref_state, subtract_off, turbulence;
+    // diffusive terms (TurbulenceClosures.jl): rho*nu, WithDivergence, C_smag, 1/Pr_t,
+    // kappa = R_d/cp_d and MSLP for theta_v
+    double rho_nu, C_smag, inv_Pr_turb, kappa, MSLP;
+    int with_divergence;
 };
 
 struct Mesh {
@@ -110,6 +130,10 @@ struct Model {
     unsigned* d_status = nullptr;
     void* d_scratch = nullptr;       // two state-sized stage buffers (S1, S2) for the fused stage kernels
     size_t scratch_bytes = 0;
+    std::vector<double> lvv64;       // [nlev][VV_NFIELDS] diffusive-pass reference rows
+    double* d_lvv64 = nullptr;
+    float* d_lvv32 = nullptr;
+    void* d_gf = nullptr;            // gradient-flux state (Np, NGF, nelem) in the model's precision
     double* d_red = nullptr;         // reduction partials
     size_t red_len = 0;
     std::map<GraphKey, cudaGraphExec_t> graphs;
@@ -121,6 +145,7 @@ struct Model {
 int build_brick(const cmdg_brick_desc* desc, Mesh* m);
 void lgl_nodes(int N, std::vector<double>& x, std::vector<double>& w);
 int init_model_tables(Model* md);
+int init_viscous_tables(Model* md);
 
 // kernel launchers (stage.cu)
 struct LaunchArgs {
@@ -136,6 +161,11 @@ struct LaunchArgs {
 int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
 // LSRK54CarpenterKennedy A and B coefficient arrays (5 entries each)
 void lsrk54_coefficients(const double** A, const double** B);
+
+// diffusive passes (viscous.cu): gradient flux of Qin into md->d_gf, then the
+// stage kernel with second-order fluxes
+int launch_gradient(Model* md, const void* Qin, void* gf_out, cudaStream_t s);
+int launch_viscous_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
 
 // reductions / conversions (reduce.cu)
 int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s);

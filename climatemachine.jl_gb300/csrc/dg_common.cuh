@@ -31,6 +31,14 @@ struct KParams {
     // in the parameter bank so compile-time indexed reads cost no instruction
     float DhatC32[(MAX_N + 1) * (MAX_N + 1)];
     double DhatC64[(MAX_N + 1) * (MAX_N + 1)];
+    // diffusive passes: gradient-flux state, reference rows, strong-form D
+    // (D[j][k] = d l_k / d xi at xi_j), FP32 copies of the closure constants
+    void* gf;
+    const double* lvv64;
+    const float* lvv32;
+    float DC32[(MAX_N + 1) * (MAX_N + 1)];
+    double DC64[(MAX_N + 1) * (MAX_N + 1)];
+    float rho_nu32, C_smag32, inv_Pr32, kappa32, MSLP32, grav32;
 };
 
 // Builds the launch arguments of a model (stage.cu).

@@ -249,3 +249,69 @@ int init_model_tables(Model* md) {
 }
 
 }  // namespace cmdg
+
+namespace cmdg {
+
+// Reference-state rows of the diffusive passes: theta_v_ref, h_tot_ref and
+// their DG z-derivatives, volume D plus the central face terms of
+// dgsem_interface_gradients! (src/Numerics/DGMethods/DGModel_kernels.jl:1365-1651;
+// zero jump on walls, where the boundary state of the reference state equals it).
+int init_viscous_tables(Model* md) {
+    const Mesh& m = *md->mesh;
+    const cmdg_atmos_params& p = md->prm;
+    const int Nq = m.Nq, nz = m.nz, nlev = m.nlev, N = m.N;
+    md->lvv64.assign((size_t)nlev * VV_NFIELDS, 0.0);
+    auto V = [&](int lev, int f) -> double& { return md->lvv64[(size_t)lev * VV_NFIELDS + f]; };
+    auto L = [&](int lev, int f) { return md->lvl64[(size_t)lev * LV_NFIELDS + f]; };
+    const double kappa = p.R_d / p.cp_d;
+    std::vector<double> thv(nlev), ht(nlev);
+    for (int lev = 0; lev < nlev; ++lev) {
+        const double rho = L(lev, LV_RHO_REF), pr = L(lev, LV_P_REF);
+        if (p.ref_state && rho > 0) {
+            const double T = pr / (p.R_d * rho);
+            thv[lev] = T / std::pow(pr / p.MSLP, kappa);
+            ht[lev] = (L(lev, LV_RHOE_REF) + pr) / rho;
+        } else {
+            thv[lev] = 0.0;
+            ht[lev] = 0.0;
+        }
+        V(lev, VV_THV_REF) = thv[lev];
+        V(lev, VV_HT_REF) = ht[lev];
+        V(lev, VV_P_REF) = pr;
+        V(lev, VV_RHO_REF) = rho;
+    }
+    const double inv_w0 = 1.0 / m.omega[0];
+    auto ddz = [&](const std::vector<double>& f, int lev) {
+        const int ez = lev / Nq, k = lev % Nq;
+        double s = 0;
+        for (int n = 0; n < Nq; ++n) s += m.D[k * Nq + n] * f[ez * Nq + n];
+        double g = m.dzlev[lev] * s;
+        const double lift = m.dzlev[lev] * inv_w0;
+        if (k == 0) {  // bottom face, n_z = -1
+            int eb = ez - 1;
+            if (eb < 0) eb = m.desc.periodic[2] ? nz - 1 : -1;
+            if (eb >= 0) g += lift * (-1.0) * (f[eb * Nq + N] - f[lev]) * 0.5;
+        }
+        if (k == N) {  // top face, n_z = +1
+            int et = ez + 1;
+            if (et >= nz) et = m.desc.periodic[2] ? 0 : -1;
+            if (et >= 0) g += lift * (1.0) * (f[et * Nq + 0] - f[lev]) * 0.5;
+        }
+        return g;
+    };
+    for (int lev = 0; lev < nlev; ++lev) {
+        V(lev, VV_DTHV_REF) = ddz(thv, lev);
+        V(lev, VV_DHT_REF) = ddz(ht, lev);
+    }
+    std::vector<float> v32(md->lvv64.begin(), md->lvv64.end());
+    CMDG_CUDA_CHECK(cudaMalloc(&md->d_lvv64, sizeof(double) * md->lvv64.size()));
+    CMDG_CUDA_CHECK(cudaMalloc(&md->d_lvv32, sizeof(float) * v32.size()));
+    CMDG_CUDA_CHECK(cudaMemcpy(md->d_lvv64, md->lvv64.data(), sizeof(double) * md->lvv64.size(), cudaMemcpyHostToDevice));
+    CMDG_CUDA_CHECK(cudaMemcpy(md->d_lvv32, v32.data(), sizeof(float) * v32.size(), cudaMemcpyHostToDevice));
+    const size_t elt = md->precision == CMDG_MIXED ? sizeof(float) : sizeof(double);
+    CMDG_CUDA_CHECK(cudaMalloc(&md->d_gf, (size_t)m.nelem * NGF * m.Np * elt));
+    CMDG_CUDA_CHECK(cudaMemset(md->d_gf, 0, (size_t)m.nelem * NGF * m.Np * elt));
+    return CMDG_OK;
+}
+
+}  // namespace cmdg

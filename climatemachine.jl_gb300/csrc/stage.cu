@@ -387,12 +387,24 @@ KParams make_params(Model* md, const LaunchArgs& a) {
     for (int i = 0; i < (MAX_N + 1) * (MAX_N + 1); ++i) {
         P.DhatC64[i] = i < (int)m.Dhat.size() ? m.Dhat[i] : 0.0;
         P.DhatC32[i] = (float)P.DhatC64[i];
+        P.DC64[i] = i < (int)m.D.size() ? m.D[i] : 0.0;
+        P.DC32[i] = (float)P.DC64[i];
     }
+    P.gf = md->d_gf;
+    P.lvv64 = md->d_lvv64;
+    P.lvv32 = md->d_lvv32;
+    P.rho_nu32 = (float)md->ph.rho_nu;
+    P.C_smag32 = (float)md->ph.C_smag;
+    P.inv_Pr32 = (float)md->ph.inv_Pr_turb;
+    P.kappa32 = (float)md->ph.kappa;
+    P.MSLP32 = (float)md->ph.MSLP;
+    P.grav32 = (float)md->ph.grav;
     return P;
 }
 
 int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
     const Mesh& m = *md->mesh;
+    if (md->prm.turbulence != CMDG_TURB_NONE) return launch_viscous_stage(md, a, s);
     const KParams P = make_params(md, a);
     const bool mixed = md->precision == CMDG_MIXED;
     cudaError_t err = cudaErrorNotSupported;

@@ -206,6 +206,15 @@ int cmdg_weighted_sums_mixed(cmdg_model* model, const float* d_Qp, int nfields, 
  * src/Numerics/DGMethods/SpaceDiscretization.jl:307-365). */
 int cmdg_courant_dt(cmdg_model* model, const double* d_Q, double CFL, double* h_dt, void* stream);
 
+/* Gradient-flux state of d_Q (the diffusive pass that precedes every
+ * tendency of a model with a turbulence closure) into d_gf, column-major
+ * (Np, 10, nelem) in the model's precision: grad h_tot (3), S = sym(grad u)
+ * as S11, S21, S31, S22, S32, S33, and N^2 (zero for ConstantDynamicViscosity).
+ * Replaces launch_volume_gradients! + launch_interface_gradients! filling
+ * dg.state_gradient_flux (src/Numerics/DGMethods/SpaceDiscretization.jl:502-728,
+ * src/Numerics/DGMethods/DGModel.jl:132-230). */
+int cmdg_gradient_flux(cmdg_model* model, void* d_gf, const void* d_Q, void* stream);
+
 /* Device status word accumulated by the kernels since the last call
  * (bit 0: non-finite tendency seen); reading clears it.
  * Replaces checked_wait's error flag (src/Arrays/MPIStateArrays.jl:910-936). */

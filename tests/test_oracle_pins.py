@@ -73,3 +73,27 @@ def test_weightedsum_is_compensated():
     Q[:, 0, :] = 1.0
     # sum of M over the unit cube is its volume
     assert m.weightedsum(Q, 0) == pytest.approx(1.0, rel=1e-15)
+
+
+def test_viscous_shear_wave_decays_at_the_analytic_rate():
+    """Second-order fluxes of the oracle (ConstantDynamicViscosity): a shear
+    wave u = A sin(k z) in a uniform periodic box decays as exp(-nu k^2 t)."""
+    L, A, rho0, T0 = 1000.0, 0.5, 1.2, 300.0
+    nu = 50.0
+    m = O.OracleModel(4, (1, 1, 4), (0, 0, 0), (L, L, L), periodic=(1, 1, 1), turbulence="constant",
+                      rho_nu=rho0 * nu)
+    c = O.EARTH
+    z = m.aux[:, O.AUX["z"], :]
+    Q = m.state()
+    u = A * np.sin(2 * np.pi * z / L)
+    Q[:, 0] = rho0
+    Q[:, 1] = rho0 * u
+    Q[:, 4] = rho0 * (c["cv_d"] * (T0 - c["T_0"]) + 0.5 * u * u)
+    k = 2 * np.pi / L
+    tend = 20.0
+    dt = m.courant_dt(Q, 0.3)
+    m.solve(Q, dt, tend)
+    M = m.vgeo[:, O.VGEO["M"], :]
+    # projection of rho*u on sin(k z) over the box
+    amp = np.sum(M * Q[:, 1] * np.sin(k * z)) / np.sum(M * rho0 * np.sin(k * z) ** 2)
+    assert amp / A == pytest.approx(np.exp(-nu * k * k * tend), rel=2e-4)
