@@ -16,9 +16,10 @@ from .atmos import EARTH, AtmosModel, HydrostaticState, DryAdiabaticProfile, Iso
 from .dgmodel import DGModel, BrickGrid, euclidean_distance, weightedsum, norm
 from .odesolvers import LSRK54CarpenterKennedy, solve_, dostep_
 from ._lib import CmdgError, load as load_library
+from .ensemble import Ensemble
 
 __all__ = [
     "EARTH", "AtmosModel", "HydrostaticState", "DryAdiabaticProfile", "IsothermalProfile", "DGModel", "BrickGrid",
     "euclidean_distance", "weightedsum", "norm", "LSRK54CarpenterKennedy", "solve_", "dostep_", "CmdgError",
-    "load_library",
+    "load_library", "Ensemble",
 ]

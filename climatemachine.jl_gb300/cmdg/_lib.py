@@ -26,6 +26,8 @@ EXPORTS = (
     "cmdg_from_perturbation", "cmdg_tendency_mixed", "cmdg_lsrk54_step_mixed", "cmdg_weighted_sums",
     "cmdg_weighted_sums_mixed", "cmdg_courant_dt", "cmdg_status_word", "cmdg_lsrk54_step_noalloc",
     "cmdg_model_set_kernel", "cmdg_model_get_kernel", "cmdg_model_autotune", "cmdg_gradient_flux",
+    "cmdg_batch_create", "cmdg_batch_destroy", "cmdg_batch_set_tiling", "cmdg_batch_get_tiling",
+    "cmdg_batch_lsrk54_step", "cmdg_batch_autotune",
 )
 
 
@@ -95,6 +97,12 @@ def load(path: str | None = None):
         "cmdg_model_get_kernel": [P, ctypes.POINTER(I), ctypes.POINTER(I)],
         "cmdg_model_autotune": [P, I, P, I, ctypes.POINTER(I), P],
         "cmdg_gradient_flux": [P, P, P, P],
+        "cmdg_batch_create": [P, I, PP],
+        "cmdg_batch_destroy": [P],
+        "cmdg_batch_set_tiling": [P, I, I, I],
+        "cmdg_batch_get_tiling": [P, I, ctypes.POINTER(I), ctypes.POINTER(I)],
+        "cmdg_batch_lsrk54_step": [P, P, P, P, I, P],
+        "cmdg_batch_autotune": [P, P, P, I, P, I, ctypes.POINTER(I), P],
     }
     for name, args in proto.items():
         fn = getattr(L, name)

@@ -76,3 +76,25 @@ def bubble_model(ne=(20, 20, 20), N=4, L=2500.0, precision="fp64", numerical_flu
     model = AtmosModel(orientation="flat", gravity=True,
                        ref_state=HydrostaticState(DryAdiabaticProfile(300.0, 0.0), subtract_off=True))
     return DGModel(model, grid, numerical_flux=numerical_flux, precision=precision)
+
+
+def bubble_ensemble_specs(n=64, seed=2024, L=2500.0):
+    """Seeded members of the uneven rising-bubble ensemble: element counts per
+    direction U{8..16}, N in U{3, 4, 5}, amplitude U[0.5, 3] K, radius
+    U[150, 400] m, centred mid-domain 350 m above the bottom."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(n):
+        ne = tuple(int(x) for x in rng.integers(8, 17, size=3))
+        N = int(rng.integers(3, 6))
+        amp = float(rng.uniform(0.5, 3.0))
+        rc = float(rng.uniform(150.0, 400.0))
+        specs.append(dict(ne=ne, N=N, amp=amp, rc=rc, center=(L / 2, L / 2, 350.0)))
+    return specs
+
+
+def bubble_member(spec, L=2500.0, precision="mixed"):
+    """Model and FP64 initial state of one ensemble member."""
+    dg = bubble_model(ne=spec["ne"], N=spec["N"], L=L, precision=precision)
+    Q0 = rising_bubble(dg.grid.coordinates(), amp=spec["amp"], rc=spec["rc"], center=spec["center"])
+    return dg, Q0

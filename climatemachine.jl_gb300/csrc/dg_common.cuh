@@ -41,6 +41,18 @@ struct KParams {
     float rho_nu32, C_smag32, inv_Pr32, kappa32, MSLP32, grav32;
 };
 
+// A run of consecutive elements [e0, e1) of ensemble member `member`, of
+// polynomial order N.
+struct BatchTile {
+    int member, e0, e1, N;
+};
+// Ensemble stage launch over the tiles of one polynomial order N (3..5) with
+// `grid` CTAs, and the number of CTAs of that order resident on the device
+// (stage.cu).
+cudaError_t launch_batch_stage(const KParams* d_params, const BatchTile* d_tiles, int ntiles, int N, int grid,
+                               cudaStream_t s);
+int batch_resident_ctas(int N);
+
 // Builds the launch arguments of a model (stage.cu).
 KParams make_params(Model* md, const LaunchArgs& a);
 // Column-kernel launcher (column.cu); returns cudaErrorNotSupported when no

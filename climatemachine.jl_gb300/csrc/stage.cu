@@ -89,14 +89,16 @@ struct Ahead {
 
 // PERSIST: a grid of resident CTAs walks the elements with the next element's
 // inputs fetched one element ahead; otherwise one CTA per element.
+// Processes elements e_first, e_first + e_stride, ... below e_end with the
+// whole CTA; with PERSIST the next element's inputs are fetched one element
+// ahead.  Ends with a barrier, so the shared memory may be reused at once.
 template <int N, typename R, bool MIXED, int MODE, bool PERSIST>
-__global__ void __launch_bounds__(Dims<N>::NT, MIXED ? (PERSIST ? Dims<N>::MIN_CTAS : Dims<N>::MIN_CTAS_DIRECT)
-                                                     : Dims<N>::MIN_CTAS64) stage_kernel(const KParams P) {
+__device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem_raw, int e_first, int e_stride,
+                                           int e_end) {
     using Dm = Dims<N>;
     using SM = Smem<N, R>;
     constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, W = SM::W;
     constexpr int ESTRIDE = NSTATE * Np;  // elements of R (or double) per element
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     R* const sm = reinterpret_cast<R*>(smem_raw);
     R* const s_node = sm + SM::NODE;
     R* const s_F = sm + SM::FLUX;
@@ -146,10 +148,11 @@ __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? (PERSIST ? Dims<N>::MIN_C
         }
     };
 
-    int e = blockIdx.x;
+    int e = e_first;
     Ahead<R> cur;
-    if (e < P.nelem) fetch(e, cur);
-    for (; e < P.nelem; e += gridDim.x) {
+    if (PERSIST && e < e_end) fetch(e, cur);
+    for (; e < e_end; e += e_stride) {
+        if (!PERSIST) fetch(e, cur);
         // RK register of this element (consumed in phase 3), then next element's inputs
         double dq_old[NSTATE];
         const size_t ebase = (size_t)e * ESTRIDE + t;
@@ -158,8 +161,8 @@ __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? (PERSIST ? Dims<N>::MIN_C
             for (int s = 0; s < NSTATE; ++s) dq_old[s] = P.dQ[ebase + s * Np];
         }
         Ahead<R> nxt;
-        const int en = e + gridDim.x;
-        if (PERSIST && en < P.nelem) fetch(en, nxt);
+        const int en = e + e_stride;
+        if (PERSIST && en < e_end) fetch(en, nxt);
 
         const int ez = cur.ez;
         const R xi[3] = {KConst<R>::metric(P, e, 0), KConst<R>::metric(P, e, 1), KConst<R>::metric(P, e, 2)};
@@ -305,9 +308,15 @@ __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? (PERSIST ? Dims<N>::MIN_C
         }
         // also separates this element's shared-memory reads from the next one's writes
         if (__syncthreads_or(bad) && t == 0) atomicOr(P.status, 1u);
-        if (!PERSIST) break;
-        cur = nxt;
+        if (PERSIST) cur = nxt;
     }
+}
+
+template <int N, typename R, bool MIXED, int MODE, bool PERSIST>
+__global__ void __launch_bounds__(Dims<N>::NT, MIXED ? (PERSIST ? Dims<N>::MIN_CTAS : Dims<N>::MIN_CTAS_DIRECT)
+                                                     : Dims<N>::MIN_CTAS64) stage_kernel(const KParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    stage_body<N, R, MIXED, MODE, PERSIST>(P, smem_raw, blockIdx.x, PERSIST ? gridDim.x : P.nelem, P.nelem);
 }
 
 template <int N, typename R, bool MIXED, int MODE, bool PERSIST>
@@ -351,6 +360,50 @@ cudaError_t launch_typed(const KParams& P, int mode, int grid, cudaStream_t s) {
 template <int N>
 cudaError_t launch_N(const KParams& P, bool mixed, int mode, int grid, cudaStream_t s) {
     return mixed ? launch_typed<N, float, true>(P, mode, grid, s) : launch_typed<N, double, false>(P, mode, grid, s);
+}
+
+// ---------------------------------------------------------------------------
+// Ensembles: one launch per stage and polynomial order advances every member
+// of that order.  The CTAs walk a list of tiles (runs of consecutive elements
+// of one member); each tile reads its member's launch parameters from global
+// memory and runs the node-kernel body with the CTA shape of its order.
+template <int N>
+__global__ void __launch_bounds__(Dims<N>::NT, Dims<N>::MIN_CTAS_DIRECT)
+    batch_stage_kernel(const KParams* __restrict__ params, const BatchTile* __restrict__ tiles, int ntiles) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    for (int it = blockIdx.x; it < ntiles; it += gridDim.x) {
+        const BatchTile T = tiles[it];
+        stage_body<N, float, true, 1, false>(params[T.member], smem_raw, T.e0, 1, T.e1);
+    }
+}
+
+template <int N>
+cudaError_t launch_batch_N(const KParams* d_params, const BatchTile* d_tiles, int ntiles, int grid, cudaStream_t s) {
+    constexpr size_t bytes = Smem<N, float>::BYTES;
+    static unsigned long long configured = 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (!(configured & (1ull << (dev & 63)))) {
+        e = cudaFuncSetAttribute(batch_stage_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e != cudaSuccess) return e;
+        configured |= 1ull << (dev & 63);
+    }
+    batch_stage_kernel<N><<<grid, Dims<N>::NT, bytes, s>>>(d_params, d_tiles, ntiles);
+    return cudaGetLastError();
+}
+
+template <int N>
+int resident_N() {
+    int dev = 0, per_sm = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    constexpr size_t bytes = Smem<N, float>::BYTES;
+    cudaFuncSetAttribute(batch_stage_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_stage_kernel<N>, Dims<N>::NT, bytes) !=
+        cudaSuccess)
+        return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    return per_sm * sms;
 }
 
 }  // namespace
@@ -423,6 +476,26 @@ int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
         return CMDG_ERR_CUDA;
     }
     return CMDG_OK;
+}
+
+cudaError_t launch_batch_stage(const KParams* d_params, const BatchTile* d_tiles, int ntiles, int N, int grid,
+                               cudaStream_t s) {
+    if (ntiles <= 0) return cudaSuccess;
+    switch (N) {
+        case 3: return launch_batch_N<3>(d_params, d_tiles, ntiles, grid, s);
+        case 4: return launch_batch_N<4>(d_params, d_tiles, ntiles, grid, s);
+        case 5: return launch_batch_N<5>(d_params, d_tiles, ntiles, grid, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+int batch_resident_ctas(int N) {
+    switch (N) {
+        case 3: return resident_N<3>();
+        case 4: return resident_N<4>();
+        case 5: return resident_N<5>();
+        default: return 0;
+    }
 }
 
 }  // namespace cmdg

@@ -173,6 +173,36 @@ int cmdg_lsrk54_step(cmdg_model* model, double* d_Q, double* d_dQ, double t, dou
 int cmdg_lsrk54_step_noalloc(cmdg_model* model, void* d_Q, double* d_dQ, double t, double dt, int nsteps,
                              void* stream);
 
+/* Ensembles.  A batch advances n mixed-precision, inviscid brick models of
+ * any sizes and polynomial orders N = 3..5 together.  Members are grouped by
+ * order; each LSRK54 stage of a group is one launch of a tile-walking kernel
+ * (a tile is a run of consecutive elements of one member), the groups' stage
+ * chains run on their own streams, and the steps of a call are captured in one
+ * CUDA graph (stream != NULL).  The batch owns two stage buffers per member.
+ * No counterpart in the reference (there, ensemble members are separate
+ * solver runs). */
+typedef struct cmdg_batch cmdg_batch;
+int cmdg_batch_create(cmdg_model* const* models, int n, cmdg_batch** out);
+int cmdg_batch_destroy(cmdg_batch* batch);
+/* Tiling of the members of order N (0 = every order): tile_elems elements per
+ * tile; grid_ctas -1 = one CTA per tile, 0 = one wave of resident CTAs,
+ * n > 0 = n CTAs. */
+int cmdg_batch_set_tiling(cmdg_batch* batch, int N, int tile_elems, int grid_ctas);
+int cmdg_batch_get_tiling(const cmdg_batch* batch, int N, int* tile_elems, int* grid_ctas);
+/* nsteps LSRK54 steps of every member; h_Q, h_dQ, h_dt: host arrays of n
+ * device state pointers (FP32 perturbations), n device RK registers and n
+ * time steps.  Same per-member semantics as cmdg_lsrk54_step_mixed. */
+int cmdg_batch_lsrk54_step(cmdg_batch* batch, void* const* h_Q, double* const* h_dQ, const double* h_dt, int nsteps,
+                           void* stream);
+/* Autotuner, per order over tile_elems {1, 2, 4, 8, 16} x grid {one CTA per
+ * tile, one wave of resident CTAs}: times `reps` stage launches each on
+ * copies of the members' states (the states are not changed; the RK
+ * registers are overwritten, which the next step ignores), keeps each order's
+ * fastest, and writes ms per stage launch to h_ms as [order 3, 4, 5][candidate]
+ * (0 for an order without members). */
+int cmdg_batch_autotune(cmdg_batch* batch, void* const* h_Q, double* const* h_dQ, int reps, double* h_ms,
+                        int h_ms_len, int* n_candidates, void* stream);
+
 /* Mixed precision: converts an FP64 state to the FP32 perturbation
  * q' = q - q_ref (the subtraction is done in FP64) and back.
  * No counterpart in the reference (the reference state lives in aux.ref_state,

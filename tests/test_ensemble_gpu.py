@@ -1,0 +1,102 @@
+"""Ensembles: the batch kernel advances members of uneven size and order as
+the single-model kernel does (the same per-element arithmetic), the
+graph-captured steps repeat, every tiling gives bitwise-equal results, and a
+member stays within 1e-5 of the FP64 oracle."""
+import numpy as np
+import pytest
+import torch
+
+import cmdg
+import oracle as O
+from cmdg import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import __graft_entry__ as g
+
+    g.build()
+    torch.cuda.set_device(0)
+
+
+def members(n=5, seed=3):
+    specs = workloads.bubble_ensemble_specs(n=n, seed=seed)
+    # small members keep the test quick, orders 3, 4 and 5 all present
+    for i, s in enumerate(specs):
+        s["ne"] = (2 + i % 3, 3, 2 + (i * 7) % 4)
+        s["N"] = 3 + i % 3
+    return specs
+
+
+def test_ensemble_matches_single_model_steps():
+    specs = members()
+    pairs = [workloads.bubble_member(s) for s in specs]
+    dgs = [p[0] for p in pairs]
+    dts = [0.6 * dg.courant_dt(dg.init_ode_state(Q0), 0.4) for dg, Q0 in pairs]
+    # sequential reference: the same node-kernel body, one CTA per element
+    ref = []
+    for (dg, Q0), dt in zip(pairs, dts):
+        dg.set_kernel("node", -1)
+        Q = dg.init_ode_state(Q0)
+        lsrk = cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt)
+        cmdg.dostep_(Q, lsrk, None, 0.0, nsteps=3)
+        ref.append(Q.cpu().numpy())
+    ens = cmdg.Ensemble(dgs)
+    Qs = [dg.init_ode_state(Q0) for dg, Q0 in pairs]
+    dQs = [torch.zeros(Q.shape, dtype=torch.float64, device="cuda") for Q in Qs]
+    ens.lsrk54_step(Qs, dQs, dts, nsteps=1)
+    ens.lsrk54_step(Qs, dQs, dts, nsteps=2)  # a second graph
+    # the same FP32 element arithmetic: equal up to the compiler's FMA
+    # contraction choices in the two kernels' instantiations
+    for Q, r in zip(Qs, ref):
+        got = Q.cpu().numpy()
+        scale = np.abs(r).max(axis=(0, 2), keepdims=True)
+        assert (np.abs(got - r) <= 1e-6 * scale).all()
+    assert all(dg.status_word() == 0 for dg in dgs)
+
+
+def test_ensemble_autotune_and_tilings_keep_results():
+    """Every tiling runs the same kernel per order, so results are bitwise equal."""
+    specs = members(n=4, seed=9)
+    pairs = [workloads.bubble_member(s) for s in specs]
+    dgs = [p[0] for p in pairs]
+    dts = [0.5 * dg.courant_dt(dg.init_ode_state(Q0), 0.4) for dg, Q0 in pairs]
+    outs = []
+    for tiling in [(1, -1), (4, 0), (16, 7), None]:
+        ens = cmdg.Ensemble(dgs)
+        Qs = [dg.init_ode_state(Q0) for dg, Q0 in pairs]
+        dQs = [torch.zeros(Q.shape, dtype=torch.float64, device="cuda") for Q in Qs]
+        if tiling is None:
+            ms, choice = ens.autotune(Qs, dQs, reps=2)
+            for N in (3, 4, 5):
+                assert len(ms[N]) == 10 and all(m > 0 for m in ms[N])
+                assert choice[N][0] in (1, 2, 4, 8, 16) and choice[N][1] in (-1, 0)
+        else:
+            ens.set_tiling(*tiling)
+            assert ens.get_tiling()[4] == tiling
+        ens.lsrk54_step(Qs, dQs, dts, nsteps=2)
+        outs.append([Q.cpu().numpy() for Q in Qs])
+    for other in outs[1:]:
+        for a, b in zip(outs[0], other):
+            assert np.array_equal(a, b)
+    assert all(dg.status_word() == 0 for dg in dgs)
+
+
+def test_ensemble_member_close_to_fp64_oracle():
+    spec = dict(ne=(3, 3, 3), N=4, amp=2.5, rc=700.0, center=(1250.0, 1250.0, 900.0))
+    dg, Q0 = workloads.bubble_member(spec)
+    L = 2500.0
+    om = O.OracleModel(4, spec["ne"], (0, 0, 0), (L, L, L), periodic=(1, 1, 0), orientation="flat", gravity=True,
+                       ref_state=True, profile="dry_adiabatic", T_surface=300.0, T_min=0.0)
+    dt = om.courant_dt(Q0, 0.4)
+    Qo, _ = om.lsrk54(Q0.copy(), dt, 50)
+    ens = cmdg.Ensemble([dg])
+    Q = dg.init_ode_state(Q0)
+    dQ = torch.zeros(Q.shape, dtype=torch.float64, device="cuda")
+    ens.lsrk54_step([Q], [dQ], [dt], nsteps=50)
+    err, ref = om.field_l2(dg.from_perturbation(Q).cpu().numpy(), Qo)
+    err = np.array([err[0], np.sqrt(np.sum(err[1:4] ** 2)), err[4]])
+    ref = np.array([ref[0], np.sqrt(np.sum(ref[1:4] ** 2)), ref[4]])
+    assert (err / ref < 1e-5).all(), err / ref
