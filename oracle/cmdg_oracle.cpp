@@ -2,17 +2,20 @@
 //
 // A plain-C++ FP64 restatement of ClimateMachine.jl's DG spectral-element
 // tendency for the dry AtmosModel (DGModel volume/interface kernels, gradient
-// and diffusive passes), its LSRK54CarpenterKennedy integrator, the brick
-// geometry it runs on and the weighted reductions used to report errors.
+// and diffusive passes), its LSRK54CarpenterKennedy integrator, the brick and
+// stacked cubed-shell geometry it runs on and the weighted reductions used to
+// report errors.
 //
 // It is the checker for the CUDA library: only tests/, __graft_entry__.smoke()
 // and bench.py's CPU-baseline leg may load it.  Nothing in the product path
 // links, loads or calls this file.
 //
 // Parity status: pinned.  The isentropic-vortex golden errors of
-// test/Numerics/DGMethods/Euler/isentropicvortex.jl:105-106 and the LSRK54
+// test/Numerics/DGMethods/Euler/isentropicvortex.jl:105-106, the LSRK54
 // convergence order of test/Numerics/ODESolvers/ode_tests_convergence.jl:41
-// are reproduced by tests/test_oracle_pins.py.
+// and the discrete hydrostatic balance of
+// test/Atmos/Model/discrete_hydrostatic_balance.jl (LES brick and GCM cubed
+// shell) are reproduced by tests/test_oracle_pins.py.
 //
 // Every function cites the reference file:line (paths relative to the
 // ClimateMachine.jl project root) whose algorithm it restates.  Third-party
@@ -37,6 +40,8 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <stdexcept>
 #include <vector>
 
 #ifdef _OPENMP
@@ -60,7 +65,8 @@ typedef struct {
     // CLIMAParameters.jl 0.2.0 planet / SGS constants
     double R_d, cp_d, cv_d, T_0, grav, MSLP, inv_Pr_turb;
     int numflux;        // 0 = Rusanov (NumericalFluxes.jl:219-285), 1 = central (:298-340)
-    int orientation;    // 0 = NoOrientation, 1 = FlatOrientation (Orientations.jl:138-150, 246-258)
+    int orientation;    // 0 = NoOrientation, 1 = FlatOrientation, 2 = SphericalOrientation
+                        // (Orientations.jl:138-150, 246-258, 161-175)
     int gravity;        // 1 = Gravity() source (tendencies_momentum.jl:60-72)
     int ref_state;      // 0 = NoReferenceState, 1 = HydrostaticState (ref_state.jl:36-60)
     int subtract_off;   // HydrostaticState.subtract_off
@@ -71,7 +77,20 @@ typedef struct {
     double rho_nu;      // dynamic viscosity for turbulence==1
     int with_divergence;// WithDivergence for turbulence==1
     double C_smag;      // Smagorinsky coefficient for turbulence==2
+    double planet_radius; // SphericalOrientation: Phi = g (|x| - planet_radius)
 } om_params;
+
+// StackedCubedSphereTopology (Topologies.jl:1620-1760) over a
+// CubedShellTopology (Topologies.jl:1067-1240) with the equiangular warp
+// (Topologies.jl:1254-1305); radial element edges grid1d(r_inner, r_outer,
+// nelem = nvert) (Topologies.jl:2001).
+typedef struct {
+    int N;
+    int nhorz;                // elements per cube-face edge
+    int nvert;                // elements per stack
+    double r_inner, r_outer;
+    int bc_inner, bc_outer;   // boundary tags (> 0)
+} om_shell;
 
 }  // extern "C"
 
@@ -86,7 +105,9 @@ enum { AX = 0, AY, AZ, APHI, AGPX, AGPY, AGPZ, ARHO_REF, AP_REF, AT_REF, ARHOE_R
 constexpr int NS = 5;   // rho, rhou(3), rhoe
 
 struct Model {
+    int kind = 0;                            // 0 = brick, 1 = stacked cubed shell
     om_brick mesh;
+    om_shell shell;
     om_params prm;
     int N, Nq, Np, Nfp;
     int64_t nelem;
@@ -205,73 +226,26 @@ int64_t elem_index(const om_brick& b, int ix, int iy, int iz) {
     return (int64_t)iz + (int64_t)b.ne[2] * ((int64_t)ix + (int64_t)b.ne[0] * iy);
 }
 
-void build_geometry(Model& m) {
-    const om_brick& b = m.mesh;
+void alloc_geometry(Model& m) {
+    m.vgeo.assign((size_t)m.nelem * NVGEO * m.Np, 0.0);
+    m.sgeo.assign((size_t)m.nelem * 6 * m.Nfp * NSGEO, 0.0);
+    m.vmapM.assign((size_t)m.nelem * 6 * m.Nfp, 0);
+    m.vmapP.assign((size_t)m.nelem * 6 * m.Nfp, 0);
+    m.elemtobndy.assign((size_t)m.nelem * 6, 0);
+    m.elemtoelem.assign((size_t)m.nelem * 6, 0);
+}
+
+// Node coordinates of element e from its 8 corners (trilinear blend,
+// Metrics.jl:85-121), an optional mesh warp applied node by node
+// (Grids.jl:1050-1056), then dx/dxi (Metrics.jl:215-270), the curl-invariant
+// metric terms, J, normals and surface Jacobian (Metrics.jl:431-724) and
+// M, MI, sM, vMI (Grids.jl:1068-1096).
+void element_geometry(Model& m, int64_t e, const double c[3][8], void (*warp)(double&, double&, double&)) {
     int N = m.N, Nq = m.Nq, Np = m.Np, Nfp = m.Nfp;
-    int64_t nelem = m.nelem;
-    m.vgeo.assign((size_t)nelem * NVGEO * Np, 0.0);
-    m.sgeo.assign((size_t)nelem * 6 * Nfp * NSGEO, 0.0);
-    m.vmapM.assign((size_t)nelem * 6 * Nfp, 0);
-    m.vmapP.assign((size_t)nelem * 6 * Nfp, 0);
-    m.elemtobndy.assign((size_t)nelem * 6, 0);
-    m.elemtoelem.assign((size_t)nelem * 6, 0);
     std::vector<std::vector<int>> fmask;
     face_masks(Nq, fmask);
     const std::vector<double>& xi = m.xi;
-
-    // connectivity
-    for (int iy = 0; iy < b.ne[1]; ++iy)
-        for (int ix = 0; ix < b.ne[0]; ++ix)
-            for (int iz = 0; iz < b.ne[2]; ++iz) {
-                int64_t e = elem_index(b, ix, iy, iz);
-                int idx[3] = {ix, iy, iz};
-                for (int f = 0; f < 6; ++f) {
-                    int d = f / 2, side = f % 2;
-                    int nb[3] = {idx[0], idx[1], idx[2]};
-                    nb[d] += side ? 1 : -1;
-                    int64_t e2 = e;
-                    int f2 = f;
-                    int tag = 0;
-                    if (nb[d] < 0 || nb[d] >= b.ne[d]) {
-                        if (b.periodic[d]) {
-                            nb[d] = (nb[d] + b.ne[d]) % b.ne[d];
-                            e2 = elem_index(b, nb[0], nb[1], nb[2]);
-                            f2 = f ^ 1;
-                        } else {
-                            tag = side ? b.bc_hi[d] : b.bc_lo[d];
-                            if (tag <= 0) tag = 1;
-                        }
-                    } else {
-                        e2 = elem_index(b, nb[0], nb[1], nb[2]);
-                        f2 = f ^ 1;
-                    }
-                    m.elemtobndy[e * 6 + f] = tag;
-                    m.elemtoelem[e * 6 + f] = e2;
-                    for (int n = 0; n < Nfp; ++n) {
-                        m.vmapM[(e * 6 + f) * Nfp + n] = e * Np + fmask[f][n];
-                        m.vmapP[(e * 6 + f) * Nfp + n] = e2 * Np + fmask[f2][n];
-                    }
-                }
-            }
-
-    std::vector<double> xg[3];
-    for (int d = 0; d < 3; ++d) {
-        xg[d].resize(b.ne[d] + 1);
-        for (int i = 0; i <= b.ne[d]; ++i) xg[d][i] = range_value(b.lo[d], b.hi[d], b.ne[d], i);
-    }
-
-#pragma omp parallel for schedule(static)
-    for (int64_t e = 0; e < nelem; ++e) {
-        int64_t iz = e % b.ne[2];
-        int64_t ix = (e / b.ne[2]) % b.ne[0];
-        int64_t iy = e / ((int64_t)b.ne[2] * b.ne[0]);
-        double c[3][8];
-        for (int v = 0; v < 8; ++v) {
-            int bi = v & 1, bj = (v >> 1) & 1, bk = (v >> 2) & 1;
-            c[0][v] = xg[0][ix + bi];
-            c[1][v] = xg[1][iy + bj];
-            c[2][v] = xg[2][iz + bk];
-        }
+    {
         std::vector<double> X[3], Xr[3][3];
         for (int d = 0; d < 3; ++d) {
             X[d].assign(Np, 0.0);
@@ -290,6 +264,8 @@ void build_geometry(Model& m) {
                              b1 * b2 * a3 * c[d][3] + a1 * a2 * b3 * c[d][4] + b1 * a2 * b3 * c[d][5] +
                              a1 * b2 * b3 * c[d][6] + b1 * b2 * b3 * c[d][7]) / 8;
                     }
+        if (warp)
+            for (int n = 0; n < Np; ++n) warp(X[0][n], X[1][n], X[2][n]);
         // dx/dxi, Metrics.jl:246-266
         for (int k = 0; k < Nq; ++k)
             for (int j = 0; j < Nq; ++j)
@@ -390,6 +366,207 @@ void build_geometry(Model& m) {
                     SG(m, e, f, n, SSM) *= m.omega[a] * m.omega[bb];
                 }
         (void)N;
+    }
+}
+
+
+void build_geometry(Model& m) {
+    const om_brick& b = m.mesh;
+    int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp;
+    int64_t nelem = m.nelem;
+    alloc_geometry(m);
+    std::vector<std::vector<int>> fmask;
+    face_masks(Nq, fmask);
+
+    // connectivity
+    for (int iy = 0; iy < b.ne[1]; ++iy)
+        for (int ix = 0; ix < b.ne[0]; ++ix)
+            for (int iz = 0; iz < b.ne[2]; ++iz) {
+                int64_t e = elem_index(b, ix, iy, iz);
+                int idx[3] = {ix, iy, iz};
+                for (int f = 0; f < 6; ++f) {
+                    int d = f / 2, side = f % 2;
+                    int nb[3] = {idx[0], idx[1], idx[2]};
+                    nb[d] += side ? 1 : -1;
+                    int64_t e2 = e;
+                    int f2 = f;
+                    int tag = 0;
+                    if (nb[d] < 0 || nb[d] >= b.ne[d]) {
+                        if (b.periodic[d]) {
+                            nb[d] = (nb[d] + b.ne[d]) % b.ne[d];
+                            e2 = elem_index(b, nb[0], nb[1], nb[2]);
+                            f2 = f ^ 1;
+                        } else {
+                            tag = side ? b.bc_hi[d] : b.bc_lo[d];
+                            if (tag <= 0) tag = 1;
+                        }
+                    } else {
+                        e2 = elem_index(b, nb[0], nb[1], nb[2]);
+                        f2 = f ^ 1;
+                    }
+                    m.elemtobndy[e * 6 + f] = tag;
+                    m.elemtoelem[e * 6 + f] = e2;
+                    for (int n = 0; n < Nfp; ++n) {
+                        m.vmapM[(e * 6 + f) * Nfp + n] = e * Np + fmask[f][n];
+                        m.vmapP[(e * 6 + f) * Nfp + n] = e2 * Np + fmask[f2][n];
+                    }
+                }
+            }
+
+    std::vector<double> xg[3];
+    for (int d = 0; d < 3; ++d) {
+        xg[d].resize(b.ne[d] + 1);
+        for (int i = 0; i <= b.ne[d]; ++i) xg[d][i] = range_value(b.lo[d], b.hi[d], b.ne[d], i);
+    }
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < nelem; ++e) {
+        int64_t iz = e % b.ne[2];
+        int64_t ix = (e / b.ne[2]) % b.ne[0];
+        int64_t iy = e / ((int64_t)b.ne[2] * b.ne[0]);
+        double c[3][8];
+        for (int v = 0; v < 8; ++v) {
+            int bi = v & 1, bj = (v >> 1) & 1, bk = (v >> 2) & 1;
+            c[0][v] = xg[0][ix + bi];
+            c[1][v] = xg[1][iy + bj];
+            c[2][v] = xg[2][iz + bk];
+        }
+        element_geometry(m, e, c, nullptr);
+    }
+}
+
+// Equiangular cubed-sphere warp, Topologies.jl:1265-1305 (Ronchi, Iacono and
+// Paolucci 1996): a point (a, b, c) on the cube of half-width
+// R = max(|a|, |b|, |c|) goes to the sphere of radius R; the face is the
+// first coordinate of largest magnitude.
+void equiangular_warp(double& a, double& b, double& c) {
+    const double R = std::max(std::max(std::fabs(a), std::fabs(b)), std::fabs(c));
+    auto f = [](double sR, double xi, double eta, double& z1, double& z2, double& z3) {
+        const double X = std::tan(M_PI * xi / 4), Y = std::tan(M_PI * eta / 4);
+        z1 = sR / std::sqrt(X * X + Y * Y + 1);
+        z2 = X * z1;
+        z3 = Y * z1;
+    };
+    const double A = std::fabs(a), B = std::fabs(b), C = std::fabs(c);
+    const int fdim = (A >= B && A >= C) ? 1 : (B >= C ? 2 : 3);
+    double x1, x2, x3;
+    if (fdim == 1 && a < 0) f(-R, b / a, c / a, x1, x2, x3);
+    else if (fdim == 2 && b < 0) f(-R, a / b, c / b, x2, x1, x3);
+    else if (fdim == 1 && a > 0) f(R, b / a, c / a, x1, x2, x3);
+    else if (fdim == 2 && b > 0) f(R, a / b, c / b, x2, x1, x3);
+    else if (fdim == 3 && c > 0) f(R, b / c, a / c, x3, x2, x1);
+    else f(-R, b / c, a / c, x3, x2, x1);
+    a = x1;
+    b = x2;
+    c = x3;
+}
+
+// Stacked cubed shell.  Base elements follow cubedshellmesh (Topologies.jl:
+// 1150-1240): CartesianIndices((Ne, Ne, 6)), the six blocks of the developed
+// net mapped onto the faces of the cube [-1, 1]^3 by their vertex lattice
+// points; stacks are contiguous, element e = iz + nvert * h (Topologies.jl:
+// 1680-1700; the reference's space-filling-curve renumbering is a
+// permutation and is not applied).  Lower corners are the base vertices times
+// r_j, upper corners times r_{j+1}.  Horizontal neighbours share two lattice
+// vertices; face-node maps vmapP match node coordinates (the reference builds
+// the same map from elemtoordr, Grids.jl:559-638).
+void build_shell_geometry(Model& m) {
+    const om_shell& sh = m.shell;
+    const int Ne = sh.nhorz, nv = sh.nvert, Nq = m.Nq, Np = m.Np, Nfp = m.Nfp;
+    alloc_geometry(m);
+    std::vector<std::vector<int>> fmask;
+    face_masks(Nq, fmask);
+    const int64_t nbase = 6LL * Ne * Ne;
+    // lattice vertex ids and cube coordinates of the 4 base vertices
+    std::vector<int64_t> bvert(nbase * 4);
+    std::vector<double> bcoord(nbase * 4 * 3);
+    for (int64_t h = 0; h < nbase; ++h) {
+        const int i = (int)(h % Ne) + 1, j = (int)((h / Ne) % Ne) + 1, blck = (int)(h / ((int64_t)Ne * Ne)) + 1;
+        for (int n = 1; n <= 4; ++n) {
+            const int ix = i + (n - 1) % 2, jx = j + (n - 1) / 2;
+            int L[3];
+            switch (blck) {
+                case 1: L[0] = 1; L[1] = Ne + 2 - ix; L[2] = jx; break;
+                case 2: L[0] = ix; L[1] = 1; L[2] = jx; break;
+                case 3: L[0] = Ne + 1; L[1] = ix; L[2] = jx; break;
+                case 4: L[0] = ix; L[1] = jx; L[2] = Ne + 1; break;
+                case 5: L[0] = ix; L[1] = Ne + 1; L[2] = Ne + 2 - jx; break;
+                default: L[0] = ix; L[1] = Ne + 2 - jx; L[2] = 1; break;
+            }
+            bvert[h * 4 + n - 1] = (L[0] - 1) + (int64_t)(Ne + 1) * ((L[1] - 1) + (int64_t)(Ne + 1) * (L[2] - 1));
+            for (int d = 0; d < 3; ++d) bcoord[(h * 4 + n - 1) * 3 + d] = (double)(2 * (L[d] - 1) - Ne) / Ne;
+        }
+    }
+    std::vector<double> rr(nv + 1);
+    for (int k = 0; k <= nv; ++k) rr[k] = range_value(sh.r_inner, sh.r_outer, nv, k);
+    // horizontal neighbours: base faces 1..4 are vertex pairs (1,3), (2,4), (1,2), (3,4)
+    const int fv[4][2] = {{0, 2}, {1, 3}, {0, 1}, {2, 3}};
+    std::map<std::pair<int64_t, int64_t>, std::vector<std::pair<int64_t, int>>> edges;
+    for (int64_t h = 0; h < nbase; ++h)
+        for (int f = 0; f < 4; ++f) {
+            int64_t a = bvert[h * 4 + fv[f][0]], b = bvert[h * 4 + fv[f][1]];
+            edges[{std::min(a, b), std::max(a, b)}].push_back({h, f});
+        }
+    std::vector<int64_t> hn(nbase * 4);
+    std::vector<int> hf(nbase * 4);
+    for (auto& kv : edges) {
+        if (kv.second.size() != 2) throw std::runtime_error("cubed shell: an edge without exactly two elements");
+        auto a = kv.second[0], b = kv.second[1];
+        hn[a.first * 4 + a.second] = b.first; hf[a.first * 4 + a.second] = b.second;
+        hn[b.first * 4 + b.second] = a.first; hf[b.first * 4 + b.second] = a.second;
+    }
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m.nelem; ++e) {
+        const int64_t h = e / nv;
+        const int iz = (int)(e % nv);
+        double c[3][8];
+        for (int v = 0; v < 4; ++v)
+            for (int d = 0; d < 3; ++d) {
+                c[d][v] = bcoord[(h * 4 + v) * 3 + d] * rr[iz];
+                c[d][4 + v] = bcoord[(h * 4 + v) * 3 + d] * rr[iz + 1];
+            }
+        element_geometry(m, e, c, equiangular_warp);
+    }
+    for (int64_t e = 0; e < m.nelem; ++e) {
+        const int64_t h = e / nv;
+        const int iz = (int)(e % nv);
+        for (int f = 0; f < 6; ++f) {
+            int64_t e2 = e;
+            int f2 = f, tag = 0;
+            if (f < 4) {
+                e2 = hn[h * 4 + f] * nv + iz;
+                f2 = hf[h * 4 + f];
+            } else if (f == 4) {
+                if (iz == 0) tag = sh.bc_inner > 0 ? sh.bc_inner : 1;
+                else { e2 = e - 1; f2 = 5; }
+            } else {
+                if (iz == nv - 1) tag = sh.bc_outer > 0 ? sh.bc_outer : 1;
+                else { e2 = e + 1; f2 = 4; }
+            }
+            m.elemtobndy[e * 6 + f] = tag;
+            m.elemtoelem[e * 6 + f] = e2;
+            for (int n = 0; n < Nfp; ++n) {
+                const int vM = fmask[f][n];
+                m.vmapM[(e * 6 + f) * Nfp + n] = e * Np + vM;
+                if (tag) {
+                    m.vmapP[(e * 6 + f) * Nfp + n] = e * Np + vM;
+                    continue;
+                }
+                // the neighbour's face node at the same physical point
+                double best = INFINITY;
+                int vb = -1;
+                for (int n2 = 0; n2 < Nfp; ++n2) {
+                    const int v2 = fmask[f2][n2];
+                    double d2 = 0;
+                    for (int d = 0; d < 3; ++d) {
+                        const double dx = VGc(m, e, VX1 + d, vM) - VGc(m, e2, VX1 + d, v2);
+                        d2 += dx * dx;
+                    }
+                    if (d2 < best) { best = d2; vb = v2; }
+                }
+                if (best > 1e-16 * sh.r_outer * sh.r_outer) throw std::runtime_error("cubed shell: unmatched face node");
+                m.vmapP[(e * 6 + f) * Nfp + n] = e2 * Np + vb;
+            }
+        }
     }
 }
 
@@ -536,10 +713,18 @@ void init_aux(Model& m) {
             AUX(m, e, AY, n) = VG(m, e, VX2, n);
             AUX(m, e, AZ, n) = VG(m, e, VX3, n);
         }
-    // Orientation: Phi = g z (Orientations.jl:246-258), grad Phi by DG
-    if (p.orientation == 1) {
+    // Orientation: Phi = g z (FlatOrientation, Orientations.jl:246-258) or
+    // g (|x| - planet_radius) (SphericalOrientation, :161-175), grad Phi by DG
+    if (p.orientation == 1 || p.orientation == 2) {
         for (int64_t e = 0; e < m.nelem; ++e)
-            for (int n = 0; n < Np; ++n) AUX(m, e, APHI, n) = p.grav * AUX(m, e, AZ, n);
+            for (int n = 0; n < Np; ++n) {
+                if (p.orientation == 1) {
+                    AUX(m, e, APHI, n) = p.grav * AUX(m, e, AZ, n);
+                } else {
+                    const double x = AUX(m, e, AX, n), y = AUX(m, e, AY, n), z = AUX(m, e, AZ, n);
+                    AUX(m, e, APHI, n) = p.grav * (std::sqrt(x * x + y * y + z * z) - p.planet_radius);
+                }
+            }
         aux_field_gradient(m, APHI, AGPX);
     }
     // Hydrostatic reference state (ref_state.jl:143-185)
@@ -1007,6 +1192,30 @@ om_model* om_create(const om_brick* b, const om_params* p) {
     lgl(m->N, m->xi, m->omega);
     spectral_derivative(m->xi, m->D);
     build_geometry(*m);
+    init_aux(*m);
+    return m;
+}
+
+om_model* om_create_shell(const om_shell* sh, const om_params* p) {
+    Model* m = new Model();
+    m->kind = 1;
+    m->shell = *sh;
+    std::memset(&m->mesh, 0, sizeof(m->mesh));
+    m->prm = *p;
+    m->N = sh->N;
+    m->Nq = sh->N + 1;
+    m->Np = m->Nq * m->Nq * m->Nq;
+    m->Nfp = m->Nq * m->Nq;
+    m->nelem = 6LL * sh->nhorz * sh->nhorz * sh->nvert;
+    m->ngf = p->turbulence == 2 ? 10 : 9;
+    lgl(m->N, m->xi, m->omega);
+    spectral_derivative(m->xi, m->D);
+    try {
+        build_shell_geometry(*m);
+    } catch (const std::exception&) {
+        delete m;
+        return nullptr;
+    }
     init_aux(*m);
     return m;
 }

@@ -71,6 +71,19 @@ class Params(ctypes.Structure):
         ("rho_nu", ctypes.c_double),
         ("with_divergence", ctypes.c_int),
         ("C_smag", ctypes.c_double),
+        ("planet_radius", ctypes.c_double),
+    ]
+
+
+class Shell(ctypes.Structure):
+    _fields_ = [
+        ("N", ctypes.c_int),
+        ("nhorz", ctypes.c_int),
+        ("nvert", ctypes.c_int),
+        ("r_inner", ctypes.c_double),
+        ("r_outer", ctypes.c_double),
+        ("bc_inner", ctypes.c_int),
+        ("bc_outer", ctypes.c_int),
     ]
 
 
@@ -95,6 +108,8 @@ def lib():
         dp = ctypes.POINTER(ctypes.c_double)
         L.om_create.restype = P
         L.om_create.argtypes = [ctypes.POINTER(Brick), ctypes.POINTER(Params)]
+        L.om_create_shell.restype = P
+        L.om_create_shell.argtypes = [ctypes.POINTER(Shell), ctypes.POINTER(Params)]
         L.om_free.argtypes = [P]
         L.om_nelem.restype = ctypes.c_int64
         L.om_nelem.argtypes = [P]
@@ -151,23 +166,18 @@ VGEO = dict(xi1x1=0, xi2x1=1, xi3x1=2, xi1x2=3, xi2x2=4, xi3x2=5, xi1x3=6, xi2x3
 class OracleModel:
     """A brick mesh + dry AtmosModel configuration evaluated by the oracle."""
 
-    def __init__(self, N, ne, lo, hi, periodic=(1, 1, 1), bc_lo=(1, 1, 1), bc_hi=(2, 2, 2), **physics):
-        b = Brick()
-        b.N = N
-        for d in range(3):
-            b.ne[d] = ne[d]
-            b.lo[d] = lo[d]
-            b.hi[d] = hi[d]
-            b.periodic[d] = int(periodic[d])
-            b.bc_lo[d] = bc_lo[d]
-            b.bc_hi[d] = bc_hi[d]
+    def __init__(self, N, ne=None, lo=None, hi=None, periodic=(1, 1, 1), bc_lo=(1, 1, 1), bc_hi=(2, 2, 2),
+                 shell=None, **physics):
+        """Brick (N, ne, lo, hi, periodic, bc_lo, bc_hi) or, with
+        ``shell=dict(nhorz, nvert, r_inner, r_outer)``, a stacked
+        equiangular cubed shell with walls at both radii."""
         p = Params()
         consts = dict(EARTH)
         consts.update({k: v for k, v in physics.items() if k in EARTH})
-        for k in ("R_d", "cp_d", "cv_d", "T_0", "grav", "MSLP", "inv_Pr_turb"):
+        for k in ("R_d", "cp_d", "cv_d", "T_0", "grav", "MSLP", "inv_Pr_turb", "planet_radius"):
             setattr(p, k, consts[k])
         p.numflux = {"rusanov": 0, "central": 1}[physics.get("numflux", "rusanov")]
-        p.orientation = {"none": 0, "flat": 1}[physics.get("orientation", "none")]
+        p.orientation = {"none": 0, "flat": 1, "sphere": 2}[physics.get("orientation", "none")]
         p.gravity = int(physics.get("gravity", False))
         p.ref_state = int(physics.get("ref_state", False))
         p.subtract_off = int(physics.get("subtract_off", True))
@@ -178,9 +188,33 @@ class OracleModel:
         p.rho_nu = physics.get("rho_nu", 0.0)
         p.with_divergence = int(physics.get("with_divergence", False))
         p.C_smag = physics.get("C_smag", consts["C_smag"])
-        self.brick, self.params, self.consts = b, p, consts
+        self.params, self.consts = p, consts
         self.L = lib()
-        self.h = self.L.om_create(ctypes.byref(b), ctypes.byref(p))
+        if shell is None:
+            b = Brick()
+            b.N = N
+            for d in range(3):
+                b.ne[d] = ne[d]
+                b.lo[d] = lo[d]
+                b.hi[d] = hi[d]
+                b.periodic[d] = int(periodic[d])
+                b.bc_lo[d] = bc_lo[d]
+                b.bc_hi[d] = bc_hi[d]
+            self.brick = b
+            self.h = self.L.om_create(ctypes.byref(b), ctypes.byref(p))
+        else:
+            sh = Shell()
+            sh.N = N
+            sh.nhorz = shell["nhorz"]
+            sh.nvert = shell["nvert"]
+            sh.r_inner = shell["r_inner"]
+            sh.r_outer = shell["r_outer"]
+            sh.bc_inner = shell.get("bc_inner", 1)
+            sh.bc_outer = shell.get("bc_outer", 2)
+            self.shell = sh
+            self.h = self.L.om_create_shell(ctypes.byref(sh), ctypes.byref(p))
+            if not self.h:
+                raise RuntimeError("oracle: cubed-shell construction failed")
         self.N = N
         self.Nq = N + 1
         self.Np = self.L.om_Np(self.h)
