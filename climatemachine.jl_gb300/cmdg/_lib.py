@@ -20,7 +20,7 @@ CMDG_FP64, CMDG_MIXED = 0, 1
 
 # Every exported symbol of include/cmdg.h (checked by the CPU test suite).
 EXPORTS = (
-    "cmdg_last_error", "cmdg_version", "cmdg_mesh_create_brick", "cmdg_mesh_destroy", "cmdg_mesh_info",
+    "cmdg_last_error", "cmdg_version", "cmdg_mesh_create_brick", "cmdg_mesh_create_shell", "cmdg_mesh_destroy", "cmdg_mesh_info",
     "cmdg_mesh_coordinates", "cmdg_mesh_mass", "cmdg_model_create", "cmdg_model_destroy",
     "cmdg_model_reference_state", "cmdg_tendency", "cmdg_lsrk54_step", "cmdg_to_perturbation",
     "cmdg_from_perturbation", "cmdg_tendency_mixed", "cmdg_lsrk54_step_mixed", "cmdg_weighted_sums",
@@ -52,7 +52,12 @@ class AtmosParams(ctypes.Structure):
                 ("gravity", ctypes.c_int), ("ref_state", ctypes.c_int), ("subtract_off", ctypes.c_int),
                 ("profile", ctypes.c_int), ("T_surface", ctypes.c_double), ("T_min", ctypes.c_double),
                 ("turbulence", ctypes.c_int), ("rho_nu", ctypes.c_double), ("with_divergence", ctypes.c_int),
-                ("C_smag", ctypes.c_double)]
+                ("C_smag", ctypes.c_double), ("planet_radius", ctypes.c_double)]
+
+
+class ShellDesc(ctypes.Structure):
+    _fields_ = [("N", ctypes.c_int), ("nhorz", ctypes.c_int), ("nvert", ctypes.c_int), ("r_inner", ctypes.c_double),
+                ("r_outer", ctypes.c_double), ("bc_inner", ctypes.c_int), ("bc_outer", ctypes.c_int)]
 
 
 _lib = None
@@ -75,6 +80,7 @@ def load(path: str | None = None):
     L.cmdg_version.restype = ctypes.c_char_p
     proto = {
         "cmdg_mesh_create_brick": [ctypes.POINTER(BrickDesc), PP],
+        "cmdg_mesh_create_shell": [ctypes.POINTER(ShellDesc), PP],
         "cmdg_mesh_destroy": [P],
         "cmdg_mesh_info": [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int)],
         "cmdg_mesh_coordinates": [P, P],

@@ -44,7 +44,7 @@ class HydrostaticState:
 
 @dataclass
 class AtmosModel:
-    orientation: str = "none"            # "none" | "flat"
+    orientation: str = "none"            # "none" | "flat" | "sphere"
     ref_state: HydrostaticState | None = None
     gravity: bool = False                # source = (Gravity(),)
     turbulence: str = "none"             # "none" | "constant" | "smagorinsky"
@@ -55,10 +55,10 @@ class AtmosModel:
 
     def c_params(self, numerical_flux: str) -> AtmosParams:
         p = AtmosParams()
-        for k in ("R_d", "cp_d", "cv_d", "T_0", "grav", "MSLP", "inv_Pr_turb"):
+        for k in ("R_d", "cp_d", "cv_d", "T_0", "grav", "MSLP", "inv_Pr_turb", "planet_radius"):
             setattr(p, k, float(self.constants[k]))
         p.numflux = {"rusanov": 0, "central": 1}[numerical_flux]
-        p.orientation = {"none": 0, "flat": 1}[self.orientation]
+        p.orientation = {"none": 0, "flat": 1, "sphere": 2}[self.orientation]
         p.gravity = int(self.gravity)
         rs = self.ref_state
         p.ref_state = int(rs is not None)

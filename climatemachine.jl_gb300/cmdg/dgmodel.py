@@ -17,7 +17,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import AtmosParams, BrickDesc, call
+from ._lib import AtmosParams, BrickDesc, ShellDesc, call
 
 NSTATE = 5
 
@@ -67,6 +67,12 @@ class BrickGrid:
             _lib._lib.cmdg_mesh_destroy(self.h)
             self.h = None
 
+    def _sizes(self):
+        nelem = ctypes.c_int64()
+        Np = ctypes.c_int()
+        call("cmdg_mesh_info", self.h, ctypes.byref(nelem), ctypes.byref(Np))
+        return nelem.value, Np.value
+
     def coordinates(self) -> np.ndarray:
         xyz = np.empty((self.nelem, 3, self.Np), dtype=np.float64)
         call("cmdg_mesh_coordinates", self.h, ctypes.c_void_p(xyz.ctypes.data))
@@ -76,6 +82,31 @@ class BrickGrid:
         M = np.empty((self.nelem, self.Np), dtype=np.float64)
         call("cmdg_mesh_mass", self.h, ctypes.c_void_p(M.ctypes.data))
         return M
+
+
+class CubedShellGrid(BrickGrid):
+    """StackedCubedSphereTopology(nhorz, grid1d(r_inner, r_outer, nelem=nvert);
+    boundary=(1, 2)) + DiscontinuousSpectralElementGrid(meshwarp =
+    equiangular_cubed_sphere_warp) (src/Numerics/Mesh/Topologies.jl:1067-1305,
+    1620-1760; src/Numerics/Mesh/Grids.jl:1028-1110), as
+    AtmosGCMConfiguration builds it (src/Driver/driver_configs.jl:344-420).
+
+    Columns are contiguous: element e = iz + nvert * h.
+    """
+
+    def __init__(self, N, nhorz, nvert, r_inner, r_outer, boundary=(1, 2)):
+        _lib.load()
+        d = ShellDesc()
+        d.N, d.nhorz, d.nvert = int(N), int(nhorz), int(nvert)
+        d.r_inner, d.r_outer = float(r_inner), float(r_outer)
+        d.bc_inner, d.bc_outer = int(boundary[0]), int(boundary[1])
+        h = ctypes.c_void_p()
+        call("cmdg_mesh_create_shell", ctypes.byref(d), ctypes.byref(h))
+        self.h = h
+        self.desc = d
+        self.nelem, self.Np = self._sizes()
+        self.N, self.Nq = int(N), int(N) + 1
+        self.ne = (6 * int(nhorz) * int(nhorz), 1, int(nvert))
 
 
 class DGModel:

@@ -11,6 +11,8 @@ nodes in the same way, src/Numerics/DGMethods/SpaceDiscretization.jl:79-148).
   (dry-adiabatic) hydrostatic background of potential temperature theta0,
   with a cos^2 bump of amplitude A and radius rc centred at (xc, yc, zc)
   (the structure of experiments/TestCase/risingbubble.jl:23-91).
+* ``gcm_initial_state``: isothermal hydrostatic atmosphere on the cubed shell
+  with a seeded zonal wind and a Gaussian temperature anomaly.
 """
 from __future__ import annotations
 
@@ -18,8 +20,8 @@ import math
 
 import numpy as np
 
-from .atmos import EARTH, AtmosModel, DryAdiabaticProfile, HydrostaticState
-from .dgmodel import BrickGrid, DGModel
+from .atmos import EARTH, AtmosModel, DryAdiabaticProfile, HydrostaticState, IsothermalProfile
+from .dgmodel import BrickGrid, CubedShellGrid, DGModel
 
 
 def isentropic_vortex(xyz: np.ndarray, t: float = 0.0, *, p_inf=1e5, T_inf=300.0, translation_speed=150.0,
@@ -98,3 +100,52 @@ def bubble_member(spec, L=2500.0, precision="mixed"):
     dg = bubble_model(ne=spec["ne"], N=spec["N"], L=L, precision=precision)
     Q0 = rising_bubble(dg.grid.coordinates(), amp=spec["amp"], rc=spec["rc"], center=spec["center"])
     return dg, Q0
+
+
+def gcm_shell_model(nhorz=12, nvert=6, N=4, H=30e3, precision="fp64", numerical_flux="rusanov", T_ref=285.0,
+                    subtract_off=True):
+    """Dry shallow-atmosphere GCM on the stacked equiangular cubed shell:
+    6 x nhorz^2 columns of nvert elements between the planet radius and a lid
+    H above it, walls at both (AtmosGCMConfiguration's boundary = (1, 2)),
+    SphericalOrientation + Gravity, HydrostaticState(IsothermalProfile(T_ref)),
+    inviscid."""
+    R = EARTH["planet_radius"]
+    grid = CubedShellGrid(N, nhorz, nvert, R, R + H)
+    model = AtmosModel(orientation="sphere", gravity=True,
+                       ref_state=HydrostaticState(IsothermalProfile(T_ref), subtract_off=subtract_off))
+    return DGModel(model, grid, numerical_flux=numerical_flux, precision=precision)
+
+
+def gcm_initial_state(xyz: np.ndarray, *, seed=2024, T_ref=285.0, u_max=30.0, dT=1.0, radius=1.0e6, z_c=10e3,
+                      z_w=5e3, consts=EARTH) -> np.ndarray:
+    """Isothermal (T_ref) hydrostatic atmosphere with a seeded zonal wind and a
+    Gaussian temperature anomaly, evaluated at the nodes.
+
+    Wind: u_zonal = u_max cos(lat) (1 + sin(k lon + phase)) / 2 (0 .. u_max),
+    k in {1, 2, 3} and phase from the seed, along the local east vector.
+    Anomaly: dT exp(-(d / radius)^2 - ((z - z_c) / z_w)^2) with d the
+    great-circle distance to a seeded centre.  The pressure keeps the
+    hydrostatic profile p = MSLP exp(-g z / (R_d T_ref)) and rho = p / (R_d T)."""
+    R_d, cv, T0, g, p0, a = (consts[k] for k in ("R_d", "cv_d", "T_0", "grav", "MSLP", "planet_radius"))
+    rng = np.random.default_rng(seed)
+    k = int(rng.integers(1, 4))
+    phase = float(rng.uniform(0, 2 * np.pi))
+    lon_c = float(rng.uniform(-np.pi, np.pi))
+    lat_c = float(rng.uniform(-np.pi / 3, np.pi / 3))
+    x, y, z3 = xyz[:, 0], xyz[:, 1], xyz[:, 2]
+    r = np.sqrt(x * x + y * y + z3 * z3)
+    z = r - a
+    lat = np.arcsin(z3 / r)
+    lon = np.arctan2(y, x)
+    u = u_max * np.cos(lat) * 0.5 * (1.0 + np.sin(k * lon + phase))
+    cosd = np.sin(lat) * np.sin(lat_c) + np.cos(lat) * np.cos(lat_c) * np.cos(lon - lon_c)
+    d = a * np.arccos(np.clip(cosd, -1.0, 1.0))
+    T = T_ref + dT * np.exp(-((d / radius) ** 2) - ((z - z_c) / z_w) ** 2)
+    p = p0 * np.exp(-g * z / (R_d * T_ref))
+    rho = p / (R_d * T)
+    Q = np.zeros((xyz.shape[0], 5, xyz.shape[2]))
+    Q[:, 0] = rho
+    Q[:, 1] = rho * (-np.sin(lon) * u)
+    Q[:, 2] = rho * (np.cos(lon) * u)
+    Q[:, 4] = rho * (cv * (T - T0) + 0.5 * u * u + g * z)
+    return Q

@@ -150,6 +150,20 @@ int cmdg_mesh_create_brick(const cmdg_brick_desc* desc, cmdg_mesh** out) {
     return CMDG_OK;
 }
 
+int cmdg_mesh_create_shell(const cmdg_shell_desc* desc, cmdg_mesh** out) {
+    CMDG_ARG_CHECK(out != nullptr, "output pointer is NULL");
+    *out = nullptr;
+    cmdg_mesh* mh = new cmdg_mesh();
+    int rc = build_shell(desc, &mh->m);
+    if (rc) {
+        if (mh->m.d_nbr) cudaFree(mh->m.d_nbr);
+        delete mh;
+        return rc;
+    }
+    *out = mh;
+    return CMDG_OK;
+}
+
 int cmdg_mesh_destroy(cmdg_mesh* mesh) {
     if (!mesh) return CMDG_OK;
     cudaFree(mesh->m.d_emetric);
@@ -170,6 +184,10 @@ int cmdg_mesh_coordinates(const cmdg_mesh* mesh, double* h_xyz) {
     CMDG_ARG_CHECK(mesh != nullptr && h_xyz != nullptr, "NULL argument");
     const Mesh& m = mesh->m;
     const int Nq = m.Nq, Np = m.Np;
+    if (m.kind == MESH_SHELL) {
+        std::memcpy(h_xyz, m.xyz.data(), sizeof(double) * m.xyz.size());
+        return CMDG_OK;
+    }
     for (int64_t e = 0; e < m.nelem; ++e) {
         const int64_t iz = e % m.nz;
         const int64_t ix = (e / m.nz) % m.desc.ne[0];
@@ -193,6 +211,12 @@ int cmdg_mesh_mass(const cmdg_mesh* mesh, double* h_M) {
     CMDG_ARG_CHECK(mesh != nullptr && h_M != nullptr, "NULL argument");
     const Mesh& m = mesh->m;
     const int Nq = m.Nq, Np = m.Np;
+    if (m.kind == MESH_SHELL) {
+        for (int64_t e = 0; e < m.nelem; ++e)
+            for (int node = 0; node < Np; ++node)
+                h_M[(size_t)e * Np + node] = m.cgeo[((size_t)e * CG_NFIELDS + CG_M) * Np + node];
+        return CMDG_OK;
+    }
     for (int64_t e = 0; e < m.nelem; ++e) {
         const double J = 1.0 / (m.emetric[3 * e] * m.emetric[3 * e + 1] * m.emetric[3 * e + 2]);
         for (int node = 0; node < Np; ++node) {
@@ -210,8 +234,16 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
     CMDG_ARG_CHECK(precision == CMDG_FP64 || precision == CMDG_MIXED, "unknown precision %d", precision);
     CMDG_ARG_CHECK(p->numflux == CMDG_FLUX_RUSANOV || p->numflux == CMDG_FLUX_CENTRAL, "unknown numerical flux %d",
                    p->numflux);
-    CMDG_ARG_CHECK(p->orientation == CMDG_ORIENT_NONE || p->orientation == CMDG_ORIENT_FLAT,
-                   "orientation %d is not available on a brick", p->orientation);
+    const bool shell = mesh->m.kind == MESH_SHELL;
+    if (shell) {
+        CMDG_ARG_CHECK(p->orientation == CMDG_ORIENT_NONE || p->orientation == CMDG_ORIENT_SPHERE,
+                       "orientation %d is not available on a cubed shell", p->orientation);
+        CMDG_ARG_CHECK(p->turbulence == CMDG_TURB_NONE, "the cubed-shell kernels are inviscid");
+        CMDG_ARG_CHECK(p->orientation != CMDG_ORIENT_SPHERE || p->planet_radius > 0, "planet_radius must be positive");
+    } else {
+        CMDG_ARG_CHECK(p->orientation == CMDG_ORIENT_NONE || p->orientation == CMDG_ORIENT_FLAT,
+                       "orientation %d is not available on a brick", p->orientation);
+    }
     CMDG_ARG_CHECK(p->R_d > 0 && p->cv_d > 0 && p->cp_d > 0, "gas constants must be positive");
     CMDG_ARG_CHECK(p->turbulence == CMDG_TURB_NONE || p->turbulence == CMDG_TURB_CONSTANT ||
                        p->turbulence == CMDG_TURB_SMAGORINSKY,
@@ -242,6 +274,7 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
     md.ph.MSLP = p->MSLP;
     md.ph.with_divergence = p->with_divergence;
     int rc = init_model_tables(&md);
+    if (rc == CMDG_OK && shell) rc = init_shell_tables(&md);
     if (rc == CMDG_OK && p->turbulence != CMDG_TURB_NONE) rc = init_viscous_tables(&md);
     if (rc == CMDG_OK) {
         cudaError_t e = cudaMalloc(&md.d_status, sizeof(unsigned));
@@ -274,6 +307,11 @@ int cmdg_model_destroy(cmdg_model* model) {
     cudaFree(md.d_lvv64);
     cudaFree(md.d_lvv32);
     cudaFree(md.d_gf);
+    cudaFree(md.d_geo64);
+    cudaFree(md.d_geo32);
+    cudaFree(md.d_mass);
+    cudaFree(md.d_dxmin);
+    cudaFree(md.d_ref64);
     release_quad(&md);
     delete model;
     return CMDG_OK;
@@ -285,12 +323,13 @@ int cmdg_model_reference_state(const cmdg_model* model, double* h_ref) {
     CMDG_ARG_CHECK(h_ref != nullptr, "NULL output");
     const Model& md = model->m;
     const Mesh& m = *md.mesh;
+    const bool pernode = !md.ref64.empty();
     for (int64_t e = 0; e < m.nelem; ++e)
         for (int node = 0; node < m.Np; ++node) {
             const int lev = (int)(e % m.nz) * m.Nq + node / m.Nfp;
             const double* L = &md.lvl64[(size_t)lev * LV_NFIELDS];
-            h_ref[((size_t)e * 3 + 0) * m.Np + node] = L[LV_RHO_REF];
-            h_ref[((size_t)e * 3 + 1) * m.Np + node] = L[LV_RHOE_REF];
+            h_ref[((size_t)e * 3 + 0) * m.Np + node] = pernode ? md.ref64[((size_t)e * 2 + 0) * m.Np + node] : L[LV_RHO_REF];
+            h_ref[((size_t)e * 3 + 1) * m.Np + node] = pernode ? md.ref64[((size_t)e * 2 + 1) * m.Np + node] : L[LV_RHOE_REF];
             h_ref[((size_t)e * 3 + 2) * m.Np + node] = L[LV_P_REF];
         }
     return CMDG_OK;
@@ -385,6 +424,7 @@ int cmdg_gradient_flux(cmdg_model* model, void* d_gf, const void* d_Q, void* str
     if (rc) return rc;
     CMDG_ARG_CHECK(d_gf != nullptr && d_Q != nullptr, "NULL buffer");
     CMDG_ARG_CHECK(model->m.prm.turbulence != CMDG_TURB_NONE, "the model has no diffusive terms");
+    CMDG_ARG_CHECK(model->m.mesh->kind == MESH_BRICK, "the diffusive passes run on brick meshes");
     return launch_gradient(&model->m, d_Q, d_gf, (cudaStream_t)stream);
 }
 

@@ -185,6 +185,7 @@ extern "C" int cmdg_batch_create(cmdg_model* const* models, int n, cmdg_batch** 
         CMDG_ARG_CHECK(md.mesh->N >= BATCH_NMIN && md.mesh->N <= BATCH_NMAX,
                        "member %d: N=%d outside the ensemble range [3, 5]", m, md.mesh->N);
         CMDG_ARG_CHECK(md.prm.turbulence == CMDG_TURB_NONE, "member %d: ensembles are inviscid", m);
+        CMDG_ARG_CHECK(md.mesh->kind == MESH_BRICK, "member %d: ensembles run on brick meshes", m);
     }
     Batch* b = new Batch();
     for (int m = 0; m < n; ++m) b->members.push_back(&models[m]->m);

@@ -84,8 +84,33 @@ struct Physics {
     int with_divergence;
 };
 
+// mesh kinds: affine brick, or stacked cubed shell (curvilinear, per-node metrics)
+enum { MESH_BRICK = 0, MESH_SHELL = 1 };
+
+// per-node geometry of a curvilinear mesh, (Np, CG_NFIELDS, nelem) on the host
+enum CurvGeoField {
+    CG_XI = 0,       // curl-invariant dxi_d/dx_j, 9 words: d-major (d = 0..2, then j = 0..2)
+    CG_J = 9,        // det(dx/dxi)
+    CG_M = 10,       // J w_i w_j w_k
+    CG_DXMIN = 11,   // distance to the nearest neighbouring node along the element lines
+    CG_NFIELDS = 12
+};
+// per-node kernel geometry of a model on a curvilinear mesh, (Np, KG_NFIELDS, nelem)
+enum KernelGeoField {
+    KG_JXI = 0,      // J dxi_d/dx_j, 9 words, d-major
+    KG_INVJ = 9,
+    KG_GPHI = 10,    // DG gradient of the geopotential, 3 words
+    KG_DRHO = 13,    // reference density at the node minus its level value
+    KG_DRHOE = 14,   // reference total energy at the node minus its level value
+    KG_DCRHO = 15,   // pressure coefficient R_d T_0 - (R_d/cv_d) Phi at the node minus its level value
+    KG_DPREF = 16,   // reference pressure at the node minus its level value
+    KG_NFIELDS = 17
+};
+
 struct Mesh {
+    int kind = MESH_BRICK;
     cmdg_brick_desc desc;
+    cmdg_shell_desc shell;
     int N = 0, Nq = 0, Np = 0, Nfp = 0;
     int64_t nelem = 0;
     int nz = 0;                      // elements per column
@@ -97,6 +122,11 @@ struct Mesh {
     std::vector<int> nbr;            // [nelem][NBR_STRIDE]: 6 neighbours (or -tag), vertical index ez, spare
     std::vector<double> zlev;        // [nlev] node height of each vertical level
     std::vector<double> dzlev;       // [nlev] dz/dxi3 derivative helper (xi3x3 per level)
+    // curvilinear meshes: node coordinates (Np, 3, nelem) and geometry (Np, CG_NFIELDS, nelem);
+    // zlev holds the radius of each level, and nbr[7] the horizontal face
+    // orientation codes (4 bits per face: neighbour face 0..3, bit 2 = the
+    // in-face horizontal index runs reversed)
+    std::vector<double> xyz, cgeo;
     // device copies
     double* d_emetric = nullptr;
     float* d_emetric32 = nullptr;
@@ -137,12 +167,23 @@ struct Model {
     double* d_red = nullptr;         // reduction partials
     size_t red_len = 0;
     std::map<GraphKey, cudaGraphExec_t> graphs;
+    double* d_geo64 = nullptr;       // curvilinear meshes: (Np, KG_NFIELDS, nelem)
+    float* d_geo32 = nullptr;
+    double* d_mass = nullptr;        // curvilinear meshes: M per node
+    std::vector<double> ref64;       // curvilinear meshes: (Np, 2, nelem) rho_ref, rhoe_ref per node
+    double* d_ref64 = nullptr;
+    double* d_dxmin = nullptr;       // curvilinear meshes: nearest-node distance per node
     int grid_ctas = 0;               // persistent grid size of the stage kernel (0 = from occupancy)
     int kernel_kind = 0;             // KERNEL_NODE or KERNEL_COLUMN
 };
 
-// host-side setup (mesh.cpp)
+// host-side setup (mesh.cpp, shell_mesh.cpp)
 int build_brick(const cmdg_brick_desc* desc, Mesh* m);
+int build_shell(const cmdg_shell_desc* desc, Mesh* m);
+void lgl_derivative(Mesh* m);
+int init_shell_tables(Model* md);
+// virtual temperature and pressure of the reference profile at height z
+void temperature_profile(const cmdg_atmos_params& p, double z, double& Tv, double& pres);
 void lgl_nodes(int N, std::vector<double>& x, std::vector<double>& w);
 int init_model_tables(Model* md);
 int init_viscous_tables(Model* md);
@@ -159,6 +200,8 @@ struct LaunchArgs {
     int last_stage = 0;      // stage 5: the register is not written
 };
 int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
+// curvilinear stage kernel (shell.cu)
+int launch_shell_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
 // LSRK54CarpenterKennedy A and B coefficient arrays (5 entries each)
 void lsrk54_coefficients(const double** A, const double** B);
 

@@ -39,6 +39,9 @@ struct KParams {
     float DC32[(MAX_N + 1) * (MAX_N + 1)];
     double DC64[(MAX_N + 1) * (MAX_N + 1)];
     float rho_nu32, C_smag32, inv_Pr32, kappa32, MSLP32, grav32;
+    // curvilinear meshes: per-node kernel geometry (Np, KG_NFIELDS, nelem) in
+    // the working precision
+    const void* geo;
 };
 
 // A run of consecutive elements [e0, e1) of ensemble member `member`, of

@@ -53,6 +53,35 @@ void lgl_nodes(int N, std::vector<double>& x, std::vector<double>& w) {
     if (N % 2 == 0) x[N / 2] = 0.0;
 }
 
+// LGL nodes and weights, the barycentric differentiation matrix
+// (src/Numerics/Mesh/Elements.jl:34-82) and the weak-form operator Dhat.
+void lgl_derivative(Mesh* m) {
+    const int Nq = m->Nq;
+    lgl_nodes(m->N, m->xi, m->omega);
+    // barycentric differentiation matrix (src/Numerics/Mesh/Elements.jl:34-82)
+    std::vector<double> wb(Nq, 1.0);
+    for (int j = 0; j < Nq; ++j) {
+        for (int i = 0; i < Nq; ++i)
+            if (i != j) wb[j] *= (m->xi[j] - m->xi[i]);
+        wb[j] = 1.0 / wb[j];
+    }
+    m->D.assign(Nq * Nq, 0.0);
+    for (int j = 0; j < Nq; ++j)
+        for (int k = 0; k < Nq; ++k) {
+            if (j == k) {
+                double s = 0;
+                for (int l = 0; l < Nq; ++l)
+                    if (l != k) s += 1.0 / (m->xi[k] - m->xi[l]);
+                m->D[j * Nq + k] = s;
+            } else {
+                m->D[j * Nq + k] = (wb[k] / wb[j]) / (m->xi[j] - m->xi[k]);
+            }
+        }
+    m->Dhat.assign(Nq * Nq, 0.0);
+    for (int i = 0; i < Nq; ++i)
+        for (int n = 0; n < Nq; ++n) m->Dhat[i * Nq + n] = m->D[n * Nq + i] * m->omega[n] / m->omega[i];
+}
+
 static double blend(double a, double b, int n, int i) {
     return (double)(((long double)a * (n - i) + (long double)b * i) / n);
 }
@@ -79,29 +108,7 @@ int build_brick(const cmdg_brick_desc* d, Mesh* m) {
     m->nlev = m->nz * m->Nq;
     const int Nq = m->Nq;
 
-    lgl_nodes(m->N, m->xi, m->omega);
-    // barycentric differentiation matrix (src/Numerics/Mesh/Elements.jl:34-82)
-    std::vector<double> wb(Nq, 1.0);
-    for (int j = 0; j < Nq; ++j) {
-        for (int i = 0; i < Nq; ++i)
-            if (i != j) wb[j] *= (m->xi[j] - m->xi[i]);
-        wb[j] = 1.0 / wb[j];
-    }
-    m->D.assign(Nq * Nq, 0.0);
-    for (int j = 0; j < Nq; ++j)
-        for (int k = 0; k < Nq; ++k) {
-            if (j == k) {
-                double s = 0;
-                for (int l = 0; l < Nq; ++l)
-                    if (l != k) s += 1.0 / (m->xi[k] - m->xi[l]);
-                m->D[j * Nq + k] = s;
-            } else {
-                m->D[j * Nq + k] = (wb[k] / wb[j]) / (m->xi[j] - m->xi[k]);
-            }
-        }
-    m->Dhat.assign(Nq * Nq, 0.0);
-    for (int i = 0; i < Nq; ++i)
-        for (int n = 0; n < Nq; ++n) m->Dhat[i * Nq + n] = m->D[n * Nq + i] * m->omega[n] / m->omega[i];
+    lgl_derivative(m);
 
     m->emetric.assign(nelem * 3, 0.0);
     m->nbr.assign(nelem * NBR_STRIDE, 0);
@@ -158,7 +165,7 @@ int build_brick(const cmdg_brick_desc* d, Mesh* m) {
 
 // Temperature profiles (Thermodynamics.TemperatureProfiles: IsothermalProfile,
 // DryAdiabaticProfile) as used by HydrostaticState (src/Atmos/Model/ref_state.jl:70-82).
-static void temperature_profile(const cmdg_atmos_params& p, double z, double& Tv, double& pres) {
+void temperature_profile(const cmdg_atmos_params& p, double z, double& Tv, double& pres) {
     if (p.profile == CMDG_PROFILE_ISOTHERMAL) {
         Tv = p.T_surface;
         pres = p.MSLP * std::exp(-z * p.grav / (p.R_d * Tv));
@@ -187,7 +194,10 @@ int init_model_tables(Model* md) {
     std::vector<double> pz(nlev, 0.0), rz(nlev, 0.0);
     for (int lev = 0; lev < nlev; ++lev) {
         const double z = m.zlev[lev];
-        L(lev, LV_PHI) = (p.orientation == CMDG_ORIENT_FLAT) ? p.grav * z : 0.0;
+        // z: height on a brick, radius on a cubed shell
+        L(lev, LV_PHI) = (p.orientation == CMDG_ORIENT_FLAT)     ? p.grav * z
+                         : (p.orientation == CMDG_ORIENT_SPHERE) ? p.grav * (z - p.planet_radius)
+                                                                 : 0.0;
     }
     // element-local DG derivative along a column
     auto ddz = [&](const std::vector<double>& f, int lev) {
@@ -200,7 +210,8 @@ int init_model_tables(Model* md) {
     for (int lev = 0; lev < nlev; ++lev) phi[lev] = L(lev, LV_PHI);
     for (int lev = 0; lev < nlev; ++lev) L(lev, LV_GPHIZ) = ddz(phi, lev);
     if (p.ref_state) {
-        CMDG_ARG_CHECK(p.orientation == CMDG_ORIENT_FLAT, "a hydrostatic reference state needs FlatOrientation");
+        CMDG_ARG_CHECK(p.orientation == CMDG_ORIENT_FLAT || p.orientation == CMDG_ORIENT_SPHERE,
+                       "a hydrostatic reference state needs an orientation");
         for (int lev = 0; lev < nlev; ++lev) {
             double Tv, pres;
             temperature_profile(p, L(lev, LV_PHI) / p.grav, Tv, pres);

@@ -1,7 +1,8 @@
 // Element-wise conversions and global reductions of libcmdg.
 //
 //  * to/from perturbation: q' = q - q_ref evaluated in FP64 and rounded to
-//    FP32 (and back), the reference state taken per vertical node level.
+//    FP32 (and back), the reference state taken per vertical node level, or
+//    per node on a curvilinear mesh.
 //  * compensated weighted sums: sum_nodes M q in double-double (TwoSum /
 //    TwoProd) per block, block partials summed on the host in double-double
 //    (weightedsum, src/Arrays/MPIStateArrays.jl:655-675, which accumulates in
@@ -19,33 +20,36 @@ __device__ __forceinline__ int node_level(int64_t e, int node, int nz, int Nq, i
     return (int)(e % nz) * Nq + node / Nfp;
 }
 
+// reference value of field s at a node: per-node table (curvilinear meshes) or level row
+__device__ __forceinline__ double ref_value(const double* lvl, const double* refn, int64_t e, int node, int s,
+                                            int Np, int nz, int Nq) {
+    if (s != 0 && s != 4) return 0.0;
+    if (refn) return refn[((size_t)e * 2 + (s == 4)) * Np + node];
+    const double* L = lvl + (size_t)node_level(e, node, nz, Nq, Nq * Nq) * LV_NFIELDS;
+    return (s == 0) ? L[LV_RHO_REF] : L[LV_RHOE_REF];
+}
+
 __global__ void to_perturbation_kernel(float* __restrict__ Qp, const double* __restrict__ Q, const double* lvl,
-                                       int64_t nelem, int Np, int Nq, int nz) {
+                                       const double* refn, int64_t nelem, int Np, int Nq, int nz) {
     const int64_t total = nelem * NSTATE * Np;
-    const int Nfp = Nq * Nq;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
          idx += (int64_t)gridDim.x * blockDim.x) {
         const int node = (int)(idx % Np);
         const int s = (int)((idx / Np) % NSTATE);
         const int64_t e = idx / ((int64_t)Np * NSTATE);
-        const double* L = lvl + (size_t)node_level(e, node, nz, Nq, Nfp) * LV_NFIELDS;
-        double ref = (s == 0) ? L[LV_RHO_REF] : (s == 4) ? L[LV_RHOE_REF] : 0.0;
-        Qp[idx] = (float)(Q[idx] - ref);
+        Qp[idx] = (float)(Q[idx] - ref_value(lvl, refn, e, node, s, Np, nz, Nq));
     }
 }
 
 __global__ void from_perturbation_kernel(double* __restrict__ Q, const float* __restrict__ Qp, const double* lvl,
-                                         int64_t nelem, int Np, int Nq, int nz) {
+                                         const double* refn, int64_t nelem, int Np, int Nq, int nz) {
     const int64_t total = nelem * NSTATE * Np;
-    const int Nfp = Nq * Nq;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
          idx += (int64_t)gridDim.x * blockDim.x) {
         const int node = (int)(idx % Np);
         const int s = (int)((idx / Np) % NSTATE);
         const int64_t e = idx / ((int64_t)Np * NSTATE);
-        const double* L = lvl + (size_t)node_level(e, node, nz, Nq, Nfp) * LV_NFIELDS;
-        double ref = (s == 0) ? L[LV_RHO_REF] : (s == 4) ? L[LV_RHOE_REF] : 0.0;
-        Q[idx] = ref + (double)Qp[idx];
+        Q[idx] = ref_value(lvl, refn, e, node, s, Np, nz, Nq) + (double)Qp[idx];
     }
 }
 
@@ -68,10 +72,12 @@ __device__ __forceinline__ dd two_prod(double a, double b) {
 }
 
 // Block partial (hi, lo) of sum M * q over all nodes for one field.
-// M = J w_i w_j w_k with J = (dx/2)(dy/2)(dz/2) = 1/(xi1 xi2 xi3) on an affine brick element.
+// M = J w_i w_j w_k with J = (dx/2)(dy/2)(dz/2) = 1/(xi1 xi2 xi3) on an affine
+// brick element, or the per-node M of a curvilinear mesh (mnode != NULL).
 template <bool MIXED>
 __global__ void weighted_sum_kernel(const void* Qv, int field, const double* emetric, const double* w, const double* lvl,
-                                    int64_t nelem, int Np, int Nq, int nz, double* partial) {
+                                    int64_t nelem, int Np, int Nq, int nz, const double* mnode, const double* refn,
+                                    double* partial) {
     const int Nfp = Nq * Nq;
     dd acc{0.0, 0.0};
     const int64_t total = nelem * Np;
@@ -80,13 +86,12 @@ __global__ void weighted_sum_kernel(const void* Qv, int field, const double* eme
         const int node = (int)(idx % Np);
         const int64_t e = idx / Np;
         const int i = node % Nq, j = (node / Nq) % Nq, k = node / Nfp;
-        const double J = 1.0 / (emetric[3 * e] * emetric[3 * e + 1] * emetric[3 * e + 2]);
-        const double M = J * (w[i] * w[j] * w[k]);
+        const double M = mnode ? mnode[idx]
+                               : (1.0 / (emetric[3 * e] * emetric[3 * e + 1] * emetric[3 * e + 2])) * (w[i] * w[j] * w[k]);
         const size_t qi = ((size_t)e * NSTATE + field) * Np + node;
         double qv;
         if (MIXED) {
-            const double* L = lvl + (size_t)node_level(e, node, nz, Nq, Nfp) * LV_NFIELDS;
-            double ref = (field == 0) ? L[LV_RHO_REF] : (field == 4) ? L[LV_RHOE_REF] : 0.0;
+            const double ref = ref_value(lvl, refn, e, node, field, Np, nz, Nq);
             // sum M*ref + M*q' as two exact products
             acc = dd_add(acc, two_prod(M, ref));
             qv = (double)static_cast<const float*>(Qv)[qi];
@@ -118,7 +123,8 @@ __global__ void weighted_sum_kernel(const void* Qv, int field, const double* eme
 // max over nodes of (|u| + c) / dx_min with dx_min the distance to the
 // nearest neighbouring node of the same element along xi1, xi2 or xi3.
 __global__ void courant_kernel(const double* __restrict__ Q, const double* emetric, const double* xi, const double* lvl,
-                               Physics ph, int64_t nelem, int Np, int Nq, int nz, double* partial) {
+                               Physics ph, int64_t nelem, int Np, int Nq, int nz, const double* dxmin,
+                               double* partial) {
     const int Nfp = Nq * Nq;
     double best = 0.0;
     const int64_t total = nelem * Np;
@@ -128,11 +134,15 @@ __global__ void courant_kernel(const double* __restrict__ Q, const double* emetr
         const int64_t e = idx / Np;
         const int ijk[3] = {node % Nq, (node / Nq) % Nq, node / Nfp};
         double md = INFINITY;
-        for (int d = 0; d < 3; ++d) {
-            const double h = 2.0 / emetric[3 * e + d];
-            const int a = ijk[d];
-            if (a > 0) md = fmin(md, 0.5 * h * (xi[a] - xi[a - 1]));
-            if (a < Nq - 1) md = fmin(md, 0.5 * h * (xi[a + 1] - xi[a]));
+        if (dxmin) {
+            md = dxmin[idx];
+        } else {
+            for (int d = 0; d < 3; ++d) {
+                const double h = 2.0 / emetric[3 * e + d];
+                const int a = ijk[d];
+                if (a > 0) md = fmin(md, 0.5 * h * (xi[a] - xi[a - 1]));
+                if (a < Nq - 1) md = fmin(md, 0.5 * h * (xi[a + 1] - xi[a]));
+            }
         }
         const double* L = lvl + (size_t)node_level(e, node, nz, Nq, Nfp) * LV_NFIELDS;
         double q[NSTATE];
@@ -201,14 +211,14 @@ void release_quad(const Model* md) {
 
 int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s) {
     const Mesh& m = *md->mesh;
-    to_perturbation_kernel<<<RED_BLOCKS * 4, 256, 0, s>>>(Qp, Q, md->d_lvl64, m.nelem, m.Np, m.Nq, m.nz);
+    to_perturbation_kernel<<<RED_BLOCKS * 4, 256, 0, s>>>(Qp, Q, md->d_lvl64, md->d_ref64, m.nelem, m.Np, m.Nq, m.nz);
     CMDG_CUDA_CHECK(cudaGetLastError());
     return CMDG_OK;
 }
 
 int launch_from_perturbation(Model* md, double* Q, const float* Qp, cudaStream_t s) {
     const Mesh& m = *md->mesh;
-    from_perturbation_kernel<<<RED_BLOCKS * 4, 256, 0, s>>>(Q, Qp, md->d_lvl64, m.nelem, m.Np, m.Nq, m.nz);
+    from_perturbation_kernel<<<RED_BLOCKS * 4, 256, 0, s>>>(Q, Qp, md->d_lvl64, md->d_ref64, m.nelem, m.Np, m.Nq, m.nz);
     CMDG_CUDA_CHECK(cudaGetLastError());
     return CMDG_OK;
 }
@@ -234,10 +244,12 @@ int weighted_sums(Model* md, const void* Q, bool mixed, int nfields, const int* 
         CMDG_ARG_CHECK(fields[f] >= 0 && fields[f] < NSTATE, "field index %d out of range", fields[f]);
         if (mixed)
             weighted_sum_kernel<true><<<RED_BLOCKS, RED_THREADS, 0, s>>>(Q, fields[f], m.d_emetric, dq.w, md->d_lvl64,
-                                                                        m.nelem, m.Np, m.Nq, m.nz, md->d_red);
+                                                                        m.nelem, m.Np, m.Nq, m.nz, md->d_mass,
+                                                                        md->d_ref64, md->d_red);
         else
             weighted_sum_kernel<false><<<RED_BLOCKS, RED_THREADS, 0, s>>>(Q, fields[f], m.d_emetric, dq.w, md->d_lvl64,
-                                                                         m.nelem, m.Np, m.Nq, m.nz, md->d_red);
+                                                                         m.nelem, m.Np, m.Nq, m.nz, md->d_mass,
+                                                                        md->d_ref64, md->d_red);
         CMDG_CUDA_CHECK(cudaGetLastError());
         CMDG_CUDA_CHECK(cudaMemcpyAsync(h.data(), md->d_red, sizeof(double) * 2 * RED_BLOCKS, cudaMemcpyDeviceToHost, s));
         CMDG_CUDA_CHECK(cudaStreamSynchronize(s));
@@ -255,7 +267,7 @@ int courant_dt(Model* md, const double* Q, double CFL, double* dt, cudaStream_t 
     if ((rc = quad(md, dq))) return rc;
     const Mesh& m = *md->mesh;
     courant_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(Q, m.d_emetric, dq.xi, md->d_lvl64, md->ph, m.nelem, m.Np, m.Nq,
-                                                     m.nz, md->d_red);
+                                                     m.nz, md->d_dxmin, md->d_red);
     CMDG_CUDA_CHECK(cudaGetLastError());
     std::vector<double> h(RED_BLOCKS);
     CMDG_CUDA_CHECK(cudaMemcpyAsync(h.data(), md->d_red, sizeof(double) * RED_BLOCKS, cudaMemcpyDeviceToHost, s));

@@ -1,0 +1,349 @@
+// Fused DG tendency + LSRK stage kernel for curvilinear (cubed-shell) meshes.
+//
+// The brick kernel's three phases with per-node geometry: one CTA owns one
+// element for a whole stage;
+//   phase 1  every node evaluates the thermodynamics and first-order flux of
+//            its state and stages the contravariant fluxes
+//            Ft_d = J (dxi_d/dx) . F, d = 1..3, in shared memory, and forms
+//            the gravity source -rho grad(Phi) with the DG gradient of Phi;
+//   phase 2  every face node takes the outward normal n = +-J dxi_d/dx / |.|
+//            and surface Jacobian |J dxi_d/dx| of its own volume node, the
+//            interior normal flux F.n = +-Ft_d / |J dxi_d/dx| from phase 1,
+//            gathers the neighbour's state at the matching node (horizontal
+//            faces through the face-orientation code of the connectivity
+//            row; walls reflect the normal momentum,
+//            rho u+ = rho u- - 2 (rho u- . n) n), and stores the lifted
+//            Rusanov or central flux vMI sM F* = |J dxi_d/dx| / (J w_0) F*;
+//   phase 3  every node contracts Ft_d with the weak-form derivative Dhat,
+//            scales by 1/J, subtracts its face terms, adds the source and
+//            finishes the tendency or the LSRK 2N stage update.
+// With M = J w_i w_j w_k this is M^-1 D^T M (dxi_d/dx . F) of
+// src/Numerics/DGMethods/DGModel_kernels.jl:64-548 and the interface term of
+// :588-901 (NumericalFluxes.jl:219-340; bc_momentum.jl:25-34), with the
+// geometry of src/Numerics/Mesh/Metrics.jl:431-724 (normals and sJ from
+// J dxi_d/dx at the face node) and Grids.jl:1068-1096.
+//
+// The geopotential and reference pressure are per vertical level (every node
+// of a level has the same radius); the reference density and energy are the
+// level row plus a per-node difference (the discrete hydrostatic balance on
+// curved elements varies along a level).  In mixed precision the
+// reference-state jump q_ref(-) - q_ref(+) in the Rusanov penalty is the
+// FP64-computed level jump across vertical faces plus the difference of the
+// two nodes' per-node parts.
+#include "dg_common.cuh"
+
+namespace cmdg {
+namespace {
+
+template <int N>
+struct ShellDims {
+    static constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp, NF = 6 * Nfp;
+    static constexpr int NT = (((Np > NF) ? Np : NF) + 31) / 32 * 32;
+    static constexpr int MIN_CTAS = N == 2 ? 12 : N == 3 ? 8 : N == 4 ? 6 : 4;
+    static constexpr int MIN_CTAS64 = N == 5 ? 2 : 3;
+};
+
+template <int N, typename R>
+struct ShellSmem {
+    static constexpr int Nq = N + 1, Np = Nq * Nq * Nq, Nfp = Nq * Nq, W = Slot<R>::W;
+    static constexpr int NODE = 0;
+    static constexpr int FLUX = NODE + Np * W;
+    static constexpr int FACE = FLUX + 3 * Np * W;
+    static constexpr int DMAT = FACE + 6 * Nfp * W;
+    static constexpr int TOTAL = DMAT + Nq * Nq;
+    static constexpr size_t BYTES = sizeof(R) * TOTAL;
+};
+
+template <int N, typename R, bool MIXED, int MODE>
+__global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CTAS : ShellDims<N>::MIN_CTAS64)
+    shell_stage_kernel(const KParams P) {
+    using Dm = ShellDims<N>;
+    using SM = ShellSmem<N, R>;
+    constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, W = SM::W;
+    constexpr int ESTRIDE = NSTATE * Np, GSTRIDE = KG_NFIELDS * Np;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* const sm = reinterpret_cast<R*>(smem_raw);
+    R* const s_node = sm + SM::NODE;
+    R* const s_F = sm + SM::FLUX;
+    R* const s_fs = sm + SM::FACE;
+    R* const s_D = sm + SM::DMAT;
+
+    const int t = threadIdx.x;
+    const int e = blockIdx.x;
+    const R* __restrict__ Qin = static_cast<const R*>(P.Qin);
+    R* __restrict__ Qout = static_cast<R*>(P.Qout);
+    const R* __restrict__ ge = static_cast<const R*>(P.geo) + (size_t)e * GSTRIDE;
+    const Physics& ph = P.ph;
+    const bool node_thread = t < Np;
+    const bool face_thread = t < 6 * Nfp;
+    const bool read_reg = (MODE == 0) ? (P.beta != 0) : !P.first_stage;
+
+    const int nk = node_thread ? t / Nfp : 0;
+    const int nj = node_thread ? (t - nk * Nfp) / Nq : 0;
+    const int ni = node_thread ? t - nk * Nfp - nj * Nq : 0;
+    const int f = face_thread ? t / Nfp : 0;
+    const int fn = face_thread ? t - f * Nfp : 0;
+    const int fd = f >> 1, fside = f & 1;
+    const int fa = fn % Nq, fb = fn / Nq;
+    const int vM = fd == 0 ? fside * N + Nq * fn : (fd == 1 ? fa + Nq * (fside * N + Nq * fb) : fn + Nfp * (fside * N));
+    const int kM = vM / Nfp;
+    const R sgn = fside ? R(1) : R(-1);
+
+    if (t < Nq * Nq) s_D[t] = static_cast<const R*>(P.Dhat)[t];
+    const int* nbr = P.nbr + NBR_STRIDE * e;
+    const int ez = __ldg(nbr + 6);
+    const size_t ebase = (size_t)e * ESTRIDE + t;
+
+    // ---------------- phase 1: node thermodynamics, contravariant fluxes, gravity
+    R q[NSTATE], src[3] = {0, 0, 0}, invJ = 0;
+    double dq_old[NSTATE];
+    if (node_thread) {
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) q[s] = Qin[ebase + s * Np];
+        if (read_reg) {
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) dq_old[s] = P.dQ[ebase + s * Np];
+        }
+        R Jx[9];
+#pragma unroll
+        for (int w = 0; w < 9; ++w) Jx[w] = ge[(KG_JXI + w) * Np + t];
+        invJ = ge[KG_INVJ * Np + t];
+        Level<R> lv = load_level<R>(P, ez * Nq + nk);
+        if (ph.ref_state) {
+            // the reference density varies along a level on curved elements
+            lv.rho_ref += ge[KG_DRHO * Np + t];
+            lv.href += ge[KG_DRHOE * Np + t];
+            if (!MIXED) {
+                // rounding-sized per-node parts, below FP32 resolution
+                const R dp = ge[KG_DPREF * Np + t];
+                lv.p_ref += dp;
+                lv.href += dp;
+            }
+        }
+        if (!MIXED) lv.crho += ge[KG_DCRHO * Np + t];
+        const Thermo<R, MIXED> th = thermo<R, MIXED>(q, lv, P);
+        R* rec = s_node + t * W;
+        st5<R>(rec, q);
+        rec[5] = th.c;
+        rec[6] = th.rinv;
+        R F0[NSTATE], F1[NSTATE], F2[NSTATE];
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) {
+            F0[s] = flux_d<R, MIXED>(q, th, 0, s);
+            F1[s] = flux_d<R, MIXED>(q, th, 1, s);
+            F2[s] = flux_d<R, MIXED>(q, th, 2, s);
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            R Ft[NSTATE];
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) Ft[s] = Jx[d * 3 + 0] * F0[s] + Jx[d * 3 + 1] * F1[s] + Jx[d * 3 + 2] * F2[s];
+            st5<R>(s_F + (d * Np + t) * W, Ft);
+        }
+        if (ph.gravity) {
+            const R rho_s = MIXED ? ((ph.ref_state && ph.subtract_off) ? q[0] : lv.rho_ref + q[0])
+                                  : ((ph.ref_state && ph.subtract_off) ? q[0] - lv.rho_ref : q[0]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) src[c] = -rho_s * ge[(KG_GPHI + c) * Np + t];
+        }
+    }
+    __syncthreads();
+
+    // ---------------- phase 2: one numerical flux per face node
+    if (face_thread) {
+        const R j0 = ge[(KG_JXI + fd * 3 + 0) * Np + vM];
+        const R j1 = ge[(KG_JXI + fd * 3 + 1) * Np + vM];
+        const R j2 = ge[(KG_JXI + fd * 3 + 2) * Np + vM];
+        const R iJm = ge[KG_INVJ * Np + vM];
+        const R sJ = sqrt_r(j0 * j0 + j1 * j1 + j2 * j2);
+        const R rs = rcp_r(sJ);
+        const R nv[3] = {sgn * j0 * rs, sgn * j1 * rs, sgn * j2 * rs};
+        R qm[NSTATE], Fm[NSTATE], qp[NSTATE], Fp[NSTATE], jr[NSTATE] = {0, 0, 0, 0, 0};
+        const R* rec = s_node + vM * W;
+        ld5<R>(rec, qm);
+        const R c_m = rec[5], ri_m = rec[6];
+        ld5<R>(s_F + (fd * Np + vM) * W, Fm);
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) Fm[s] *= sgn * rs;
+        const R mn_m = qm[1] * nv[0] + qm[2] * nv[1] + qm[3] * nv[2];
+        const R lam_m = fabs(mn_m * ri_m) + c_m;
+        const int nb = __ldg(nbr + f);
+        int ezp = ez, kP = kM;
+        const R* gp = ge;  // geometry of the node across the face (own node on a wall)
+        int vP = vM;
+        if (nb >= 0) {
+            if (fd == 2) {
+                kP = fside ? 0 : N;
+                vP = fn + Nfp * kP;
+                ezp = ez + (fside ? 1 : -1);
+                if (MIXED && ph.numflux == CMDG_FLUX_RUSANOV) {
+                    const int ej = fside ? ezp : ez;
+                    const R sj = fside ? R(-1) : R(1);
+                    jr[0] = sj * (R)P.jump32[2 * ej + 0];
+                    jr[4] = sj * (R)P.jump32[2 * ej + 1];
+                }
+            } else {
+                const unsigned code = ((unsigned)__ldg(nbr + 7) >> (4 * f)) & 15u;
+                const int f2 = (int)(code & 3u);
+                const int a2 = (code & 4u) ? N - fa : fa;
+                const int side2 = (f2 & 1) ? N : 0;
+                vP = (f2 < 2) ? side2 + Nq * (a2 + Nq * fb) : a2 + Nq * (side2 + Nq * fb);
+            }
+            const R* qn = Qin + (size_t)nb * ESTRIDE + vP;
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) qp[s] = qn[s * Np];
+            gp = static_cast<const R*>(P.geo) + (size_t)nb * GSTRIDE;
+        } else {
+            // Impenetrable(FreeSlip) + Insulating wall
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) qp[s] = qm[s];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) qp[1 + c] = qm[1 + c] - R(2) * mn_m * nv[c];
+        }
+        Level<R> lvp = load_level<R>(P, ezp * Nq + kP);
+        if (!MIXED) lvp.crho += gp[KG_DCRHO * Np + vP];
+        if (ph.ref_state) {
+            const R drp = gp[KG_DRHO * Np + vP], dep = gp[KG_DRHOE * Np + vP];
+            lvp.rho_ref += drp;
+            lvp.href += dep;
+            if (!MIXED) {
+                const R dpp = gp[KG_DPREF * Np + vP];
+                lvp.p_ref += dpp;
+                lvp.href += dpp;
+            }
+            if (MIXED && ph.numflux == CMDG_FLUX_RUSANOV) {
+                // per-node part of the reference jump q_ref(-) - q_ref(+)
+                jr[0] += ge[KG_DRHO * Np + vM] - drp;
+                jr[4] += ge[KG_DRHOE * Np + vM] - dep;
+            }
+        }
+        const Thermo<R, MIXED> thp = thermo<R, MIXED>(qp, lvp, P);
+        const R mn_p = qp[1] * nv[0] + qp[2] * nv[1] + qp[3] * nv[2];
+        const R un_p = mn_p * thp.rinv;
+        Fp[0] = mn_p;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) Fp[1 + c] = mn_p * thp.u[c] + thp.pflux * nv[c];
+        Fp[4] = un_p * thp.H;
+        const R lam_p = fabs(un_p) + thp.c;
+        const R lift = sJ * iJm * KConst<R>::inv_w0(P);
+        const R hmw = (ph.numflux == CMDG_FLUX_RUSANOV) ? R(0.5) * fmax(lam_m, lam_p) : R(0);
+        const R hl = R(0.5) * lift, pl = hmw * lift;
+        R fs[NSTATE];
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) fs[s] = hl * (Fm[s] + Fp[s]) + pl * ((qm[s] - qp[s]) + jr[s]);
+        st5<R>(s_fs + (f * Nfp + fn) * W, fs);
+    }
+    __syncthreads();
+
+    // ---------------- phase 3: volume contraction, face terms, source, update
+    int bad = 0;
+    if (node_thread) {
+        R acc[NSTATE] = {0, 0, 0, 0, 0};
+        const R* F1 = s_F + (0 * Np + Nq * (nj + Nq * nk)) * W;
+        const R* F2 = s_F + (1 * Np + ni + Nfp * nk) * W;
+        const R* F3 = s_F + (2 * Np + ni + Nq * nj) * W;
+#pragma unroll
+        for (int n = 0; n < Nq; ++n) {
+            R v1[NSTATE], v2[NSTATE], v3[NSTATE];
+            ld5<R>(F1 + n * W, v1);
+            ld5<R>(F2 + n * Nq * W, v2);
+            ld5<R>(F3 + n * Nfp * W, v3);
+            const R d1 = s_D[ni * Nq + n], d2 = s_D[nj * Nq + n], d3 = s_D[nk * Nq + n];
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) acc[s] = fma(d1, v1[s], fma(d2, v2[s], fma(d3, v3[s], acc[s])));
+        }
+        R rhs[NSTATE];
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) rhs[s] = invJ * acc[s];
+        auto sub_face = [&](int ff, int idx) {
+            R v[NSTATE];
+            ld5<R>(s_fs + (ff * Nfp + idx) * W, v);
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) rhs[s] -= v[s];
+        };
+        if (ni == 0) sub_face(0, nj + Nq * nk);
+        if (ni == N) sub_face(1, nj + Nq * nk);
+        if (nj == 0) sub_face(2, ni + Nq * nk);
+        if (nj == N) sub_face(3, ni + Nq * nk);
+        if (nk == 0) sub_face(4, ni + Nq * nj);
+        if (nk == N) sub_face(5, ni + Nq * nj);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) rhs[1 + c] += src[c];
+        const R rkb_dt = KConst<R>::rkb_dt(P);
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) {
+            if (!isfinite(rhs[s])) bad = 1;
+            const size_t idx = ebase + s * Np;
+            if (MODE == 0) {
+                double out = P.alpha * (double)rhs[s];
+                if (read_reg) out = fma(P.beta, dq_old[s], out);
+                P.dQ[idx] = out;
+            } else {
+                double dq;
+                if (MIXED) {
+                    if (read_reg) {
+                        dq = fma(P.rka, dq_old[s], f32_to_f64_bits((float)rhs[s]));
+                        Qout[idx] = fma(rkb_dt, (R)f64_to_f32_bits(dq), q[s]);
+                    } else {
+                        dq = f32_to_f64_bits((float)rhs[s]);
+                        Qout[idx] = fma(rkb_dt, rhs[s], q[s]);
+                    }
+                } else {
+                    dq = read_reg ? fma(P.rka, dq_old[s], (double)rhs[s]) : (double)rhs[s];
+                    Qout[idx] = (R)fma(P.rkb_dt, dq, (double)q[s]);
+                }
+                if (!P.last_stage) P.dQ[idx] = dq;
+            }
+        }
+    }
+    if (__syncthreads_or(bad) && t == 0) atomicOr(P.status, 1u);
+}
+
+template <int N, typename R, bool MIXED, int MODE>
+cudaError_t launch_shell_typed(const KParams& P, cudaStream_t s) {
+    constexpr size_t bytes = ShellSmem<N, R>::BYTES;
+    static unsigned long long configured = 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (!(configured & (1ull << (dev & 63)))) {
+        e = cudaFuncSetAttribute(shell_stage_kernel<N, R, MIXED, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)bytes);
+        if (e != cudaSuccess) return e;
+        configured |= 1ull << (dev & 63);
+    }
+    shell_stage_kernel<N, R, MIXED, MODE><<<(unsigned)P.nelem, ShellDims<N>::NT, bytes, s>>>(P);
+    return cudaGetLastError();
+}
+
+template <int N>
+cudaError_t launch_shell_N(const KParams& P, bool mixed, int mode, cudaStream_t s) {
+    if (mixed)
+        return mode == 0 ? launch_shell_typed<N, float, true, 0>(P, s) : launch_shell_typed<N, float, true, 1>(P, s);
+    return mode == 0 ? launch_shell_typed<N, double, false, 0>(P, s) : launch_shell_typed<N, double, false, 1>(P, s);
+}
+
+}  // namespace
+
+int launch_shell_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
+    const Mesh& m = *md->mesh;
+    const KParams P = make_params(md, a);
+    const bool mixed = md->precision == CMDG_MIXED;
+    cudaError_t err;
+    switch (m.N) {
+        case 2: err = launch_shell_N<2>(P, mixed, a.mode, s); break;
+        case 3: err = launch_shell_N<3>(P, mixed, a.mode, s); break;
+        case 4: err = launch_shell_N<4>(P, mixed, a.mode, s); break;
+        case 5: err = launch_shell_N<5>(P, mixed, a.mode, s); break;
+        default:
+            set_error("no cubed-shell stage kernel for N=%d", m.N);
+            return CMDG_ERR_ARG;
+    }
+    if (err != cudaSuccess) {
+        set_error("cubed-shell stage kernel launch failed: %s", cudaGetErrorString(err));
+        return CMDG_ERR_CUDA;
+    }
+    return CMDG_OK;
+}
+
+}  // namespace cmdg

@@ -452,11 +452,13 @@ KParams make_params(Model* md, const LaunchArgs& a) {
     P.kappa32 = (float)md->ph.kappa;
     P.MSLP32 = (float)md->ph.MSLP;
     P.grav32 = (float)md->ph.grav;
+    P.geo = mixed ? (const void*)md->d_geo32 : (const void*)md->d_geo64;
     return P;
 }
 
 int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
     const Mesh& m = *md->mesh;
+    if (m.kind == MESH_SHELL) return launch_shell_stage(md, a, s);
     if (md->prm.turbulence != CMDG_TURB_NONE) return launch_viscous_stage(md, a, s);
     const KParams P = make_params(md, a);
     const bool mixed = md->precision == CMDG_MIXED;

@@ -52,7 +52,7 @@ enum { CMDG_FP64 = 0, CMDG_MIXED = 1 };
 /* Numerical flux for first-order terms */
 enum { CMDG_FLUX_RUSANOV = 0, CMDG_FLUX_CENTRAL = 1 };
 /* Orientation */
-enum { CMDG_ORIENT_NONE = 0, CMDG_ORIENT_FLAT = 1 };
+enum { CMDG_ORIENT_NONE = 0, CMDG_ORIENT_FLAT = 1, CMDG_ORIENT_SPHERE = 2 };
 /* Reference-state temperature profile */
 enum { CMDG_PROFILE_ISOTHERMAL = 0, CMDG_PROFILE_DRY_ADIABATIC = 1 };
 /* Turbulence closure */
@@ -86,7 +86,18 @@ typedef struct {
     double rho_nu;      /* ConstantDynamicViscosity rho*nu */
     int with_divergence;/* ConstantDynamicViscosity WithDivergence */
     double C_smag;      /* SmagorinskyLilly coefficient */
+    double planet_radius; /* SphericalOrientation: Phi = grav (|x| - planet_radius) */
 } cmdg_atmos_params;
+
+/* Stacked equiangular cubed shell: 6 nhorz^2 columns of nvert elements
+ * between radii r_inner and r_outer, walls (FreeSlip + Insulating) at both. */
+typedef struct {
+    int N;              /* polynomial order, 2..5 */
+    int nhorz;          /* elements along each cube-face edge */
+    int nvert;          /* elements per column */
+    double r_inner, r_outer;
+    int bc_inner, bc_outer; /* boundary tags (> 0) */
+} cmdg_shell_desc;
 
 typedef struct cmdg_mesh cmdg_mesh;
 typedef struct cmdg_model cmdg_model;
@@ -101,6 +112,12 @@ const char* cmdg_version(void);
  * Replaces BrickTopology/StackedBrickTopology + DiscontinuousSpectralElementGrid
  * (src/Numerics/Mesh/Topologies.jl:470-545,632; src/Numerics/Mesh/Grids.jl:267-414). */
 int cmdg_mesh_create_brick(const cmdg_brick_desc* desc, cmdg_mesh** out);
+/* Builds a stacked cubed-shell mesh: curvilinear geometry with the
+ * curl-invariant metric terms.  Replaces StackedCubedSphereTopology +
+ * DiscontinuousSpectralElementGrid(meshwarp = equiangular_cubed_sphere_warp)
+ * (src/Numerics/Mesh/Topologies.jl:1067-1305,1620-1760;
+ * src/Numerics/Mesh/Grids.jl:1028-1110; src/Numerics/Mesh/Metrics.jl:431-724). */
+int cmdg_mesh_create_shell(const cmdg_shell_desc* desc, cmdg_mesh** out);
 int cmdg_mesh_destroy(cmdg_mesh* mesh);
 /* Sizes of a mesh. */
 int cmdg_mesh_info(const cmdg_mesh* mesh, int64_t* nelem, int* Np);

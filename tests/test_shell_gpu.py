@@ -1,0 +1,161 @@
+"""Cubed-shell (GCM) path: the curvilinear stage kernel against the oracle.
+
+* geometry: node coordinates and mass matrix equal the oracle's
+  (StackedCubedSphereTopology + equiangular warp + curl-invariant metrics);
+* FP64 tendency (Rusanov and central) within 1e-9 of the oracle, N = 3, 4;
+* discrete hydrostatic balance of the GCM rest state on the GPU
+  (test/Atmos/Model/discrete_hydrostatic_balance.jl: <= 100 eps after 100 s);
+* mixed precision: tendency within 1e-4 and 100 LSRK54 steps within 1e-5 of
+  the FP64 oracle; the full GCM workload (6 x 12 x 12 x 6 elements, N = 4,
+  30 km lid) within 1e-5 of the GPU FP64 run after 200 steps;
+* compensated sums and the Courant time step against the oracle.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import cmdg
+import oracle as O
+from cmdg import workloads
+
+pytestmark = pytest.mark.gpu
+
+R = O.EARTH["planet_radius"]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import __graft_entry__ as g
+
+    g.build()
+    torch.cuda.set_device(0)
+
+
+def shell_pair(N, nh, nv, precision="fp64", numflux="rusanov", subtract_off=True, H=30e3, noise=True):
+    om = O.OracleModel(N, shell=dict(nhorz=nh, nvert=nv, r_inner=R, r_outer=R + H), numflux=numflux,
+                       orientation="sphere", gravity=True, ref_state=True, subtract_off=subtract_off,
+                       profile="isothermal", T_surface=285.0)
+    dg = workloads.gcm_shell_model(nhorz=nh, nvert=nv, N=N, H=H, precision=precision, numerical_flux=numflux,
+                                   subtract_off=subtract_off)
+    Q0 = workloads.gcm_initial_state(dg.grid.coordinates(), seed=5)
+    if noise:
+        rng = np.random.default_rng(3)
+        Q0[:, 1:4] += rng.uniform(-0.5, 0.5, size=Q0[:, 1:4].shape)
+    return om, dg, Q0
+
+
+def rel_max(got, ref):
+    out = []
+    for s in range(5):
+        sl = slice(1, 4) if 1 <= s <= 3 else slice(s, s + 1)
+        out.append(np.abs(got[:, s] - ref[:, s]).max() / np.abs(ref[:, sl]).max())
+    return np.array(out)
+
+
+def field_rel(om, got, ref):
+    err, nrm = om.field_l2(got, ref)
+    err = np.array([err[0], np.sqrt(np.sum(err[1:4] ** 2)), err[4]])
+    nrm = np.array([nrm[0], np.sqrt(np.sum(nrm[1:4] ** 2)), nrm[4]])
+    return err / nrm
+
+
+def test_shell_geometry_matches_oracle():
+    om, dg, _ = shell_pair(4, 3, 2)
+    vg = om.vgeo
+    xyz = dg.grid.coordinates()
+    assert np.abs(xyz - vg[:, 12:15]).max() < 1e-8 * R
+    M = dg.grid.mass()
+    assert np.abs(M / vg[:, 9] - 1).max() < 1e-10
+
+
+@pytest.mark.parametrize("numflux", ["rusanov", "central"])
+@pytest.mark.parametrize("N", [3, 4])
+def test_shell_fp64_tendency_matches_oracle(N, numflux):
+    om, dg, Q0 = shell_pair(N, 2, 3, numflux=numflux)
+    ref = om.tendency(Q0)
+    Q = dg.init_ode_state(Q0)
+    dQ = dg.new_state(torch.float64)
+    dg(dQ, Q, None, 0.0)
+    err = rel_max(dQ.cpu().numpy(), ref)
+    assert (err < 1e-9).all(), err
+    assert dg.status_word() == 0
+
+
+def test_shell_gcm_rest_state_stays_balanced_on_gpu():
+    # GCM configuration of discrete_hydrostatic_balance.jl: 3 x 3 horizontal
+    # elements per panel, 3 vertical, 50 km lid, N = 4, central flux,
+    # subtract_off = false, IsothermalProfile, 100 s at Courant 0.1
+    dg = workloads.gcm_shell_model(nhorz=3, nvert=3, N=4, H=50e3, numerical_flux="central", subtract_off=False,
+                                   T_ref=290.0)
+    ref = dg.reference_state()
+    Q0 = np.zeros((dg.grid.nelem, 5, dg.grid.Np))
+    Q0[:, 0] = ref[:, 0]
+    Q0[:, 4] = ref[:, 1]
+    Q = dg.init_ode_state(Q0)
+    dt = dg.courant_dt(Q, 0.1)
+    nsteps = math.ceil(100.0 / dt)
+    lsrk = cmdg.LSRK54CarpenterKennedy(dg, Q, dt=100.0 / nsteps)
+    cmdg.dostep_(Q, lsrk, None, 0.0, nsteps=nsteps)
+    Qg = torch.from_numpy(Q0).cuda()
+    err = cmdg.euclidean_distance(dg, Q, Qg) / cmdg.norm(dg, Qg)
+    assert err <= 100 * np.finfo(np.float64).eps, err
+
+
+@pytest.mark.parametrize("N", [3, 4])
+def test_shell_mixed_tendency_close_to_oracle(N):
+    om, dg, Q0 = shell_pair(N, 2, 3, precision="mixed")
+    ref = om.tendency(Q0)
+    Qp = dg.init_ode_state(Q0)
+    dQ = dg.new_state(torch.float64)
+    dg(dQ, Qp, None, 0.0)
+    got = dQ.cpu().numpy()
+    err = [np.linalg.norm(got[:, s] - ref[:, s]) / np.linalg.norm(ref[:, s]) for s in range(5)]
+    assert max(err) < 1e-4, err
+
+
+def test_shell_mixed_100_steps_within_1e5_of_fp64_oracle():
+    om, dg, Q0 = shell_pair(4, 3, 3, precision="mixed", noise=False)
+    dt = om.courant_dt(Q0, 0.4)
+    Qo, _ = om.lsrk54(Q0.copy(), dt, 100)
+    Qp = dg.init_ode_state(Q0)
+    lsrk = cmdg.LSRK54CarpenterKennedy(dg, Qp, dt=dt)
+    cmdg.dostep_(Qp, lsrk, None, 0.0, nsteps=100)
+    rel = field_rel(om, dg.from_perturbation(Qp).cpu().numpy(), Qo)
+    assert (rel < 1e-5).all(), rel
+    assert dg.status_word() == 0
+
+
+def test_shell_sums_and_courant_match_oracle():
+    om, dg, Q0 = shell_pair(3, 2, 2)
+    Q = dg.init_ode_state(Q0)
+    sums = dg.weighted_sums(Q, (0, 4))
+    assert sums[0] == pytest.approx(om.weightedsum(Q0, 0), rel=1e-13)
+    assert sums[1] == pytest.approx(om.weightedsum(Q0, 4), rel=1e-13)
+    assert dg.courant_dt(Q, 0.4) == pytest.approx(om.courant_dt(Q0, 0.4), rel=1e-10)
+
+
+def test_gcm_workload_mixed_200_steps_within_1e5_of_fp64():
+    """The GCM workload: 6 x 12 x 12 x 6 elements, N = 4, 30 km lid,
+    isothermal 285 K, seeded zonal wind and 1 K anomaly; mixed vs FP64 on the
+    GPU after 200 LSRK54 steps at CFL 0.4."""
+    d64 = workloads.gcm_shell_model(precision="fp64")
+    dmx = workloads.gcm_shell_model(precision="mixed")
+    Q0 = workloads.gcm_initial_state(d64.grid.coordinates())
+    Q64 = d64.init_ode_state(Q0)
+    dt = d64.courant_dt(Q64, 0.4)
+    l64 = cmdg.LSRK54CarpenterKennedy(d64, Q64, dt=dt)
+    cmdg.dostep_(Q64, l64, None, 0.0, nsteps=200)
+    Qp = dmx.init_ode_state(Q0)
+    lmx = cmdg.LSRK54CarpenterKennedy(dmx, Qp, dt=dt)
+    cmdg.dostep_(Qp, lmx, None, 0.0, nsteps=200)
+    got = dmx.from_perturbation(Qp)
+    M = torch.from_numpy(d64.grid.mass()).cuda()
+    rel = []
+    for sl in (slice(0, 1), slice(1, 4), slice(4, 5)):
+        err = torch.sqrt((M[:, None] * (got[:, sl] - Q64[:, sl]) ** 2).sum())
+        ref = torch.sqrt((M[:, None] * Q64[:, sl] ** 2).sum())
+        rel.append(float(err / ref))
+    assert max(rel) < 1e-5, rel
+    assert d64.status_word() == 0 and dmx.status_word() == 0
