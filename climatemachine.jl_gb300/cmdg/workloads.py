@@ -13,6 +13,8 @@ nodes in the same way, src/Numerics/DGMethods/SpaceDiscretization.jl:79-148).
   (the structure of experiments/TestCase/risingbubble.jl:23-91).
 * ``gcm_initial_state``: isothermal hydrostatic atmosphere on the cubed shell
   with a seeded zonal wind and a Gaussian temperature anomaly.
+* ``les_initial_state``: stably stratified box with a seeded divergence-free
+  k^-5/3 velocity field (SmagorinskyLilly LES).
 """
 from __future__ import annotations
 
@@ -148,4 +150,62 @@ def gcm_initial_state(xyz: np.ndarray, *, seed=2024, T_ref=285.0, u_max=30.0, dT
     Q[:, 1] = rho * (-np.sin(lon) * u)
     Q[:, 2] = rho * (np.cos(lon) * u)
     Q[:, 4] = rho * (cv * (T - T0) + 0.5 * u * u + g * z)
+    return Q
+
+
+def les_model(ne=(32, 32, 16), N=4, L=(3200.0, 3200.0, 1600.0), precision="fp64", theta0=300.0):
+    """Compressible Navier-Stokes LES: SmagorinskyLilly (C_s = 0.21) on a
+    brick periodic in x and y with FreeSlip/Insulating walls in z (a stratified
+    state needs them), FlatOrientation + Gravity,
+    HydrostaticState(DryAdiabaticProfile(theta0)), Rusanov flux."""
+    grid = BrickGrid(N, ne, (0.0, 0.0, 0.0), L, periodicity=(True, True, False), boundary=((0, 0), (0, 0), (1, 2)))
+    model = AtmosModel(orientation="flat", gravity=True,
+                       ref_state=HydrostaticState(DryAdiabaticProfile(theta0, 0.0), subtract_off=True),
+                       turbulence="smagorinsky", C_smag=EARTH["C_smag"])
+    return DGModel(model, grid, numerical_flux="rusanov", precision=precision)
+
+
+def les_initial_state(xyz: np.ndarray, L=(3200.0, 3200.0, 1600.0), *, seed=2024, theta0=300.0, N_bv=0.01,
+                      u_rms=1.0, nmodes=48, consts=EARTH) -> np.ndarray:
+    """Stably stratified (Brunt-Vaisala frequency N_bv) hydrostatic state,
+    theta = theta0 exp(N_bv^2 z / g) with the matching Exner pressure, plus a
+    seeded divergence-free velocity: the curl of a vector potential summed
+    over nmodes Fourier modes periodic in x and y, amplitudes following a
+    k^-5/3 energy spectrum, scaled to an rms speed u_rms."""
+    R_d, cp, cv, T0, g, p0 = (consts[k] for k in ("R_d", "cp_d", "cv_d", "T_0", "grav", "MSLP"))
+    rng = np.random.default_rng(seed)
+    x, y, z = xyz[:, 0], xyz[:, 1], xyz[:, 2]
+    u = np.zeros_like(x)
+    v = np.zeros_like(x)
+    w = np.zeros_like(x)
+    for _ in range(nmodes):
+        n = rng.integers(1, 9, size=2) * rng.choice([-1, 1], size=2)
+        kz = float(rng.uniform(0.5, 8.0)) * np.pi / L[2]
+        kv = np.array([2 * np.pi * n[0] / L[0], 2 * np.pi * n[1] / L[1], kz])
+        kmag = float(np.linalg.norm(kv))
+        a = rng.normal(size=3)
+        a -= kv * (a @ kv) / kmag**2  # potential amplitude normal to k
+        a *= kmag ** (-5.0 / 6.0 - 1.0) / np.linalg.norm(a)  # |u_k| ~ k^(-5/6): E(k) ~ k^-5/3
+        ph = float(rng.uniform(0, 2 * np.pi))
+        arg = kv[0] * x + kv[1] * y + kv[2] * z + ph
+        c = np.cos(arg)
+        # u = curl(a sin(k.x + phase)) = (k x a) cos(k.x + phase)
+        cr = np.cross(kv, a)
+        u += cr[0] * c
+        v += cr[1] * c
+        w += cr[2] * c
+    scale = u_rms / np.sqrt(np.mean(u * u + v * v + w * w))
+    u, v, w = u * scale, v * scale, w * scale
+    S = N_bv**2 / g
+    th = theta0 * np.exp(S * z)
+    # hydrostatic Exner function for theta(z): dpi/dz = -g / (cp theta)
+    pi_ex = 1.0 + g / (cp * theta0 * S) * (np.exp(-S * z) - 1.0)
+    rho = p0 / (R_d * th) * pi_ex ** (cv / R_d)
+    T = th * pi_ex
+    Q = np.zeros((xyz.shape[0], 5, xyz.shape[2]))
+    Q[:, 0] = rho
+    Q[:, 1] = rho * u
+    Q[:, 2] = rho * v
+    Q[:, 3] = rho * w
+    Q[:, 4] = rho * (cv * (T - T0) + 0.5 * (u * u + v * v + w * w) + g * z)
     return Q

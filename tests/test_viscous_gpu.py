@@ -110,3 +110,27 @@ def test_mixed_viscous_close_to_fp64_oracle(turb, kw):
     err = np.array([err[0], np.sqrt(np.sum(err[1:4] ** 2)), err[4]])
     refn = np.array([refn[0], np.sqrt(np.sum(refn[1:4] ** 2)), refn[4]])
     assert (err / refn < 1e-5).all(), err / refn
+
+
+def test_les_workload_mixed_100_steps_within_1e5_of_fp64():
+    """The Smagorinsky LES workload: 32 x 32 x 16 elements, N = 4, stable
+    stratification N_bv = 0.01 1/s, seeded divergence-free k^-5/3 velocity of
+    rms 1 m/s; mixed vs FP64 on the GPU after 100 LSRK54 steps at CFL 0.4."""
+    from cmdg import workloads
+
+    d64 = workloads.les_model(precision="fp64")
+    dmx = workloads.les_model(precision="mixed")
+    Q0 = workloads.les_initial_state(d64.grid.coordinates())
+    Qa = d64.init_ode_state(Q0)
+    dt = d64.courant_dt(Qa, 0.4)
+    Qb = dmx.init_ode_state(Q0)
+    cmdg.dostep_(Qa, cmdg.LSRK54CarpenterKennedy(d64, Qa, dt=dt), None, 0.0, nsteps=100)
+    cmdg.dostep_(Qb, cmdg.LSRK54CarpenterKennedy(dmx, Qb, dt=dt), None, 0.0, nsteps=100)
+    got = dmx.from_perturbation(Qb)
+    M = torch.from_numpy(d64.grid.mass()).cuda()
+    rel = []
+    for sl in (slice(0, 1), slice(1, 4), slice(4, 5)):
+        err = torch.sqrt((M[:, None] * (got[:, sl] - Qa[:, sl]) ** 2).sum())
+        rel.append(float(err / torch.sqrt((M[:, None] * Qa[:, sl] ** 2).sum())))
+    assert max(rel) < 1e-5, rel
+    assert d64.status_word() == 0 and dmx.status_word() == 0
