@@ -24,6 +24,17 @@ cpu_baseline  the C++ oracle (the CPU restatement of the reference) on the
 --impl reference times the reference's CPU path (the oracle port, the
 reference itself is Julia and cannot run here) on the same workload.
 
+--workload selects another configuration for the same measurement (the
+default, the line the benchmark contract reads, is the bubble above):
+  gcm       cubed-shell GCM, 6 x 12 x 12 x 6 elements, N=4 (648,000 nodes),
+            30 km lid, isothermal 285 K, seeded zonal wind + 1 K anomaly;
+            algorithmic bytes 224 (mixed) / 264 (FP64) per node-stage
+  les       SmagorinskyLilly LES, 32 x 32 x 16 elements, N=4 (2,048,000
+            nodes), N_bv = 0.01 1/s, seeded k^-5/3 velocity; 200 / 320 B
+  ensemble  64 seeded rising-bubble members of 8^3..16^3 elements and
+            N = 3..5, mixed; batched (one graph of per-order launches) vs
+            64 sequential single-member solves
+
 Multi-GPU: replicas only — each rank advances its own bubble; value is the
 sum over ranks of the work divided by the slowest rank's time.
 """
@@ -55,6 +66,89 @@ BYTES_FP64 = 2 * 5 * 8 + 2 * 5 * 8
 WORKLOAD = ("rising bubble: 20x20x20 elements, N=4 (1e6 nodes, 5e6 DOF), [0,2500 m]^3, periodic x/y, "
             "FreeSlip walls z, dry Euler + gravity, HydrostaticState(DryAdiabatic 300 K), +2 K cos^2 bubble "
             "r=250 m at z=350 m, Rusanov, LSRK54 at CFL 0.4")
+
+
+WORKLOADS = {
+    "bubble": dict(desc=WORKLOAD, bytes_mixed=BYTES_MIXED, bytes_fp64=BYTES_FP64, launches_per_stage=1,
+                   kernel="stage_kernel<4,float,mixed,stage>", profile="stage_kernel_mixed_bubble20.md"),
+    "gcm": dict(desc="cubed-shell GCM: 6x12x12x6 elements, N=4 (648,000 nodes), R=6.371e6 m, 30 km lid, walls, "
+                     "SphericalOrientation + gravity, HydrostaticState(Isothermal 285 K), seeded zonal wind 0-30 m/s "
+                     "+ 1 K Gaussian anomaly, Rusanov, LSRK54 at CFL 0.4",
+                bytes_mixed=224, bytes_fp64=264, launches_per_stage=1,
+                kernel="shell_stage_kernel<4,float,mixed,stage>", profile="shell_stage_kernel_mixed_gcm.md"),
+    "les": dict(desc="SmagorinskyLilly LES: 32x32x16 elements, N=4 (2,048,000 nodes), 3200x3200x1600 m, periodic "
+                     "x/y, walls z, N_bv=0.01 1/s, seeded k^-5/3 velocity rms 1 m/s, Rusanov, LSRK54 at CFL 0.4",
+                bytes_mixed=200, bytes_fp64=320, launches_per_stage=2,
+                kernel="viscous_stage_kernel<4,float,mixed,stage,smagorinsky>", profile="none"),
+}
+
+
+def bench_ensemble(args, cmdg, workloads, torch, barrier, stream, flush):
+    """64 seeded bubble members (8^3..16^3 elements, N = 3..5), mixed:
+    batched steps (one CUDA graph per call of per-order tile-walking launches)
+    against 64 sequential single-member solves (each member autotuned, one
+    graph-captured call per member)."""
+    specs = workloads.bubble_ensemble_specs(n=64)
+    pairs = [workloads.bubble_member(s) for s in specs]
+    dgs = [p[0] for p in pairs]
+    Q0s = [dg.init_ode_state(Q0) for dg, Q0 in pairs]
+    dts = [dg.courant_dt(dg.from_perturbation(Q), CFL) for dg, Q in zip(dgs, Q0s)]
+    nodes = sum(dg.grid.nelem * dg.grid.Np for dg in dgs)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        barrier()
+        ms = []
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            ms.append((a, b))
+        barrier()
+        return sum(a.elapsed_time(b) for a, b in ms)
+
+    Qs = [Q.clone() for Q in Q0s]
+    lsrks = [cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt) for dg, Q, dt in zip(dgs, Qs, dts)]
+    for dg in dgs:
+        dg.autotune(reps=3)
+
+    def seq():
+        for Q, lsrk in zip(Qs, lsrks):
+            cmdg.dostep_(Q, lsrk, None, 0.0)
+
+    ens = cmdg.Ensemble(dgs)
+    Qe = [Q.clone() for Q in Q0s]
+    dQe = [torch.zeros(Q.shape, dtype=torch.float64, device="cuda") for Q in Qe]
+    _, tiling = ens.autotune(Qe, dQe, reps=5)
+
+    def bat():
+        ens.lsrk54_step(Qe, dQe, dts, nsteps=1)
+
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        ms_b = timed(bat)
+    ms_s = timed(seq)
+    work = NFIELD * nodes * NSTAGE * args.steps
+    peak, peak_kind = measured_peak()
+    ach = BYTES_MIXED * nodes / (ms_b / args.steps / NSTAGE * 1e-3) / 1e9
+    line = {"metric": "DOF-stage updates/s", "value": work / (ms_b * 1e-3), "unit": "DOF-stage/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_b / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": "64-member rising-bubble ensemble, elements U{8..16}^3, N U{3,4,5}, amplitude "
+                                   "U[0.5,3] K, radius U[150,400] m, mixed", "nodes": nodes,
+                       "tiling": {str(k): v for k, v in tiling.items()},
+                       "l2": "256 MiB buffer written between timed steps"},
+            "sequential": {"value": work / (ms_s * 1e-3), "ms_per_step": ms_s / args.steps},
+            "speedup_vs_sequential": ms_s / ms_b,
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "peak_source": peak_kind, "kernel": "batch_stage_kernel<N>", "bytes_per_node_stage":
+                         BYTES_MIXED},
+            "gpu_launches": args.steps * NSTAGE * 3, "clocks": clk.summary()}
+    print(json.dumps(line))
+    return 0
 
 
 def measured_peak():
@@ -145,6 +239,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="cmdg", choices=["cmdg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="bubble", choices=["bubble", "gcm", "les", "ensemble"])
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -190,7 +285,18 @@ def main():
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
+    if args.workload == "ensemble":
+        return bench_ensemble(args, cmdg, workloads, torch, barrier, stream, flush)
+
+    spec = WORKLOADS[args.workload]
+
     def build(precision):
+        if args.workload == "gcm":
+            dg = workloads.gcm_shell_model(precision=precision)
+            return dg, workloads.gcm_initial_state(dg.grid.coordinates())
+        if args.workload == "les":
+            dg = workloads.les_model(precision=precision)
+            return dg, workloads.les_initial_state(dg.grid.coordinates())
         dg = workloads.bubble_model(ne=NE, N=N, L=L, precision=precision)
         xyz = dg.grid.coordinates()
         Q0 = workloads.rising_bubble(xyz, theta0=300.0, amp=2.0, rc=250.0, center=(1250.0, 1250.0, 350.0))
@@ -267,10 +373,10 @@ def main():
     peak, peak_kind = measured_peak()
     stage_ms_mx = ms_mx / args.steps / NSTAGE
     stage_ms_64 = ms_64 / args.steps / NSTAGE
-    ach_mx = BYTES_MIXED * nodes / (stage_ms_mx * 1e-3) / 1e9
-    ach_64 = BYTES_FP64 * nodes / (stage_ms_64 * 1e-3) / 1e9
+    ach_mx = spec["bytes_mixed"] * nodes / (stage_ms_mx * 1e-3) / 1e9
+    ach_64 = spec["bytes_fp64"] * nodes / (stage_ms_64 * 1e-3) / 1e9
     traffic = None
-    tpath = os.path.join(REPO, "profiles", "stage_kernel_mixed_bubble20.md")
+    tpath = os.path.join(REPO, "profiles", spec["profile"])
     if os.path.exists(tpath):
         for line in open(tpath):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -280,7 +386,7 @@ def main():
                     traffic = None
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and args.workload == "bubble":
         try:
             r = run_cpu_reference(1, sample_steps=2)
             cpu = {"value": r["value"], "unit": "DOF-stage/s", "cores": r["threads"], "kind": "port",
@@ -294,7 +400,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mx / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "path": "mixed FP32 perturbation / FP64 RK register",
+            "config": {"workload": spec["desc"], "path": "mixed FP32 perturbation / FP64 RK register",
                        "l2": "256 MiB buffer written between timed steps (L2 is 129 MB)",
                        "parallelism": f"replicas x{world}", "dt": dt},
             "fp64": {"value": v64, "ms_per_step": ms_64 / args.steps,
@@ -305,11 +411,11 @@ def main():
             "mixed_vs_fp64_rel_l2": rel,
             "roofline": {"bound": "hbm", "achieved": ach_mx, "peak": peak, "unit": "GB/s", "frac": ach_mx / peak,
                          "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "stage_kernel<4,float,mixed,stage>", "bytes_per_node_stage": BYTES_MIXED},
+                         "kernel": spec["kernel"], "bytes_per_node_stage": spec["bytes_mixed"]},
             "cpu_baseline": cpu,
             "e2e": {"value": ve2e, "unit": "DOF-stage/s", "h2d_bytes_per_step": int(host.numel() * 8),
                     "d2h_bytes_per_step": int(host.numel() * 8)},
-            "gpu_launches": args.steps * NSTAGE,
+            "gpu_launches": args.steps * NSTAGE * spec["launches_per_stage"],
             "clocks": clk.summary(),
         }
         print(json.dumps(line))
