@@ -227,6 +227,65 @@ __device__ __forceinline__ void normal_flux(const R q[NSTATE], const Thermo<R, M
 }
 
 
+// Planar shared-memory records of five fields for n nodes: fields 0..3 in a
+// plane of 16-byte vectors (float4; two double2 planes in FP64) and field 4
+// in a scalar plane.  A warp reading or writing consecutive records touches
+// consecutive 16-byte (and 4/8-byte) words, so the accesses are free of bank
+// conflicts; a record still moves with one 128-bit and one 32-bit access in
+// FP32.  Plane offsets are kept 16-byte aligned (planar_words).
+template <typename R>
+struct Planar5;
+template <>
+struct Planar5<float> {
+    static __device__ __forceinline__ void ld(const float* base, int n, int i, float v[NSTATE]) {
+        const float4 a = reinterpret_cast<const float4*>(base)[i];
+        v[0] = a.x;
+        v[1] = a.y;
+        v[2] = a.z;
+        v[3] = a.w;
+        v[4] = base[4 * n + i];
+    }
+    static __device__ __forceinline__ void st(float* base, int n, int i, const float v[NSTATE]) {
+        reinterpret_cast<float4*>(base)[i] = make_float4(v[0], v[1], v[2], v[3]);
+        base[4 * n + i] = v[4];
+    }
+};
+template <>
+struct Planar5<double> {
+    static __device__ __forceinline__ void ld(const double* base, int n, int i, double v[NSTATE]) {
+        const double2 a = reinterpret_cast<const double2*>(base)[i];
+        const double2 b = reinterpret_cast<const double2*>(base + 2 * n)[i];
+        v[0] = a.x;
+        v[1] = a.y;
+        v[2] = b.x;
+        v[3] = b.y;
+        v[4] = base[4 * n + i];
+    }
+    static __device__ __forceinline__ void st(double* base, int n, int i, const double v[NSTATE]) {
+        reinterpret_cast<double2*>(base)[i] = make_double2(v[0], v[1]);
+        reinterpret_cast<double2*>(base + 2 * n)[i] = make_double2(v[2], v[3]);
+        base[4 * n + i] = v[4];
+    }
+};
+// words of R taken by `words` words rounded up to 16 bytes
+template <typename R>
+constexpr int planar_pad(int words) {
+    return (int)(((size_t)words * sizeof(R) + 15) / 16 * 16 / sizeof(R));
+}
+// pair of values per node (sound speed, 1/rho) as an 8- or 16-byte vector plane
+template <typename R>
+struct Pair;
+template <>
+struct Pair<float> {
+    using V = float2;
+    static __device__ __forceinline__ V make(float a, float b) { return make_float2(a, b); }
+};
+template <>
+struct Pair<double> {
+    using V = double2;
+    static __device__ __forceinline__ V make(double a, double b) { return make_double2(a, b); }
+};
+
 // Shared-memory record of one node or face node: the five fields packed
 // contiguously (plus two spare slots) so a record moves with 128-bit accesses.
 template <typename R>

@@ -45,11 +45,14 @@ struct ShellDims {
 
 template <int N, typename R>
 struct ShellSmem {
-    static constexpr int Nq = N + 1, Np = Nq * Nq * Nq, Nfp = Nq * Nq, W = Slot<R>::W;
+    static constexpr int Nq = N + 1, Np = Nq * Nq * Nq, Nfp = Nq * Nq;
+    // planar five-field records (Planar5) as in the brick kernel
+    static constexpr int P5N = planar_pad<R>(5 * Np);
     static constexpr int NODE = 0;
-    static constexpr int FLUX = NODE + Np * W;
-    static constexpr int FACE = FLUX + 3 * Np * W;
-    static constexpr int DMAT = FACE + 6 * Nfp * W;
+    static constexpr int CR = NODE + P5N;
+    static constexpr int FLUX = CR + planar_pad<R>(2 * Np);
+    static constexpr int FACE = FLUX + 3 * P5N;
+    static constexpr int DMAT = FACE + planar_pad<R>(5 * 6 * Nfp);
     static constexpr int TOTAL = DMAT + Nq * Nq;
     static constexpr size_t BYTES = sizeof(R) * TOTAL;
 };
@@ -59,11 +62,14 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
     shell_stage_kernel(const KParams P) {
     using Dm = ShellDims<N>;
     using SM = ShellSmem<N, R>;
-    constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, W = SM::W;
+    constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, NFN = 6 * Nfp;
     constexpr int ESTRIDE = NSTATE * Np, GSTRIDE = KG_NFIELDS * Np;
+    using PL = Planar5<R>;
+    using CRV = typename Pair<R>::V;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* const sm = reinterpret_cast<R*>(smem_raw);
     R* const s_node = sm + SM::NODE;
+    CRV* const s_cr = reinterpret_cast<CRV*>(sm + SM::CR);
     R* const s_F = sm + SM::FLUX;
     R* const s_fs = sm + SM::FACE;
     R* const s_D = sm + SM::DMAT;
@@ -122,10 +128,8 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
         }
         if (!MIXED) lv.crho += ge[KG_DCRHO * Np + t];
         const Thermo<R, MIXED> th = thermo<R, MIXED>(q, lv, P);
-        R* rec = s_node + t * W;
-        st5<R>(rec, q);
-        rec[5] = th.c;
-        rec[6] = th.rinv;
+        PL::st(s_node, Np, t, q);
+        s_cr[t] = Pair<R>::make(th.c, th.rinv);
         R F0[NSTATE], F1[NSTATE], F2[NSTATE];
 #pragma unroll
         for (int s = 0; s < NSTATE; ++s) {
@@ -138,7 +142,7 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
             R Ft[NSTATE];
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) Ft[s] = Jx[d * 3 + 0] * F0[s] + Jx[d * 3 + 1] * F1[s] + Jx[d * 3 + 2] * F2[s];
-            st5<R>(s_F + (d * Np + t) * W, Ft);
+            PL::st(s_F + d * SM::P5N, Np, t, Ft);
         }
         if (ph.gravity) {
             const R rho_s = MIXED ? ((ph.ref_state && ph.subtract_off) ? q[0] : lv.rho_ref + q[0])
@@ -159,10 +163,10 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
         const R rs = rcp_r(sJ);
         const R nv[3] = {sgn * j0 * rs, sgn * j1 * rs, sgn * j2 * rs};
         R qm[NSTATE], Fm[NSTATE], qp[NSTATE], Fp[NSTATE], jr[NSTATE] = {0, 0, 0, 0, 0};
-        const R* rec = s_node + vM * W;
-        ld5<R>(rec, qm);
-        const R c_m = rec[5], ri_m = rec[6];
-        ld5<R>(s_F + (fd * Np + vM) * W, Fm);
+        PL::ld(s_node, Np, vM, qm);
+        const CRV cr = s_cr[vM];
+        const R c_m = cr.x, ri_m = cr.y;
+        PL::ld(s_F + fd * SM::P5N, Np, vM, Fm);
 #pragma unroll
         for (int s = 0; s < NSTATE; ++s) Fm[s] *= sgn * rs;
         const R mn_m = qm[1] * nv[0] + qm[2] * nv[1] + qm[3] * nv[2];
@@ -231,7 +235,7 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
         R fs[NSTATE];
 #pragma unroll
         for (int s = 0; s < NSTATE; ++s) fs[s] = hl * (Fm[s] + Fp[s]) + pl * ((qm[s] - qp[s]) + jr[s]);
-        st5<R>(s_fs + (f * Nfp + fn) * W, fs);
+        PL::st(s_fs, NFN, f * Nfp + fn, fs);
     }
     __syncthreads();
 
@@ -239,15 +243,13 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
     int bad = 0;
     if (node_thread) {
         R acc[NSTATE] = {0, 0, 0, 0, 0};
-        const R* F1 = s_F + (0 * Np + Nq * (nj + Nq * nk)) * W;
-        const R* F2 = s_F + (1 * Np + ni + Nfp * nk) * W;
-        const R* F3 = s_F + (2 * Np + ni + Nq * nj) * W;
+        const int L1 = Nq * (nj + Nq * nk), L2 = ni + Nfp * nk, L3 = ni + Nq * nj;
 #pragma unroll
         for (int n = 0; n < Nq; ++n) {
             R v1[NSTATE], v2[NSTATE], v3[NSTATE];
-            ld5<R>(F1 + n * W, v1);
-            ld5<R>(F2 + n * Nq * W, v2);
-            ld5<R>(F3 + n * Nfp * W, v3);
+            PL::ld(s_F, Np, L1 + n, v1);
+            PL::ld(s_F + SM::P5N, Np, L2 + n * Nq, v2);
+            PL::ld(s_F + 2 * SM::P5N, Np, L3 + n * Nfp, v3);
             const R d1 = s_D[ni * Nq + n], d2 = s_D[nj * Nq + n], d3 = s_D[nk * Nq + n];
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) acc[s] = fma(d1, v1[s], fma(d2, v2[s], fma(d3, v3[s], acc[s])));
@@ -257,7 +259,7 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
         for (int s = 0; s < NSTATE; ++s) rhs[s] = invJ * acc[s];
         auto sub_face = [&](int ff, int idx) {
             R v[NSTATE];
-            ld5<R>(s_fs + (ff * Nfp + idx) * W, v);
+            PL::ld(s_fs, NFN, ff * Nfp + idx, v);
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) rhs[s] -= v[s];
         };

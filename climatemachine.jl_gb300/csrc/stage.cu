@@ -65,14 +65,15 @@ struct Dims {
 
 template <int N, typename R>
 struct Smem {
-    static constexpr int Nq = N + 1, Np = Nq * Nq * Nq, Nfp = Nq * Nq, W = Slot<R>::W;
-    // node records: q (5), sound speed (slot 5), 1/rho (slot 6)
+    static constexpr int Nq = N + 1, Np = Nq * Nq * Nq, Nfp = Nq * Nq;
+    // planar five-field records (Planar5): node states, volume fluxes by
+    // direction, lifted face fluxes; (sound speed, 1/rho) pairs per node
+    static constexpr int P5N = planar_pad<R>(5 * Np);      // one five-field plane set over the nodes
     static constexpr int NODE = 0;
-    // volume fluxes by direction
-    static constexpr int FLUX = NODE + Np * W;
-    // lifted face fluxes
-    static constexpr int FACE = FLUX + 3 * Np * W;
-    static constexpr int DMAT = FACE + 6 * Nfp * W;
+    static constexpr int CR = NODE + P5N;
+    static constexpr int FLUX = CR + planar_pad<R>(2 * Np);
+    static constexpr int FACE = FLUX + 3 * P5N;
+    static constexpr int DMAT = FACE + planar_pad<R>(5 * 6 * Nfp);
     static constexpr int TOTAL = DMAT + Nq * Nq;
     static constexpr size_t BYTES = sizeof(R) * TOTAL;
 };
@@ -97,10 +98,13 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
                                            int e_end) {
     using Dm = Dims<N>;
     using SM = Smem<N, R>;
-    constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, W = SM::W;
+    constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, NFN = 6 * Nfp;
     constexpr int ESTRIDE = NSTATE * Np;  // elements of R (or double) per element
+    using PL = Planar5<R>;
+    using CRV = typename Pair<R>::V;
     R* const sm = reinterpret_cast<R*>(smem_raw);
     R* const s_node = sm + SM::NODE;
+    CRV* const s_cr = reinterpret_cast<CRV*>(sm + SM::CR);
     R* const s_F = sm + SM::FLUX;
     R* const s_fs = sm + SM::FACE;
     R* const s_D = sm + SM::DMAT;
@@ -172,16 +176,14 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
         if (node_thread) {
             const Level<R> lv = load_level<R>(P, ez * Nq + nk);
             const Thermo<R, MIXED> th = thermo<R, MIXED>(cur.q, lv, P);
-            R* rec = s_node + t * W;
-            st5<R>(rec, cur.q);
-            rec[5] = th.c;
-            rec[6] = th.rinv;
+            PL::st(s_node, Np, t, cur.q);
+            s_cr[t] = Pair<R>::make(th.c, th.rinv);
 #pragma unroll
             for (int dd = 0; dd < 3; ++dd) {
                 R F[NSTATE];
 #pragma unroll
                 for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(cur.q, th, dd, s);
-                st5<R>(s_F + (dd * Np + t) * W, F);
+                PL::st(s_F + dd * SM::P5N, Np, t, F);
             }
             if (ph.gravity) {
                 R rho_s = MIXED ? ((ph.ref_state && ph.subtract_off) ? cur.q[0] : lv.rho_ref + cur.q[0])
@@ -194,10 +196,10 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
         // ---------------- phase 2: one numerical flux per face node
         if (face_thread) {
             R qm[NSTATE], Fm[NSTATE], Fp[NSTATE], qp[NSTATE], jr[NSTATE] = {0, 0, 0, 0, 0};
-            const R* rec = s_node + vM * W;
-            ld5<R>(rec, qm);
-            const R c_m = rec[5], ri_m = rec[6];
-            ld5<R>(s_F + (fd * Np + vM) * W, Fm);
+            PL::ld(s_node, Np, vM, qm);
+            const CRV cr = s_cr[vM];
+            const R c_m = cr.x, ri_m = cr.y;
+            PL::ld(s_F + fd * SM::P5N, Np, vM, Fm);
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) Fm[s] *= sgn;
             const R lam_m = fabs(pick3(fd, qm[1], qm[2], qm[3]) * ri_m) + c_m;
@@ -235,7 +237,7 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
             R fs[NSTATE];
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) fs[s] = hl * (Fm[s] + Fp[s]) + pl * ((qm[s] - qp[s]) + jr[s]);
-            st5<R>(s_fs + (f * Nfp + fn) * W, fs);
+            PL::st(s_fs, NFN, f * Nfp + fn, fs);
         }
         __syncthreads();
 
@@ -243,15 +245,15 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
         int bad = 0;
         if (node_thread) {
             R acc1[NSTATE] = {0, 0, 0, 0, 0}, acc2[NSTATE] = {0, 0, 0, 0, 0}, acc3[NSTATE] = {0, 0, 0, 0, 0};
-            const R* F1 = s_F + (0 * Np + Nq * (nj + Nq * nk)) * W;  // line along xi1
-            const R* F2 = s_F + (1 * Np + ni + Nfp * nk) * W;        // line along xi2 (stride Nq)
-            const R* F3 = s_F + (2 * Np + ni + Nq * nj) * W;         // line along xi3 (stride Nfp)
+            const int L1 = Nq * (nj + Nq * nk);  // line along xi1 (stride 1)
+            const int L2 = ni + Nfp * nk;        // line along xi2 (stride Nq)
+            const int L3 = ni + Nq * nj;         // line along xi3 (stride Nfp)
 #pragma unroll
             for (int n = 0; n < Nq; ++n) {
                 R v1[NSTATE], v2[NSTATE], v3[NSTATE];
-                ld5<R>(F1 + n * W, v1);
-                ld5<R>(F2 + n * Nq * W, v2);
-                ld5<R>(F3 + n * Nfp * W, v3);
+                PL::ld(s_F, Np, L1 + n, v1);
+                PL::ld(s_F + SM::P5N, Np, L2 + n * Nq, v2);
+                PL::ld(s_F + 2 * SM::P5N, Np, L3 + n * Nfp, v3);
                 const R d1 = s_D[ni * Nq + n], d2 = s_D[nj * Nq + n], d3 = s_D[nk * Nq + n];
 #pragma unroll
                 for (int s = 0; s < NSTATE; ++s) {
@@ -266,7 +268,7 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
             // face terms (vMI sM F*, lifted in phase 2), in face order 1..6
             auto sub_face = [&](int ff, int idx) {
                 R v[NSTATE];
-                ld5<R>(s_fs + (ff * Nfp + idx) * W, v);
+                PL::ld(s_fs, NFN, ff * Nfp + idx, v);
 #pragma unroll
                 for (int s = 0; s < NSTATE; ++s) rhs[s] -= v[s];
             };
