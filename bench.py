@@ -320,6 +320,9 @@ def main():
 
     dg64, Q0 = build("fp64")
     dgmx, _ = build("mixed")
+    kernels = {}
+    for name, dg in (("fp64", dg64), ("mixed", dgmx)):
+        kernels[name] = dg.autotune(reps=10)[1]
     dt = dg64.courant_dt(dg64.init_ode_state(Q0), CFL)
     nodes = dg64.grid.nelem * dg64.grid.Np
 
@@ -402,7 +405,8 @@ def main():
             "data": "synthetic",
             "config": {"workload": spec["desc"], "path": "mixed FP32 perturbation / FP64 RK register",
                        "l2": "256 MiB buffer written between timed steps (L2 is 129 MB)",
-                       "parallelism": f"replicas x{world}", "dt": dt},
+                       "parallelism": f"replicas x{world}", "dt": dt,
+                       "stage_kernel": {k: list(v) for k, v in kernels.items()}},
             "fp64": {"value": v64, "ms_per_step": ms_64 / args.steps,
                      "roofline": {"bound": "hbm", "achieved": ach_64, "peak": peak, "unit": "GB/s",
                                   "frac": ach_64 / peak}},

@@ -193,8 +193,9 @@ class DGModel:
     # ------------------------------------------------------------------ launch configuration
     KERNELS = {"node": 0, "column": 1}
 
-    def set_kernel(self, kind: str = "node", grid_ctas: int = 0):
-        """Stage-kernel family ("node" or "column") and persistent grid size."""
+    def set_kernel(self, kind: str = "node", grid_ctas: int = -1):
+        """Stage-kernel family ("node" or "column") and grid: -1 = one CTA per
+        element (the default), 0 = one wave of resident CTAs, n > 0 = n CTAs."""
         call("cmdg_model_set_kernel", self.h, self.KERNELS[kind], int(grid_ctas))
 
     def get_kernel(self):

@@ -45,14 +45,16 @@ struct ColCfg<5> {
 
 template <int N, typename R>
 struct ColSmem {
-    static constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp, W = 8;
-    // per element: xi1 and xi2 flux records, node records (q, c, 1/rho) of
-    // the horizontal-face nodes, lifted horizontal face fluxes
+    static constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp;
+    // per element, planar five-field records (Planar5): xi1 and xi2 fluxes,
+    // states and (c, 1/rho) of the horizontal-face nodes, lifted horizontal
+    // face fluxes
     static constexpr int F1 = 0;
-    static constexpr int F2 = F1 + Np * W;
-    static constexpr int NODE = F2 + Np * W;
-    static constexpr int FACE = NODE + 4 * Nfp * W;
-    static constexpr int PER_ELEM = FACE + 4 * Nfp * W;
+    static constexpr int F2 = F1 + planar_pad<R>(5 * Np);
+    static constexpr int NODE = F2 + planar_pad<R>(5 * Np);
+    static constexpr int CR = NODE + planar_pad<R>(5 * 4 * Nfp);
+    static constexpr int FACE = CR + planar_pad<R>(2 * 4 * Nfp);
+    static constexpr int PER_ELEM = FACE + planar_pad<R>(5 * 4 * Nfp);
     static constexpr int DMAT = ColCfg<N>::EPB * PER_ELEM;
     static constexpr int TOTAL = DMAT + Nq * Nq;
     static constexpr size_t BYTES = sizeof(R) * TOTAL;
@@ -97,9 +99,11 @@ __device__ __forceinline__ void face_flux(const KParams& P, const R qm[NSTATE], 
 
 template <int N, typename R, bool MIXED, int MODE>
 __global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kernel(const KParams P) {
-    constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp, W = 8, EPB = ColCfg<N>::EPB;
+    constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp, EPB = ColCfg<N>::EPB, NH = 4 * Nfp;
     constexpr int ESTRIDE = NSTATE * Np;
     using CS = ColSmem<N, R>;
+    using PL = Planar5<R>;
+    using CRV = typename Pair<R>::V;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* const sm = reinterpret_cast<R*>(smem_raw);
 
@@ -113,6 +117,7 @@ __global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kerne
     R* const sF1 = sm + el * CS::PER_ELEM + CS::F1;
     R* const sF2 = sm + el * CS::PER_ELEM + CS::F2;
     R* const sNode = sm + el * CS::PER_ELEM + CS::NODE;
+    CRV* const sCR = reinterpret_cast<CRV*>(sm + el * CS::PER_ELEM + CS::CR);
     R* const sFace = sm + el * CS::PER_ELEM + CS::FACE;
     R* const sD = sm + CS::DMAT;
     const R* __restrict__ Qin = static_cast<const R*>(P.Qin);
@@ -171,28 +176,26 @@ __global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kerne
             R F[NSTATE];
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(q[k], th, 0, s);
-            st5<R>(sF1 + node * W, F);
+            PL::st(sF1, Np, node, F);
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(q[k], th, 1, s);
-            st5<R>(sF2 + node * W, F);
+            PL::st(sF2, Np, node, F);
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) F3[k][s] = flux_d<R, MIXED>(q[k], th, 2, s);
             // node records of horizontal-face nodes, at their in-face index
-            R* rec = nullptr;
-            if (ci == 0) rec = sNode + (0 * Nfp + cj + Nq * k) * W;
-            if (ci == N) rec = sNode + (1 * Nfp + cj + Nq * k) * W;
-            if (rec) {
-                st5<R>(rec, q[k]);
-                rec[5] = th.c;
-                rec[6] = th.rinv;
+            int ri = -1;
+            if (ci == 0) ri = 0 * Nfp + cj + Nq * k;
+            if (ci == N) ri = 1 * Nfp + cj + Nq * k;
+            if (ri >= 0) {
+                PL::st(sNode, NH, ri, q[k]);
+                sCR[ri] = Pair<R>::make(th.c, th.rinv);
             }
-            rec = nullptr;
-            if (cj == 0) rec = sNode + (2 * Nfp + ci + Nq * k) * W;
-            if (cj == N) rec = sNode + (3 * Nfp + ci + Nq * k) * W;
-            if (rec) {
-                st5<R>(rec, q[k]);
-                rec[5] = th.c;
-                rec[6] = th.rinv;
+            ri = -1;
+            if (cj == 0) ri = 2 * Nfp + ci + Nq * k;
+            if (cj == N) ri = 3 * Nfp + ci + Nq * k;
+            if (ri >= 0) {
+                PL::st(sNode, NH, ri, q[k]);
+                sCR[ri] = Pair<R>::make(th.c, th.rinv);
             }
             if (k == 0) {
                 c_end[0] = th.c;
@@ -268,18 +271,18 @@ __global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kerne
         for (int f = 0; f < 4; ++f) {
             const int d = f >> 1;
             const R sgn = (f & 1) ? R(1) : R(-1);
-            const R* rec = sNode + (f * Nfp + c) * W;
             R qm[NSTATE], Fm[NSTATE];
-            ld5<R>(rec, qm);
-            const R c_m = rec[5], ri_m = rec[6];
-            ld5<R>((d == 0 ? sF1 : sF2) + vMh[f] * W, Fm);
+            PL::ld(sNode, NH, f * Nfp + c, qm);
+            const CRV cr = sCR[f * Nfp + c];
+            const R c_m = cr.x, ri_m = cr.y;
+            PL::ld(d == 0 ? sF1 : sF2, Np, vMh[f], Fm);
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) Fm[s] *= sgn;
             const R lam_m = fabs(qm[1 + d] * ri_m) + c_m;
             const R jr[NSTATE] = {0, 0, 0, 0, 0};
             R fs[NSTATE];
             face_flux<R, MIXED>(P, qm, Fm, lam_m, qh[f], nbf[f] < 0, lvh, d, sgn, jr, xi[d] * inv_w0, fs);
-            st5<R>(sFace + (f * Nfp + c) * W, fs);
+            PL::st(sFace, NH, f * Nfp + c, fs);
         }
         R Di[Nq], Dj[Nq];
 #pragma unroll
@@ -290,13 +293,12 @@ __global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kerne
 #pragma unroll
         for (int k = 0; k < Nq; ++k) {
             R c1[NSTATE] = {0, 0, 0, 0, 0}, c2[NSTATE] = {0, 0, 0, 0, 0};
-            const R* L1 = sF1 + (Nq * (cj + Nq * k)) * W;
-            const R* L2 = sF2 + (ci + Nfp * k) * W;
+            const int L1 = Nq * (cj + Nq * k), L2 = ci + Nfp * k;
 #pragma unroll
             for (int n = 0; n < Nq; ++n) {
                 R v1[NSTATE], v2[NSTATE];
-                ld5<R>(L1 + n * W, v1);
-                ld5<R>(L2 + n * Nq * W, v2);
+                PL::ld(sF1, Np, L1 + n, v1);
+                PL::ld(sF2, Np, L2 + n * Nq, v2);
 #pragma unroll
                 for (int s = 0; s < NSTATE; ++s) {
                     c1[s] = fma(Di[n], v1[s], c1[s]);
@@ -315,7 +317,7 @@ __global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kerne
     for (int k = 0; k < Nq; ++k) {
         auto sub_face = [&](int f, int idx) {
             R v[NSTATE];
-            ld5<R>(sFace + (f * Nfp + idx) * W, v);
+            PL::ld(sFace, NH, f * Nfp + idx, v);
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) acc[k][s] -= v[s];
         };

@@ -1,7 +1,7 @@
 // Device-side building blocks shared by the fused stage kernels: kernel
 // parameters, precision-dependent constants, IEEE-754 conversions on the
 // integer pipe, per-level reference-state rows, dry-air thermodynamics and
-// first-order fluxes of the AtmosModel, and packed shared-memory records.
+// first-order fluxes of the AtmosModel, and planar shared-memory records.
 #pragma once
 
 #include "cmdg_internal.h"
@@ -285,49 +285,6 @@ struct Pair<double> {
     using V = double2;
     static __device__ __forceinline__ V make(double a, double b) { return make_double2(a, b); }
 };
-
-// Shared-memory record of one node or face node: the five fields packed
-// contiguously (plus two spare slots) so a record moves with 128-bit accesses.
-template <typename R>
-struct Slot {
-    static constexpr int W = 8;  // record width in elements of R
-};
-
-template <typename R>
-__device__ __forceinline__ void ld5(const R* p, R v[NSTATE]);
-template <>
-__device__ __forceinline__ void ld5<float>(const float* p, float v[NSTATE]) {
-    const float4 a = *reinterpret_cast<const float4*>(p);
-    v[0] = a.x;
-    v[1] = a.y;
-    v[2] = a.z;
-    v[3] = a.w;
-    v[4] = p[4];
-}
-template <>
-__device__ __forceinline__ void ld5<double>(const double* p, double v[NSTATE]) {
-    const double2 a = *reinterpret_cast<const double2*>(p);
-    const double2 b = *reinterpret_cast<const double2*>(p + 2);
-    v[0] = a.x;
-    v[1] = a.y;
-    v[2] = b.x;
-    v[3] = b.y;
-    v[4] = p[4];
-}
-template <typename R>
-__device__ __forceinline__ void st5(R* p, const R v[NSTATE]);
-template <>
-__device__ __forceinline__ void st5<float>(float* p, const float v[NSTATE]) {
-    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
-    p[4] = v[4];
-}
-template <>
-__device__ __forceinline__ void st5<double>(double* p, const double v[NSTATE]) {
-    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
-    *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
-    p[4] = v[4];
-}
-
 
 }  // namespace
 }  // namespace cmdg

@@ -126,13 +126,14 @@ __device__ __forceinline__ void grad_args(const KParams& P, const R q[NSTATE], c
 template <int N, typename R, bool MIXED, bool SMAG>
 __global__ void __launch_bounds__(VDims<N>::NT) gradient_kernel(const KParams P, const void* Qv, R* __restrict__ gf) {
     using Dm = VDims<N>;
-    constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, W = 8;
+    constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, NFN = 6 * Nfp;
     constexpr int ESTRIDE = NSTATE * Np;
+    using PL = Planar5<R>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    R* const s_q = reinterpret_cast<R*>(smem_raw);  // [Np][W] states
-    R* const s_G = s_q + Np * W;                       // [Np][W] gradient arguments
-    R* const s_dG = s_G + Np * W;                      // [6][Nfp][W] face terms
-    R* const s_D = s_dG + 6 * Nfp * W;                 // strong-form D
+    R* const s_q = reinterpret_cast<R*>(smem_raw);      // planar records: states
+    R* const s_G = s_q + planar_pad<R>(5 * Np);            // gradient arguments
+    R* const s_dG = s_G + planar_pad<R>(5 * Np);           // face terms
+    R* const s_D = s_dG + planar_pad<R>(5 * NFN);          // strong-form D
 
     const int e = blockIdx.x, t = threadIdx.x;
     const R* __restrict__ Qin = static_cast<const R*>(Qv);
@@ -176,15 +177,15 @@ __global__ void __launch_bounds__(VDims<N>::NT) gradient_kernel(const KParams P,
         const int lev = ez * Nq + nk;
         R G[5];
         grad_args<R, MIXED, SMAG>(P, q, load_level<R>(P, lev), load_vlevel<R>(P, lev), G);
-        st5<R>(s_q + t * W, q);
-        st5<R>(s_G + t * W, G);
+        PL::st(s_q, Np, t, q);
+        PL::st(s_G, Np, t, G);
     }
     __syncthreads();
 
     // phase 2: face terms lift n (G+ - G-) c, c = 1/2 inside, 1 on walls
     if (face_thread) {
         R Gm[5], Gp[5];
-        ld5<R>(s_G + vM * W, Gm);
+        PL::ld(s_G, Np, vM, Gm);
         R c;
         if (nb >= 0) {
             grad_args<R, MIXED, SMAG>(P, qp, load_level<R>(P, levp), load_vlevel<R>(P, levp), Gp);
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(VDims<N>::NT) gradient_kernel(const KParams P,
         } else {
             // FreeSlip state for the gradient flux: rhou+ = rhou- - (rhou-.n) n
             R qb[NSTATE];
-            ld5<R>(s_q + vM * W, qb);
+            PL::ld(s_q, Np, vM, qb);
             qb[1 + 0] = fd == 0 ? R(0) : qb[1];
             qb[1 + 1] = fd == 1 ? R(0) : qb[2];
             qb[1 + 2] = fd == 2 ? R(0) : qb[3];
@@ -204,22 +205,20 @@ __global__ void __launch_bounds__(VDims<N>::NT) gradient_kernel(const KParams P,
         R out[5];
 #pragma unroll
         for (int g = 0; g < 5; ++g) out[g] = w * (Gp[g] - Gm[g]);
-        st5<R>(s_dG + (f * Nfp + fn) * W, out);
+        PL::st(s_dG, NFN, f * Nfp + fn, out);
     }
     __syncthreads();
 
     // phase 3: volume gradient (strong form), face terms, reference part, transform
     if (node_thread) {
         R g1[5] = {0, 0, 0, 0, 0}, g2[5] = {0, 0, 0, 0, 0}, g3[5] = {0, 0, 0, 0, 0};
-        const R* L1 = s_G + (Nq * (nj + Nq * nk)) * W;
-        const R* L2 = s_G + (ni + Nfp * nk) * W;
-        const R* L3 = s_G + (ni + Nq * nj) * W;
+        const int L1 = Nq * (nj + Nq * nk), L2 = ni + Nfp * nk, L3 = ni + Nq * nj;
 #pragma unroll
         for (int n = 0; n < Nq; ++n) {
             R v1[5], v2[5], v3[5];
-            ld5<R>(L1 + n * W, v1);
-            ld5<R>(L2 + n * Nq * W, v2);
-            ld5<R>(L3 + n * Nfp * W, v3);
+            PL::ld(s_G, Np, L1 + n, v1);
+            PL::ld(s_G, Np, L2 + n * Nq, v2);
+            PL::ld(s_G, Np, L3 + n * Nfp, v3);
             const R d1 = s_D[ni * Nq + n], d2 = s_D[nj * Nq + n], d3 = s_D[nk * Nq + n];
 #pragma unroll
             for (int g = 0; g < 5; ++g) {
@@ -236,7 +235,7 @@ __global__ void __launch_bounds__(VDims<N>::NT) gradient_kernel(const KParams P,
         }
         auto add = [&](int ff, int idx, R* gd) {
             R v[5];
-            ld5<R>(s_dG + (ff * Nfp + idx) * W, v);
+            PL::ld(s_dG, NFN, ff * Nfp + idx, v);
 #pragma unroll
             for (int g = 0; g < 5; ++g) gd[g] += v[g];
         };
@@ -250,8 +249,7 @@ __global__ void __launch_bounds__(VDims<N>::NT) gradient_kernel(const KParams P,
         const VLevel<R> vv = load_vlevel<R>(P, lev);
         R thv = 0;
         if (SMAG) {
-            const R* G = s_G + t * W;
-            thv = G[4];
+            thv = s_G[4 * Np + t];
         }
         if (MIXED && P.ph.ref_state) {
             g3[3] += vv.dht_ref;
@@ -332,13 +330,16 @@ __device__ __forceinline__ void ld_gf(const R* gf, size_t base, int Np, R out[NG
 template <int N, typename R, bool MIXED, int MODE, int TURB>
 __global__ void __launch_bounds__(VDims<N>::NT) viscous_stage_kernel(const KParams P) {
     using Dm = VDims<N>;
-    constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, W = 8;
+    constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, NFN = 6 * Nfp, P5N = planar_pad<R>(5 * Np);
     constexpr int ESTRIDE = NSTATE * Np;
+    using PL = Planar5<R>;
+    using CRV = typename Pair<R>::V;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    R* const s_node = reinterpret_cast<R*>(smem_raw);  // [Np][W] q, c, 1/rho
-    R* const s_F = s_node + Np * W;                       // [3][Np][W] total flux
-    R* const s_fs = s_F + 3 * Np * W;                     // [6][Nfp][W] lifted face flux
-    R* const s_D = s_fs + 6 * Nfp * W;                    // Dhat
+    R* const s_node = reinterpret_cast<R*>(smem_raw);                      // planar records: q
+    CRV* const s_cr = reinterpret_cast<CRV*>(s_node + P5N);                 // (c, 1/rho)
+    R* const s_F = s_node + P5N + planar_pad<R>(2 * Np);                    // total flux, 3 directions
+    R* const s_fs = s_F + 3 * P5N;                                          // lifted face flux
+    R* const s_D = s_fs + planar_pad<R>(5 * NFN);                           // Dhat
 
     const int e = blockIdx.x, t = threadIdx.x;
     const R* __restrict__ Qin = static_cast<const R*>(P.Qin);
@@ -395,10 +396,8 @@ __global__ void __launch_bounds__(VDims<N>::NT) viscous_stage_kernel(const KPara
     if (node_thread) {
         const Level<R> lv = load_level<R>(P, ez * Nq + nk);
         const Thermo<R, MIXED> th = thermo<R, MIXED>(q, lv, P);
-        R* rec = s_node + t * W;
-        st5<R>(rec, q);
-        rec[5] = th.c;
-        rec[6] = th.rinv;
+        PL::st(s_node, Np, t, q);
+        s_cr[t] = Pair<R>::make(th.c, th.rinv);
         R F2[3][NSTATE];
         const R rho = MIXED ? lv.rho_ref + q[0] : q[0];
         const R ru[3] = {q[1], q[2], q[3]};
@@ -408,7 +407,7 @@ __global__ void __launch_bounds__(VDims<N>::NT) viscous_stage_kernel(const KPara
             R F[NSTATE];
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(q, th, dd, s) + F2[dd][s];
-            st5<R>(s_F + (dd * Np + t) * W, F);
+            PL::st(s_F + dd * P5N, Np, t, F);
         }
         if (ph.gravity) {
             R rho_s = MIXED ? ((ph.ref_state && ph.subtract_off) ? q[0] : lv.rho_ref + q[0])
@@ -421,13 +420,13 @@ __global__ void __launch_bounds__(VDims<N>::NT) viscous_stage_kernel(const KPara
     // phase 2: numerical flux per face node (Rusanov/central + central second order)
     if (face_thread) {
         R qm[NSTATE], Fm[NSTATE], Fp[NSTATE], jr[NSTATE] = {0, 0, 0, 0, 0};
-        const R* rec = s_node + vM * W;
-        ld5<R>(rec, qm);
-        const R c_m = rec[5], ri_m = rec[6];
+        PL::ld(s_node, Np, vM, qm);
+        const CRV cr = s_cr[vM];
+        const R c_m = cr.x, ri_m = cr.y;
         const R lam_m = fabs(pick3(fd, qm[1], qm[2], qm[3]) * ri_m) + c_m;
         const Level<R> lvm = load_level<R>(P, ez * Nq + vM / Nfp);
         if (nb >= 0) {
-            ld5<R>(s_F + (fd * Np + vM) * W, Fm);
+            PL::ld(s_F + fd * P5N, Np, vM, Fm);
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) Fm[s] *= sgn;
             if (MIXED && fd == 2 && ph.numflux == CMDG_FLUX_RUSANOV) {
@@ -464,7 +463,7 @@ __global__ void __launch_bounds__(VDims<N>::NT) viscous_stage_kernel(const KPara
         R fs[NSTATE];
 #pragma unroll
         for (int s = 0; s < NSTATE; ++s) fs[s] = hl * (Fm[s] + Fp[s]) + pl * ((qm[s] - qp[s]) + jr[s]);
-        st5<R>(s_fs + (f * Nfp + fn) * W, fs);
+        PL::st(s_fs, NFN, f * Nfp + fn, fs);
     }
     __syncthreads();
 
@@ -472,15 +471,13 @@ __global__ void __launch_bounds__(VDims<N>::NT) viscous_stage_kernel(const KPara
     int bad = 0;
     if (node_thread) {
         R acc1[NSTATE] = {0, 0, 0, 0, 0}, acc2[NSTATE] = {0, 0, 0, 0, 0}, acc3[NSTATE] = {0, 0, 0, 0, 0};
-        const R* F1 = s_F + (0 * Np + Nq * (nj + Nq * nk)) * W;
-        const R* F2 = s_F + (1 * Np + ni + Nfp * nk) * W;
-        const R* F3 = s_F + (2 * Np + ni + Nq * nj) * W;
+        const int L1 = Nq * (nj + Nq * nk), L2 = ni + Nfp * nk, L3 = ni + Nq * nj;
 #pragma unroll
         for (int n = 0; n < Nq; ++n) {
             R v1[NSTATE], v2[NSTATE], v3[NSTATE];
-            ld5<R>(F1 + n * W, v1);
-            ld5<R>(F2 + n * Nq * W, v2);
-            ld5<R>(F3 + n * Nfp * W, v3);
+            PL::ld(s_F, Np, L1 + n, v1);
+            PL::ld(s_F + P5N, Np, L2 + n * Nq, v2);
+            PL::ld(s_F + 2 * P5N, Np, L3 + n * Nfp, v3);
             const R d1 = s_D[ni * Nq + n], d2 = s_D[nj * Nq + n], d3 = s_D[nk * Nq + n];
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) {
@@ -494,7 +491,7 @@ __global__ void __launch_bounds__(VDims<N>::NT) viscous_stage_kernel(const KPara
         for (int s = 0; s < NSTATE; ++s) rhs[s] = xi[0] * acc1[s] + xi[1] * acc2[s] + xi[2] * acc3[s];
         auto sub_face = [&](int ff, int idx) {
             R v[NSTATE];
-            ld5<R>(s_fs + (ff * Nfp + idx) * W, v);
+            PL::ld(s_fs, NFN, ff * Nfp + idx, v);
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) rhs[s] -= v[s];
         };
@@ -543,8 +540,8 @@ cudaError_t opt_in(K kernel, size_t bytes) {
 
 template <int N, typename R, bool MIXED>
 cudaError_t launch_grad_typed(const KParams& P, const void* Q, void* gf, int turb, cudaStream_t s) {
-    constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp, W = 8;
-    constexpr size_t bytes = sizeof(R) * (2 * Np * W + 6 * Nfp * W + Nq * Nq);
+    constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp;
+    constexpr size_t bytes = sizeof(R) * (2 * planar_pad<R>(5 * Np) + planar_pad<R>(30 * Nfp) + Nq * Nq);
     cudaError_t e;
     if (turb == CMDG_TURB_SMAGORINSKY) {
         if ((e = opt_in(gradient_kernel<N, R, MIXED, true>, bytes)) != cudaSuccess) return e;
@@ -558,8 +555,9 @@ cudaError_t launch_grad_typed(const KParams& P, const void* Q, void* gf, int tur
 
 template <int N, typename R, bool MIXED, int MODE>
 cudaError_t launch_vstage_typed(const KParams& P, int turb, cudaStream_t s) {
-    constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp, W = 8;
-    constexpr size_t bytes = sizeof(R) * (4 * Np * W + 6 * Nfp * W + Nq * Nq);
+    constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp;
+    constexpr size_t bytes =
+        sizeof(R) * (4 * planar_pad<R>(5 * Np) + planar_pad<R>(2 * Np) + planar_pad<R>(30 * Nfp) + Nq * Nq);
     cudaError_t e;
     if (turb == CMDG_TURB_SMAGORINSKY) {
         if ((e = opt_in(viscous_stage_kernel<N, R, MIXED, MODE, CMDG_TURB_SMAGORINSKY>, bytes)) != cudaSuccess) return e;

@@ -144,7 +144,7 @@ int cmdg_model_reference_state(const cmdg_model* model, double* h_ref);
  * nodes; mixed precision, N = 3..5; other models fall back to the node
  * kernel).  For the node kernel, grid_ctas > 0 fixes the size of its
  * persistent grid, 0 = one wave of resident CTAs, -1 = no persistence (one
- * CTA per element).  No counterpart in the reference (the
+ * CTA per element, the default).  No counterpart in the reference (the
  * launch configuration of a KernelAbstractions kernel is fixed,
  * src/Numerics/DGMethods/SpaceDiscretization.jl:1120-1133). */
 enum { CMDG_KERNEL_NODE = 0, CMDG_KERNEL_COLUMN = 1 };

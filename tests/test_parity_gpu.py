@@ -23,6 +23,9 @@ from cmdg import workloads
 pytestmark = pytest.mark.gpu
 
 TOL64 = 1e-10
+# stage-kernel configurations: one CTA per element, a resident wave walking
+# the elements, one thread per vertical line of nodes
+KERNELS = {"node": ("node", -1), "persistent": ("node", 0), "column": ("column", 0)}
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -124,11 +127,11 @@ def test_isentropic_vortex_golden_through_gpu():
     assert err == pytest.approx(3.7918869862613858e00, rel=1e-10)
 
 
-@pytest.mark.parametrize("kernel", ["node", "column"])
+@pytest.mark.parametrize("kernel", ["node", "persistent", "column"])
 @pytest.mark.parametrize("N", [3, 4, 5])
 def test_mixed_tendency_close_to_oracle(kernel, N):
     om, dg, Q0 = make_pair("bubble", N, (3, 3, 4), precision="mixed")
-    dg.set_kernel(kernel)
+    dg.set_kernel(*KERNELS[kernel])
     ref = om.tendency(Q0)
     Qp = dg.init_ode_state(Q0)
     dQ = dg.new_state(torch.float64)
@@ -138,10 +141,10 @@ def test_mixed_tendency_close_to_oracle(kernel, N):
     assert max(err) < 1e-4, err
 
 
-@pytest.mark.parametrize("kernel", ["node", "column"])
+@pytest.mark.parametrize("kernel", ["node", "persistent", "column"])
 def test_mixed_bubble_100_steps_within_1e5_of_fp64_oracle(kernel):
     om, dg, Q0 = make_pair("bubble", 4, (4, 4, 4), precision="mixed")
-    dg.set_kernel(kernel)
+    dg.set_kernel(*KERNELS[kernel])
     dt = om.courant_dt(Q0, 0.4)
     Qo, _ = om.lsrk54(Q0.copy(), dt, 100)
     Qp = dg.init_ode_state(Q0)
@@ -213,17 +216,18 @@ def test_mixed_kernels_agree_and_autotune_keeps_results(kind):
     om, dg, Q0 = make_pair(kind, 4, (5, 4, 6), precision="mixed")
     dt = 0.5 * om.courant_dt(Q0, 0.4)
     outs = {}
-    for kernel in ("node", "column"):
-        dg.set_kernel(kernel)
+    for kernel in ("node", "persistent", "column"):
+        dg.set_kernel(*KERNELS[kernel])
         Qp = dg.init_ode_state(Q0)
         lsrk = cmdg.LSRK54CarpenterKennedy(dg, Qp, dt=dt)
         cmdg.dostep_(Qp, lsrk, None, 0.0, nsteps=5)
         outs[kernel] = dg.from_perturbation(Qp).cpu().numpy()
-    err, ref = om.field_l2(outs["node"], outs["column"])
-    # momentum as one vector field (rho*w of the vortex is noise-sized)
-    err = np.array([err[0], np.sqrt(np.sum(err[1:4] ** 2)), err[4]])
-    ref = np.array([ref[0], np.sqrt(np.sum(ref[1:4] ** 2)), ref[4]])
-    assert (err / ref < 1e-6).all(), err / ref
+    for other in ("persistent", "column"):
+        err, ref = om.field_l2(outs["node"], outs[other])
+        # momentum as one vector field (rho*w of the vortex is noise-sized)
+        err = np.array([err[0], np.sqrt(np.sum(err[1:4] ** 2)), err[4]])
+        ref = np.array([ref[0], np.sqrt(np.sum(ref[1:4] ** 2)), ref[4]])
+        assert (err / ref < 1e-6).all(), (other, err / ref)
     ms, choice = dg.autotune(reps=3)
     assert len(ms) == 3 and all(m > 0 for m in ms)
     assert choice[0] in ("node", "column")
