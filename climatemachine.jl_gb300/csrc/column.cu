@@ -359,7 +359,8 @@ __global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kerne
                 }
             }
     }
-    if (__syncthreads_or(bad) && lt == 0) atomicOr(P.status, 1u);
+    // one pass per CTA: no barrier at the end, one vote per warp
+    if (__any_sync(0xffffffffu, bad) && (lt & 31) == 0) atomicOr(P.status, 1u);
 }
 
 template <int N, int MODE>

@@ -298,7 +298,8 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
             }
         }
     }
-    if (__syncthreads_or(bad) && t == 0) atomicOr(P.status, 1u);
+    // one CTA per element: no barrier at the end, one vote per warp
+    if (__any_sync(0xffffffffu, bad) && (t & 31) == 0) atomicOr(P.status, 1u);
 }
 
 template <int N, typename R, bool MIXED, int MODE>

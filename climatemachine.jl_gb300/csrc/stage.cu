@@ -308,8 +308,13 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
                 }
             }
         }
-        // also separates this element's shared-memory reads from the next one's writes
-        if (__syncthreads_or(bad) && t == 0) atomicOr(P.status, 1u);
+        if (PERSIST || e + e_stride < e_end) {
+            // also separates this element's shared-memory reads from the next one's writes
+            if (__syncthreads_or(bad) && t == 0) atomicOr(P.status, 1u);
+        } else {
+            // last element of this CTA: no barrier, one vote per warp
+            if (__any_sync(0xffffffffu, bad) && (t & 31) == 0) atomicOr(P.status, 1u);
+        }
         if (PERSIST) cur = nxt;
     }
 }

@@ -529,7 +529,8 @@ __global__ void __launch_bounds__(VDims<N>::NT) viscous_stage_kernel(const KPara
             }
         }
     }
-    if (__syncthreads_or(bad) && t == 0) atomicOr(P.status, 1u);
+    // one pass per CTA: no barrier at the end, one vote per warp
+    if (__any_sync(0xffffffffu, bad) && (t & 31) == 0) atomicOr(P.status, 1u);
 }
 
 template <typename K>
