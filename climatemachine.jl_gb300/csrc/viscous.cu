@@ -328,7 +328,9 @@ __device__ __forceinline__ void ld_gf(const R* gf, size_t base, int Np, R out[NG
 }
 
 template <int N, typename R, bool MIXED, int MODE, int TURB>
-__global__ void __launch_bounds__(VDims<N>::NT) viscous_stage_kernel(const KParams P) {
+// FP32: 6 resident CTAs per SM (measured on the Smagorinsky LES: 183 us per
+// stage against 195 us at the compiler's choice of 90 registers, 4 CTAs)
+__global__ void __launch_bounds__(VDims<N>::NT, (sizeof(R) == 4 ? 6 : 1)) viscous_stage_kernel(const KParams P) {
     using Dm = VDims<N>;
     constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, NFN = 6 * Nfp, P5N = planar_pad<R>(5 * Np);
     constexpr int ESTRIDE = NSTATE * Np;
