@@ -28,6 +28,7 @@ EXPORTS = (
     "cmdg_model_set_kernel", "cmdg_model_get_kernel", "cmdg_model_autotune", "cmdg_gradient_flux",
     "cmdg_batch_create", "cmdg_batch_destroy", "cmdg_batch_set_tiling", "cmdg_batch_get_tiling",
     "cmdg_batch_lsrk54_step", "cmdg_batch_autotune",
+    "cmdg_filter_matrix", "cmdg_apply_filter", "cmdg_apply_tmar",
 )
 
 
@@ -109,6 +110,9 @@ def load(path: str | None = None):
         "cmdg_batch_get_tiling": [P, I, ctypes.POINTER(I), ctypes.POINTER(I)],
         "cmdg_batch_lsrk54_step": [P, P, P, P, I, P],
         "cmdg_batch_autotune": [P, P, P, I, P, I, ctypes.POINTER(I), P],
+        "cmdg_filter_matrix": [I, I, I, I, D, P],
+        "cmdg_apply_filter": [P, P, P, P, I, P, I, P],
+        "cmdg_apply_tmar": [P, P, P, I, P],
     }
     for name, args in proto.items():
         fn = getattr(L, name)

@@ -312,6 +312,8 @@ int cmdg_model_destroy(cmdg_model* model) {
     cudaFree(md.d_mass);
     cudaFree(md.d_dxmin);
     cudaFree(md.d_ref64);
+    cudaFree(md.d_filter_corr);
+    cudaFree(md.d_omega);
     release_quad(&md);
     delete model;
     return CMDG_OK;

@@ -173,6 +173,9 @@ struct Model {
     std::vector<double> ref64;       // curvilinear meshes: (Np, 2, nelem) rho_ref, rhoe_ref per node
     double* d_ref64 = nullptr;
     double* d_dxmin = nullptr;       // curvilinear meshes: nearest-node distance per node
+    std::vector<float> filter_corr;  // mixed precision: vertical-filter change of the reference state per level
+    float* d_filter_corr = nullptr;
+    double* d_omega = nullptr;       // LGL weights on the device (TMAR filter)
     int grid_ctas = -1;              // stage-kernel grid: -1 = one CTA per element (the measured best
                                      // on GB300), 0 = one wave of resident CTAs, n > 0 = n CTAs
     int kernel_kind = 0;             // KERNEL_NODE or KERNEL_COLUMN

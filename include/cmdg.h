@@ -220,6 +220,24 @@ int cmdg_batch_lsrk54_step(cmdg_batch* batch, void* const* h_Q, double* const* h
 int cmdg_batch_autotune(cmdg_batch* batch, void* const* h_Q, double* const* h_dQ, int reps, double* h_ms,
                         int h_ms_len, int* n_candidates, void* stream);
 
+/* Filters applied to a state between steps (src/Numerics/Mesh/Filters.jl).
+ * cmdg_filter_matrix: spectral_filter_matrix of an ExponentialFilter
+ * (sigma = exp(-alpha eta^s)), CutoffFilter (sigma = 0) or
+ * BoydVandevenFilter, (N+1)^2 doubles, row i = output node i
+ * (Filters.jl:114-128, 172-306); host only.
+ * cmdg_apply_filter: applies the horizontal matrix along xi1 and xi2 and the
+ * vertical one along xi3 (direction CMDG_DIR_*) to the listed fields of a
+ * model's state in place (FP64 state, or the FP32 perturbation of a mixed
+ * model; mixed needs Nc >= 1 horizontally) — Filters.apply!(Q, fields, grid,
+ * filter; direction) (:408-505).  Brick meshes.
+ * cmdg_apply_tmar: TMARFilter on the listed fields (:369-407, 794-892). */
+enum { CMDG_FILTER_EXPONENTIAL = 0, CMDG_FILTER_CUTOFF = 1, CMDG_FILTER_BOYD_VANDEVEN = 2 };
+enum { CMDG_DIR_EVERY = 0, CMDG_DIR_HORIZONTAL = 1, CMDG_DIR_VERTICAL = 2 };
+int cmdg_filter_matrix(int N, int kind, int Nc, int s, double alpha, double* h_W);
+int cmdg_apply_filter(cmdg_model* model, void* d_Q, const double* h_Wh, const double* h_Wv, int direction,
+                      const int* h_fields, int nfields, void* stream);
+int cmdg_apply_tmar(cmdg_model* model, void* d_Q, const int* h_fields, int nfields, void* stream);
+
 /* Mixed precision: converts an FP64 state to the FP32 perturbation
  * q' = q - q_ref (the subtraction is done in FP64) and back.
  * No counterpart in the reference (the reference state lives in aux.ref_state,

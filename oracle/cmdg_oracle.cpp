@@ -1442,6 +1442,143 @@ void om_init_bubble(const om_model* m, double* Q, double theta0, double amp, dou
         }
 }
 
+// ----------------------------------------------------------------------------
+// Filters (src/Numerics/Mesh/Filters.jl).
+// ----------------------------------------------------------------------------
+// spectral_filter_matrix (Filters.jl:114-128): W = V diag(Sigma) V^-1 with V
+// the orthonormal Legendre polynomials at the LGL points (GaussQuadrature
+// orthonormal_poly: P~_n = sqrt((2n+1)/2) P_n) and Sigma_n = 1 for n < Nc,
+// sigma((n - Nc)/(N - Nc)) for n >= Nc.  kind 0 = ExponentialFilter
+// (sigma = exp(-alpha eta^s), :172-213), 1 = CutoffFilter (sigma = 0,
+// :275-306), 2 = BoydVandevenFilter (sigma = erfc(sqrt(s) chi a)/2,
+// a = 2|eta| - 1, chi = sqrt(-log1p(-a^2)/a^2) or 1, :231-269).  W is written
+// row-major: W[i*Nq + n] multiplies node n for output node i.
+int om_filter_matrix(int N, int kind, int Nc, int s, double alpha, double* W) {
+    if (N < 1 || Nc < 0 || Nc > N) return -1;
+    const int Nq = N + 1;
+    std::vector<double> r, w;
+    lgl(N, r, w);
+    std::vector<double> V((size_t)Nq * Nq), Sig(Nq, 1.0);
+    for (int i = 0; i < Nq; ++i) {
+        double p0 = 1.0, p1 = r[i];
+        for (int n = 0; n < Nq; ++n) {
+            double pn;
+            if (n == 0) pn = 1.0;
+            else if (n == 1) pn = r[i];
+            else {
+                pn = ((2 * n - 1) * r[i] * p1 - (n - 1) * p0) / n;
+                p0 = p1;
+                p1 = pn;
+            }
+            V[(size_t)i * Nq + n] = std::sqrt((2.0 * n + 1) / 2) * pn;
+        }
+    }
+    for (int n = Nc; n <= N; ++n) {
+        const double eta = (N == Nc) ? 0.0 : (double)(n - Nc) / (N - Nc);
+        double sg;
+        if (kind == 0) sg = std::exp(-alpha * std::pow(eta, s));
+        else if (kind == 1) sg = 0.0;
+        else {
+            const double a = 2 * std::fabs(eta) - 1;
+            const double chi = (a == 0) ? 1.0 : std::sqrt(-std::log1p(-a * a) / (a * a));
+            sg = std::erfc(std::sqrt((double)s) * chi * a) / 2;
+        }
+        Sig[n] = sg;
+    }
+    // W = V diag(Sig) V^-1: solve W V = V diag(Sig) row by row (Gauss-Jordan on V^T)
+    std::vector<double> A((size_t)Nq * Nq), B((size_t)Nq * Nq);
+    for (int i = 0; i < Nq; ++i)
+        for (int j = 0; j < Nq; ++j) {
+            A[(size_t)i * Nq + j] = V[(size_t)j * Nq + i];            // V^T
+            B[(size_t)i * Nq + j] = V[(size_t)j * Nq + i] * Sig[i];   // (V diag Sig)^T
+        }
+    // solve V^T W^T = (V diag Sig)^T with partial pivoting
+    for (int c = 0; c < Nq; ++c) {
+        int piv = c;
+        for (int i = c + 1; i < Nq; ++i)
+            if (std::fabs(A[(size_t)i * Nq + c]) > std::fabs(A[(size_t)piv * Nq + c])) piv = i;
+        for (int j = 0; j < Nq; ++j) {
+            std::swap(A[(size_t)c * Nq + j], A[(size_t)piv * Nq + j]);
+            std::swap(B[(size_t)c * Nq + j], B[(size_t)piv * Nq + j]);
+        }
+        const double d = A[(size_t)c * Nq + c];
+        for (int j = 0; j < Nq; ++j) {
+            A[(size_t)c * Nq + j] /= d;
+            B[(size_t)c * Nq + j] /= d;
+        }
+        for (int i = 0; i < Nq; ++i) {
+            if (i == c) continue;
+            const double f = A[(size_t)i * Nq + c];
+            if (f == 0) continue;
+            for (int j = 0; j < Nq; ++j) {
+                A[(size_t)i * Nq + j] -= f * A[(size_t)c * Nq + j];
+                B[(size_t)i * Nq + j] -= f * B[(size_t)c * Nq + j];
+            }
+        }
+    }
+    for (int i = 0; i < Nq; ++i)
+        for (int j = 0; j < Nq; ++j) W[(size_t)i * Nq + j] = B[(size_t)j * Nq + i];
+    return 0;
+}
+
+// kernel_apply_filter! (Filters.jl:651-790) through apply_async!
+// (:440-505): horizontal pass (xi1 then xi2 with Wh) then vertical pass (xi3
+// with Wv), each a sum over the line in place; direction 0 = every,
+// 1 = horizontal, 2 = vertical; fields: the filtered state indices.
+void om_apply_filter(const om_model* m, double* Q, const double* Wh, const double* Wv, int direction,
+                     const int* fields, int nfields) {
+    const int Nq = m->Nq, Np = m->Np;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m->nelem; ++e) {
+        std::vector<double> a(Np), b(Np);
+        for (int fi = 0; fi < nfields; ++fi) {
+            double* q = Q + ((size_t)e * NS + fields[fi]) * Np;
+            for (int n = 0; n < Np; ++n) a[n] = q[n];
+            auto pass = [&](const double* W, int d) {
+                for (int k = 0; k < Nq; ++k)
+                    for (int j = 0; j < Nq; ++j)
+                        for (int i = 0; i < Nq; ++i) {
+                            const int ijk = i + Nq * (j + Nq * k);
+                            const int row = d == 0 ? i : (d == 1 ? j : k);
+                            double acc = 0;
+                            for (int n = 0; n < Nq; ++n) {
+                                const int src = d == 0 ? n + Nq * (j + Nq * k)
+                                                       : (d == 1 ? i + Nq * (n + Nq * k) : i + Nq * (j + Nq * n));
+                                acc += W[row * Nq + n] * a[src];
+                            }
+                            b[ijk] = acc;
+                        }
+                a.swap(b);
+            };
+            if (direction == 0 || direction == 1) {
+                pass(Wh, 0);
+                pass(Wh, 1);
+            }
+            if (direction == 0 || direction == 2) pass(Wv, 2);
+            for (int n = 0; n < Np; ++n) q[n] = a[n];
+        }
+    }
+}
+
+// TMARFilter, kernel_apply_TMAR_filter! (Filters.jl:794-892): per element
+// and field, r = sum(M q) / sum(M max(q, 0)) (0 when sum(M q) <= 0) and
+// q <- r q where q >= 0, 0 elsewhere.
+void om_apply_tmar(const om_model* m, double* Q, const int* fields, int nfields) {
+    const int Np = m->Np;
+    for (int64_t e = 0; e < m->nelem; ++e)
+        for (int fi = 0; fi < nfields; ++fi) {
+            double* q = Q + ((size_t)e * NS + fields[fi]) * Np;
+            double MJQ = 0, MJQc = 0;
+            for (int n = 0; n < Np; ++n) {
+                const double M = VGc(*m, e, VM, n);
+                MJQ += M * q[n];
+                MJQc += M * (q[n] >= 0 ? q[n] : 0.0);
+            }
+            const double r = MJQ > 0 ? MJQ / MJQc : 0.0;
+            for (int n = 0; n < Np; ++n) q[n] = q[n] >= 0 ? r * q[n] : 0.0;
+        }
+}
+
 // Rest state equal to the reference state (discrete_hydrostatic_balance.jl:25-30)
 void om_init_rest(const om_model* m, double* Q) {
     for (int64_t e = 0; e < m->nelem; ++e)

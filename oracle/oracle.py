@@ -141,6 +141,11 @@ def lib():
         L.om_init_vortex.argtypes = [P, dp, D, D, D, D, D, D, D, D]
         L.om_init_bubble.argtypes = [P, dp, D, D, D, D, D, D]
         L.om_init_rest.argtypes = [P, dp]
+        L.om_filter_matrix.restype = ctypes.c_int
+        L.om_filter_matrix.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, D, dp]
+        ip = ctypes.POINTER(ctypes.c_int)
+        L.om_apply_filter.argtypes = [P, dp, dp, dp, ctypes.c_int, ip, ctypes.c_int]
+        L.om_apply_tmar.argtypes = [P, dp, ip, ctypes.c_int]
         L.om_lsrk54_scalar.restype = D
         L.om_lsrk54_scalar.argtypes = [D, D, D]
         _lib = L
@@ -328,6 +333,39 @@ class OracleModel:
         Q = self.state()
         self.L.om_init_rest(self.h, _ptr(Q))
         return Q
+
+
+FILTER_KINDS = {"exponential": 0, "cutoff": 1, "boyd_vandeven": 2}
+
+
+def filter_matrix(N, kind, Nc, s=32, alpha=None):
+    """spectral_filter_matrix of the named filter, W[i, n] (row = output node)."""
+    if alpha is None:
+        alpha = -np.log(np.finfo(np.float64).eps)
+    W = np.zeros((N + 1, N + 1))
+    if lib().om_filter_matrix(N, FILTER_KINDS[kind], Nc, s, alpha, _ptr(W)):
+        raise ValueError("bad filter arguments")
+    return W
+
+
+def _fields(fields):
+    arr = (ctypes.c_int * len(fields))(*fields)
+    return arr, len(fields)
+
+
+def apply_filter(model, Q, Wh, Wv, direction="every", fields=(0, 1, 2, 3, 4)):
+    d = {"every": 0, "horizontal": 1, "vertical": 2}[direction]
+    arr, n = _fields(fields)
+    Wh = np.ascontiguousarray(Wh, dtype=np.float64)
+    Wv = np.ascontiguousarray(Wv, dtype=np.float64)
+    lib().om_apply_filter(model.h, _ptr(Q), _ptr(Wh), _ptr(Wv), d, arr, n)
+    return Q
+
+
+def apply_tmar(model, Q, fields):
+    arr, n = _fields(fields)
+    lib().om_apply_tmar(model.h, _ptr(Q), arr, n)
+    return Q
 
 
 def lsrk54_scalar(q0: float, dt: float, timeend: float) -> float:

@@ -1,0 +1,94 @@
+"""GPU filters against the oracle: spectral filters (exponential, cutoff,
+Boyd-Vandeven; every, horizontal, vertical direction; field subsets) on the
+FP64 state within 1e-13 and on the mixed-precision perturbation within 1e-6,
+the CutoffFilter known answer, and TMAR."""
+import numpy as np
+import pytest
+import torch
+
+import cmdg
+import oracle as O
+from cmdg import filters, workloads
+
+pytestmark = pytest.mark.gpu
+L = 2500.0
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import __graft_entry__ as g
+
+    g.build()
+    torch.cuda.set_device(0)
+
+
+def pair(N=4, ne=(3, 2, 4), precision="fp64"):
+    om = O.OracleModel(N, ne, (0, 0, 0), (L, L, L), periodic=(1, 1, 0), orientation="flat", gravity=True,
+                       ref_state=True, profile="dry_adiabatic", T_surface=300.0, T_min=0.0)
+    dg = workloads.bubble_model(ne=ne, N=N, L=L, precision=precision)
+    Q0 = om.init_bubble(rc=900.0, xc=1100.0, yc=1300.0, zc=800.0)
+    rng = np.random.default_rng(9)
+    Q0[:, 1:4] += rng.uniform(-3, 3, size=Q0[:, 1:4].shape)
+    return om, dg, Q0
+
+
+def rel(got, ref):
+    out = []
+    for sl in (slice(0, 1), slice(1, 4), slice(4, 5)):
+        out.append(np.abs(got[:, sl] - ref[:, sl]).max() / np.abs(ref[:, sl]).max())
+    return np.array(out)
+
+
+CASES = [("exponential", (0, 0), 32, "every", (0, 1, 2, 3, 4)), ("cutoff", (3, 2), 0, "vertical", (0, 4)),
+         ("boyd_vandeven", (1, 1), 8, "horizontal", (1, 2, 3)), ("exponential", (2, 1), 4, "every", (0, 3, 4))]
+
+
+@pytest.mark.parametrize("kind,Nc,s,direction,fields", CASES)
+def test_fp64_spectral_filter_matches_oracle(kind, Nc, s, direction, fields):
+    om, dg, Q0 = pair()
+    cls = {"exponential": filters.ExponentialFilter, "cutoff": filters.CutoffFilter,
+           "boyd_vandeven": filters.BoydVandevenFilter}[kind]
+    filt = cls(dg.grid, Nc) if kind == "cutoff" else cls(dg.grid, Nc, s)
+    Q = dg.init_ode_state(Q0)
+    filters.apply_(Q, fields, dg, filt, direction)
+    ref = O.apply_filter(om, Q0.copy(), filt.filter_matrices[0], filt.filter_matrices[1], direction, fields)
+    assert (rel(Q.cpu().numpy(), ref) < 1e-13).all()
+
+
+@pytest.mark.parametrize("kind,Nc,s,direction,fields", [c for c in CASES if c[1][0] >= 1])
+def test_mixed_spectral_filter_close_to_fp64_oracle(kind, Nc, s, direction, fields):
+    om, dg, Q0 = pair(precision="mixed")
+    cls = {"exponential": filters.ExponentialFilter, "cutoff": filters.CutoffFilter,
+           "boyd_vandeven": filters.BoydVandevenFilter}[kind]
+    filt = cls(dg.grid, Nc) if kind == "cutoff" else cls(dg.grid, Nc, s)
+    Qp = dg.init_ode_state(Q0)
+    filters.apply_(Qp, fields, dg, filt, direction)
+    ref = O.apply_filter(om, Q0.copy(), filt.filter_matrices[0], filt.filter_matrices[1], direction, fields)
+    got = dg.from_perturbation(Qp).cpu().numpy()
+    assert (rel(got, ref) < 1e-6).all(), rel(got, ref)
+
+
+def test_cutoff_known_answer_on_gpu():
+    grid = cmdg.BrickGrid(3, (2, 1, 2), (-1, -1, -1), (1, 1, 1))
+    dg = cmdg.DGModel(cmdg.AtmosModel(), grid)
+    xyz = grid.coordinates()
+    lo, hi = xyz.min(axis=2, keepdims=True), xyz.max(axis=2, keepdims=True)
+    r = 2 * (xyz - lo) / (hi - lo) - 1
+    x, y, z = r[:, 0], r[:, 1], r[:, 2]
+    low = 1 + 4 * x * y + 5 * z + 6 * z * x
+    hh = (3 * x**2 - 1) / 2 * (5 * y**3 - 3 * y) / 2 + (5 * x**3 - 3 * x) / 2 + (3 * y**2 - 1) / 2
+    hv = (5 * z**3 - 3 * z) / 2 * y
+    Q = torch.from_numpy(np.stack([low + hh + hv] * 5, axis=1)).cuda()
+    filters.apply_(Q, (0, 1, 2, 3, 4), dg, filters.CutoffFilter(grid, 2), "every")
+    assert np.abs(Q.cpu().numpy() - low[:, None, :]).max() < 1e-12
+
+
+def test_tmar_matches_oracle():
+    om, dg, Q0 = pair()
+    Q0[:, 3] = np.random.default_rng(1).normal(0.2, 1.0, size=Q0[:, 3].shape)  # a field with negative values
+    Q = dg.init_ode_state(Q0)
+    filters.apply_(Q, (3,), dg, filters.TMARFilter())
+    ref = O.apply_tmar(om, Q0.copy(), (3,))
+    got = Q.cpu().numpy()
+    assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
+    assert (got[:, 3] >= 0).all()
