@@ -33,28 +33,33 @@ struct ColCfg;
 template <>
 struct ColCfg<3> {
     static constexpr int EPB = 8;  // 128 threads
+    static constexpr int MIN_CTAS = 4;
 };
 template <>
 struct ColCfg<4> {
     static constexpr int EPB = 5;  // 125 threads
+    static constexpr int MIN_CTAS = 5;
 };
 template <>
 struct ColCfg<5> {
     static constexpr int EPB = 4;  // 144 threads
+    static constexpr int MIN_CTAS = 3;
 };
 
 template <int N, typename R>
 struct ColSmem {
     static constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp;
     // per element, planar five-field records (Planar5): xi1 and xi2 fluxes,
-    // states and (c, 1/rho) of the horizontal-face nodes, lifted horizontal
-    // face fluxes
+    // states and (c, 1/rho) of the horizontal-face nodes, then the lifted
+    // horizontal face fluxes in place of those states
     static constexpr int F1 = 0;
     static constexpr int F2 = F1 + planar_pad<R>(5 * Np);
     static constexpr int NODE = F2 + planar_pad<R>(5 * Np);
     static constexpr int CR = NODE + planar_pad<R>(5 * 4 * Nfp);
-    static constexpr int FACE = CR + planar_pad<R>(2 * 4 * Nfp);
-    static constexpr int PER_ELEM = FACE + planar_pad<R>(5 * 4 * Nfp);
+    // the lifted face flux of in-face node c replaces that node's record: the
+    // thread that reads the record is the one that writes the flux
+    static constexpr int FACE = NODE;
+    static constexpr int PER_ELEM = CR + planar_pad<R>(2 * 4 * Nfp);
     static constexpr int DMAT = ColCfg<N>::EPB * PER_ELEM;
     static constexpr int TOTAL = DMAT + Nq * Nq;
     static constexpr size_t BYTES = sizeof(R) * TOTAL;
@@ -98,7 +103,7 @@ __device__ __forceinline__ void face_flux(const KParams& P, const R qm[NSTATE], 
 }
 
 template <int N, typename R, bool MIXED, int MODE>
-__global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kernel(const KParams P) {
+__global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1), ColCfg<N>::MIN_CTAS) column_kernel(const KParams P) {
     constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp, EPB = ColCfg<N>::EPB, NH = 4 * Nfp;
     constexpr int ESTRIDE = NSTATE * Np;
     using CS = ColSmem<N, R>;
@@ -125,116 +130,98 @@ __global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kerne
     const bool read_reg = (MODE == 0) ? (P.beta != 0) : !P.first_stage;
     if (lt < Nq * Nq) sD[lt] = dhat_c<R>(P, lt);
 
-    // ---------------- loads: element row, own line, neighbours' face nodes
+    // ---------------- loads: element row, own line
     const int4 nb03 = __ldg(reinterpret_cast<const int4*>(P.nbr + NBR_STRIDE * e));
     const int4 nb45 = __ldg(reinterpret_cast<const int4*>(P.nbr + NBR_STRIDE * e + 4));
     const int nbf[4] = {nb03.x, nb03.y, nb03.z, nb03.w};
     const int nbb = nb45.x, nbt = nb45.y, ez = nb45.z;
     const R xi[3] = {KConst<R>::metric(P, e, 0), KConst<R>::metric(P, e, 1), KConst<R>::metric(P, e, 2)};
-    R q[Nq][NSTATE];
-    {
-        const R* qe = Qin + (size_t)e * ESTRIDE + c;
-#pragma unroll
-        for (int k = 0; k < Nq; ++k)
-#pragma unroll
-            for (int s = 0; s < NSTATE; ++s) q[k][s] = qe[s * Np + k * Nfp];
-    }
-    R qb[NSTATE], qt[NSTATE], qh[4][NSTATE];
-    if (nbb >= 0) {
-        const R* qn = Qin + (size_t)nbb * ESTRIDE + c + N * Nfp;
-#pragma unroll
-        for (int s = 0; s < NSTATE; ++s) qb[s] = qn[s * Np];
-    }
-    if (nbt >= 0) {
-        const R* qn = Qin + (size_t)nbt * ESTRIDE + c;
-#pragma unroll
-        for (int s = 0; s < NSTATE; ++s) qt[s] = qn[s * Np];
-    }
-    // in-face node c = (a, b) of horizontal face f; neighbour node on face f^1
-    const int ca = c % Nq, cb = c / Nq;
-    const int vPh[4] = {N + Nq * c, Nq * c, ca + Nq * (N + Nq * cb), ca + Nq * (Nq * cb)};
-#pragma unroll
-    for (int f = 0; f < 4; ++f) {
-        if (nbf[f] >= 0) {
-            const R* qn = Qin + (size_t)nbf[f] * ESTRIDE + vPh[f];
-#pragma unroll
-            for (int s = 0; s < NSTATE; ++s) qh[f][s] = qn[s * Np];
-        }
-    }
+    const R* qe = Qin + (size_t)e * ESTRIDE + c;
 
-    // ---------------- phase A: line thermodynamics, fluxes, xi3 terms
+    // ---------------- phase A: line thermodynamics and fluxes; the xi3
+    // contraction is accumulated node by node (acc[m] += Dhat[m][k] F3(k)),
+    // so only one line node's xi3 flux is live at a time
     R acc[Nq][NSTATE];
+#pragma unroll
+    for (int m = 0; m < Nq; ++m)
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) acc[m][s] = 0;
     R gsrc[Nq];
-    {
-        R F3[Nq][NSTATE];
-        R c_end[2], ri_end[2];
+    R qend[2][NSTATE], Fend[2][NSTATE], c_end[2], ri_end[2];
 #pragma unroll
-        for (int k = 0; k < Nq; ++k) {
-            const Level<R> lv = load_level<R>(P, ez * Nq + k);
-            const Thermo<R, MIXED> th = thermo<R, MIXED>(q[k], lv, P);
-            const int node = c + k * Nfp;
-            R F[NSTATE];
+    for (int k = 0; k < Nq; ++k) {
+        R qk[NSTATE];
 #pragma unroll
-            for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(q[k], th, 0, s);
-            PL::st(sF1, Np, node, F);
+        for (int s = 0; s < NSTATE; ++s) qk[s] = qe[s * Np + k * Nfp];
+        const Level<R> lv = load_level<R>(P, ez * Nq + k);
+        const Thermo<R, MIXED> th = thermo<R, MIXED>(qk, lv, P);
+        const int node = c + k * Nfp;
+        R F[NSTATE];
 #pragma unroll
-            for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(q[k], th, 1, s);
-            PL::st(sF2, Np, node, F);
+        for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(qk, th, 0, s);
+        PL::st(sF1, Np, node, F);
 #pragma unroll
-            for (int s = 0; s < NSTATE; ++s) F3[k][s] = flux_d<R, MIXED>(q[k], th, 2, s);
-            // node records of horizontal-face nodes, at their in-face index
-            int ri = -1;
-            if (ci == 0) ri = 0 * Nfp + cj + Nq * k;
-            if (ci == N) ri = 1 * Nfp + cj + Nq * k;
-            if (ri >= 0) {
-                PL::st(sNode, NH, ri, q[k]);
-                sCR[ri] = Pair<R>::make(th.c, th.rinv);
-            }
-            ri = -1;
-            if (cj == 0) ri = 2 * Nfp + ci + Nq * k;
-            if (cj == N) ri = 3 * Nfp + ci + Nq * k;
-            if (ri >= 0) {
-                PL::st(sNode, NH, ri, q[k]);
-                sCR[ri] = Pair<R>::make(th.c, th.rinv);
-            }
-            if (k == 0) {
-                c_end[0] = th.c;
-                ri_end[0] = th.rinv;
-            }
-            if (k == N) {
-                c_end[1] = th.c;
-                ri_end[1] = th.rinv;
-            }
-            gsrc[k] = 0;
-            if (ph.gravity) {
-                R rho_s = MIXED ? ((ph.ref_state && ph.subtract_off) ? q[k][0] : lv.rho_ref + q[k][0])
-                                : ((ph.ref_state && ph.subtract_off) ? q[k][0] - lv.rho_ref : q[k][0]);
-                gsrc[k] = -rho_s * lv.gphiz;
-            }
-        }
-        // xi3 contraction in registers: acc[k] = xi3 sum_n Dhat[k][n] F3[n]
+        for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(qk, th, 1, s);
+        PL::st(sF2, Np, node, F);
 #pragma unroll
-        for (int k = 0; k < Nq; ++k)
+        for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(qk, th, 2, s);
+#pragma unroll
+        for (int m = 0; m < Nq; ++m)
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) acc[m][s] = fma(dhat_c<R>(P, m * Nq + k), F[s], acc[m][s]);
+        if (k == 0 || k == N) {
+            const int side = k == 0 ? 0 : 1;
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) {
-                R a = 0;
-#pragma unroll
-                for (int n = 0; n < Nq; ++n) a = fma(dhat_c<R>(P, k * Nq + n), F3[n][s], a);
-                acc[k][s] = xi[2] * a;
+                qend[side][s] = qk[s];
+                Fend[side][s] = F[s];
             }
-        // bottom (face 5 of the reference, xi3 = -1) and top (face 6) of the line
+            c_end[side] = th.c;
+            ri_end[side] = th.rinv;
+        }
+        // node records of horizontal-face nodes, at their in-face index
+        int ri = -1;
+        if (ci == 0) ri = 0 * Nfp + cj + Nq * k;
+        if (ci == N) ri = 1 * Nfp + cj + Nq * k;
+        if (ri >= 0) {
+            PL::st(sNode, NH, ri, qk);
+            sCR[ri] = Pair<R>::make(th.c, th.rinv);
+        }
+        ri = -1;
+        if (cj == 0) ri = 2 * Nfp + ci + Nq * k;
+        if (cj == N) ri = 3 * Nfp + ci + Nq * k;
+        if (ri >= 0) {
+            PL::st(sNode, NH, ri, qk);
+            sCR[ri] = Pair<R>::make(th.c, th.rinv);
+        }
+        gsrc[k] = 0;
+        if (ph.gravity) {
+            R rho_s = MIXED ? ((ph.ref_state && ph.subtract_off) ? qk[0] : lv.rho_ref + qk[0])
+                            : ((ph.ref_state && ph.subtract_off) ? qk[0] - lv.rho_ref : qk[0]);
+            gsrc[k] = -rho_s * lv.gphiz;
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < Nq; ++m)
+#pragma unroll
+        for (int s = 0; s < NSTATE; ++s) acc[m][s] *= xi[2];
+    // bottom (face 5 of the reference, xi3 = -1) and top (face 6) of the line
+    {
         const R lift3 = xi[2] * KConst<R>::inv_w0(P);
 #pragma unroll
         for (int side = 0; side < 2; ++side) {
             const int k = side ? N : 0;
             const R sgn = side ? R(1) : R(-1);
             const int nbv = side ? nbt : nbb;
-            R Fm[NSTATE], jr[NSTATE] = {0, 0, 0, 0, 0};
+            R Fm[NSTATE], qv[NSTATE], jr[NSTATE] = {0, 0, 0, 0, 0};
 #pragma unroll
-            for (int s = 0; s < NSTATE; ++s) Fm[s] = sgn * F3[k][s];
-            const R lam_m = fabs(q[k][3] * ri_end[side]) + c_end[side];
+            for (int s = 0; s < NSTATE; ++s) Fm[s] = sgn * Fend[side][s];
+            const R lam_m = fabs(qend[side][3] * ri_end[side]) + c_end[side];
             int lev_p = ez * Nq + k;
             if (nbv >= 0) {
+                const R* qn = Qin + (size_t)nbv * ESTRIDE + c + (side ? 0 : N * Nfp);
+#pragma unroll
+                for (int s = 0; s < NSTATE; ++s) qv[s] = qn[s * Np];
                 int ezp = ez + (side ? 1 : -1);
                 ezp = ezp < 0 ? ezp + P.nz : (ezp >= P.nz ? ezp - P.nz : ezp);
                 lev_p = ezp * Nq + (side ? 0 : N);
@@ -247,7 +234,7 @@ __global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kerne
             }
             const Level<R> lvp = load_level<R>(P, lev_p);
             R fs[NSTATE];
-            face_flux<R, MIXED>(P, q[k], Fm, lam_m, side ? qt : qb, nbv < 0, lvp, 2, sgn, jr, lift3, fs);
+            face_flux<R, MIXED>(P, qend[side], Fm, lam_m, qv, nbv < 0, lvp, 2, sgn, jr, lift3, fs);
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) acc[k][s] -= fs[s];
         }
@@ -255,15 +242,9 @@ __global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kerne
     __syncthreads();
 
     // ---------------- phase B: horizontal faces (in-face node c of faces 1-4), xi1/xi2 terms
-    double dq_old[Nq][NSTATE];
-    const size_t ebase = (size_t)e * ESTRIDE + c;
-    if (read_reg) {
-#pragma unroll
-        for (int k = 0; k < Nq; ++k)
-#pragma unroll
-            for (int s = 0; s < NSTATE; ++s) dq_old[k][s] = P.dQ[ebase + s * Np + k * Nfp];
-    }
     {
+        const int ca = c % Nq, cb = c / Nq;
+        const int vPh[4] = {N + Nq * c, Nq * c, ca + Nq * (N + Nq * cb), ca + Nq * (Nq * cb)};
         const int vMh[4] = {Nq * c, N + Nq * c, ca + Nfp * cb, ca + Nq * N + Nfp * cb};
         const R inv_w0 = KConst<R>::inv_w0(P);
         const Level<R> lvh = load_level<R>(P, ez * Nq + cb);
@@ -271,6 +252,12 @@ __global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kerne
         for (int f = 0; f < 4; ++f) {
             const int d = f >> 1;
             const R sgn = (f & 1) ? R(1) : R(-1);
+            R qh[NSTATE];
+            if (nbf[f] >= 0) {
+                const R* qn = Qin + (size_t)nbf[f] * ESTRIDE + vPh[f];
+#pragma unroll
+                for (int s = 0; s < NSTATE; ++s) qh[s] = qn[s * Np];
+            }
             R qm[NSTATE], Fm[NSTATE];
             PL::ld(sNode, NH, f * Nfp + c, qm);
             const CRV cr = sCR[f * Nfp + c];
@@ -281,7 +268,7 @@ __global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kerne
             const R lam_m = fabs(qm[1 + d] * ri_m) + c_m;
             const R jr[NSTATE] = {0, 0, 0, 0, 0};
             R fs[NSTATE];
-            face_flux<R, MIXED>(P, qm, Fm, lam_m, qh[f], nbf[f] < 0, lvh, d, sgn, jr, xi[d] * inv_w0, fs);
+            face_flux<R, MIXED>(P, qm, Fm, lam_m, qh, nbf[f] < 0, lvh, d, sgn, jr, xi[d] * inv_w0, fs);
             PL::st(sFace, NH, f * Nfp + c, fs);
         }
         R Di[Nq], Dj[Nq];
@@ -311,8 +298,10 @@ __global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kerne
     }
     __syncthreads();
 
-    // ---------------- phase C: horizontal face terms, source, update
+    // ---------------- phase C: horizontal face terms, source, update (the
+    // line's state and RK register are read here, where they are used)
     int bad = 0;
+    const size_t ebase = (size_t)e * ESTRIDE + c;
 #pragma unroll
     for (int k = 0; k < Nq; ++k) {
         auto sub_face = [&](int f, int idx) {
@@ -331,7 +320,14 @@ __global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kerne
         const R rkb_dt = KConst<R>::rkb_dt(P);
         R* Qout = static_cast<R*>(P.Qout);
 #pragma unroll
-        for (int k = 0; k < Nq; ++k)
+        for (int k = 0; k < Nq; ++k) {
+            R qk[NSTATE];
+            double dq_old[NSTATE];
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) {
+                qk[s] = qe[s * Np + k * Nfp];
+                if (read_reg) dq_old[s] = P.dQ[ebase + s * Np + k * Nfp];
+            }
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) {
                 const R rhs = acc[k][s];
@@ -339,25 +335,26 @@ __global__ void __launch_bounds__(ColCfg<N>::EPB*(N + 1) * (N + 1)) column_kerne
                 const size_t idx = ebase + s * Np + k * Nfp;
                 if (MODE == 0) {
                     double out = P.alpha * (double)rhs;
-                    if (read_reg) out = fma(P.beta, dq_old[k][s], out);
+                    if (read_reg) out = fma(P.beta, dq_old[s], out);
                     P.dQ[idx] = out;
                 } else {
                     double dq;
                     if (MIXED) {
                         if (read_reg) {
-                            dq = fma(P.rka, dq_old[k][s], f32_to_f64_bits((float)rhs));
-                            Qout[idx] = fma(rkb_dt, (R)f64_to_f32_bits(dq), q[k][s]);
+                            dq = fma(P.rka, dq_old[s], f32_to_f64_bits((float)rhs));
+                            Qout[idx] = fma(rkb_dt, (R)f64_to_f32_bits(dq), qk[s]);
                         } else {
                             dq = f32_to_f64_bits((float)rhs);
-                            Qout[idx] = fma(rkb_dt, rhs, q[k][s]);
+                            Qout[idx] = fma(rkb_dt, rhs, qk[s]);
                         }
                     } else {
-                        dq = read_reg ? fma(P.rka, dq_old[k][s], (double)rhs) : (double)rhs;
-                        Qout[idx] = (R)fma(P.rkb_dt, dq, (double)q[k][s]);
+                        dq = read_reg ? fma(P.rka, dq_old[s], (double)rhs) : (double)rhs;
+                        Qout[idx] = (R)fma(P.rkb_dt, dq, (double)qk[s]);
                     }
                     if (!P.last_stage) P.dQ[idx] = dq;
                 }
             }
+        }
     }
     // one pass per CTA: no barrier at the end, one vote per warp
     if (__any_sync(0xffffffffu, bad) && (lt & 31) == 0) atomicOr(P.status, 1u);
