@@ -267,6 +267,30 @@ struct Planar5<double> {
         base[4 * n + i] = v[4];
     }
 };
+// Asynchronous global->shared copies (cp.async, 4 or 8 bytes per thread):
+// the data goes to shared memory without passing through registers, so a
+// CTA can keep the next element's loads in flight while it computes.  Each
+// thread waits only for its own copy groups (cp.async.wait_group, a
+// hardware wait that ends when the thread's copies have landed).
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+template <typename R>
+__device__ __forceinline__ void cp_async_r(R* smem, const R* gmem) {
+    if constexpr (sizeof(R) == 4) cp_async4(smem, gmem);
+    else cp_async8(smem, gmem);
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
+}
+
 // words of R taken by `words` words rounded up to 16 bytes
 template <typename R>
 constexpr int planar_pad(int words) {

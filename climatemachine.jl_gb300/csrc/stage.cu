@@ -78,8 +78,19 @@ struct Smem {
     static constexpr size_t BYTES = sizeof(R) * TOTAL;
 };
 
-// Per-element inputs of one thread, loaded one element ahead (software
-// pipelining across the elements a persistent CTA visits).
+// Double-buffered staging of the next element's inputs for the persistent
+// kernel (byte offsets after Smem): states (5 x Np, R), RK register
+// (5 x Np, FP64), neighbour states at the face nodes (5 x 6 Nfp, R).
+template <int N, typename R>
+struct SmemAsync {
+    static constexpr int Nq = N + 1, Np = Nq * Nq * Nq, NFN = 6 * Nq * Nq;
+    static constexpr size_t QB = (Smem<N, R>::BYTES + 15) / 16 * 16;
+    static constexpr size_t DQB = QB + (2 * NSTATE * Np * sizeof(R) + 15) / 16 * 16;
+    static constexpr size_t QPB = DQB + 2 * NSTATE * Np * sizeof(double);
+    static constexpr size_t BYTES = QPB + 2 * NSTATE * NFN * sizeof(R);
+};
+
+// Per-element inputs of one thread.
 template <typename R>
 struct Ahead {
     R q[NSTATE];   // own node state (node threads)
@@ -88,11 +99,13 @@ struct Ahead {
     int ez;        // vertical element index of the element
 };
 
-// PERSIST: a grid of resident CTAs walks the elements with the next element's
-// inputs fetched one element ahead; otherwise one CTA per element.
 // Processes elements e_first, e_first + e_stride, ... below e_end with the
-// whole CTA; with PERSIST the next element's inputs are fetched one element
-// ahead.  Ends with a barrier, so the shared memory may be reused at once.
+// whole CTA.  PERSIST: a grid of resident CTAs walks the elements and copies
+// the next element's state, RK register and neighbour face states into
+// double-buffered shared memory with cp.async while it computes the current
+// one, so every CTA keeps memory requests in flight throughout (with plain
+// loads a CTA loads only at its start, which leaves HBM underused).  Every
+// thread reads back only the words it copied itself.
 template <int N, typename R, bool MIXED, int MODE, bool PERSIST>
 __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem_raw, int e_first, int e_stride,
                                            int e_end) {
@@ -152,21 +165,73 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
         }
     };
 
+    // persistent staging buffers and their copy issue (groups A: state and
+    // register of an element; B: neighbour face states)
+    using SA = SmemAsync<N, R>;
+    R* const qbuf = reinterpret_cast<R*>(smem_raw + SA::QB);
+    double* const dqbuf = reinterpret_cast<double*>(smem_raw + SA::DQB);
+    R* const qpbuf = reinterpret_cast<R*>(smem_raw + SA::QPB);
+    auto issue_A = [&](int ee, int b) {
+        if (ee < e_end && node_thread) {
+            const size_t base = (size_t)ee * ESTRIDE + t;
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) cp_async_r<R>(qbuf + (b * NSTATE + s) * Np + t, Qin + base + s * Np);
+            if (read_reg) {
+#pragma unroll
+                for (int s = 0; s < NSTATE; ++s) cp_async8(dqbuf + (b * NSTATE + s) * Np + t, P.dQ + base + s * Np);
+            }
+        }
+        cp_async_commit();
+    };
+    auto issue_B = [&](int ee, int nbv, int b) {
+        if (ee < e_end && nbv >= 0) {
+            const R* qn = Qin + (size_t)nbv * ESTRIDE + vP;
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) cp_async_r<R>(qpbuf + (b * NSTATE + s) * NFN + t, qn + s * Np);
+        }
+        cp_async_commit();
+    };
+
     int e = e_first;
     Ahead<R> cur;
-    if (PERSIST && e < e_end) fetch(e, cur);
-    for (; e < e_end; e += e_stride) {
-        if (!PERSIST) fetch(e, cur);
-        // RK register of this element (consumed in phase 3), then next element's inputs
+    int ez_n = 0, nb_n = -1;
+    if (PERSIST) {
+        if (e < e_end) {
+            ez_n = __ldg(P.nbr + NBR_STRIDE * e + 6);
+            nb_n = face_thread ? __ldg(P.nbr + NBR_STRIDE * e + f) : -1;
+        }
+        issue_A(e, 0);
+        issue_B(e, nb_n, 0);
+    }
+    for (int it = 0; e < e_end; e += e_stride, ++it) {
+        const int en = e + e_stride;
+        const int b = it & 1;
         double dq_old[NSTATE];
         const size_t ebase = (size_t)e * ESTRIDE + t;
-        if (node_thread && read_reg) {
+        if (PERSIST) {
+            cur.ez = ez_n;
+            cur.nb = nb_n;
+            if (en < e_end) {  // connectivity of the next element, used after phase 1
+                ez_n = __ldg(P.nbr + NBR_STRIDE * en + 6);
+                nb_n = face_thread ? __ldg(P.nbr + NBR_STRIDE * en + f) : -1;
+            }
+            cp_async_wait<1>();  // group A of this element has landed
+            if (node_thread) {
 #pragma unroll
-            for (int s = 0; s < NSTATE; ++s) dq_old[s] = P.dQ[ebase + s * Np];
+                for (int s = 0; s < NSTATE; ++s) cur.q[s] = qbuf[(b * NSTATE + s) * Np + t];
+                if (read_reg) {
+#pragma unroll
+                    for (int s = 0; s < NSTATE; ++s) dq_old[s] = dqbuf[(b * NSTATE + s) * Np + t];
+                }
+            }
+            issue_A(en, b ^ 1);
+        } else {
+            fetch(e, cur);
+            if (node_thread && read_reg) {
+#pragma unroll
+                for (int s = 0; s < NSTATE; ++s) dq_old[s] = P.dQ[ebase + s * Np];
+            }
         }
-        Ahead<R> nxt;
-        const int en = e + e_stride;
-        if (PERSIST && en < e_end) fetch(en, nxt);
 
         const int ez = cur.ez;
         const R xi[3] = {KConst<R>::metric(P, e, 0), KConst<R>::metric(P, e, 1), KConst<R>::metric(P, e, 2)};
@@ -189,6 +254,14 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
                 R rho_s = MIXED ? ((ph.ref_state && ph.subtract_off) ? cur.q[0] : lv.rho_ref + cur.q[0])
                                 : ((ph.ref_state && ph.subtract_off) ? cur.q[0] - lv.rho_ref : cur.q[0]);
                 gsrc = -rho_s * lv.gphiz;
+            }
+        }
+        if (PERSIST) {
+            issue_B(en, nb_n, b ^ 1);
+            cp_async_wait<2>();  // group B of this element has landed
+            if (cur.nb >= 0) {
+#pragma unroll
+                for (int s = 0; s < NSTATE; ++s) cur.qp[s] = qpbuf[(b * NSTATE + s) * NFN + t];
             }
         }
         __syncthreads();
@@ -315,8 +388,8 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
             // last element of this CTA: no barrier, one vote per warp
             if (__any_sync(0xffffffffu, bad) && (t & 31) == 0) atomicOr(P.status, 1u);
         }
-        if (PERSIST) cur = nxt;
     }
+    if (PERSIST) cp_async_wait<0>();  // the trailing (empty) groups
 }
 
 template <int N, typename R, bool MIXED, int MODE, bool PERSIST>
@@ -328,7 +401,7 @@ __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? (PERSIST ? Dims<N>::MIN_C
 
 template <int N, typename R, bool MIXED, int MODE, bool PERSIST>
 cudaError_t launch_mode(const KParams& P, int grid_ctas, cudaStream_t s) {
-    constexpr size_t bytes = Smem<N, R>::BYTES;
+    constexpr size_t bytes = PERSIST ? SmemAsync<N, R>::BYTES : Smem<N, R>::BYTES;
     // per-device set-up: opt in to > 48 KB of dynamic shared memory and size a
     // persistent grid from the occupancy of this instantiation
     static int resident[64] = {0};
