@@ -78,6 +78,8 @@ typedef struct {
     int with_divergence;// WithDivergence for turbulence==1
     double C_smag;      // Smagorinsky coefficient for turbulence==2
     double planet_radius; // SphericalOrientation: Phi = g (|x| - planet_radius)
+    int hyperdiffusion; // 0 = NoHyperDiffusion, 1 = DryBiharmonic (TurbulenceClosures.jl:793-848)
+    double tau_hyper;   // DryBiharmonic.tau_timescale
 } om_params;
 
 // StackedCubedSphereTopology (Topologies.jl:1620-1760) over a
@@ -101,7 +103,7 @@ enum { XI1X1 = 0, XI2X1, XI3X1, XI1X2, XI2X2, XI3X2, XI1X3, XI2X3, XI3X3, VM, VM
 constexpr int NSGEO = 5;
 enum { SN1 = 0, SN2, SN3, SSM, SVMI };
 // auxiliary fields per node (own ordering; content as AtmosModel.jl:465-481)
-enum { AX = 0, AY, AZ, APHI, AGPX, AGPY, AGPZ, ARHO_REF, AP_REF, AT_REF, ARHOE_REF, ATHV, AAIRT, ADELTA, NAUX };
+enum { AX = 0, AY, AZ, APHI, AGPX, AGPY, AGPZ, ARHO_REF, AP_REF, AT_REF, ARHOE_REF, ATHV, AAIRT, ADELTA, AHDELTA, NAUX };
 constexpr int NS = 5;   // rho, rhou(3), rhoe
 
 struct Model {
@@ -118,6 +120,13 @@ struct Model {
     std::vector<int64_t> elemtoelem;
     int ngf;                                 // gradient-flux words per node
     std::vector<double> gradflux;            // (Np, ngf, nelem)
+    // hyperdiffusion: Qhypervisc_grad (Np, 12, nelem) holds grad(u_h, h_tot)
+    // after the gradient pass and nu grad^3 (u_h, h_tot) after the gradients
+    // of the laplacians; Qhypervisc_div (Np, 4, nelem) the laplacians
+    std::vector<double> hgrad, hdiv;
+    int ngl = 4;                             // GradientLaplacian states per node
+    int law = 0;                             // 0 = AtmosModel, 1 = scalar constant-tensor hyperdiffusion
+    double Hten[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // law 1: tensor H, column-major
 };
 
 // ----------------------------------------------------------------------------
@@ -766,6 +775,13 @@ void init_aux(Model& m) {
             // invJ = [xi1x1 xi1x2 xi1x3; xi2x1 ...; xi3x1 ...]
             double det = a * (f * j - g * i) - b * (d * j - g * h) + c * (d * i - f * h);
             AUX(m, e, ADELTA, n) = 2 / (std::cbrt(det) * std::max(1, m.N));
+            // lengthscale_horizontal, Geometry.jl:129-151: the columns dx/dxi_1 and
+            // dx/dxi_2 of invJ^-1 (cofactors / det), their lengths 2/N, averaged
+            double c1[3] = {(f * j - g * i) / det, -(d * j - g * h) / det, (d * i - f * h) / det};
+            double c2[3] = {-(b * j - c * i) / det, (a * j - c * h) / det, -(a * i - b * h) / det};
+            double D1 = std::sqrt(c1[0] * c1[0] + c1[1] * c1[1] + c1[2] * c1[2]) * 2 / m.N;
+            double D2 = std::sqrt(c2[0] * c2[0] + c2[1] * c2[1] + c2[2] * c2[2]) * 2 / m.N;
+            AUX(m, e, AHDELTA, n) = (D1 + D2) / 2;
         }
 }
 
@@ -811,11 +827,29 @@ void flux_first_order(const om_params& p, const double q[NS], const NodeAux& a, 
 
 // Second-order flux (tendencies_momentum.jl:37-42, tendencies_energy.jl:27-31,
 // 51-56; turbulence_tensors TurbulenceClosures.jl:199-225, 368-404, 472-505).
-void flux_second_order(const Model& m, const double q[NS], const double* gf, const NodeAux& a, double F[3][NS]) {
+//
+// With hyperdiffusion, hd holds the node's nu grad^3 words (3 c + d for
+// u_h[c], 9 + d for h_tot) and the fluxes HyperdiffViscousFlux and
+// HyperdiffEnthalpyFlux are added (tendencies_momentum.jl:51-54,
+// tendencies_energy.jl:40-48).
+void hyper_flux(const double q[NS], const double* hd, double F[3][NS]) {
+    double rho = q[0];
+    const double* ru = q + 1;
+    for (int d = 0; d < 3; ++d) {
+        for (int c = 0; c < 3; ++c) F[d][1 + c] += rho * hd[3 * c + d];
+        F[d][4] += (hd[d] * ru[0] + hd[3 + d] * ru[1] + hd[6 + d] * ru[2]) + hd[9 + d] * rho;
+    }
+}
+
+void flux_second_order(const Model& m, const double q[NS], const double* gf, const NodeAux& a, double F[3][NS],
+                       const double* hd = nullptr) {
     const om_params& p = m.prm;
     for (int d = 0; d < 3; ++d)
         for (int s = 0; s < NS; ++s) F[d][s] = 0;
-    if (p.turbulence == 0) return;
+    if (p.turbulence == 0) {
+        if (hd) hyper_flux(q, hd, F);
+        return;
+    }
     double rho = q[0];
     const double* ru = q + 1;
     double S[3][3] = {{gf[3], gf[4], gf[5]}, {gf[4], gf[6], gf[7]}, {gf[5], gf[7], gf[8]}};
@@ -859,6 +893,7 @@ void flux_second_order(const Model& m, const double q[NS], const double* gf, con
         double tr = tau[d][0] * ru[0] + tau[d][1] * ru[1] + tau[d][2] * ru[2];
         F[d][4] = tr + (-Dt[d] * gf[d]) * rho;
     }
+    if (hd) hyper_flux(q, hd, F);
 }
 
 // Gravity source (tendencies_momentum.jl:64-72)
@@ -1014,6 +1049,277 @@ void gradient_pass(Model& m, const double* Q) {
     }
 }
 
+// ----------------------------------------------------------------------------
+// Hyperdiffusion passes (DGModel.jl:200-301), shared by the AtmosModel's
+// DryBiharmonic closure (TurbulenceClosures.jl:793-848; GradientLaplacian
+// states s = u_h[0..2], h_tot) and the constant-tensor scalar hyperdiffusion
+// of test/Numerics/DGMethods/advection_diffusion (one state, rho).
+// Qhypervisc_grad word 3 s + d holds d/dx_d of state s (first the gradient,
+// later the hyperdiffusive state), Qhypervisc_div word s its laplacian.
+// ----------------------------------------------------------------------------
+
+// compute_gradient_argument! (TurbulenceClosures.jl:813-827):
+// u_h = (I - khat khat') u with khat = grad Phi / g, and h_tot.
+void hyper_argument(const om_params& p, const double G[5], const NodeAux& a, double H[4]) {
+    double k[3] = {a.gPhi[0] / p.grav, a.gPhi[1] / p.grav, a.gPhi[2] / p.grav};
+    for (int r = 0; r < 3; ++r) {
+        double acc = 0;
+        for (int c = 0; c < 3; ++c) acc += ((r == c ? 1.0 : 0.0) - k[r] * k[c]) * G[c];
+        H[r] = acc;
+    }
+    H[3] = G[3];
+}
+
+inline double& HG(Model& m, int64_t e, int w, int n) { return m.hgrad[(e * 3 * m.ngl + w) * m.Np + n]; }
+inline double HGc(const Model& m, int64_t e, int w, int n) { return m.hgrad[(e * 3 * m.ngl + w) * m.Np + n]; }
+inline double& HD(Model& m, int64_t e, int s, int n) { return m.hdiv[(e * m.ngl + s) * m.Np + n]; }
+inline double HDc(const Model& m, int64_t e, int s, int n) { return m.hdiv[(e * m.ngl + s) * m.Np + n]; }
+
+// GradientLaplacian arguments of node n of element e (the minus-side state)
+void node_hyper_args(const Model& m, const double* Q, int64_t e, int n, double* H) {
+    if (m.law == 1) {
+        H[0] = Q[e * m.Np + n];  // compute_gradient_argument!: transform.rho = state.rho
+        return;
+    }
+    double q[NS], G[5];
+    load_q(m, Q, e, n, q);
+    NodeAux a = node_aux(m, e, n);
+    gradient_argument(m.prm, q, a.Phi, a.thv, G);
+    hyper_argument(m.prm, G, a, H);
+}
+
+// Gradients of the GradientLaplacian states into Qhypervisc_grad: the
+// strong-form volume gradient (volume_gradients!, DGModel_kernels.jl:1083-1098,
+// horizontal then vertical increment) and the central interface correction
+// vMI sM (G* - n G-) (dgsem_interface_gradients!, :1618-1627), with
+// G* = n G+ of the FreeSlip gradient boundary state on walls.
+void hyper_gradient_pass(Model& m, const double* Q) {
+    const om_params& p = m.prm;
+    const int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp, ngl = m.ngl;
+    m.hgrad.assign((size_t)m.nelem * 3 * ngl * Np, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m.nelem; ++e) {
+        std::vector<double> H(Np * ngl);
+        for (int n = 0; n < Np; ++n) node_hyper_args(m, Q, e, n, &H[n * ngl]);
+        for (int k = 0; k < Nq; ++k)
+            for (int j = 0; j < Nq; ++j)
+                for (int i = 0; i < Nq; ++i) {
+                    int ijk = i + Nq * (j + Nq * k);
+                    for (int s = 0; s < ngl; ++s) {
+                        double G1 = 0, G2 = 0, G3 = 0;
+                        for (int n = 0; n < Nq; ++n) {
+                            G1 += Dm(m, i, n) * H[(n + Nq * (j + Nq * k)) * ngl + s];
+                            G2 += Dm(m, j, n) * H[(i + Nq * (n + Nq * k)) * ngl + s];
+                            G3 += Dm(m, k, n) * H[(i + Nq * (j + Nq * n)) * ngl + s];
+                        }
+                        for (int d = 0; d < 3; ++d) {
+                            double gH = VGc(m, e, XI1X1 + 3 * d, ijk) * G1 + VGc(m, e, XI2X1 + 3 * d, ijk) * G2;
+                            double gV = VGc(m, e, XI3X1 + 3 * d, ijk) * G3;
+                            HG(m, e, 3 * s + d, ijk) = gH + gV;
+                        }
+                    }
+                }
+        for (int f = 0; f < 6; ++f)
+            for (int n = 0; n < Nfp; ++n) {
+                int64_t idM = m.vmapM[(e * 6 + f) * Nfp + n], idP = m.vmapP[(e * 6 + f) * Nfp + n];
+                int vM = (int)(idM % Np);
+                int64_t eP = idP / Np; int vP = (int)(idP % Np);
+                int tag = m.elemtobndy[e * 6 + f];
+                double nv[3] = {SGc(m, e, f, n, SN1), SGc(m, e, f, n, SN2), SGc(m, e, f, n, SN3)};
+                double sM = SGc(m, e, f, n, SSM), vMI = SGc(m, e, f, n, SVMI);
+                const double* HM = &H[vM * ngl];
+                double HP[4], Hs[3][4];
+                if (tag == 0) {
+                    node_hyper_args(m, Q, eP, vP, HP);
+                    for (int d = 0; d < 3; ++d)
+                        for (int s = 0; s < ngl; ++s) Hs[d][s] = nv[d] * (HP[s] + HM[s]) / 2;
+                } else {
+                    double qM[NS], qP[NS], G[5];
+                    load_q(m, Q, e, vM, qM);
+                    bc_state_grad(qM, nv, qP);
+                    NodeAux aM = node_aux(m, e, vM);
+                    gradient_argument(p, qP, aM.Phi, aM.thv, G);
+                    hyper_argument(p, G, aM, HP);
+                    for (int d = 0; d < 3; ++d)
+                        for (int s = 0; s < ngl; ++s) Hs[d][s] = nv[d] * HP[s];
+                }
+                for (int s = 0; s < ngl; ++s)
+                    for (int d = 0; d < 3; ++d) HG(m, e, 3 * s + d, vM) += vMI * sM * (Hs[d][s] - nv[d] * HM[s]);
+            }
+    }
+}
+
+// Laplacians Qhypervisc_div = M^-1 (D^T M grad G + sum_f L^T Mf (grad G)*):
+// volume_divergence_of_gradients! (DGModel_kernels.jl:2132-2330, horizontal
+// then vertical increment) and interface_divergence_of_gradients!
+// (:2360-2495) with the central penalty (grad G+ + grad G-)' n / 2
+// (NumericalFluxes.jl:720-730); on walls grad G+ = grad G-
+// (src/Atmos/Model/boundaryconditions.jl:88-95).
+void hyper_divergence_pass(Model& m) {
+    const int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp, ngl = m.ngl;
+    m.hdiv.assign((size_t)m.nelem * ngl * Np, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m.nelem; ++e) {
+        std::vector<double> S1(Np * ngl), S2(Np * ngl), S3(Np * ngl);
+        for (int n = 0; n < Np; ++n) {
+            double M = VGc(m, e, VM, n);
+            for (int s = 0; s < ngl; ++s) {
+                double G1 = HGc(m, e, 3 * s + 0, n), G2 = HGc(m, e, 3 * s + 1, n), G3 = HGc(m, e, 3 * s + 2, n);
+                S1[n * ngl + s] = M * (VGc(m, e, XI1X1, n) * G1 + VGc(m, e, XI1X2, n) * G2 + VGc(m, e, XI1X3, n) * G3);
+                S2[n * ngl + s] = M * (VGc(m, e, XI2X1, n) * G1 + VGc(m, e, XI2X2, n) * G2 + VGc(m, e, XI2X3, n) * G3);
+                S3[n * ngl + s] = M * (VGc(m, e, XI3X1, n) * G1 + VGc(m, e, XI3X2, n) * G2 + VGc(m, e, XI3X3, n) * G3);
+            }
+        }
+        for (int k = 0; k < Nq; ++k)
+            for (int j = 0; j < Nq; ++j)
+                for (int i = 0; i < Nq; ++i) {
+                    int ijk = i + Nq * (j + Nq * k);
+                    double MI = VGc(m, e, VMI, ijk);
+                    for (int s = 0; s < ngl; ++s) {
+                        double lh = 0, lv = 0;
+                        for (int n = 0; n < Nq; ++n) {
+                            lh -= MI * Dm(m, n, i) * S1[(n + Nq * (j + Nq * k)) * ngl + s];
+                            lh -= MI * Dm(m, n, j) * S2[(i + Nq * (n + Nq * k)) * ngl + s];
+                        }
+                        for (int n = 0; n < Nq; ++n) lv -= MI * Dm(m, n, k) * S3[(i + Nq * (j + Nq * n)) * ngl + s];
+                        HD(m, e, s, ijk) = lh + lv;
+                    }
+                }
+        for (int f = 0; f < 6; ++f)
+            for (int n = 0; n < Nfp; ++n) {
+                int64_t idM = m.vmapM[(e * 6 + f) * Nfp + n], idP = m.vmapP[(e * 6 + f) * Nfp + n];
+                int vM = (int)(idM % Np);
+                int64_t eP = idP / Np; int vP = (int)(idP % Np);
+                int tag = m.elemtobndy[e * 6 + f];
+                if (tag != 0) { eP = e; vP = vM; }
+                double nv[3] = {SGc(m, e, f, n, SN1), SGc(m, e, f, n, SN2), SGc(m, e, f, n, SN3)};
+                double sM = SGc(m, e, f, n, SSM), vMI = SGc(m, e, f, n, SVMI);
+                for (int s = 0; s < ngl; ++s) {
+                    double acc = 0;
+                    for (int d = 0; d < 3; ++d)
+                        acc += (HGc(m, eP, 3 * s + d, vP) + HGc(m, e, 3 * s + d, vM)) * (nv[d] / 2);
+                    HD(m, e, s, vM) += vMI * sM * acc;
+                }
+            }
+    }
+}
+
+// transform_post_gradient_laplacian! of a gradient g (word 3 s + d) at a node:
+// DryBiharmonic nu_4 g with nu_4 = (Delta_h / 2)^4 / 2 / tau
+// (TurbulenceClosures.jl:829-848), or eta = H g for the constant tensor H
+// (test/Numerics/DGMethods/advection_diffusion/advection_diffusion_model.jl:310-326).
+void hyper_transform(const Model& m, int64_t e, int n, const double* g, double* out) {
+    if (m.law == 1) {
+        for (int d = 0; d < 3; ++d) out[d] = m.Hten[d] * g[0] + m.Hten[d + 3] * g[1] + m.Hten[d + 6] * g[2];
+        return;
+    }
+    double h = AUXc(m, e, AHDELTA, n) / 2;
+    double nu4 = h * h * h * h / 2 / m.prm.tau_hyper;
+    for (int w = 0; w < 12; ++w) out[w] = nu4 * g[w];
+}
+
+// Hyperdiffusive state into Qhypervisc_grad: volume_gradients_of_laplacians!
+// (DGModel_kernels.jl:2525-2845; horizontal kernel writes T(grad_H lap), the
+// vertical one adds T(grad_V lap)) and interface_gradients_of_laplacians!
+// adding T(n (lap+ - lap-) / 2) (NumericalFluxes.jl:768-790); zero on walls
+// where lap+ = lap-.
+void hyper_gradlap_pass(Model& m) {
+    const int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp, ngl = m.ngl, nw = 3 * m.ngl;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m.nelem; ++e) {
+        for (int k = 0; k < Nq; ++k)
+            for (int j = 0; j < Nq; ++j)
+                for (int i = 0; i < Nq; ++i) {
+                    int ijk = i + Nq * (j + Nq * k);
+                    double gH[12], gV[12], tH[12], tV[12];
+                    for (int s = 0; s < ngl; ++s) {
+                        double L1 = 0, L2 = 0, L3 = 0;
+                        for (int n = 0; n < Nq; ++n) {
+                            L1 += Dm(m, i, n) * HDc(m, e, s, n + Nq * (j + Nq * k));
+                            L2 += Dm(m, j, n) * HDc(m, e, s, i + Nq * (n + Nq * k));
+                            L3 += Dm(m, k, n) * HDc(m, e, s, i + Nq * (j + Nq * n));
+                        }
+                        for (int d = 0; d < 3; ++d) {
+                            gH[3 * s + d] = VGc(m, e, XI1X1 + 3 * d, ijk) * L1 + VGc(m, e, XI2X1 + 3 * d, ijk) * L2;
+                            gV[3 * s + d] = VGc(m, e, XI3X1 + 3 * d, ijk) * L3;
+                        }
+                    }
+                    hyper_transform(m, e, ijk, gH, tH);
+                    hyper_transform(m, e, ijk, gV, tV);
+                    for (int w = 0; w < nw; ++w) HG(m, e, w, ijk) = tH[w] + tV[w];
+                }
+        for (int f = 0; f < 6; ++f)
+            for (int n = 0; n < Nfp; ++n) {
+                if (m.elemtobndy[e * 6 + f] != 0) continue;
+                int64_t idM = m.vmapM[(e * 6 + f) * Nfp + n], idP = m.vmapP[(e * 6 + f) * Nfp + n];
+                int vM = (int)(idM % Np);
+                int64_t eP = idP / Np; int vP = (int)(idP % Np);
+                double nv[3] = {SGc(m, e, f, n, SN1), SGc(m, e, f, n, SN2), SGc(m, e, f, n, SN3)};
+                double sM = SGc(m, e, f, n, SSM), vMI = SGc(m, e, f, n, SVMI);
+                double G[12], T[12];
+                for (int s = 0; s < ngl; ++s) {
+                    double dl = HDc(m, eP, s, vP) - HDc(m, e, s, vM);
+                    for (int d = 0; d < 3; ++d) G[3 * s + d] = nv[d] * dl / 2;
+                }
+                hyper_transform(m, e, vM, G, T);
+                for (int w = 0; w < nw; ++w) HG(m, e, w, vM) += vMI * sM * T[w];
+            }
+    }
+}
+
+void hyper_passes(Model& m, const double* Q) {
+    hyper_gradient_pass(m, Q);
+    hyper_divergence_pass(m);
+    hyper_gradlap_pass(m);
+}
+
+// Tendency of the constant-tensor scalar hyperdiffusion model
+// (periodic_3D_hyperdiffusion.jl with advection = diffusion = false):
+// d rho/dt = -div(eta), eta = H grad(lap rho); weak-form volume divergence
+// (DGModel_kernels.jl:64-300) and the central second-order numerical flux
+// (eta- + eta+)' n / 2 (NumericalFluxes.jl:670-715).
+void scalar_hyper_tendency(Model& m, double* T, const double* Q, double alpha, double beta) {
+    const int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp;
+    hyper_passes(m, Q);
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m.nelem; ++e) {
+        std::vector<double> F1(Np), F2(Np), F3(Np);
+        for (int n = 0; n < Np; ++n) {
+            double M = VGc(m, e, VM, n);
+            double F[3] = {HGc(m, e, 0, n), HGc(m, e, 1, n), HGc(m, e, 2, n)};
+            F1[n] = M * (VGc(m, e, XI1X1, n) * F[0] + VGc(m, e, XI1X2, n) * F[1] + VGc(m, e, XI1X3, n) * F[2]);
+            F2[n] = M * (VGc(m, e, XI2X1, n) * F[0] + VGc(m, e, XI2X2, n) * F[1] + VGc(m, e, XI2X3, n) * F[2]);
+            F3[n] = M * (VGc(m, e, XI3X1, n) * F[0] + VGc(m, e, XI3X2, n) * F[1] + VGc(m, e, XI3X3, n) * F[2]);
+        }
+        for (int k = 0; k < Nq; ++k)
+            for (int j = 0; j < Nq; ++j)
+                for (int i = 0; i < Nq; ++i) {
+                    int ijk = i + Nq * (j + Nq * k);
+                    double MI = VGc(m, e, VMI, ijk);
+                    double lh = 0, lv = 0;
+                    for (int n = 0; n < Nq; ++n) {
+                        lh += MI * Dm(m, n, i) * F1[n + Nq * (j + Nq * k)];
+                        lh += MI * Dm(m, n, j) * F2[i + Nq * (n + Nq * k)];
+                    }
+                    for (int n = 0; n < Nq; ++n) lv += MI * Dm(m, n, k) * F3[i + Nq * (j + Nq * n)];
+                    size_t idx = (size_t)e * Np + ijk;
+                    double Th = (beta != 0) ? alpha * lh + beta * T[idx] : alpha * lh;
+                    T[idx] = alpha * lv + Th;
+                }
+        for (int f = 0; f < 6; ++f)
+            for (int n = 0; n < Nfp; ++n) {
+                int64_t idM = m.vmapM[(e * 6 + f) * Nfp + n], idP = m.vmapP[(e * 6 + f) * Nfp + n];
+                int vM = (int)(idM % Np);
+                int64_t eP = idP / Np; int vP = (int)(idP % Np);
+                double nv[3] = {SGc(m, e, f, n, SN1), SGc(m, e, f, n, SN2), SGc(m, e, f, n, SN3)};
+                double sM = SGc(m, e, f, n, SSM), vMI = SGc(m, e, f, n, SVMI);
+                double fl = 0;
+                for (int d = 0; d < 3; ++d) fl += (HGc(m, e, d, vM) + HGc(m, eP, d, vP)) * (nv[d] / 2);
+                T[(size_t)e * Np + vM] -= alpha * vMI * sM * fl;
+            }
+    }
+}
+
 // Numerical flux F*.n at one face node: Rusanov/central first order
 // (NumericalFluxes.jl:219-340, boundary wrapper :163-205) plus central
 // second order (:668-715; zero on FreeSlip/Insulating walls,
@@ -1047,15 +1353,23 @@ void face_flux(const Model& m, const double* Q, int64_t e, int f, int n, double 
         double mw = std::max(wM, wP);
         for (int s = 0; s < NS; ++s) fl[s] += mw * (qM[s] - qP[s]) / 2;
     }
-    if (p.turbulence != 0 && tag == 0) {
-        const double* gM = &m.gradflux[0];
-        double gfM[10], gfP[10];
-        for (int s = 0; s < ngf; ++s) {
-            gfM[s] = gM[(e * ngf + s) * Np + vM];
-            gfP[s] = gM[(eP * ngf + s) * Np + vP];
+    if ((p.turbulence != 0 || p.hyperdiffusion != 0) && tag == 0) {
+        double gfM[10] = {0}, gfP[10] = {0}, hdM[12], hdP[12];
+        if (p.turbulence != 0) {
+            const double* gM = &m.gradflux[0];
+            for (int s = 0; s < ngf; ++s) {
+                gfM[s] = gM[(e * ngf + s) * Np + vM];
+                gfP[s] = gM[(eP * ngf + s) * Np + vP];
+            }
         }
-        flux_second_order(m, qM, gfM, aM, FM);
-        flux_second_order(m, qP, gfP, aP, FP);
+        if (p.hyperdiffusion != 0)
+            for (int w = 0; w < 12; ++w) {
+                hdM[w] = HGc(m, e, w, vM);
+                hdP[w] = HGc(m, eP, w, vP);
+            }
+        const bool hyp = p.hyperdiffusion != 0;
+        flux_second_order(m, qM, gfM, aM, FM, hyp ? hdM : nullptr);
+        flux_second_order(m, qP, gfP, aP, FP, hyp ? hdP : nullptr);
         for (int s = 0; s < NS; ++s) {
             double acc = 0;
             for (int d = 0; d < 3; ++d) acc += (FM[d][s] + FP[d][s]) * (nv[d] / 2);
@@ -1071,6 +1385,7 @@ void tendency(Model& m, double* T, const double* Q, double t, double alpha, doub
     int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp, ngf = m.ngf;
     update_aux(m, Q);
     if (p.turbulence != 0) gradient_pass(m, Q);
+    if (p.hyperdiffusion != 0) hyper_passes(m, Q);
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < m.nelem; ++e) {
         std::vector<double> F1(Np * NS), F2(Np * NS), F3(Np * NS), Src(Np * NS);
@@ -1080,10 +1395,13 @@ void tendency(Model& m, double* T, const double* Q, double t, double alpha, doub
             NodeAux a = node_aux(m, e, n);
             double F[3][NS], G[3][NS];
             flux_first_order(p, q, a, F);
-            if (p.turbulence != 0) {
-                double gf[10];
-                for (int s = 0; s < ngf; ++s) gf[s] = m.gradflux[(e * ngf + s) * Np + n];
-                flux_second_order(m, q, gf, a, G);
+            if (p.turbulence != 0 || p.hyperdiffusion != 0) {
+                double gf[10] = {0}, hd[12];
+                if (p.turbulence != 0)
+                    for (int s = 0; s < ngf; ++s) gf[s] = m.gradflux[(e * ngf + s) * Np + n];
+                if (p.hyperdiffusion != 0)
+                    for (int w = 0; w < 12; ++w) hd[w] = HGc(m, e, w, n);
+                flux_second_order(m, q, gf, a, G, p.hyperdiffusion != 0 ? hd : nullptr);
                 for (int d = 0; d < 3; ++d)
                     for (int s = 0; s < NS; ++s) F[d][s] += G[d][s];
             }
@@ -1220,6 +1538,48 @@ om_model* om_create_shell(const om_shell* sh, const om_params* p) {
     return m;
 }
 
+// Constant-tensor scalar hyperdiffusion on a brick (one state per node,
+// layout (Np, 1, nelem)); H column-major 3x3.
+om_model* om_create_scalar_hyper(const om_brick* b, const double* H) {
+    om_params p;
+    std::memset(&p, 0, sizeof(p));
+    Model* m = new Model();
+    m->mesh = *b;
+    m->prm = p;
+    m->law = 1;
+    m->ngl = 1;
+    for (int i = 0; i < 9; ++i) m->Hten[i] = H[i];
+    m->N = b->N;
+    m->Nq = b->N + 1;
+    m->Np = m->Nq * m->Nq * m->Nq;
+    m->Nfp = m->Nq * m->Nq;
+    m->nelem = (int64_t)b->ne[0] * b->ne[1] * b->ne[2];
+    m->ngf = 9;
+    lgl(m->N, m->xi, m->omega);
+    spectral_derivative(m->xi, m->D);
+    build_geometry(*m);
+    init_aux(*m);
+    return m;
+}
+
+void om_scalar_hyper_tendency(om_model* m, double* dQ, const double* Q, double alpha, double beta) {
+    scalar_hyper_tendency(*m, dQ, Q, alpha, beta);
+}
+
+// nsteps LSRK54 steps (LowStorageRungeKuttaMethod.jl:102-158) of the scalar model
+void om_scalar_hyper_lsrk54(om_model* m, double* Q, double* dQ, double dt, int nsteps) {
+    size_t len = (size_t)m->nelem * m->Np;
+    for (int it = 0; it < nsteps; ++it)
+        for (int s = 0; s < 5; ++s) {
+            scalar_hyper_tendency(*m, dQ, Q, 1.0, 1.0);
+            double a = RKA[(s + 1) % 5], b = RKB[s];
+            for (size_t i = 0; i < len; ++i) {
+                Q[i] += b * dt * dQ[i];
+                dQ[i] *= a;
+            }
+        }
+}
+
 void om_free(om_model* m) { delete m; }
 
 int64_t om_nelem(const om_model* m) { return m->nelem; }
@@ -1256,6 +1616,15 @@ void om_gradient_pass(om_model* m, const double* Q) {
     update_aux(*m, Q);
     gradient_pass(*m, Q);
 }
+
+// Hyperdiffusion passes only: afterwards om_hyper_grad holds nu grad^3
+// (Np, 12, nelem) and om_hyper_div the laplacians (Np, 4, nelem).
+void om_hyper_pass(om_model* m, const double* Q) {
+    update_aux(*m, Q);
+    hyper_passes(*m, Q);
+}
+const double* om_hyper_grad(const om_model* m) { return m->hgrad.data(); }
+const double* om_hyper_div(const om_model* m) { return m->hdiv.data(); }
 
 // nsteps LSRK54 steps of size dt from time t0 (dQ is the solver's register)
 void om_lsrk54(om_model* m, double* Q, double* dQ, double t0, double dt, int nsteps) {

@@ -72,6 +72,8 @@ class Params(ctypes.Structure):
         ("with_divergence", ctypes.c_int),
         ("C_smag", ctypes.c_double),
         ("planet_radius", ctypes.c_double),
+        ("hyperdiffusion", ctypes.c_int),
+        ("tau_hyper", ctypes.c_double),
     ]
 
 
@@ -126,6 +128,10 @@ def lib():
         L.om_set_threads.argtypes = [ctypes.c_int]
         L.om_tendency.argtypes = [P, dp, dp, D, D, D]
         L.om_gradient_pass.argtypes = [P, dp]
+        L.om_hyper_pass.argtypes = [P, dp]
+        for name in ("om_hyper_grad", "om_hyper_div"):
+            getattr(L, name).restype = dp
+            getattr(L, name).argtypes = [P]
         L.om_lsrk54.argtypes = [P, dp, dp, D, D, ctypes.c_int]
         L.om_solve.restype = ctypes.c_int
         L.om_solve.argtypes = [P, dp, D, D, D]
@@ -146,6 +152,10 @@ def lib():
         ip = ctypes.POINTER(ctypes.c_int)
         L.om_apply_filter.argtypes = [P, dp, dp, dp, ctypes.c_int, ip, ctypes.c_int]
         L.om_apply_tmar.argtypes = [P, dp, ip, ctypes.c_int]
+        L.om_create_scalar_hyper.restype = P
+        L.om_create_scalar_hyper.argtypes = [ctypes.POINTER(Brick), dp]
+        L.om_scalar_hyper_tendency.argtypes = [P, dp, dp, D, D]
+        L.om_scalar_hyper_lsrk54.argtypes = [P, dp, dp, D, ctypes.c_int]
         L.om_lsrk54_scalar.restype = D
         L.om_lsrk54_scalar.argtypes = [D, D, D]
         _lib = L
@@ -162,8 +172,9 @@ def set_threads(n: int) -> int:
 
 
 # Auxiliary field indices of the oracle's (Np, NAUX, nelem) aux array
-AUX = dict(x=0, y=1, z=2, Phi=3, gPhi=4, rho_ref=7, p_ref=8, T_ref=9, rhoe_ref=10, theta_v=11, air_T=12, Delta=13)
-NAUX = 14
+AUX = dict(x=0, y=1, z=2, Phi=3, gPhi=4, rho_ref=7, p_ref=8, T_ref=9, rhoe_ref=10, theta_v=11, air_T=12, Delta=13,
+           Delta_h=14)
+NAUX = 15
 VGEO = dict(xi1x1=0, xi2x1=1, xi3x1=2, xi1x2=3, xi2x2=4, xi3x2=5, xi1x3=6, xi2x3=7, xi3x3=8, M=9, MI=10, MH=11,
             x1=12, x2=13, x3=14, JcV=15)
 
@@ -193,6 +204,8 @@ class OracleModel:
         p.rho_nu = physics.get("rho_nu", 0.0)
         p.with_divergence = int(physics.get("with_divergence", False))
         p.C_smag = physics.get("C_smag", consts["C_smag"])
+        p.hyperdiffusion = {"none": 0, "dry_biharmonic": 1}[physics.get("hyperdiffusion", "none")]
+        p.tau_hyper = physics.get("tau_hyper", 0.0)
         self.params, self.consts = p, consts
         self.L = lib()
         if shell is None:
@@ -290,6 +303,13 @@ class OracleModel:
         self.L.om_gradient_pass(self.h, _ptr(Q))
         return self.gradflux
 
+    def hyper_pass(self, Q):
+        """Hyperdiffusion passes of Q: returns (nu grad^3 (nelem, 12, Np),
+        laplacians (nelem, 4, Np))."""
+        self.L.om_hyper_pass(self.h, _ptr(Q))
+        return (self._view(self.L.om_hyper_grad, (self.nelem, 12, self.Np)),
+                self._view(self.L.om_hyper_div, (self.nelem, 4, self.Np)))
+
     def lsrk54(self, Q, dt, nsteps, t0=0.0, dQ=None):
         if dQ is None:
             dQ = self.state()
@@ -371,3 +391,50 @@ def apply_tmar(model, Q, fields):
 def lsrk54_scalar(q0: float, dt: float, timeend: float) -> float:
     """q' = q cos t integrated with the oracle's LSRK54 (exact: q0 exp(sin t))."""
     return lib().om_lsrk54_scalar(q0, dt, timeend)
+
+
+class ScalarHyperdiffusion:
+    """Constant-tensor scalar hyperdiffusion d rho/dt = -div(H grad lap rho)
+    on a brick (the AdvectionDiffusion model of
+    test/Numerics/DGMethods/advection_diffusion/periodic_3D_hyperdiffusion.jl),
+    evaluated by the same hyperdiffusion passes as the AtmosModel closure."""
+
+    def __init__(self, N, ne, lo, hi, H, periodic=(1, 1, 1)):
+        b = Brick()
+        b.N = N
+        for d in range(3):
+            b.ne[d], b.lo[d], b.hi[d], b.periodic[d] = ne[d], lo[d], hi[d], int(periodic[d])
+            b.bc_lo[d], b.bc_hi[d] = 1, 2
+        self.L = lib()
+        Hc = np.ascontiguousarray(np.asarray(H, dtype=np.float64).T.reshape(9))  # column-major
+        self.brick = b
+        self.h = self.L.om_create_scalar_hyper(ctypes.byref(b), _ptr(Hc))
+        self.N, self.Nq = N, N + 1
+        self.Np = self.L.om_Np(self.h)
+        self.nelem = self.L.om_nelem(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.om_free(self.h)
+            self.h = None
+
+    @property
+    def vgeo(self):
+        ptr = self.L.om_vgeo(self.h)
+        n = self.nelem * 16 * self.Np
+        return np.array(np.ctypeslib.as_array(ptr, shape=(n,))).reshape(self.nelem, 16, self.Np)
+
+    def state(self):
+        return np.zeros((self.nelem, 1, self.Np), dtype=np.float64)
+
+    def tendency(self, Q, alpha=1.0, beta=0.0, dQ=None):
+        if dQ is None:
+            dQ = self.state()
+        self.L.om_scalar_hyper_tendency(self.h, _ptr(dQ), _ptr(Q), alpha, beta)
+        return dQ
+
+    def lsrk54(self, Q, dt, nsteps, dQ=None):
+        if dQ is None:
+            dQ = self.state()
+        self.L.om_scalar_hyper_lsrk54(self.h, _ptr(Q), _ptr(dQ), dt, nsteps)
+        return Q, dQ

@@ -11,6 +11,10 @@ Pins (reference paths relative to the ClimateMachine.jl project root):
     the LES brick and on the GCM stacked cubed shell (3 x 3 horizontal
     elements per panel, 3 vertical, 50 km, N=4, IsothermalProfile,
     subtract_off = false, 100 s of LSRK54 at Courant 0.1)
+  * constant-tensor scalar hyperdiffusion, 3D, EveryDirection, N=4, levels
+    1 and 2 — test/Numerics/DGMethods/advection_diffusion/
+    periodic_3D_hyperdiffusion.jl:229-231 (the hyperdiffusion passes that the
+    AtmosModel's DryBiharmonic closure also runs)
 Geometry checks of the cubed shell (Topologies.jl:1067-1305, Metrics.jl:431-724):
 shell volume from the mass matrix, the discrete metric identities (a uniform
 state has zero tendency) and the face-node maps (a linear density advected by
@@ -159,3 +163,64 @@ def test_shell_face_maps_give_the_analytic_advective_tendency():
     # (1.7e-2, 1.9e-3, 1.6e-4 at 2, 4, 8 elements per panel edge); a wrong
     # face map gives an O(1) error
     assert err < 5e-3, err
+
+
+GOLDEN_HYPER_3D = {1: 1.7363355506160003e-01, 2: 7.3049474767548042e-02}
+
+
+@pytest.mark.parametrize("level", [1, 2])
+def test_periodic_3d_hyperdiffusion_golden(level):
+    """rho = sin(x + 2y + 3z) under d rho/dt = -div(H grad lap rho) on the
+    periodic [0, 2 pi]^3 cube for t = 1, dt = dx^4 / 25 / sum(H) rounded to
+    divide 1; the weighted L2 distance to the exact decay matches the
+    reference's golden value."""
+    ne = 4 * 2 ** (level - 1)
+    H = np.array([[9, 3, 5], [3, 7, 4], [5, 4, 10]]) / 50 / 100
+    m = O.ScalarHyperdiffusion(4, (ne,) * 3, (0, 0, 0), (2 * np.pi,) * 3, H)
+    vg = m.vgeo
+    x, y, z = (vg[:, O.VGEO[c]] for c in ("x1", "x2", "x3"))
+    k = np.array([1.0, 2.0, 3.0])
+    c = (k @ k) * np.sum(np.outer(k, k) * H)
+    Q = m.state()
+    Q[:, 0] = np.sin(x + 2 * y + 3 * z)
+    # min_node_distance (Grids.jl:454-520): nearest node along the element lines
+    X = np.stack([x, y, z], 1).reshape(m.nelem, 3, m.Nq, m.Nq, m.Nq)
+    dx = min(np.sqrt((np.diff(X, axis=a) ** 2).sum(1)).min() for a in (2, 3, 4))
+    nsteps = math.ceil(1 / (dx**4 / 25 / H.sum()))
+    m.lsrk54(Q, 1 / nsteps, nsteps)
+    Qe = np.sin(x + 2 * y + 3 * z) * np.exp(-c)
+    err = math.sqrt(np.sum(vg[:, O.VGEO["M"]] * (Q[:, 0] - Qe) ** 2))
+    assert err == pytest.approx(GOLDEN_HYPER_3D[level], rel=1e-10)
+
+
+def test_dry_biharmonic_acts_on_horizontal_velocity():
+    """DryBiharmonic on a flat brick: the hyperdiffusive momentum tendency of
+    u = A sin(k x) converges (at first order, as the central-flux LDG chain
+    does) to -nu_4 k^4 rho u with nu_4 = (Delta_h / 2)^4 / 2 / tau, while the
+    vertical velocity (removed by u_h = (I - khat khat') u) is left alone."""
+    L, A, rho0, tau = 1000.0, 1.0, 1.2, 100.0
+    c = O.EARTH
+    errs = []
+    for nex in (8, 16):
+        kw = dict(N=4, ne=(nex, 1, 1), lo=(0, 0, 0), hi=(L, 500, 500), periodic=(1, 1, 1), numflux="central",
+                  orientation="flat")
+        m0 = O.OracleModel(**kw)
+        m1 = O.OracleModel(**kw, hyperdiffusion="dry_biharmonic", tau_hyper=tau)
+        aux = m1.aux
+        x = aux[:, O.AUX["x"]]
+        dh = aux[:, O.AUX["Delta_h"]]
+        assert np.allclose(dh, (L / nex / 4 + 500 / 4) / 2, rtol=1e-12)
+        k = 2 * np.pi / L
+        Q = m1.state()
+        u = A * np.sin(k * x)
+        Q[:, 0] = rho0
+        Q[:, 1] = rho0 * u
+        Q[:, 3] = rho0 * u
+        Q[:, 4] = rho0 * (c["cv_d"] * (300.0 - c["T_0"]) + u * u)
+        d = m1.tendency(Q.copy()) - m0.tendency(Q.copy())
+        nu4 = (dh / 2) ** 4 / 2 / tau
+        errs.append(np.abs(d[:, 1] / nu4 + k**4 * Q[:, 1]).max() / (k**4 * rho0 * A))
+        # round-off of the difference of two full tendencies only (w hyperdiffused would give d[:, 1])
+        assert np.abs(d[:, 3]).max() <= 1e-3 * np.abs(d[:, 1]).max()
+        assert np.abs(d[:, 0]).max() == 0.0
+    assert math.log2(errs[0] / errs[1]) > 0.8
