@@ -31,6 +31,9 @@ default, the line the benchmark contract reads, is the bubble above):
             algorithmic bytes 224 (mixed) / 264 (FP64) per node-stage
   les       SmagorinskyLilly LES, 32 x 32 x 16 elements, N=4 (2,048,000
             nodes), N_bv = 0.01 1/s, seeded k^-5/3 velocity; 200 / 320 B
+  hyper     the bubble above with DryBiharmonic hyperdiffusion (tau = 1 h):
+            per stage the gradient, laplacian and gradient-of-laplacian passes
+            and the stage kernel with hyperdiffusive fluxes; 308 / 536 B
   ensemble  64 seeded rising-bubble members of 8^3..16^3 elements and
             N = 3..5, mixed; batched (one graph of per-order launches) vs
             64 sequential single-member solves
@@ -80,6 +83,13 @@ WORKLOADS = {
                      "x/y, walls z, N_bv=0.01 1/s, seeded k^-5/3 velocity rms 1 m/s, Rusanov, LSRK54 at CFL 0.4",
                 bytes_mixed=200, bytes_fp64=320, launches_per_stage=2,
                 kernel="viscous_stage_kernel<4,float,mixed,stage,smagorinsky>", profile="none"),
+    # per node-stage: stage kernel 120 + nu grad^3 read 36; gradient pass 20 + 36; laplacian 36 + 12;
+    # gradient of the laplacian 12 + 36 (FP32 words; FP64 doubles all but the RK register's 80)
+    "hyper": dict(desc="rising bubble of the default workload with DryBiharmonic(tau = 3600 s) hyperdiffusion: "
+                       "20x20x20 elements, N=4 (1e6 nodes), Rusanov, LSRK54 at CFL 0.4",
+                  bytes_mixed=308, bytes_fp64=536, launches_per_stage=4,
+                  kernel="hyperdiffusion passes + viscous_stage_kernel<4,float,mixed,stage,none,hyper>",
+                  profile="hyper_passes_mixed_bubble20.md"),
 }
 
 
@@ -239,7 +249,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="cmdg", choices=["cmdg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="bubble", choices=["bubble", "gcm", "les", "ensemble"])
+    ap.add_argument("--workload", default="bubble", choices=["bubble", "gcm", "les", "hyper", "ensemble"])
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -297,7 +307,10 @@ def main():
         if args.workload == "les":
             dg = workloads.les_model(precision=precision)
             return dg, workloads.les_initial_state(dg.grid.coordinates())
-        dg = workloads.bubble_model(ne=NE, N=N, L=L, precision=precision)
+        if args.workload == "hyper":
+            dg = workloads.hyper_bubble_model(ne=NE, N=N, L=L, precision=precision)
+        else:
+            dg = workloads.bubble_model(ne=NE, N=N, L=L, precision=precision)
         xyz = dg.grid.coordinates()
         Q0 = workloads.rising_bubble(xyz, theta0=300.0, amp=2.0, rc=250.0, center=(1250.0, 1250.0, 350.0))
         return dg, Q0

@@ -12,7 +12,7 @@ for sm_103a behind a C ABI, include/cmdg.h).  Names follow the reference:
     lsrk  = LSRK54CarpenterKennedy(dg, Q, dt=dt, t0=0.0)
     solve_(Q, lsrk, timeend=...)                              # solve!(Q, lsrk; timeend)
 """
-from .atmos import EARTH, AtmosModel, HydrostaticState, DryAdiabaticProfile, IsothermalProfile
+from .atmos import EARTH, AtmosModel, HydrostaticState, DryAdiabaticProfile, IsothermalProfile, DryBiharmonic
 from .dgmodel import DGModel, BrickGrid, CubedShellGrid, euclidean_distance, weightedsum, norm
 from .odesolvers import LSRK54CarpenterKennedy, solve_, dostep_
 from ._lib import CmdgError, load as load_library
@@ -20,7 +20,7 @@ from .ensemble import Ensemble
 from . import filters, partition
 
 __all__ = [
-    "EARTH", "AtmosModel", "HydrostaticState", "DryAdiabaticProfile", "IsothermalProfile", "DGModel", "BrickGrid", "CubedShellGrid",
+    "EARTH", "AtmosModel", "HydrostaticState", "DryBiharmonic", "DryAdiabaticProfile", "IsothermalProfile", "DGModel", "BrickGrid", "CubedShellGrid",
     "euclidean_distance", "weightedsum", "norm", "LSRK54CarpenterKennedy", "solve_", "dostep_", "CmdgError",
     "load_library", "Ensemble",
 ]

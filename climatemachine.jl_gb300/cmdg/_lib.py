@@ -26,6 +26,7 @@ EXPORTS = (
     "cmdg_from_perturbation", "cmdg_tendency_mixed", "cmdg_lsrk54_step_mixed", "cmdg_weighted_sums",
     "cmdg_weighted_sums_mixed", "cmdg_courant_dt", "cmdg_status_word", "cmdg_lsrk54_step_noalloc",
     "cmdg_model_set_kernel", "cmdg_model_get_kernel", "cmdg_model_autotune", "cmdg_gradient_flux",
+    "cmdg_hyperdiffusive_state",
     "cmdg_batch_create", "cmdg_batch_destroy", "cmdg_batch_set_tiling", "cmdg_batch_get_tiling",
     "cmdg_batch_lsrk54_step", "cmdg_batch_autotune",
     "cmdg_filter_matrix", "cmdg_apply_filter", "cmdg_apply_tmar",
@@ -53,7 +54,8 @@ class AtmosParams(ctypes.Structure):
                 ("gravity", ctypes.c_int), ("ref_state", ctypes.c_int), ("subtract_off", ctypes.c_int),
                 ("profile", ctypes.c_int), ("T_surface", ctypes.c_double), ("T_min", ctypes.c_double),
                 ("turbulence", ctypes.c_int), ("rho_nu", ctypes.c_double), ("with_divergence", ctypes.c_int),
-                ("C_smag", ctypes.c_double), ("planet_radius", ctypes.c_double)]
+                ("C_smag", ctypes.c_double), ("planet_radius", ctypes.c_double),
+                ("hyperdiffusion", ctypes.c_int), ("tau_hyper", ctypes.c_double)]
 
 
 class ShellDesc(ctypes.Structure):
@@ -104,6 +106,7 @@ def load(path: str | None = None):
         "cmdg_model_get_kernel": [P, ctypes.POINTER(I), ctypes.POINTER(I)],
         "cmdg_model_autotune": [P, I, P, I, ctypes.POINTER(I), P],
         "cmdg_gradient_flux": [P, P, P, P],
+        "cmdg_hyperdiffusive_state": [P, P, P, P],
         "cmdg_batch_create": [P, I, PP],
         "cmdg_batch_destroy": [P],
         "cmdg_batch_set_tiling": [P, I, I, I],

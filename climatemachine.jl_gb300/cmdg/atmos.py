@@ -5,7 +5,8 @@ AtmosPhysics{FT}(param_set; ref_state, turbulence, moisture); orientation,
 source)`` (src/Atmos/Model/AtmosModel.jl:154-375) for the subset the GPU
 path implements: DryModel moisture, TotalEnergyModel, Compressible, Rusanov
 or central first-order flux, Gravity() source, HydrostaticState reference
-state, NoOrientation or FlatOrientation.
+state, NoOrientation or FlatOrientation, ConstantDynamicViscosity or
+SmagorinskyLilly turbulence and DryBiharmonic hyperdiffusion.
 
 The planet constants are CLIMAParameters.jl 0.2.0's Earth values.
 """
@@ -43,6 +44,14 @@ class HydrostaticState:
 
 
 @dataclass
+class DryBiharmonic:
+    """DryBiharmonic(tau_timescale) horizontal hyperdiffusion
+    (src/Common/TurbulenceClosures/TurbulenceClosures.jl:793-848):
+    nu_4 = (Delta_h / 2)^4 / 2 / tau acting on u_h and h_tot."""
+    tau_timescale: float = 8 * 3600.0
+
+
+@dataclass
 class AtmosModel:
     orientation: str = "none"            # "none" | "flat" | "sphere"
     ref_state: HydrostaticState | None = None
@@ -51,6 +60,7 @@ class AtmosModel:
     rho_nu: float = 0.0
     with_divergence: bool = False
     C_smag: float = EARTH["C_smag"]
+    hyperdiffusion: DryBiharmonic | None = None   # None = NoHyperDiffusion()
     constants: dict = field(default_factory=lambda: dict(EARTH))
 
     def c_params(self, numerical_flux: str) -> AtmosParams:
@@ -73,4 +83,7 @@ class AtmosModel:
         p.rho_nu = self.rho_nu
         p.with_divergence = int(self.with_divergence)
         p.C_smag = self.C_smag
+        hd = self.hyperdiffusion
+        p.hyperdiffusion = 0 if hd is None else 1
+        p.tau_hyper = 0.0 if hd is None else float(hd.tau_timescale)
         return p

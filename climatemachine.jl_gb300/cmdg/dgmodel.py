@@ -230,6 +230,13 @@ class DGModel:
         call("cmdg_gradient_flux", self.h, _dptr(gf), _dptr(Q), _stream())
         return gf
 
+    def hyperdiffusive_state(self, Q) -> torch.Tensor:
+        """Hyperdiffusive state (nelem, 9, Np) of Q: word 3 c + d holds
+        nu_4 d/dx_d lap(c) for c = u, v, h_tot."""
+        hd = torch.zeros((self.grid.nelem, 9, self.grid.Np), dtype=self.state_dtype, device=self.device)
+        call("cmdg_hyperdiffusive_state", self.h, _dptr(hd), _dptr(Q), _stream())
+        return hd
+
     def status_word(self) -> int:
         st = ctypes.c_uint32()
         call("cmdg_status_word", self.h, ctypes.byref(st), _stream())

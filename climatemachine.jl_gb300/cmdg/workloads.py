@@ -22,7 +22,7 @@ import math
 
 import numpy as np
 
-from .atmos import EARTH, AtmosModel, DryAdiabaticProfile, HydrostaticState, IsothermalProfile
+from .atmos import EARTH, AtmosModel, DryAdiabaticProfile, DryBiharmonic, HydrostaticState, IsothermalProfile
 from .dgmodel import BrickGrid, CubedShellGrid, DGModel
 
 
@@ -80,6 +80,18 @@ def bubble_model(ne=(20, 20, 20), N=4, L=2500.0, precision="fp64", numerical_flu
     model = AtmosModel(orientation="flat", gravity=True,
                        ref_state=HydrostaticState(DryAdiabaticProfile(300.0, 0.0), subtract_off=True))
     return DGModel(model, grid, numerical_flux=numerical_flux, precision=precision)
+
+
+def hyper_bubble_model(ne=(20, 20, 20), N=4, L=2500.0, precision="fp64", tau=3600.0):
+    """The rising-bubble configuration of bubble_model with DryBiharmonic(tau)
+    horizontal hyperdiffusion (src/Common/TurbulenceClosures/
+    TurbulenceClosures.jl:793-848)."""
+    grid = BrickGrid(N, ne, (0.0, 0.0, 0.0), (L, L, L), periodicity=(True, True, False),
+                     boundary=((0, 0), (0, 0), (1, 2)))
+    model = AtmosModel(orientation="flat", gravity=True,
+                       ref_state=HydrostaticState(DryAdiabaticProfile(300.0, 0.0), subtract_off=True),
+                       hyperdiffusion=DryBiharmonic(tau))
+    return DGModel(model, grid, numerical_flux="rusanov", precision=precision)
 
 
 def bubble_ensemble_specs(n=64, seed=2024, L=2500.0):

@@ -184,7 +184,8 @@ extern "C" int cmdg_batch_create(cmdg_model* const* models, int n, cmdg_batch** 
         CMDG_ARG_CHECK(md.precision == CMDG_MIXED, "member %d: ensembles run the mixed-precision path", m);
         CMDG_ARG_CHECK(md.mesh->N >= BATCH_NMIN && md.mesh->N <= BATCH_NMAX,
                        "member %d: N=%d outside the ensemble range [3, 5]", m, md.mesh->N);
-        CMDG_ARG_CHECK(md.prm.turbulence == CMDG_TURB_NONE, "member %d: ensembles are inviscid", m);
+        CMDG_ARG_CHECK(md.prm.turbulence == CMDG_TURB_NONE && md.prm.hyperdiffusion == CMDG_HYPER_NONE,
+                       "member %d: ensembles are inviscid", m);
         CMDG_ARG_CHECK(md.mesh->kind == MESH_BRICK, "member %d: ensembles run on brick meshes", m);
     }
     Batch* b = new Batch();

@@ -176,6 +176,10 @@ struct Model {
     std::vector<float> filter_corr;  // mixed precision: vertical-filter change of the reference state per level
     float* d_filter_corr = nullptr;
     double* d_omega = nullptr;       // LGL weights on the device (TMAR filter)
+    void* d_hd = nullptr;            // hyperdiffusion: gradient, then nu grad^3, (Np, 9, nelem)
+    void* d_hlap = nullptr;          // hyperdiffusion: laplacians (Np, 3, nelem)
+    std::vector<double> glap_ref64;  // [nlev] DG d/dz of the laplacian of the reference h_tot
+    float* d_glap_ref = nullptr;
     int grid_ctas = -1;              // stage-kernel grid: -1 = one CTA per element (the measured best
                                      // on GB300), 0 = one wave of resident CTAs, n > 0 = n CTAs
     int kernel_kind = 0;             // KERNEL_NODE or KERNEL_COLUMN
@@ -213,6 +217,12 @@ void lsrk54_coefficients(const double** A, const double** B);
 // stage kernel with second-order fluxes
 int launch_gradient(Model* md, const void* Qin, void* gf_out, cudaStream_t s);
 int launch_viscous_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
+
+// hyperdiffusion (hyper.cu): reference rows and buffers, the three passes of
+// Qin into hd_out (nu grad^3, (Np, 9, nelem)), and the stage with them
+int init_hyper_tables(Model* md);
+int launch_hyper_passes(Model* md, const void* Qin, void* hd_out, cudaStream_t s);
+int launch_hyper_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
 
 // reductions / conversions (reduce.cu)
 int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s);

@@ -42,6 +42,14 @@ struct KParams {
     // curvilinear meshes: per-node kernel geometry (Np, KG_NFIELDS, nelem) in
     // the working precision
     const void* geo;
+    // hyperdiffusion: gradient / hyperdiffusive state (Np, 9, nelem),
+    // laplacians (Np, 3, nelem), the FP64-computed z-gradient of the laplacian
+    // of the reference h_tot per level (mixed precision) and tau
+    void* hd;
+    void* hlap;
+    const float* glap_ref32;
+    double inv_tau_hyper;
+    float inv_tau_hyper32;
 };
 
 // A run of consecutive elements [e0, e1) of ensemble member `member`, of
@@ -76,6 +84,7 @@ struct KConst<double> {
     static __device__ __forceinline__ double inv_w0(const KParams& P) { return P.inv_w0; }
     static __device__ __forceinline__ double rkb_dt(const KParams& P) { return P.rkb_dt; }
     static __device__ __forceinline__ double metric(const KParams& P, int e, int d) { return P.emetric[3 * e + d]; }
+    static __device__ __forceinline__ double inv_tau(const KParams& P) { return P.inv_tau_hyper; }
 };
 template <>
 struct KConst<float> {
@@ -84,6 +93,7 @@ struct KConst<float> {
     static __device__ __forceinline__ float inv_w0(const KParams& P) { return P.inv_w032; }
     static __device__ __forceinline__ float rkb_dt(const KParams& P) { return P.rkb_dt32; }
     static __device__ __forceinline__ float metric(const KParams& P, int e, int d) { return P.emetric32[3 * e + d]; }
+    static __device__ __forceinline__ float inv_tau(const KParams& P) { return P.inv_tau_hyper32; }
 };
 
 // FP32 -> FP64 by IEEE-754 field arithmetic on the integer pipe (on this GPU

@@ -319,9 +319,11 @@ int init_viscous_tables(Model* md) {
     CMDG_CUDA_CHECK(cudaMalloc(&md->d_lvv32, sizeof(float) * v32.size()));
     CMDG_CUDA_CHECK(cudaMemcpy(md->d_lvv64, md->lvv64.data(), sizeof(double) * md->lvv64.size(), cudaMemcpyHostToDevice));
     CMDG_CUDA_CHECK(cudaMemcpy(md->d_lvv32, v32.data(), sizeof(float) * v32.size(), cudaMemcpyHostToDevice));
-    const size_t elt = md->precision == CMDG_MIXED ? sizeof(float) : sizeof(double);
-    CMDG_CUDA_CHECK(cudaMalloc(&md->d_gf, (size_t)m.nelem * NGF * m.Np * elt));
-    CMDG_CUDA_CHECK(cudaMemset(md->d_gf, 0, (size_t)m.nelem * NGF * m.Np * elt));
+    if (p.turbulence != CMDG_TURB_NONE) {
+        const size_t elt = md->precision == CMDG_MIXED ? sizeof(float) : sizeof(double);
+        CMDG_CUDA_CHECK(cudaMalloc(&md->d_gf, (size_t)m.nelem * NGF * m.Np * elt));
+        CMDG_CUDA_CHECK(cudaMemset(md->d_gf, 0, (size_t)m.nelem * NGF * m.Np * elt));
+    }
     return CMDG_OK;
 }
 

@@ -533,12 +533,18 @@ KParams make_params(Model* md, const LaunchArgs& a) {
     P.MSLP32 = (float)md->ph.MSLP;
     P.grav32 = (float)md->ph.grav;
     P.geo = mixed ? (const void*)md->d_geo32 : (const void*)md->d_geo64;
+    P.hd = md->d_hd;
+    P.hlap = md->d_hlap;
+    P.glap_ref32 = md->d_glap_ref;
+    P.inv_tau_hyper = md->prm.tau_hyper > 0 ? 1.0 / md->prm.tau_hyper : 0.0;
+    P.inv_tau_hyper32 = (float)P.inv_tau_hyper;
     return P;
 }
 
 int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
     const Mesh& m = *md->mesh;
     if (m.kind == MESH_SHELL) return launch_shell_stage(md, a, s);
+    if (md->prm.hyperdiffusion != CMDG_HYPER_NONE) return launch_hyper_stage(md, a, s);
     if (md->prm.turbulence != CMDG_TURB_NONE) return launch_viscous_stage(md, a, s);
     const KParams P = make_params(md, a);
     const bool mixed = md->precision == CMDG_MIXED;

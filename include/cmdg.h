@@ -57,6 +57,9 @@ enum { CMDG_ORIENT_NONE = 0, CMDG_ORIENT_FLAT = 1, CMDG_ORIENT_SPHERE = 2 };
 enum { CMDG_PROFILE_ISOTHERMAL = 0, CMDG_PROFILE_DRY_ADIABATIC = 1 };
 /* Turbulence closure */
 enum { CMDG_TURB_NONE = 0, CMDG_TURB_CONSTANT = 1, CMDG_TURB_SMAGORINSKY = 2 };
+/* Hyperdiffusion (NoHyperDiffusion / DryBiharmonic,
+ * src/Common/TurbulenceClosures/TurbulenceClosures.jl:793-848) */
+enum { CMDG_HYPER_NONE = 0, CMDG_HYPER_DRY_BIHARMONIC = 1 };
 
 /* Brick mesh (BrickTopology / StackedBrickTopology + DiscontinuousSpectralElementGrid,
  * src/Numerics/Mesh/Topologies.jl:470-545,632; src/Numerics/Mesh/Grids.jl:267-414). */
@@ -87,6 +90,8 @@ typedef struct {
     int with_divergence;/* ConstantDynamicViscosity WithDivergence */
     double C_smag;      /* SmagorinskyLilly coefficient */
     double planet_radius; /* SphericalOrientation: Phi = grav (|x| - planet_radius) */
+    int hyperdiffusion; /* CMDG_HYPER_* (brick meshes with FlatOrientation) */
+    double tau_hyper;   /* DryBiharmonic tau_timescale (s) */
 } cmdg_atmos_params;
 
 /* Stacked equiangular cubed shell: 6 nhorz^2 columns of nvert elements
@@ -279,6 +284,20 @@ int cmdg_courant_dt(cmdg_model* model, const double* d_Q, double CFL, double* h_
  * dg.state_gradient_flux (src/Numerics/DGMethods/SpaceDiscretization.jl:502-728,
  * src/Numerics/DGMethods/DGModel.jl:132-230). */
 int cmdg_gradient_flux(cmdg_model* model, void* d_gf, const void* d_Q, void* stream);
+
+/* Hyperdiffusive state of d_Q (the passes that precede every tendency of a
+ * model with DryBiharmonic hyperdiffusion) into d_hd, column-major
+ * (Np, 9, nelem) in the model's precision: word 3 c + d holds
+ * nu_4 d/dx_d (laplacian of c) for c = u, v, h_tot (the horizontal velocity
+ * u_h of a flat brick has no vertical component), nu_4 = (Delta_h/2)^4/2/tau.
+ * Replaces the hyperdiffusive part of launch_volume_gradients! +
+ * launch_interface_gradients!, launch_volume_divergence_of_gradients! +
+ * launch_interface_divergence_of_gradients! and
+ * launch_volume_gradients_of_laplacians! +
+ * launch_interface_gradients_of_laplacians! filling Qhypervisc_grad
+ * (src/Numerics/DGMethods/SpaceDiscretization.jl:502-1090,
+ * src/Numerics/DGMethods/DGModel.jl:132-301). */
+int cmdg_hyperdiffusive_state(cmdg_model* model, void* d_hd, const void* d_Q, void* stream);
 
 /* Device status word accumulated by the kernels since the last call
  * (bit 0: non-finite tendency seen); reading clears it.
