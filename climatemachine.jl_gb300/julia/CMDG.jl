@@ -53,6 +53,9 @@ struct AtmosParams
     rho_nu::Cdouble
     with_divergence::Cint
     C_smag::Cdouble
+    planet_radius::Cdouble   # SphericalOrientation
+    hyperdiffusion::Cint     # 0 = NoHyperDiffusion, 1 = DryBiharmonic
+    tau_hyper::Cdouble       # DryBiharmonic tau_timescale
 end
 
 check(rc::Cint) =
