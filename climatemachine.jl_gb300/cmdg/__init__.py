@@ -17,7 +17,7 @@ from .dgmodel import DGModel, BrickGrid, CubedShellGrid, euclidean_distance, wei
 from .odesolvers import LSRK54CarpenterKennedy, solve_, dostep_
 from ._lib import CmdgError, load as load_library
 from .ensemble import Ensemble
-from . import filters, partition
+from . import checkpoint, filters, partition
 
 __all__ = [
     "EARTH", "AtmosModel", "HydrostaticState", "DryBiharmonic", "DryAdiabaticProfile", "IsothermalProfile", "DGModel", "BrickGrid", "CubedShellGrid",
