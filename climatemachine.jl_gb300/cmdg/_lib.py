@@ -17,6 +17,7 @@ CMDG_OK = 0
 ERRORS = {1: "CMDG_ERR_ARG", 2: "CMDG_ERR_CUDA", 3: "CMDG_ERR_UNSUPPORTED", 4: "CMDG_ERR_NONFINITE",
           5: "CMDG_ERR_TIMEOUT", 6: "CMDG_ERR_ALLOC", 7: "CMDG_ERR_STATE"}
 CMDG_FP64, CMDG_MIXED = 0, 1
+CMDG_DIR_EVERY, CMDG_DIR_HORIZONTAL, CMDG_DIR_VERTICAL = 0, 1, 2
 
 # Every exported symbol of include/cmdg.h (checked by the CPU test suite).
 EXPORTS = (
@@ -55,7 +56,7 @@ class AtmosParams(ctypes.Structure):
                 ("profile", ctypes.c_int), ("T_surface", ctypes.c_double), ("T_min", ctypes.c_double),
                 ("turbulence", ctypes.c_int), ("rho_nu", ctypes.c_double), ("with_divergence", ctypes.c_int),
                 ("C_smag", ctypes.c_double), ("planet_radius", ctypes.c_double),
-                ("hyperdiffusion", ctypes.c_int), ("tau_hyper", ctypes.c_double)]
+                ("hyperdiffusion", ctypes.c_int), ("tau_hyper", ctypes.c_double), ("hyper_direction", ctypes.c_int)]
 
 
 class ShellDesc(ctypes.Structure):

@@ -22,6 +22,10 @@ file instead of HDF5/JLD2 (no HDF5 library is available to this package):
 
 ``h_Q`` is always the full FP64 state (a mixed-precision model's FP32
 perturbation is converted back), so a checkpoint restarts either precision.
+A mixed-precision model also stores its FP32 perturbation state as ``h_Qp``
+(``dtype`` ``<f4``): ``restart_ode_state`` restarts such a model from it bit
+for bit (the FP64 sum q_ref + q' rounds perturbations more than 2^29 below
+the reference value, so the FP64 record alone does not round-trip them).
 ``h_aux`` holds this library's auxiliary state, the reference state
 ``(rho_ref, rhoe_ref, p_ref)`` at the nodes (the rest of the reference's aux
 -- coordinates, geopotential, metric-derived fields -- is rebuilt from the
@@ -48,21 +52,27 @@ def checkpoint_path(checkpoint_dir: str, name: str, rank: int, num: int) -> str:
     return os.path.join(checkpoint_dir, "%s_checkpoint_mpirank%04d_num%04d.cmdg" % (nm, rank, num))
 
 
-def _as_host_f64(a) -> np.ndarray:
+DTYPES = {"<f8": np.float64, "<f4": np.float32}
+
+
+def _as_host(a, dtype=np.float64) -> np.ndarray:
     if hasattr(a, "detach"):  # torch tensor on any device
-        a = a.detach().to("cpu").double().numpy()
-    a = np.ascontiguousarray(a, dtype=np.float64)
+        a = a.detach().to("cpu").numpy()
+    a = np.ascontiguousarray(a, dtype=dtype)
     if a.ndim != 3:
         raise ValueError(f"expected a (nelem, nstate, Np) array, got shape {a.shape}")
     return a
 
 
 def write_checkpoint_arrays(h_Q, h_aux, t: float, checkpoint_dir: str, name: str, rank: int = 0, num: int = 0,
-                            aux_fields=None) -> str:
+                            aux_fields=None, h_Qp=None) -> str:
     """write_checkpoint(Q, A, odesolver, checkpoint_dir, name, mpicomm, num)
-    with the arrays and the time given directly; returns the file path.
-    The file is written under a temporary name and renamed into place."""
-    arrays = {"h_Q": _as_host_f64(h_Q), "h_aux": _as_host_f64(h_aux)}
+    with the arrays and the time given directly (and optionally the FP32
+    perturbation state of a mixed model); returns the file path.  The file
+    is written under a temporary name and renamed into place."""
+    arrays = {"h_Q": _as_host(h_Q), "h_aux": _as_host(h_aux)}
+    if h_Qp is not None:
+        arrays["h_Qp"] = _as_host(h_Qp, np.float32)
     meta = {"format": "cmdg-checkpoint", "version": 1, "t": float(t), "name": name, "rank": int(rank),
             "num": int(num), "aux_fields": list(aux_fields or AUX_FIELDS), "arrays": {}}
     # two passes: the header length fixes the array offsets
@@ -70,8 +80,8 @@ def write_checkpoint_arrays(h_Q, h_aux, t: float, checkpoint_dir: str, name: str
     for _ in range(3):
         off = (16 + len(header) + ALIGN - 1) // ALIGN * ALIGN
         for k, a in arrays.items():
-            meta["arrays"][k] = {"dtype": "<f8", "shape": [a.shape[2], a.shape[1], a.shape[0]], "offset": off,
-                                 "nbytes": a.nbytes}
+            meta["arrays"][k] = {"dtype": "<f8" if a.dtype == np.float64 else "<f4",
+                                 "shape": [a.shape[2], a.shape[1], a.shape[0]], "offset": off, "nbytes": a.nbytes}
             off = (off + a.nbytes + ALIGN - 1) // ALIGN * ALIGN
         new = json.dumps(meta, sort_keys=True).encode()
         if len(new) == len(header):
@@ -86,7 +96,7 @@ def write_checkpoint_arrays(h_Q, h_aux, t: float, checkpoint_dir: str, name: str
         fh.write(header)
         for k, a in arrays.items():
             fh.seek(meta["arrays"][k]["offset"])
-            fh.write(a.astype("<f8", copy=False).tobytes(order="C"))
+            fh.write(a.astype(a.dtype.newbyteorder("<"), copy=False).tobytes(order="C"))
     os.replace(tmp, path)
     return path
 
@@ -96,6 +106,12 @@ def read_checkpoint(checkpoint_dir: str, name: str, rank: int = 0, num: int = 0)
     ``(h_Q, h_aux, t)``, host arrays shaped (nelem, nstate, Np) (the memory
     of the reference's (Np, nstate, nelem) arrays).  Raises like the
     reference when the file is missing (Checkpoint.jl:115-121)."""
+    rec, t = read_checkpoint_records(checkpoint_dir, name, rank, num)
+    return rec["h_Q"], rec["h_aux"], t
+
+
+def read_checkpoint_records(checkpoint_dir: str, name: str, rank: int = 0, num: int = 0):
+    """Every record of a checkpoint file as a dict of host arrays, and t."""
     path = checkpoint_path(checkpoint_dir, name, rank, num)
     if not os.path.isfile(path):
         raise FileNotFoundError(f"Cannot restore from checkpoint in {path}, file not found")
@@ -106,16 +122,18 @@ def read_checkpoint(checkpoint_dir: str, name: str, rank: int = 0, num: int = 0)
         meta = json.loads(fh.read(hlen).decode())
         out = {}
         size = os.fstat(fh.fileno()).st_size
-        for k in ("h_Q", "h_aux"):
-            d = meta["arrays"][k]
-            if d["dtype"] != "<f8" or d["offset"] + d["nbytes"] > size:
+        if "h_Q" not in meta["arrays"] or "h_aux" not in meta["arrays"]:
+            raise ValueError(f"{path}: h_Q or h_aux missing")
+        for k, d in meta["arrays"].items():
+            if d["dtype"] not in DTYPES or d["offset"] + d["nbytes"] > size:
                 raise ValueError(f"{path}: record {k} is truncated or of an unknown type")
+            dt = DTYPES[d["dtype"]]
             Np, ns, ne = d["shape"]
-            if Np * ns * ne * 8 != d["nbytes"]:
+            if Np * ns * ne * np.dtype(dt).itemsize != d["nbytes"]:
                 raise ValueError(f"{path}: record {k} has an inconsistent shape")
             fh.seek(d["offset"])
-            out[k] = np.frombuffer(fh.read(d["nbytes"]), dtype="<f8").reshape(ne, ns, Np).astype(np.float64)
-    return out["h_Q"], out["h_aux"], float(meta["t"])
+            out[k] = np.frombuffer(fh.read(d["nbytes"]), dtype=d["dtype"]).reshape(ne, ns, Np).astype(dt)
+    return out, float(meta["t"])
 
 
 def rm_checkpoint(checkpoint_dir: str, name: str, rank: int = 0, num: int = 0) -> None:
@@ -131,4 +149,18 @@ def write_checkpoint(dg, Q, odesolver, checkpoint_dir: str, name: str, rank: int
     perturbation of a mixed model) and its solver's time."""
     h_Q = dg.full_state(Q)
     t = odesolver.gettime() if hasattr(odesolver, "gettime") else float(odesolver)
-    return write_checkpoint_arrays(h_Q, dg.reference_state(), t, checkpoint_dir, name, rank, num)
+    return write_checkpoint_arrays(h_Q, dg.reference_state(), t, checkpoint_dir, name, rank, num,
+                                   h_Qp=Q if dg.mixed else None)
+
+
+def restart_ode_state(dg, checkpoint_dir: str, name: str, rank: int = 0, num: int = 0):
+    """restart_ode_state (src/Numerics/DGMethods/DGModel.jl:429-443) from a
+    checkpoint file: the device state in the model's own representation and
+    the checkpoint time.  A mixed model takes the stored FP32 perturbation
+    when the file has one (bitwise restart), else converts h_Q."""
+    import torch
+
+    rec, t = read_checkpoint_records(checkpoint_dir, name, rank, num)
+    if dg.mixed and "h_Qp" in rec:
+        return torch.from_numpy(rec["h_Qp"]).to(dg.device), t
+    return dg.init_ode_state(rec["h_Q"]), t

@@ -115,15 +115,19 @@ class DGModel:
     precision="fp64": plain Float64 state.
     precision="mixed": FP32 state perturbation about the FP64 hydrostatic
     reference state with an FP64 RK register (see ``to_perturbation``).
+    diffusion_direction ("every" or "horizontal", the reference's
+    ``diffusion_direction`` keyword): directions of the hyperdiffusion passes.
     """
 
-    def __init__(self, balance_law, grid: BrickGrid, numerical_flux: str = "rusanov", precision: str = "fp64"):
+    def __init__(self, balance_law, grid: BrickGrid, numerical_flux: str = "rusanov", precision: str = "fp64",
+                 diffusion_direction: str = "every"):
         self.balance_law = balance_law
         self.grid = grid
         self.numerical_flux = numerical_flux
         self.precision = precision
         self.mixed = precision == "mixed"
         p: AtmosParams = balance_law.c_params(numerical_flux)
+        p.hyper_direction = {"every": _lib.CMDG_DIR_EVERY, "horizontal": _lib.CMDG_DIR_HORIZONTAL}[diffusion_direction]
         self._params = p
         h = ctypes.c_void_p()
         call("cmdg_model_create", grid.h, ctypes.byref(p), _lib.CMDG_MIXED if self.mixed else _lib.CMDG_FP64,
@@ -231,9 +235,11 @@ class DGModel:
         return gf
 
     def hyperdiffusive_state(self, Q) -> torch.Tensor:
-        """Hyperdiffusive state (nelem, 9, Np) of Q: word 3 c + d holds
-        nu_4 d/dx_d lap(c) for c = u, v, h_tot."""
-        hd = torch.zeros((self.grid.nelem, 9, self.grid.Np), dtype=self.state_dtype, device=self.device)
+        """Hyperdiffusive state of Q, word 3 c + d = nu_4 d/dx_d lap(c):
+        (nelem, 9, Np) on a brick (c = u, v, h_tot; u_h has no vertical
+        component), (nelem, 12, Np) on the cubed shell (c = u_h[0..2], h_tot)."""
+        nw = 12 if isinstance(self.grid, CubedShellGrid) else 9
+        hd = torch.zeros((self.grid.nelem, nw, self.grid.Np), dtype=self.state_dtype, device=self.device)
         call("cmdg_hyperdiffusive_state", self.h, _dptr(hd), _dptr(Q), _stream())
         return hd
 

@@ -117,17 +117,21 @@ def bubble_member(spec, L=2500.0, precision="mixed"):
 
 
 def gcm_shell_model(nhorz=12, nvert=6, N=4, H=30e3, precision="fp64", numerical_flux="rusanov", T_ref=285.0,
-                    subtract_off=True):
+                    subtract_off=True, tau_hyper=None, diffusion_direction="horizontal"):
     """Dry shallow-atmosphere GCM on the stacked equiangular cubed shell:
     6 x nhorz^2 columns of nvert elements between the planet radius and a lid
     H above it, walls at both (AtmosGCMConfiguration's boundary = (1, 2)),
     SphericalOrientation + Gravity, HydrostaticState(IsothermalProfile(T_ref)),
-    inviscid."""
+    inviscid, with DryBiharmonic(tau_hyper) hyperdiffusion in the horizontal
+    directions when tau_hyper is given (as experiments/AtmosGCM/heldsuarez.jl
+    configures it: diffdir = HorizontalDirection())."""
     R = EARTH["planet_radius"]
     grid = CubedShellGrid(N, nhorz, nvert, R, R + H)
     model = AtmosModel(orientation="sphere", gravity=True,
-                       ref_state=HydrostaticState(IsothermalProfile(T_ref), subtract_off=subtract_off))
-    return DGModel(model, grid, numerical_flux=numerical_flux, precision=precision)
+                       ref_state=HydrostaticState(IsothermalProfile(T_ref), subtract_off=subtract_off),
+                       hyperdiffusion=None if tau_hyper is None else DryBiharmonic(tau_hyper))
+    return DGModel(model, grid, numerical_flux=numerical_flux, precision=precision,
+                   diffusion_direction=diffusion_direction)
 
 
 def gcm_initial_state(xyz: np.ndarray, *, seed=2024, T_ref=285.0, u_max=30.0, dT=1.0, radius=1.0e6, z_c=10e3,

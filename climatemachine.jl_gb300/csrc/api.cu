@@ -253,10 +253,12 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
     CMDG_ARG_CHECK(p->hyperdiffusion == CMDG_HYPER_NONE || p->hyperdiffusion == CMDG_HYPER_DRY_BIHARMONIC,
                    "unknown hyperdiffusion %d", p->hyperdiffusion);
     if (p->hyperdiffusion != CMDG_HYPER_NONE) {
-        CMDG_ARG_CHECK(!shell, "the cubed-shell kernels have no hyperdiffusion");
-        CMDG_ARG_CHECK(p->orientation == CMDG_ORIENT_FLAT,
-                       "DryBiharmonic needs FlatOrientation (u_h = (I - khat khat') u)");
+        CMDG_ARG_CHECK(p->orientation == (shell ? CMDG_ORIENT_SPHERE : CMDG_ORIENT_FLAT),
+                       "DryBiharmonic needs %s (u_h = (I - khat khat') u)",
+                       shell ? "SphericalOrientation on a cubed shell" : "FlatOrientation on a brick");
         CMDG_ARG_CHECK(p->tau_hyper > 0, "DryBiharmonic tau_timescale must be positive");
+        CMDG_ARG_CHECK(p->hyper_direction == CMDG_DIR_EVERY || p->hyper_direction == CMDG_DIR_HORIZONTAL,
+                       "hyperdiffusion direction %d: EveryDirection or HorizontalDirection", p->hyper_direction);
     }
     cmdg_model* mo = new cmdg_model();
     Model& md = mo->m;
@@ -283,9 +285,10 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
     md.ph.with_divergence = p->with_divergence;
     int rc = init_model_tables(&md);
     if (rc == CMDG_OK && shell) rc = init_shell_tables(&md);
-    if (rc == CMDG_OK && (p->turbulence != CMDG_TURB_NONE || p->hyperdiffusion != CMDG_HYPER_NONE))
+    if (rc == CMDG_OK && !shell && (p->turbulence != CMDG_TURB_NONE || p->hyperdiffusion != CMDG_HYPER_NONE))
         rc = init_viscous_tables(&md);
-    if (rc == CMDG_OK && p->hyperdiffusion != CMDG_HYPER_NONE) rc = init_hyper_tables(&md);
+    if (rc == CMDG_OK && p->hyperdiffusion != CMDG_HYPER_NONE)
+        rc = shell ? init_shell_hyper_tables(&md) : init_hyper_tables(&md);
     if (rc == CMDG_OK) {
         cudaError_t e = cudaMalloc(&md.d_status, sizeof(unsigned));
         if (e == cudaSuccess) e = cudaMemset(md.d_status, 0, sizeof(unsigned));
@@ -320,6 +323,8 @@ int cmdg_model_destroy(cmdg_model* model) {
     cudaFree(md.d_hd);
     cudaFree(md.d_hlap);
     cudaFree(md.d_glap_ref);
+    cudaFree(md.d_nu4);
+    cudaFree(md.d_hglap_ref);
     cudaFree(md.d_geo64);
     cudaFree(md.d_geo32);
     cudaFree(md.d_mass);

@@ -180,6 +180,8 @@ struct Model {
     void* d_hlap = nullptr;          // hyperdiffusion: laplacians (Np, 3, nelem)
     std::vector<double> glap_ref64;  // [nlev] DG d/dz of the laplacian of the reference h_tot
     float* d_glap_ref = nullptr;
+    void* d_nu4 = nullptr;           // cubed shell: nu_4 per node, (Np, nelem), model precision
+    float* d_hglap_ref = nullptr;    // cubed shell, mixed: nu_4 grad lap h_ref per node, (Np, 3, nelem)
     int grid_ctas = -1;              // stage-kernel grid: -1 = one CTA per element (the measured best
                                      // on GB300), 0 = one wave of resident CTAs, n > 0 = n CTAs
     int kernel_kind = 0;             // KERNEL_NODE or KERNEL_COLUMN
@@ -223,6 +225,10 @@ int launch_viscous_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
 int init_hyper_tables(Model* md);
 int launch_hyper_passes(Model* md, const void* Qin, void* hd_out, cudaStream_t s);
 int launch_hyper_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
+// the same passes on the cubed shell (hyper_shell.cu): tables, then Qin into
+// hd_out (nu grad^3 of u_h[0..2], h_tot, (Np, 12, nelem))
+int init_shell_hyper_tables(Model* md);
+int launch_shell_hyper_passes(Model* md, const void* Qin, void* hd_out, cudaStream_t s);
 
 // reductions / conversions (reduce.cu)
 int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s);

@@ -50,6 +50,11 @@ struct KParams {
     const float* glap_ref32;
     double inv_tau_hyper;
     float inv_tau_hyper32;
+    // cubed shell: nu_4 per node (working precision) and, mixed, the FP64
+    // reference part nu_4 grad lap h_ref per node (Np, 3, nelem)
+    const void* nu4;
+    const float* hglap_ref32;
+    int hyper_horizontal;  // 1: the passes run in the horizontal directions only (HorizontalDirection)
 };
 
 // A run of consecutive elements [e0, e1) of ensemble member `member`, of

@@ -109,6 +109,8 @@ __global__ void __launch_bounds__(VDims<N>::NT) hyper_grad_kernel(const KParams 
         levp = ezp * Nq + x.vP / Nfp;
     }
     const R xi[3] = {KConst<R>::metric(P, e, 0), KConst<R>::metric(P, e, 1), KConst<R>::metric(P, e, 2)};
+    // HorizontalDirection: no xi3 derivatives and no xi3-face terms
+    const R xz = P.hyper_horizontal ? R(0) : xi[2];
 
     if (x.node) {
         R H[3];
@@ -136,7 +138,7 @@ __global__ void __launch_bounds__(VDims<N>::NT) hyper_grad_kernel(const KParams 
             c = R(1);
         }
         const R sgn = x.fside ? R(1) : R(-1);
-        const R w = c * sgn * pick3(x.fd, xi[0], xi[1], xi[2]) * KConst<R>::inv_w0(P);
+        const R w = c * sgn * pick3(x.fd, xi[0], xi[1], xz) * KConst<R>::inv_w0(P);
 #pragma unroll
         for (int s = 0; s < 3; ++s) s_dH[s * NFN + t] = w * (Hp[s] - s_H[s * Np + x.vM]);
     }
@@ -159,7 +161,7 @@ __global__ void __launch_bounds__(VDims<N>::NT) hyper_grad_kernel(const KParams 
         for (int s = 0; s < 3; ++s) {
             g1[s] *= xi[0];
             g2[s] *= xi[1];
-            g3[s] *= xi[2];
+            g3[s] *= xz;
         }
         auto add = [&](int ff, R* gd) {
             const int idx = ff * Nfp + x.on_face(ff);
@@ -210,11 +212,13 @@ __global__ void __launch_bounds__(VDims<N>::NT) hyper_div_kernel(const KParams P
         for (int s = 0; s < 3; ++s) Gp[s] = gn[(size_t)s * 3 * Np];
     }
     const R xi[3] = {KConst<R>::metric(P, e, 0), KConst<R>::metric(P, e, 1), KConst<R>::metric(P, e, 2)};
+    // HorizontalDirection: no xi3 derivatives and no xi3-face terms
+    const R xz = P.hyper_horizontal ? R(0) : xi[2];
     __syncthreads();
 
     if (x.face) {
         const R sgn = x.fside ? R(1) : R(-1);
-        const R w = sgn * pick3(x.fd, xi[0], xi[1], xi[2]) * KConst<R>::inv_w0(P);
+        const R w = sgn * pick3(x.fd, xi[0], xi[1], xz) * KConst<R>::inv_w0(P);
 #pragma unroll
         for (int s = 0; s < 3; ++s) {
             const R Gm = s_G[(3 * s + x.fd) * Np + x.vM];
@@ -238,7 +242,7 @@ __global__ void __launch_bounds__(VDims<N>::NT) hyper_div_kernel(const KParams P
         }
         R lap[3];
 #pragma unroll
-        for (int s = 0; s < 3; ++s) lap[s] = -(xi[0] * a1[s] + xi[1] * a2[s] + xi[2] * a3[s]);
+        for (int s = 0; s < 3; ++s) lap[s] = -(xi[0] * a1[s] + xi[1] * a2[s] + xz * a3[s]);
         auto add = [&](int ff) {
             const int idx = ff * Nfp + x.on_face(ff);
 #pragma unroll
@@ -284,6 +288,8 @@ __global__ void __launch_bounds__(VDims<N>::NT) hyper_glap_kernel(const KParams 
         for (int s = 0; s < 3; ++s) Lp[s] = ln[(size_t)s * Np];
     }
     const R xi[3] = {KConst<R>::metric(P, e, 0), KConst<R>::metric(P, e, 1), KConst<R>::metric(P, e, 2)};
+    // HorizontalDirection: no xi3 derivatives and no xi3-face terms
+    const R xz = P.hyper_horizontal ? R(0) : xi[2];
     // nu_4 = (Delta_h / 2)^4 / 2 / tau, Delta_h = (2/(N xi1x1) + 2/(N xi2x2)) / 2 on an affine brick,
     // in the working precision (FP64 divisions would dominate an FP32 pass)
     const R h2 = (R(2) / (R(N) * xi[0]) + R(2) / (R(N) * xi[1])) / R(4);
@@ -292,7 +298,7 @@ __global__ void __launch_bounds__(VDims<N>::NT) hyper_glap_kernel(const KParams 
 
     if (x.face) {
         const R sgn = x.fside ? R(1) : R(-1);
-        const R w = sgn * pick3(x.fd, xi[0], xi[1], xi[2]) * KConst<R>::inv_w0(P);
+        const R w = sgn * pick3(x.fd, xi[0], xi[1], xz) * KConst<R>::inv_w0(P);
 #pragma unroll
         for (int s = 0; s < 3; ++s)
             s_dL[s * NFN + t] = nb >= 0 ? w * (Lp[s] - s_L[s * Np + x.vM]) / R(2) : R(0);
@@ -316,7 +322,7 @@ __global__ void __launch_bounds__(VDims<N>::NT) hyper_glap_kernel(const KParams 
         for (int s = 0; s < 3; ++s) {
             g1[s] *= xi[0];
             g2[s] *= xi[1];
-            g3[s] *= xi[2];
+            g3[s] *= xz;
         }
         auto add = [&](int ff, R* gd) {
             const int idx = ff * Nfp + x.on_face(ff);
@@ -378,7 +384,9 @@ int init_hyper_tables(Model* md) {
     const bool zper = m.desc.periodic[2] != 0;
     const double inv_w0 = 1.0 / m.omega[0];
     std::vector<double> gz(nlev), lap(nlev);
-    for (int lev = 0; lev < nlev; ++lev) gz[lev] = md->lvv64[(size_t)lev * VV_NFIELDS + VV_DHT_REF];
+    // HorizontalDirection: h_ref depends on z only, its horizontal derivatives vanish
+    const bool horiz = md->prm.hyper_direction == CMDG_DIR_HORIZONTAL;
+    for (int lev = 0; lev < nlev; ++lev) gz[lev] = horiz ? 0.0 : md->lvv64[(size_t)lev * VV_NFIELDS + VV_DHT_REF];
     auto below = [&](int ez) { return ez > 0 ? ez - 1 : (zper ? nz - 1 : -1); };
     auto above = [&](int ez) { return ez + 1 < nz ? ez + 1 : (zper ? 0 : -1); };
     for (int lev = 0; lev < nlev; ++lev) {
@@ -480,5 +488,7 @@ extern "C" int cmdg_hyperdiffusive_state(cmdg_model* model, void* d_hd, const vo
     CMDG_ARG_CHECK(model != nullptr, "model is NULL");
     CMDG_ARG_CHECK(d_hd != nullptr && d_Q != nullptr, "NULL buffer");
     CMDG_ARG_CHECK(model->m.prm.hyperdiffusion != CMDG_HYPER_NONE, "the model has no hyperdiffusion");
+    if (model->m.mesh->kind == MESH_SHELL)
+        return launch_shell_hyper_passes(&model->m, d_Q, d_hd, (cudaStream_t)stream);
     return launch_hyper_passes(&model->m, d_Q, d_hd, (cudaStream_t)stream);
 }

@@ -30,18 +30,10 @@
 // reference-state jump q_ref(-) - q_ref(+) in the Rusanov penalty is the
 // FP64-computed level jump across vertical faces plus the difference of the
 // two nodes' per-node parts.
-#include "dg_common.cuh"
+#include "shell_common.cuh"
 
 namespace cmdg {
 namespace {
-
-template <int N>
-struct ShellDims {
-    static constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp, NF = 6 * Nfp;
-    static constexpr int NT = (((Np > NF) ? Np : NF) + 31) / 32 * 32;
-    static constexpr int MIN_CTAS = N == 2 ? 12 : N == 3 ? 8 : N == 4 ? 6 : 4;
-    static constexpr int MIN_CTAS64 = N == 5 ? 2 : 3;
-};
 
 template <int N, typename R>
 struct ShellSmem {
@@ -57,8 +49,15 @@ struct ShellSmem {
     static constexpr size_t BYTES = sizeof(R) * TOTAL;
 };
 
-template <int N, typename R, bool MIXED, int MODE>
-__global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CTAS : ShellDims<N>::MIN_CTAS64)
+// HYPER: DryBiharmonic hyperdiffusion, whose state nu grad^3 (Np, 12, nelem;
+// word 3 c + d = nu d/dx_d lap(u_h[c]), 9 + d = nu d/dx_d lap(h_tot)) is read
+// from P.hd: the hyperdiffusive fluxes (tendencies_momentum.jl:51-54,
+// tendencies_energy.jl:40-48) join the volume flux and, with the neighbour's
+// state, the central second-order interface flux; walls carry the
+// first-order flux only (boundaryconditions.jl:113-185).
+template <int N, typename R, bool MIXED, int MODE, bool HYPER>
+__global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER ? 4 : ShellDims<N>::MIN_CTAS)
+                                                          : ShellDims<N>::MIN_CTAS64)
     shell_stage_kernel(const KParams P) {
     using Dm = ShellDims<N>;
     using SM = ShellSmem<N, R>;
@@ -137,6 +136,21 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
             F1[s] = flux_d<R, MIXED>(q, th, 1, s);
             F2[s] = flux_d<R, MIXED>(q, th, 2, s);
         }
+        if (HYPER) {
+            const R* hn = static_cast<const R*>(P.hd) + (size_t)e * 12 * Np + t;
+            R hd[12];
+#pragma unroll
+            for (int w = 0; w < 12; ++w) hd[w] = hn[w * Np];
+            const R rho = MIXED ? lv.rho_ref + q[0] : q[0];
+            auto add_hyper = [&](R(&F)[NSTATE], int d) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) F[1 + c] += rho * hd[3 * c + d];
+                F[4] += (hd[d] * q[1] + hd[3 + d] * q[2] + hd[6 + d] * q[3]) + hd[9 + d] * rho;
+            };
+            add_hyper(F0, 0);
+            add_hyper(F1, 1);
+            add_hyper(F2, 2);
+        }
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             R Ft[NSTATE];
@@ -187,11 +201,7 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
                     jr[4] = sj * (R)P.jump32[2 * ej + 1];
                 }
             } else {
-                const unsigned code = ((unsigned)__ldg(nbr + 7) >> (4 * f)) & 15u;
-                const int f2 = (int)(code & 3u);
-                const int a2 = (code & 4u) ? N - fa : fa;
-                const int side2 = (f2 & 1) ? N : 0;
-                vP = (f2 < 2) ? side2 + Nq * (a2 + Nq * fb) : a2 + Nq * (side2 + Nq * fb);
+                vP = shell_partner<N>(nbr, f, fn);
             }
             const R* qn = Qin + (size_t)nb * ESTRIDE + vP;
 #pragma unroll
@@ -203,6 +213,15 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
             for (int s = 0; s < NSTATE; ++s) qp[s] = qm[s];
 #pragma unroll
             for (int c = 0; c < 3; ++c) qp[1 + c] = qm[1 + c] - R(2) * mn_m * nv[c];
+            if (HYPER) {
+                // the staged flux holds the second-order part too: walls take the first-order one
+                const Level<R> lvm = shell_level<R, MIXED>(P, ge, Np, vM, ez * Nq + kM);
+                const Thermo<R, MIXED> thm = thermo<R, MIXED>(qm, lvm, P);
+                Fm[0] = mn_m;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) Fm[1 + c] = mn_m * thm.u[c] + thm.pflux * nv[c];
+                Fm[4] = mn_m * thm.rinv * thm.H;
+            }
         }
         Level<R> lvp = load_level<R>(P, ezp * Nq + kP);
         if (!MIXED) lvp.crho += gp[KG_DCRHO * Np + vP];
@@ -228,6 +247,18 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
 #pragma unroll
         for (int c = 0; c < 3; ++c) Fp[1 + c] = mn_p * thp.u[c] + thp.pflux * nv[c];
         Fp[4] = un_p * thp.H;
+        if (HYPER && nb >= 0) {
+            // neighbour's hyperdiffusive flux . n
+            const R* hn = static_cast<const R*>(P.hd) + (size_t)nb * 12 * Np + vP;
+            R hn_n[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                hn_n[c] = nv[0] * hn[(3 * c + 0) * Np] + nv[1] * hn[(3 * c + 1) * Np] + nv[2] * hn[(3 * c + 2) * Np];
+            const R rho_p = MIXED ? lvp.rho_ref + qp[0] : qp[0];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) Fp[1 + c] += rho_p * hn_n[c];
+            Fp[4] += (hn_n[0] * qp[1] + hn_n[1] * qp[2] + hn_n[2] * qp[3]) + hn_n[3] * rho_p;
+        }
         const R lam_p = fabs(un_p) + thp.c;
         const R lift = sJ * iJm * KConst<R>::inv_w0(P);
         const R hmw = (ph.numflux == CMDG_FLUX_RUSANOV) ? R(0.5) * fmax(lam_m, lam_p) : R(0);
@@ -302,7 +333,7 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
     if (__any_sync(0xffffffffu, bad) && (t & 31) == 0) atomicOr(P.status, 1u);
 }
 
-template <int N, typename R, bool MIXED, int MODE>
+template <int N, typename R, bool MIXED, int MODE, bool HYPER>
 cudaError_t launch_shell_typed(const KParams& P, cudaStream_t s) {
     constexpr size_t bytes = ShellSmem<N, R>::BYTES;
     static unsigned long long configured = 0;
@@ -310,34 +341,46 @@ cudaError_t launch_shell_typed(const KParams& P, cudaStream_t s) {
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (!(configured & (1ull << (dev & 63)))) {
-        e = cudaFuncSetAttribute(shell_stage_kernel<N, R, MIXED, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)bytes);
+        e = cudaFuncSetAttribute(shell_stage_kernel<N, R, MIXED, MODE, HYPER>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
         if (e != cudaSuccess) return e;
         configured |= 1ull << (dev & 63);
     }
-    shell_stage_kernel<N, R, MIXED, MODE><<<(unsigned)P.nelem, ShellDims<N>::NT, bytes, s>>>(P);
+    shell_stage_kernel<N, R, MIXED, MODE, HYPER><<<(unsigned)P.nelem, ShellDims<N>::NT, bytes, s>>>(P);
     return cudaGetLastError();
 }
 
-template <int N>
+template <int N, bool HYPER>
 cudaError_t launch_shell_N(const KParams& P, bool mixed, int mode, cudaStream_t s) {
     if (mixed)
-        return mode == 0 ? launch_shell_typed<N, float, true, 0>(P, s) : launch_shell_typed<N, float, true, 1>(P, s);
-    return mode == 0 ? launch_shell_typed<N, double, false, 0>(P, s) : launch_shell_typed<N, double, false, 1>(P, s);
+        return mode == 0 ? launch_shell_typed<N, float, true, 0, HYPER>(P, s)
+                         : launch_shell_typed<N, float, true, 1, HYPER>(P, s);
+    return mode == 0 ? launch_shell_typed<N, double, false, 0, HYPER>(P, s)
+                     : launch_shell_typed<N, double, false, 1, HYPER>(P, s);
+}
+
+template <int N>
+cudaError_t launch_shell_N(const KParams& P, bool mixed, int mode, bool hyper, cudaStream_t s) {
+    return hyper ? launch_shell_N<N, true>(P, mixed, mode, s) : launch_shell_N<N, false>(P, mixed, mode, s);
 }
 
 }  // namespace
 
 int launch_shell_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
     const Mesh& m = *md->mesh;
+    const bool hyper = md->prm.hyperdiffusion != CMDG_HYPER_NONE;
+    if (hyper) {
+        const int rc = launch_shell_hyper_passes(md, a.Qin, md->d_hd, s);
+        if (rc) return rc;
+    }
     const KParams P = make_params(md, a);
     const bool mixed = md->precision == CMDG_MIXED;
     cudaError_t err;
     switch (m.N) {
-        case 2: err = launch_shell_N<2>(P, mixed, a.mode, s); break;
-        case 3: err = launch_shell_N<3>(P, mixed, a.mode, s); break;
-        case 4: err = launch_shell_N<4>(P, mixed, a.mode, s); break;
-        case 5: err = launch_shell_N<5>(P, mixed, a.mode, s); break;
+        case 2: err = launch_shell_N<2>(P, mixed, a.mode, hyper, s); break;
+        case 3: err = launch_shell_N<3>(P, mixed, a.mode, hyper, s); break;
+        case 4: err = launch_shell_N<4>(P, mixed, a.mode, hyper, s); break;
+        case 5: err = launch_shell_N<5>(P, mixed, a.mode, hyper, s); break;
         default:
             set_error("no cubed-shell stage kernel for N=%d", m.N);
             return CMDG_ERR_ARG;

@@ -538,6 +538,9 @@ KParams make_params(Model* md, const LaunchArgs& a) {
     P.glap_ref32 = md->d_glap_ref;
     P.inv_tau_hyper = md->prm.tau_hyper > 0 ? 1.0 / md->prm.tau_hyper : 0.0;
     P.inv_tau_hyper32 = (float)P.inv_tau_hyper;
+    P.nu4 = md->d_nu4;
+    P.hyper_horizontal = md->prm.hyper_direction == CMDG_DIR_HORIZONTAL;
+    P.hglap_ref32 = md->d_hglap_ref;
     return P;
 }
 

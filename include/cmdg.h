@@ -92,6 +92,8 @@ typedef struct {
     double planet_radius; /* SphericalOrientation: Phi = grav (|x| - planet_radius) */
     int hyperdiffusion; /* CMDG_HYPER_* (brick meshes with FlatOrientation) */
     double tau_hyper;   /* DryBiharmonic tau_timescale (s) */
+    int hyper_direction;/* diffusion_direction of the hyperdiffusion passes: CMDG_DIR_EVERY or
+                           CMDG_DIR_HORIZONTAL (DGModel.jl:22-65, SpaceDiscretization.jl:731-1083) */
 } cmdg_atmos_params;
 
 /* Stacked equiangular cubed shell: 6 nhorz^2 columns of nvert elements
@@ -286,10 +288,12 @@ int cmdg_courant_dt(cmdg_model* model, const double* d_Q, double CFL, double* h_
 int cmdg_gradient_flux(cmdg_model* model, void* d_gf, const void* d_Q, void* stream);
 
 /* Hyperdiffusive state of d_Q (the passes that precede every tendency of a
- * model with DryBiharmonic hyperdiffusion) into d_hd, column-major
- * (Np, 9, nelem) in the model's precision: word 3 c + d holds
- * nu_4 d/dx_d (laplacian of c) for c = u, v, h_tot (the horizontal velocity
- * u_h of a flat brick has no vertical component), nu_4 = (Delta_h/2)^4/2/tau.
+ * model with DryBiharmonic hyperdiffusion) into d_hd, column-major in the
+ * model's precision: word 3 c + d holds nu_4 d/dx_d (laplacian of c),
+ * nu_4 = (Delta_h/2)^4/2/tau.  Brick: (Np, 9, nelem), c = u, v, h_tot (the
+ * horizontal velocity u_h of a flat brick has no vertical component); cubed
+ * shell: (Np, 12, nelem), c = u_h[0], u_h[1], u_h[2], h_tot.  d_hd must
+ * hold that many words.
  * Replaces the hyperdiffusive part of launch_volume_gradients! +
  * launch_interface_gradients!, launch_volume_divergence_of_gradients! +
  * launch_interface_divergence_of_gradients! and

@@ -80,6 +80,8 @@ typedef struct {
     double planet_radius; // SphericalOrientation: Phi = g (|x| - planet_radius)
     int hyperdiffusion; // 0 = NoHyperDiffusion, 1 = DryBiharmonic (TurbulenceClosures.jl:793-848)
     double tau_hyper;   // DryBiharmonic.tau_timescale
+    int hyper_direction;// DGModel diffusion_direction of the hyperdiffusion passes:
+                        // 0 = EveryDirection, 1 = HorizontalDirection (SpaceDiscretization.jl:731-1083)
 } om_params;
 
 // StackedCubedSphereTopology (Topologies.jl:1620-1760) over a
@@ -1096,6 +1098,8 @@ void node_hyper_args(const Model& m, const double* Q, int64_t e, int n, double* 
 void hyper_gradient_pass(Model& m, const double* Q) {
     const om_params& p = m.prm;
     const int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp, ngl = m.ngl;
+    const bool horiz = p.hyper_direction == 1;
+    const int nface = horiz ? 4 : 6;
     m.hgrad.assign((size_t)m.nelem * 3 * ngl * Np, 0.0);
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < m.nelem; ++e) {
@@ -1115,11 +1119,11 @@ void hyper_gradient_pass(Model& m, const double* Q) {
                         for (int d = 0; d < 3; ++d) {
                             double gH = VGc(m, e, XI1X1 + 3 * d, ijk) * G1 + VGc(m, e, XI2X1 + 3 * d, ijk) * G2;
                             double gV = VGc(m, e, XI3X1 + 3 * d, ijk) * G3;
-                            HG(m, e, 3 * s + d, ijk) = gH + gV;
+                            HG(m, e, 3 * s + d, ijk) = horiz ? gH : gH + gV;
                         }
                     }
                 }
-        for (int f = 0; f < 6; ++f)
+        for (int f = 0; f < nface; ++f)
             for (int n = 0; n < Nfp; ++n) {
                 int64_t idM = m.vmapM[(e * 6 + f) * Nfp + n], idP = m.vmapP[(e * 6 + f) * Nfp + n];
                 int vM = (int)(idM % Np);
@@ -1157,6 +1161,8 @@ void hyper_gradient_pass(Model& m, const double* Q) {
 // (src/Atmos/Model/boundaryconditions.jl:88-95).
 void hyper_divergence_pass(Model& m) {
     const int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp, ngl = m.ngl;
+    const bool horiz = m.prm.hyper_direction == 1;
+    const int nface = horiz ? 4 : 6;
     m.hdiv.assign((size_t)m.nelem * ngl * Np, 0.0);
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < m.nelem; ++e) {
@@ -1182,10 +1188,10 @@ void hyper_divergence_pass(Model& m) {
                             lh -= MI * Dm(m, n, j) * S2[(i + Nq * (n + Nq * k)) * ngl + s];
                         }
                         for (int n = 0; n < Nq; ++n) lv -= MI * Dm(m, n, k) * S3[(i + Nq * (j + Nq * n)) * ngl + s];
-                        HD(m, e, s, ijk) = lh + lv;
+                        HD(m, e, s, ijk) = horiz ? lh : lh + lv;
                     }
                 }
-        for (int f = 0; f < 6; ++f)
+        for (int f = 0; f < nface; ++f)
             for (int n = 0; n < Nfp; ++n) {
                 int64_t idM = m.vmapM[(e * 6 + f) * Nfp + n], idP = m.vmapP[(e * 6 + f) * Nfp + n];
                 int vM = (int)(idM % Np);
@@ -1225,6 +1231,8 @@ void hyper_transform(const Model& m, int64_t e, int n, const double* g, double* 
 // where lap+ = lap-.
 void hyper_gradlap_pass(Model& m) {
     const int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp, ngl = m.ngl, nw = 3 * m.ngl;
+    const bool horiz = m.prm.hyper_direction == 1;
+    const int nface = horiz ? 4 : 6;
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < m.nelem; ++e) {
         for (int k = 0; k < Nq; ++k)
@@ -1246,9 +1254,9 @@ void hyper_gradlap_pass(Model& m) {
                     }
                     hyper_transform(m, e, ijk, gH, tH);
                     hyper_transform(m, e, ijk, gV, tV);
-                    for (int w = 0; w < nw; ++w) HG(m, e, w, ijk) = tH[w] + tV[w];
+                    for (int w = 0; w < nw; ++w) HG(m, e, w, ijk) = horiz ? tH[w] : tH[w] + tV[w];
                 }
-        for (int f = 0; f < 6; ++f)
+        for (int f = 0; f < nface; ++f)
             for (int n = 0; n < Nfp; ++n) {
                 if (m.elemtobndy[e * 6 + f] != 0) continue;
                 int64_t idM = m.vmapM[(e * 6 + f) * Nfp + n], idP = m.vmapP[(e * 6 + f) * Nfp + n];
@@ -1280,6 +1288,9 @@ void hyper_passes(Model& m, const double* Q) {
 // (eta- + eta+)' n / 2 (NumericalFluxes.jl:670-715).
 void scalar_hyper_tendency(Model& m, double* T, const double* Q, double alpha, double beta) {
     const int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp;
+    // HorizontalDirection: the model direction restricts the tendency too
+    const bool horiz = m.prm.hyper_direction == 1;
+    const int nface = horiz ? 4 : 6;
     hyper_passes(m, Q);
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < m.nelem; ++e) {
@@ -1302,11 +1313,12 @@ void scalar_hyper_tendency(Model& m, double* T, const double* Q, double alpha, d
                         lh += MI * Dm(m, n, j) * F2[i + Nq * (n + Nq * k)];
                     }
                     for (int n = 0; n < Nq; ++n) lv += MI * Dm(m, n, k) * F3[i + Nq * (j + Nq * n)];
+                    if (horiz) lv = 0;
                     size_t idx = (size_t)e * Np + ijk;
                     double Th = (beta != 0) ? alpha * lh + beta * T[idx] : alpha * lh;
                     T[idx] = alpha * lv + Th;
                 }
-        for (int f = 0; f < 6; ++f)
+        for (int f = 0; f < nface; ++f)
             for (int n = 0; n < Nfp; ++n) {
                 int64_t idM = m.vmapM[(e * 6 + f) * Nfp + n], idP = m.vmapP[(e * 6 + f) * Nfp + n];
                 int vM = (int)(idM % Np);
@@ -1540,9 +1552,10 @@ om_model* om_create_shell(const om_shell* sh, const om_params* p) {
 
 // Constant-tensor scalar hyperdiffusion on a brick (one state per node,
 // layout (Np, 1, nelem)); H column-major 3x3.
-om_model* om_create_scalar_hyper(const om_brick* b, const double* H) {
+om_model* om_create_scalar_hyper(const om_brick* b, const double* H, int direction) {
     om_params p;
     std::memset(&p, 0, sizeof(p));
+    p.hyper_direction = direction;
     Model* m = new Model();
     m->mesh = *b;
     m->prm = p;

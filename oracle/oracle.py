@@ -74,6 +74,7 @@ class Params(ctypes.Structure):
         ("planet_radius", ctypes.c_double),
         ("hyperdiffusion", ctypes.c_int),
         ("tau_hyper", ctypes.c_double),
+        ("hyper_direction", ctypes.c_int),
     ]
 
 
@@ -153,7 +154,7 @@ def lib():
         L.om_apply_filter.argtypes = [P, dp, dp, dp, ctypes.c_int, ip, ctypes.c_int]
         L.om_apply_tmar.argtypes = [P, dp, ip, ctypes.c_int]
         L.om_create_scalar_hyper.restype = P
-        L.om_create_scalar_hyper.argtypes = [ctypes.POINTER(Brick), dp]
+        L.om_create_scalar_hyper.argtypes = [ctypes.POINTER(Brick), dp, ctypes.c_int]
         L.om_scalar_hyper_tendency.argtypes = [P, dp, dp, D, D]
         L.om_scalar_hyper_lsrk54.argtypes = [P, dp, dp, D, ctypes.c_int]
         L.om_lsrk54_scalar.restype = D
@@ -206,6 +207,7 @@ class OracleModel:
         p.C_smag = physics.get("C_smag", consts["C_smag"])
         p.hyperdiffusion = {"none": 0, "dry_biharmonic": 1}[physics.get("hyperdiffusion", "none")]
         p.tau_hyper = physics.get("tau_hyper", 0.0)
+        p.hyper_direction = {"every": 0, "horizontal": 1}[physics.get("hyper_direction", "every")]
         self.params, self.consts = p, consts
         self.L = lib()
         if shell is None:
@@ -399,7 +401,7 @@ class ScalarHyperdiffusion:
     test/Numerics/DGMethods/advection_diffusion/periodic_3D_hyperdiffusion.jl),
     evaluated by the same hyperdiffusion passes as the AtmosModel closure."""
 
-    def __init__(self, N, ne, lo, hi, H, periodic=(1, 1, 1)):
+    def __init__(self, N, ne, lo, hi, H, periodic=(1, 1, 1), direction="every"):
         b = Brick()
         b.N = N
         for d in range(3):
@@ -408,7 +410,7 @@ class ScalarHyperdiffusion:
         self.L = lib()
         Hc = np.ascontiguousarray(np.asarray(H, dtype=np.float64).T.reshape(9))  # column-major
         self.brick = b
-        self.h = self.L.om_create_scalar_hyper(ctypes.byref(b), _ptr(Hc))
+        self.h = self.L.om_create_scalar_hyper(ctypes.byref(b), _ptr(Hc), {"every": 0, "horizontal": 1}[direction])
         self.N, self.Nq = N, N + 1
         self.Np = self.L.om_Np(self.h)
         self.nelem = self.L.om_nelem(self.h)

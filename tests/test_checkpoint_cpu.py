@@ -73,3 +73,13 @@ def test_rm_checkpoint(tmp_path):
     ck.rm_checkpoint(str(tmp_path), "r", rank=1, num=2)
     assert not os.path.exists(path)
     ck.rm_checkpoint(str(tmp_path), "r", rank=1, num=2)  # force = true: no error
+
+
+def test_fp32_record_round_trip(tmp_path):
+    Q, A = arrays()
+    Qp = Q.astype(np.float32)
+    ck.write_checkpoint_arrays(Q, A, 2.0, str(tmp_path), "p", h_Qp=Qp)
+    rec, t = ck.read_checkpoint_records(str(tmp_path), "p")
+    assert t == 2.0 and rec["h_Qp"].dtype == np.float32 and np.array_equal(rec["h_Qp"], Qp)
+    Q2, A2, _ = ck.read_checkpoint(str(tmp_path), "p")
+    assert np.array_equal(Q2, Q) and np.array_equal(A2, A)

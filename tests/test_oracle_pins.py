@@ -11,10 +11,11 @@ Pins (reference paths relative to the ClimateMachine.jl project root):
     the LES brick and on the GCM stacked cubed shell (3 x 3 horizontal
     elements per panel, 3 vertical, 50 km, N=4, IsothermalProfile,
     subtract_off = false, 100 s of LSRK54 at Courant 0.1)
-  * constant-tensor scalar hyperdiffusion, 3D, EveryDirection, N=4, levels
-    1 and 2 — test/Numerics/DGMethods/advection_diffusion/
-    periodic_3D_hyperdiffusion.jl:229-231 (the hyperdiffusion passes that the
-    AtmosModel's DryBiharmonic closure also runs)
+  * constant-tensor scalar hyperdiffusion, 3D, EveryDirection and
+    HorizontalDirection, N=4, levels 1 and 2 — test/Numerics/DGMethods/
+    advection_diffusion/periodic_3D_hyperdiffusion.jl:229-235 (the
+    hyperdiffusion passes that the AtmosModel's DryBiharmonic closure also
+    runs)
 Geometry checks of the cubed shell (Topologies.jl:1067-1305, Metrics.jl:431-724):
 shell volume from the mass matrix, the discrete metric identities (a uniform
 state has zero tendency) and the face-node maps (a linear density advected by
@@ -165,22 +166,27 @@ def test_shell_face_maps_give_the_analytic_advective_tendency():
     assert err < 5e-3, err
 
 
-GOLDEN_HYPER_3D = {1: 1.7363355506160003e-01, 2: 7.3049474767548042e-02}
+GOLDEN_HYPER_3D = {("every", 1): 1.7363355506160003e-01, ("every", 2): 7.3049474767548042e-02,
+                   ("horizontal", 1): 1.9244127301149615e-02, ("horizontal", 2): 5.8325158696244947e-03}
 
 
-@pytest.mark.parametrize("level", [1, 2])
-def test_periodic_3d_hyperdiffusion_golden(level):
+@pytest.mark.parametrize("direction,level", [("every", 1), ("every", 2), ("horizontal", 1), ("horizontal", 2)])
+def test_periodic_3d_hyperdiffusion_golden(direction, level):
     """rho = sin(x + 2y + 3z) under d rho/dt = -div(H grad lap rho) on the
     periodic [0, 2 pi]^3 cube for t = 1, dt = dx^4 / 25 / sum(H) rounded to
     divide 1; the weighted L2 distance to the exact decay matches the
-    reference's golden value."""
+    reference's golden value (EveryDirection, and HorizontalDirection, where
+    the passes and the tendency use the xi1, xi2 directions and faces 1-4)."""
     ne = 4 * 2 ** (level - 1)
     H = np.array([[9, 3, 5], [3, 7, 4], [5, 4, 10]]) / 50 / 100
-    m = O.ScalarHyperdiffusion(4, (ne,) * 3, (0, 0, 0), (2 * np.pi,) * 3, H)
+    m = O.ScalarHyperdiffusion(4, (ne,) * 3, (0, 0, 0), (2 * np.pi,) * 3, H, direction=direction)
     vg = m.vgeo
     x, y, z = (vg[:, O.VGEO[c]] for c in ("x1", "x2", "x3"))
     k = np.array([1.0, 2.0, 3.0])
-    c = (k @ k) * np.sum(np.outer(k, k) * H)
+    if direction == "every":
+        c = (k @ k) * np.sum(np.outer(k, k) * H)
+    else:
+        c = (k[:2] @ k[:2]) * np.sum((np.outer(k, k) * H)[:2, :2])
     Q = m.state()
     Q[:, 0] = np.sin(x + 2 * y + 3 * z)
     # min_node_distance (Grids.jl:454-520): nearest node along the element lines
@@ -190,7 +196,7 @@ def test_periodic_3d_hyperdiffusion_golden(level):
     m.lsrk54(Q, 1 / nsteps, nsteps)
     Qe = np.sin(x + 2 * y + 3 * z) * np.exp(-c)
     err = math.sqrt(np.sum(vg[:, O.VGEO["M"]] * (Q[:, 0] - Qe) ** 2))
-    assert err == pytest.approx(GOLDEN_HYPER_3D[level], rel=1e-10)
+    assert err == pytest.approx(GOLDEN_HYPER_3D[(direction, level)], rel=1e-10)
 
 
 def test_dry_biharmonic_acts_on_horizontal_velocity():
