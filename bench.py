@@ -13,8 +13,10 @@ value      mixed FP32/FP64 path (FP32 perturbation state, FP64 RK register),
            with CUDA events on the launching stream.
 fp64       the plain FP64 path, measured the same way.
 e2e        the same metric through the C ABI with the FP64 state in pinned
-           host memory: each step copies the state host->device, runs the
-           step and copies the result back, all inside the timed region.
+           host memory (cmdg_lsrk54_step_mixed_host): each step reads the
+           state from host memory over the host link (NVLink-C2C on GB300)
+           into the device's FP32 perturbation, runs the step and writes the
+           FP64 result back into host memory, all inside the timed region.
 roofline   the dominant kernel (the fused mixed stage kernel) against the
            measured HBM copy bandwidth; algorithmic bytes per node-stage
            B = 2*5*4 (state r/w, FP32) + 2*5*8 (RK register r/w, FP64) = 120.
@@ -353,17 +355,14 @@ def main():
     rel_vec = [rel[0], math.sqrt(float(np.sum((a[:, 1:4] - b[:, 1:4]) ** 2 * M[:, None, :]))) /
                math.sqrt(float(np.sum(b[:, 1:4] ** 2 * M[:, None, :]))), rel[4]]
 
-    # e2e: host FP64 state, H2D + step + D2H per step through the C ABI
+    # e2e: the FP64 state lives in pinned host memory; every step goes through
+    # the C ABI's host-state entry point, which reads it over the host link,
+    # steps, and writes the FP64 result back into host memory
     host = torch.from_numpy(np.ascontiguousarray(Q0)).pin_memory()
-    Qd = torch.empty_like(host, device="cuda")
     Qp = dgmx.new_state(torch.float32)
     dQ = torch.zeros(host.shape, dtype=torch.float64, device="cuda")
     def e2e_step():
-        Qd.copy_(host, non_blocking=True)
-        dgmx.to_perturbation(Qd, out=Qp)
-        dgmx.lsrk54_step(Qp, dQ, 0.0, dt, 1)
-        dgmx.from_perturbation(Qp, out=Qd)
-        host.copy_(Qd, non_blocking=True)
+        dgmx.lsrk54_step_host(host, Qp, dQ, 0.0, dt, 1)
 
     for _ in range(2):
         e2e_step()

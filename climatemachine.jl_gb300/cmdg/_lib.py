@@ -27,7 +27,7 @@ EXPORTS = (
     "cmdg_from_perturbation", "cmdg_tendency_mixed", "cmdg_lsrk54_step_mixed", "cmdg_weighted_sums",
     "cmdg_weighted_sums_mixed", "cmdg_courant_dt", "cmdg_status_word", "cmdg_lsrk54_step_noalloc",
     "cmdg_model_set_kernel", "cmdg_model_get_kernel", "cmdg_model_autotune", "cmdg_gradient_flux",
-    "cmdg_hyperdiffusive_state",
+    "cmdg_hyperdiffusive_state", "cmdg_lsrk54_step_mixed_host",
     "cmdg_batch_create", "cmdg_batch_destroy", "cmdg_batch_set_tiling", "cmdg_batch_get_tiling",
     "cmdg_batch_lsrk54_step", "cmdg_batch_autotune",
     "cmdg_filter_matrix", "cmdg_apply_filter", "cmdg_apply_tmar",
@@ -108,6 +108,7 @@ def load(path: str | None = None):
         "cmdg_model_autotune": [P, I, P, I, ctypes.POINTER(I), P],
         "cmdg_gradient_flux": [P, P, P, P],
         "cmdg_hyperdiffusive_state": [P, P, P, P],
+        "cmdg_lsrk54_step_mixed_host": [P, P, P, P, D, D, I, P],
         "cmdg_batch_create": [P, I, PP],
         "cmdg_batch_destroy": [P],
         "cmdg_batch_set_tiling": [P, I, I, I],

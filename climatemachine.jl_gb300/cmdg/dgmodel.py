@@ -194,6 +194,18 @@ class DGModel:
         fn = "cmdg_lsrk54_step_mixed" if self.mixed else "cmdg_lsrk54_step"
         call(fn, self.h, _dptr(Q), _dptr(dQ), float(t), float(dt), int(nsteps), _stream())
 
+    def lsrk54_step_host(self, h_Q: torch.Tensor, Qp: torch.Tensor, dQ: torch.Tensor, t, dt, nsteps=1):
+        """Mixed-precision steps of an FP64 state in pinned host memory
+        (``h_Q.is_pinned()``): the device reads h_Q into the FP32
+        perturbation Qp, steps with the FP64 register dQ and writes the result
+        back into h_Q, ordered on the current stream."""
+        if not self.mixed:
+            raise ValueError("lsrk54_step_host needs a mixed-precision model")
+        if h_Q.device.type != "cpu" or not h_Q.is_pinned() or h_Q.dtype != torch.float64 or not h_Q.is_contiguous():
+            raise ValueError("h_Q must be a contiguous pinned FP64 host tensor")
+        call("cmdg_lsrk54_step_mixed_host", self.h, ctypes.c_void_p(h_Q.data_ptr()), _dptr(Qp), _dptr(dQ), float(t),
+             float(dt), int(nsteps), _stream())
+
     # ------------------------------------------------------------------ launch configuration
     KERNELS = {"node": 0, "column": 1}
 

@@ -402,6 +402,31 @@ int cmdg_lsrk54_step_mixed(cmdg_model* model, float* d_Qp, double* d_dQ, double 
     return run_steps(&model->m, d_Qp, d_dQ, dt, nsteps, (cudaStream_t)stream);
 }
 
+int cmdg_lsrk54_step_mixed_host(cmdg_model* model, double* h_Q, float* d_Qp, double* d_dQ, double t, double dt,
+                                int nsteps, void* stream) {
+    int rc = check_model(model);
+    if (rc) return rc;
+    CMDG_ARG_CHECK(model->m.precision == CMDG_MIXED, "cmdg_lsrk54_step_mixed_host needs a mixed-precision model");
+    CMDG_ARG_CHECK(h_Q != nullptr && d_Qp != nullptr && d_dQ != nullptr, "NULL state");
+    CMDG_ARG_CHECK(nsteps >= 0, "nsteps must be >= 0");
+    CMDG_ARG_CHECK(std::isfinite(dt) && dt > 0, "dt must be positive and finite");
+    // the host state must be page-locked (mapped into the device's address space)
+    cudaPointerAttributes attr;
+    cudaError_t e = cudaPointerGetAttributes(&attr, h_Q);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("h_Q: %s", cudaGetErrorString(e));
+        return CMDG_ERR_ARG;
+    }
+    CMDG_ARG_CHECK(attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr,
+                   "h_Q must be page-locked host memory (cudaHostAlloc, cudaMallocHost or cudaHostRegister)");
+    double* dev_view = static_cast<double*>(attr.devicePointer);
+    const cudaStream_t s = (cudaStream_t)stream;
+    if ((rc = launch_to_perturbation(&model->m, d_Qp, dev_view, s))) return rc;
+    if (nsteps > 0 && (rc = cmdg_lsrk54_step_mixed(model, d_Qp, d_dQ, t, dt, nsteps, stream))) return rc;
+    return launch_from_perturbation(&model->m, dev_view, d_Qp, s);
+}
+
 int cmdg_to_perturbation(cmdg_model* model, float* d_Qp, const double* d_Q, void* stream) {
     int rc = check_model(model);
     if (rc) return rc;

@@ -282,28 +282,45 @@ struct Planar5<double> {
         base[4 * n + i] = v[4];
     }
 };
-// Asynchronous global->shared copies (cp.async, 4 or 8 bytes per thread):
-// the data goes to shared memory without passing through registers, so a
-// CTA can keep the next element's loads in flight while it computes.  Each
-// thread waits only for its own copy groups (cp.async.wait_group, a
-// hardware wait that ends when the thread's copies have landed).
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+// Bulk asynchronous global->shared copies (the TMA engine, cp.async.bulk)
+// completing on a shared-memory mbarrier: one thread issues a contiguous
+// copy of a multiple of 16 bytes between 16-byte-aligned addresses and arms
+// the barrier with the byte count; the consumers wait on the barrier's
+// phase.  Every wait is bounded: after the limit the caller records an error
+// and carries on (its shared-memory reads then see stale data, never
+// out-of-bounds addresses).
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
 }
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// orders this thread's earlier generic-proxy shared-memory accesses before
+// later async-proxy (bulk copy) writes to the same buffers
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
 }
-template <typename R>
-__device__ __forceinline__ void cp_async_r(R* smem, const R* gmem) {
-    if constexpr (sizeof(R) == 4) cp_async4(smem, gmem);
-    else cp_async8(smem, gmem);
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int PENDING>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// waits for the phase of `parity` to complete; false after 2^16 polls (each
+// poll may suspend the thread for a hardware-defined interval)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    for (int i = 0; i < (1 << 16); ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
 }
 
 // words of R taken by `words` words rounded up to 16 bytes

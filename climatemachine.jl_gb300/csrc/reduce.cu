@@ -9,6 +9,7 @@
 //    DoubleFloat{Float64}).
 //  * nondiffusive Courant number (src/Numerics/DGMethods/SpaceDiscretization.jl:307-365,
 //    src/Atmos/Model/courant.jl, minimum node distance src/Numerics/Mesh/Grids.jl:1228-1334).
+#include <algorithm>
 #include <cmath>
 
 #include "cmdg_internal.h"
@@ -29,28 +30,36 @@ __device__ __forceinline__ double ref_value(const double* lvl, const double* ref
     return (s == 0) ? L[LV_RHO_REF] : L[LV_RHOE_REF];
 }
 
+// One CTA per element (grid-stride over elements), one thread per node; each
+// thread issues its five loads before converting, and no index needs a
+// division.  Q may be page-locked host memory mapped into the device's
+// address space: the kernel then reads it over the host link.
 __global__ void to_perturbation_kernel(float* __restrict__ Qp, const double* __restrict__ Q, const double* lvl,
                                        const double* refn, int64_t nelem, int Np, int Nq, int nz) {
-    const int64_t total = nelem * NSTATE * Np;
-    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int node = (int)(idx % Np);
-        const int s = (int)((idx / Np) % NSTATE);
-        const int64_t e = idx / ((int64_t)Np * NSTATE);
-        Qp[idx] = (float)(Q[idx] - ref_value(lvl, refn, e, node, s, Np, nz, Nq));
-    }
+    for (int64_t e = blockIdx.x; e < nelem; e += gridDim.x)
+        for (int node = threadIdx.x; node < Np; node += blockDim.x) {
+            const size_t base = (size_t)e * NSTATE * Np + node;
+            double v[NSTATE];
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) v[s] = Q[base + (size_t)s * Np];
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s)
+                Qp[base + (size_t)s * Np] = (float)(v[s] - ref_value(lvl, refn, e, node, s, Np, nz, Nq));
+        }
 }
 
 __global__ void from_perturbation_kernel(double* __restrict__ Q, const float* __restrict__ Qp, const double* lvl,
                                          const double* refn, int64_t nelem, int Np, int Nq, int nz) {
-    const int64_t total = nelem * NSTATE * Np;
-    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int node = (int)(idx % Np);
-        const int s = (int)((idx / Np) % NSTATE);
-        const int64_t e = idx / ((int64_t)Np * NSTATE);
-        Q[idx] = ref_value(lvl, refn, e, node, s, Np, nz, Nq) + (double)Qp[idx];
-    }
+    for (int64_t e = blockIdx.x; e < nelem; e += gridDim.x)
+        for (int node = threadIdx.x; node < Np; node += blockDim.x) {
+            const size_t base = (size_t)e * NSTATE * Np + node;
+            float v[NSTATE];
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) v[s] = Qp[base + (size_t)s * Np];
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s)
+                Q[base + (size_t)s * Np] = ref_value(lvl, refn, e, node, s, Np, nz, Nq) + (double)v[s];
+        }
 }
 
 struct dd {
@@ -165,6 +174,7 @@ __global__ void courant_kernel(const double* __restrict__ Q, const double* emetr
 }
 
 constexpr int RED_BLOCKS = 304;  // 2 x 152 SMs
+constexpr int CONVERT_CTAS = 152 * 16;  // state conversions: 16 resident 128-thread CTAs per SM
 constexpr int RED_THREADS = 256;
 
 int ensure_red(Model* md) {
@@ -211,14 +221,16 @@ void release_quad(const Model* md) {
 
 int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s) {
     const Mesh& m = *md->mesh;
-    to_perturbation_kernel<<<RED_BLOCKS * 4, 256, 0, s>>>(Qp, Q, md->d_lvl64, md->d_ref64, m.nelem, m.Np, m.Nq, m.nz);
+    const unsigned grid = (unsigned)std::min<int64_t>(m.nelem, CONVERT_CTAS);
+    to_perturbation_kernel<<<grid, 128, 0, s>>>(Qp, Q, md->d_lvl64, md->d_ref64, m.nelem, m.Np, m.Nq, m.nz);
     CMDG_CUDA_CHECK(cudaGetLastError());
     return CMDG_OK;
 }
 
 int launch_from_perturbation(Model* md, double* Q, const float* Qp, cudaStream_t s) {
     const Mesh& m = *md->mesh;
-    from_perturbation_kernel<<<RED_BLOCKS * 4, 256, 0, s>>>(Q, Qp, md->d_lvl64, md->d_ref64, m.nelem, m.Np, m.Nq, m.nz);
+    const unsigned grid = (unsigned)std::min<int64_t>(m.nelem, CONVERT_CTAS);
+    from_perturbation_kernel<<<grid, 128, 0, s>>>(Q, Qp, md->d_lvl64, md->d_ref64, m.nelem, m.Np, m.Nq, m.nz);
     CMDG_CUDA_CHECK(cudaGetLastError());
     return CMDG_OK;
 }

@@ -78,17 +78,32 @@ struct Smem {
     static constexpr size_t BYTES = sizeof(R) * TOTAL;
 };
 
-// Double-buffered staging of the next element's inputs for the persistent
-// kernel (byte offsets after Smem): states (5 x Np, R), RK register
-// (5 x Np, FP64), neighbour states at the face nodes (5 x 6 Nfp, R).
+// Double-buffered staging of the persistent kernel (byte offsets after
+// Smem): per buffer the 16-byte-aligned window around one element's state
+// block (5 x Np words of R; the element's block starts 0..15 bytes into the
+// window) and around its RK register block (5 x Np doubles), then one
+// mbarrier per buffer.
 template <int N, typename R>
-struct SmemAsync {
-    static constexpr int Nq = N + 1, Np = Nq * Nq * Nq, NFN = 6 * Nq * Nq;
+struct SmemTma {
+    static constexpr int Np = (N + 1) * (N + 1) * (N + 1);
     static constexpr size_t QB = (Smem<N, R>::BYTES + 15) / 16 * 16;
-    static constexpr size_t DQB = QB + (2 * NSTATE * Np * sizeof(R) + 15) / 16 * 16;
-    static constexpr size_t QPB = DQB + 2 * NSTATE * Np * sizeof(double);
-    static constexpr size_t BYTES = QPB + 2 * NSTATE * NFN * sizeof(R);
+    static constexpr size_t QBLK = (NSTATE * Np * sizeof(R) + 32 + 15) / 16 * 16;
+    static constexpr size_t DB = QB + 2 * QBLK;
+    static constexpr size_t DBLK = (NSTATE * Np * sizeof(double) + 32 + 15) / 16 * 16;
+    static constexpr size_t BAR = DB + 2 * DBLK;
+    static constexpr size_t BYTES = BAR + 2 * sizeof(uint64_t);
 };
+
+// 16-byte-aligned window [lo, hi) around the byte range [a, a + n) of an
+// array [base, end); false when the window leaves the array (then the
+// element is read with plain loads).
+__device__ __forceinline__ bool bulk_window(uintptr_t base, uintptr_t end, uintptr_t a, size_t n, uintptr_t& lo,
+                                            uint32_t& bytes) {
+    lo = a & ~(uintptr_t)15;
+    const uintptr_t hi = (a + n + 15) & ~(uintptr_t)15;
+    bytes = (uint32_t)(hi - lo);
+    return lo >= base && hi <= end;
+}
 
 // Per-element inputs of one thread.
 template <typename R>
@@ -100,12 +115,11 @@ struct Ahead {
 };
 
 // Processes elements e_first, e_first + e_stride, ... below e_end with the
-// whole CTA.  PERSIST: a grid of resident CTAs walks the elements and copies
-// the next element's state, RK register and neighbour face states into
-// double-buffered shared memory with cp.async while it computes the current
-// one, so every CTA keeps memory requests in flight throughout (with plain
-// loads a CTA loads only at its start, which leaves HBM underused).  Every
-// thread reads back only the words it copied itself.
+// whole CTA.  PERSIST: a grid of resident CTAs walks the elements; while it
+// computes one element, the TMA engine copies the next element's state and
+// RK register blocks (contiguous in the (Np, 5, nelem) layout) into the other
+// of two shared-memory buffers, so every CTA keeps memory requests in flight
+// throughout without per-thread copy instructions.
 template <int N, typename R, bool MIXED, int MODE, bool PERSIST>
 __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem_raw, int e_first, int e_stride,
                                            int e_end) {
@@ -145,6 +159,13 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
     const int oside = fside ^ 1;
     const int vP = fd == 0 ? oside * N + Nq * fn : (fd == 1 ? fa + Nq * (oside * N + Nq * fb) : fn + Nfp * (oside * N));
     const int kM = vM / Nfp, kP = vP / Nfp;
+    // record of this node in the plane of the direction-d flux: the
+    // contraction index d is the slowest (d = 2 is the natural order), so a
+    // warp reading one position n of many lines, or one face, touches
+    // consecutive records
+    auto dir_rec = [&](int d) {
+        return d == 0 ? ni * Nfp + (nj + Nq * nk) : (d == 1 ? nj * Nfp + (ni + Nq * nk) : t);
+    };
     const R sgn = fside ? R(1) : R(-1);
 
     if (t < Nq * Nq) s_D[t] = static_cast<const R*>(P.Dhat)[t];
@@ -165,66 +186,99 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
         }
     };
 
-    // persistent staging buffers and their copy issue (groups A: state and
-    // register of an element; B: neighbour face states)
-    using SA = SmemAsync<N, R>;
-    R* const qbuf = reinterpret_cast<R*>(smem_raw + SA::QB);
-    double* const dqbuf = reinterpret_cast<double*>(smem_raw + SA::DQB);
-    R* const qpbuf = reinterpret_cast<R*>(smem_raw + SA::QPB);
-    auto issue_A = [&](int ee, int b) {
-        if (ee < e_end && node_thread) {
-            const size_t base = (size_t)ee * ESTRIDE + t;
-#pragma unroll
-            for (int s = 0; s < NSTATE; ++s) cp_async_r<R>(qbuf + (b * NSTATE + s) * Np + t, Qin + base + s * Np);
-            if (read_reg) {
-#pragma unroll
-                for (int s = 0; s < NSTATE; ++s) cp_async8(dqbuf + (b * NSTATE + s) * Np + t, P.dQ + base + s * Np);
-            }
+    // persistent staging: buffers, barriers, and the copy issue by thread 0
+    using ST = SmemTma<N, R>;
+    uint64_t* const bars = reinterpret_cast<uint64_t*>(smem_raw + ST::BAR);
+    const uintptr_t q_base = reinterpret_cast<uintptr_t>(Qin);
+    const uintptr_t q_end = q_base + (size_t)P.nelem * ESTRIDE * sizeof(R);
+    const uintptr_t d_base = reinterpret_cast<uintptr_t>(P.dQ);
+    const uintptr_t d_end = d_base + (size_t)P.nelem * ESTRIDE * sizeof(double);
+    // window of element ee's state (fs) and register (fd) blocks; shifts in words
+    auto windows = [&](int ee, uintptr_t& qlo, uint32_t& qbytes, bool& qok, uintptr_t& dlo, uint32_t& dbytes,
+                       bool& dok) {
+        const uintptr_t qa = q_base + (size_t)ee * ESTRIDE * sizeof(R);
+        qok = bulk_window(q_base, q_end, qa, ESTRIDE * sizeof(R), qlo, qbytes);
+        dok = false;
+        dbytes = 0;
+        dlo = 0;
+        if (read_reg) {
+            const uintptr_t da = d_base + (size_t)ee * ESTRIDE * sizeof(double);
+            dok = bulk_window(d_base, d_end, da, ESTRIDE * sizeof(double), dlo, dbytes);
         }
-        cp_async_commit();
     };
-    auto issue_B = [&](int ee, int nbv, int b) {
-        if (ee < e_end && nbv >= 0) {
-            const R* qn = Qin + (size_t)nbv * ESTRIDE + vP;
-#pragma unroll
-            for (int s = 0; s < NSTATE; ++s) cp_async_r<R>(qpbuf + (b * NSTATE + s) * NFN + t, qn + s * Np);
+    int issued0 = 0, issued1 = 0;  // copies armed per buffer (thread 0)
+    auto issue = [&](int ee, int b) {  // thread 0 only
+        if (b) ++issued1;
+        else ++issued0;
+        uint32_t total = 0;
+        uintptr_t qlo = 0, dlo = 0;
+        uint32_t qbytes = 0, dbytes = 0;
+        bool qok = false, dok = false;
+        if (ee < e_end) {
+            windows(ee, qlo, qbytes, qok, dlo, dbytes, dok);
+            total = (qok ? qbytes : 0u) + (dok ? dbytes : 0u);
         }
-        cp_async_commit();
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&bars[b], total);
+        if (qok) bulk_copy_g2s(smem_raw + ST::QB + b * ST::QBLK, reinterpret_cast<const void*>(qlo), qbytes, &bars[b]);
+        if (dok) bulk_copy_g2s(smem_raw + ST::DB + b * ST::DBLK, reinterpret_cast<const void*>(dlo), dbytes, &bars[b]);
     };
+    bool timed_out = false;
 
     int e = e_first;
     Ahead<R> cur;
-    int ez_n = 0, nb_n = -1;
     if (PERSIST) {
-        if (e < e_end) {
-            ez_n = __ldg(P.nbr + NBR_STRIDE * e + 6);
-            nb_n = face_thread ? __ldg(P.nbr + NBR_STRIDE * e + f) : -1;
+        if (t == 0) {
+            mbar_init(&bars[0], 1);
+            mbar_init(&bars[1], 1);
+            mbar_fence_init();
         }
-        issue_A(e, 0);
-        issue_B(e, nb_n, 0);
+        __syncthreads();
+        if (t == 0) issue(e, 0);
     }
     for (int it = 0; e < e_end; e += e_stride, ++it) {
-        const int en = e + e_stride;
         const int b = it & 1;
         double dq_old[NSTATE];
         const size_t ebase = (size_t)e * ESTRIDE + t;
         if (PERSIST) {
-            cur.ez = ez_n;
-            cur.nb = nb_n;
-            if (en < e_end) {  // connectivity of the next element, used after phase 1
-                ez_n = __ldg(P.nbr + NBR_STRIDE * en + 6);
-                nb_n = face_thread ? __ldg(P.nbr + NBR_STRIDE * en + f) : -1;
+            // the other buffer was read at the start of the previous element,
+            // before that element's closing barrier: copy the next element into it
+            if (t == 0) issue(e + e_stride, b ^ 1);
+            const int* nbr = P.nbr + NBR_STRIDE * e;
+            cur.ez = __ldg(nbr + 6);
+            cur.nb = face_thread ? __ldg(nbr + f) : -1;
+            if (cur.nb >= 0) {
+                const R* qn = Qin + (size_t)cur.nb * ESTRIDE + vP;
+#pragma unroll
+                for (int s = 0; s < NSTATE; ++s) cur.qp[s] = qn[s * Np];
             }
-            cp_async_wait<1>();  // group A of this element has landed
+            if (!mbar_wait_bounded(&bars[b], (uint32_t)((it >> 1) & 1))) timed_out = true;
+            uintptr_t qlo, dlo;
+            uint32_t qbytes, dbytes;
+            bool qok, dok;
+            windows(e, qlo, qbytes, qok, dlo, dbytes, dok);
             if (node_thread) {
+                if (qok) {
+                    const R* qs = reinterpret_cast<const R*>(smem_raw + ST::QB + b * ST::QBLK) +
+                                  (q_base + (size_t)e * ESTRIDE * sizeof(R) - qlo) / sizeof(R);
 #pragma unroll
-                for (int s = 0; s < NSTATE; ++s) cur.q[s] = qbuf[(b * NSTATE + s) * Np + t];
+                    for (int s = 0; s < NSTATE; ++s) cur.q[s] = qs[s * Np + t];
+                } else {
+#pragma unroll
+                    for (int s = 0; s < NSTATE; ++s) cur.q[s] = Qin[ebase + s * Np];
+                }
                 if (read_reg) {
+                    if (dok) {
+                        const double* ds = reinterpret_cast<const double*>(smem_raw + ST::DB + b * ST::DBLK) +
+                                           (d_base + (size_t)e * ESTRIDE * sizeof(double) - dlo) / sizeof(double);
 #pragma unroll
-                    for (int s = 0; s < NSTATE; ++s) dq_old[s] = dqbuf[(b * NSTATE + s) * Np + t];
+                        for (int s = 0; s < NSTATE; ++s) dq_old[s] = ds[s * Np + t];
+                    } else {
+#pragma unroll
+                        for (int s = 0; s < NSTATE; ++s) dq_old[s] = P.dQ[ebase + s * Np];
+                    }
                 }
             }
-            issue_A(en, b ^ 1);
         } else {
             fetch(e, cur);
             if (node_thread && read_reg) {
@@ -248,20 +302,12 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
                 R F[NSTATE];
 #pragma unroll
                 for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(cur.q, th, dd, s);
-                PL::st(s_F + dd * SM::P5N, Np, t, F);
+                PL::st(s_F + dd * SM::P5N, Np, dir_rec(dd), F);
             }
             if (ph.gravity) {
                 R rho_s = MIXED ? ((ph.ref_state && ph.subtract_off) ? cur.q[0] : lv.rho_ref + cur.q[0])
                                 : ((ph.ref_state && ph.subtract_off) ? cur.q[0] - lv.rho_ref : cur.q[0]);
                 gsrc = -rho_s * lv.gphiz;
-            }
-        }
-        if (PERSIST) {
-            issue_B(en, nb_n, b ^ 1);
-            cp_async_wait<2>();  // group B of this element has landed
-            if (cur.nb >= 0) {
-#pragma unroll
-                for (int s = 0; s < NSTATE; ++s) cur.qp[s] = qpbuf[(b * NSTATE + s) * NFN + t];
             }
         }
         __syncthreads();
@@ -272,7 +318,7 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
             PL::ld(s_node, Np, vM, qm);
             const CRV cr = s_cr[vM];
             const R c_m = cr.x, ri_m = cr.y;
-            PL::ld(s_F + fd * SM::P5N, Np, vM, Fm);
+            PL::ld(s_F + fd * SM::P5N, Np, fside * N * Nfp + fn, Fm);  // dir_rec(fd) of vM
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) Fm[s] *= sgn;
             const R lam_m = fabs(pick3(fd, qm[1], qm[2], qm[3]) * ri_m) + c_m;
@@ -318,14 +364,14 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
         int bad = 0;
         if (node_thread) {
             R acc1[NSTATE] = {0, 0, 0, 0, 0}, acc2[NSTATE] = {0, 0, 0, 0, 0}, acc3[NSTATE] = {0, 0, 0, 0, 0};
-            const int L1 = Nq * (nj + Nq * nk);  // line along xi1 (stride 1)
-            const int L2 = ni + Nfp * nk;        // line along xi2 (stride Nq)
+            const int L1 = nj + Nq * nk;  // line along xi1 (records n Nfp + L1)
+            const int L2 = ni + Nq * nk;  // line along xi2 (records n Nfp + L2)
             const int L3 = ni + Nq * nj;         // line along xi3 (stride Nfp)
 #pragma unroll
             for (int n = 0; n < Nq; ++n) {
                 R v1[NSTATE], v2[NSTATE], v3[NSTATE];
-                PL::ld(s_F, Np, L1 + n, v1);
-                PL::ld(s_F + SM::P5N, Np, L2 + n * Nq, v2);
+                PL::ld(s_F, Np, L1 + n * Nfp, v1);
+                PL::ld(s_F + SM::P5N, Np, L2 + n * Nfp, v2);
                 PL::ld(s_F + 2 * SM::P5N, Np, L3 + n * Nfp, v3);
                 const R d1 = s_D[ni * Nq + n], d2 = s_D[nj * Nq + n], d3 = s_D[nk * Nq + n];
 #pragma unroll
@@ -389,7 +435,17 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
             if (__any_sync(0xffffffffu, bad) && (t & 31) == 0) atomicOr(P.status, 1u);
         }
     }
-    if (PERSIST) cp_async_wait<0>();  // the trailing (empty) groups
+    if (PERSIST && timed_out) {
+        // a staging copy did not complete in time: report it, and before the
+        // CTA's shared memory is released wait (bounded) once more for the
+        // copies of both buffers
+        if (t == 0) {
+            atomicOr(P.status, 2u);
+            // phases complete in order: waiting for each buffer's latest armed phase covers the rest
+            if (issued0 > 0) mbar_wait_bounded(&bars[0], (uint32_t)((issued0 - 1) & 1));
+            if (issued1 > 0) mbar_wait_bounded(&bars[1], (uint32_t)((issued1 - 1) & 1));
+        }
+    }
 }
 
 template <int N, typename R, bool MIXED, int MODE, bool PERSIST>
@@ -401,7 +457,7 @@ __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? (PERSIST ? Dims<N>::MIN_C
 
 template <int N, typename R, bool MIXED, int MODE, bool PERSIST>
 cudaError_t launch_mode(const KParams& P, int grid_ctas, cudaStream_t s) {
-    constexpr size_t bytes = PERSIST ? SmemAsync<N, R>::BYTES : Smem<N, R>::BYTES;
+    constexpr size_t bytes = PERSIST ? SmemTma<N, R>::BYTES : Smem<N, R>::BYTES;
     // per-device set-up: opt in to > 48 KB of dynamic shared memory and size a
     // persistent grid from the occupancy of this instantiation
     static int resident[64] = {0};

@@ -211,6 +211,10 @@ __global__ void __launch_bounds__(VDims<N>::NT, (sizeof(R) == 4 ? (HYPER ? 4 : 6
     const int vP = fd == 0 ? oside * N + Nq * fn : (fd == 1 ? fa + Nq * (oside * N + Nq * fb) : fn + Nfp * (oside * N));
     const R sgn = fside ? R(1) : R(-1);
     if (t < Nq * Nq) s_D[t] = static_cast<const R*>(P.Dhat)[t];
+    // record of this node in the direction-d flux plane (contraction index slowest)
+    auto dir_rec = [&](int d) {
+        return d == 0 ? ni * Nfp + (nj + Nq * nk) : (d == 1 ? nj * Nfp + (ni + Nq * nk) : t);
+    };
 
     const size_t ebase = (size_t)e * ESTRIDE + t;
     R q[NSTATE], g[NGF], hd[9];
@@ -268,7 +272,7 @@ __global__ void __launch_bounds__(VDims<N>::NT, (sizeof(R) == 4 ? (HYPER ? 4 : 6
             R F[NSTATE];
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) F[s] = flux_d<R, MIXED>(q, th, dd, s) + F2[dd][s];
-            PL::st(s_F + dd * P5N, Np, t, F);
+            PL::st(s_F + dd * P5N, Np, dir_rec(dd), F);
         }
         if (ph.gravity) {
             R rho_s = MIXED ? ((ph.ref_state && ph.subtract_off) ? q[0] : lv.rho_ref + q[0])
@@ -287,7 +291,7 @@ __global__ void __launch_bounds__(VDims<N>::NT, (sizeof(R) == 4 ? (HYPER ? 4 : 6
         const R lam_m = fabs(pick3(fd, qm[1], qm[2], qm[3]) * ri_m) + c_m;
         const Level<R> lvm = load_level<R>(P, ez * Nq + vM / Nfp);
         if (nb >= 0) {
-            PL::ld(s_F + fd * P5N, Np, vM, Fm);
+            PL::ld(s_F + fd * P5N, Np, fside * N * Nfp + fn, Fm);  // dir_rec(fd) of vM
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) Fm[s] *= sgn;
             if (MIXED && fd == 2 && ph.numflux == CMDG_FLUX_RUSANOV) {
@@ -339,12 +343,12 @@ __global__ void __launch_bounds__(VDims<N>::NT, (sizeof(R) == 4 ? (HYPER ? 4 : 6
     int bad = 0;
     if (node_thread) {
         R acc1[NSTATE] = {0, 0, 0, 0, 0}, acc2[NSTATE] = {0, 0, 0, 0, 0}, acc3[NSTATE] = {0, 0, 0, 0, 0};
-        const int L1 = Nq * (nj + Nq * nk), L2 = ni + Nfp * nk, L3 = ni + Nq * nj;
+        const int L1 = nj + Nq * nk, L2 = ni + Nq * nk, L3 = ni + Nq * nj;
 #pragma unroll
         for (int n = 0; n < Nq; ++n) {
             R v1[NSTATE], v2[NSTATE], v3[NSTATE];
-            PL::ld(s_F, Np, L1 + n, v1);
-            PL::ld(s_F + P5N, Np, L2 + n * Nq, v2);
+            PL::ld(s_F, Np, L1 + n * Nfp, v1);
+            PL::ld(s_F + P5N, Np, L2 + n * Nfp, v2);
             PL::ld(s_F + 2 * P5N, Np, L3 + n * Nfp, v3);
             const R d1 = s_D[ni * Nq + n], d2 = s_D[nj * Nq + n], d3 = s_D[nk * Nq + n];
 #pragma unroll

@@ -263,6 +263,17 @@ int cmdg_tendency_mixed(cmdg_model* model, double* d_dQ, const float* d_Qp, doub
 int cmdg_lsrk54_step_mixed(cmdg_model* model, float* d_Qp, double* d_dQ, double t, double dt, int nsteps,
                            void* stream);
 
+/* Mixed-precision LSRK54 steps of an FP64 state h_Q (Np, 5, nelem) held in
+ * page-locked host memory (cudaHostAlloc / cudaMallocHost /
+ * cudaHostRegister; anything else is refused with CMDG_ERR_ARG): the device
+ * reads h_Q over the host link into the FP32 perturbation d_Qp, advances
+ * nsteps steps with the FP64 register d_dQ, and writes the FP64 result back
+ * into h_Q, all ordered on `stream` (synchronize it before reading h_Q).
+ * The dostep! of a reference solver whose state lives in host memory
+ * (src/Numerics/ODESolvers/LowStorageRungeKuttaMethod.jl:102-158). */
+int cmdg_lsrk54_step_mixed_host(cmdg_model* model, double* h_Q, float* d_Qp, double* d_dQ, double t, double dt,
+                                int nsteps, void* stream);
+
 /* Compensated weighted sums sum_nodes M * Q[:, field, :] for nfields fields
  * (FP64 state), result into host memory; double-double accumulation.
  * Replaces weightedsum(Q, states) (src/Arrays/MPIStateArrays.jl:655-675). */

@@ -232,3 +232,53 @@ def test_mixed_kernels_agree_and_autotune_keeps_results(kind):
     assert len(ms) == 3 and all(m > 0 for m in ms)
     assert choice[0] in ("node", "column")
     assert dg.status_word() == 0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("grid", [0, 7])
+def test_persistent_kernel_bitwise_equals_one_cta_per_element(precision, grid):
+    """The persistent kernel stages each element's state and RK register
+    with bulk copies into a two-buffer ring (plain loads for an element whose
+    16-byte-aligned window would leave the array, e.g. the last of 27) and
+    computes exactly what the one-CTA-per-element kernel computes, for a
+    resident wave (grid 0) and for 7 CTAs walking ~4 elements each."""
+    om, dg, Q0 = make_pair("bubble", 4, (3, 3, 3), precision=precision)
+    outs, tends = [], []
+    for kernel in (("node", -1), ("node", grid)):
+        dg.set_kernel(*kernel)
+        Q = dg.init_ode_state(Q0)
+        lsrk = cmdg.LSRK54CarpenterKennedy(dg, Q, dt=0.05)
+        cmdg.dostep_(Q, lsrk, None, 0.0, nsteps=3)
+        outs.append(Q.cpu().numpy())
+        dQ = torch.ones(Q.shape, dtype=torch.float64, device=Q.device)
+        dg(dQ, Q, None, 0.0, 0.5, 0.25)  # tendency with the register read (beta != 0)
+        tends.append(dQ.cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
+    assert np.array_equal(tends[0], tends[1])
+    assert dg.status_word() == 0
+
+
+def test_host_state_steps_equal_device_steps():
+    """cmdg_lsrk54_step_mixed_host (the state in pinned host memory, read and
+    written by the device over the host link) gives the same bits as
+    converting on the device and stepping; pageable memory is refused."""
+    import ctypes
+
+    from cmdg import _lib
+
+    om, dg, Q0 = make_pair("bubble", 4, (3, 3, 3), precision="mixed")
+    dt = 0.05
+    Qp = dg.init_ode_state(Q0)
+    dQ = torch.zeros(Qp.shape, dtype=torch.float64, device=Qp.device)
+    dg.lsrk54_step(Qp, dQ, 0.0, dt, 3)
+    ref = dg.from_perturbation(Qp).cpu()
+    h = torch.from_numpy(Q0.copy()).pin_memory()
+    Qp2 = dg.new_state(torch.float32)
+    dQ2 = torch.zeros(Qp.shape, dtype=torch.float64, device=Qp.device)
+    dg.lsrk54_step_host(h, Qp2, dQ2, 0.0, dt, 3)
+    torch.cuda.synchronize()
+    assert torch.equal(h, ref)
+    pageable = np.ascontiguousarray(Q0.copy())
+    with pytest.raises(_lib.CmdgError, match="page-locked"):
+        _lib.call("cmdg_lsrk54_step_mixed_host", dg.h, ctypes.c_void_p(pageable.ctypes.data),
+                  ctypes.c_void_p(Qp2.data_ptr()), ctypes.c_void_p(dQ2.data_ptr()), 0.0, dt, 1, None)
