@@ -13,14 +13,14 @@ for sm_103a behind a C ABI, include/cmdg.h).  Names follow the reference:
     solve_(Q, lsrk, timeend=...)                              # solve!(Q, lsrk; timeend)
 """
 from .atmos import EARTH, AtmosModel, HydrostaticState, DryAdiabaticProfile, IsothermalProfile, DryBiharmonic
-from .dgmodel import DGModel, BrickGrid, CubedShellGrid, euclidean_distance, weightedsum, norm
+from .dgmodel import DGModel, BrickGrid, CubedShellGrid, ArraysGrid, euclidean_distance, weightedsum, norm
 from .odesolvers import LSRK54CarpenterKennedy, solve_, dostep_
 from ._lib import CmdgError, load as load_library
 from .ensemble import Ensemble
 from . import checkpoint, filters, partition
 
 __all__ = [
-    "EARTH", "AtmosModel", "HydrostaticState", "DryBiharmonic", "DryAdiabaticProfile", "IsothermalProfile", "DGModel", "BrickGrid", "CubedShellGrid",
+    "EARTH", "AtmosModel", "HydrostaticState", "DryBiharmonic", "DryAdiabaticProfile", "IsothermalProfile", "DGModel", "BrickGrid", "CubedShellGrid", "ArraysGrid",
     "euclidean_distance", "weightedsum", "norm", "LSRK54CarpenterKennedy", "solve_", "dostep_", "CmdgError",
     "load_library", "Ensemble",
 ]

@@ -27,7 +27,7 @@ EXPORTS = (
     "cmdg_from_perturbation", "cmdg_tendency_mixed", "cmdg_lsrk54_step_mixed", "cmdg_weighted_sums",
     "cmdg_weighted_sums_mixed", "cmdg_courant_dt", "cmdg_status_word", "cmdg_lsrk54_step_noalloc",
     "cmdg_model_set_kernel", "cmdg_model_get_kernel", "cmdg_model_autotune", "cmdg_gradient_flux",
-    "cmdg_hyperdiffusive_state", "cmdg_lsrk54_step_mixed_host",
+    "cmdg_hyperdiffusive_state", "cmdg_lsrk54_step_mixed_host", "cmdg_mesh_create_arrays", "cmdg_model_set_reference",
     "cmdg_batch_create", "cmdg_batch_destroy", "cmdg_batch_set_tiling", "cmdg_batch_get_tiling",
     "cmdg_batch_lsrk54_step", "cmdg_batch_autotune",
     "cmdg_filter_matrix", "cmdg_apply_filter", "cmdg_apply_tmar",
@@ -62,6 +62,11 @@ class AtmosParams(ctypes.Structure):
 class ShellDesc(ctypes.Structure):
     _fields_ = [("N", ctypes.c_int), ("nhorz", ctypes.c_int), ("nvert", ctypes.c_int), ("r_inner", ctypes.c_double),
                 ("r_outer", ctypes.c_double), ("bc_inner", ctypes.c_int), ("bc_outer", ctypes.c_int)]
+
+
+class GridArrays(ctypes.Structure):
+    _fields_ = [("N", ctypes.c_int), ("nelem", ctypes.c_int64), ("vgeo", ctypes.c_void_p),
+                ("vmap_plus", ctypes.c_void_p), ("elemtobndy", ctypes.c_void_p)]
 
 
 _lib = None
@@ -109,6 +114,8 @@ def load(path: str | None = None):
         "cmdg_gradient_flux": [P, P, P, P],
         "cmdg_hyperdiffusive_state": [P, P, P, P],
         "cmdg_lsrk54_step_mixed_host": [P, P, P, P, D, D, I, P],
+        "cmdg_mesh_create_arrays": [ctypes.POINTER(GridArrays), PP],
+        "cmdg_model_set_reference": [P, P],
         "cmdg_batch_create": [P, I, PP],
         "cmdg_batch_destroy": [P],
         "cmdg_batch_set_tiling": [P, I, I, I],

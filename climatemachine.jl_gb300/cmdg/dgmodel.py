@@ -109,6 +109,34 @@ class CubedShellGrid(BrickGrid):
         self.ne = (6 * int(nhorz) * int(nhorz), 1, int(nvert))
 
 
+class ArraysGrid(BrickGrid):
+    """A mesh given by the reference's own DiscontinuousSpectralElementGrid
+    arrays (src/Numerics/Mesh/Grids.jl:76-125, 559-638): vgeo (Np, 16,
+    nelem), vmap+ (Nfp, 6, nelem, 1-based) and elemtobndy (6, nelem), passed
+    here in numpy's C order of the same memory: (nelem, 16, Np),
+    (nelem, 6, Nfp), (nelem, 6)."""
+
+    def __init__(self, N, vgeo: np.ndarray, vmap_plus: np.ndarray, elemtobndy: np.ndarray):
+        _lib.load()
+        vg = np.ascontiguousarray(vgeo, dtype=np.float64)
+        vp = np.ascontiguousarray(vmap_plus, dtype=np.int64)
+        eb = np.ascontiguousarray(elemtobndy, dtype=np.int64)
+        nelem = vg.shape[0]
+        Nq = int(N) + 1
+        if vg.shape != (nelem, 16, Nq**3) or vp.shape != (nelem, 6, Nq * Nq) or eb.shape != (nelem, 6):
+            raise ValueError("grid arrays have inconsistent shapes")
+        d = _lib.GridArrays()
+        d.N, d.nelem = int(N), int(nelem)
+        d.vgeo, d.vmap_plus, d.elemtobndy = vg.ctypes.data, vp.ctypes.data, eb.ctypes.data
+        h = ctypes.c_void_p()
+        call("cmdg_mesh_create_arrays", ctypes.byref(d), ctypes.byref(h))
+        self.h = h
+        self.desc = d
+        self.nelem, self.Np = self._sizes()
+        self.N, self.Nq = int(N), Nq
+        self.ne = (int(nelem), 1, 1)
+
+
 class DGModel:
     """DGModel(balance_law, grid, numerical_flux_first_order, ...) on the GPU.
 
@@ -156,6 +184,14 @@ class DGModel:
         if not self.mixed:
             return Q64
         return self.to_perturbation(Q64)
+
+    def set_reference(self, aux7: np.ndarray):
+        """Geopotential and reference state of a model on an ArraysGrid:
+        (nelem, 7, Np) = Phi, dPhi/dx1..3, rho_ref, rhoe_ref, p_ref."""
+        a = np.ascontiguousarray(aux7, dtype=np.float64)
+        if a.shape != (self.grid.nelem, 7, self.grid.Np):
+            raise ValueError(f"aux7 must be (nelem, 7, Np), got {a.shape}")
+        call("cmdg_model_set_reference", self.h, ctypes.c_void_p(a.ctypes.data))
 
     def reference_state(self) -> np.ndarray:
         out = np.empty((self.grid.nelem, 3, self.grid.Np), dtype=np.float64)

@@ -164,11 +164,27 @@ int cmdg_mesh_create_shell(const cmdg_shell_desc* desc, cmdg_mesh** out) {
     return CMDG_OK;
 }
 
+int cmdg_mesh_create_arrays(const cmdg_grid_arrays* desc, cmdg_mesh** out) {
+    CMDG_ARG_CHECK(out != nullptr, "output pointer is NULL");
+    *out = nullptr;
+    cmdg_mesh* mh = new cmdg_mesh();
+    int rc = build_arrays(desc, &mh->m);
+    if (rc) {
+        cudaFree(mh->m.d_nbr);
+        cudaFree(mh->m.d_fpart);
+        delete mh;
+        return rc;
+    }
+    *out = mh;
+    return CMDG_OK;
+}
+
 int cmdg_mesh_destroy(cmdg_mesh* mesh) {
     if (!mesh) return CMDG_OK;
     cudaFree(mesh->m.d_emetric);
     cudaFree(mesh->m.d_nbr);
     cudaFree(mesh->m.d_emetric32);
+    cudaFree(mesh->m.d_fpart);
     delete mesh;
     return CMDG_OK;
 }
@@ -184,7 +200,7 @@ int cmdg_mesh_coordinates(const cmdg_mesh* mesh, double* h_xyz) {
     CMDG_ARG_CHECK(mesh != nullptr && h_xyz != nullptr, "NULL argument");
     const Mesh& m = mesh->m;
     const int Nq = m.Nq, Np = m.Np;
-    if (m.kind == MESH_SHELL) {
+    if (m.kind != MESH_BRICK) {
         std::memcpy(h_xyz, m.xyz.data(), sizeof(double) * m.xyz.size());
         return CMDG_OK;
     }
@@ -211,7 +227,7 @@ int cmdg_mesh_mass(const cmdg_mesh* mesh, double* h_M) {
     CMDG_ARG_CHECK(mesh != nullptr && h_M != nullptr, "NULL argument");
     const Mesh& m = mesh->m;
     const int Nq = m.Nq, Np = m.Np;
-    if (m.kind == MESH_SHELL) {
+    if (m.kind != MESH_BRICK) {
         for (int64_t e = 0; e < m.nelem; ++e)
             for (int node = 0; node < Np; ++node)
                 h_M[(size_t)e * Np + node] = m.cgeo[((size_t)e * CG_NFIELDS + CG_M) * Np + node];
@@ -235,7 +251,13 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
     CMDG_ARG_CHECK(p->numflux == CMDG_FLUX_RUSANOV || p->numflux == CMDG_FLUX_CENTRAL, "unknown numerical flux %d",
                    p->numflux);
     const bool shell = mesh->m.kind == MESH_SHELL;
-    if (shell) {
+    const bool arrays = mesh->m.kind == MESH_ARRAYS;
+    if (arrays) {
+        CMDG_ARG_CHECK(p->turbulence == CMDG_TURB_NONE && p->hyperdiffusion == CMDG_HYPER_NONE,
+                       "the grid-arrays kernels are inviscid");
+        CMDG_ARG_CHECK(p->orientation >= CMDG_ORIENT_NONE && p->orientation <= CMDG_ORIENT_SPHERE,
+                       "unknown orientation %d", p->orientation);
+    } else if (shell) {
         CMDG_ARG_CHECK(p->orientation == CMDG_ORIENT_NONE || p->orientation == CMDG_ORIENT_SPHERE,
                        "orientation %d is not available on a cubed shell", p->orientation);
         CMDG_ARG_CHECK(p->turbulence == CMDG_TURB_NONE, "the cubed-shell kernels are inviscid");
@@ -285,6 +307,7 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
     md.ph.with_divergence = p->with_divergence;
     int rc = init_model_tables(&md);
     if (rc == CMDG_OK && shell) rc = init_shell_tables(&md);
+    if (rc == CMDG_OK && arrays) rc = init_arrays_tables(&md);
     if (rc == CMDG_OK && !shell && (p->turbulence != CMDG_TURB_NONE || p->hyperdiffusion != CMDG_HYPER_NONE))
         rc = init_viscous_tables(&md);
     if (rc == CMDG_OK && p->hyperdiffusion != CMDG_HYPER_NONE)
@@ -325,6 +348,7 @@ int cmdg_model_destroy(cmdg_model* model) {
     cudaFree(md.d_glap_ref);
     cudaFree(md.d_nu4);
     cudaFree(md.d_hglap_ref);
+    cudaFree(md.d_fjump);
     cudaFree(md.d_geo64);
     cudaFree(md.d_geo32);
     cudaFree(md.d_mass);
@@ -343,16 +367,27 @@ int cmdg_model_reference_state(const cmdg_model* model, double* h_ref) {
     CMDG_ARG_CHECK(h_ref != nullptr, "NULL output");
     const Model& md = model->m;
     const Mesh& m = *md.mesh;
-    const bool pernode = !md.ref64.empty();
+    const bool pernode = !md.ref64.empty(), pernode_p = !md.pref64.empty();
     for (int64_t e = 0; e < m.nelem; ++e)
         for (int node = 0; node < m.Np; ++node) {
             const int lev = (int)(e % m.nz) * m.Nq + node / m.Nfp;
             const double* L = &md.lvl64[(size_t)lev * LV_NFIELDS];
             h_ref[((size_t)e * 3 + 0) * m.Np + node] = pernode ? md.ref64[((size_t)e * 2 + 0) * m.Np + node] : L[LV_RHO_REF];
             h_ref[((size_t)e * 3 + 1) * m.Np + node] = pernode ? md.ref64[((size_t)e * 2 + 1) * m.Np + node] : L[LV_RHOE_REF];
-            h_ref[((size_t)e * 3 + 2) * m.Np + node] = L[LV_P_REF];
+            h_ref[((size_t)e * 3 + 2) * m.Np + node] = pernode_p ? md.pref64[(size_t)e * m.Np + node] : L[LV_P_REF];
         }
     return CMDG_OK;
+}
+
+int cmdg_model_set_reference(cmdg_model* model, const double* h_aux7) {
+    int rc = check_model(model);
+    if (rc) return rc;
+    CMDG_ARG_CHECK(h_aux7 != nullptr, "NULL aux");
+    CMDG_ARG_CHECK(model->m.mesh->kind == MESH_ARRAYS,
+                   "cmdg_model_set_reference applies to models on grid-arrays meshes (the generated meshes build "
+                   "their reference state)");
+    CMDG_CUDA_CHECK(cudaDeviceSynchronize());  // no stage may be reading the tables being replaced
+    return set_arrays_reference(&model->m, h_aux7);
 }
 
 int cmdg_tendency(cmdg_model* model, double* d_dQ, const double* d_Q, double t, double alpha, double beta,

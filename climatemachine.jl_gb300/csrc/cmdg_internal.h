@@ -84,8 +84,10 @@ struct Physics {
     int with_divergence;
 };
 
-// mesh kinds: affine brick, or stacked cubed shell (curvilinear, per-node metrics)
-enum { MESH_BRICK = 0, MESH_SHELL = 1 };
+// mesh kinds: affine brick, stacked cubed shell (curvilinear, per-node
+// metrics), or a mesh given by the reference's grid arrays (per-node metrics,
+// reference state and facing nodes)
+enum { MESH_BRICK = 0, MESH_SHELL = 1, MESH_ARRAYS = 2 };
 
 // per-node geometry of a curvilinear mesh, (Np, CG_NFIELDS, nelem) on the host
 enum CurvGeoField {
@@ -127,6 +129,9 @@ struct Mesh {
     // orientation codes (4 bits per face: neighbour face 0..3, bit 2 = the
     // in-face horizontal index runs reversed)
     std::vector<double> xyz, cgeo;
+    // grid-arrays meshes: the facing node of every face node, (Nfp, 6, nelem)
+    std::vector<int> fpart;
+    int* d_fpart = nullptr;
     // device copies
     double* d_emetric = nullptr;
     float* d_emetric32 = nullptr;
@@ -182,6 +187,11 @@ struct Model {
     float* d_glap_ref = nullptr;
     void* d_nu4 = nullptr;           // cubed shell: nu_4 per node, (Np, nelem), model precision
     float* d_hglap_ref = nullptr;    // cubed shell, mixed: nu_4 grad lap h_ref per node, (Np, 3, nelem)
+    // grid-arrays meshes: per-node kernel geometry on the host, per-node p_ref,
+    // FP64-computed reference jumps (rho, rhoe) per face node, reference set?
+    std::vector<double> arrays_geo, pref64;
+    float* d_fjump = nullptr;
+    bool has_reference = false;
     int grid_ctas = -1;              // stage-kernel grid: -1 = one CTA per element (the measured best
                                      // on GB300), 0 = one wave of resident CTAs, n > 0 = n CTAs
     int kernel_kind = 0;             // KERNEL_NODE or KERNEL_COLUMN
@@ -190,6 +200,9 @@ struct Model {
 // host-side setup (mesh.cpp, shell_mesh.cpp)
 int build_brick(const cmdg_brick_desc* desc, Mesh* m);
 int build_shell(const cmdg_shell_desc* desc, Mesh* m);
+int build_arrays(const cmdg_grid_arrays* desc, Mesh* m);
+int init_arrays_tables(Model* md);
+int set_arrays_reference(Model* md, const double* aux7);
 void lgl_derivative(Mesh* m);
 int init_shell_tables(Model* md);
 // virtual temperature and pressure of the reference profile at height z
@@ -212,6 +225,8 @@ struct LaunchArgs {
 int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
 // curvilinear stage kernel (shell.cu)
 int launch_shell_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
+// grid-arrays stage kernel (arrays.cu)
+int launch_arrays_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
 // LSRK54CarpenterKennedy A and B coefficient arrays (5 entries each)
 void lsrk54_coefficients(const double** A, const double** B);
 

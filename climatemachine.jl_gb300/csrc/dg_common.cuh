@@ -55,6 +55,10 @@ struct KParams {
     const void* nu4;
     const float* hglap_ref32;
     int hyper_horizontal;  // 1: the passes run in the horizontal directions only (HorizontalDirection)
+    // grid-arrays meshes: facing node of each face node (Nfp, 6, nelem) and
+    // the FP64-computed reference jumps (rho, rhoe) per face node
+    const int* fpart;
+    const float* fjump;
 };
 
 // A run of consecutive elements [e0, e1) of ensemble member `member`, of

@@ -209,7 +209,8 @@ int init_model_tables(Model* md) {
     std::vector<double> phi(nlev);
     for (int lev = 0; lev < nlev; ++lev) phi[lev] = L(lev, LV_PHI);
     for (int lev = 0; lev < nlev; ++lev) L(lev, LV_GPHIZ) = ddz(phi, lev);
-    if (p.ref_state) {
+    // (a mesh from grid arrays takes its reference state per node from the caller)
+    if (p.ref_state && m.kind != MESH_ARRAYS) {
         CMDG_ARG_CHECK(p.orientation == CMDG_ORIENT_FLAT || p.orientation == CMDG_ORIENT_SPHERE,
                        "a hydrostatic reference state needs an orientation");
         for (int lev = 0; lev < nlev; ++lev) {

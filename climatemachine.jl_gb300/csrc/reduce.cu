@@ -131,9 +131,11 @@ __global__ void weighted_sum_kernel(const void* Qv, int field, const double* eme
 
 // max over nodes of (|u| + c) / dx_min with dx_min the distance to the
 // nearest neighbouring node of the same element along xi1, xi2 or xi3.
+// geo (grid-arrays meshes): per-node kernel geometry whose KG_DCRHO plane holds
+// the node's pressure coefficient; otherwise the level row's
 __global__ void courant_kernel(const double* __restrict__ Q, const double* emetric, const double* xi, const double* lvl,
                                Physics ph, int64_t nelem, int Np, int Nq, int nz, const double* dxmin,
-                               double* partial) {
+                               const double* geo, double* partial) {
     const int Nfp = Nq * Nq;
     double best = 0.0;
     const int64_t total = nelem * Np;
@@ -159,7 +161,8 @@ __global__ void courant_kernel(const double* __restrict__ Q, const double* emetr
         const double rinv = 1.0 / q[0];
         const double u0 = q[1] * rinv, u1 = q[2] * rinv, u2 = q[3] * rinv;
         const double ke2 = q[1] * u0 + q[2] * u1 + q[3] * u2;
-        const double p = ph.gm1 * (q[4] - 0.5 * ke2) + q[0] * L[LV_CRHO];
+        const double crho = geo ? geo[((size_t)e * KG_NFIELDS + KG_DCRHO) * Np + node] : L[LV_CRHO];
+        const double p = ph.gm1 * (q[4] - 0.5 * ke2) + q[0] * crho;
         const double c = sqrt(ph.gamma * p * rinv);
         best = fmax(best, (sqrt(u0 * u0 + u1 * u1 + u2 * u2) + c) / md);
     }
@@ -279,7 +282,8 @@ int courant_dt(Model* md, const double* Q, double CFL, double* dt, cudaStream_t 
     if ((rc = quad(md, dq))) return rc;
     const Mesh& m = *md->mesh;
     courant_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(Q, m.d_emetric, dq.xi, md->d_lvl64, md->ph, m.nelem, m.Np, m.Nq,
-                                                     m.nz, md->d_dxmin, md->d_red);
+                                                     m.nz, md->d_dxmin,
+                                                     m.kind == MESH_ARRAYS ? md->d_geo64 : nullptr, md->d_red);
     CMDG_CUDA_CHECK(cudaGetLastError());
     std::vector<double> h(RED_BLOCKS);
     CMDG_CUDA_CHECK(cudaMemcpyAsync(h.data(), md->d_red, sizeof(double) * RED_BLOCKS, cudaMemcpyDeviceToHost, s));

@@ -596,6 +596,8 @@ KParams make_params(Model* md, const LaunchArgs& a) {
     P.inv_tau_hyper32 = (float)P.inv_tau_hyper;
     P.nu4 = md->d_nu4;
     P.hyper_horizontal = md->prm.hyper_direction == CMDG_DIR_HORIZONTAL;
+    P.fpart = m.d_fpart;
+    P.fjump = md->d_fjump;
     P.hglap_ref32 = md->d_hglap_ref;
     return P;
 }
@@ -603,6 +605,14 @@ KParams make_params(Model* md, const LaunchArgs& a) {
 int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
     const Mesh& m = *md->mesh;
     if (m.kind == MESH_SHELL) return launch_shell_stage(md, a, s);
+    if (m.kind == MESH_ARRAYS) {
+        const cmdg_atmos_params& p = md->prm;
+        if (!md->has_reference && (p.orientation != CMDG_ORIENT_NONE || p.gravity || p.ref_state)) {
+            set_error("a model on a grid-arrays mesh needs cmdg_model_set_reference before its first tendency");
+            return CMDG_ERR_STATE;
+        }
+        return launch_arrays_stage(md, a, s);
+    }
     if (md->prm.hyperdiffusion != CMDG_HYPER_NONE) return launch_hyper_stage(md, a, s);
     if (md->prm.turbulence != CMDG_TURB_NONE) return launch_viscous_stage(md, a, s);
     const KParams P = make_params(md, a);

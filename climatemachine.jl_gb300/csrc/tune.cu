@@ -67,7 +67,7 @@ extern "C" int cmdg_model_autotune(cmdg_model* model, int reps, double* h_ms, in
     const int saved_kind = md->kernel_kind, saved_grid = md->grid_ctas;
     std::vector<Candidate> cands = {{KERNEL_NODE, 0}, {KERNEL_NODE, -1}};
     // one kernel family for viscous models and for curvilinear meshes
-    if (md->prm.turbulence != CMDG_TURB_NONE || md->prm.hyperdiffusion != CMDG_HYPER_NONE || m.kind == MESH_SHELL)
+    if (md->prm.turbulence != CMDG_TURB_NONE || md->prm.hyperdiffusion != CMDG_HYPER_NONE || m.kind != MESH_BRICK)
         cands = {{KERNEL_NODE, -1}};
     else if (mixed && m.N >= 3 && m.N <= 5) cands.push_back({KERNEL_COLUMN, 0});
     std::vector<double> ms(cands.size(), 0.0);

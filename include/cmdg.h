@@ -125,6 +125,26 @@ int cmdg_mesh_create_brick(const cmdg_brick_desc* desc, cmdg_mesh** out);
  * (src/Numerics/Mesh/Topologies.jl:1067-1305,1620-1760;
  * src/Numerics/Mesh/Grids.jl:1028-1110; src/Numerics/Mesh/Metrics.jl:431-724). */
 int cmdg_mesh_create_shell(const cmdg_shell_desc* desc, cmdg_mesh** out);
+
+/* A mesh from the reference's own grid arrays (a DiscontinuousSpectralElementGrid
+ * of any topology: warped bricks, cubed shells, ...), host arrays in Julia's
+ * column-major layout:
+ *   vgeo       (Np, 16, nelem) FP64: xi1x1, xi2x1, xi3x1, xi1x2, ..., xi3x3,
+ *              M, MI, MH, x1, x2, x3, JcV (src/Numerics/Mesh/Grids.jl:76-125);
+ *   vmap_plus  (Nfp, 6, nelem) 1-based global node index of the node facing
+ *              each face node (Grids.jl:559-638; the face nodes are numbered
+ *              by the reference's face masks, Grids.jl:580-597);
+ *   elemtobndy (6, nelem) 0 on interior faces, the boundary tag (> 0) on
+ *              walls (FreeSlip + Insulating).
+ * Faces must be conforming (every node of a face faces one element). */
+typedef struct {
+    int N;                      /* polynomial order, 2..5 */
+    int64_t nelem;
+    const double* vgeo;
+    const int64_t* vmap_plus;
+    const int64_t* elemtobndy;
+} cmdg_grid_arrays;
+int cmdg_mesh_create_arrays(const cmdg_grid_arrays* desc, cmdg_mesh** out);
 int cmdg_mesh_destroy(cmdg_mesh* mesh);
 /* Sizes of a mesh. */
 int cmdg_mesh_info(const cmdg_mesh* mesh, int64_t* nelem, int* Np);
@@ -142,6 +162,15 @@ int cmdg_mesh_mass(const cmdg_mesh* mesh, double* h_M);
  * src/Atmos/Model/ref_state.jl:143-263). */
 int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* params, int precision, cmdg_model** out);
 int cmdg_model_destroy(cmdg_model* model);
+/* Geopotential and reference state of a model on a mesh from grid arrays,
+ * host (Np, 7, nelem) FP64: Phi, dPhi/dx1, dPhi/dx2, dPhi/dx3, rho_ref,
+ * rhoe_ref, p_ref -- the reference's aux.orientation.Phi, aux.orientation.gradPhi
+ * and aux.ref_state.(rho, rhoe, p) (src/Common/Orientations/Orientations.jl:57-136,
+ * src/Atmos/Model/ref_state.jl:66-67).  Required before the first tendency
+ * of such a model whose orientation, gravity or reference state uses them;
+ * may be called again to replace them. */
+int cmdg_model_set_reference(cmdg_model* model, const double* h_aux7);
+
 /* Reference state at the nodes into host memory, (Np, 3, nelem):
  * rho_ref, rhoe_ref, p_ref (aux.ref_state, src/Atmos/Model/ref_state.jl:66-67). */
 int cmdg_model_reference_state(const cmdg_model* model, double* h_ref);

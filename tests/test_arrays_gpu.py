@@ -1,0 +1,142 @@
+"""Meshes given by the reference's own grid arrays (cmdg_mesh_create_arrays
++ cmdg_model_set_reference): the oracle's vgeo, vmap+ and elemtobndy -- in
+the layouts of src/Numerics/Mesh/Grids.jl:76-125, 559-638 -- and its aux
+values (Phi, grad Phi, rho_ref, rhoe_ref, p_ref) feed the GPU model, which
+then reproduces the oracle's tendency and steps on a periodic brick, a
+walled brick with gravity and a hydrostatic reference state, and the cubed
+shell (arbitrary face orientations through the facing-node table).
+
+Bounds as in the other parity tests: FP64 <= 1e-10 (bricks) / 1e-9 (shell)
+of the field scale; mixed precision <= 1e-4 for one tendency and <= 1e-5
+relative L2 after steps."""
+import numpy as np
+import pytest
+import torch
+
+import cmdg
+import oracle as O
+from cmdg import workloads
+
+pytestmark = pytest.mark.gpu
+
+R = O.EARTH["planet_radius"]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import __graft_entry__ as g
+
+    g.build()
+    torch.cuda.set_device(0)
+
+
+def aux7(om):
+    a = om.aux
+    A = O.AUX
+    return np.stack([a[:, A["Phi"]], a[:, A["gPhi"]], a[:, A["gPhi"] + 1], a[:, A["gPhi"] + 2], a[:, A["rho_ref"]],
+                     a[:, A["rhoe_ref"]], a[:, A["p_ref"]]], axis=1)
+
+
+def arrays_model(om, N, model, numflux="rusanov", precision="fp64", set_ref=True):
+    grid = cmdg.ArraysGrid(N, om.vgeo, om.vmapP + 1, om.elemtobndy)
+    dg = cmdg.DGModel(model, grid, numerical_flux=numflux, precision=precision)
+    if set_ref:
+        dg.set_reference(aux7(om))
+    return dg
+
+
+def rel_max(got, ref):
+    out = []
+    for s in range(5):
+        sl = slice(1, 4) if 1 <= s <= 3 else slice(s, s + 1)
+        out.append(np.abs(got[:, s] - ref[:, s]).max() / np.abs(ref[:, sl]).max())
+    return np.array(out)
+
+
+def cases(kind, N, precision="fp64"):
+    if kind == "vortex":
+        L = 1 / 20
+        om = O.OracleModel(N, (3, 2, 4), (-L,) * 3, (L,) * 3, periodic=(1, 1, 1))
+        Q0 = om.init_vortex(0.0)
+        return om, arrays_model(om, N, cmdg.AtmosModel(), precision=precision, set_ref=False), Q0, 1e-10
+    if kind == "bubble":
+        Lb = 2500.0
+        om = O.OracleModel(N, (3, 2, 4), (0, 0, 0), (Lb, Lb, Lb), periodic=(1, 1, 0), orientation="flat",
+                           gravity=True, ref_state=True, profile="dry_adiabatic", T_surface=300.0, T_min=0.0)
+        model = cmdg.AtmosModel(orientation="flat", gravity=True,
+                                ref_state=cmdg.HydrostaticState(cmdg.DryAdiabaticProfile(300.0, 0.0)))
+        Q0 = om.init_bubble(rc=900.0, xc=1100.0, yc=1300.0, zc=800.0)
+        Q0[:, 1:4] += np.random.default_rng(11).uniform(-2, 2, size=Q0[:, 1:4].shape)
+        return om, arrays_model(om, N, model, precision=precision), Q0, 1e-10
+    om = O.OracleModel(N, shell=dict(nhorz=2, nvert=3, r_inner=R, r_outer=R + 30e3), orientation="sphere",
+                       gravity=True, ref_state=True, profile="isothermal", T_surface=285.0)
+    model = cmdg.AtmosModel(orientation="sphere", gravity=True,
+                            ref_state=cmdg.HydrostaticState(cmdg.IsothermalProfile(285.0)))
+    Q0 = workloads.gcm_initial_state(om.aux[:, 0:3], seed=5)
+    Q0[:, 1:4] += np.random.default_rng(3).uniform(-0.5, 0.5, size=Q0[:, 1:4].shape)
+    return om, arrays_model(om, N, model, precision=precision), Q0, 1e-9
+
+
+@pytest.mark.parametrize("N", [3, 4])
+@pytest.mark.parametrize("kind", ["vortex", "bubble", "shell"])
+def test_fp64_tendency_on_grid_arrays_matches_oracle(kind, N):
+    om, dg, Q0, tol = cases(kind, N)
+    ref = om.tendency(Q0)
+    dQ = dg.new_state(torch.float64)
+    dg(dQ, dg.init_ode_state(Q0), None, 0.0)
+    err = rel_max(dQ.cpu().numpy(), ref)
+    assert (err < tol).all(), err
+    assert np.allclose(dg.grid.coordinates(), om.aux[:, 0:3], rtol=0, atol=1e-9 * np.abs(om.aux[:, 0:3]).max())
+
+
+@pytest.mark.parametrize("kind", ["bubble", "shell"])
+def test_fp64_steps_on_grid_arrays_match_oracle(kind):
+    om, dg, Q0, tol = cases(kind, 4)
+    dt = 0.5 * om.courant_dt(Q0, 0.4)
+    assert dg.courant_dt(dg.init_ode_state(Q0), 0.4) == pytest.approx(om.courant_dt(Q0, 0.4), rel=1e-12)
+    Qo, _ = om.lsrk54(Q0.copy(), dt, 5)
+    Q = dg.init_ode_state(Q0)
+    cmdg.dostep_(Q, cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt), None, 0.0, nsteps=5)
+    err = rel_max(Q.cpu().numpy(), Qo)
+    assert (err < tol).all(), err
+
+
+@pytest.mark.parametrize("kind", ["bubble", "shell"])
+def test_mixed_on_grid_arrays_close_to_fp64_oracle(kind):
+    om, dg, Q0, _ = cases(kind, 4, precision="mixed")
+    ref = om.tendency(Q0)
+    Qp = dg.init_ode_state(Q0)
+    dQ = dg.new_state(torch.float64)
+    dg(dQ, Qp, None, 0.0)
+    got = dQ.cpu().numpy()
+    errs = [np.linalg.norm(got[:, sl] - ref[:, sl]) / np.linalg.norm(ref[:, sl])
+            for sl in (slice(0, 1), slice(1, 4), slice(4, 5))]
+    assert max(errs) < 1e-4, errs
+    dt = om.courant_dt(Q0, 0.4)
+    Qo, _ = om.lsrk54(Q0.copy(), dt, 30)
+    cmdg.dostep_(Qp, cmdg.LSRK54CarpenterKennedy(dg, Qp, dt=dt), None, 0.0, nsteps=30)
+    err, refn = om.field_l2(dg.from_perturbation(Qp).cpu().numpy(), Qo)
+    err = np.array([err[0], np.sqrt(np.sum(err[1:4] ** 2)), err[4]])
+    refn = np.array([refn[0], np.sqrt(np.sum(refn[1:4] ** 2)), refn[4]])
+    assert (err / refn < 1e-5).all(), err / refn
+    assert dg.status_word() == 0
+
+
+def test_grid_arrays_errors():
+    om, dg, Q0, _ = cases("bubble", 3)
+    grid = cmdg.ArraysGrid(3, om.vgeo, om.vmapP + 1, om.elemtobndy)
+    model = cmdg.AtmosModel(orientation="flat", gravity=True,
+                            ref_state=cmdg.HydrostaticState(cmdg.DryAdiabaticProfile(300.0, 0.0)))
+    dg2 = cmdg.DGModel(model, grid)
+    dQ = dg2.new_state(torch.float64)
+    with pytest.raises(cmdg.CmdgError, match="set_reference"):
+        dg2(dQ, dg2.init_ode_state(Q0), None, 0.0)
+    bad = om.vmapP + 1
+    e_int = int(np.nonzero((om.elemtobndy == 0).all(axis=1))[0][0])
+    bad[e_int, 0, 3] = bad[e_int, 1, 3]  # one node of face 1 faces another element
+    with pytest.raises(cmdg.CmdgError, match="different elements"):
+        cmdg.ArraysGrid(3, om.vgeo, bad, om.elemtobndy)
+    bad2 = om.vmapP + 1
+    bad2[0, 0, 0] = 10**12
+    with pytest.raises(cmdg.CmdgError, match="out of range"):
+        cmdg.ArraysGrid(3, om.vgeo, bad2, om.elemtobndy)
