@@ -11,11 +11,15 @@
 // links, loads or calls this file.
 //
 // Parity status: pinned.  The isentropic-vortex golden errors of
-// test/Numerics/DGMethods/Euler/isentropicvortex.jl:105-106, the LSRK54
-// convergence order of test/Numerics/ODESolvers/ode_tests_convergence.jl:41
-// and the discrete hydrostatic balance of
-// test/Atmos/Model/discrete_hydrostatic_balance.jl (LES brick and GCM cubed
-// shell) are reproduced by tests/test_oracle_pins.py.
+// test/Numerics/DGMethods/Euler/isentropicvortex.jl:105-106, the
+// manufactured-solution Navier-Stokes golden error of
+// test/Numerics/DGMethods/compressible_Navier_Stokes/mms_bc_atmos.jl:232-235
+// (viscous path, warped brick), the 3D hyperdiffusion golden errors of
+// test/Numerics/DGMethods/advection_diffusion/periodic_3D_hyperdiffusion.jl,
+// the LSRK54 convergence order of
+// test/Numerics/ODESolvers/ode_tests_convergence.jl:41 and the discrete
+// hydrostatic balance of test/Atmos/Model/discrete_hydrostatic_balance.jl
+// (LES brick and GCM cubed shell) are reproduced by tests/test_oracle_pins.py.
 //
 // Every function cites the reference file:line (paths relative to the
 // ClimateMachine.jl project root) whose algorithm it restates.  Third-party
@@ -59,6 +63,8 @@ typedef struct {
     double lo[3], hi[3];      // domain extents
     int periodic[3];          // 1 = periodic in that direction
     int bc_lo[3], bc_hi[3];   // boundary tags for non-periodic faces (>0)
+    int warp;                 // 0 = none; 1 = the 3D mesh warp of test/Numerics/DGMethods/
+                              // compressible_Navier_Stokes/mms_bc_atmos.jl:268-276
 } om_brick;
 
 typedef struct {
@@ -82,6 +88,9 @@ typedef struct {
     double tau_hyper;   // DryBiharmonic.tau_timescale
     int hyper_direction;// DGModel diffusion_direction of the hyperdiffusion passes:
                         // 0 = EveryDirection, 1 = HorizontalDirection (SpaceDiscretization.jl:731-1083)
+    int mms;            // 1 = the manufactured-solution AtmosModel of mms_bc_atmos.jl: source terms
+                        // and InitStateBC wall states supplied per node (om_set_mms), and
+                        // total_specific_enthalpy overridden to zero (mms_bc_atmos.jl:45-48)
 } om_params;
 
 // StackedCubedSphereTopology (Topologies.jl:1620-1760) over a
@@ -127,6 +136,8 @@ struct Model {
     // of the laplacians; Qhypervisc_div (Np, 4, nelem) the laplacians
     std::vector<double> hgrad, hdiv;
     int ngl = 4;                             // GradientLaplacian states per node
+    const double* mms_src = nullptr;         // mms: source terms at the nodes, (Np, 5, nelem)
+    const double* mms_exact = nullptr;       // mms: InitStateBC state at the nodes, (Np, 5, nelem)
     int law = 0;                             // 0 = AtmosModel, 1 = scalar constant-tensor hyperdiffusion
     double Hten[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // law 1: tensor H, column-major
 };
@@ -381,6 +392,14 @@ void element_geometry(Model& m, int64_t e, const double c[3][8], void (*warp)(do
 }
 
 
+// The 3D mesh warp of mms_bc_atmos.jl:268-276.
+void mms_warp(double& x1, double& x2, double& x3) {
+    const double a = x1, b = x2, c = x3;
+    x1 = a + (a - 0.5) * std::cos(2 * M_PI * b * c) / 4;
+    x2 = b + std::exp(std::sin(2 * M_PI * (a * b + c))) / 20;
+    x3 = c + a / 4 + b * b / 2 + std::sin(a * b * c);
+}
+
 void build_geometry(Model& m) {
     const om_brick& b = m.mesh;
     int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp;
@@ -441,7 +460,7 @@ void build_geometry(Model& m) {
             c[1][v] = xg[1][iy + bj];
             c[2][v] = xg[2][iz + bk];
         }
-        element_geometry(m, e, c, nullptr);
+        element_geometry(m, e, c, b.warp == 1 ? mms_warp : nullptr);
     }
 }
 
@@ -923,7 +942,7 @@ void gradient_argument(const om_params& p, const double q[NS], double Phi, doubl
     G[0] = rinv * q[1]; G[1] = rinv * q[2]; G[2] = rinv * q[3];
     Thermo t = phase_dry(p, q[0], q[4], q + 1, Phi);
     double e_tot = q[4] * (1 / q[0]);
-    G[3] = e_tot + p.R_d * t.T;
+    G[3] = p.mms ? 0.0 : e_tot + p.R_d * t.T;  // mms: total_specific_enthalpy := 0
     G[4] = thv;
 }
 
@@ -1032,7 +1051,8 @@ void gradient_pass(Model& m, const double* Q) {
                     for (int d = 0; d < 3; ++d)
                         for (int s = 0; s < ng; ++s) Gs[d][s] = nv[d] * (GP[s] + GM[s]) / 2;
                 } else {
-                    bc_state_grad(qM, nv, qP);
+                    if (p.mms) load_q(m, m.mms_exact, e, vM, qP);  // InitStateBC (bc_initstate.jl:12-26)
+                    else bc_state_grad(qM, nv, qP);
                     // boundary_state! refreshes aux+ (theta_v) from state+
                     Thermo t = phase_dry(p, qP[0], qP[4], qP + 1, aM.Phi);
                     double thvP = virtual_pottemp(p, t.T, t.p);
@@ -1350,6 +1370,7 @@ void face_flux(const Model& m, const double* Q, int64_t e, int f, int n, double 
     NodeAux aM = node_aux(m, e, vM);
     NodeAux aP = node_aux(m, eP, vP);
     if (tag == 0) load_q(m, Q, eP, vP, qP);
+    else if (p.mms) load_q(m, m.mms_exact, e, vM, qP);  // InitStateBC (bc_initstate.jl:12-26)
     else bc_state_first(qM, nv, qP);
     for (int s = 0; s < NS; ++s) fl[s] = 0;
     double FM[3][NS], FP[3][NS];
@@ -1385,6 +1406,17 @@ void face_flux(const Model& m, const double* Q, int64_t e, int f, int n, double 
         for (int s = 0; s < NS; ++s) {
             double acc = 0;
             for (int d = 0; d < 3; ++d) acc += (FM[d][s] + FP[d][s]) * (nv[d] / 2);
+            fl[s] += acc;
+        }
+    } else if (p.mms && p.turbulence != 0 && tag != 0) {
+        // InitStateBC second order: the one-sided flux of the boundary state
+        // with the interior gradient flux (NumericalFluxes.jl:872-966)
+        double gfM[10] = {0};
+        for (int s = 0; s < ngf; ++s) gfM[s] = m.gradflux[(e * ngf + s) * Np + vM];
+        flux_second_order(m, qP, gfM, aM, FP, nullptr);
+        for (int s = 0; s < NS; ++s) {
+            double acc = 0;
+            for (int d = 0; d < 3; ++d) acc += FP[d][s] * nv[d];
             fl[s] += acc;
         }
     }
@@ -1424,6 +1456,8 @@ void tendency(Model& m, double* T, const double* Q, double t, double alpha, doub
                 F3[n * NS + s] = M * (VGc(m, e, XI3X1, n) * F[0][s] + VGc(m, e, XI3X2, n) * F[1][s] + VGc(m, e, XI3X3, n) * F[2][s]);
             }
             source(p, q, a, &Src[n * NS]);
+            if (p.mms)  // MMSSource (mms_bc_atmos.jl:60-80)
+                for (int s = 0; s < NS; ++s) Src[n * NS + s] += m.mms_src[(e * NS + s) * Np + n];
         }
         for (int k = 0; k < Nq; ++k)
             for (int j = 0; j < Nq; ++j)
@@ -1628,6 +1662,13 @@ void om_tendency(om_model* m, double* dQ, const double* Q, double t, double alph
 void om_gradient_pass(om_model* m, const double* Q) {
     update_aux(*m, Q);
     gradient_pass(*m, Q);
+}
+
+// Manufactured-solution inputs of the next tendency (Np, 5, nelem): source
+// terms and the InitStateBC state at the nodes, at the tendency's time.
+void om_set_mms(om_model* m, const double* src, const double* exact) {
+    m->mms_src = src;
+    m->mms_exact = exact;
 }
 
 // Hyperdiffusion passes only: afterwards om_hyper_grad holds nu grad^3

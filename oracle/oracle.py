@@ -47,6 +47,7 @@ class Brick(ctypes.Structure):
         ("periodic", ctypes.c_int * 3),
         ("bc_lo", ctypes.c_int * 3),
         ("bc_hi", ctypes.c_int * 3),
+        ("warp", ctypes.c_int),
     ]
 
 
@@ -75,6 +76,7 @@ class Params(ctypes.Structure):
         ("hyperdiffusion", ctypes.c_int),
         ("tau_hyper", ctypes.c_double),
         ("hyper_direction", ctypes.c_int),
+        ("mms", ctypes.c_int),
     ]
 
 
@@ -130,6 +132,7 @@ def lib():
         L.om_tendency.argtypes = [P, dp, dp, D, D, D]
         L.om_gradient_pass.argtypes = [P, dp]
         L.om_hyper_pass.argtypes = [P, dp]
+        L.om_set_mms.argtypes = [P, dp, dp]
         for name in ("om_hyper_grad", "om_hyper_div"):
             getattr(L, name).restype = dp
             getattr(L, name).argtypes = [P]
@@ -208,6 +211,7 @@ class OracleModel:
         p.hyperdiffusion = {"none": 0, "dry_biharmonic": 1}[physics.get("hyperdiffusion", "none")]
         p.tau_hyper = physics.get("tau_hyper", 0.0)
         p.hyper_direction = {"every": 0, "horizontal": 1}[physics.get("hyper_direction", "every")]
+        p.mms = int(physics.get("mms", False))
         self.params, self.consts = p, consts
         self.L = lib()
         if shell is None:
@@ -220,6 +224,7 @@ class OracleModel:
                 b.periodic[d] = int(periodic[d])
                 b.bc_lo[d] = bc_lo[d]
                 b.bc_hi[d] = bc_hi[d]
+            b.warp = int(physics.get("warp", 0))
             self.brick = b
             self.h = self.L.om_create(ctypes.byref(b), ctypes.byref(p))
         else:
@@ -304,6 +309,12 @@ class OracleModel:
     def gradient_pass(self, Q):
         self.L.om_gradient_pass(self.h, _ptr(Q))
         return self.gradflux
+
+    def set_mms(self, src, exact):
+        """Source terms and InitStateBC state (nelem, 5, Np) for the next
+        tendency of an mms model; the arrays must stay alive until then."""
+        self._mms = (np.ascontiguousarray(src, dtype=np.float64), np.ascontiguousarray(exact, dtype=np.float64))
+        self.L.om_set_mms(self.h, _ptr(self._mms[0]), _ptr(self._mms[1]))
 
     def hyper_pass(self, Q):
         """Hyperdiffusion passes of Q: returns (nu grad^3 (nelem, 12, Np),

@@ -11,6 +11,12 @@ Pins (reference paths relative to the ClimateMachine.jl project root):
     the LES brick and on the GCM stacked cubed shell (3 x 3 horizontal
     elements per panel, 3 vertical, 50 km, N=4, IsothermalProfile,
     subtract_off = false, 100 s of LSRK54 at Courant 0.1)
+  * compressible Navier-Stokes manufactured solution, 3D, N=4, 4^3 elements
+    of a warped (curvilinear) brick with InitStateBC walls,
+    ConstantDynamicViscosity(1/100, WithDivergence), level 1 —
+    test/Numerics/DGMethods/compressible_Navier_Stokes/mms_bc_atmos.jl:232-235
+    (source terms derived here with sympy from the manufactured solution of
+    mms_solution.jl:17-95)
   * constant-tensor scalar hyperdiffusion, 3D, EveryDirection and
     HorizontalDirection, N=4, levels 1 and 2 — test/Numerics/DGMethods/
     advection_diffusion/periodic_3D_hyperdiffusion.jl:229-235 (the
@@ -230,3 +236,73 @@ def test_dry_biharmonic_acts_on_horizontal_velocity():
         assert np.abs(d[:, 3]).max() <= 1e-3 * np.abs(d[:, 1]).max()
         assert np.abs(d[:, 0]).max() == 0.0
     assert math.log2(errs[0] / errs[1]) > 0.8
+
+
+def mms_functions(gamma, mu):
+    """The manufactured solution of
+    test/Numerics/DGMethods/compressible_Navier_Stokes/mms_solution.jl
+    (3D): the state q = (rho, U, V, W, E) and the source dq/dt + div F(q)
+    of the compressible Navier-Stokes flux with p = (gamma - 1)(E - |U|^2 /
+    (2 rho)) and tau = 2 mu (eps - tr(eps) I / 3), derived symbolically."""
+    sp = pytest.importorskip("sympy")
+    x, y, z, t = sp.symbols("x y z t", real=True)
+    c = sp.cos(sp.pi * t)
+    shape = sp.sin(sp.pi * x) * sp.cos(sp.pi * y)
+    rho = c * shape * sp.cos(sp.pi * z) + 3
+    U = c * rho * shape * sp.cos(sp.pi * z)
+    V = c * rho * shape * sp.cos(sp.pi * z)
+    W = c * rho * shape * sp.sin(sp.pi * z)
+    E = c * shape * sp.cos(sp.pi * z) + 100
+    P = (gamma - 1) * (E - (U**2 + V**2 + W**2) / (2 * rho))
+    X, mom = (x, y, z), (U, V, W)
+    vel = tuple(m / rho for m in mom)
+    grad = [[sp.diff(vel[i], X[j]) for j in range(3)] for i in range(3)]
+    eps = [[(grad[i][j] + grad[j][i]) / 2 for j in range(3)] for i in range(3)]
+    tr = eps[0][0] + eps[1][1] + eps[2][2]
+    tau = [[2 * mu * (eps[i][j] - (tr / 3 if i == j else 0)) for j in range(3)] for i in range(3)]
+    flux = [[mom[d]] + [vel[d] * mom[i] + (P if i == d else 0) - tau[d][i] for i in range(3)]
+            + [vel[d] * (E + P) - sum(vel[i] * tau[d][i] for i in range(3))] for d in range(3)]
+    q = (rho, U, V, W, E)
+    src = [sp.diff(q[s], t) + sum(sp.diff(flux[d][s], X[d]) for d in range(3)) for s in range(5)]
+    return (sp.lambdify((t, x, y, z), q, modules="numpy", cse=True),
+            sp.lambdify((t, x, y, z), src, modules="numpy", cse=True))
+
+
+def test_mms_navier_stokes_golden():
+    """mms_bc_atmos.jl, 3D, level 1: 800 LSRK54 steps to t = 1 on the warped
+    [0, 1]^3 brick with the exact solution as the wall state (InitStateBC for
+    the first-order, gradient and second-order fluxes), T_0 = 0 and
+    total_specific_enthalpy = 0 as the test overrides them; the weighted L2
+    distance to the exact solution matches the reference's golden value."""
+    from fractions import Fraction as Fr
+
+    c = O.EARTH
+    fq, fs = mms_functions(c["cp_d"] / c["cv_d"], Fr(1, 100))
+    om = O.OracleModel(4, (4, 4, 4), (0, 0, 0), (1, 1, 1), periodic=(0, 0, 0), bc_lo=(1, 1, 1), bc_hi=(1, 1, 1),
+                       warp=1, mms=True, T_0=0.0, turbulence="constant", rho_nu=0.01, with_divergence=True)
+    X = [om.aux[:, O.AUX[k]] for k in ("x", "y", "z")]
+
+    def ev(f, tt):
+        return np.stack([np.broadcast_to(v, X[0].shape) for v in f(tt, *X)], axis=1).astype(np.float64)
+
+    A = [float(Fr(a)) for a in (0, Fr(-567301805773, 1357537059087), Fr(-2404267990393, 2016746695238),
+                                  Fr(-3550918686646, 2091501179385), Fr(-1275806237668, 842570457699))]
+    B = [float(b) for b in (Fr(1432997174477, 9575080441755), Fr(5161836677717, 13612068292357),
+                            Fr(1720146321549, 2090206949498), Fr(3134564353537, 4481467310338),
+                            Fr(2277821191437, 14882151754819))]
+    C = [float(x) for x in (Fr(0), Fr(1432997174477, 9575080441755), Fr(2526269341429, 6820363962896),
+                            Fr(2006345519317, 3224310063776), Fr(2802321613138, 2924317926251))]
+    nsteps = math.ceil(1 / (5e-3 / 4))
+    dt = 1 / nsteps
+    Q = ev(fq, 0.0).copy()
+    dQ = np.zeros_like(Q)
+    for step in range(nsteps):
+        t0 = step * dt
+        for s in range(5):
+            ts = t0 + C[s] * dt
+            om.set_mms(ev(fs, ts), ev(fq, ts))
+            om.tendency(Q, t=ts, alpha=1.0, beta=1.0, dQ=dQ)
+            Q += B[s] * dt * dQ
+            dQ *= A[(s + 1) % 5]
+    err = om.euclidean_distance(Q, ev(fq, 1.0))
+    assert err == pytest.approx(3.3983777728925593e-02, rel=1e-10)
