@@ -84,7 +84,8 @@ WORKLOADS = {
     "les": dict(desc="SmagorinskyLilly LES: 32x32x16 elements, N=4 (2,048,000 nodes), 3200x3200x1600 m, periodic "
                      "x/y, walls z, N_bv=0.01 1/s, seeded k^-5/3 velocity rms 1 m/s, Rusanov, LSRK54 at CFL 0.4",
                 bytes_mixed=200, bytes_fp64=320, launches_per_stage=2,
-                kernel="viscous_stage_kernel<4,float,mixed,stage,smagorinsky>", profile="none"),
+                kernel="gradient_kernel + viscous_stage_kernel<4,float,mixed,stage,smagorinsky>",
+                profile="viscous_stage_kernel_mixed_les.md"),
     # per node-stage: stage kernel 120 + nu grad^3 read 36; gradient pass 20 + 36; laplacian 36 + 12;
     # gradient of the laplacian 12 + 36 (FP32 words; FP64 doubles all but the RK register's 80)
     "hyper": dict(desc="rising bubble of the default workload with DryBiharmonic(tau = 3600 s) hyperdiffusion: "
