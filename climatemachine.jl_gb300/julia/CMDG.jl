@@ -15,6 +15,7 @@ module CMDG
 
 using CUDA
 using ClimateMachine.ODESolvers: LowStorageRungeKutta2N, AbstractODESolver
+using ClimateMachine.Mesh.Grids: polynomialorders
 import ClimateMachine.ODESolvers: dostep!
 import ClimateMachine.DGMethods: SpaceDiscretization
 
@@ -90,6 +91,49 @@ function CMDGModel(brick::Brick, params::AtmosParams, grid, balance_law, state_a
         ccall((:cmdg_mesh_destroy, libcmdg), Cint, (Ptr{Cvoid},), x.mesh)
     end
     return dg
+end
+
+struct GridArrays
+    N::Cint
+    nelem::Int64
+    vgeo::Ptr{Cdouble}
+    vmap_plus::Ptr{Int64}
+    elemtobndy::Ptr{Int64}
+end
+
+"""
+    CMDGModel(dg::DGModel, params; precision = CMDG_FP64)
+
+GPU model on the reference DGModel's own grid arrays and reference state:
+`vgeo`, `vmap⁺`, `elemtobndy` of `dg.grid` and `Φ`, `∇Φ`, `ρ_ref`, `ρe_ref`,
+`p_ref` of `dg.state_auxiliary` (cmdg_mesh_create_arrays +
+cmdg_model_set_reference).  `aux_index` gives the aux columns of
+orientation.Φ, the three components of orientation.∇Φ and ref_state.ρ,
+ref_state.ρe and ref_state.p (`varsindices` of the model's Auxiliary vars).
+"""
+function CMDGModel(dg, params::AtmosParams, aux_index::NTuple{7, Int}; precision = CMDG_FP64)
+    g = dg.grid
+    N = Cint(polynomialorders(g)[1])
+    vgeo = Array(g.vgeo)
+    vmapP = Array{Int64}(Array(g.vmap⁺))
+    e2b = Array{Int64}(Array(g.elemtobndy))
+    nelem = Int64(size(vgeo, 3))
+    arr = GridArrays(N, nelem, pointer(vgeo), pointer(vmapP), pointer(e2b))
+    mesh = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve vgeo vmapP e2b begin
+        check(ccall((:cmdg_mesh_create_arrays, libcmdg), Cint, (Ref{GridArrays}, Ref{Ptr{Cvoid}}), arr, mesh))
+    end
+    model = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:cmdg_model_create, libcmdg), Cint, (Ptr{Cvoid}, Ref{AtmosParams}, Cint, Ref{Ptr{Cvoid}}),
+                mesh[], params, precision, model))
+    aux7 = Array(Array(dg.state_auxiliary.data)[:, collect(aux_index), 1:nelem])
+    check(ccall((:cmdg_model_set_reference, libcmdg), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), model[], aux7))
+    cm = CMDGModel(mesh[], model[], g, dg.balance_law, dg.state_auxiliary)
+    finalizer(cm) do x
+        ccall((:cmdg_model_destroy, libcmdg), Cint, (Ptr{Cvoid},), x.model)
+        ccall((:cmdg_mesh_destroy, libcmdg), Cint, (Ptr{Cvoid},), x.mesh)
+    end
+    return cm
 end
 
 # tendency .= α dQ/dt(Q) + β tendency   (DGModel.jl:85)
