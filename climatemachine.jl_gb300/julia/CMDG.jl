@@ -57,6 +57,7 @@ struct AtmosParams
     planet_radius::Cdouble   # SphericalOrientation
     hyperdiffusion::Cint     # 0 = NoHyperDiffusion, 1 = DryBiharmonic
     tau_hyper::Cdouble       # DryBiharmonic tau_timescale
+    hyper_direction::Cint    # 0 = EveryDirection, 1 = HorizontalDirection (diffusion_direction)
 end
 
 check(rc::Cint) =
