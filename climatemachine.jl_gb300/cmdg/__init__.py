@@ -12,9 +12,12 @@ for sm_103a behind a C ABI, include/cmdg.h).  Names follow the reference:
     lsrk  = LSRK54CarpenterKennedy(dg, Q, dt=dt, t0=0.0)
     solve_(Q, lsrk, timeend=...)                              # solve!(Q, lsrk; timeend)
 """
-from .atmos import EARTH, AtmosModel, HydrostaticState, DryAdiabaticProfile, IsothermalProfile, DryBiharmonic
-from .dgmodel import DGModel, BrickGrid, CubedShellGrid, ArraysGrid, euclidean_distance, weightedsum, norm
-from .odesolvers import LSRK54CarpenterKennedy, solve_, dostep_
+from .atmos import (EARTH, AtmosModel, HydrostaticState, DryAdiabaticProfile, IsothermalProfile, DryBiharmonic,
+                    AtmosAcousticGravityLinearModel)
+from .dgmodel import (DGModel, BrickGrid, CubedShellGrid, ArraysGrid, euclidean_distance, weightedsum, norm,
+                      remainder_DGModel)
+from .odesolvers import (LSRK54CarpenterKennedy, ARK2GiraldoKellyConstantinescu, LinearBackwardEulerSolver,
+                         ManyColumnLU, LowStorageVariant, solve_, dostep_)
 from ._lib import CmdgError, load as load_library
 from .ensemble import Ensemble
 from . import checkpoint, filters, partition
@@ -22,5 +25,6 @@ from . import checkpoint, filters, partition
 __all__ = [
     "EARTH", "AtmosModel", "HydrostaticState", "DryBiharmonic", "DryAdiabaticProfile", "IsothermalProfile", "DGModel", "BrickGrid", "CubedShellGrid", "ArraysGrid",
     "euclidean_distance", "weightedsum", "norm", "LSRK54CarpenterKennedy", "solve_", "dostep_", "CmdgError",
-    "load_library", "Ensemble",
+    "load_library", "Ensemble", "AtmosAcousticGravityLinearModel", "remainder_DGModel",
+    "ARK2GiraldoKellyConstantinescu", "LinearBackwardEulerSolver", "ManyColumnLU", "LowStorageVariant",
 ]

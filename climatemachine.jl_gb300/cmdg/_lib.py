@@ -31,6 +31,8 @@ EXPORTS = (
     "cmdg_batch_create", "cmdg_batch_destroy", "cmdg_batch_set_tiling", "cmdg_batch_get_tiling",
     "cmdg_batch_lsrk54_step", "cmdg_batch_autotune",
     "cmdg_filter_matrix", "cmdg_apply_filter", "cmdg_apply_tmar",
+    "cmdg_linear_tendency", "cmdg_hevi_create", "cmdg_hevi_destroy", "cmdg_hevi_info", "cmdg_hevi_solve",
+    "cmdg_hevi_step",
 )
 
 
@@ -125,6 +127,12 @@ def load(path: str | None = None):
         "cmdg_filter_matrix": [I, I, I, I, D, P],
         "cmdg_apply_filter": [P, P, P, P, I, P, I, P],
         "cmdg_apply_tmar": [P, P, P, I, P],
+        "cmdg_linear_tendency": [P, P, P, D, D, D, P],
+        "cmdg_hevi_create": [P, D, I, I, PP],
+        "cmdg_hevi_destroy": [P],
+        "cmdg_hevi_info": [P, ctypes.POINTER(D), ctypes.POINTER(I), ctypes.POINTER(ctypes.c_int64)],
+        "cmdg_hevi_solve": [P, P, P, P],
+        "cmdg_hevi_step": [P, P, D, I, P],
     }
     for name, args in proto.items():
         fn = getattr(L, name)

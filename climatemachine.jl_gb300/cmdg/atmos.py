@@ -87,3 +87,19 @@ class AtmosModel:
         p.hyperdiffusion = 0 if hd is None else 1
         p.tau_hyper = 0.0 if hd is None else float(hd.tau_timescale)
         return p
+
+
+@dataclass
+class AtmosAcousticGravityLinearModel:
+    """AtmosAcousticGravityLinearModel(atmos) (src/Atmos/Model/linear.jl:
+    242-262): the acoustic and gravity terms of the dry AtmosModel linearized
+    about its hydrostatic reference state -- fluxes rho u, p_L I and
+    (rhoe_ref + p_ref) / rho_ref rho u with
+    p_L = rho R_d T_0 + R_d / cv_d (rhoe - rho Phi), source -rho grad Phi,
+    wavespeed the reference sound speed.  Discretized by a DGModel in
+    VerticalDirection that shares the atmos model's auxiliary state."""
+    atmos: AtmosModel
+
+    def __post_init__(self):
+        if self.atmos.ref_state is None:
+            raise ValueError("AtmosAcousticGravityLinearModel needs a model with a reference state")

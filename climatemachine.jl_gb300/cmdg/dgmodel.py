@@ -148,7 +148,27 @@ class DGModel:
     """
 
     def __init__(self, balance_law, grid: BrickGrid, numerical_flux: str = "rusanov", precision: str = "fp64",
-                 diffusion_direction: str = "every"):
+                 diffusion_direction: str = "every", direction: str = "every", state_auxiliary: "DGModel" = None):
+        from .atmos import AtmosAcousticGravityLinearModel
+
+        if isinstance(balance_law, AtmosAcousticGravityLinearModel):
+            # DGModel(linearmodel, grid, ...; direction = VerticalDirection(),
+            # state_auxiliary = dg.state_auxiliary): the linear operator on the
+            # parent model's tables (no model of its own)
+            if direction != "vertical" or not isinstance(state_auxiliary, DGModel):
+                raise ValueError("the linear model runs in direction='vertical' with state_auxiliary=<its DGModel>")
+            if state_auxiliary.mixed:
+                raise ValueError("the linear model runs FP64 models")
+            self.balance_law, self.grid, self.numerical_flux = balance_law, grid, numerical_flux
+            self.precision, self.mixed, self.direction = "fp64", False, direction
+            self.parent = state_auxiliary
+            self.h = state_auxiliary.h
+            self.device = state_auxiliary.device
+            self._borrowed = True
+            return
+        if direction != "every" or state_auxiliary is not None:
+            raise ValueError("the AtmosModel DGModel runs in every direction with its own auxiliary state")
+        self.direction = direction
         self.balance_law = balance_law
         self.grid = grid
         self.numerical_flux = numerical_flux
@@ -164,9 +184,15 @@ class DGModel:
         self.device = torch.device("cuda", torch.cuda.current_device())
 
     def __del__(self):
+        if getattr(self, "_borrowed", False):
+            return
         if getattr(self, "h", None) and _lib._lib is not None:
             _lib._lib.cmdg_model_destroy(self.h)
             self.h = None
+
+    @property
+    def is_linear(self) -> bool:
+        return getattr(self, "_borrowed", False)
 
     # ------------------------------------------------------------------ state
     @property
@@ -220,6 +246,9 @@ class DGModel:
         b = (1.0 if increment else 0.0) if beta is None else float(beta)
         if tendency.dtype != torch.float64:
             raise ValueError("the tendency / RK register is FP64 in every precision")
+        if self.is_linear:
+            call("cmdg_linear_tendency", self.h, _dptr(tendency), _dptr(Q), float(t), a, b, _stream())
+            return tendency
         fn = "cmdg_tendency_mixed" if self.mixed else "cmdg_tendency"
         if Q.dtype != self.state_dtype:
             raise ValueError(f"state dtype {Q.dtype} does not match the model ({self.state_dtype})")
@@ -295,6 +324,28 @@ class DGModel:
         st = ctypes.c_uint32()
         call("cmdg_status_word", self.h, ctypes.byref(st), _stream())
         return st.value
+
+
+class RemainderDGModel:
+    """remainder_DGModel(dg, (lineardg,)) (src/Numerics/DGMethods/remainder.jl):
+    the tendency of the full model minus the linear one, evaluated as the full
+    tendency followed by the linear tendency with alpha = -1."""
+
+    def __init__(self, main: DGModel, subs):
+        subs = tuple(subs)
+        if len(subs) != 1 or not subs[0].is_linear or subs[0].parent is not main:
+            raise ValueError("remainder_DGModel(dg, (lineardg,)) with the linear model of dg")
+        self.main, self.subs = main, subs
+        self.grid = main.grid
+
+    def __call__(self, tendency, Q, param=None, t=0.0, increment=False):
+        self.main(tendency, Q, param, t, increment=increment)
+        self.subs[0](tendency, Q, param, t, alpha=-1.0, beta=1.0)
+        return tendency
+
+
+def remainder_DGModel(dg: DGModel, subs, **_kw) -> RemainderDGModel:
+    return RemainderDGModel(dg, subs)
 
 
 def _host(Q: torch.Tensor) -> np.ndarray:

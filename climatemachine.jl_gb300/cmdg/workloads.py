@@ -169,6 +169,52 @@ def gcm_initial_state(xyz: np.ndarray, *, seed=2024, T_ref=285.0, u_max=30.0, dT
     return Q
 
 
+def acoustic_wave_model(nhorz=10, nvert=5, N=5, H=10e3, T_ref=300.0):
+    """The acoustic wave on the sphere of
+    test/Numerics/DGMethods/Euler/acousticwave_1d_imex.jl: stacked cubed
+    shell (nhorz x nhorz per cube face, nvert levels, lid H), FP64,
+    SphericalOrientation + Gravity, HydrostaticState(IsothermalProfile(T_ref)),
+    inviscid, Rusanov flux, walls at both radii."""
+    R = EARTH["planet_radius"]
+    grid = CubedShellGrid(N, nhorz, nvert, R, R + H)
+    model = AtmosModel(orientation="sphere", gravity=True, ref_state=HydrostaticState(IsothermalProfile(T_ref)))
+    return DGModel(model, grid, numerical_flux="rusanov", precision="fp64")
+
+
+def acoustic_wave_state(xyz: np.ndarray, p_ref: np.ndarray, *, H=10e3, T_ref=300.0, alpha=3.0, gamma=100.0,
+                        nv=1, consts=EARTH) -> np.ndarray:
+    """AcousticWaveSetup (acousticwave_1d_imex.jl): at rest, T = T_ref and
+    p = p_ref + gamma f(beta) sin(nv pi z / H), beta = min(1, alpha
+    acos(cos(lat) cos(lon))), f = (1 + cos(pi beta)) / 2; rho = p / (R_d T),
+    rhoe = rho (cv_d (T - T_0) + Phi).  xyz (nelem, 3, Np) node coordinates,
+    p_ref (nelem, Np) the reference pressure."""
+    g, a, R_d, cv, T0 = (consts[k] for k in ("grav", "planet_radius", "R_d", "cv_d", "T_0"))
+    x, y, z3 = xyz[:, 0], xyz[:, 1], xyz[:, 2]
+    r = np.sqrt(x * x + y * y + z3 * z3)
+    Phi = g * (r - a)
+    lam = np.arctan2(y, x)
+    phi = np.arcsin(z3 / r)
+    z = Phi / g
+    beta = np.minimum(1.0, alpha * np.arccos(np.cos(phi) * np.cos(lam)))
+    f = (1 + np.cos(np.pi * beta)) / 2
+    p = p_ref + gamma * f * np.sin(nv * np.pi * z / H)
+    Q = np.zeros((xyz.shape[0], 5, xyz.shape[2]))
+    rho = p / (R_d * T_ref)
+    Q[:, 0] = rho
+    Q[:, 4] = rho * (cv * (T_ref - T0) + Phi)
+    return Q
+
+
+def acoustic_wave_dt(H=10e3, nvert=5, N=5, T_ref=300.0, dt_factor=445, consts=EARTH):
+    """dt of acousticwave_1d_imex.jl: dt_factor x the vertical acoustic
+    element time over N^2, shortened to hit one hour exactly; and the number
+    of steps in an hour."""
+    cs = math.sqrt(consts["cp_d"] / consts["cv_d"] * consts["R_d"] * T_ref)
+    dt = dt_factor * (H / nvert) / cs / N**2
+    dt = 3600 / math.ceil(3600 / dt)
+    return dt, math.ceil(3600 / dt)
+
+
 def les_model(ne=(32, 32, 16), N=4, L=(3200.0, 3200.0, 1600.0), precision="fp64", theta0=300.0):
     """Compressible Navier-Stokes LES: SmagorinskyLilly (C_s = 0.21) on a
     brick periodic in x and y with FreeSlip/Insulating walls in z (a stratified

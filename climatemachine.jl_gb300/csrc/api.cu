@@ -356,6 +356,8 @@ int cmdg_model_destroy(cmdg_model* model) {
     cudaFree(md.d_ref64);
     cudaFree(md.d_filter_corr);
     cudaFree(md.d_omega);
+    cudaFree(md.d_lin64);
+    cudaFree(md.d_linface64);
     release_quad(&md);
     delete model;
     return CMDG_OK;

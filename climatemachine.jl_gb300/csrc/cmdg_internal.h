@@ -192,6 +192,10 @@ struct Model {
     std::vector<double> arrays_geo, pref64;
     float* d_fjump = nullptr;
     bool has_reference = false;
+    // linear (acoustic-gravity) model in VerticalDirection: per-node table
+    // (Np, 10, nelem) and bottom/top face table (Nfp, 4, 2, nelem), FP64
+    double* d_lin64 = nullptr;
+    double* d_linface64 = nullptr;
     int grid_ctas = -1;              // stage-kernel grid: -1 = one CTA per element (the measured best
                                      // on GB300), 0 = one wave of resident CTAs, n > 0 = n CTAs
     int kernel_kind = 0;             // KERNEL_NODE or KERNEL_COLUMN

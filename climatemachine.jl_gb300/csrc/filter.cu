@@ -260,7 +260,9 @@ extern "C" int cmdg_apply_filter(cmdg_model* model, void* d_Q, const double* h_W
     CMDG_ARG_CHECK(direction >= CMDG_DIR_EVERY && direction <= CMDG_DIR_VERTICAL, "unknown direction %d", direction);
     Model* md = &model->m;
     const Mesh& m = *md->mesh;
-    CMDG_ARG_CHECK(m.kind == MESH_BRICK, "filters run on brick meshes");
+    // element-local line filters; the mixed path's reference-state correction is per level of a brick
+    CMDG_ARG_CHECK(m.kind == MESH_BRICK || md->precision == CMDG_FP64,
+                   "mixed-precision filters run on brick meshes");
     const bool horiz = direction != CMDG_DIR_VERTICAL, vert = direction != CMDG_DIR_HORIZONTAL;
     CMDG_ARG_CHECK(!horiz || h_Wh != nullptr, "horizontal filter matrix is NULL");
     CMDG_ARG_CHECK(!vert || h_Wv != nullptr, "vertical filter matrix is NULL");

@@ -265,7 +265,8 @@ int cmdg_batch_autotune(cmdg_batch* batch, void* const* h_Q, double* const* h_dQ
  * vertical one along xi3 (direction CMDG_DIR_*) to the listed fields of a
  * model's state in place (FP64 state, or the FP32 perturbation of a mixed
  * model; mixed needs Nc >= 1 horizontally) — Filters.apply!(Q, fields, grid,
- * filter; direction) (:408-505).  Brick meshes.
+ * filter; direction) (:408-505).  Any mesh for FP64 models (the filters act
+ * along the element lines); mixed-precision models on brick meshes.
  * cmdg_apply_tmar: TMARFilter on the listed fields (:369-407, 794-892). */
 enum { CMDG_FILTER_EXPONENTIAL = 0, CMDG_FILTER_CUTOFF = 1, CMDG_FILTER_BOYD_VANDEVEN = 2 };
 enum { CMDG_DIR_EVERY = 0, CMDG_DIR_HORIZONTAL = 1, CMDG_DIR_VERTICAL = 2 };
@@ -273,6 +274,44 @@ int cmdg_filter_matrix(int N, int kind, int Nc, int s, double alpha, double* h_W
 int cmdg_apply_filter(cmdg_model* model, void* d_Q, const double* h_Wh, const double* h_Wv, int direction,
                       const int* h_fields, int nfields, void* stream);
 int cmdg_apply_tmar(cmdg_model* model, void* d_Q, const int* h_fields, int nfields, void* stream);
+
+/* HEVI (horizontally explicit, vertically implicit) stepping, FP64 models with
+ * a hydrostatic reference state on wall-bounded element stacks (cubed shell,
+ * or a brick non-periodic in z).
+ *
+ * cmdg_linear_tendency: d_dQ = alpha * L(d_Q) + beta * d_dQ, the tendency of
+ * AtmosAcousticGravityLinearModel(model) as a DGModel in VerticalDirection
+ * sharing the model's auxiliary state (src/Atmos/Model/linear.jl:1-57,
+ * 150-262; src/Atmos/Model/linear_tendencies.jl; DGModel.jl:85-427 with
+ * direction = VerticalDirection()): fluxes rho u, p_L I,
+ * (rhoe_ref + p_ref) / rho_ref rho u with p_L = rho R_d T_0 + R_d / cv_d
+ * (rhoe - rho Phi), source -rho grad Phi, Rusanov flux at the reference
+ * sound speed on faces 5 and 6.  d_dQ must not alias d_Q.
+ *
+ * cmdg_hevi_create: ARK2GiraldoKellyConstantinescu(dg, lineardg,
+ * LinearBackwardEulerSolver(ManyColumnLU()), Q; dt, split_explicit_implicit,
+ * paperversion, variant = LowStorageVariant())
+ * (src/Numerics/ODESolvers/AdditiveRungeKuttaMethod.jl:839-897, 413-538):
+ * builds and LU-factors, without pivoting, the banded matrix of
+ * Q - alpha L(Q), alpha = dt (1 - 1/sqrt(2)), for every vertical node line
+ * (src/Numerics/SystemSolvers/columnwise_lu_solver.jl:92-158, 228-488).
+ * Owns that matrix and seven state-sized FP64 buffers.
+ * cmdg_hevi_solve: besolver!(Q, Qhat, alpha): d_Q = d_Qhat + alpha L(d_Q)
+ * (BackwardEulerSolvers.jl; linearsolve! columnwise_lu_solver.jl:110-127,
+ * 615-780); d_Q may alias d_Qhat.
+ * cmdg_hevi_step: nsteps ARK2 steps of d_Q (dostep!, :413-538); the explicit
+ * part is the model's full tendency (split_explicit_implicit = 0) or the
+ * remainder full - linear (1, remainder_DGModel).
+ * cmdg_hevi_info: the implicit coefficient alpha, the band half-width
+ * 5 (N+1) - 1 and the number of vertical lines. */
+typedef struct cmdg_hevi cmdg_hevi;
+int cmdg_linear_tendency(cmdg_model* model, double* d_dQ, const double* d_Q, double t, double alpha, double beta,
+                         void* stream);
+int cmdg_hevi_create(cmdg_model* model, double dt, int split_explicit_implicit, int paperversion, cmdg_hevi** out);
+int cmdg_hevi_destroy(cmdg_hevi* hevi);
+int cmdg_hevi_info(const cmdg_hevi* hevi, double* alpha, int* bandwidth, int64_t* nline);
+int cmdg_hevi_solve(cmdg_hevi* hevi, double* d_Q, const double* d_Qhat, void* stream);
+int cmdg_hevi_step(cmdg_hevi* hevi, double* d_Q, double t, int nsteps, void* stream);
 
 /* Mixed precision: converts an FP64 state to the FP32 perturbation
  * q' = q - q_ref (the subtraction is done in FP64) and back.

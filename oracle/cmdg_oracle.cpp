@@ -1515,6 +1515,276 @@ void lsrk_step(Model& m, double* Q, double* dQ, double time, double dt) {
     }
 }
 
+// ----------------------------------------------------------------------------
+// HEVI: AtmosAcousticGravityLinearModel as a DGModel in VerticalDirection
+// (Atmos/Model/linear.jl:1-57, 150-160, 242-262; linear_tendencies.jl;
+// linear_atmos_tendencies.jl), the column-wise banded LU of
+// SystemSolvers/columnwise_lu_solver.jl and ARK2GiraldoKellyConstantinescu in
+// its LowStorageVariant (ODESolvers/AdditiveRungeKuttaMethod.jl:413-538,
+// 603-662, 839-897).
+// ----------------------------------------------------------------------------
+struct LinAux {
+    double Phi, gPhi[3], h_ref, c_ref;
+};
+
+inline LinAux lin_aux(const Model& m, int64_t e, int n) {
+    LinAux a;
+    a.Phi = AUXc(m, e, APHI, n);
+    a.gPhi[0] = AUXc(m, e, AGPX, n);
+    a.gPhi[1] = AUXc(m, e, AGPY, n);
+    a.gPhi[2] = AUXc(m, e, AGPZ, n);
+    // LinearEnergyFlux: (ref.rhoe + ref.p) / ref.rho (linear_tendencies.jl:62-71)
+    a.h_ref = (AUXc(m, e, ARHOE_REF, n) + AUXc(m, e, AP_REF, n)) / AUXc(m, e, ARHO_REF, n);
+    // wavespeed(::AtmosLinearModel) = soundspeed_air(ref.T) (linear.jl:150-160)
+    a.c_ref = soundspeed(m.prm, AUXc(m, e, AT_REF, n));
+    return a;
+}
+
+// linearized_air_pressure of a dry state (linear.jl:18-37, 49-57)
+inline double linearized_pressure(const om_params& p, double rho, double rhoe, double Phi) {
+    const double rho_epot = rho * Phi;
+    return rho * p.R_d * p.T_0 + p.R_d / p.cv_d * (rhoe - rho_epot);
+}
+
+// First-order flux of the linear model: Advect, LinearPressureGradient,
+// LinearEnergyFlux (linear_tendencies.jl:8-11, 21-27, 62-71).
+void linear_flux(const om_params& p, const double q[NS], const LinAux& a, double F[3][NS]) {
+    const double pL = linearized_pressure(p, q[0], q[4], a.Phi);
+    for (int d = 0; d < 3; ++d) {
+        F[d][0] = q[1 + d];
+        for (int c = 0; c < 3; ++c) F[d][1 + c] = (c == d) ? pL : 0.0;
+        F[d][4] = a.h_ref * q[1 + d];
+    }
+}
+
+// Rusanov flux of the linear model across face f at face node n of element e
+// (NumericalFluxes.jl:223-285 with the linear wavespeed; FreeSlip/Insulating
+// boundary state on walls, boundaryconditions.jl:60-95, bc_momentum.jl:25-34).
+void linear_face_flux(const Model& m, const double* Q, int64_t e, int f, int n, double fl[NS]) {
+    const om_params& p = m.prm;
+    const int Np = m.Np, Nfp = m.Nfp;
+    const int64_t idM = m.vmapM[(e * 6 + f) * Nfp + n], idP = m.vmapP[(e * 6 + f) * Nfp + n];
+    const int vM = (int)(idM % Np);
+    int64_t eP = idP / Np;
+    int vP = (int)(idP % Np);
+    const int tag = m.elemtobndy[e * 6 + f];
+    if (tag != 0) { eP = e; vP = vM; }
+    const double nv[3] = {SGc(m, e, f, n, SN1), SGc(m, e, f, n, SN2), SGc(m, e, f, n, SN3)};
+    double qM[NS], qP[NS];
+    load_q(m, Q, e, vM, qM);
+    if (tag == 0) load_q(m, Q, eP, vP, qP);
+    else bc_state_first(qM, nv, qP);
+    const LinAux aM = lin_aux(m, e, vM), aP = lin_aux(m, eP, vP);
+    double FM[3][NS], FP[3][NS];
+    linear_flux(p, qM, aM, FM);
+    linear_flux(p, qP, aP, FP);
+    const double mw = std::max(aM.c_ref, aP.c_ref);
+    for (int s = 0; s < NS; ++s) {
+        double acc = 0;
+        for (int d = 0; d < 3; ++d) acc += (FM[d][s] + FP[d][s]) * (nv[d] / 2);
+        fl[s] = acc + mw * (qM[s] - qP[s]) / 2;
+    }
+}
+
+// lineardg(T, Q; alpha, beta): T = alpha * L(Q) + beta * T with the vertical
+// volume kernel (DGModel_kernels.jl:312-548: M xi3 . F, M^-1 D^T, the
+// Gravity source -rho grad Phi of linear_tendencies.jl:33-45) and the
+// interface kernel on faces 5 and 6 (:588-901).
+void linear_tendency(Model& m, double* T, const double* Q, double alpha, double beta) {
+    const om_params& p = m.prm;
+    const int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m.nelem; ++e) {
+        std::vector<double> F3(Np * NS), Src(Np * NS);
+        for (int n = 0; n < Np; ++n) {
+            double q[NS];
+            load_q(m, Q, e, n, q);
+            const LinAux a = lin_aux(m, e, n);
+            double F[3][NS];
+            linear_flux(p, q, a, F);
+            const double M = VGc(m, e, VM, n);
+            for (int s = 0; s < NS; ++s)
+                F3[n * NS + s] = M * (VGc(m, e, XI3X1, n) * F[0][s] + VGc(m, e, XI3X2, n) * F[1][s] + VGc(m, e, XI3X3, n) * F[2][s]);
+            Src[n * NS + 0] = 0;
+            for (int c = 0; c < 3; ++c) Src[n * NS + 1 + c] = -q[0] * a.gPhi[c];
+            Src[n * NS + 4] = 0;
+        }
+        for (int k = 0; k < Nq; ++k)
+            for (int j = 0; j < Nq; ++j)
+                for (int i = 0; i < Nq; ++i) {
+                    const int ijk = i + Nq * (j + Nq * k);
+                    const double MI = VGc(m, e, VMI, ijk);
+                    for (int s = 0; s < NS; ++s) {
+                        double lv = 0;
+                        for (int kk = 0; kk < Nq; ++kk) lv += MI * Dm(m, kk, k) * F3[(i + Nq * (j + Nq * kk)) * NS + s];
+                        lv += Src[ijk * NS + s];
+                        const size_t idx = (size_t)(e * NS + s) * Np + ijk;
+                        T[idx] = (beta != 0) ? alpha * lv + beta * T[idx] : alpha * lv;
+                    }
+                }
+        for (int f = 4; f < 6; ++f)
+            for (int n = 0; n < Nfp; ++n) {
+                double fl[NS];
+                linear_face_flux(m, Q, e, f, n, fl);
+                const int vM = (int)(m.vmapM[(e * 6 + f) * Nfp + n] % Np);
+                const double sM = SGc(m, e, f, n, SSM), vMI = SGc(m, e, f, n, SVMI);
+                for (int s = 0; s < NS; ++s) T[(size_t)(e * NS + s) * Np + vM] -= alpha * vMI * sM * fl[s];
+            }
+    }
+}
+
+// Elements per vertical stack; 0 when the mesh has no wall-bounded columns.
+int stack_height(const Model& m) {
+    if (m.kind == 1) return m.shell.nvert;
+    if (m.kind == 0 && m.law == 0 && !m.mesh.periodic[2]) return m.mesh.ne[2];
+    return 0;
+}
+
+// ARK2GiraldoKellyConstantinescu (AdditiveRungeKuttaMethod.jl:839-897) with a
+// LinearBackwardEulerSolver(ManyColumnLU()) (BackwardEulerSolvers.jl,
+// columnwise_lu_solver.jl).  One banded matrix per vertical line (i, j) of
+// each stack; unknown r = s + 5 (k + Nq v) of stack level v; bandwidths
+// p = q = 5 Nq - 1 (eband = 1, columnwise_lu_solver.jl:56-74).
+struct Hevi {
+    Model* m = nullptr;
+    double dt = 0, alpha = 0;
+    int split = 0;
+    double Ae[3][3], Ai[3][3], B[3], C[3];
+    int nvert = 0, n = 0, bw = 0;
+    int64_t nline = 0;
+    std::vector<double> AB;    // line-major; A(row, col) at [(line * (2 bw + 1) + bw + row - col) * n + col]
+    std::vector<double> S1, S2, R0, R1, R2, Qhat, Qtt;
+};
+
+inline size_t line_state_index(const Hevi& h, int64_t line, int r) {
+    const Model& m = *h.m;
+    const int Nq = m.Nq, Nfp = m.Nfp;
+    const int s = r % NS, k = (r / NS) % Nq, v = r / (NS * Nq);
+    const int64_t col = line / Nfp;
+    const int ij = (int)(line % Nfp);
+    const int64_t e = v + (int64_t)h.nvert * col;
+    return (size_t)(e * NS + s) * m.Np + ij + Nfp * k;
+}
+
+inline double& band(Hevi& h, int64_t line, int row, int col) {
+    return h.AB[((size_t)line * (2 * h.bw + 1) + h.bw + row - col) * h.n + col];
+}
+
+// banded_matrix of the EulerOperator Q - alpha L(Q) (columnwise_lu_solver.jl:
+// 228-312, 404-488: the operator applied to unit states, one per (element
+// level mod 2 eband + 1, k, s)), then band_lu! (:129-158, 555-600; Golub &
+// Van Loan Algorithm 4.3.1 without pivoting).
+void hevi_factorize(Hevi& h) {
+    Model& m = *h.m;
+    const int Nq = m.Nq, Nfp = m.Nfp, Np = m.Np;
+    const size_t len = (size_t)m.nelem * NS * Np;
+    h.n = NS * Nq * h.nvert;
+    h.bw = NS * Nq - 1;
+    h.nline = (m.nelem / h.nvert) * Nfp;
+    h.AB.assign((size_t)h.nline * (2 * h.bw + 1) * h.n, 0.0);
+    std::vector<double> E(len), R(len);
+    const double eps = -h.alpha;
+    for (int vi = 0; vi < 3 && vi < h.nvert; ++vi)
+        for (int k = 0; k < Nq; ++k)
+            for (int s = 0; s < NS; ++s) {
+                std::fill(E.begin(), E.end(), 0.0);
+                for (int64_t e = 0; e < m.nelem; ++e)
+                    if ((e % h.nvert) % 3 == vi)
+                        for (int ij = 0; ij < Nfp; ++ij) E[(size_t)(e * NS + s) * Np + ij + Nfp * k] = 1.0;
+                linear_tendency(m, R.data(), E.data(), 1.0, 0.0);
+                for (int64_t line = 0; line < h.nline; ++line)
+                    for (int v = 0; v < h.nvert; ++v) {
+                        int vs = -1;
+                        for (int d = -1; d <= 1; ++d)
+                            if (v + d >= 0 && v + d < h.nvert && (v + d) % 3 == vi) vs = v + d;
+                        if (vs < 0) continue;
+                        const int col = s + NS * (k + Nq * vs);
+                        for (int r = NS * Nq * v; r < NS * Nq * (v + 1); ++r) {
+                            const size_t idx = line_state_index(h, line, r);
+                            const double val = E[idx] + eps * R[idx];  // EulerOperator: Q + eps L(Q)
+                            if (std::abs(r - col) <= h.bw) band(h, line, r, col) = val;
+                            else if (val != 0) throw std::runtime_error("HEVI: coupling outside the band");
+                        }
+                    }
+            }
+    const int n = h.n, bw = h.bw;
+#pragma omp parallel for schedule(static)
+    for (int64_t line = 0; line < h.nline; ++line)
+        for (int kk = 0; kk < n; ++kk) {
+            const double Aq = band(h, line, kk, kk);
+            for (int ii = 1; ii <= bw && kk + ii < n; ++ii) band(h, line, kk + ii, kk) /= Aq;
+            for (int jj = 1; jj <= bw && kk + jj < n; ++jj) {
+                const double Ajj = band(h, line, kk, kk + jj);
+                for (int ii = 1; ii <= bw && kk + ii < n; ++ii)
+                    band(h, line, kk + ii, kk + jj) -= band(h, line, kk + ii, kk) * Ajj;
+            }
+        }
+}
+
+// linearsolve! of the factorization: Q .= Qrhs, band_forward!, band_back!
+// (columnwise_lu_solver.jl:110-127, 615-690, 704-780).
+void hevi_solve(Hevi& h, double* Q, const double* Qrhs) {
+    Model& m = *h.m;
+    const size_t len = (size_t)m.nelem * NS * m.Np;
+    if (Q != Qrhs) std::memcpy(Q, Qrhs, len * sizeof(double));
+    const int n = h.n, bw = h.bw;
+#pragma omp parallel for schedule(static)
+    for (int64_t line = 0; line < h.nline; ++line) {
+        std::vector<double> b(n);
+        for (int r = 0; r < n; ++r) b[r] = Q[line_state_index(h, line, r)];
+        for (int jj = 0; jj < n; ++jj)
+            for (int ii = 1; ii <= bw && jj + ii < n; ++ii) b[jj + ii] -= band(h, line, jj + ii, jj) * b[jj];
+        for (int jj = n - 1; jj >= 0; --jj) {
+            b[jj] /= band(h, line, jj, jj);
+            for (int ii = 1; ii <= bw && jj - ii >= 0; ++ii) b[jj - ii] -= band(h, line, jj - ii, jj) * b[jj];
+        }
+        for (int r = 0; r < n; ++r) Q[line_state_index(h, line, r)] = b[r];
+    }
+}
+
+// rhs!: the full tendency, or the remainder f - l when split (remainder.jl)
+void hevi_rhs(Hevi& h, double* R, const double* Q, double t) {
+    tendency(*h.m, R, Q, t, 1.0, 0.0);
+    if (h.split) linear_tendency(*h.m, R, Q, -1.0, 1.0);
+}
+
+// dostep!(Q, ark, ::LowStorageVariant, p, time) (AdditiveRungeKuttaMethod.jl:413-538)
+void hevi_step(Hevi& h, double* Q, double time) {
+    Model& m = *h.m;
+    const size_t len = (size_t)m.nelem * NS * m.Np;
+    const double dt = h.dt;
+    double* Sst[3] = {Q, h.S1.data(), h.S2.data()};
+    double* Rst[3] = {h.R0.data(), h.R1.data(), h.R2.data()};
+    hevi_rhs(h, Rst[0], Sst[0], time + h.C[0] * dt);
+    for (int is = 1; is < 3; ++is) {
+        const double stagetime = time + h.C[is] * dt;
+        double rk[3];
+        for (int js = 0; js < is; ++js)
+            rk[js] = h.split ? h.Ai[is][js] / h.Ai[is][is] : (h.Ai[is][js] - h.Ae[is][js]) / h.Ai[is][is];
+#pragma omp parallel for schedule(static)
+        for (size_t i = 0; i < len; ++i) {
+            double qh = Q[i], qs = -0.0;
+            for (int js = 0; js < is; ++js) {
+                const double common = rk[js] * Sst[js][i];
+                qh += common + dt * h.Ae[is][js] * Rst[js][i];
+                qs -= common;
+            }
+            Sst[is][i] = qs;
+            h.Qhat[i] = qh;
+            h.Qtt[i] = qh;
+        }
+        hevi_solve(h, h.Qtt.data(), h.Qhat.data());
+#pragma omp parallel for schedule(static)
+        for (size_t i = 0; i < len; ++i) Sst[is][i] += h.Qtt[i];
+        hevi_rhs(h, Rst[is], Sst[is], stagetime);
+    }
+    if (h.split)
+        for (int is = 0; is < 3; ++is) linear_tendency(m, Rst[is], Sst[is], 1.0, 1.0);
+#pragma omp parallel for schedule(static)
+    for (size_t i = 0; i < len; ++i)
+        for (int is = 0; is < 3; ++is) Q[i] += h.B[is] * dt * Rst[is][i];
+}
+
 // TwoSum-based double-double accumulate (DoubleFloats.jl semantics)
 struct DD {
     double hi = 0, lo = 0;
@@ -1726,6 +1996,56 @@ double om_lsrk54_scalar(double q0, double dt, double timeend) {
 }
 
 // Weighted L2 norm sqrt(sum M Q^2), MPIStateArrays.jl:583-606
+typedef struct Hevi om_hevi;
+
+// AtmosAcousticGravityLinearModel tendency in VerticalDirection
+void om_linear_tendency(om_model* m, double* dQ, const double* Q, double alpha, double beta) {
+    linear_tendency(*m, dQ, Q, alpha, beta);
+}
+
+// ARK2GiraldoKellyConstantinescu(dg, lineardg, LinearBackwardEulerSolver(ManyColumnLU()), Q;
+// dt, split_explicit_implicit, paperversion); NULL when the mesh has no wall-bounded stacks.
+om_hevi* om_hevi_create(om_model* m, double dt, int split, int paperversion) {
+    const int nv = stack_height(*m);
+    if (nv <= 0 || m->law != 0 || m->prm.ref_state != 1) return nullptr;
+    Hevi* h = new Hevi();
+    h->m = m;
+    h->dt = dt;
+    h->split = split;
+    h->nvert = nv;
+    const double s2 = std::sqrt(2.0);
+    const double a32 = paperversion ? (3 + 2 * s2) / 6 : 0.5;
+    const double Ae[3][3] = {{0, 0, 0}, {2 - s2, 0, 0}, {1 - a32, a32, 0}};
+    const double Ai[3][3] = {{0, 0, 0}, {1 - 1 / s2, 1 - 1 / s2, 0}, {1 / (2 * s2), 1 / (2 * s2), 1 - 1 / s2}};
+    const double B[3] = {1 / (2 * s2), 1 / (2 * s2), 1 - 1 / s2}, C[3] = {0, 2 - s2, 1};
+    std::memcpy(h->Ae, Ae, sizeof(Ae));
+    std::memcpy(h->Ai, Ai, sizeof(Ai));
+    std::memcpy(h->B, B, sizeof(B));
+    std::memcpy(h->C, C, sizeof(C));
+    h->alpha = dt * h->Ai[1][1];
+    const size_t len = (size_t)m->nelem * NS * m->Np;
+    for (auto* v : {&h->S1, &h->S2, &h->R0, &h->R1, &h->R2, &h->Qhat, &h->Qtt}) v->assign(len, 0.0);
+    try {
+        hevi_factorize(*h);
+    } catch (const std::exception&) {
+        delete h;
+        return nullptr;
+    }
+    return h;
+}
+
+void om_hevi_free(om_hevi* h) { delete h; }
+
+// besolver!(Q, Qhat, alpha): Q = Qhat + alpha L(Q) by the factorization
+void om_hevi_solve(om_hevi* h, double* Q, const double* Qhat) { hevi_solve(*h, Q, Qhat); }
+
+double om_hevi_alpha(const om_hevi* h) { return h->alpha; }
+int om_hevi_bandwidth(const om_hevi* h) { return h->bw; }
+
+void om_hevi_step(om_hevi* h, double* Q, double t0, int nsteps) {
+    for (int i = 0; i < nsteps; ++i) hevi_step(*h, Q, t0 + i * h->dt);
+}
+
 double om_norm(const om_model* m, const double* Q) {
     double acc = 0;
     for (int64_t e = 0; e < m->nelem; ++e)

@@ -162,6 +162,15 @@ def lib():
         L.om_scalar_hyper_lsrk54.argtypes = [P, dp, dp, D, ctypes.c_int]
         L.om_lsrk54_scalar.restype = D
         L.om_lsrk54_scalar.argtypes = [D, D, D]
+        L.om_linear_tendency.argtypes = [P, dp, dp, D, D]
+        L.om_hevi_create.restype = P
+        L.om_hevi_create.argtypes = [P, D, ctypes.c_int, ctypes.c_int]
+        L.om_hevi_free.argtypes = [P]
+        L.om_hevi_solve.argtypes = [P, dp, dp]
+        L.om_hevi_alpha.restype = D
+        L.om_hevi_alpha.argtypes = [P]
+        L.om_hevi_bandwidth.argtypes = [P]
+        L.om_hevi_step.argtypes = [P, dp, D, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -365,6 +374,46 @@ class OracleModel:
     def init_rest(self):
         Q = self.state()
         self.L.om_init_rest(self.h, _ptr(Q))
+        return Q
+
+    def linear_tendency(self, Q, alpha=1.0, beta=0.0, dQ=None):
+        """AtmosAcousticGravityLinearModel tendency in VerticalDirection."""
+        if dQ is None:
+            dQ = self.state()
+        self.L.om_linear_tendency(self.h, _ptr(dQ), _ptr(Q), alpha, beta)
+        return dQ
+
+
+class OracleHevi:
+    """ARK2GiraldoKellyConstantinescu (LowStorageVariant) of an OracleModel
+    with the vertical AtmosAcousticGravityLinearModel solved implicitly by the
+    column-wise banded LU (AdditiveRungeKuttaMethod.jl:413-538, 839-897;
+    columnwise_lu_solver.jl)."""
+
+    def __init__(self, model: OracleModel, dt: float, split_explicit_implicit: bool = False,
+                 paperversion: bool = False):
+        self.model = model
+        self.L = model.L
+        self.dt = float(dt)
+        self.h = self.L.om_hevi_create(model.h, self.dt, int(split_explicit_implicit), int(paperversion))
+        if not self.h:
+            raise ValueError("oracle HEVI needs wall-bounded stacks and a hydrostatic reference state")
+        self.alpha = self.L.om_hevi_alpha(self.h)
+        self.bandwidth = self.L.om_hevi_bandwidth(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.om_hevi_free(self.h)
+            self.h = None
+
+    def solve(self, Qhat):
+        """Q with Q - alpha L(Q) = Qhat."""
+        Q = np.empty_like(Qhat)
+        self.L.om_hevi_solve(self.h, _ptr(Q), _ptr(np.ascontiguousarray(Qhat)))
+        return Q
+
+    def step(self, Q, nsteps=1, t0=0.0):
+        self.L.om_hevi_step(self.h, _ptr(Q), t0, nsteps)
         return Q
 
 

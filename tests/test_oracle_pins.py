@@ -22,6 +22,11 @@ Pins (reference paths relative to the ClimateMachine.jl project root):
     advection_diffusion/periodic_3D_hyperdiffusion.jl:229-235 (the
     hyperdiffusion passes that the AtmosModel's DryBiharmonic closure also
     runs)
+  * HEVI: acoustic wave on the sphere, FP64, N=5, 10 x 10 x 6 x 5 elements,
+    ARK2GiraldoKellyConstantinescu with ManyColumnLU on the vertical
+    AtmosAcousticGravityLinearModel (both splittings) and a vertical
+    exponential filter — test/Numerics/DGMethods/Euler/acousticwave_1d_imex.jl
+    (rtol sqrt(eps) in the reference; held here to 1e-11)
 Geometry checks of the cubed shell (Topologies.jl:1067-1305, Metrics.jl:431-724):
 shell volume from the mass matrix, the discrete metric identities (a uniform
 state has zero tendency) and the face-node maps (a linear density advected by
@@ -306,3 +311,91 @@ def test_mms_navier_stokes_golden():
             dQ *= A[(s + 1) % 5]
     err = om.euclidean_distance(Q, ev(fq, 1.0))
     assert err == pytest.approx(3.3983777728925593e-02, rel=1e-10)
+
+
+# ----------------------------------------------------------------------------
+# HEVI: AtmosAcousticGravityLinearModel (VerticalDirection), column LU,
+# ARK2GiraldoKellyConstantinescu
+# ----------------------------------------------------------------------------
+GOLDEN_ACOUSTIC_WAVE = 9.5073452847149594e13  # acousticwave_1d_imex.jl, expected_result[Float64]
+
+
+def acoustic_wave(nh=10, nv=5, N=5, H=10e3):
+    """AcousticWaveSetup of test/Numerics/DGMethods/Euler/acousticwave_1d_imex.jl
+    on the oracle's cubed shell: the model, its initial state and (dt, nsteps)."""
+    m = O.OracleModel(N, shell=dict(nhorz=nh, nvert=nv, r_inner=R_EARTH, r_outer=R_EARTH + H), orientation="sphere",
+                      gravity=True, ref_state=True, profile="isothermal", T_surface=300.0)
+    c = m.consts
+    aux = m.aux
+    x, y, z3 = aux[:, O.AUX["x"]], aux[:, O.AUX["y"]], aux[:, O.AUX["z"]]
+    Phi, p_ref = aux[:, O.AUX["Phi"]], aux[:, O.AUX["p_ref"]]
+    lam = np.arctan2(y, x)
+    phi = np.arcsin(z3 / np.sqrt(x * x + y * y + z3 * z3))
+    z = Phi / c["grav"]
+    beta = np.minimum(1.0, 3.0 * np.arccos(np.cos(phi) * np.cos(lam)))
+    p = p_ref + 100.0 * (1 + np.cos(np.pi * beta)) / 2 * np.sin(np.pi * z / H)
+    T = 300.0
+    Q = m.state()
+    rho = p / (c["R_d"] * T)
+    Q[:, 0] = rho
+    Q[:, 4] = rho * (c["cv_d"] * (T - c["T_0"]) + Phi)
+    cs = math.sqrt(c["cp_d"] / c["cv_d"] * c["R_d"] * T)
+    dt = 445 * (H / nv) / cs / N**2
+    dt = 3600 / math.ceil(3600 / dt)
+    return m, Q, dt, math.ceil(3600 / dt)
+
+
+@pytest.mark.parametrize("split", [False, True])
+def test_acoustic_wave_hevi_golden(split):
+    """acousticwave_1d_imex.jl (Float64, both splittings): N = 5, 10 x 10 x 6
+    x 5 cubed-shell elements, 36 ARK2GiraldoKellyConstantinescu steps of 100 s
+    with LinearBackwardEulerSolver(ManyColumnLU()) on the vertical
+    AtmosAcousticGravityLinearModel and a vertical ExponentialFilter(grid, 0,
+    18) after every step; ||Q|| after one hour.  The reference compares at
+    rtol sqrt(eps) and its model also carries a passive tracer rho chi = 1
+    whose weighted norm (3e-10 of ||Q||) is below that tolerance; the golden
+    value agrees with the norm of the five dry fields to 6e-13."""
+    m, Q, dt, nsteps = acoustic_wave()
+    assert (dt, nsteps) == (100.0, 36)
+    hv = O.OracleHevi(m, dt, split_explicit_implicit=split)
+    W = O.filter_matrix(m.N, "exponential", 0, 18)
+    for i in range(nsteps):
+        hv.step(Q, 1, i * dt)
+        O.apply_filter(m, Q, W, W, direction="vertical")
+    assert abs(m.norm(Q) / GOLDEN_ACOUSTIC_WAVE - 1) < 1e-11
+
+
+def test_column_lu_inverts_the_backward_euler_operator():
+    """besolver!: Q = Qhat + alpha L(Q) (BackwardEulerSolvers.jl) through the
+    band LU (columnwise_lu_solver.jl), checked with the operator itself."""
+    m, Q0, _, _ = acoustic_wave(nh=2, nv=3, N=3)
+    hv = O.OracleHevi(m, 80.0)
+    assert hv.bandwidth == 5 * 4 - 1
+    assert hv.alpha == 80.0 * (1 - 1 / math.sqrt(2))
+    rng = np.random.default_rng(4)
+    Qhat = Q0 * (1 + rng.uniform(-1e-3, 1e-3, size=Q0.shape))
+    Qhat[:, 1:4] = rng.uniform(-1, 1, size=Qhat[:, 1:4].shape)
+    Q = hv.solve(Qhat)
+    res = Q - hv.alpha * m.linear_tendency(Q) - Qhat
+    for s in range(5):
+        assert np.abs(res[:, s]).max() < 1e-11 * np.abs(Qhat[:, s]).max()
+
+
+def test_linear_model_is_linear_and_vertical():
+    m, Q0, _, _ = acoustic_wave(nh=2, nv=3, N=3)
+    rng = np.random.default_rng(9)
+    A = Q0 * (1 + rng.uniform(-1e-2, 1e-2, size=Q0.shape))
+    B = rng.uniform(-1, 1, size=Q0.shape)
+    LA, LB = m.linear_tendency(A), m.linear_tendency(B)
+    L = m.linear_tendency(2.0 * A - 3.0 * B)
+    scale = np.abs(2.0 * LA).max(axis=(0, 2))
+    assert (np.abs(L - (2.0 * LA - 3.0 * LB)).max(axis=(0, 2)) <= 1e-12 * scale + 1e-300).all()
+    # a state that varies only along one horizontal node line of one element
+    # changes the tendency of that line (and its vertical neighbours) only
+    E = np.zeros_like(Q0)
+    E[5, 4, 3] = 1.0                      # element 5, rhoe, node (i, j, k) = (3, 0, 0)
+    LE = m.linear_tendency(E)
+    Nq = m.Nq
+    touched = {(e, n % (Nq * Nq)) for e, s, n in zip(*np.nonzero(LE))}
+    assert touched and all(n == 3 for _, n in touched)
+    assert {e for e, _ in touched} <= {4, 5, 6}
