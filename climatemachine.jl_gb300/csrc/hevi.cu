@@ -26,9 +26,10 @@
 // the line are formed by the same thread, so the kernel needs no shared
 // memory and no barrier.  The band storage is line-fastest,
 // AB[(b * n + col) * nline + line] with band row b = bw + row - col, so that
-// the thread-per-line factorisation and substitutions read it coalesced; the
-// substitutions keep a window of bw + 1 right-hand-side values in registers
-// (the reference's l_b window).
+// the thread-per-line factorization and substitutions read it coalesced.
+// One thread per line keeps every lane of GB300's narrow FP64 pipe busy;
+// the substitutions skip the band entries that the element coupling makes
+// exact zeros (see fwd_len / bwd_len).
 #include <cmath>
 #include <vector>
 
@@ -247,39 +248,117 @@ __global__ void band_lu_kernel(double* AB, LineMap lm, int bw, unsigned* err) {
     }
 }
 
-// band_forward! then band_back! of one line per thread: b -> (L U)^-1 b.
-// y is a state-sized scratch; out may alias b; accumulate adds x to out.
-template <int Nq>
-__global__ void __launch_bounds__(128) band_solve_kernel(const double* __restrict__ AB, const double* b,
-                                                         double* __restrict__ y, double* out, LineMap lm,
-                                                         int accumulate) {
-    constexpr int BW = 5 * Nq - 1;
+// Structure of the factors.  The vertical operator couples the unknowns of
+// one element densely and neighbouring elements only through their facing
+// nodes: the bottom layer (k = 0, 5 unknowns, block positions 0..4) of
+// element v + 1 and the top layer of element v.  With block size
+// NB = 5 (N + 1) = bw + 1, the LU factors of a column at block position p
+// then have their non-zero band entries in contiguous runs:
+//   L(j + i, j), i = 1 .. fwd_len(p) = bw - max(0, p - 5)
+//   U(j - i, j), i = 1 .. bwd_len(p) = p < 5 ? bw : p
+// (the sub-diagonal block A(v+1, v) U(v, v)^-1 has rows only in the bottom
+// layer of v + 1; the super-diagonal block L(v, v)^-1 A(v, v+1) columns only
+// there).  Every other band entry is an exact zero, which
+// band_pattern_kernel verifies after the factorization.
+__host__ __device__ constexpr int fwd_len(int p, int bw) { return bw - (p > 5 ? p - 5 : 0); }
+__host__ __device__ constexpr int bwd_len(int p, int bw) { return p < 5 ? bw : p; }
+
+// checks the zero pattern and turns the pivots into their reciprocals (the
+// back substitution multiplies)
+__global__ void band_pattern_kernel(double* AB, LineMap lm, int bw, unsigned* err) {
     const int64_t line = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (line >= lm.nline) return;
-    const int n = lm.n;
-    const size_t NL = (size_t)lm.nline;
-    double w[BW + 1];
+    const int nb = bw + 1;
+    bool bad = false;
+    for (int col = 0; col < lm.n; ++col) {
+        const int p = col % nb;
+        for (int i = fwd_len(p, bw) + 1; i <= bw; ++i) bad |= band_at(AB, lm, bw, line, col + i, col) != 0;
+        for (int i = bwd_len(p, bw) + 1; i <= bw; ++i) bad |= band_at(AB, lm, bw, line, col - i, col) != 0;
+        double& d = band_at(AB, lm, bw, line, col, col);
+        d = 1.0 / d;
+    }
+    if (bad) atomicOr(err, 4u);
+}
+
+// one warp per CTA: the column count is small (a few warps per SM), so the
+// grid is spread evenly over the SMs
+constexpr int SOLVE_THREADS = 32;
+
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// columns ahead whose factor entries are prefetched into L2
+constexpr int SOLVE_PREFETCH = 3;
+
+// band_forward! then band_back! (Golub & Van Loan Alg. 4.3.2, 4.3.3), one
+// thread per line (all lanes do useful FP64 work), the factors read
+// coalesced across neighbouring lines.  The window of bw + 1 right-hand-side
+// values (the reference's l_b) is a register ring: row r lives in slot
+// r mod NB, and the loop over the NB positions of an element block is
+// unrolled, so every slot index and every run length is a compile-time
+// constant and only the structurally non-zero band entries are touched.
+// The factor entries SOLVE_PREFETCH columns ahead are prefetched into L2 (a
+// column count of a few warps per SM leaves nothing else to hide the DRAM
+// latency).  y is a state-sized scratch; out may alias b; accumulate adds
+// x to out.
+template <int Nq>
+__global__ void __launch_bounds__(SOLVE_THREADS) band_solve_kernel(const double* __restrict__ AB, const double* b,
+                                                                   double* __restrict__ y, double* out, LineMap lm,
+                                                                   int accumulate) {
+    constexpr int NB = 5 * Nq, BW = NB - 1;
+    const int64_t line = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (line >= lm.nline) return;
+    const int n = lm.n, nz = lm.nz;
+    const size_t NL = (size_t)lm.nline, RS = (size_t)n * NL;  // column and band-row strides
+    const double* A = AB + line;
+    double w[NB];
 #pragma unroll
-    for (int ii = 0; ii <= BW; ++ii) w[ii] = ii < n ? b[line_index<Nq>(lm, line, ii)] : 0.0;
-    for (int jj = 0; jj < n; ++jj) {
+    for (int i = 0; i < NB; ++i) w[i] = b[line_index<Nq>(lm, line, i)];
+    for (int d = 0; d < SOLVE_PREFETCH && d < n; ++d)
+        for (int i = 1; i <= BW; ++i) prefetch_l2(A + (size_t)(BW + i) * RS + (size_t)d * NL);
+    for (int v = 0; v < nz; ++v) {
 #pragma unroll
-        for (int ii = 1; ii <= BW; ++ii) w[ii] -= AB[((size_t)(BW + ii) * n + jj) * NL + line] * w[0];
-        y[line_index<Nq>(lm, line, jj)] = w[0];
+        for (int p = 0; p < NB; ++p) {
+            const int jj = v * NB + p;
+            if (jj + SOLVE_PREFETCH < n) {
+                const double* Ap = A + (size_t)(jj + SOLVE_PREFETCH) * NL;
 #pragma unroll
-        for (int ii = 0; ii < BW; ++ii) w[ii] = w[ii + 1];
-        w[BW] = (jj + BW + 1 < n) ? b[line_index<Nq>(lm, line, jj + BW + 1)] : 0.0;
+                for (int i = 1; i <= BW; ++i)
+                    if (i <= fwd_len((p + SOLVE_PREFETCH) % NB, BW)) prefetch_l2(Ap + (size_t)(BW + i) * RS);
+            }
+            const double* Aj = A + (size_t)jj * NL;
+            const double w0 = w[p];
+#pragma unroll
+            for (int i = 1; i <= BW; ++i)
+                if (i <= fwd_len(p, BW)) w[(p + i) % NB] -= Aj[(size_t)(BW + i) * RS] * w0;
+            y[line_index<Nq>(lm, line, jj)] = w0;
+            w[p] = (jj + NB < n) ? b[line_index<Nq>(lm, line, jj + NB)] : 0.0;
+        }
     }
 #pragma unroll
-    for (int ii = 0; ii <= BW; ++ii) w[BW - ii] = (n - 1 - ii >= 0) ? y[line_index<Nq>(lm, line, n - 1 - ii)] : 0.0;
-    for (int jj = n - 1; jj >= 0; --jj) {
-        w[BW] /= AB[((size_t)BW * n + jj) * NL + line];
+    for (int i = 0; i < NB; ++i) w[BW - i] = y[line_index<Nq>(lm, line, n - 1 - i)];
+    for (int d = 0; d < SOLVE_PREFETCH && d < n; ++d)
+        for (int i = 0; i <= BW; ++i) prefetch_l2(A + (size_t)(BW - i) * RS + (size_t)(n - 1 - d) * NL);
+    for (int v = nz - 1; v >= 0; --v) {
 #pragma unroll
-        for (int ii = 1; ii <= BW; ++ii) w[BW - ii] -= AB[((size_t)(BW - ii) * n + jj) * NL + line] * w[BW];
-        const size_t o = line_index<Nq>(lm, line, jj);
-        out[o] = accumulate ? out[o] + w[BW] : w[BW];
+        for (int p = NB - 1; p >= 0; --p) {
+            const int jj = v * NB + p;
+            if (jj - SOLVE_PREFETCH >= 0) {
+                const double* Ap = A + (size_t)(jj - SOLVE_PREFETCH) * NL;
 #pragma unroll
-        for (int ii = BW - 1; ii >= 0; --ii) w[ii + 1] = w[ii];
-        w[0] = (jj - BW - 1 >= 0) ? y[line_index<Nq>(lm, line, jj - BW - 1)] : 0.0;
+                for (int i = 0; i <= BW; ++i)
+                    if (i <= bwd_len((p + NB - SOLVE_PREFETCH) % NB, BW)) prefetch_l2(Ap + (size_t)(BW - i) * RS);
+            }
+            const double* Aj = A + (size_t)jj * NL;
+            const double x = w[p] * Aj[(size_t)BW * RS];  // reciprocal pivot
+#pragma unroll
+            for (int i = 1; i <= BW; ++i)
+                if (i <= bwd_len(p, BW)) w[(p - i + NB) % NB] -= Aj[(size_t)(BW - i) * RS] * x;
+            const size_t o = line_index<Nq>(lm, line, jj);
+            out[o] = accumulate ? out[o] + x : x;
+            w[p] = (jj - NB >= 0) ? y[line_index<Nq>(lm, line, jj - NB)] : 0.0;
+        }
     }
 }
 
@@ -465,7 +544,7 @@ struct Hevi {
     LineMap lm{};
     int bw = 0;
     size_t len = 0;
-    double* d_AB = nullptr;
+    double* d_AB = nullptr;   // band matrix, then its LU factors (reciprocal pivots), line-fastest
     double* d_buf = nullptr;  // S1, S2, R0, R1, R2, Qhat, Y
     unsigned* d_err = nullptr;
     double* S(int i) const { return d_buf + (size_t)(i - 1) * len; }          // i = 1, 2
@@ -497,6 +576,8 @@ int hevi_assemble_N(Hevi* h, cudaStream_t s) {
             }
     band_lu_kernel<<<(unsigned)((h->lm.nline + 127) / 128), 128, 0, s>>>(h->d_AB, h->lm, h->bw, h->d_err);
     CMDG_CUDA_CHECK(cudaGetLastError());
+    band_pattern_kernel<<<(unsigned)((h->lm.nline + 127) / 128), 128, 0, s>>>(h->d_AB, h->lm, h->bw, h->d_err);
+    CMDG_CUDA_CHECK(cudaGetLastError());
     return CMDG_OK;
 }
 
@@ -509,16 +590,21 @@ int hevi_assemble(Hevi* h, cudaStream_t s) {
     }
 }
 
-int hevi_solve(Hevi* h, const double* b, double* out, int accumulate, cudaStream_t s) {
-    const unsigned grid = (unsigned)((h->lm.nline + 127) / 128);
-    switch (h->md->mesh->N) {
-        case 2: band_solve_kernel<3><<<grid, 128, 0, s>>>(h->d_AB, b, h->Y(), out, h->lm, accumulate); break;
-        case 3: band_solve_kernel<4><<<grid, 128, 0, s>>>(h->d_AB, b, h->Y(), out, h->lm, accumulate); break;
-        case 4: band_solve_kernel<5><<<grid, 128, 0, s>>>(h->d_AB, b, h->Y(), out, h->lm, accumulate); break;
-        default: band_solve_kernel<6><<<grid, 128, 0, s>>>(h->d_AB, b, h->Y(), out, h->lm, accumulate); break;
-    }
+template <int Nq>
+int hevi_solve_N(Hevi* h, const double* b, double* out, int accumulate, cudaStream_t s) {
+    const unsigned grid = (unsigned)((h->lm.nline + SOLVE_THREADS - 1) / SOLVE_THREADS);
+    band_solve_kernel<Nq><<<grid, SOLVE_THREADS, 0, s>>>(h->d_AB, b, h->Y(), out, h->lm, accumulate);
     CMDG_CUDA_CHECK(cudaGetLastError());
     return CMDG_OK;
+}
+
+int hevi_solve(Hevi* h, const double* b, double* out, int accumulate, cudaStream_t s) {
+    switch (h->md->mesh->N) {
+        case 2: return hevi_solve_N<3>(h, b, out, accumulate, s);
+        case 3: return hevi_solve_N<4>(h, b, out, accumulate, s);
+        case 4: return hevi_solve_N<5>(h, b, out, accumulate, s);
+        default: return hevi_solve_N<6>(h, b, out, accumulate, s);
+    }
 }
 
 // rhs!: the full tendency, or the remainder f - l when split
@@ -653,8 +739,9 @@ int cmdg_hevi_create(cmdg_model* model, double dt, int split_explicit_implicit, 
         rc = CMDG_ERR_CUDA;
     }
     if (!rc && err) {
-        set_error(err & 1u ? "HEVI: the linear operator couples unknowns outside the column band"
-                           : "HEVI: zero or non-finite pivot in the column LU");
+        set_error((err & 1u)   ? "HEVI: the linear operator couples unknowns outside the column band"
+                  : (err & 2u) ? "HEVI: zero or non-finite pivot in the column LU"
+                               : "HEVI: the column LU factors have non-zeros outside the element-coupling pattern");
         rc = CMDG_ERR_NONFINITE;
     }
     if (rc) {
