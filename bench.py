@@ -39,6 +39,13 @@ default, the line the benchmark contract reads, is the bubble above):
   ensemble  64 seeded rising-bubble members of 8^3..16^3 elements and
             N = 3..5, mixed; batched (one graph of per-order launches) vs
             64 sequential single-member solves
+  hevi      the acoustic wave on the sphere of acousticwave_1d_imex.jl
+            (N = 5, 10 x 10 x 6 x 5 cubed-shell elements, 648,000 nodes,
+            FP64): ARK2GiraldoKellyConstantinescu steps of 100 s with the
+            vertical acoustic-gravity linear model solved by the column LU;
+            a stage is one of the 3 explicit stages of a step; the roofline
+            kernel is the band substitution, algorithmic bytes = the
+            structurally non-zero factor entries + the state words it moves
 
 Multi-GPU: replicas only — each rank advances its own bubble; value is the
 sum over ranks of the work divided by the slowest rank's time.
@@ -164,6 +171,151 @@ def bench_ensemble(args, cmdg, workloads, torch, barrier, stream, flush):
     return 0
 
 
+def bench_hevi(args, cmdg, workloads, torch, barrier, stream, flush):
+    """ARK2 + column-LU (HEVI) steps of the acoustic wave on the sphere, FP64;
+    beside it the explicit LSRK54 path of the same model at its own Courant
+    time step, as simulated seconds per wall-clock second."""
+    import numpy as np
+
+    dg = workloads.acoustic_wave_model()
+    dt, _ = workloads.acoustic_wave_dt()
+    Q0 = workloads.acoustic_wave_state(dg.grid.coordinates(), dg.reference_state()[:, 2])
+    lin = cmdg.DGModel(cmdg.AtmosAcousticGravityLinearModel(dg.balance_law), dg.grid, direction="vertical",
+                       state_auxiliary=dg)
+    Q = dg.init_ode_state(Q0)
+    ark = cmdg.ARK2GiraldoKellyConstantinescu(dg, lin, cmdg.LinearBackwardEulerSolver(cmdg.ManyColumnLU()), Q,
+                                              dt=dt)
+    nodes = dg.grid.nelem * dg.grid.Np
+    nz = dg.grid.ne[2]
+    NB = 5 * (dg.grid.N + 1)
+    fwd = sum(NB - 1 - max(0, p - 5) for p in range(NB))
+    bwd = sum((NB - 1 if p < 5 else p) + 1 for p in range(NB))
+    solve_bytes = 8 * ark.nline * (fwd + bwd) * nz + 8 * 5 * nodes * 5  # factors + b, y (w, r), out (r, w)
+
+    def step():
+        cmdg.dostep_(Q, ark, None, 0.0, 1)
+
+    for _ in range(args.warmup):
+        step()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        barrier()
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+        barrier()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    # the substitution alone, timed on its own (it is 2 of the ~9 launches of a step)
+    X = dg.new_state(torch.float64)
+    Qh = Q.clone()
+    for _ in range(3):
+        ark.backward_euler_solve(X, Qh)
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    s0.record(stream)
+    for _ in range(20):
+        ark.backward_euler_solve(X, Qh)
+    s1.record(stream)
+    barrier()
+    solve_ms = s0.elapsed_time(s1) / 20
+    # e2e: the FP64 state in pinned host memory, copied in and out every step
+    host = torch.from_numpy(np.ascontiguousarray(Q0)).pin_memory()
+    Qd = dg.init_ode_state(Q0)
+    ark_e = cmdg.ARK2GiraldoKellyConstantinescu(dg, lin, cmdg.LinearBackwardEulerSolver(cmdg.ManyColumnLU()), Qd,
+                                                dt=dt)
+
+    def e2e_step():
+        Qd.copy_(host, non_blocking=True)
+        cmdg.dostep_(Qd, ark_e, None, 0.0, 1)
+        host.copy_(Qd, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    ms_e2e = e0.elapsed_time(e1)
+    # the explicit alternative: LSRK54 at the model's Courant time step
+    Qx = dg.init_ode_state(Q0)
+    dt_x = dg.courant_dt(Qx, CFL)
+    lsrk = cmdg.LSRK54CarpenterKennedy(dg, Qx, dt=dt_x)
+    nx = 50
+    cmdg.dostep_(Qx, lsrk, None, 0.0, 3)
+    x0, x1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    x0.record(stream)
+    cmdg.dostep_(Qx, lsrk, None, 0.0, nx)
+    x1.record(stream)
+    barrier()
+    ms_x = x0.elapsed_time(x1)
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            sys.path.insert(0, os.path.join(REPO, "oracle"))
+            import oracle as O
+
+            O.set_threads(os.cpu_count())
+            R = O.EARTH["planet_radius"]
+            om = O.OracleModel(5, shell=dict(nhorz=10, nvert=5, r_inner=R, r_outer=R + 10e3), orientation="sphere",
+                               gravity=True, ref_state=True, profile="isothermal", T_surface=300.0)
+            ohv = O.OracleHevi(om, dt)
+            Qo = np.ascontiguousarray(Q0)
+            t0 = time.perf_counter()
+            ohv.step(Qo, 2)
+            el = time.perf_counter() - t0
+            cpu = {"value": NFIELD * om.nelem * om.Np * 3 * 2 / el, "unit": "DOF-stage/s", "cores": os.cpu_count(),
+                   "kind": "port", "sample": "2 ARK2 steps of the full acoustic-wave mesh, FP64 oracle "
+                                             "(factorization excluded)"}
+        except Exception as exc:
+            cpu = {"value": None, "error": str(exc)[:200]}
+
+    work = NFIELD * nodes * 3 * args.steps
+    peak, peak_kind = measured_peak()
+    ach = solve_bytes / (solve_ms * 1e-3) / 1e9
+    traffic = profile_traffic("hevi_band_solve_acoustic_wave.md")
+    line = {"metric": "DOF-stage updates/s", "value": work / (ms * 1e-3), "unit": "DOF-stage/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "acoustic wave on the sphere (acousticwave_1d_imex.jl): cubed shell 6x10x10x5, "
+                                   "N=5 (648,000 nodes), 10 km lid, isothermal 300 K, HEVI "
+                                   "ARK2GiraldoKellyConstantinescu, dt = 100 s, ManyColumnLU",
+                       "dt": dt, "stages_per_step": 3, "column_lines": ark.nline, "band_half_width": ark.bandwidth,
+                       "l2": "256 MiB buffer written between timed steps"},
+            "simulated_s_per_wall_s": dt * args.steps / (ms * 1e-3),
+            "explicit_lsrk54": {"dt": dt_x, "ms_per_step": ms_x / nx,
+                                "simulated_s_per_wall_s": dt_x * nx / (ms_x * 1e-3)},
+            "column_solve_ms": solve_ms,
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "traffic": traffic, "peak_source": peak_kind, "kernel": "band_solve_kernel<6>",
+                         "bytes_per_solve": solve_bytes},
+            "cpu_baseline": cpu,
+            "e2e": {"value": work / (ms_e2e * 1e-3), "unit": "DOF-stage/s", "h2d_bytes_per_step": int(host.numel() * 8),
+                    "d2h_bytes_per_step": int(host.numel() * 8)},
+            "gpu_launches": args.steps * 9, "clocks": clk.summary()}
+    print(json.dumps(line))
+    return 0
+
+
+def profile_traffic(name):
+    """DRAM bytes per launch of a profiled kernel, from its summary under profiles/."""
+    path = os.path.join(REPO, "profiles", name)
+    if os.path.exists(path):
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                try:
+                    return float(line.split(":", 1)[1].split()[0])
+                except ValueError:
+                    return None
+    return None
+
+
 def measured_peak():
     path = os.path.join(REPO, "MEASURED_PEAKS.json")
     try:
@@ -252,7 +404,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="cmdg", choices=["cmdg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="bubble", choices=["bubble", "gcm", "les", "hyper", "ensemble"])
+    ap.add_argument("--workload", default="bubble", choices=["bubble", "gcm", "les", "hyper", "ensemble", "hevi"])
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -300,6 +452,8 @@ def main():
 
     if args.workload == "ensemble":
         return bench_ensemble(args, cmdg, workloads, torch, barrier, stream, flush)
+    if args.workload == "hevi":
+        return bench_hevi(args, cmdg, workloads, torch, barrier, stream, flush)
 
     spec = WORKLOADS[args.workload]
 
@@ -395,15 +549,7 @@ def main():
     stage_ms_64 = ms_64 / args.steps / NSTAGE
     ach_mx = spec["bytes_mixed"] * nodes / (stage_ms_mx * 1e-3) / 1e9
     ach_64 = spec["bytes_fp64"] * nodes / (stage_ms_64 * 1e-3) / 1e9
-    traffic = None
-    tpath = os.path.join(REPO, "profiles", spec["profile"])
-    if os.path.exists(tpath):
-        for line in open(tpath):
-            if line.startswith("traffic_bytes_per_launch:"):
-                try:
-                    traffic = float(line.split(":", 1)[1].split()[0])
-                except ValueError:
-                    traffic = None
+    traffic = profile_traffic(spec["profile"])
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and args.workload == "bubble":
