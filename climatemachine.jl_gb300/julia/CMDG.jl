@@ -2,9 +2,11 @@
     CMDG
 
 Julia `ccall` shim over libcmdg.so (include/cmdg.h): a `SpaceDiscretization`
-whose functor runs the GPU DG tendency, and a `dostep!` method that runs a
-whole LSRK54CarpenterKennedy step in one fused GPU call.  `solve!`,
-callbacks and `invoke!` of ClimateMachine.jl are used unchanged.
+whose functor runs the GPU DG tendency, a `dostep!` method that runs a
+whole LSRK54CarpenterKennedy step in one fused GPU call, and the HEVI pair:
+the vertical acoustic-gravity linear model and an
+ARK2GiraldoKellyConstantinescu solver whose column LU lives on the GPU.
+`solve!`, callbacks and `invoke!` of ClimateMachine.jl are used unchanged.
 
 State arrays are the reference's `MPIStateArray.data` (`(Np, nstate,
 nelem)` CuArrays), passed by pointer.  Not exercised in this repository's
@@ -154,6 +156,54 @@ function dostep!(Q, lsrk::LowStorageRungeKutta2N{T, RT, AT, 5}, p, time) where {
     check(ccall((:cmdg_lsrk54_step, libcmdg), Cint,
                 (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, Cdouble, Cdouble, Cint, Ptr{Cvoid}),
                 dg.model, pointer(Q.data), pointer(lsrk.dQ.data), time, lsrk.dt, 1, stream_handle()))
+end
+
+"""
+    CMDGLinearModel(dg::CMDGModel)
+
+`DGModel(AtmosAcousticGravityLinearModel(model), grid, ...; direction =
+VerticalDirection(), state_auxiliary = dg.state_auxiliary)` on the GPU
+(Atmos/Model/linear.jl): its functor is `cmdg_linear_tendency`.
+"""
+struct CMDGLinearModel <: SpaceDiscretization
+    parent::CMDGModel
+end
+function (lm::CMDGLinearModel)(tendency, Q, _, t, α, β)
+    check(ccall((:cmdg_linear_tendency, libcmdg), Cint,
+                (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, Cdouble, Cdouble, Cdouble, Ptr{Cvoid}),
+                lm.parent.model, pointer(tendency.data), pointer(Q.data), t, α, β, stream_handle()))
+end
+(lm::CMDGLinearModel)(tendency, Q, p, t; increment = false) = lm(tendency, Q, p, t, true, increment)
+
+"""
+    CMDGHEVI(dg::CMDGModel, dt; t0 = 0, split_explicit_implicit = false, paperversion = false)
+
+Stands in for `ARK2GiraldoKellyConstantinescu(dg_or_rem_dg, lineardg,
+LinearBackwardEulerSolver(ManyColumnLU()), Q; dt, t0,
+split_explicit_implicit, paperversion)` (AdditiveRungeKuttaMethod.jl:
+839-897): the column LU of the vertical linear model is assembled and
+factored on the GPU at construction (`cmdg_hevi_create`) and each
+`dostep!` is `cmdg_hevi_step`.  Carries the `dt`, `t`, `steps` fields that
+`solve!` reads and updates.
+"""
+mutable struct CMDGHEVI <: AbstractODESolver
+    hevi::Ptr{Cvoid}
+    dg::CMDGModel
+    dt::Float64
+    t::Float64
+    steps::Int
+end
+function CMDGHEVI(dg::CMDGModel, dt; t0 = 0, split_explicit_implicit = false, paperversion = false)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:cmdg_hevi_create, libcmdg), Cint, (Ptr{Cvoid}, Cdouble, Cint, Cint, Ref{Ptr{Cvoid}}),
+                dg.model, dt, split_explicit_implicit, paperversion, h))
+    solver = CMDGHEVI(h[], dg, Float64(dt), Float64(t0), 0)
+    finalizer(x -> ccall((:cmdg_hevi_destroy, libcmdg), Cint, (Ptr{Cvoid},), x.hevi), solver)
+    return solver
+end
+function dostep!(Q, ark::CMDGHEVI, p, time)
+    check(ccall((:cmdg_hevi_step, libcmdg), Cint, (Ptr{Cvoid}, CuPtr{Float64}, Cdouble, Cint, Ptr{Cvoid}),
+                ark.hevi, pointer(Q.data), time, 1, stream_handle()))
 end
 
 """Compensated Σ M q over `fields` (weightedsum, MPIStateArrays.jl:655)."""
