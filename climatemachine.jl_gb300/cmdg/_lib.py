@@ -32,7 +32,7 @@ EXPORTS = (
     "cmdg_batch_lsrk54_step", "cmdg_batch_autotune",
     "cmdg_filter_matrix", "cmdg_apply_filter", "cmdg_apply_tmar",
     "cmdg_linear_tendency", "cmdg_hevi_create", "cmdg_hevi_destroy", "cmdg_hevi_info", "cmdg_hevi_solve",
-    "cmdg_hevi_step",
+    "cmdg_hevi_step", "cmdg_apply_mp_filter",
 )
 
 
@@ -133,6 +133,7 @@ def load(path: str | None = None):
         "cmdg_hevi_info": [P, ctypes.POINTER(D), ctypes.POINTER(I), ctypes.POINTER(ctypes.c_int64)],
         "cmdg_hevi_solve": [P, P, P, P],
         "cmdg_hevi_step": [P, P, D, I, P],
+        "cmdg_apply_mp_filter": [P, P, P, P, I, P, I, P],
     }
     for name, args in proto.items():
         fn = getattr(L, name)

@@ -66,6 +66,21 @@ class BoydVandevenFilter(_Spectral):
         super().__init__(grid, Nc, s)
 
 
+class MassPreservingCutoffFilter:
+    """MassPreservingCutoffFilter(grid, Nc=N) (Filters.jl:309-345): zeroes the
+    Legendre modes >= Nc and restores each element's mass-weighted integral
+    after each directional pass (for meshes with a non-constant Jacobian).
+    The matrices are modified_filter_matrix with sigma = 0: the cutoff
+    matrix, or the identity for Nc > N."""
+
+    def __init__(self, grid, Nc=None):
+        Nc = grid.N if Nc is None else Nc
+        Nc = (Nc, Nc) if isinstance(Nc, int) else tuple(Nc)
+        self.Nc = Nc
+        self.filter_matrices = tuple(np.eye(grid.N + 1) if c > grid.N else filter_matrix(grid.N, "cutoff", c)
+                                     for c in Nc)
+
+
 class TMARFilter:
     """Truncation and mass-aware rescaling (Filters.jl:369-407)."""
 
@@ -77,6 +92,12 @@ def apply_(Q, target, dg, filt, direction: str = "every"):
     arr = (ctypes.c_int * len(fields))(*fields)
     if isinstance(filt, TMARFilter):
         call("cmdg_apply_tmar", dg.h, _dptr(Q), arr, len(fields), _stream())
+        return Q
+    if isinstance(filt, MassPreservingCutoffFilter):
+        Wh = np.ascontiguousarray(filt.filter_matrices[0])
+        Wv = np.ascontiguousarray(filt.filter_matrices[1])
+        call("cmdg_apply_mp_filter", dg.h, _dptr(Q), ctypes.c_void_p(Wh.ctypes.data), ctypes.c_void_p(Wv.ctypes.data),
+             DIRECTIONS[direction], arr, len(fields), _stream())
         return Q
     Wh = np.ascontiguousarray(filt.filter_matrices[0])
     Wv = np.ascontiguousarray(filt.filter_matrices[1])

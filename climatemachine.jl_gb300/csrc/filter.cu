@@ -222,6 +222,80 @@ __global__ void __launch_bounds__(256) tmar_kernel(void* Qv, const double* emetr
     }
 }
 
+// MassPreservingCutoffFilter pass (Filters.jl:895-1065), FP64: one CTA per
+// element; the filtered fields are swept along xi1 and xi2 (horizontal) or
+// xi3 (vertical) with W in shared memory, then shifted by the element's lost
+// mass (sum M q_before - sum M q_after) / sum M, the three sums reduced in
+// the CTA.
+template <int N>
+__global__ void __launch_bounds__(((N + 1) * (N + 1) * (N + 1) + 31) / 32 * 32)
+    mp_filter_kernel(double* Qv, const double* emetric, const double* mnode, const double* w, const FilterArgs A) {
+    constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp;
+    constexpr int NT = (Np + 31) / 32 * 32;
+    constexpr int NW = NT / 32;
+    __shared__ double s_q[Np];
+    __shared__ double red[3][NW];
+    const int e = blockIdx.x, t = threadIdx.x;
+    const bool node = t < Np;
+    const int k = t / Nfp, j = (t - k * Nfp) / Nq, i = t - k * Nfp - j * Nq;
+    double* Q = Qv + (size_t)e * NSTATE * Np;
+    const double M = !node ? 0.0
+                     : mnode ? mnode[(size_t)e * Np + t]
+                             : (1.0 / (emetric[3 * e] * emetric[3 * e + 1] * emetric[3 * e + 2])) *
+                                   (w[i] * w[j] * w[k]);
+    auto sweep = [&](double v, int d) {
+        if (node) s_q[t] = v;
+        __syncthreads();
+        double acc = 0;
+        if (node) {
+            const int row = d == 0 ? i : (d == 1 ? j : k);
+            const int base = d == 0 ? Nq * (j + Nq * k) : (d == 1 ? i + Nfp * k : i + Nq * j);
+            const int st = d == 0 ? 1 : (d == 1 ? Nq : Nfp);
+#pragma unroll
+            for (int n = 0; n < Nq; ++n)
+                acc += (d == 2 ? A.Wv64[row * Nq + n] : A.Wh64[row * Nq + n]) * s_q[base + n * st];
+        }
+        __syncthreads();
+        return acc;
+    };
+    for (int s = 0; s < NSTATE; ++s) {
+        if (!((A.field_mask >> s) & 1u)) continue;
+        const double q = node ? Q[s * Np + t] : 0.0;
+        double v = q;
+        if (A.horizontal) {
+            v = sweep(v, 0);
+            v = sweep(v, 1);
+        } else {
+            v = sweep(v, 2);
+        }
+        // three sums: warp shuffles, then the warps' partials
+        double r0 = M * q, r1 = M * v, r2 = M;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            r0 += __shfl_down_sync(0xffffffffu, r0, off);
+            r1 += __shfl_down_sync(0xffffffffu, r1, off);
+            r2 += __shfl_down_sync(0xffffffffu, r2, off);
+        }
+        if ((t & 31) == 0) {
+            red[0][t >> 5] = r0;
+            red[1][t >> 5] = r1;
+            red[2][t >> 5] = r2;
+        }
+        __syncthreads();
+        if (t == 0) {
+            for (int wi = 1; wi < NW; ++wi) {
+                red[0][0] += red[0][wi];
+                red[1][0] += red[1][wi];
+                red[2][0] += red[2][wi];
+            }
+        }
+        __syncthreads();
+        const double Minv = 1 / red[2][0];
+        if (node) Q[s * Np + t] = v + Minv * (red[0][0] - red[1][0]);
+        __syncthreads();
+    }
+}
+
 }  // namespace
 
 static int field_mask_of(const int* fields, int nfields, unsigned* mask) {
@@ -320,6 +394,49 @@ extern "C" int cmdg_apply_filter(cmdg_model* model, void* d_Q, const double* h_W
         return CMDG_ERR_CUDA;
     }
     if (A.corr) CMDG_CUDA_CHECK(cudaStreamSynchronize(s));  // the host table may be rewritten by the next call
+    return CMDG_OK;
+}
+
+extern "C" int cmdg_apply_mp_filter(cmdg_model* model, double* d_Q, const double* h_Wh, const double* h_Wv,
+                                    int direction, const int* h_fields, int nfields, void* stream) {
+    CMDG_ARG_CHECK(model != nullptr && d_Q != nullptr && h_fields != nullptr, "NULL argument");
+    CMDG_ARG_CHECK(direction >= CMDG_DIR_EVERY && direction <= CMDG_DIR_VERTICAL, "unknown direction %d", direction);
+    Model* md = &model->m;
+    const Mesh& m = *md->mesh;
+    CMDG_ARG_CHECK(md->precision == CMDG_FP64, "the mass-preserving cutoff filter runs FP64 models");
+    const bool horiz = direction != CMDG_DIR_VERTICAL, vert = direction != CMDG_DIR_HORIZONTAL;
+    CMDG_ARG_CHECK(!horiz || h_Wh != nullptr, "horizontal filter matrix is NULL");
+    CMDG_ARG_CHECK(!vert || h_Wv != nullptr, "vertical filter matrix is NULL");
+    FilterArgs A{};
+    int rc = field_mask_of(h_fields, nfields, &A.field_mask);
+    if (rc) return rc;
+    const int Nq = m.Nq;
+    A.Q = d_Q;
+    A.nz = m.nz;
+    for (int i = 0; i < Nq * Nq; ++i) {
+        A.Wh64[i] = horiz ? h_Wh[i] : 0.0;
+        A.Wv64[i] = vert ? h_Wv[i] : 0.0;
+    }
+    if (!md->d_omega) {
+        CMDG_CUDA_CHECK(cudaMalloc(&md->d_omega, sizeof(double) * m.omega.size()));
+        CMDG_CUDA_CHECK(cudaMemcpy(md->d_omega, m.omega.data(), sizeof(double) * m.omega.size(), cudaMemcpyHostToDevice));
+    }
+    const double* mnode = m.kind == MESH_BRICK ? nullptr : md->d_mass;
+    CMDG_ARG_CHECK(m.kind == MESH_BRICK || mnode != nullptr, "no mass matrix on this mesh");
+    cudaStream_t s = (cudaStream_t)stream;
+    // horizontal pass, then vertical pass, each with its own mass restoration
+    for (int pass = 0; pass < 2; ++pass) {
+        if ((pass == 0 && !horiz) || (pass == 1 && !vert)) continue;
+        A.horizontal = pass == 0;
+        A.vertical = pass == 1;
+        switch (m.N) {
+            case 2: mp_filter_kernel<2><<<(unsigned)m.nelem, 32, 0, s>>>(d_Q, m.d_emetric, mnode, md->d_omega, A); break;
+            case 3: mp_filter_kernel<3><<<(unsigned)m.nelem, 64, 0, s>>>(d_Q, m.d_emetric, mnode, md->d_omega, A); break;
+            case 4: mp_filter_kernel<4><<<(unsigned)m.nelem, 128, 0, s>>>(d_Q, m.d_emetric, mnode, md->d_omega, A); break;
+            default: mp_filter_kernel<5><<<(unsigned)m.nelem, 224, 0, s>>>(d_Q, m.d_emetric, mnode, md->d_omega, A); break;
+        }
+        CMDG_CUDA_CHECK(cudaGetLastError());
+    }
     return CMDG_OK;
 }
 

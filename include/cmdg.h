@@ -267,13 +267,20 @@ int cmdg_batch_autotune(cmdg_batch* batch, void* const* h_Q, double* const* h_dQ
  * model; mixed needs Nc >= 1 horizontally) — Filters.apply!(Q, fields, grid,
  * filter; direction) (:408-505).  Any mesh for FP64 models (the filters act
  * along the element lines); mixed-precision models on brick meshes.
- * cmdg_apply_tmar: TMARFilter on the listed fields (:369-407, 794-892). */
+ * cmdg_apply_tmar: TMARFilter on the listed fields (:369-407, 794-892).
+ * cmdg_apply_mp_filter: MassPreservingCutoffFilter (:309-345, 542-606,
+ * 895-1065) with the cutoff matrices of cmdg_filter_matrix (the identity for
+ * Nc > N): a horizontal pass (xi1, xi2) and/or a vertical pass (xi3), each
+ * followed by the per-element shift that restores sum M q of every listed
+ * field; FP64 models, any mesh. */
 enum { CMDG_FILTER_EXPONENTIAL = 0, CMDG_FILTER_CUTOFF = 1, CMDG_FILTER_BOYD_VANDEVEN = 2 };
 enum { CMDG_DIR_EVERY = 0, CMDG_DIR_HORIZONTAL = 1, CMDG_DIR_VERTICAL = 2 };
 int cmdg_filter_matrix(int N, int kind, int Nc, int s, double alpha, double* h_W);
 int cmdg_apply_filter(cmdg_model* model, void* d_Q, const double* h_Wh, const double* h_Wv, int direction,
                       const int* h_fields, int nfields, void* stream);
 int cmdg_apply_tmar(cmdg_model* model, void* d_Q, const int* h_fields, int nfields, void* stream);
+int cmdg_apply_mp_filter(cmdg_model* model, double* d_Q, const double* h_Wh, const double* h_Wv, int direction,
+                         const int* h_fields, int nfields, void* stream);
 
 /* HEVI (horizontally explicit, vertically implicit) stepping, FP64 models with
  * a hydrostatic reference state on wall-bounded element stacks (cubed shell,

@@ -2303,6 +2303,61 @@ void om_apply_filter(const om_model* m, double* Q, const double* Wh, const doubl
     }
 }
 
+// MassPreservingCutoffFilter (Filters.jl:316-345, 542-606, 895-1065): one
+// pass per direction class (horizontal: xi1 then xi2 with Wh; vertical: xi3
+// with Wv; both for every direction, horizontal first), each followed by
+// the shift that restores the element's mass-weighted integral of every
+// filtered field: q += (sum M q_before - sum M q_after) / sum M.
+void om_apply_mp_filter(const om_model* m, double* Q, const double* Wh, const double* Wv, int direction,
+                        const int* fields, int nfields) {
+    const int Nq = m->Nq, Np = m->Np;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < m->nelem; ++e) {
+        std::vector<double> a(Np), b(Np);
+        double Ms = 0;
+        for (int n = 0; n < Np; ++n) Ms += VGc(*m, e, VM, n);
+        for (int pass = 0; pass < 2; ++pass) {
+            const bool horiz = pass == 0;
+            if (horiz && direction == 2) continue;
+            if (!horiz && direction == 1) continue;
+            for (int fi = 0; fi < nfields; ++fi) {
+                double* q = Q + ((size_t)e * NS + fields[fi]) * Np;
+                double before = 0;
+                for (int n = 0; n < Np; ++n) {
+                    a[n] = q[n];
+                    before += VGc(*m, e, VM, n) * q[n];
+                }
+                auto sweep = [&](const double* W, int d) {
+                    for (int k = 0; k < Nq; ++k)
+                        for (int j = 0; j < Nq; ++j)
+                            for (int i = 0; i < Nq; ++i) {
+                                const int ijk = i + Nq * (j + Nq * k);
+                                const int row = d == 0 ? i : (d == 1 ? j : k);
+                                double acc = 0;
+                                for (int n = 0; n < Nq; ++n) {
+                                    const int src = d == 0 ? n + Nq * (j + Nq * k)
+                                                           : (d == 1 ? i + Nq * (n + Nq * k) : i + Nq * (j + Nq * n));
+                                    acc += W[row * Nq + n] * a[src];
+                                }
+                                b[ijk] = acc;
+                            }
+                    a.swap(b);
+                };
+                if (horiz) {
+                    sweep(Wh, 0);
+                    sweep(Wh, 1);
+                } else {
+                    sweep(Wv, 2);
+                }
+                double after = 0;
+                for (int n = 0; n < Np; ++n) after += VGc(*m, e, VM, n) * a[n];
+                const double Minv = 1 / Ms;
+                for (int n = 0; n < Np; ++n) q[n] = a[n] + Minv * (before - after);
+            }
+        }
+    }
+}
+
 // TMARFilter, kernel_apply_TMAR_filter! (Filters.jl:794-892): per element
 // and field, r = sum(M q) / sum(M max(q, 0)) (0 when sum(M q) <= 0) and
 // q <- r q where q >= 0, 0 elsewhere.

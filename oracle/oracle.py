@@ -156,6 +156,7 @@ def lib():
         ip = ctypes.POINTER(ctypes.c_int)
         L.om_apply_filter.argtypes = [P, dp, dp, dp, ctypes.c_int, ip, ctypes.c_int]
         L.om_apply_tmar.argtypes = [P, dp, ip, ctypes.c_int]
+        L.om_apply_mp_filter.argtypes = [P, dp, dp, dp, ctypes.c_int, ip, ctypes.c_int]
         L.om_create_scalar_hyper.restype = P
         L.om_create_scalar_hyper.argtypes = [ctypes.POINTER(Brick), dp, ctypes.c_int]
         L.om_scalar_hyper_tendency.argtypes = [P, dp, dp, D, D]
@@ -441,6 +442,16 @@ def apply_filter(model, Q, Wh, Wv, direction="every", fields=(0, 1, 2, 3, 4)):
     Wh = np.ascontiguousarray(Wh, dtype=np.float64)
     Wv = np.ascontiguousarray(Wv, dtype=np.float64)
     lib().om_apply_filter(model.h, _ptr(Q), _ptr(Wh), _ptr(Wv), d, arr, n)
+    return Q
+
+
+def apply_mp_filter(model, Q, Wh, Wv, direction="every", fields=(0, 1, 2, 3, 4)):
+    """MassPreservingCutoffFilter application (Filters.jl:542-606, 895-1065)."""
+    arr, n = _fields(fields)
+    Wh = np.ascontiguousarray(Wh, dtype=np.float64)
+    Wv = np.ascontiguousarray(Wv, dtype=np.float64)
+    lib().om_apply_mp_filter(model.h, _ptr(Q), _ptr(Wh), _ptr(Wv), {"every": 0, "horizontal": 1, "vertical": 2}[direction],
+                             arr, n)
     return Q
 
 

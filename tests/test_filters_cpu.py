@@ -65,3 +65,42 @@ def test_oracle_cutoff_filter_known_answer(direction):
         assert np.abs(Q[:, s] - keep).max() < 1e-12
     for s in (1, 3):
         assert np.abs(Q[:, s] - (low + hh + hv)).max() == 0
+
+
+@pytest.mark.parametrize("direction", ["every", "horizontal", "vertical"])
+def test_oracle_mass_preserving_cutoff_known_answer(direction):
+    """filter.jl "Mass Preserving Cutoff filter application": on an affine
+    element the removed Legendre modes carry no mass, so the result is the
+    cutoff result (N = 3, Nc = 2, fields 1 and 3 of 4 in the reference)."""
+    om = O.OracleModel(3, (1, 1, 1), (-1, -1, -1), (1, 1, 1), periodic=(1, 1, 1))
+    low, hh, hv = legendre_fields(om.vgeo[:, 12:15])
+    Q = np.stack([low + hh + hv] * 5, axis=1)
+    W = O.filter_matrix(3, "cutoff", 2)
+    O.apply_mp_filter(om, Q, W, W, direction, fields=(0, 2))
+    keep = {"every": low, "horizontal": low + hv, "vertical": low + hh}[direction]
+    for s in (0, 2):
+        assert np.abs(Q[:, s] - keep).max() < 1e-12
+    for s in (1, 3, 4):
+        assert np.abs(Q[:, s] - (low + hh + hv)).max() == 0
+
+
+def test_oracle_mass_preserving_cutoff_keeps_mass_on_the_shell():
+    """filter.jl "MassPreservingCutoffFilter on the sphere": on the cubed shell
+    (non-constant Jacobian, radii 1 and 1.2) the mass-preserving filter keeps
+    every field's weighted sum, the plain cutoff filter does not."""
+    om = O.OracleModel(4, shell=dict(nhorz=1, nvert=1, r_inner=1.0, r_outer=1.2))
+    xyz = om.vgeo[:, 12:15]
+    low, hh, hv = legendre_fields(xyz)
+    x, y = xyz[:, 0], xyz[:, 1]
+    # fields without the shell's symmetries (their per-element losses must not cancel)
+    Q0 = np.stack([low + hh + hv + 3 * x, np.exp(1.5 * x + 0.5 * y), (x + 2) ** 4 * (y + 1.5) ** 2, low, hh], axis=1)
+    W = O.filter_matrix(4, "cutoff", 2)
+    fields = (0, 1, 2)
+    Q = Q0.copy()
+    O.apply_mp_filter(om, Q, W, W, "every", fields=fields)
+    Qc = Q0.copy()
+    O.apply_filter(om, Qc, W, W, "every", fields=fields)
+    for s in fields:
+        before = om.weightedsum(Q0, s)
+        assert abs(om.weightedsum(Q, s) - before) <= 1e-13 * abs(before) + 1e-15
+        assert abs(om.weightedsum(Qc, s) - before) > 1e-8 * abs(before)

@@ -1,7 +1,9 @@
 """GPU filters against the oracle: spectral filters (exponential, cutoff,
 Boyd-Vandeven; every, horizontal, vertical direction; field subsets) on the
 FP64 state within 1e-13 and on the mixed-precision perturbation within 1e-6,
-the CutoffFilter known answer, and TMAR."""
+the CutoffFilter known answer, TMAR, and the MassPreservingCutoffFilter
+(oracle parity on bricks and on the cubed shell, mass kept per field, the
+vertical exponential filter on the shell)."""
 import numpy as np
 import pytest
 import torch
@@ -92,3 +94,57 @@ def test_tmar_matches_oracle():
     got = Q.cpu().numpy()
     assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
     assert (got[:, 3] >= 0).all()
+
+
+@pytest.mark.parametrize("direction", ["every", "horizontal", "vertical"])
+def test_mass_preserving_cutoff_matches_oracle_on_brick(direction):
+    om, dg, Q0 = pair()
+    filt = filters.MassPreservingCutoffFilter(dg.grid, 2)
+    Q = dg.init_ode_state(Q0)
+    filters.apply_(Q, (0, 1, 4), dg, filt, direction)
+    ref = O.apply_mp_filter(om, Q0.copy(), filt.filter_matrices[0], filt.filter_matrices[1], direction, (0, 1, 4))
+    assert rel(Q.cpu().numpy(), ref).max() < 1e-13
+
+
+def shell_pair(N=4):
+    R = O.EARTH["planet_radius"]
+    om = O.OracleModel(N, shell=dict(nhorz=2, nvert=2, r_inner=R, r_outer=R + 30e3), orientation="sphere",
+                       gravity=True, ref_state=True, profile="isothermal", T_surface=285.0)
+    dg = workloads.gcm_shell_model(nhorz=2, nvert=2, N=N)
+    Q0 = workloads.gcm_initial_state(dg.grid.coordinates(), seed=3)
+    return om, dg, Q0
+
+
+def test_mass_preserving_cutoff_on_the_shell_matches_oracle_and_keeps_mass():
+    om, dg, Q0 = shell_pair()
+    filt = filters.MassPreservingCutoffFilter(dg.grid, 2)
+    Q = dg.init_ode_state(Q0)
+    before = dg.weighted_sums(Q, (0, 1, 2, 3, 4))
+    filters.apply_(Q, (0, 1, 2, 3, 4), dg, filt, "every")
+    after = dg.weighted_sums(Q, (0, 1, 2, 3, 4))
+    ref = O.apply_mp_filter(om, Q0.copy(), filt.filter_matrices[0], filt.filter_matrices[1], "every")
+    assert rel(Q.cpu().numpy(), ref).max() < 1e-12
+    for b, a in zip(before, after):
+        # compensated sums over 41k nodes of a field whose sum cancels partly
+        assert abs(a - b) <= 1e-11 * max(abs(b), 1.0)
+    # the plain cutoff filter changes the weighted sums on the curved mesh
+    Qc = dg.init_ode_state(Q0)
+    filters.apply_(Qc, (0, 4), dg, filters.CutoffFilter(dg.grid, 2), "every")
+    c = dg.weighted_sums(Qc, (0, 4))
+    assert abs(c[0] - before[0]) > 1e-9 * abs(before[0])
+
+
+def test_fp64_filters_run_on_the_shell():
+    om, dg, Q0 = shell_pair(5)
+    filt = filters.ExponentialFilter(dg.grid, 0, 18)
+    Q = dg.init_ode_state(Q0)
+    filters.apply_(Q, (0, 1, 2, 3, 4), dg, filt, "vertical")
+    ref = O.apply_filter(om, Q0.copy(), filt.filter_matrices[0], filt.filter_matrices[1], "vertical")
+    assert rel(Q.cpu().numpy(), ref).max() < 1e-13
+
+
+def test_mass_preserving_cutoff_refuses_mixed_models():
+    _, dgm, Q0 = pair(precision="mixed")
+    Qp = dgm.init_ode_state(Q0)
+    with pytest.raises(cmdg.CmdgError):
+        filters.apply_(Qp, (0,), dgm, filters.MassPreservingCutoffFilter(dgm.grid, 2))
