@@ -157,8 +157,6 @@ class DGModel:
             # parent model's tables (no model of its own)
             if direction != "vertical" or not isinstance(state_auxiliary, DGModel):
                 raise ValueError("the linear model runs in direction='vertical' with state_auxiliary=<its DGModel>")
-            if state_auxiliary.mixed:
-                raise ValueError("the linear model runs FP64 models")
             self.balance_law, self.grid, self.numerical_flux = balance_law, grid, numerical_flux
             self.precision, self.mixed, self.direction = "fp64", False, direction
             self.parent = state_auxiliary

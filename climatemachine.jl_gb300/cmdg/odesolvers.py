@@ -78,7 +78,9 @@ class ARK2GiraldoKellyConstantinescu:
     split_explicit_implicit, variant = LowStorageVariant(), paperversion)
     (AdditiveRungeKuttaMethod.jl:839-897): F the full DGModel (or
     remainder_DGModel(dg, (lineardg,)) with split_explicit_implicit=True),
-    L the vertical linear DGModel of the same model."""
+    L the vertical linear DGModel of the same model.  Q is the FP64 state;
+    with a mixed-precision dg the explicit tendencies run on its FP32
+    perturbation (the stage algebra and the column solve stay FP64)."""
 
     def __init__(self, F, L, backward_euler_solver, Q: torch.Tensor, dt: float = None, t0: float = 0.0,
                  split_explicit_implicit: bool = False, variant=None, paperversion: bool = False):

@@ -169,16 +169,17 @@ def gcm_initial_state(xyz: np.ndarray, *, seed=2024, T_ref=285.0, u_max=30.0, dT
     return Q
 
 
-def acoustic_wave_model(nhorz=10, nvert=5, N=5, H=10e3, T_ref=300.0):
+def acoustic_wave_model(nhorz=10, nvert=5, N=5, H=10e3, T_ref=300.0, precision="fp64"):
     """The acoustic wave on the sphere of
     test/Numerics/DGMethods/Euler/acousticwave_1d_imex.jl: stacked cubed
-    shell (nhorz x nhorz per cube face, nvert levels, lid H), FP64,
+    shell (nhorz x nhorz per cube face, nvert levels, lid H),
     SphericalOrientation + Gravity, HydrostaticState(IsothermalProfile(T_ref)),
-    inviscid, Rusanov flux, walls at both radii."""
+    inviscid, Rusanov flux, walls at both radii.  precision="mixed" runs the
+    explicit tendency of HEVI steps on the FP32 perturbation."""
     R = EARTH["planet_radius"]
     grid = CubedShellGrid(N, nhorz, nvert, R, R + H)
     model = AtmosModel(orientation="sphere", gravity=True, ref_state=HydrostaticState(IsothermalProfile(T_ref)))
-    return DGModel(model, grid, numerical_flux="rusanov", precision="fp64")
+    return DGModel(model, grid, numerical_flux="rusanov", precision=precision)
 
 
 def acoustic_wave_state(xyz: np.ndarray, p_ref: np.ndarray, *, H=10e3, T_ref=300.0, alpha=3.0, gamma=100.0,

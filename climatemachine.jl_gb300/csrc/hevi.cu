@@ -1,4 +1,4 @@
-// HEVI time stepping (sm_103a, FP64): the AtmosAcousticGravityLinearModel
+// HEVI time stepping (sm_103a): the AtmosAcousticGravityLinearModel
 // as a DGModel in VerticalDirection, its column-wise banded LU, and
 // ARK2GiraldoKellyConstantinescu in the LowStorageVariant.
 //
@@ -18,6 +18,12 @@
 //                     by band forward / back substitution (Alg. 4.3.2, 4.3.3).
 //   ARK scheme        ODESolvers/AdditiveRungeKuttaMethod.jl:413-538 (stage
 //                     and solution updates :559-662), tableau :839-897.
+//
+// Precision: the state, the ARK stage algebra, the linear operator and the
+// column LU are FP64.  The explicit tendency is FP64 on an FP64 model, or
+// the mixed kernels (FP32 perturbation about the FP64 reference state, FP64
+// output) on a mixed model: GB300's FP64 pipe is narrow and the explicit
+// tendency is the larger part of a step.
 //
 // GPU mapping.  A vertical line is the (i, j) node column of one element
 // stack: nz elements x Nq levels x 5 states = n unknowns, r = s + 5 (k + Nq v).
@@ -406,7 +412,6 @@ int init_linear_tables(Model* md) {
     if (md->d_lin64) return CMDG_OK;
     const Mesh& m = *md->mesh;
     const cmdg_atmos_params& p = md->prm;
-    CMDG_ARG_CHECK(md->precision == CMDG_FP64, "the linear model and HEVI run FP64 models");
     CMDG_ARG_CHECK(p.ref_state != 0, "AtmosAcousticGravityLinearModel needs a model with a reference state");
     if (m.kind != MESH_BRICK && m.kind != MESH_SHELL) {
         set_error("the linear model runs on brick and cubed-shell meshes");
@@ -546,6 +551,7 @@ struct Hevi {
     size_t len = 0;
     double* d_AB = nullptr;   // band matrix, then its LU factors (reciprocal pivots), line-fastest
     double* d_buf = nullptr;  // S1, S2, R0, R1, R2, Qhat, Y
+    float* d_Sp = nullptr;    // mixed models: FP32 perturbation of the stage state
     unsigned* d_err = nullptr;
     double* S(int i) const { return d_buf + (size_t)(i - 1) * len; }          // i = 1, 2
     double* R(int i) const { return d_buf + (size_t)(2 + i) * len; }          // i = 0..2
@@ -607,10 +613,20 @@ int hevi_solve(Hevi* h, const double* b, double* out, int accumulate, cudaStream
     }
 }
 
-// rhs!: the full tendency, or the remainder f - l when split
+// rhs!: the full tendency, or the remainder f - l when split.  A mixed
+// model evaluates the explicit tendency on the FP32 perturbation of the FP64
+// stage state (FP64 output); the ARK algebra and the solve stay FP64.
 int hevi_rhs(Hevi* h, double* R, const double* Q, cudaStream_t s) {
-    LaunchArgs a{Q, nullptr, R, 1.0, 0.0, 0.0, 0.0, 0, 0, 0};
-    int rc = launch_stage(h->md, a, s);
+    int rc;
+    if (h->md->precision == CMDG_MIXED) {
+        rc = launch_to_perturbation(h->md, h->d_Sp, Q, s);
+        if (rc) return rc;
+        LaunchArgs a{h->d_Sp, nullptr, R, 1.0, 0.0, 0.0, 0.0, 0, 0, 0};
+        rc = launch_stage(h->md, a, s);
+    } else {
+        LaunchArgs a{Q, nullptr, R, 1.0, 0.0, 0.0, 0.0, 0, 0, 0};
+        rc = launch_stage(h->md, a, s);
+    }
     if (rc) return rc;
     if (h->split) return launch_linear_tendency(h->md, Q, R, -1.0, 1.0, s);
     return CMDG_OK;
@@ -719,7 +735,8 @@ int cmdg_hevi_create(cmdg_model* model, double dt, int split_explicit_implicit, 
     cudaError_t e1 = cudaMalloc(&h->d_AB, sizeof(double) * ab);
     cudaError_t e2 = cudaMalloc(&h->d_buf, sizeof(double) * 7 * h->len);
     cudaError_t e3 = cudaMalloc(&h->d_err, sizeof(unsigned));
-    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+    cudaError_t e4 = md->precision == CMDG_MIXED ? cudaMalloc(&h->d_Sp, sizeof(float) * h->len) : cudaSuccess;
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) {
         cudaGetLastError();
         cmdg_hevi_destroy(ho);
         set_error("HEVI: device allocation of %zu bytes failed", sizeof(double) * (ab + 7 * h->len));
@@ -756,6 +773,7 @@ int cmdg_hevi_destroy(cmdg_hevi* hevi) {
     if (!hevi) return CMDG_OK;
     cudaFree(hevi->h.d_AB);
     cudaFree(hevi->h.d_buf);
+    cudaFree(hevi->h.d_Sp);
     cudaFree(hevi->h.d_err);
     delete hevi;
     return CMDG_OK;

@@ -282,9 +282,12 @@ int cmdg_apply_tmar(cmdg_model* model, void* d_Q, const int* h_fields, int nfiel
 int cmdg_apply_mp_filter(cmdg_model* model, double* d_Q, const double* h_Wh, const double* h_Wv, int direction,
                          const int* h_fields, int nfields, void* stream);
 
-/* HEVI (horizontally explicit, vertically implicit) stepping, FP64 models with
- * a hydrostatic reference state on wall-bounded element stacks (cubed shell,
- * or a brick non-periodic in z).
+/* HEVI (horizontally explicit, vertically implicit) stepping of FP64 states,
+ * for models with a hydrostatic reference state on wall-bounded element
+ * stacks (cubed shell, or a brick non-periodic in z).  The linear operator,
+ * the column LU and the ARK stage algebra are FP64; a mixed-precision model
+ * evaluates the explicit tendency on the FP32 perturbation of each stage
+ * state (cmdg_tendency_mixed semantics), an FP64 model in FP64.
  *
  * cmdg_linear_tendency: d_dQ = alpha * L(d_Q) + beta * d_dQ, the tendency of
  * AtmosAcousticGravityLinearModel(model) as a DGModel in VerticalDirection

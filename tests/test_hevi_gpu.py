@@ -15,8 +15,10 @@
   (N = 5, 10 x 10 x 6 x 5 cubed-shell elements, 36 ARK2 steps of 100 s with
   ManyColumnLU and a vertical exponential filter of order 18): the norm of
   the state after one hour against the reference's golden value;
-* configuration errors (mixed precision, periodic columns, no reference
-  state) are refused with an error code.
+* the same with the explicit tendency on a mixed model's FP32 perturbation:
+  the golden norm to 1e-9; rho, rhoe within 1e-6 and the momentum within
+  5e-5 of the FP64 run;
+* configuration errors (periodic columns, no reference state) are refused.
 """
 import math
 
@@ -202,12 +204,50 @@ def test_acoustic_wave_hevi_golden(split):
     assert abs(n / GOLDEN_ACOUSTIC_WAVE - 1) < 1e-11, n
 
 
+def test_mixed_explicit_part_acoustic_wave_golden():
+    """HEVI with the explicit tendency on the FP32 perturbation (mixed model):
+    the one-hour acoustic wave keeps the golden norm to 1e-9 (the reference's
+    own check is rtol sqrt(eps) = 1.5e-8) and stays close (relative L2 per
+    field group) to the FP64 run."""
+    dt, nsteps = workloads.acoustic_wave_dt()
+    out = {}
+    for precision in ("fp64", "mixed"):
+        dg = workloads.acoustic_wave_model(precision=precision)
+        Q0 = workloads.acoustic_wave_state(dg.grid.coordinates(), dg.reference_state()[:, 2])
+        Q = torch.from_numpy(Q0).to("cuda")
+        lin = linear_dg(dg)
+        ark = cmdg.ARK2GiraldoKellyConstantinescu(dg, lin, cmdg.LinearBackwardEulerSolver(cmdg.ManyColumnLU()), Q,
+                                                  dt=dt)
+        filt = ExponentialFilter(dg.grid, 0, 18)
+
+        def cbfilter(solver, Q, dg=dg, filt=filt):
+            apply_(Q, (0, 1, 2, 3, 4), dg, filt, direction="vertical")
+
+        # the filter of a mixed model acts on its FP32 perturbation: filter a
+        # FP64 model's copy of the state instead, so both runs filter alike
+        if precision == "mixed":
+            dg64 = workloads.acoustic_wave_model()
+
+            def cbfilter(solver, Q, dg64=dg64, filt=filt):  # noqa: F811
+                apply_(Q, (0, 1, 2, 3, 4), dg64, filt, direction="vertical")
+
+        cmdg.solve_(Q, ark, numberofsteps=nsteps, adjustfinalstep=False, callbacks=(cbfilter,))
+        out[precision] = (dg, Q)
+    dg64, Q64 = out["fp64"]
+    n = cmdg.norm(dg64, out["mixed"][1])
+    assert abs(n / GOLDEN_ACOUSTIC_WAVE - 1) < 1e-9, n
+    a, b = out["mixed"][1].cpu().numpy(), Q64.cpu().numpy()
+    M = dg64.grid.mass()
+    # rho and rhoe to 1e-6; the momentum, a small acoustic residual of the
+    # FP32 perturbation tendency's pressure-gradient / buoyancy balance, to
+    # 5e-5 (measured 1.8e-5 after the hour)
+    for sl, tol in ((slice(0, 1), 1e-6), (slice(1, 4), 5e-5), (slice(4, 5), 1e-6)):
+        err = math.sqrt(float(np.sum((a[:, sl] - b[:, sl]) ** 2 * M[:, None, :])))
+        ref = math.sqrt(float(np.sum(b[:, sl] ** 2 * M[:, None, :])))
+        assert err <= tol * ref, (sl, err / ref)
+
+
 def test_hevi_configuration_errors():
-    # mixed precision
-    dgm = workloads.gcm_shell_model(nhorz=2, nvert=2, N=3, precision="mixed")
-    with pytest.raises(ValueError):
-        cmdg.DGModel(cmdg.AtmosAcousticGravityLinearModel(dgm.balance_law), dgm.grid, direction="vertical",
-                     state_auxiliary=dgm)
     # periodic columns have no wall-bounded stacks
     grid = cmdg.BrickGrid(3, (2, 2, 2), (0, 0, 0), (1000.0, 1000.0, 1000.0), periodicity=(True, True, True))
     model = cmdg.AtmosModel(orientation="flat", gravity=True, ref_state=cmdg.HydrostaticState())
