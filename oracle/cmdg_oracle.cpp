@@ -1,10 +1,12 @@
 // cmdg oracle — TEST INFRASTRUCTURE ONLY.
 //
 // A plain-C++ FP64 restatement of ClimateMachine.jl's DG spectral-element
-// tendency for the dry AtmosModel (DGModel volume/interface kernels, gradient
-// and diffusive passes), its LSRK54CarpenterKennedy integrator, the brick and
-// stacked cubed-shell geometry it runs on and the weighted reductions used to
-// report errors.
+// tendency for the dry AtmosModel (DGModel volume/interface kernels, gradient,
+// diffusive and hyperdiffusion passes), its LSRK54CarpenterKennedy
+// integrator, the HEVI scheme (vertical acoustic-gravity linear model, column
+// LU, ARK2GiraldoKellyConstantinescu), the modal filters, the brick and
+// stacked cubed-shell geometry it runs on and the weighted reductions used
+// to report errors.
 //
 // It is the checker for the CUDA library: only tests/, __graft_entry__.smoke()
 // and bench.py's CPU-baseline leg may load it.  Nothing in the product path
@@ -17,9 +19,13 @@
 // (viscous path, warped brick), the 3D hyperdiffusion golden errors of
 // test/Numerics/DGMethods/advection_diffusion/periodic_3D_hyperdiffusion.jl,
 // the LSRK54 convergence order of
-// test/Numerics/ODESolvers/ode_tests_convergence.jl:41 and the discrete
+// test/Numerics/ODESolvers/ode_tests_convergence.jl:41, the discrete
 // hydrostatic balance of test/Atmos/Model/discrete_hydrostatic_balance.jl
-// (LES brick and GCM cubed shell) are reproduced by tests/test_oracle_pins.py.
+// (LES brick and GCM cubed shell) and the HEVI acoustic-wave golden norm of
+// test/Numerics/DGMethods/Euler/acousticwave_1d_imex.jl (vertical linear
+// model, column LU, ARK2GiraldoKellyConstantinescu, vertical filter) are
+// reproduced by tests/test_oracle_pins.py; the filters by
+// tests/test_filters_cpu.py against test/Numerics/Mesh/filter.jl.
 //
 // Every function cites the reference file:line (paths relative to the
 // ClimateMachine.jl project root) whose algorithm it restates.  Third-party
