@@ -218,6 +218,11 @@ int set_arrays_reference(Model* md, const double* aux7) {
     CMDG_CUDA_CHECK(cudaMemcpy(md->d_ref64, md->ref64.data(), sizeof(double) * md->ref64.size(), cudaMemcpyHostToDevice));
     CMDG_CUDA_CHECK(cudaMemcpy(md->d_fjump, jump.data(), sizeof(float) * jump.size(), cudaMemcpyHostToDevice));
     md->has_reference = true;
+    // the linear model's tables hold the previous reference state
+    cudaFree(md->d_lin64);
+    cudaFree(md->d_linface64);
+    md->d_lin64 = nullptr;
+    md->d_linface64 = nullptr;
     for (auto& kv : md->graphs) cudaGraphExecDestroy(kv.second);
     md->graphs.clear();
     return CMDG_OK;

@@ -196,6 +196,7 @@ struct Model {
     // (Np, 10, nelem) and bottom/top face table (Nfp, 4, 2, nelem), FP64
     double* d_lin64 = nullptr;
     double* d_linface64 = nullptr;
+    int lin_nz = 0;                  // grid-arrays meshes: elements per stack found for the linear model
     int grid_ctas = -1;              // stage-kernel grid: -1 = one CTA per element (the measured best
                                      // on GB300), 0 = one wave of resident CTAs, n > 0 = n CTAs
     int kernel_kind = 0;             // KERNEL_NODE or KERNEL_COLUMN

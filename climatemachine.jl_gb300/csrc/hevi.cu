@@ -49,7 +49,7 @@ namespace {
 enum LinField {
     LT_MX0 = 0,  // M dxi3/dx_c, 3 words
     LT_MI = 3,   // 1 / M
-    LT_PHI = 4,  // geopotential
+    LT_CRHO = 4, // pressure coefficient of rho: R_d T_0 - (R_d / cv_d) Phi
     LT_H = 5,    // (rhoe_ref + p_ref) / rho_ref
     LT_G0 = 6,   // DG gradient of the geopotential, 3 words
     LT_C = 9,    // reference sound speed
@@ -67,7 +67,7 @@ struct LinParams {
     int64_t nelem;
     int nz;
     double alpha, beta;
-    double R_d, T_0, kv;   // pL = (rho R_d) T_0 + kv (rhoe - rho Phi), kv = R_d / cv_d
+    double kv;       // R_d / cv_d: p_L = kv rhoe + crho rho
     double D[64];    // D[kk * Nq + k] = d l_k / dxi at xi_kk
 };
 
@@ -92,8 +92,9 @@ __device__ __forceinline__ void lin_load(const LinParams& P, int64_t e, int node
     const double* L = P.lt + (size_t)e * LT_NFIELDS * Np;
 #pragma unroll
     for (int s = 0; s < 5; ++s) a.q[s] = Qe[s * Np + node];
-    const double phi = L[LT_PHI * Np + node];
-    a.pL = a.q[0] * P.R_d * P.T_0 + P.kv * (a.q[4] - a.q[0] * phi);
+    // linearized_air_pressure rho R_d T_0 + R_d / cv_d (rhoe - rho Phi), grouped
+    // as R_d / cv_d rhoe + (R_d T_0 - R_d / cv_d Phi) rho
+    a.pL = P.kv * a.q[4] + L[LT_CRHO * Np + node] * a.q[0];
     a.h = L[LT_H * Np + node];
     a.c = L[LT_C * Np + node];
 }
@@ -401,9 +402,40 @@ __global__ void ark_solution_kernel(double* Q, const double* R0, const double* R
     }
 }
 
-int stack_height(const Mesh& m) {
+// Elements per wall-bounded stack of a grid-arrays mesh, 0 when its
+// elements are not stacked: element e = v + nz h, face 5 (xi3 = -1) of level
+// 0 and face 6 of level nz - 1 on walls, and between levels the facing node
+// of node (i, j) of one face being node (i, j) of the other
+// (StackedBrickTopology / StackedCubedSphereTopology order).
+int arrays_stack_height(const Mesh& m) {
+    const int Nfp = m.Nfp, Nq = m.Nq;
+    const int* row0 = &m.nbr[0];
+    if (row0[4] >= 0) return 0;
+    int nz = 1;
+    for (int64_t e = 0; m.nbr[(size_t)e * NBR_STRIDE + 5] >= 0; ++e) {
+        if (m.nbr[(size_t)e * NBR_STRIDE + 5] != e + 1 || e + 1 >= m.nelem) return 0;
+        ++nz;
+    }
+    if (m.nelem % nz != 0) return 0;
+    for (int64_t e = 0; e < m.nelem; ++e) {
+        const int v = (int)(e % nz);
+        const int* row = &m.nbr[(size_t)e * NBR_STRIDE];
+        if ((v == 0) != (row[4] < 0) || (v == nz - 1) != (row[5] < 0)) return 0;
+        if (v > 0 && row[4] != e - 1) return 0;
+        if (v < nz - 1 && row[5] != e + 1) return 0;
+        for (int fn = 0; fn < Nfp; ++fn) {
+            if (v > 0 && m.fpart[((size_t)e * 6 + 4) * Nfp + fn] != fn + Nfp * (Nq - 1)) return 0;
+            if (v < nz - 1 && m.fpart[((size_t)e * 6 + 5) * Nfp + fn] != fn) return 0;
+        }
+    }
+    return nz;
+}
+
+int stack_height(const Model* md) {
+    const Mesh& m = *md->mesh;
     if (m.kind == MESH_SHELL) return m.nz;
     if (m.kind == MESH_BRICK && !m.desc.periodic[2]) return m.nz;
+    if (m.kind == MESH_ARRAYS) return md->lin_nz;
     return 0;
 }
 
@@ -413,11 +445,19 @@ int init_linear_tables(Model* md) {
     const Mesh& m = *md->mesh;
     const cmdg_atmos_params& p = md->prm;
     CMDG_ARG_CHECK(p.ref_state != 0, "AtmosAcousticGravityLinearModel needs a model with a reference state");
-    if (m.kind != MESH_BRICK && m.kind != MESH_SHELL) {
-        set_error("the linear model runs on brick and cubed-shell meshes");
-        return CMDG_ERR_UNSUPPORTED;
+    if (m.kind == MESH_ARRAYS) {
+        if (!md->has_reference) {
+            set_error("set the reference state (cmdg_model_set_reference) before the linear model");
+            return CMDG_ERR_STATE;
+        }
+        md->lin_nz = arrays_stack_height(m);
+        if (md->lin_nz == 0) {
+            set_error("the vertical linear model needs stacked elements with walls at both ends of each stack "
+                      "(StackedBrickTopology / StackedCubedSphereTopology order)");
+            return CMDG_ERR_UNSUPPORTED;
+        }
     }
-    const int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp, nz = m.nz;
+    const int Nq = m.Nq, Np = m.Np, Nfp = m.Nfp, nz = m.kind == MESH_ARRAYS ? md->lin_nz : m.nz;
     const int64_t nelem = m.nelem;
     std::vector<double> lt((size_t)nelem * LT_NFIELDS * Np), lf((size_t)nelem * 2 * LF_NFIELDS * Nfp);
     const double cs2 = p.cp_d / p.cv_d * p.R_d;
@@ -426,6 +466,8 @@ int init_linear_tables(Model* md) {
     if (m.kind == MESH_SHELL) {
         geo.resize((size_t)nelem * KG_NFIELDS * Np);
         CMDG_CUDA_CHECK(cudaMemcpy(geo.data(), md->d_geo64, sizeof(double) * geo.size(), cudaMemcpyDeviceToHost));
+    } else if (m.kind == MESH_ARRAYS) {
+        geo = md->arrays_geo;
     }
     for (int64_t e = 0; e < nelem; ++e) {
         const int ez = (int)(e % nz);
@@ -442,7 +484,7 @@ int init_linear_tables(Model* md) {
                 T[(LT_MX0 + 1) * Np + n] = 0.0;
                 T[(LT_MX0 + 2) * Np + n] = M * em[2];
                 T[LT_MI * Np + n] = 1.0 / M;
-                T[LT_PHI * Np + n] = L[LV_PHI];
+                T[LT_CRHO * Np + n] = p.R_d * p.T_0 - (p.R_d / p.cv_d) * L[LV_PHI];
                 T[LT_G0 * Np + n] = 0.0;
                 T[(LT_G0 + 1) * Np + n] = 0.0;
                 T[(LT_G0 + 2) * Np + n] = L[LV_GPHIZ];
@@ -466,12 +508,19 @@ int init_linear_tables(Model* md) {
                 const double M = G[CG_M * Np + n];
                 for (int c = 0; c < 3; ++c) T[(LT_MX0 + c) * Np + n] = M * G[(CG_XI + 6 + c) * Np + n];
                 T[LT_MI * Np + n] = 1.0 / M;
-                const double r = std::sqrt(X[n] * X[n] + X[Np + n] * X[Np + n] + X[2 * Np + n] * X[2 * Np + n]);
-                const double phi = (p.orientation == CMDG_ORIENT_SPHERE) ? p.grav * (r - p.planet_radius) : 0.0;
-                T[LT_PHI * Np + n] = phi;
                 for (int c = 0; c < 3; ++c) T[(LT_G0 + c) * Np + n] = K[(KG_GPHI + c) * Np + n];
-                double Tv, pr;
-                temperature_profile(p, phi / p.grav, Tv, pr);
+                double pr;
+                if (m.kind == MESH_ARRAYS) {
+                    // the caller's geopotential (as its pressure coefficient) and reference pressure
+                    T[LT_CRHO * Np + n] = K[KG_DCRHO * Np + n];
+                    pr = md->pref64[(size_t)e * Np + n];
+                } else {
+                    const double r = std::sqrt(X[n] * X[n] + X[Np + n] * X[Np + n] + X[2 * Np + n] * X[2 * Np + n]);
+                    const double phi = (p.orientation == CMDG_ORIENT_SPHERE) ? p.grav * (r - p.planet_radius) : 0.0;
+                    T[LT_CRHO * Np + n] = p.R_d * p.T_0 - (p.R_d / p.cv_d) * phi;
+                    double Tv;
+                    temperature_profile(p, phi / p.grav, Tv, pr);
+                }
                 const double rho = md->ref64[((size_t)e * 2 + 0) * Np + n];
                 const double rhoe = md->ref64[((size_t)e * 2 + 1) * Np + n];
                 T[LT_H * Np + n] = (rhoe + pr) / rho;
@@ -509,11 +558,9 @@ int launch_linear_N(Model* md, const double* Q, double* T, double alpha, double 
     P.lt = md->d_lin64;
     P.lf = md->d_linface64;
     P.nelem = m.nelem;
-    P.nz = m.nz;
+    P.nz = stack_height(md);
     P.alpha = alpha;
     P.beta = beta;
-    P.R_d = p.R_d;
-    P.T_0 = p.T_0;
     P.kv = p.R_d / p.cv_d;
     for (int i = 0; i < Nq * Nq; ++i) P.D[i] = m.D[i];
     const int64_t threads = m.nelem * (int64_t)m.Nfp;
@@ -527,7 +574,7 @@ int launch_linear_N(Model* md, const double* Q, double* T, double alpha, double 
 int launch_linear_tendency(Model* md, const double* Q, double* T, double alpha, double beta, cudaStream_t s) {
     int rc = init_linear_tables(md);
     if (rc) return rc;
-    CMDG_ARG_CHECK(stack_height(*md->mesh) > 0,
+    CMDG_ARG_CHECK(stack_height(md) > 0,
                    "the vertical linear model needs walls at the bottom and top of each column (non-periodic z)");
     switch (md->mesh->N) {
         case 2: return launch_linear_N<3>(md, Q, T, alpha, beta, s);
@@ -573,7 +620,7 @@ int hevi_assemble_N(Hevi* h, cudaStream_t s) {
     for (int vi = 0; vi < 3 && vi < h->lm.nz; ++vi)
         for (int k = 0; k < Nq; ++k)
             for (int st = 0; st < 5; ++st) {
-                unit_state_kernel<Nq><<<(unsigned)((len + 255) / 256), 256, 0, s>>>(E, m.nelem, m.nz, vi, k, st);
+                unit_state_kernel<Nq><<<(unsigned)((len + 255) / 256), 256, 0, s>>>(E, m.nelem, h->lm.nz, vi, k, st);
                 int rc = launch_linear_N<Nq>(md, E, R, 1.0, 0.0, s);
                 if (rc) return rc;
                 band_scatter_kernel<Nq><<<(unsigned)((ntot + 255) / 256), 256, 0, s>>>(E, R, h->d_AB, h->lm, h->bw, vi,
@@ -698,7 +745,7 @@ int cmdg_hevi_create(cmdg_model* model, double dt, int split_explicit_implicit, 
     int rc = init_linear_tables(md);
     if (rc) return rc;
     const Mesh& m = *md->mesh;
-    const int nz = stack_height(m);
+    const int nz = stack_height(md);
     if (nz <= 0) {
         set_error("HEVI needs wall-bounded element stacks (a cubed shell, or a brick non-periodic in z)");
         return CMDG_ERR_UNSUPPORTED;

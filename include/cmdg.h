@@ -284,7 +284,10 @@ int cmdg_apply_mp_filter(cmdg_model* model, double* d_Q, const double* h_Wh, con
 
 /* HEVI (horizontally explicit, vertically implicit) stepping of FP64 states,
  * for models with a hydrostatic reference state on wall-bounded element
- * stacks (cubed shell, or a brick non-periodic in z).  The linear operator,
+ * stacks: a cubed shell, a brick non-periodic in z, or a mesh from grid
+ * arrays whose elements are in stacked order (element e = v + nz h, walls at
+ * both ends of every stack, found from vmap_plus / elemtobndy; the
+ * reference state must be set first).  The linear operator,
  * the column LU and the ARK stage algebra are FP64; a mixed-precision model
  * evaluates the explicit tendency on the FP32 perturbation of each stage
  * state (cmdg_tendency_mixed semantics), an FP64 model in FP64.

@@ -18,6 +18,8 @@
 * the same with the explicit tendency on a mixed model's FP32 perturbation:
   the golden norm to 1e-9; rho, rhoe within 1e-6 and the momentum within
   5e-5 of the FP64 run;
+* on a mesh from the reference's own grid arrays (stacks found from
+  vmap+ / elemtobndy): linear tendency and ARK2 steps against the oracle;
 * configuration errors (periodic columns, no reference state) are refused.
 """
 import math
@@ -245,6 +247,42 @@ def test_mixed_explicit_part_acoustic_wave_golden():
         err = math.sqrt(float(np.sum((a[:, sl] - b[:, sl]) ** 2 * M[:, None, :])))
         ref = math.sqrt(float(np.sum(b[:, sl] ** 2 * M[:, None, :])))
         assert err <= tol * ref, (sl, err / ref)
+
+
+def test_hevi_on_the_reference_grid_arrays():
+    """The oracle's own vgeo, vmap+ and elemtobndy of a stacked cubed shell and
+    its aux values (cmdg_mesh_create_arrays + cmdg_model_set_reference): the
+    stacks are found from the arrays, the linear tendency and three ARK2
+    steps match the oracle."""
+    N, H = 3, 10e3
+    om = O.OracleModel(N, shell=dict(nhorz=2, nvert=3, r_inner=R, r_outer=R + H), orientation="sphere",
+                       gravity=True, ref_state=True, profile="isothermal", T_surface=300.0)
+    a, A = om.aux, O.AUX
+    aux7 = np.stack([a[:, A["Phi"]], a[:, A["gPhi"]], a[:, A["gPhi"] + 1], a[:, A["gPhi"] + 2], a[:, A["rho_ref"]],
+                     a[:, A["rhoe_ref"]], a[:, A["p_ref"]]], axis=1)
+    grid = cmdg.ArraysGrid(N, om.vgeo, om.vmapP + 1, om.elemtobndy)
+    model = cmdg.AtmosModel(orientation="sphere", gravity=True,
+                            ref_state=cmdg.HydrostaticState(cmdg.IsothermalProfile(300.0)))
+    dg = cmdg.DGModel(model, grid)
+    lin = linear_dg(dg)
+    Q0 = workloads.acoustic_wave_state(om.vgeo[:, 12:15], a[:, A["p_ref"]], H=H)
+    Q = dg.init_ode_state(Q0)
+    dQ = dg.new_state(torch.float64)
+    with pytest.raises(cmdg.CmdgError):  # the reference state is not set yet
+        lin(dQ, Q, None, 0.0)
+    dg.set_reference(aux7)
+    rng = np.random.default_rng(12)
+    Qn = Q0.copy()
+    Qn[:, 1:4] += rng.uniform(-2, 2, size=Qn[:, 1:4].shape)
+    lin(dQ, dg.init_ode_state(Qn), None, 0.0)
+    assert rel_fields(dQ.cpu().numpy(), om.linear_tendency(Qn)).max() < 1e-10
+    dt = 60.0
+    ref = O.OracleHevi(om, dt).step(Q0.copy(), 3)
+    ark = cmdg.ARK2GiraldoKellyConstantinescu(dg, lin, cmdg.LinearBackwardEulerSolver(cmdg.ManyColumnLU()), Q,
+                                              dt=dt)
+    cmdg.dostep_(Q, ark, None, 0.0, 3)
+    err = rel_fields(Q.cpu().numpy(), ref)
+    assert err[[0, 4]].max() < 1e-9 and err[1:4].max() < 1e-8, err
 
 
 def test_hevi_configuration_errors():
