@@ -316,7 +316,8 @@ int cmdg_apply_mp_filter(cmdg_model* model, double* d_Q, const double* h_Wh, con
  * part is the model's full tendency (split_explicit_implicit = 0) or the
  * remainder full - linear (1, remainder_DGModel).
  * cmdg_hevi_info: the implicit coefficient alpha, the band half-width
- * 5 (N+1) - 1 and the number of vertical lines. */
+ * 5 (N+1) - 1 and the number of vertical lines.
+ * A solver refers to its model: destroy the solver before the model. */
 typedef struct cmdg_hevi cmdg_hevi;
 int cmdg_linear_tendency(cmdg_model* model, double* d_dQ, const double* d_Q, double t, double alpha, double beta,
                          void* stream);
