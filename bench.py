@@ -59,6 +59,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 REPO = os.path.dirname(os.path.abspath(__file__))
@@ -346,7 +347,7 @@ class ClockSampler:
     def __init__(self, index=0):
         self.proc = None
         self.index = index
-        self.path = os.path.join(REPO, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"cmdg_clocks_bench_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
