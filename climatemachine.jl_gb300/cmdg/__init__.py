@@ -17,7 +17,7 @@ from .atmos import (EARTH, AtmosModel, HydrostaticState, DryAdiabaticProfile, Is
 from .dgmodel import (DGModel, BrickGrid, CubedShellGrid, ArraysGrid, euclidean_distance, weightedsum, norm,
                       remainder_DGModel)
 from .odesolvers import (LSRK54CarpenterKennedy, ARK2GiraldoKellyConstantinescu, LinearBackwardEulerSolver,
-                         ManyColumnLU, LowStorageVariant, solve_, dostep_)
+                         ManyColumnLU, SingleColumnLU, LowStorageVariant, solve_, dostep_)
 from ._lib import CmdgError, load as load_library
 from .ensemble import Ensemble
 from . import checkpoint, filters, partition
@@ -26,5 +26,6 @@ __all__ = [
     "EARTH", "AtmosModel", "HydrostaticState", "DryBiharmonic", "DryAdiabaticProfile", "IsothermalProfile", "DGModel", "BrickGrid", "CubedShellGrid", "ArraysGrid",
     "euclidean_distance", "weightedsum", "norm", "LSRK54CarpenterKennedy", "solve_", "dostep_", "CmdgError",
     "load_library", "Ensemble", "AtmosAcousticGravityLinearModel", "remainder_DGModel",
-    "ARK2GiraldoKellyConstantinescu", "LinearBackwardEulerSolver", "ManyColumnLU", "LowStorageVariant",
+    "ARK2GiraldoKellyConstantinescu", "LinearBackwardEulerSolver", "ManyColumnLU", "SingleColumnLU",
+    "LowStorageVariant",
 ]

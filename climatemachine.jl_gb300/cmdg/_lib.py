@@ -128,7 +128,7 @@ def load(path: str | None = None):
         "cmdg_apply_filter": [P, P, P, P, I, P, I, P],
         "cmdg_apply_tmar": [P, P, P, I, P],
         "cmdg_linear_tendency": [P, P, P, D, D, D, P],
-        "cmdg_hevi_create": [P, D, I, I, PP],
+        "cmdg_hevi_create": [P, D, I, I, I, PP],
         "cmdg_hevi_destroy": [P],
         "cmdg_hevi_info": [P, ctypes.POINTER(D), ctypes.POINTER(I), ctypes.POINTER(ctypes.c_int64)],
         "cmdg_hevi_solve": [P, P, P, P],

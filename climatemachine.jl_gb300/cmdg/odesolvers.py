@@ -56,6 +56,12 @@ class ManyColumnLU:
     one banded LU factorization, without pivoting, per vertical node line."""
 
 
+class SingleColumnLU:
+    """SingleColumnLU() (columnwise_lu_solver.jl:17-23): one banded LU (the
+    first column's) for every column; the library refuses it unless all
+    column matrices agree (an affine brick, for instance)."""
+
+
 class LowStorageVariant:
     """LowStorageVariant() of the additive Runge-Kutta schemes."""
 
@@ -66,8 +72,8 @@ class LinearBackwardEulerSolver:
     factored once for the solver's dt."""
 
     def __init__(self, solver, isadjustable: bool = False, preconditioner_update_freq: int = -1):
-        if not isinstance(solver, ManyColumnLU):
-            raise ValueError("the GPU backward Euler solver is ManyColumnLU()")
+        if not isinstance(solver, (ManyColumnLU, SingleColumnLU)):
+            raise ValueError("the GPU backward Euler solver is ManyColumnLU() or SingleColumnLU()")
         self.solver = solver
         self.isadjustable = isadjustable
         self.preconditioner_update_freq = preconditioner_update_freq
@@ -91,7 +97,8 @@ class ARK2GiraldoKellyConstantinescu:
         if variant is not None and not isinstance(variant, LowStorageVariant):
             raise ValueError("the GPU ARK2 scheme runs the LowStorageVariant")
         if not isinstance(backward_euler_solver, LinearBackwardEulerSolver):
-            raise ValueError("backward_euler_solver must be a LinearBackwardEulerSolver(ManyColumnLU())")
+            raise ValueError("backward_euler_solver must be a LinearBackwardEulerSolver(ManyColumnLU() or "
+                             "SingleColumnLU())")
         if not (isinstance(L, DGModel) and L.is_linear):
             raise ValueError("L must be the vertical linear DGModel")
         dg = L.parent
@@ -109,8 +116,9 @@ class ARK2GiraldoKellyConstantinescu:
         self.steps = 0
         self.split_explicit_implicit = bool(split_explicit_implicit)
         h = ctypes.c_void_p()
+        self.single_column = isinstance(backward_euler_solver.solver, SingleColumnLU)
         call("cmdg_hevi_create", dg.h, self.dt, int(self.split_explicit_implicit), int(paperversion),
-             ctypes.byref(h))
+             int(self.single_column), ctypes.byref(h))
         self.h = h
         alpha, bw, nline = ctypes.c_double(), ctypes.c_int(), ctypes.c_int64()
         call("cmdg_hevi_info", h, ctypes.byref(alpha), ctypes.byref(bw), ctypes.byref(nline))

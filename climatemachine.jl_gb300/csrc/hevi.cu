@@ -287,6 +287,25 @@ __global__ void band_pattern_kernel(double* AB, LineMap lm, int bw, unsigned* er
     if (bad) atomicOr(err, 4u);
 }
 
+// SingleColumnLU: every line's factors must equal the first line's to
+// rounding (entries within 1e-10 of the larger of the entry and the pivot
+// row's scale); copies the first line's factors out
+__global__ void band_single_kernel(const double* AB, double* AB1, LineMap lm, int bw, unsigned* err) {
+    const int64_t line = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (line >= lm.nline) return;
+    const int nb = 2 * bw + 1;
+    bool bad = false;
+    for (int b = 0; b < nb; ++b)
+        for (int col = 0; col < lm.n; ++col) {
+            const size_t i0 = ((size_t)b * lm.n + col) * lm.nline;
+            const double v = AB[i0 + line], v0 = AB[i0];
+            const double scale = fabs(v0) + fabs(1.0 / AB[((size_t)bw * lm.n + col) * lm.nline]);
+            bad |= !(fabs(v - v0) <= 1e-10 * scale);
+            if (line == 0) AB1[(size_t)b * lm.n + col] = v0;
+        }
+    if (bad) atomicOr(err, 8u);
+}
+
 // one warp per CTA: the column count is small (a few warps per SM), so the
 // grid is spread evenly over the SMs
 constexpr int SOLVE_THREADS = 32;
@@ -312,13 +331,15 @@ constexpr int SOLVE_PREFETCH = 3;
 template <int Nq>
 __global__ void __launch_bounds__(SOLVE_THREADS) band_solve_kernel(const double* __restrict__ AB, const double* b,
                                                                    double* __restrict__ y, double* out, LineMap lm,
-                                                                   int accumulate) {
+                                                                   int accumulate, int single) {
     constexpr int NB = 5 * Nq, BW = NB - 1;
     const int64_t line = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (line >= lm.nline) return;
     const int n = lm.n, nz = lm.nz;
-    const size_t NL = (size_t)lm.nline, RS = (size_t)n * NL;  // column and band-row strides
-    const double* A = AB + line;
+    // column and band-row strides: one factorization per line, or the
+    // first line's for all (SingleColumnLU)
+    const size_t NL = single ? 1 : (size_t)lm.nline, RS = (size_t)n * NL;
+    const double* A = single ? AB : AB + line;
     double w[NB];
 #pragma unroll
     for (int i = 0; i < NB; ++i) w[i] = b[line_index<Nq>(lm, line, i)];
@@ -597,6 +618,8 @@ struct Hevi {
     int bw = 0;
     size_t len = 0;
     double* d_AB = nullptr;   // band matrix, then its LU factors (reciprocal pivots), line-fastest
+    int single = 0;           // SingleColumnLU: d_AB1 holds the first line's factors, (2 bw + 1, n)
+    double* d_AB1 = nullptr;
     double* d_buf = nullptr;  // S1, S2, R0, R1, R2, Qhat, Y
     float* d_Sp = nullptr;    // mixed models: FP32 perturbation of the stage state
     unsigned* d_err = nullptr;
@@ -631,6 +654,11 @@ int hevi_assemble_N(Hevi* h, cudaStream_t s) {
     CMDG_CUDA_CHECK(cudaGetLastError());
     band_pattern_kernel<<<(unsigned)((h->lm.nline + 127) / 128), 128, 0, s>>>(h->d_AB, h->lm, h->bw, h->d_err);
     CMDG_CUDA_CHECK(cudaGetLastError());
+    if (h->single) {
+        band_single_kernel<<<(unsigned)((h->lm.nline + 127) / 128), 128, 0, s>>>(h->d_AB, h->d_AB1, h->lm, h->bw,
+                                                                                h->d_err);
+        CMDG_CUDA_CHECK(cudaGetLastError());
+    }
     return CMDG_OK;
 }
 
@@ -646,7 +674,8 @@ int hevi_assemble(Hevi* h, cudaStream_t s) {
 template <int Nq>
 int hevi_solve_N(Hevi* h, const double* b, double* out, int accumulate, cudaStream_t s) {
     const unsigned grid = (unsigned)((h->lm.nline + SOLVE_THREADS - 1) / SOLVE_THREADS);
-    band_solve_kernel<Nq><<<grid, SOLVE_THREADS, 0, s>>>(h->d_AB, b, h->Y(), out, h->lm, accumulate);
+    band_solve_kernel<Nq><<<grid, SOLVE_THREADS, 0, s>>>(h->single ? h->d_AB1 : h->d_AB, b, h->Y(), out, h->lm,
+                                                         accumulate, h->single);
     CMDG_CUDA_CHECK(cudaGetLastError());
     return CMDG_OK;
 }
@@ -737,7 +766,8 @@ int cmdg_linear_tendency(cmdg_model* model, double* d_dQ, const double* d_Q, dou
     return launch_linear_tendency(&model->m, d_Q, d_dQ, alpha, beta, (cudaStream_t)stream);
 }
 
-int cmdg_hevi_create(cmdg_model* model, double dt, int split_explicit_implicit, int paperversion, cmdg_hevi** out) {
+int cmdg_hevi_create(cmdg_model* model, double dt, int split_explicit_implicit, int paperversion, int single_column,
+                     cmdg_hevi** out) {
     CMDG_ARG_CHECK(model != nullptr && out != nullptr, "NULL argument");
     *out = nullptr;
     CMDG_ARG_CHECK(std::isfinite(dt) && dt > 0, "dt must be positive and finite");
@@ -759,6 +789,7 @@ int cmdg_hevi_create(cmdg_model* model, double dt, int split_explicit_implicit, 
     h->md = md;
     h->dt = dt;
     h->split = split_explicit_implicit ? 1 : 0;
+    h->single = single_column ? 1 : 0;
     const double s2 = std::sqrt(2.0);
     const double a32 = paperversion ? (3 + 2 * s2) / 6 : 0.5;
     const double Ae[3][3] = {{0, 0, 0}, {2 - s2, 0, 0}, {1 - a32, a32, 0}};
@@ -783,7 +814,8 @@ int cmdg_hevi_create(cmdg_model* model, double dt, int split_explicit_implicit, 
     cudaError_t e2 = cudaMalloc(&h->d_buf, sizeof(double) * 7 * h->len);
     cudaError_t e3 = cudaMalloc(&h->d_err, sizeof(unsigned));
     cudaError_t e4 = md->precision == CMDG_MIXED ? cudaMalloc(&h->d_Sp, sizeof(float) * h->len) : cudaSuccess;
-    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) {
+    cudaError_t e5 = h->single ? cudaMalloc(&h->d_AB1, sizeof(double) * (2 * h->bw + 1) * h->lm.n) : cudaSuccess;
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess || e5 != cudaSuccess) {
         cudaGetLastError();
         cmdg_hevi_destroy(ho);
         set_error("HEVI: device allocation of %zu bytes failed", sizeof(double) * (ab + 7 * h->len));
@@ -802,15 +834,23 @@ int cmdg_hevi_create(cmdg_model* model, double dt, int split_explicit_implicit, 
         set_error("HEVI: reading the assembly status failed");
         rc = CMDG_ERR_CUDA;
     }
-    if (!rc && err) {
+    if (!rc && (err & 7u)) {
         set_error((err & 1u)   ? "HEVI: the linear operator couples unknowns outside the column band"
                   : (err & 2u) ? "HEVI: zero or non-finite pivot in the column LU"
                                : "HEVI: the column LU factors have non-zeros outside the element-coupling pattern");
         rc = CMDG_ERR_NONFINITE;
     }
+    if (!rc && (err & 8u)) {
+        set_error("HEVI: SingleColumnLU needs identical column matrices (use ManyColumnLU on this mesh)");
+        rc = CMDG_ERR_ARG;
+    }
     if (rc) {
         cmdg_hevi_destroy(ho);
         return rc;
+    }
+    if (h->single) {  // only the first line's factors are kept
+        cudaFree(h->d_AB);
+        h->d_AB = nullptr;
     }
     *out = ho;
     return CMDG_OK;
@@ -819,6 +859,7 @@ int cmdg_hevi_create(cmdg_model* model, double dt, int split_explicit_implicit, 
 int cmdg_hevi_destroy(cmdg_hevi* hevi) {
     if (!hevi) return CMDG_OK;
     cudaFree(hevi->h.d_AB);
+    cudaFree(hevi->h.d_AB1);
     cudaFree(hevi->h.d_buf);
     cudaFree(hevi->h.d_Sp);
     cudaFree(hevi->h.d_err);

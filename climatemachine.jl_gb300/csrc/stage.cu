@@ -60,7 +60,10 @@ struct Dims {
     // the FP64 kernels are FP64-pipe bound; they keep enough CTAs to cover the barriers
     static constexpr int MIN_CTAS64 = N == 5 ? 2 : 3;
     // one CTA per element (no look-ahead registers): a tighter register budget
-    static constexpr int MIN_CTAS_DIRECT = N == 2 ? 16 : N == 3 ? 12 : N == 4 ? 7 : 5;
+#ifndef CMDG_MIN_CTAS_DIRECT_N4
+#define CMDG_MIN_CTAS_DIRECT_N4 7
+#endif
+    static constexpr int MIN_CTAS_DIRECT = N == 2 ? 16 : N == 3 ? 12 : N == 4 ? CMDG_MIN_CTAS_DIRECT_N4 : 5;
 };
 
 template <int N, typename R>

@@ -176,10 +176,11 @@ end
 (lm::CMDGLinearModel)(tendency, Q, p, t; increment = false) = lm(tendency, Q, p, t, true, increment)
 
 """
-    CMDGHEVI(dg::CMDGModel, dt; t0 = 0, split_explicit_implicit = false, paperversion = false)
+    CMDGHEVI(dg::CMDGModel, dt; t0 = 0, split_explicit_implicit = false, paperversion = false,
+             single_column = false)
 
 Stands in for `ARK2GiraldoKellyConstantinescu(dg_or_rem_dg, lineardg,
-LinearBackwardEulerSolver(ManyColumnLU()), Q; dt, t0,
+LinearBackwardEulerSolver(ManyColumnLU() or SingleColumnLU()), Q; dt, t0,
 split_explicit_implicit, paperversion)` (AdditiveRungeKuttaMethod.jl:
 839-897): the column LU of the vertical linear model is assembled and
 factored on the GPU at construction (`cmdg_hevi_create`) and each
@@ -193,10 +194,11 @@ mutable struct CMDGHEVI <: AbstractODESolver
     t::Float64
     steps::Int
 end
-function CMDGHEVI(dg::CMDGModel, dt; t0 = 0, split_explicit_implicit = false, paperversion = false)
+function CMDGHEVI(dg::CMDGModel, dt; t0 = 0, split_explicit_implicit = false, paperversion = false,
+                  single_column = false)
     h = Ref{Ptr{Cvoid}}(C_NULL)
-    check(ccall((:cmdg_hevi_create, libcmdg), Cint, (Ptr{Cvoid}, Cdouble, Cint, Cint, Ref{Ptr{Cvoid}}),
-                dg.model, dt, split_explicit_implicit, paperversion, h))
+    check(ccall((:cmdg_hevi_create, libcmdg), Cint, (Ptr{Cvoid}, Cdouble, Cint, Cint, Cint, Ref{Ptr{Cvoid}}),
+                dg.model, dt, split_explicit_implicit, paperversion, single_column, h))
     solver = CMDGHEVI(h[], dg, Float64(dt), Float64(t0), 0)
     finalizer(x -> ccall((:cmdg_hevi_destroy, libcmdg), Cint, (Ptr{Cvoid},), x.hevi), solver)
     return solver

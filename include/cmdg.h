@@ -308,7 +308,10 @@ int cmdg_apply_mp_filter(cmdg_model* model, double* d_Q, const double* h_Wh, con
  * builds and LU-factors, without pivoting, the banded matrix of
  * Q - alpha L(Q), alpha = dt (1 - 1/sqrt(2)), for every vertical node line
  * (src/Numerics/SystemSolvers/columnwise_lu_solver.jl:92-158, 228-488).
- * Owns that matrix and seven state-sized FP64 buffers.
+ * single_column = 1 is SingleColumnLU(): one factorization (the first
+ * line's) serves every line; refused with CMDG_ERR_ARG unless all column
+ * matrices agree to 1e-10 (e.g. an affine brick with level-dependent
+ * coefficients).  Owns the factors and seven state-sized FP64 buffers.
  * cmdg_hevi_solve: besolver!(Q, Qhat, alpha): d_Q = d_Qhat + alpha L(d_Q)
  * (BackwardEulerSolvers.jl; linearsolve! columnwise_lu_solver.jl:110-127,
  * 615-780); d_Q may alias d_Qhat.
@@ -321,7 +324,8 @@ int cmdg_apply_mp_filter(cmdg_model* model, double* d_Q, const double* h_Wh, con
 typedef struct cmdg_hevi cmdg_hevi;
 int cmdg_linear_tendency(cmdg_model* model, double* d_dQ, const double* d_Q, double t, double alpha, double beta,
                          void* stream);
-int cmdg_hevi_create(cmdg_model* model, double dt, int split_explicit_implicit, int paperversion, cmdg_hevi** out);
+int cmdg_hevi_create(cmdg_model* model, double dt, int split_explicit_implicit, int paperversion, int single_column,
+                     cmdg_hevi** out);
 int cmdg_hevi_destroy(cmdg_hevi* hevi);
 int cmdg_hevi_info(const cmdg_hevi* hevi, double* alpha, int* bandwidth, int64_t* nline);
 int cmdg_hevi_solve(cmdg_hevi* hevi, double* d_Q, const double* d_Qhat, void* stream);

@@ -20,6 +20,8 @@
   5e-5 of the FP64 run;
 * on a mesh from the reference's own grid arrays (stacks found from
   vmap+ / elemtobndy): linear tendency and ARK2 steps against the oracle;
+* SingleColumnLU on an affine brick equals ManyColumnLU and is refused on
+  the cubed shell;
 * configuration errors (periodic columns, no reference state) are refused.
 """
 import math
@@ -177,6 +179,29 @@ def test_brick_ark2_steps_match_oracle():
                                               dt=dt)
     cmdg.dostep_(Q, ark, None, 0.0, 4)
     assert rel_fields(Q.cpu().numpy(), ref).max() < 1e-9
+
+
+def test_single_column_lu_on_an_affine_brick():
+    """SingleColumnLU (one factorization for every node column) on a brick,
+    whose column matrices agree: the same steps as ManyColumnLU to rounding
+    and as the oracle; refused on the cubed shell, whose columns differ."""
+    om, dg, Q0 = brick_pair(3)
+    dt = 0.5
+    lin = linear_dg(dg)
+    out = []
+    for solver in (cmdg.ManyColumnLU(), cmdg.SingleColumnLU()):
+        Q = dg.init_ode_state(Q0)
+        ark = cmdg.ARK2GiraldoKellyConstantinescu(dg, lin, cmdg.LinearBackwardEulerSolver(solver), Q, dt=dt)
+        cmdg.dostep_(Q, ark, None, 0.0, 4)
+        out.append(Q.cpu().numpy())
+    assert rel_fields(out[1], out[0]).max() < 1e-12
+    ref = O.OracleHevi(om, dt).step(Q0.copy(), 4)
+    assert rel_fields(out[1], ref).max() < 1e-9
+    _, dgs, Qs0 = shell_pair(3, 2, 2)
+    lins = linear_dg(dgs)
+    with pytest.raises(cmdg.CmdgError):
+        cmdg.ARK2GiraldoKellyConstantinescu(dgs, lins, cmdg.LinearBackwardEulerSolver(cmdg.SingleColumnLU()),
+                                            dgs.init_ode_state(Qs0), dt=10.0)
 
 
 @pytest.mark.parametrize("split", [False, True])
