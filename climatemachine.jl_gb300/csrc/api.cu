@@ -260,7 +260,10 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
     } else if (shell) {
         CMDG_ARG_CHECK(p->orientation == CMDG_ORIENT_NONE || p->orientation == CMDG_ORIENT_SPHERE,
                        "orientation %d is not available on a cubed shell", p->orientation);
-        CMDG_ARG_CHECK(p->turbulence == CMDG_TURB_NONE, "the cubed-shell kernels are inviscid");
+        CMDG_ARG_CHECK(p->turbulence == CMDG_TURB_NONE || p->turbulence == CMDG_TURB_CONSTANT,
+                       "the cubed-shell kernels run ConstantDynamicViscosity or no closure");
+        CMDG_ARG_CHECK(p->turbulence == CMDG_TURB_NONE || p->hyperdiffusion == CMDG_HYPER_NONE,
+                       "the cubed-shell kernels run viscosity or hyperdiffusion, not both");
         CMDG_ARG_CHECK(p->orientation != CMDG_ORIENT_SPHERE || p->planet_radius > 0, "planet_radius must be positive");
     } else {
         CMDG_ARG_CHECK(p->orientation == CMDG_ORIENT_NONE || p->orientation == CMDG_ORIENT_FLAT,
@@ -312,6 +315,7 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
         rc = init_viscous_tables(&md);
     if (rc == CMDG_OK && p->hyperdiffusion != CMDG_HYPER_NONE)
         rc = shell ? init_shell_hyper_tables(&md) : init_hyper_tables(&md);
+    if (rc == CMDG_OK && shell && p->turbulence != CMDG_TURB_NONE) rc = init_shell_visc_tables(&md);
     if (rc == CMDG_OK) {
         cudaError_t e = cudaMalloc(&md.d_status, sizeof(unsigned));
         if (e == cudaSuccess) e = cudaMemset(md.d_status, 0, sizeof(unsigned));
@@ -348,6 +352,7 @@ int cmdg_model_destroy(cmdg_model* model) {
     cudaFree(md.d_glap_ref);
     cudaFree(md.d_nu4);
     cudaFree(md.d_hglap_ref);
+    cudaFree(md.d_vgref);
     cudaFree(md.d_fjump);
     cudaFree(md.d_geo64);
     cudaFree(md.d_geo32);
@@ -506,6 +511,7 @@ int cmdg_gradient_flux(cmdg_model* model, void* d_gf, const void* d_Q, void* str
     if (rc) return rc;
     CMDG_ARG_CHECK(d_gf != nullptr && d_Q != nullptr, "NULL buffer");
     CMDG_ARG_CHECK(model->m.prm.turbulence != CMDG_TURB_NONE, "the model has no diffusive terms");
+    CMDG_ARG_CHECK(model->m.mesh->kind == MESH_BRICK, "cmdg_gradient_flux exposes the brick gradient-flux layout");
     CMDG_ARG_CHECK(model->m.mesh->kind == MESH_BRICK, "the diffusive passes run on brick meshes");
     return launch_gradient(&model->m, d_Q, d_gf, (cudaStream_t)stream);
 }

@@ -187,6 +187,7 @@ struct Model {
     float* d_glap_ref = nullptr;
     void* d_nu4 = nullptr;           // cubed shell: nu_4 per node, (Np, nelem), model precision
     float* d_hglap_ref = nullptr;    // cubed shell, mixed: nu_4 grad lap h_ref per node, (Np, 3, nelem)
+    float* d_vgref = nullptr;        // cubed shell, viscous, mixed: grad h_ref per node, (Np, 3, nelem)
     // grid-arrays meshes: per-node kernel geometry on the host, per-node p_ref,
     // FP64-computed reference jumps (rho, rhoe) per face node, reference set?
     std::vector<double> arrays_geo, pref64;
@@ -249,6 +250,11 @@ int launch_hyper_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
 // hd_out (nu grad^3 of u_h[0..2], h_tot, (Np, 12, nelem))
 int init_shell_hyper_tables(Model* md);
 int launch_shell_hyper_passes(Model* md, const void* Qin, void* hd_out, cudaStream_t s);
+// ConstantDynamicViscosity on the cubed shell (hyper_shell.cu): the gradient
+// buffer (grad u, grad h_tot, (Np, 12, nelem)) and, mixed, grad h_ref; the
+// gradient pass of Qin into gout
+int init_shell_visc_tables(Model* md);
+int launch_shell_visc_gradient(Model* md, const void* Qin, void* gout, cudaStream_t s);
 
 // reductions / conversions (reduce.cu)
 int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s);

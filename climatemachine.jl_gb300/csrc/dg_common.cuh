@@ -54,6 +54,10 @@ struct KParams {
     // reference part nu_4 grad lap h_ref per node (Np, 3, nelem)
     const void* nu4;
     const float* hglap_ref32;
+    // cubed shell with ConstantDynamicViscosity, mixed: the FP64-computed
+    // gradient of the reference h_tot per node (Np, 3, nelem); the viscous
+    // gradient pass writes grad u, grad h_tot (Np, 12, nelem) into gf
+    const float* vgref32;
     int hyper_horizontal;  // 1: the passes run in the horizontal directions only (HorizontalDirection)
     // grid-arrays meshes: facing node of each face node (Nfp, 6, nelem) and
     // the FP64-computed reference jumps (rho, rhoe) per face node

@@ -72,7 +72,9 @@ __device__ __forceinline__ R shell_face_normal(const KParams& P, const R* g, int
 // GradientLaplacian arguments (u_h[0..2], h_tot) of a state at a node with
 // reference row lv (per-node parts included) and geometry g; in the mixed
 // form h_tot is the perturbation h' = (H' rho_ref - H_ref rho') / (rho rho_ref)
-template <typename R, bool MIXED>
+// PROJECT = false: the gradient arguments of the diffusive closures, u and
+// h_tot (AtmosModel.jl:622-650, energy.jl:20-31)
+template <typename R, bool MIXED, bool PROJECT = true>
 __device__ __forceinline__ void shell_hyper_args(const KParams& P, const R q[NSTATE], const Level<R>& lv, const R* g,
                                                  int Np, int n, R H[4]) {
     const R gm1 = KConst<R>::gm1(P);
@@ -83,7 +85,7 @@ __device__ __forceinline__ void shell_hyper_args(const KParams& P, const R q[NST
     const R u[3] = {q[1] * rinv, q[2] * rinv, q[3] * rinv};
     const R ku = k[0] * u[0] + k[1] * u[1] + k[2] * u[2];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) H[c] = u[c] - k[c] * ku;
+    for (int c = 0; c < 3; ++c) H[c] = PROJECT ? u[c] - k[c] * ku : u[c];
     const R ke2 = q[1] * u[0] + q[2] * u[1] + q[3] * u[2];
     if (MIXED && P.ph.ref_state) {
         const R pp = gm1 * (q[4] - R(0.5) * ke2) + q[0] * lv.crho;
@@ -147,7 +149,7 @@ __device__ __forceinline__ int shell_partner_level(const ShellIdx<N>& x, int ez,
     return ezp * Nq + vP / Nfp;
 }
 
-template <int N, typename R, bool MIXED>
+template <int N, typename R, bool MIXED, bool PROJECT = true>
 __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(const KParams P, const void* Qv,
                                                                             R* __restrict__ hg) {
     using Ix = ShellIdx<N>;
@@ -184,7 +186,7 @@ __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(cons
     if (x.node) {
         R H[4];
         const Level<R> lv = shell_level<R, MIXED>(P, ge, Np, t, ez * Nq + x.nk);
-        shell_hyper_args<R, MIXED>(P, q, lv, ge, Np, t, H);
+        shell_hyper_args<R, MIXED, PROJECT>(P, q, lv, ge, Np, t, H);
         PL::st(s_q, Np, t, q);
 #pragma unroll
         for (int s = 0; s < 4; ++s) s_H[s * Np + t] = H[s];
@@ -194,11 +196,11 @@ __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(cons
     if (x.face) {
         R nv[3], Hp[4], c;
         R lift = shell_face_normal<R>(P, ge, Np, x.fd, x.fside ? R(1) : R(-1), x.vM, nv);
-        if (P.hyper_horizontal && x.fd == 2) lift = R(0);  // HorizontalDirection: no terms on the xi3 faces
+        if (PROJECT && P.hyper_horizontal && x.fd == 2) lift = R(0);  // HorizontalDirection: no xi3 face terms
         if (nb >= 0) {
             const R* gp = geo + (size_t)nb * GSTRIDE;
             const Level<R> lvp = shell_level<R, MIXED>(P, gp, Np, vP, shell_partner_level<N>(x, ez, vP));
-            shell_hyper_args<R, MIXED>(P, qp, lvp, gp, Np, vP, Hp);
+            shell_hyper_args<R, MIXED, PROJECT>(P, qp, lvp, gp, Np, vP, Hp);
             c = R(0.5);
         } else {
             // FreeSlip state of the gradient flux: rhou+ = rhou- - (rhou-.n) n
@@ -208,7 +210,7 @@ __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(cons
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc) qb[1 + cc] -= mn * nv[cc];
             const Level<R> lvm = shell_level<R, MIXED>(P, ge, Np, x.vM, ez * Nq + x.kM);
-            shell_hyper_args<R, MIXED>(P, qb, lvm, ge, Np, x.vM, Hp);
+            shell_hyper_args<R, MIXED, PROJECT>(P, qb, lvm, ge, Np, x.vM, Hp);
             c = R(1);
         }
 #pragma unroll
@@ -222,7 +224,7 @@ __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(cons
 
     if (x.node) {
         R g[12];
-        shell_strong_gradient<N, R>(x, s_H, s_dF, s_D, ge, t, P.hyper_horizontal != 0, g);
+        shell_strong_gradient<N, R>(x, s_H, s_dF, s_D, ge, t, PROJECT && P.hyper_horizontal != 0, g);
         R* o = hg + (size_t)e * 12 * Np + t;
 #pragma unroll
         for (int w = 0; w < 12; ++w) o[w * Np] = g[w];
@@ -404,6 +406,31 @@ cudaError_t launch_shell_passes_typed(const KParams& P, const void* Q, void* hd,
     return cudaGetLastError();
 }
 
+// the viscous gradient pass: grad u, grad h_tot (Np, 12, nelem)
+template <int N, typename R, bool MIXED>
+cudaError_t launch_shell_visc_typed(const KParams& P, const void* Q, void* gout, cudaStream_t s) {
+    constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp, NFN = 6 * Nfp, NT = ShellDims<N>::NT;
+    constexpr size_t b1 = sizeof(R) * (planar_pad<R>(5 * Np) + 4 * Np + 12 * NFN + Nq * Nq);
+    cudaError_t e;
+    if ((e = opt_in(shell_hyper_grad_kernel<N, R, MIXED, false>, b1)) != cudaSuccess) return e;
+    shell_hyper_grad_kernel<N, R, MIXED, false><<<P.nelem, NT, b1, s>>>(P, Q, static_cast<R*>(gout));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shell_visc(const KParams& P, int N, bool mixed, const void* Q, void* gout, cudaStream_t s) {
+    switch (N) {
+        case 2: return mixed ? launch_shell_visc_typed<2, float, true>(P, Q, gout, s)
+                             : launch_shell_visc_typed<2, double, false>(P, Q, gout, s);
+        case 3: return mixed ? launch_shell_visc_typed<3, float, true>(P, Q, gout, s)
+                             : launch_shell_visc_typed<3, double, false>(P, Q, gout, s);
+        case 4: return mixed ? launch_shell_visc_typed<4, float, true>(P, Q, gout, s)
+                             : launch_shell_visc_typed<4, double, false>(P, Q, gout, s);
+        case 5: return mixed ? launch_shell_visc_typed<5, float, true>(P, Q, gout, s)
+                             : launch_shell_visc_typed<5, double, false>(P, Q, gout, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 cudaError_t launch_shell_passes(const KParams& P, int N, bool mixed, const void* Q, void* hd, void* hl,
                                 cudaStream_t s) {
     switch (N) {
@@ -523,6 +550,80 @@ int launch_shell_hyper_passes(Model* md, const void* Qin, void* hd_out, cudaStre
     const cudaError_t err = launch_shell_passes(P, m.N, md->precision == CMDG_MIXED, Qin, hd_out, md->d_hlap, s);
     if (err != cudaSuccess) {
         set_error("cubed-shell hyperdiffusion pass launch failed: %s", cudaGetErrorString(err));
+        return CMDG_ERR_CUDA;
+    }
+    return CMDG_OK;
+}
+
+// The gradient buffer of the viscous pass and, in mixed precision, the
+// FP64 gradient of the reference h_tot (the viscous pass on the reference
+// state at rest: u = 0, h_tot = h_ref; the pass is linear in its arguments).
+int init_shell_visc_tables(Model* md) {
+    const Mesh& m = *md->mesh;
+    const int Np = m.Np;
+    const size_t nn = (size_t)m.nelem * Np;
+    const bool mixed = md->precision == CMDG_MIXED;
+    const size_t elt = mixed ? sizeof(float) : sizeof(double);
+    CMDG_CUDA_CHECK(cudaMalloc(&md->d_gf, nn * 12 * elt));
+    CMDG_CUDA_CHECK(cudaMemset(md->d_gf, 0, nn * 12 * elt));
+    CMDG_CUDA_CHECK(cudaMalloc(&md->d_vgref, nn * 3 * sizeof(float)));
+    CMDG_CUDA_CHECK(cudaMemset(md->d_vgref, 0, nn * 3 * sizeof(float)));
+    if (!mixed || !md->prm.ref_state) return CMDG_OK;
+    std::vector<double> qref(nn * NSTATE, 0.0);
+    for (int64_t e = 0; e < m.nelem; ++e)
+        for (int n = 0; n < Np; ++n) {
+            qref[((size_t)e * NSTATE + 0) * Np + n] = md->ref64[((size_t)e * 2 + 0) * Np + n];
+            qref[((size_t)e * NSTATE + 4) * Np + n] = md->ref64[((size_t)e * 2 + 1) * Np + n];
+        }
+    double *dq = nullptr, *dg = nullptr;
+    cudaError_t ce = cudaMalloc(&dq, nn * NSTATE * sizeof(double));
+    if (ce == cudaSuccess) ce = cudaMalloc(&dg, nn * 12 * sizeof(double));
+    if (ce == cudaSuccess) ce = cudaMemcpy(dq, qref.data(), nn * NSTATE * sizeof(double), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) {
+        LaunchArgs a;
+        a.Qin = dq;
+        a.Qout = nullptr;
+        a.dQ = nullptr;
+        a.alpha = a.beta = a.rka = a.rkb_dt = 0;
+        a.mode = 0;
+        KParams P = make_params(md, a);
+        P.Dhat = md->d_Dhat64;
+        P.geo = md->d_geo64;
+        ce = launch_shell_visc(P, m.N, false, dq, dg, 0);
+        if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
+    }
+    std::vector<double> g64;
+    if (ce == cudaSuccess) {
+        g64.resize(nn * 12);
+        ce = cudaMemcpy(g64.data(), dg, nn * 12 * sizeof(double), cudaMemcpyDeviceToHost);
+    }
+    cudaFree(dq);
+    cudaFree(dg);
+    if (ce != cudaSuccess) {
+        set_error("reference viscous gradient pass failed: %s", cudaGetErrorString(ce));
+        return CMDG_ERR_CUDA;
+    }
+    std::vector<float> ref32(nn * 3);
+    for (int64_t e = 0; e < m.nelem; ++e)
+        for (int j = 0; j < 3; ++j)
+            for (int n = 0; n < Np; ++n)
+                ref32[((size_t)e * 3 + j) * Np + n] = (float)g64[((size_t)e * 12 + 9 + j) * Np + n];
+    CMDG_CUDA_CHECK(cudaMemcpy(md->d_vgref, ref32.data(), nn * 3 * sizeof(float), cudaMemcpyHostToDevice));
+    return CMDG_OK;
+}
+
+int launch_shell_visc_gradient(Model* md, const void* Qin, void* gout, cudaStream_t s) {
+    const Mesh& m = *md->mesh;
+    LaunchArgs a;
+    a.Qin = Qin;
+    a.Qout = nullptr;
+    a.dQ = nullptr;
+    a.alpha = a.beta = a.rka = a.rkb_dt = 0;
+    a.mode = 0;
+    const KParams P = make_params(md, a);
+    const cudaError_t err = launch_shell_visc(P, m.N, md->precision == CMDG_MIXED, Qin, gout, s);
+    if (err != cudaSuccess) {
+        set_error("cubed-shell viscous gradient pass launch failed: %s", cudaGetErrorString(err));
         return CMDG_ERR_CUDA;
     }
     return CMDG_OK;

@@ -31,6 +31,7 @@
 // FP64-computed level jump across vertical faces plus the difference of the
 // two nodes' per-node parts.
 #include "shell_common.cuh"
+#include "viscous_common.cuh"
 
 namespace cmdg {
 namespace {
@@ -55,8 +56,42 @@ struct ShellSmem {
 // tendencies_energy.jl:40-48) join the volume flux and, with the neighbour's
 // state, the central second-order interface flux; walls carry the
 // first-order flux only (boundaryconditions.jl:113-185).
-template <int N, typename R, bool MIXED, int MODE, bool HYPER>
-__global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER ? 4 : ShellDims<N>::MIN_CTAS)
+//
+// VISC: ConstantDynamicViscosity, whose gradient state grad u, grad h_tot
+// (Np, 12, nelem; word 3 c + d = d u_c / dx_d, 9 + d = d h_tot / dx_d, in
+// mixed precision d h' / dx_d with the FP64 grad h_ref added here) is read
+// from P.gf: the viscous fluxes tau rho, tau . rho u - D_t grad h_tot rho
+// (tendencies_momentum.jl:37-42, tendencies_energy.jl:27-31, 51-56;
+// TurbulenceClosures.jl:199-225, 368-404) join the volume flux and, with
+// the neighbour's state, the central second-order interface flux; walls
+// carry the first-order flux only.
+// gradient-flux words [grad h_tot (3), S11, S21, S31, S22, S32, S33] from the
+// shell viscous pass's grad u, grad h_tot at node n of element e (compute_gradient_flux!,
+// TurbulenceClosures.jl:240-252, energy.jl:10-11)
+template <typename R, bool MIXED>
+__device__ __forceinline__ void shell_gf(const KParams& P, int64_t e, int n, int Np, R gf[NGF]) {
+    const R* g = static_cast<const R*>(P.gf) + (size_t)e * 12 * Np + n;
+    R G[12];
+#pragma unroll
+    for (int w = 0; w < 12; ++w) G[w] = g[w * Np];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) gf[d] = G[9 + d];
+    if (MIXED && P.ph.ref_state) {
+        const float* r = P.vgref32 + (size_t)e * 3 * Np + n;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) gf[d] += (R)r[d * Np];
+    }
+    gf[3] = G[0];
+    gf[4] = (G[1] + G[3]) / 2;
+    gf[5] = (G[2] + G[6]) / 2;
+    gf[6] = G[4];
+    gf[7] = (G[5] + G[7]) / 2;
+    gf[8] = G[8];
+    if (NGF > 9) gf[NGF - 1] = 0;
+}
+
+template <int N, typename R, bool MIXED, int MODE, bool HYPER, bool VISC>
+__global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER || VISC ? 4 : ShellDims<N>::MIN_CTAS)
                                                           : ShellDims<N>::MIN_CTAS64)
     shell_stage_kernel(const KParams P) {
     using Dm = ShellDims<N>;
@@ -151,6 +186,19 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER ? 4 : ShellDi
             add_hyper(F1, 1);
             add_hyper(F2, 2);
         }
+        if (VISC) {
+            R gfw[NGF], Fv[3][NSTATE];
+            shell_gf<R, MIXED>(P, e, t, Np, gfw);
+            const R rho = MIXED ? lv.rho_ref + q[0] : q[0];
+            const R ru[3] = {q[1], q[2], q[3]};
+            flux2<R, CMDG_TURB_CONSTANT>(P, rho, th.rinv, ru, gfw, R(0), R(0), Fv);
+#pragma unroll
+            for (int s2 = 0; s2 < NSTATE; ++s2) {
+                F0[s2] += Fv[0][s2];
+                F1[s2] += Fv[1][s2];
+                F2[s2] += Fv[2][s2];
+            }
+        }
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             R Ft[NSTATE];
@@ -213,7 +261,7 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER ? 4 : ShellDi
             for (int s = 0; s < NSTATE; ++s) qp[s] = qm[s];
 #pragma unroll
             for (int c = 0; c < 3; ++c) qp[1 + c] = qm[1 + c] - R(2) * mn_m * nv[c];
-            if (HYPER) {
+            if (HYPER || VISC) {
                 // the staged flux holds the second-order part too: walls take the first-order one
                 const Level<R> lvm = shell_level<R, MIXED>(P, ge, Np, vM, ez * Nq + kM);
                 const Thermo<R, MIXED> thm = thermo<R, MIXED>(qm, lvm, P);
@@ -258,6 +306,16 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER ? 4 : ShellDi
 #pragma unroll
             for (int c = 0; c < 3; ++c) Fp[1 + c] += rho_p * hn_n[c];
             Fp[4] += (hn_n[0] * qp[1] + hn_n[1] * qp[2] + hn_n[2] * qp[3]) + hn_n[3] * rho_p;
+        }
+        if (VISC && nb >= 0) {
+            // neighbour's viscous flux . n
+            R gfp[NGF], Fv[3][NSTATE];
+            shell_gf<R, MIXED>(P, nb, vP, Np, gfp);
+            const R rho_p = MIXED ? lvp.rho_ref + qp[0] : qp[0];
+            const R ru_p[3] = {qp[1], qp[2], qp[3]};
+            flux2<R, CMDG_TURB_CONSTANT>(P, rho_p, thp.rinv, ru_p, gfp, R(0), R(0), Fv);
+#pragma unroll
+            for (int s2 = 0; s2 < NSTATE; ++s2) Fp[s2] += nv[0] * Fv[0][s2] + nv[1] * Fv[1][s2] + nv[2] * Fv[2][s2];
         }
         const R lam_p = fabs(un_p) + thp.c;
         const R lift = sJ * iJm * KConst<R>::inv_w0(P);
@@ -333,7 +391,7 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER ? 4 : ShellDi
     if (__any_sync(0xffffffffu, bad) && (t & 31) == 0) atomicOr(P.status, 1u);
 }
 
-template <int N, typename R, bool MIXED, int MODE, bool HYPER>
+template <int N, typename R, bool MIXED, int MODE, bool HYPER, bool VISC>
 cudaError_t launch_shell_typed(const KParams& P, cudaStream_t s) {
     constexpr size_t bytes = ShellSmem<N, R>::BYTES;
     static unsigned long long configured = 0;
@@ -341,27 +399,30 @@ cudaError_t launch_shell_typed(const KParams& P, cudaStream_t s) {
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (!(configured & (1ull << (dev & 63)))) {
-        e = cudaFuncSetAttribute(shell_stage_kernel<N, R, MIXED, MODE, HYPER>,
+        e = cudaFuncSetAttribute(shell_stage_kernel<N, R, MIXED, MODE, HYPER, VISC>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
         if (e != cudaSuccess) return e;
         configured |= 1ull << (dev & 63);
     }
-    shell_stage_kernel<N, R, MIXED, MODE, HYPER><<<(unsigned)P.nelem, ShellDims<N>::NT, bytes, s>>>(P);
+    shell_stage_kernel<N, R, MIXED, MODE, HYPER, VISC><<<(unsigned)P.nelem, ShellDims<N>::NT, bytes, s>>>(P);
     return cudaGetLastError();
 }
 
-template <int N, bool HYPER>
+template <int N, bool HYPER, bool VISC>
 cudaError_t launch_shell_N(const KParams& P, bool mixed, int mode, cudaStream_t s) {
     if (mixed)
-        return mode == 0 ? launch_shell_typed<N, float, true, 0, HYPER>(P, s)
-                         : launch_shell_typed<N, float, true, 1, HYPER>(P, s);
-    return mode == 0 ? launch_shell_typed<N, double, false, 0, HYPER>(P, s)
-                     : launch_shell_typed<N, double, false, 1, HYPER>(P, s);
+        return mode == 0 ? launch_shell_typed<N, float, true, 0, HYPER, VISC>(P, s)
+                         : launch_shell_typed<N, float, true, 1, HYPER, VISC>(P, s);
+    return mode == 0 ? launch_shell_typed<N, double, false, 0, HYPER, VISC>(P, s)
+                     : launch_shell_typed<N, double, false, 1, HYPER, VISC>(P, s);
 }
 
+// hyperdiffusion and viscosity are exclusive on the shell (cmdg_model_create)
 template <int N>
-cudaError_t launch_shell_N(const KParams& P, bool mixed, int mode, bool hyper, cudaStream_t s) {
-    return hyper ? launch_shell_N<N, true>(P, mixed, mode, s) : launch_shell_N<N, false>(P, mixed, mode, s);
+cudaError_t launch_shell_N(const KParams& P, bool mixed, int mode, bool hyper, bool visc, cudaStream_t s) {
+    if (hyper) return launch_shell_N<N, true, false>(P, mixed, mode, s);
+    if (visc) return launch_shell_N<N, false, true>(P, mixed, mode, s);
+    return launch_shell_N<N, false, false>(P, mixed, mode, s);
 }
 
 }  // namespace
@@ -369,18 +430,23 @@ cudaError_t launch_shell_N(const KParams& P, bool mixed, int mode, bool hyper, c
 int launch_shell_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
     const Mesh& m = *md->mesh;
     const bool hyper = md->prm.hyperdiffusion != CMDG_HYPER_NONE;
+    const bool visc = md->prm.turbulence != CMDG_TURB_NONE;
     if (hyper) {
         const int rc = launch_shell_hyper_passes(md, a.Qin, md->d_hd, s);
+        if (rc) return rc;
+    }
+    if (visc) {
+        const int rc = launch_shell_visc_gradient(md, a.Qin, md->d_gf, s);
         if (rc) return rc;
     }
     const KParams P = make_params(md, a);
     const bool mixed = md->precision == CMDG_MIXED;
     cudaError_t err;
     switch (m.N) {
-        case 2: err = launch_shell_N<2>(P, mixed, a.mode, hyper, s); break;
-        case 3: err = launch_shell_N<3>(P, mixed, a.mode, hyper, s); break;
-        case 4: err = launch_shell_N<4>(P, mixed, a.mode, hyper, s); break;
-        case 5: err = launch_shell_N<5>(P, mixed, a.mode, hyper, s); break;
+        case 2: err = launch_shell_N<2>(P, mixed, a.mode, hyper, visc, s); break;
+        case 3: err = launch_shell_N<3>(P, mixed, a.mode, hyper, visc, s); break;
+        case 4: err = launch_shell_N<4>(P, mixed, a.mode, hyper, visc, s); break;
+        case 5: err = launch_shell_N<5>(P, mixed, a.mode, hyper, visc, s); break;
         default:
             set_error("no cubed-shell stage kernel for N=%d", m.N);
             return CMDG_ERR_ARG;

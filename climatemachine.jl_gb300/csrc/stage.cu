@@ -602,6 +602,7 @@ KParams make_params(Model* md, const LaunchArgs& a) {
     P.fpart = m.d_fpart;
     P.fjump = md->d_fjump;
     P.hglap_ref32 = md->d_hglap_ref;
+    P.vgref32 = md->d_vgref;
     return P;
 }
 

@@ -8,7 +8,11 @@
 * mixed precision: tendency within 1e-4 and 100 LSRK54 steps within 1e-5 of
   the FP64 oracle; the full GCM workload (6 x 12 x 12 x 6 elements, N = 4,
   30 km lid) within 1e-5 of the GPU FP64 run after 200 steps;
-* compensated sums and the Courant time step against the oracle.
+* compensated sums and the Courant time step against the oracle;
+* ConstantDynamicViscosity (with and without divergence) on the shell: the
+  FP64 tendency within 1e-9 (its viscous part within 1e-8 of its own scale),
+  FP64 LSRK54 steps within 1e-10, the mixed tendency within 1e-4 and 20
+  mixed steps within 1e-5 of the FP64 oracle.
 """
 import math
 
@@ -159,3 +163,70 @@ def test_gcm_workload_mixed_200_steps_within_1e5_of_fp64():
         rel.append(float(err / ref))
     assert max(rel) < 1e-5, rel
     assert d64.status_word() == 0 and dmx.status_word() == 0
+
+
+def visc_pair(N, nh, nv, precision="fp64", with_divergence=False, rho_nu=2e4, H=30e3):
+    """ConstantDynamicViscosity on the cubed shell: oracle and GPU models and a
+    sheared initial state (the GCM state plus seeded velocity noise)."""
+    om = O.OracleModel(N, shell=dict(nhorz=nh, nvert=nv, r_inner=R, r_outer=R + H), orientation="sphere",
+                       gravity=True, ref_state=True, profile="isothermal", T_surface=285.0, turbulence="constant",
+                       rho_nu=rho_nu, with_divergence=with_divergence)
+    grid = cmdg.CubedShellGrid(N, nh, nv, R, R + H)
+    model = cmdg.AtmosModel(orientation="sphere", gravity=True,
+                            ref_state=cmdg.HydrostaticState(cmdg.IsothermalProfile(285.0)), turbulence="constant",
+                            rho_nu=rho_nu, with_divergence=with_divergence)
+    dg = cmdg.DGModel(model, grid, precision=precision)
+    Q0 = workloads.gcm_initial_state(grid.coordinates(), seed=5)
+    rng = np.random.default_rng(8)
+    Q0[:, 1:4] += rng.uniform(-3, 3, size=Q0[:, 1:4].shape)
+    return om, dg, Q0
+
+
+@pytest.mark.parametrize("with_divergence", [False, True])
+@pytest.mark.parametrize("N", [3, 4])
+def test_shell_viscous_fp64_tendency_matches_oracle(N, with_divergence):
+    """The viscous part (tendency minus the inviscid model's) to 1e-8 of its
+    own scale, the whole tendency to 1e-9 of the field scale."""
+    om, dg, Q0 = visc_pair(N, 2, 3, with_divergence=with_divergence)
+    ref = om.tendency(Q0)
+    om0, dg0, _ = shell_pair(N, 2, 3, noise=False)
+    inv = om0.tendency(Q0)
+    Q = dg.init_ode_state(Q0)
+    dQ = dg.new_state(torch.float64)
+    dg(dQ, Q, None, 0.0)
+    got = dQ.cpu().numpy()
+    assert rel_max(got, ref).max() < 1e-9
+    vref, vgot = ref - inv, got - inv
+    for sl in (slice(1, 4), slice(4, 5)):
+        assert np.abs(vgot[:, sl] - vref[:, sl]).max() < 1e-8 * np.abs(vref[:, sl]).max()
+    assert np.abs(vref[:, 1:4]).max() > 1e-6 * np.abs(ref[:, 1:4]).max()  # the viscous part is present
+
+
+def test_shell_viscous_mixed_close_to_oracle():
+    # constant rho nu: nu = rho nu / rho grows to the lid, so the stepped runs
+    # keep it small enough for the explicit diffusive limit at Courant 0.4
+    om, dg, Q0 = visc_pair(4, 2, 3, precision="mixed", rho_nu=20.0)
+    ref = om.tendency(Q0)
+    Q = dg.init_ode_state(Q0)
+    dQ = torch.zeros(Q.shape, dtype=torch.float64, device=Q.device)
+    dg(dQ, Q, None, 0.0)
+    got = dQ.cpu().numpy()
+    err = [np.linalg.norm(got[:, s] - ref[:, s]) / np.linalg.norm(ref[:, s]) for s in range(5)]
+    assert max(err) < 1e-4, err
+    # 20 LSRK54 steps: relative L2 per field group within 1e-5 of the FP64 oracle
+    dt = om.courant_dt(Q0, 0.4)
+    Qo, _ = om.lsrk54(Q0.copy(), dt, 20)
+    lsrk = cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt)
+    cmdg.dostep_(Q, lsrk, None, 0.0, 20)
+    err = field_rel(om, dg.from_perturbation(Q).cpu().numpy(), Qo)
+    assert err.max() < 1e-5, err
+
+
+def test_shell_viscous_fp64_steps_match_oracle():
+    om, dg, Q0 = visc_pair(3, 2, 2, rho_nu=20.0)
+    dt = om.courant_dt(Q0, 0.4)
+    Qo, _ = om.lsrk54(Q0.copy(), dt, 5)
+    Q = dg.init_ode_state(Q0)
+    lsrk = cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt)
+    cmdg.dostep_(Q, lsrk, None, 0.0, 5)
+    assert rel_max(Q.cpu().numpy(), Qo).max() < 1e-10
