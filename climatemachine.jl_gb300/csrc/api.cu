@@ -260,8 +260,8 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
     } else if (shell) {
         CMDG_ARG_CHECK(p->orientation == CMDG_ORIENT_NONE || p->orientation == CMDG_ORIENT_SPHERE,
                        "orientation %d is not available on a cubed shell", p->orientation);
-        CMDG_ARG_CHECK(p->turbulence == CMDG_TURB_NONE || p->turbulence == CMDG_TURB_CONSTANT,
-                       "the cubed-shell kernels run ConstantDynamicViscosity or no closure");
+        CMDG_ARG_CHECK(p->turbulence != CMDG_TURB_SMAGORINSKY || precision == CMDG_FP64,
+                       "SmagorinskyLilly on the cubed shell runs FP64 models");
         CMDG_ARG_CHECK(p->turbulence == CMDG_TURB_NONE || p->hyperdiffusion == CMDG_HYPER_NONE,
                        "the cubed-shell kernels run viscosity or hyperdiffusion, not both");
         CMDG_ARG_CHECK(p->orientation != CMDG_ORIENT_SPHERE || p->planet_radius > 0, "planet_radius must be positive");
@@ -273,7 +273,7 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
     CMDG_ARG_CHECK(p->turbulence == CMDG_TURB_NONE || p->turbulence == CMDG_TURB_CONSTANT ||
                        p->turbulence == CMDG_TURB_SMAGORINSKY,
                    "unknown turbulence closure %d", p->turbulence);
-    CMDG_ARG_CHECK(p->turbulence != CMDG_TURB_SMAGORINSKY || p->orientation == CMDG_ORIENT_FLAT,
+    CMDG_ARG_CHECK(p->turbulence != CMDG_TURB_SMAGORINSKY || p->orientation != CMDG_ORIENT_NONE,
                    "SmagorinskyLilly needs an orientation (its buoyancy correction uses grad Phi)");
     CMDG_ARG_CHECK(p->hyperdiffusion == CMDG_HYPER_NONE || p->hyperdiffusion == CMDG_HYPER_DRY_BIHARMONIC,
                    "unknown hyperdiffusion %d", p->hyperdiffusion);
@@ -353,6 +353,7 @@ int cmdg_model_destroy(cmdg_model* model) {
     cudaFree(md.d_nu4);
     cudaFree(md.d_hglap_ref);
     cudaFree(md.d_vgref);
+    cudaFree(md.d_sdelta);
     cudaFree(md.d_fjump);
     cudaFree(md.d_geo64);
     cudaFree(md.d_geo32);

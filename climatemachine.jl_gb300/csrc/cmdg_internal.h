@@ -188,6 +188,7 @@ struct Model {
     void* d_nu4 = nullptr;           // cubed shell: nu_4 per node, (Np, nelem), model precision
     float* d_hglap_ref = nullptr;    // cubed shell, mixed: nu_4 grad lap h_ref per node, (Np, 3, nelem)
     float* d_vgref = nullptr;        // cubed shell, viscous, mixed: grad h_ref per node, (Np, 3, nelem)
+    double* d_sdelta = nullptr;      // cubed shell, SmagorinskyLilly: length scale per node (Np, nelem)
     // grid-arrays meshes: per-node kernel geometry on the host, per-node p_ref,
     // FP64-computed reference jumps (rho, rhoe) per face node, reference set?
     std::vector<double> arrays_geo, pref64;

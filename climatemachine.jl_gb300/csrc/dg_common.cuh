@@ -58,6 +58,7 @@ struct KParams {
     // gradient of the reference h_tot per node (Np, 3, nelem); the viscous
     // gradient pass writes grad u, grad h_tot (Np, 12, nelem) into gf
     const float* vgref32;
+    const double* sdelta;  // cubed shell, SmagorinskyLilly: length scale per node (Np, nelem)
     int hyper_horizontal;  // 1: the passes run in the horizontal directions only (HorizontalDirection)
     // grid-arrays meshes: facing node of each face node (Nfp, 6, nelem) and
     // the FP64-computed reference jumps (rho, rhoe) per face node

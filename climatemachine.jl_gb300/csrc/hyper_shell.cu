@@ -23,6 +23,9 @@
 // reference part nu_4 grad lap h_ref is computed once by the FP64 passes on
 // the reference state at rest (the passes are linear in their argument) and
 // added in the last pass.
+#include <algorithm>
+#include <cmath>
+
 #include "shell_common.cuh"
 #include "viscous_common.cuh"
 
@@ -74,9 +77,11 @@ __device__ __forceinline__ R shell_face_normal(const KParams& P, const R* g, int
 // form h_tot is the perturbation h' = (H' rho_ref - H_ref rho') / (rho rho_ref)
 // PROJECT = false: the gradient arguments of the diffusive closures, u and
 // h_tot (AtmosModel.jl:622-650, energy.jl:20-31)
-template <typename R, bool MIXED, bool PROJECT = true>
+// NA = 5 adds theta_v = T / (p / MSLP)^kappa (SmagorinskyLilly's N^2,
+// TurbulenceClosures.jl:446-454; FP64 only)
+template <typename R, bool MIXED, bool PROJECT = true, int NA = 4>
 __device__ __forceinline__ void shell_hyper_args(const KParams& P, const R q[NSTATE], const Level<R>& lv, const R* g,
-                                                 int Np, int n, R H[4]) {
+                                                 int Np, int n, R H[NA]) {
     const R gm1 = KConst<R>::gm1(P);
     const R ig = R(1) / VConst<R>::grav(P);
     const R k[3] = {g[(KG_GPHI + 0) * Np + n] * ig, g[(KG_GPHI + 1) * Np + n] * ig, g[(KG_GPHI + 2) * Np + n] * ig};
@@ -93,24 +98,28 @@ __device__ __forceinline__ void shell_hyper_args(const KParams& P, const R q[NST
     } else {
         const R p = gm1 * (q[4] - R(0.5) * ke2) + rho * lv.crho;
         H[3] = (q[4] + p) * rinv;
+        if (NA == 5) {
+            const R T = p * rinv / VConst<R>::R_d(P);
+            H[NA - 1] = T / pow_r(p / VConst<R>::MSLP(P), VConst<R>::kappa(P));
+        }
     }
 }
 
 // strong-form gradient of 4 node fields s_X[4][Np] at this node thread,
 // dxi_d/dx_j dX/dxi_d, plus the staged face terms s_dF[(3 s + j) NFN + face node]
-template <int N, typename R>
+template <int N, typename R, int NA = 4>
 __device__ __forceinline__ void shell_strong_gradient(const ShellIdx<N>& x, const R* s_X, const R* s_dF, const R* s_D,
-                                                      const R* g, int t, bool horiz, R out[12]) {
+                                                      const R* g, int t, bool horiz, R out[3 * NA]) {
     constexpr int Nq = N + 1, Np = Nq * Nq * Nq, Nfp = Nq * Nq, NFN = 6 * Nfp;
-    R a[4][3];
+    R a[NA][3];
 #pragma unroll
-    for (int s = 0; s < 4; ++s) a[s][0] = a[s][1] = a[s][2] = R(0);
+    for (int s = 0; s < NA; ++s) a[s][0] = a[s][1] = a[s][2] = R(0);
     const int L1 = Nq * (x.nj + Nq * x.nk), L2 = x.ni + Nfp * x.nk, L3 = x.ni + Nq * x.nj;
 #pragma unroll
     for (int n = 0; n < Nq; ++n) {
         const R d1 = s_D[x.ni * Nq + n], d2 = s_D[x.nj * Nq + n], d3 = s_D[x.nk * Nq + n];
 #pragma unroll
-        for (int s = 0; s < 4; ++s) {
+        for (int s = 0; s < NA; ++s) {
             a[s][0] = fma(d1, s_X[s * Np + L1 + n], a[s][0]);
             a[s][1] = fma(d2, s_X[s * Np + L2 + n * Nq], a[s][1]);
             a[s][2] = fma(d3, s_X[s * Np + L3 + n * Nfp], a[s][2]);
@@ -122,16 +131,16 @@ __device__ __forceinline__ void shell_strong_gradient(const ShellIdx<N>& x, cons
     const R iJ = g[KG_INVJ * Np + t];
     if (horiz) {  // HorizontalDirection: no xi3 derivative
 #pragma unroll
-        for (int s = 0; s < 4; ++s) a[s][2] = R(0);
+        for (int s = 0; s < NA; ++s) a[s][2] = R(0);
     }
 #pragma unroll
-    for (int s = 0; s < 4; ++s)
+    for (int s = 0; s < NA; ++s)
 #pragma unroll
         for (int j = 0; j < 3; ++j) out[3 * s + j] = iJ * (Jx[j] * a[s][0] + Jx[3 + j] * a[s][1] + Jx[6 + j] * a[s][2]);
     auto add = [&](int ff) {
         const int idx = ff * Nfp + x.on_face(ff);
 #pragma unroll
-        for (int w = 0; w < 12; ++w) out[w] += s_dF[w * NFN + idx];
+        for (int w = 0; w < 3 * NA; ++w) out[w] += s_dF[w * NFN + idx];
     };
     if (x.ni == 0) add(0);
     if (x.ni == N) add(1);
@@ -149,7 +158,7 @@ __device__ __forceinline__ int shell_partner_level(const ShellIdx<N>& x, int ez,
     return ezp * Nq + vP / Nfp;
 }
 
-template <int N, typename R, bool MIXED, bool PROJECT = true>
+template <int N, typename R, bool MIXED, bool PROJECT = true, int NA = 4>
 __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(const KParams P, const void* Qv,
                                                                             R* __restrict__ hg) {
     using Ix = ShellIdx<N>;
@@ -158,9 +167,9 @@ __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(cons
     using PL = Planar5<R>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* const s_q = reinterpret_cast<R*>(smem_raw);  // planar records: states
-    R* const s_H = s_q + planar_pad<R>(5 * Np);      // [4][Np] arguments
-    R* const s_dF = s_H + 4 * Np;                    // [12][NFN] lifted face terms
-    R* const s_D = s_dF + 12 * NFN;                  // strong-form D
+    R* const s_H = s_q + planar_pad<R>(5 * Np);      // [NA][Np] arguments
+    R* const s_dF = s_H + NA * Np;                   // [3 NA][NFN] lifted face terms
+    R* const s_D = s_dF + 3 * NA * NFN;              // strong-form D
 
     const int e = blockIdx.x, t = threadIdx.x;
     const Ix x(t);
@@ -184,23 +193,23 @@ __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(cons
         for (int s = 0; s < NSTATE; ++s) qp[s] = qn[s * Np];
     }
     if (x.node) {
-        R H[4];
+        R H[NA];
         const Level<R> lv = shell_level<R, MIXED>(P, ge, Np, t, ez * Nq + x.nk);
-        shell_hyper_args<R, MIXED, PROJECT>(P, q, lv, ge, Np, t, H);
+        shell_hyper_args<R, MIXED, PROJECT, NA>(P, q, lv, ge, Np, t, H);
         PL::st(s_q, Np, t, q);
 #pragma unroll
-        for (int s = 0; s < 4; ++s) s_H[s * Np + t] = H[s];
+        for (int s = 0; s < NA; ++s) s_H[s * Np + t] = H[s];
     }
     __syncthreads();
 
     if (x.face) {
-        R nv[3], Hp[4], c;
+        R nv[3], Hp[NA], c;
         R lift = shell_face_normal<R>(P, ge, Np, x.fd, x.fside ? R(1) : R(-1), x.vM, nv);
         if (PROJECT && P.hyper_horizontal && x.fd == 2) lift = R(0);  // HorizontalDirection: no xi3 face terms
         if (nb >= 0) {
             const R* gp = geo + (size_t)nb * GSTRIDE;
             const Level<R> lvp = shell_level<R, MIXED>(P, gp, Np, vP, shell_partner_level<N>(x, ez, vP));
-            shell_hyper_args<R, MIXED, PROJECT>(P, qp, lvp, gp, Np, vP, Hp);
+            shell_hyper_args<R, MIXED, PROJECT, NA>(P, qp, lvp, gp, Np, vP, Hp);
             c = R(0.5);
         } else {
             // FreeSlip state of the gradient flux: rhou+ = rhou- - (rhou-.n) n
@@ -210,11 +219,11 @@ __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(cons
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc) qb[1 + cc] -= mn * nv[cc];
             const Level<R> lvm = shell_level<R, MIXED>(P, ge, Np, x.vM, ez * Nq + x.kM);
-            shell_hyper_args<R, MIXED, PROJECT>(P, qb, lvm, ge, Np, x.vM, Hp);
+            shell_hyper_args<R, MIXED, PROJECT, NA>(P, qb, lvm, ge, Np, x.vM, Hp);
             c = R(1);
         }
 #pragma unroll
-        for (int s = 0; s < 4; ++s) {
+        for (int s = 0; s < NA; ++s) {
             const R dh = c * lift * (Hp[s] - s_H[s * Np + x.vM]);
 #pragma unroll
             for (int j = 0; j < 3; ++j) s_dF[(3 * s + j) * NFN + t] = dh * nv[j];
@@ -223,11 +232,11 @@ __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(cons
     __syncthreads();
 
     if (x.node) {
-        R g[12];
-        shell_strong_gradient<N, R>(x, s_H, s_dF, s_D, ge, t, PROJECT && P.hyper_horizontal != 0, g);
-        R* o = hg + (size_t)e * 12 * Np + t;
+        R g[3 * NA];
+        shell_strong_gradient<N, R, NA>(x, s_H, s_dF, s_D, ge, t, PROJECT && P.hyper_horizontal != 0, g);
+        R* o = hg + (size_t)e * 3 * NA * Np + t;
 #pragma unroll
-        for (int w = 0; w < 12; ++w) o[w * Np] = g[w];
+        for (int w = 0; w < 3 * NA; ++w) o[w * Np] = g[w];
     }
 }
 
@@ -407,26 +416,38 @@ cudaError_t launch_shell_passes_typed(const KParams& P, const void* Q, void* hd,
 }
 
 // the viscous gradient pass: grad u, grad h_tot (Np, 12, nelem)
-template <int N, typename R, bool MIXED>
+template <int N, typename R, bool MIXED, int NA>
 cudaError_t launch_shell_visc_typed(const KParams& P, const void* Q, void* gout, cudaStream_t s) {
     constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp, NFN = 6 * Nfp, NT = ShellDims<N>::NT;
-    constexpr size_t b1 = sizeof(R) * (planar_pad<R>(5 * Np) + 4 * Np + 12 * NFN + Nq * Nq);
+    constexpr size_t b1 = sizeof(R) * (planar_pad<R>(5 * Np) + NA * Np + 3 * NA * NFN + Nq * Nq);
     cudaError_t e;
-    if ((e = opt_in(shell_hyper_grad_kernel<N, R, MIXED, false>, b1)) != cudaSuccess) return e;
-    shell_hyper_grad_kernel<N, R, MIXED, false><<<P.nelem, NT, b1, s>>>(P, Q, static_cast<R*>(gout));
+    if ((e = opt_in(shell_hyper_grad_kernel<N, R, MIXED, false, NA>, b1)) != cudaSuccess) return e;
+    shell_hyper_grad_kernel<N, R, MIXED, false, NA><<<P.nelem, NT, b1, s>>>(P, Q, static_cast<R*>(gout));
     return cudaGetLastError();
 }
 
-cudaError_t launch_shell_visc(const KParams& P, int N, bool mixed, const void* Q, void* gout, cudaStream_t s) {
+// grad u, grad h_tot (12 words); with smag also grad theta_v (15 words, FP64)
+cudaError_t launch_shell_visc(const KParams& P, int N, bool mixed, bool smag, const void* Q, void* gout,
+                              cudaStream_t s) {
+    if (smag) {
+        if (mixed) return cudaErrorInvalidValue;
+        switch (N) {
+            case 2: return launch_shell_visc_typed<2, double, false, 5>(P, Q, gout, s);
+            case 3: return launch_shell_visc_typed<3, double, false, 5>(P, Q, gout, s);
+            case 4: return launch_shell_visc_typed<4, double, false, 5>(P, Q, gout, s);
+            case 5: return launch_shell_visc_typed<5, double, false, 5>(P, Q, gout, s);
+            default: return cudaErrorInvalidValue;
+        }
+    }
     switch (N) {
-        case 2: return mixed ? launch_shell_visc_typed<2, float, true>(P, Q, gout, s)
-                             : launch_shell_visc_typed<2, double, false>(P, Q, gout, s);
-        case 3: return mixed ? launch_shell_visc_typed<3, float, true>(P, Q, gout, s)
-                             : launch_shell_visc_typed<3, double, false>(P, Q, gout, s);
-        case 4: return mixed ? launch_shell_visc_typed<4, float, true>(P, Q, gout, s)
-                             : launch_shell_visc_typed<4, double, false>(P, Q, gout, s);
-        case 5: return mixed ? launch_shell_visc_typed<5, float, true>(P, Q, gout, s)
-                             : launch_shell_visc_typed<5, double, false>(P, Q, gout, s);
+        case 2: return mixed ? launch_shell_visc_typed<2, float, true, 4>(P, Q, gout, s)
+                             : launch_shell_visc_typed<2, double, false, 4>(P, Q, gout, s);
+        case 3: return mixed ? launch_shell_visc_typed<3, float, true, 4>(P, Q, gout, s)
+                             : launch_shell_visc_typed<3, double, false, 4>(P, Q, gout, s);
+        case 4: return mixed ? launch_shell_visc_typed<4, float, true, 4>(P, Q, gout, s)
+                             : launch_shell_visc_typed<4, double, false, 4>(P, Q, gout, s);
+        case 5: return mixed ? launch_shell_visc_typed<5, float, true, 4>(P, Q, gout, s)
+                             : launch_shell_visc_typed<5, double, false, 4>(P, Q, gout, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -563,9 +584,26 @@ int init_shell_visc_tables(Model* md) {
     const int Np = m.Np;
     const size_t nn = (size_t)m.nelem * Np;
     const bool mixed = md->precision == CMDG_MIXED;
+    const bool smag = md->prm.turbulence == CMDG_TURB_SMAGORINSKY;
     const size_t elt = mixed ? sizeof(float) : sizeof(double);
-    CMDG_CUDA_CHECK(cudaMalloc(&md->d_gf, nn * 12 * elt));
-    CMDG_CUDA_CHECK(cudaMemset(md->d_gf, 0, nn * 12 * elt));
+    const int ngw = smag ? 15 : 12;
+    CMDG_CUDA_CHECK(cudaMalloc(&md->d_gf, nn * ngw * elt));
+    CMDG_CUDA_CHECK(cudaMemset(md->d_gf, 0, nn * ngw * elt));
+    if (smag) {
+        // Smagorinsky length scale 2 / (cbrt(det(dxi/dx)) N) per node (Geometry.jl:121-122)
+        std::vector<double> delta(nn);
+        for (int64_t e = 0; e < m.nelem; ++e)
+            for (int n = 0; n < Np; ++n) {
+                const double* G = &m.cgeo[(size_t)e * CG_NFIELDS * Np];
+                auto X = [&](int w) { return G[(CG_XI + w) * Np + n]; };
+                // rows d = xi_d, columns j = x_j
+                const double a = X(0), b = X(1), c = X(2), d = X(3), f = X(4), g = X(5), h = X(6), i = X(7), j = X(8);
+                const double det = a * (f * j - g * i) - b * (d * j - g * h) + c * (d * i - f * h);
+                delta[(size_t)e * Np + n] = 2 / (std::cbrt(det) * std::max(1, m.N));
+            }
+        CMDG_CUDA_CHECK(cudaMalloc(&md->d_sdelta, nn * sizeof(double)));
+        CMDG_CUDA_CHECK(cudaMemcpy(md->d_sdelta, delta.data(), nn * sizeof(double), cudaMemcpyHostToDevice));
+    }
     CMDG_CUDA_CHECK(cudaMalloc(&md->d_vgref, nn * 3 * sizeof(float)));
     CMDG_CUDA_CHECK(cudaMemset(md->d_vgref, 0, nn * 3 * sizeof(float)));
     if (!mixed || !md->prm.ref_state) return CMDG_OK;
@@ -589,7 +627,7 @@ int init_shell_visc_tables(Model* md) {
         KParams P = make_params(md, a);
         P.Dhat = md->d_Dhat64;
         P.geo = md->d_geo64;
-        ce = launch_shell_visc(P, m.N, false, dq, dg, 0);
+        ce = launch_shell_visc(P, m.N, false, false, dq, dg, 0);
         if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
     }
     std::vector<double> g64;
@@ -621,7 +659,8 @@ int launch_shell_visc_gradient(Model* md, const void* Qin, void* gout, cudaStrea
     a.alpha = a.beta = a.rka = a.rkb_dt = 0;
     a.mode = 0;
     const KParams P = make_params(md, a);
-    const cudaError_t err = launch_shell_visc(P, m.N, md->precision == CMDG_MIXED, Qin, gout, s);
+    const cudaError_t err = launch_shell_visc(P, m.N, md->precision == CMDG_MIXED,
+                                              md->prm.turbulence == CMDG_TURB_SMAGORINSKY, Qin, gout, s);
     if (err != cudaSuccess) {
         set_error("cubed-shell viscous gradient pass launch failed: %s", cudaGetErrorString(err));
         return CMDG_ERR_CUDA;

@@ -65,15 +65,19 @@ struct ShellSmem {
 // TurbulenceClosures.jl:199-225, 368-404) join the volume flux and, with
 // the neighbour's state, the central second-order interface flux; walls
 // carry the first-order flux only.
-// gradient-flux words [grad h_tot (3), S11, S21, S31, S22, S32, S33] from the
-// shell viscous pass's grad u, grad h_tot at node n of element e (compute_gradient_flux!,
-// TurbulenceClosures.jl:240-252, energy.jl:10-11)
-template <typename R, bool MIXED>
-__device__ __forceinline__ void shell_gf(const KParams& P, int64_t e, int n, int Np, R gf[NGF]) {
-    const R* g = static_cast<const R*>(P.gf) + (size_t)e * 12 * Np + n;
-    R G[12];
+// gradient-flux words [grad h_tot (3), S11, S21, S31, S22, S32, S33, N^2]
+// from the shell viscous pass's grad u, grad h_tot (and grad theta_v with
+// SmagorinskyLilly) at node n of element e with state q and reference row
+// lv (compute_gradient_flux!, TurbulenceClosures.jl:240-252, 446-470;
+// energy.jl:10-11)
+template <typename R, bool MIXED, int VT>
+__device__ __forceinline__ void shell_gf(const KParams& P, int64_t e, int n, int Np, const R q[NSTATE],
+                                         const Level<R>& lv, R gf[NGF]) {
+    constexpr int NW = VT == CMDG_TURB_SMAGORINSKY ? 15 : 12;
+    const R* g = static_cast<const R*>(P.gf) + (size_t)e * NW * Np + n;
+    R G[NW];
 #pragma unroll
-    for (int w = 0; w < 12; ++w) G[w] = g[w * Np];
+    for (int w = 0; w < NW; ++w) G[w] = g[w * Np];
 #pragma unroll
     for (int d = 0; d < 3; ++d) gf[d] = G[9 + d];
     if (MIXED && P.ph.ref_state) {
@@ -88,12 +92,46 @@ __device__ __forceinline__ void shell_gf(const KParams& P, int64_t e, int n, int
     gf[7] = (G[5] + G[7]) / 2;
     gf[8] = G[8];
     if (NGF > 9) gf[NGF - 1] = 0;
+    if (VT == CMDG_TURB_SMAGORINSKY) {
+        // N^2 = grad theta_v . grad Phi / theta_v, theta_v of the node's state
+        const R* ge = static_cast<const R*>(P.geo) + (size_t)e * KG_NFIELDS * Np;
+        const R rho = MIXED ? lv.rho_ref + q[0] : q[0];
+        const R rinv = R(1) / rho;
+        const R ke2 = (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) * rinv;
+        const R p = KConst<R>::gm1(P) * (q[4] - R(0.5) * ke2) + rho * lv.crho;
+        const R T = p * rinv / VConst<R>::R_d(P);
+        const R thv = T / pow_r(p / VConst<R>::MSLP(P), VConst<R>::kappa(P));
+        gf[9] = (G[12] * ge[(KG_GPHI + 0) * Np + n] + G[13] * ge[(KG_GPHI + 1) * Np + n] +
+                 G[14] * ge[(KG_GPHI + 2) * Np + n]) /
+                thv;
+    }
 }
 
-template <int N, typename R, bool MIXED, int MODE, bool HYPER, bool VISC>
-__global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER || VISC ? 4 : ShellDims<N>::MIN_CTAS)
+// viscous flux rows of a node (VT = the closure), khat = grad Phi / g and the
+// Smagorinsky length scale at the node for SmagorinskyLilly
+template <typename R, bool MIXED, int VT>
+__device__ __forceinline__ void shell_visc_flux(const KParams& P, int64_t e, int n, int Np, const R q[NSTATE],
+                                                const Level<R>& lv, R rinv, R F[3][NSTATE]) {
+    R gf[NGF];
+    shell_gf<R, MIXED, VT>(P, e, n, Np, q, lv, gf);
+    const R rho = MIXED ? lv.rho_ref + q[0] : q[0];
+    const R ru[3] = {q[1], q[2], q[3]};
+    if (VT == CMDG_TURB_SMAGORINSKY) {
+        const R* ge = static_cast<const R*>(P.geo) + (size_t)e * KG_NFIELDS * Np;
+        const R ig = R(1) / VConst<R>::grav(P);
+        const R khat[3] = {ge[(KG_GPHI + 0) * Np + n] * ig, ge[(KG_GPHI + 1) * Np + n] * ig,
+                           ge[(KG_GPHI + 2) * Np + n] * ig};
+        flux2<R, CMDG_TURB_SMAGORINSKY>(P, rho, rinv, ru, gf, khat, (R)P.sdelta[(size_t)e * Np + n], F);
+    } else {
+        flux2<R, CMDG_TURB_CONSTANT>(P, rho, rinv, ru, gf, R(0), R(0), F);
+    }
+}
+
+template <int N, typename R, bool MIXED, int MODE, bool HYPER, int VT>
+__global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER || VT != 0 ? 4 : ShellDims<N>::MIN_CTAS)
                                                           : ShellDims<N>::MIN_CTAS64)
     shell_stage_kernel(const KParams P) {
+    constexpr bool VISC = VT != CMDG_TURB_NONE;
     using Dm = ShellDims<N>;
     using SM = ShellSmem<N, R>;
     constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, NFN = 6 * Nfp;
@@ -187,11 +225,8 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER || VISC ? 4 :
             add_hyper(F2, 2);
         }
         if (VISC) {
-            R gfw[NGF], Fv[3][NSTATE];
-            shell_gf<R, MIXED>(P, e, t, Np, gfw);
-            const R rho = MIXED ? lv.rho_ref + q[0] : q[0];
-            const R ru[3] = {q[1], q[2], q[3]};
-            flux2<R, CMDG_TURB_CONSTANT>(P, rho, th.rinv, ru, gfw, R(0), R(0), Fv);
+            R Fv[3][NSTATE];
+            shell_visc_flux<R, MIXED, VT>(P, e, t, Np, q, lv, th.rinv, Fv);
 #pragma unroll
             for (int s2 = 0; s2 < NSTATE; ++s2) {
                 F0[s2] += Fv[0][s2];
@@ -309,11 +344,8 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER || VISC ? 4 :
         }
         if (VISC && nb >= 0) {
             // neighbour's viscous flux . n
-            R gfp[NGF], Fv[3][NSTATE];
-            shell_gf<R, MIXED>(P, nb, vP, Np, gfp);
-            const R rho_p = MIXED ? lvp.rho_ref + qp[0] : qp[0];
-            const R ru_p[3] = {qp[1], qp[2], qp[3]};
-            flux2<R, CMDG_TURB_CONSTANT>(P, rho_p, thp.rinv, ru_p, gfp, R(0), R(0), Fv);
+            R Fv[3][NSTATE];
+            shell_visc_flux<R, MIXED, VT>(P, nb, vP, Np, qp, lvp, thp.rinv, Fv);
 #pragma unroll
             for (int s2 = 0; s2 < NSTATE; ++s2) Fp[s2] += nv[0] * Fv[0][s2] + nv[1] * Fv[1][s2] + nv[2] * Fv[2][s2];
         }
@@ -391,7 +423,7 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER || VISC ? 4 :
     if (__any_sync(0xffffffffu, bad) && (t & 31) == 0) atomicOr(P.status, 1u);
 }
 
-template <int N, typename R, bool MIXED, int MODE, bool HYPER, bool VISC>
+template <int N, typename R, bool MIXED, int MODE, bool HYPER, int VT>
 cudaError_t launch_shell_typed(const KParams& P, cudaStream_t s) {
     constexpr size_t bytes = ShellSmem<N, R>::BYTES;
     static unsigned long long configured = 0;
@@ -399,30 +431,36 @@ cudaError_t launch_shell_typed(const KParams& P, cudaStream_t s) {
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (!(configured & (1ull << (dev & 63)))) {
-        e = cudaFuncSetAttribute(shell_stage_kernel<N, R, MIXED, MODE, HYPER, VISC>,
+        e = cudaFuncSetAttribute(shell_stage_kernel<N, R, MIXED, MODE, HYPER, VT>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
         if (e != cudaSuccess) return e;
         configured |= 1ull << (dev & 63);
     }
-    shell_stage_kernel<N, R, MIXED, MODE, HYPER, VISC><<<(unsigned)P.nelem, ShellDims<N>::NT, bytes, s>>>(P);
+    shell_stage_kernel<N, R, MIXED, MODE, HYPER, VT><<<(unsigned)P.nelem, ShellDims<N>::NT, bytes, s>>>(P);
     return cudaGetLastError();
 }
 
-template <int N, bool HYPER, bool VISC>
+template <int N, bool HYPER, int VT>
 cudaError_t launch_shell_N(const KParams& P, bool mixed, int mode, cudaStream_t s) {
     if (mixed)
-        return mode == 0 ? launch_shell_typed<N, float, true, 0, HYPER, VISC>(P, s)
-                         : launch_shell_typed<N, float, true, 1, HYPER, VISC>(P, s);
-    return mode == 0 ? launch_shell_typed<N, double, false, 0, HYPER, VISC>(P, s)
-                     : launch_shell_typed<N, double, false, 1, HYPER, VISC>(P, s);
+        return mode == 0 ? launch_shell_typed<N, float, true, 0, HYPER, VT>(P, s)
+                         : launch_shell_typed<N, float, true, 1, HYPER, VT>(P, s);
+    return mode == 0 ? launch_shell_typed<N, double, false, 0, HYPER, VT>(P, s)
+                     : launch_shell_typed<N, double, false, 1, HYPER, VT>(P, s);
 }
 
-// hyperdiffusion and viscosity are exclusive on the shell (cmdg_model_create)
+// hyperdiffusion and viscosity are exclusive on the shell, SmagorinskyLilly
+// is FP64 (cmdg_model_create)
 template <int N>
-cudaError_t launch_shell_N(const KParams& P, bool mixed, int mode, bool hyper, bool visc, cudaStream_t s) {
-    if (hyper) return launch_shell_N<N, true, false>(P, mixed, mode, s);
-    if (visc) return launch_shell_N<N, false, true>(P, mixed, mode, s);
-    return launch_shell_N<N, false, false>(P, mixed, mode, s);
+cudaError_t launch_shell_N(const KParams& P, bool mixed, int mode, bool hyper, int turb, cudaStream_t s) {
+    if (hyper) return launch_shell_N<N, true, CMDG_TURB_NONE>(P, mixed, mode, s);
+    if (turb == CMDG_TURB_CONSTANT) return launch_shell_N<N, false, CMDG_TURB_CONSTANT>(P, mixed, mode, s);
+    if (turb == CMDG_TURB_SMAGORINSKY) {
+        if (mixed) return cudaErrorInvalidValue;
+        return mode == 0 ? launch_shell_typed<N, double, false, 0, false, CMDG_TURB_SMAGORINSKY>(P, s)
+                         : launch_shell_typed<N, double, false, 1, false, CMDG_TURB_SMAGORINSKY>(P, s);
+    }
+    return launch_shell_N<N, false, CMDG_TURB_NONE>(P, mixed, mode, s);
 }
 
 }  // namespace
@@ -443,10 +481,10 @@ int launch_shell_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
     const bool mixed = md->precision == CMDG_MIXED;
     cudaError_t err;
     switch (m.N) {
-        case 2: err = launch_shell_N<2>(P, mixed, a.mode, hyper, visc, s); break;
-        case 3: err = launch_shell_N<3>(P, mixed, a.mode, hyper, visc, s); break;
-        case 4: err = launch_shell_N<4>(P, mixed, a.mode, hyper, visc, s); break;
-        case 5: err = launch_shell_N<5>(P, mixed, a.mode, hyper, visc, s); break;
+        case 2: err = launch_shell_N<2>(P, mixed, a.mode, hyper, md->prm.turbulence, s); break;
+        case 3: err = launch_shell_N<3>(P, mixed, a.mode, hyper, md->prm.turbulence, s); break;
+        case 4: err = launch_shell_N<4>(P, mixed, a.mode, hyper, md->prm.turbulence, s); break;
+        case 5: err = launch_shell_N<5>(P, mixed, a.mode, hyper, md->prm.turbulence, s); break;
         default:
             set_error("no cubed-shell stage kernel for N=%d", m.N);
             return CMDG_ERR_ARG;

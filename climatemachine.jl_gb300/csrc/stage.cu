@@ -603,6 +603,7 @@ KParams make_params(Model* md, const LaunchArgs& a) {
     P.fjump = md->d_fjump;
     P.hglap_ref32 = md->d_hglap_ref;
     P.vgref32 = md->d_vgref;
+    P.sdelta = md->d_sdelta;
     return P;
 }
 

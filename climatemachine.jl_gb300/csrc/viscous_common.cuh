@@ -103,10 +103,22 @@ __device__ __forceinline__ void grad_args(const KParams& P, const R q[NSTATE], c
     }
 }
 
-// Second-order flux rows F[d][s] (fields 1..4; field 0 has none).
+template <typename R, int TURB>
+__device__ __forceinline__ void flux2(const KParams& P, R rho, R rinv, const R ru[3], const R gf[NGF],
+                                      const R khat[3], R Delta, R F[3][NSTATE]);
+
+// brick form: khat = (0, 0, khat_z)
 template <typename R, int TURB>
 __device__ __forceinline__ void flux2(const KParams& P, R rho, R rinv, const R ru[3], const R gf[NGF], R khat_z,
                                       R Delta, R F[3][NSTATE]) {
+    const R khat[3] = {R(0), R(0), khat_z};
+    flux2<R, TURB>(P, rho, rinv, ru, gf, khat, Delta, F);
+}
+
+// Second-order flux rows F[d][s] (fields 1..4; field 0 has none).
+template <typename R, int TURB>
+__device__ __forceinline__ void flux2(const KParams& P, R rho, R rinv, const R ru[3], const R gf[NGF],
+                                      const R khat[3], R Delta, R F[3][NSTATE]) {
     const R S[3][3] = {{gf[3], gf[4], gf[5]}, {gf[4], gf[6], gf[7]}, {gf[5], gf[7], gf[8]}};
     R nu[3], tau[3][3];
     const R invPr = VConst<R>::inv_Pr(P);
@@ -129,9 +141,9 @@ __device__ __forceinline__ void flux2(const KParams& P, R rho, R rinv, const R r
         const R fb2 = sqrt(fmin(fmax(R(1) - Ri * invPr, R(0)), R(1)));
         const R cd = VConst<R>::C_smag(P) * Delta;
         const R nu0 = normS * (cd * cd) + R(1e-5);
-        // nu_v = khat (nu . khat), nu_h = nu0 - nu_v, nu = nu_h + nu_v fb2 (khat = (0, 0, khat_z) on a brick)
-        const R dnk = nu0 * khat_z;
-        const R nv[3] = {R(0), R(0), khat_z * dnk};
+        // nu_v = khat (nu . khat), nu_h = nu0 - nu_v, nu = nu_h + nu_v fb2
+        const R dnk = nu0 * khat[0] + nu0 * khat[1] + nu0 * khat[2];
+        const R nv[3] = {khat[0] * dnk, khat[1] * dnk, khat[2] * dnk};
 #pragma unroll
         for (int c = 0; c < 3; ++c) nu[c] = (nu0 - nv[c]) + nv[c] * fb2;
 #pragma unroll

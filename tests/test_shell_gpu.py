@@ -12,7 +12,9 @@
 * ConstantDynamicViscosity (with and without divergence) on the shell: the
   FP64 tendency within 1e-9 (its viscous part within 1e-8 of its own scale),
   FP64 LSRK54 steps within 1e-10, the mixed tendency within 1e-4 and 20
-  mixed steps within 1e-5 of the FP64 oracle.
+  mixed steps within 1e-5 of the FP64 oracle;
+* SmagorinskyLilly on the shell (FP64): tendency within 1e-9 (viscous part
+  1e-8), steps within 1e-10; mixed precision refused.
 """
 import math
 
@@ -163,6 +165,59 @@ def test_gcm_workload_mixed_200_steps_within_1e5_of_fp64():
         rel.append(float(err / ref))
     assert max(rel) < 1e-5, rel
     assert d64.status_word() == 0 and dmx.status_word() == 0
+
+
+def smag_pair(N, nh, nv, H=30e3):
+    """SmagorinskyLilly on the cubed shell (FP64): oracle and GPU models and
+    a sheared, stratified initial state."""
+    om = O.OracleModel(N, shell=dict(nhorz=nh, nvert=nv, r_inner=R, r_outer=R + H), orientation="sphere",
+                       gravity=True, ref_state=True, profile="isothermal", T_surface=285.0, turbulence="smagorinsky")
+    grid = cmdg.CubedShellGrid(N, nh, nv, R, R + H)
+    model = cmdg.AtmosModel(orientation="sphere", gravity=True,
+                            ref_state=cmdg.HydrostaticState(cmdg.IsothermalProfile(285.0)), turbulence="smagorinsky")
+    dg = cmdg.DGModel(model, grid)
+    Q0 = workloads.gcm_initial_state(grid.coordinates(), seed=6)
+    rng = np.random.default_rng(9)
+    Q0[:, 1:4] += rng.uniform(-3, 3, size=Q0[:, 1:4].shape)
+    return om, dg, Q0
+
+
+@pytest.mark.parametrize("N", [3, 4])
+def test_shell_smagorinsky_fp64_matches_oracle(N):
+    """SmagorinskyLilly on the shell (grad theta_v for N^2, khat = grad Phi / g
+    per node, length scale per node): the tendency within 1e-9, its viscous
+    part within 1e-8 of its own scale, and 5 LSRK54 steps within 1e-10."""
+    om, dg, Q0 = smag_pair(N, 2, 3)
+    ref = om.tendency(Q0)
+    om0, _, _ = shell_pair(N, 2, 3, noise=False)
+    inv = om0.tendency(Q0)
+    Q = dg.init_ode_state(Q0)
+    dQ = dg.new_state(torch.float64)
+    dg(dQ, Q, None, 0.0)
+    got = dQ.cpu().numpy()
+    assert rel_max(got, ref).max() < 1e-9
+    vref, vgot = ref - inv, got - inv
+    for sl in (slice(1, 4), slice(4, 5)):
+        assert np.abs(vgot[:, sl] - vref[:, sl]).max() < 1e-8 * np.abs(vref[:, sl]).max()
+    # the isotropic length scale 2 / (cbrt(det dxi/dx) N) is ~2e5 m on these
+    # 5000 km x 10 km elements: the explicit diffusive limit is far below the
+    # acoustic Courant step, so the steps use dt = 0.02 s
+    Qs0 = workloads.gcm_initial_state(dg.grid.coordinates(), seed=6)
+    dt = 0.02
+    Qo, _ = om.lsrk54(Qs0.copy(), dt, 5)
+    Qs = dg.init_ode_state(Qs0)
+    lsrk = cmdg.LSRK54CarpenterKennedy(dg, Qs, dt=dt)
+    cmdg.dostep_(Qs, lsrk, None, 0.0, 5)
+    assert np.isfinite(Qo).all()
+    assert rel_max(Qs.cpu().numpy(), Qo).max() < 1e-10
+
+
+def test_shell_smagorinsky_refuses_mixed():
+    grid = cmdg.CubedShellGrid(3, 2, 2, R, R + 30e3)
+    model = cmdg.AtmosModel(orientation="sphere", gravity=True,
+                            ref_state=cmdg.HydrostaticState(cmdg.IsothermalProfile(285.0)), turbulence="smagorinsky")
+    with pytest.raises(cmdg.CmdgError):
+        cmdg.DGModel(model, grid, precision="mixed")
 
 
 def visc_pair(N, nh, nv, precision="fp64", with_divergence=False, rho_nu=2e4, H=30e3):
