@@ -27,6 +27,9 @@ Pins (reference paths relative to the ClimateMachine.jl project root):
     AtmosAcousticGravityLinearModel (both splittings) and a vertical
     exponential filter — test/Numerics/DGMethods/Euler/acousticwave_1d_imex.jl
     (rtol sqrt(eps) in the reference; held here to 1e-11)
+  * ARK2GiraldoKellyConstantinescu order 2 +- 0.35 in both splittings —
+    test/Numerics/ODESolvers/ode_tests_convergence.jl:79-116 (measured on
+    the DG system below the explicit vertical acoustic limit)
 Geometry checks of the cubed shell (Topologies.jl:1067-1305, Metrics.jl:431-724):
 shell volume from the mass matrix, the discrete metric identities (a uniform
 state has zero tendency) and the face-node maps (a linear density advected by
@@ -399,3 +402,28 @@ def test_linear_model_is_linear_and_vertical():
     touched = {(e, n % (Nq * Nq)) for e, s, n in zip(*np.nonzero(LE))}
     assert touched and all(n == 3 for _, n in touched)
     assert {e for e, _ in touched} <= {4, 5, 6}
+
+
+@pytest.mark.parametrize("split", [False, True])
+def test_ark2_is_second_order(split):
+    """ARK2GiraldoKellyConstantinescu (LowStorageVariant) converges at order 2
+    (test/Numerics/ODESolvers/ode_tests_common.jl:30 and
+    ode_tests_convergence.jl:79-116: rate within 0.35 of 2, both splittings),
+    measured here on the DG system itself: the small acoustic-wave shell
+    stepped to t = 0.8 s at dt below the explicit vertical acoustic limit
+    (larger steps damp the vertical acoustic modes instead of resolving
+    them, which is HEVI's purpose but not a convergence regime), against a
+    dt = 0.0125 s run."""
+    m, Q0, _, _ = acoustic_wave(nh=2, nv=3, N=3)
+    T = 0.8
+
+    def run(dt):
+        hv = O.OracleHevi(m, dt, split_explicit_implicit=split)
+        Q = Q0.copy()
+        hv.step(Q, int(round(T / dt)))
+        return Q
+
+    ref = run(0.0125)
+    errors = [m.euclidean_distance(run(dt), ref) for dt in (0.2, 0.1)]
+    rate = math.log2(errors[0] / errors[1])
+    assert abs(rate - 2) < 0.35, rate
