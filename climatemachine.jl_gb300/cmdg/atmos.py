@@ -5,8 +5,9 @@ AtmosPhysics{FT}(param_set; ref_state, turbulence, moisture); orientation,
 source)`` (src/Atmos/Model/AtmosModel.jl:154-375) for the subset the GPU
 path implements: DryModel moisture, TotalEnergyModel, Compressible, Rusanov
 or central first-order flux, Gravity() source, HydrostaticState reference
-state, NoOrientation or FlatOrientation, ConstantDynamicViscosity or
-SmagorinskyLilly turbulence and DryBiharmonic hyperdiffusion.
+state, NoOrientation, FlatOrientation or SphericalOrientation,
+ConstantDynamicViscosity or SmagorinskyLilly turbulence, DryBiharmonic
+hyperdiffusion, and the AtmosAcousticGravityLinearModel of HEVI stepping.
 
 The planet constants are CLIMAParameters.jl 0.2.0's Earth values.
 """
