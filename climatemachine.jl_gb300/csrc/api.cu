@@ -253,8 +253,9 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
     const bool shell = mesh->m.kind == MESH_SHELL;
     const bool arrays = mesh->m.kind == MESH_ARRAYS;
     if (arrays) {
-        CMDG_ARG_CHECK(p->turbulence == CMDG_TURB_NONE && p->hyperdiffusion == CMDG_HYPER_NONE,
-                       "the grid-arrays kernels are inviscid");
+        CMDG_ARG_CHECK(p->hyperdiffusion == CMDG_HYPER_NONE, "no hyperdiffusion on grid-arrays meshes");
+        CMDG_ARG_CHECK(p->turbulence == CMDG_TURB_NONE || precision == CMDG_FP64,
+                       "turbulence closures on grid-arrays meshes run FP64 models");
         CMDG_ARG_CHECK(p->orientation >= CMDG_ORIENT_NONE && p->orientation <= CMDG_ORIENT_SPHERE,
                        "unknown orientation %d", p->orientation);
     } else if (shell) {
@@ -311,11 +312,12 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
     int rc = init_model_tables(&md);
     if (rc == CMDG_OK && shell) rc = init_shell_tables(&md);
     if (rc == CMDG_OK && arrays) rc = init_arrays_tables(&md);
-    if (rc == CMDG_OK && !shell && (p->turbulence != CMDG_TURB_NONE || p->hyperdiffusion != CMDG_HYPER_NONE))
+    if (rc == CMDG_OK && !shell && !arrays &&
+        (p->turbulence != CMDG_TURB_NONE || p->hyperdiffusion != CMDG_HYPER_NONE))
         rc = init_viscous_tables(&md);
     if (rc == CMDG_OK && p->hyperdiffusion != CMDG_HYPER_NONE)
         rc = shell ? init_shell_hyper_tables(&md) : init_hyper_tables(&md);
-    if (rc == CMDG_OK && shell && p->turbulence != CMDG_TURB_NONE) rc = init_shell_visc_tables(&md);
+    if (rc == CMDG_OK && (shell || arrays) && p->turbulence != CMDG_TURB_NONE) rc = init_shell_visc_tables(&md);
     if (rc == CMDG_OK) {
         cudaError_t e = cudaMalloc(&md.d_status, sizeof(unsigned));
         if (e == cudaSuccess) e = cudaMemset(md.d_status, 0, sizeof(unsigned));

@@ -9,26 +9,10 @@
 // shell.cu: src/Numerics/DGMethods/DGModel_kernels.jl:64-548 and :588-901,
 // NumericalFluxes.jl:219-340, bc_momentum.jl:25-34, Metrics.jl:431-724.
 #include "shell_common.cuh"
+#include "visc_curv.cuh"
 
 namespace cmdg {
 namespace {
-
-// reference state of node n from the per-node tables (zero without a
-// reference state; the pressure coefficient always)
-template <typename R>
-__device__ __forceinline__ Level<R> node_ref(const KParams& P, const R* g, int Np, int n) {
-    Level<R> lv;
-    lv.crho = g[KG_DCRHO * Np + n];
-    lv.gphiz = R(0);
-    if (P.ph.ref_state) {
-        lv.rho_ref = g[KG_DRHO * Np + n];
-        lv.p_ref = g[KG_DPREF * Np + n];
-        lv.href = g[KG_DRHOE * Np + n] + lv.p_ref;
-    } else {
-        lv.rho_ref = lv.p_ref = lv.href = R(0);
-    }
-    return lv;
-}
 
 template <typename K>
 cudaError_t opt_in_smem(K kernel, size_t bytes) {
@@ -50,9 +34,14 @@ struct ArraysSmem {
     static constexpr size_t BYTES = sizeof(R) * TOTAL;
 };
 
-template <int N, typename R, bool MIXED, int MODE>
+// VT: the turbulence closure (FP64): the viscous fluxes of the curvilinear
+// gradient pass's output join the volume flux and, with the facing node's
+// state, the central second-order interface flux; walls carry the
+// first-order flux only.
+template <int N, typename R, bool MIXED, int MODE, int VT = CMDG_TURB_NONE>
 __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CTAS : ShellDims<N>::MIN_CTAS64)
     arrays_stage_kernel(const KParams P) {
+    constexpr bool VISC = VT != CMDG_TURB_NONE;
     using Dm = ShellDims<N>;
     using SM = ArraysSmem<N, R>;
     constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, NFN = 6 * Nfp;
@@ -116,6 +105,16 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
             F1[s] = flux_d<R, MIXED>(q, th, 1, s);
             F2[s] = flux_d<R, MIXED>(q, th, 2, s);
         }
+        if (VISC) {
+            R Fv[3][NSTATE];
+            shell_visc_flux<R, MIXED, VT>(P, e, t, Np, q, lv, th.rinv, Fv);
+#pragma unroll
+            for (int s2 = 0; s2 < NSTATE; ++s2) {
+                F0[s2] += Fv[0][s2];
+                F1[s2] += Fv[1][s2];
+                F2[s2] += Fv[2][s2];
+            }
+        }
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             R Ft[NSTATE];
@@ -171,6 +170,15 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
             for (int s = 0; s < NSTATE; ++s) qp[s] = qm[s];
 #pragma unroll
             for (int c = 0; c < 3; ++c) qp[1 + c] = qm[1 + c] - R(2) * mn_m * nv[c];
+            if (VISC) {
+                // the staged flux holds the second-order part too: walls take the first-order one
+                const Level<R> lvm = node_ref<R>(P, ge, Np, vM);
+                const Thermo<R, MIXED> thm = thermo<R, MIXED>(qm, lvm, P);
+                Fm[0] = mn_m;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) Fm[1 + c] = mn_m * thm.u[c] + thm.pflux * nv[c];
+                Fm[4] = mn_m * thm.rinv * thm.H;
+            }
         }
         const Level<R> lvp = node_ref<R>(P, gp, Np, vP);
         const Thermo<R, MIXED> thp = thermo<R, MIXED>(qp, lvp, P);
@@ -180,6 +188,13 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
 #pragma unroll
         for (int c = 0; c < 3; ++c) Fp[1 + c] = mn_p * thp.u[c] + thp.pflux * nv[c];
         Fp[4] = un_p * thp.H;
+        if (VISC && nb >= 0) {
+            // facing node's viscous flux . n
+            R Fv[3][NSTATE];
+            shell_visc_flux<R, MIXED, VT>(P, nb, vP, Np, qp, lvp, thp.rinv, Fv);
+#pragma unroll
+            for (int s2 = 0; s2 < NSTATE; ++s2) Fp[s2] += nv[0] * Fv[0][s2] + nv[1] * Fv[1][s2] + nv[2] * Fv[2][s2];
+        }
         const R lam_p = fabs(un_p) + thp.c;
         const R lift = sJ * iJm * KConst<R>::inv_w0(P);
         const R hmw = (ph.numflux == CMDG_FLUX_RUSANOV) ? R(0.5) * fmax(lam_m, lam_p) : R(0);
@@ -254,34 +269,48 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
     if (__any_sync(0xffffffffu, bad) && (t & 31) == 0) atomicOr(P.status, 1u);
 }
 
-template <int N, typename R, bool MIXED, int MODE>
+template <int N, typename R, bool MIXED, int MODE, int VT>
 cudaError_t launch_arrays_typed(const KParams& P, cudaStream_t s) {
     constexpr size_t bytes = ArraysSmem<N, R>::BYTES;
-    cudaError_t e = opt_in_smem(arrays_stage_kernel<N, R, MIXED, MODE>, bytes);
+    cudaError_t e = opt_in_smem(arrays_stage_kernel<N, R, MIXED, MODE, VT>, bytes);
     if (e != cudaSuccess) return e;
-    arrays_stage_kernel<N, R, MIXED, MODE><<<(unsigned)P.nelem, ShellDims<N>::NT, bytes, s>>>(P);
+    arrays_stage_kernel<N, R, MIXED, MODE, VT><<<(unsigned)P.nelem, ShellDims<N>::NT, bytes, s>>>(P);
     return cudaGetLastError();
 }
 
+// closures run FP64 on grid-arrays meshes (cmdg_model_create)
 template <int N>
-cudaError_t launch_arrays_N(const KParams& P, bool mixed, int mode, cudaStream_t s) {
+cudaError_t launch_arrays_N(const KParams& P, bool mixed, int mode, int turb, cudaStream_t s) {
+    if (turb == CMDG_TURB_CONSTANT)
+        return mode == 0 ? launch_arrays_typed<N, double, false, 0, CMDG_TURB_CONSTANT>(P, s)
+                         : launch_arrays_typed<N, double, false, 1, CMDG_TURB_CONSTANT>(P, s);
+    if (turb == CMDG_TURB_SMAGORINSKY)
+        return mode == 0 ? launch_arrays_typed<N, double, false, 0, CMDG_TURB_SMAGORINSKY>(P, s)
+                         : launch_arrays_typed<N, double, false, 1, CMDG_TURB_SMAGORINSKY>(P, s);
     if (mixed)
-        return mode == 0 ? launch_arrays_typed<N, float, true, 0>(P, s) : launch_arrays_typed<N, float, true, 1>(P, s);
-    return mode == 0 ? launch_arrays_typed<N, double, false, 0>(P, s) : launch_arrays_typed<N, double, false, 1>(P, s);
+        return mode == 0 ? launch_arrays_typed<N, float, true, 0, CMDG_TURB_NONE>(P, s)
+                         : launch_arrays_typed<N, float, true, 1, CMDG_TURB_NONE>(P, s);
+    return mode == 0 ? launch_arrays_typed<N, double, false, 0, CMDG_TURB_NONE>(P, s)
+                     : launch_arrays_typed<N, double, false, 1, CMDG_TURB_NONE>(P, s);
 }
 
 }  // namespace
 
 int launch_arrays_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
     const Mesh& m = *md->mesh;
+    const int turb = md->prm.turbulence;
+    if (turb != CMDG_TURB_NONE) {
+        const int rc = launch_shell_visc_gradient(md, a.Qin, md->d_gf, s);
+        if (rc) return rc;
+    }
     const KParams P = make_params(md, a);
     const bool mixed = md->precision == CMDG_MIXED;
     cudaError_t err;
     switch (m.N) {
-        case 2: err = launch_arrays_N<2>(P, mixed, a.mode, s); break;
-        case 3: err = launch_arrays_N<3>(P, mixed, a.mode, s); break;
-        case 4: err = launch_arrays_N<4>(P, mixed, a.mode, s); break;
-        case 5: err = launch_arrays_N<5>(P, mixed, a.mode, s); break;
+        case 2: err = launch_arrays_N<2>(P, mixed, a.mode, turb, s); break;
+        case 3: err = launch_arrays_N<3>(P, mixed, a.mode, turb, s); break;
+        case 4: err = launch_arrays_N<4>(P, mixed, a.mode, turb, s); break;
+        case 5: err = launch_arrays_N<5>(P, mixed, a.mode, turb, s); break;
         default:
             set_error("no grid-arrays stage kernel for N=%d", m.N);
             return CMDG_ERR_ARG;

@@ -158,7 +158,9 @@ __device__ __forceinline__ int shell_partner_level(const ShellIdx<N>& x, int ez,
     return ezp * Nq + vP / Nfp;
 }
 
-template <int N, typename R, bool MIXED, bool PROJECT = true, int NA = 4>
+// ARRAYS: a grid-arrays mesh (per-node reference values, facing node from
+// the partner table) instead of the cubed shell (levels, orientation codes)
+template <int N, typename R, bool MIXED, bool PROJECT = true, int NA = 4, bool ARRAYS = false>
 __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(const KParams P, const void* Qv,
                                                                             R* __restrict__ hg) {
     using Ix = ShellIdx<N>;
@@ -186,7 +188,9 @@ __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(cons
         for (int s = 0; s < NSTATE; ++s) q[s] = qe[s * Np];
     }
     const int nb = x.face ? __ldg(nbr + x.f) : -1;
-    const int vP = nb >= 0 ? shell_partner<N>(nbr, x.f, x.fn) : x.vM;
+    const int vP = nb < 0 ? x.vM
+                   : ARRAYS ? __ldg(P.fpart + ((size_t)e * 6 + x.f) * Nfp + x.fn)
+                            : shell_partner<N>(nbr, x.f, x.fn);
     if (nb >= 0) {
         const R* qn = Qin + (size_t)nb * ESTRIDE + vP;
 #pragma unroll
@@ -194,7 +198,7 @@ __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(cons
     }
     if (x.node) {
         R H[NA];
-        const Level<R> lv = shell_level<R, MIXED>(P, ge, Np, t, ez * Nq + x.nk);
+        const Level<R> lv = ARRAYS ? node_ref<R>(P, ge, Np, t) : shell_level<R, MIXED>(P, ge, Np, t, ez * Nq + x.nk);
         shell_hyper_args<R, MIXED, PROJECT, NA>(P, q, lv, ge, Np, t, H);
         PL::st(s_q, Np, t, q);
 #pragma unroll
@@ -208,7 +212,8 @@ __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(cons
         if (PROJECT && P.hyper_horizontal && x.fd == 2) lift = R(0);  // HorizontalDirection: no xi3 face terms
         if (nb >= 0) {
             const R* gp = geo + (size_t)nb * GSTRIDE;
-            const Level<R> lvp = shell_level<R, MIXED>(P, gp, Np, vP, shell_partner_level<N>(x, ez, vP));
+            const Level<R> lvp = ARRAYS ? node_ref<R>(P, gp, Np, vP)
+                                        : shell_level<R, MIXED>(P, gp, Np, vP, shell_partner_level<N>(x, ez, vP));
             shell_hyper_args<R, MIXED, PROJECT, NA>(P, qp, lvp, gp, Np, vP, Hp);
             c = R(0.5);
         } else {
@@ -218,7 +223,8 @@ __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(cons
             const R mn = qb[1] * nv[0] + qb[2] * nv[1] + qb[3] * nv[2];
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc) qb[1 + cc] -= mn * nv[cc];
-            const Level<R> lvm = shell_level<R, MIXED>(P, ge, Np, x.vM, ez * Nq + x.kM);
+            const Level<R> lvm =
+                ARRAYS ? node_ref<R>(P, ge, Np, x.vM) : shell_level<R, MIXED>(P, ge, Np, x.vM, ez * Nq + x.kM);
             shell_hyper_args<R, MIXED, PROJECT, NA>(P, qb, lvm, ge, Np, x.vM, Hp);
             c = R(1);
         }
@@ -416,14 +422,29 @@ cudaError_t launch_shell_passes_typed(const KParams& P, const void* Q, void* hd,
 }
 
 // the viscous gradient pass: grad u, grad h_tot (Np, 12, nelem)
-template <int N, typename R, bool MIXED, int NA>
+template <int N, typename R, bool MIXED, int NA, bool ARRAYS = false>
 cudaError_t launch_shell_visc_typed(const KParams& P, const void* Q, void* gout, cudaStream_t s) {
     constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp, NFN = 6 * Nfp, NT = ShellDims<N>::NT;
     constexpr size_t b1 = sizeof(R) * (planar_pad<R>(5 * Np) + NA * Np + 3 * NA * NFN + Nq * Nq);
     cudaError_t e;
-    if ((e = opt_in(shell_hyper_grad_kernel<N, R, MIXED, false, NA>, b1)) != cudaSuccess) return e;
-    shell_hyper_grad_kernel<N, R, MIXED, false, NA><<<P.nelem, NT, b1, s>>>(P, Q, static_cast<R*>(gout));
+    if ((e = opt_in(shell_hyper_grad_kernel<N, R, MIXED, false, NA, ARRAYS>, b1)) != cudaSuccess) return e;
+    shell_hyper_grad_kernel<N, R, MIXED, false, NA, ARRAYS><<<P.nelem, NT, b1, s>>>(P, Q, static_cast<R*>(gout));
     return cudaGetLastError();
+}
+
+// grid-arrays meshes, FP64: grad u, grad h_tot (and grad theta_v with smag)
+cudaError_t launch_arrays_visc(const KParams& P, int N, bool smag, const void* Q, void* gout, cudaStream_t s) {
+    switch (N) {
+        case 2: return smag ? launch_shell_visc_typed<2, double, false, 5, true>(P, Q, gout, s)
+                            : launch_shell_visc_typed<2, double, false, 4, true>(P, Q, gout, s);
+        case 3: return smag ? launch_shell_visc_typed<3, double, false, 5, true>(P, Q, gout, s)
+                            : launch_shell_visc_typed<3, double, false, 4, true>(P, Q, gout, s);
+        case 4: return smag ? launch_shell_visc_typed<4, double, false, 5, true>(P, Q, gout, s)
+                            : launch_shell_visc_typed<4, double, false, 4, true>(P, Q, gout, s);
+        case 5: return smag ? launch_shell_visc_typed<5, double, false, 5, true>(P, Q, gout, s)
+                            : launch_shell_visc_typed<5, double, false, 4, true>(P, Q, gout, s);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 // grad u, grad h_tot (12 words); with smag also grad theta_v (15 words, FP64)
@@ -659,8 +680,10 @@ int launch_shell_visc_gradient(Model* md, const void* Qin, void* gout, cudaStrea
     a.alpha = a.beta = a.rka = a.rkb_dt = 0;
     a.mode = 0;
     const KParams P = make_params(md, a);
-    const cudaError_t err = launch_shell_visc(P, m.N, md->precision == CMDG_MIXED,
-                                              md->prm.turbulence == CMDG_TURB_SMAGORINSKY, Qin, gout, s);
+    const bool smag = md->prm.turbulence == CMDG_TURB_SMAGORINSKY;
+    const cudaError_t err = m.kind == MESH_ARRAYS
+                                ? launch_arrays_visc(P, m.N, smag, Qin, gout, s)
+                                : launch_shell_visc(P, m.N, md->precision == CMDG_MIXED, smag, Qin, gout, s);
     if (err != cudaSuccess) {
         set_error("cubed-shell viscous gradient pass launch failed: %s", cudaGetErrorString(err));
         return CMDG_ERR_CUDA;

@@ -56,4 +56,21 @@ __device__ __forceinline__ Level<R> shell_level(const KParams& P, const R* g, in
 }
 
 }  // namespace
+// reference state of node n from the per-node tables of a grid-arrays mesh
+// (zero without a reference state; the pressure coefficient always)
+template <typename R>
+__device__ __forceinline__ Level<R> node_ref(const KParams& P, const R* g, int Np, int n) {
+    Level<R> lv;
+    lv.crho = g[KG_DCRHO * Np + n];
+    lv.gphiz = R(0);
+    if (P.ph.ref_state) {
+        lv.rho_ref = g[KG_DRHO * Np + n];
+        lv.p_ref = g[KG_DPREF * Np + n];
+        lv.href = g[KG_DRHOE * Np + n] + lv.p_ref;
+    } else {
+        lv.rho_ref = lv.p_ref = lv.href = R(0);
+    }
+    return lv;
+}
+
 }  // namespace cmdg

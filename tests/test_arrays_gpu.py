@@ -140,3 +140,47 @@ def test_grid_arrays_errors():
     bad2[0, 0, 0] = 10**12
     with pytest.raises(cmdg.CmdgError, match="out of range"):
         cmdg.ArraysGrid(3, om.vgeo, bad2, om.elemtobndy)
+
+
+def viscous_case(kind, turb, N):
+    """Closures on grid arrays: the warped (curvilinear) brick of the
+    manufactured-solution test (mms_bc_atmos.jl mesh warp, walls on all
+    sides, NoOrientation) or the cubed shell, with the oracle's own arrays."""
+    rng = np.random.default_rng(21)
+    if kind == "warped":
+        om = O.OracleModel(N, (3, 3, 3), (0, 0, 0), (1, 1, 1), periodic=(0, 0, 0), warp=1, turbulence="constant",
+                           rho_nu=0.01, with_divergence=True)
+        model = cmdg.AtmosModel(turbulence="constant", rho_nu=0.01, with_divergence=True)
+        xyz = om.aux[:, 0:3]
+        Q0 = om.state()
+        Q0[:, 0] = 1 + 0.1 * np.sin(2 * xyz[:, 0]) * np.cos(3 * xyz[:, 1])
+        Q0[:, 1:4] = rng.uniform(-0.3, 0.3, size=Q0[:, 1:4].shape)
+        Q0[:, 4] = 2.5e5 + 1e3 * np.cos(xyz[:, 2])
+        return om, arrays_model(om, N, model, set_ref=False), Q0
+    kw = dict(turbulence=turb) if turb == "smagorinsky" else dict(turbulence=turb, rho_nu=2e3)
+    om = O.OracleModel(N, shell=dict(nhorz=2, nvert=3, r_inner=R, r_outer=R + 30e3), orientation="sphere",
+                       gravity=True, ref_state=True, profile="isothermal", T_surface=285.0, **kw)
+    model = cmdg.AtmosModel(orientation="sphere", gravity=True,
+                            ref_state=cmdg.HydrostaticState(cmdg.IsothermalProfile(285.0)), **kw)
+    Q0 = workloads.gcm_initial_state(om.aux[:, 0:3], seed=5)
+    Q0[:, 1:4] += rng.uniform(-2, 2, size=Q0[:, 1:4].shape)
+    return om, arrays_model(om, N, model), Q0
+
+
+@pytest.mark.parametrize("kind,turb", [("warped", "constant"), ("shell", "constant"), ("shell", "smagorinsky")])
+def test_closures_on_grid_arrays_match_oracle(kind, turb):
+    """ConstantDynamicViscosity / SmagorinskyLilly on grid-arrays meshes
+    (FP64): the tendency within 1e-9 of the field scale."""
+    om, dg, Q0 = viscous_case(kind, turb, 3)
+    ref = om.tendency(Q0)
+    dQ = dg.new_state(torch.float64)
+    dg(dQ, dg.init_ode_state(Q0), None, 0.0)
+    err = rel_max(dQ.cpu().numpy(), ref)
+    assert (err < 1e-9).all(), err
+
+
+def test_closures_on_grid_arrays_refuse_mixed():
+    om = O.OracleModel(3, (2, 2, 2), (0, 0, 0), (1, 1, 1), periodic=(1, 1, 1))
+    grid = cmdg.ArraysGrid(3, om.vgeo, om.vmapP + 1, om.elemtobndy)
+    with pytest.raises(cmdg.CmdgError):
+        cmdg.DGModel(cmdg.AtmosModel(turbulence="constant", rho_nu=1.0), grid, precision="mixed")
