@@ -217,6 +217,16 @@ class DGModel:
             raise ValueError(f"aux7 must be (nelem, 7, Np), got {a.shape}")
         call("cmdg_model_set_reference", self.h, ctypes.c_void_p(a.ctypes.data))
 
+    def set_mms(self, src: torch.Tensor | None, wall: torch.Tensor | None, zero_enthalpy: bool = True):
+        """Manufactured-solution terms of an FP64 model on an ArraysGrid
+        (cmdg_model_set_mms): a source (nelem, 5, Np) added to the tendency,
+        the InitStateBC wall state (nelem, 5, Np), and total_specific_enthalpy
+        := 0.  The tensors stay referenced here; refill them in place between
+        tendencies."""
+        self._mms = (src, wall)
+        call("cmdg_model_set_mms", self.h, _dptr(src) if src is not None else None,
+             _dptr(wall) if wall is not None else None, int(zero_enthalpy))
+
     def reference_state(self) -> np.ndarray:
         out = np.empty((self.grid.nelem, 3, self.grid.Np), dtype=np.float64)
         call("cmdg_model_reference_state", self.h, ctypes.c_void_p(out.ctypes.data))

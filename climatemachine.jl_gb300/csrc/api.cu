@@ -389,6 +389,20 @@ int cmdg_model_reference_state(const cmdg_model* model, double* h_ref) {
     return CMDG_OK;
 }
 
+int cmdg_model_set_mms(cmdg_model* model, const double* d_src, const double* d_wall, int zero_enthalpy) {
+    int rc = check_model(model);
+    if (rc) return rc;
+    Model& md = model->m;
+    CMDG_ARG_CHECK(md.mesh->kind == MESH_ARRAYS && md.precision == CMDG_FP64,
+                   "sources and InitStateBC wall states are set on FP64 models on grid-arrays meshes");
+    md.mms_src = d_src;
+    md.mms_wall = d_wall;
+    md.mms_zero_h = zero_enthalpy ? 1 : 0;
+    for (auto& kv : md.graphs) cudaGraphExecDestroy(kv.second);
+    md.graphs.clear();
+    return CMDG_OK;
+}
+
 int cmdg_model_set_reference(cmdg_model* model, const double* h_aux7) {
     int rc = check_model(model);
     if (rc) return rc;

@@ -164,6 +164,19 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
                 jr[0] = (R)j.x;
                 jr[4] = (R)j.y;
             }
+        } else if (P.mms_wall) {
+            // InitStateBC: the caller's wall state (bc_initstate.jl:12-26)
+            const double* w = P.mms_wall + (size_t)e * ESTRIDE + vM;
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) qp[s] = (R)w[s * Np];
+            if (VISC) {
+                const Level<R> lvm = node_ref<R>(P, ge, Np, vM);
+                const Thermo<R, MIXED> thm = thermo<R, MIXED>(qm, lvm, P);
+                Fm[0] = mn_m;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) Fm[1 + c] = mn_m * thm.u[c] + thm.pflux * nv[c];
+                Fm[4] = mn_m * thm.rinv * thm.H;
+            }
         } else {
             // Impenetrable(FreeSlip) + Insulating wall
 #pragma unroll
@@ -194,6 +207,15 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
             shell_visc_flux<R, MIXED, VT>(P, nb, vP, Np, qp, lvp, thp.rinv, Fv);
 #pragma unroll
             for (int s2 = 0; s2 < NSTATE; ++s2) Fp[s2] += nv[0] * Fv[0][s2] + nv[1] * Fv[1][s2] + nv[2] * Fv[2][s2];
+        } else if (VISC && P.mms_wall) {
+            // InitStateBC second order: the one-sided flux of the wall state with
+            // the interior gradient state (NumericalFluxes.jl:872-966); the face
+            // term halves Fm + Fp, hence twice the flux here
+            R Fv[3][NSTATE];
+            shell_visc_flux<R, MIXED, VT>(P, e, vM, Np, qp, lvp, thp.rinv, Fv);
+#pragma unroll
+            for (int s2 = 0; s2 < NSTATE; ++s2)
+                Fp[s2] += R(2) * (nv[0] * Fv[0][s2] + nv[1] * Fv[1][s2] + nv[2] * Fv[2][s2]);
         }
         const R lam_p = fabs(un_p) + thp.c;
         const R lift = sJ * iJm * KConst<R>::inv_w0(P);
@@ -238,6 +260,12 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CT
         if (nk == N) sub_face(5, ni + Nq * nj);
 #pragma unroll
         for (int c = 0; c < 3; ++c) rhs[1 + c] += src[c];
+        if (P.mms_src) {
+            // the caller's source term (MMSSource, mms_bc_atmos.jl:60-80)
+            const double* sp = P.mms_src + ebase;
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) rhs[s] += (R)sp[s * Np];
+        }
         const R rkb_dt = KConst<R>::rkb_dt(P);
 #pragma unroll
         for (int s = 0; s < NSTATE; ++s) {

@@ -199,6 +199,11 @@ struct Model {
     double* d_lin64 = nullptr;
     double* d_linface64 = nullptr;
     int lin_nz = 0;                  // grid-arrays meshes: elements per stack found for the linear model
+    // grid-arrays meshes, FP64: caller-owned source and InitStateBC wall state
+    // (Np, 5, nelem) device arrays, and the zero-enthalpy override
+    const double* mms_src = nullptr;
+    const double* mms_wall = nullptr;
+    int mms_zero_h = 0;
     int grid_ctas = -1;              // stage-kernel grid: -1 = one CTA per element (the measured best
                                      // on GB300), 0 = one wave of resident CTAs, n > 0 = n CTAs
     int kernel_kind = 0;             // KERNEL_NODE or KERNEL_COLUMN

@@ -59,6 +59,12 @@ struct KParams {
     // gradient pass writes grad u, grad h_tot (Np, 12, nelem) into gf
     const float* vgref32;
     const double* sdelta;  // cubed shell, SmagorinskyLilly: length scale per node (Np, nelem)
+    // grid-arrays meshes, FP64 (cmdg_model_set_mms): a source added to the
+    // tendency, the InitStateBC wall state, both (Np, 5, nelem) or NULL, and
+    // total_specific_enthalpy := 0 in the gradient arguments
+    const double* mms_src;
+    const double* mms_wall;
+    int mms_zero_h;
     int hyper_horizontal;  // 1: the passes run in the horizontal directions only (HorizontalDirection)
     // grid-arrays meshes: facing node of each face node (Nfp, 6, nelem) and
     // the FP64-computed reference jumps (rho, rhoe) per face node

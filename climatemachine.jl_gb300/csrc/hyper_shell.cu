@@ -103,6 +103,7 @@ __device__ __forceinline__ void shell_hyper_args(const KParams& P, const R q[NST
             H[NA - 1] = T / pow_r(p / VConst<R>::MSLP(P), VConst<R>::kappa(P));
         }
     }
+    if (P.mms_zero_h) H[3] = R(0);  // total_specific_enthalpy := 0 (mms_bc_atmos.jl:45-48)
 }
 
 // strong-form gradient of 4 node fields s_X[4][Np] at this node thread,
@@ -217,12 +218,19 @@ __global__ void __launch_bounds__(ShellDims<N>::NT) shell_hyper_grad_kernel(cons
             shell_hyper_args<R, MIXED, PROJECT, NA>(P, qp, lvp, gp, Np, vP, Hp);
             c = R(0.5);
         } else {
-            // FreeSlip state of the gradient flux: rhou+ = rhou- - (rhou-.n) n
             R qb[NSTATE];
-            PL::ld(s_q, Np, x.vM, qb);
-            const R mn = qb[1] * nv[0] + qb[2] * nv[1] + qb[3] * nv[2];
+            if (ARRAYS && P.mms_wall) {
+                // InitStateBC: the caller's wall state (bc_initstate.jl:12-26)
+                const double* w = P.mms_wall + (size_t)e * ESTRIDE + x.vM;
 #pragma unroll
-            for (int cc = 0; cc < 3; ++cc) qb[1 + cc] -= mn * nv[cc];
+                for (int cc = 0; cc < NSTATE; ++cc) qb[cc] = (R)w[cc * Np];
+            } else {
+                // FreeSlip state of the gradient flux: rhou+ = rhou- - (rhou-.n) n
+                PL::ld(s_q, Np, x.vM, qb);
+                const R mn = qb[1] * nv[0] + qb[2] * nv[1] + qb[3] * nv[2];
+#pragma unroll
+                for (int cc = 0; cc < 3; ++cc) qb[1 + cc] -= mn * nv[cc];
+            }
             const Level<R> lvm =
                 ARRAYS ? node_ref<R>(P, ge, Np, x.vM) : shell_level<R, MIXED>(P, ge, Np, x.vM, ez * Nq + x.kM);
             shell_hyper_args<R, MIXED, PROJECT, NA>(P, qb, lvm, ge, Np, x.vM, Hp);

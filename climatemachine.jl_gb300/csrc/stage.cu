@@ -604,6 +604,9 @@ KParams make_params(Model* md, const LaunchArgs& a) {
     P.hglap_ref32 = md->d_hglap_ref;
     P.vgref32 = md->d_vgref;
     P.sdelta = md->d_sdelta;
+    P.mms_src = md->mms_src;
+    P.mms_wall = md->mms_wall;
+    P.mms_zero_h = md->mms_zero_h;
     return P;
 }
 

@@ -170,6 +170,16 @@ int cmdg_model_destroy(cmdg_model* model);
  * of such a model whose orientation, gravity or reference state uses them;
  * may be called again to replace them. */
 int cmdg_model_set_reference(cmdg_model* model, const double* h_aux7);
+/* Manufactured-solution runs on grid-arrays meshes (FP64 models): d_src, a
+ * source (Np, 5, nelem) added to the tendency (the MMSSource of
+ * test/Numerics/DGMethods/compressible_Navier_Stokes/mms_bc_atmos.jl:60-80);
+ * d_wall, the wall state (Np, 5, nelem) used on every wall face node for the
+ * first-order, gradient and one-sided second-order fluxes (InitStateBC,
+ * src/Atmos/Model/bc_initstate.jl:12-26, NumericalFluxes.jl:872-966) in place
+ * of FreeSlip + Insulating; zero_enthalpy = 1 sets total_specific_enthalpy to
+ * zero in the gradient arguments (mms_bc_atmos.jl:45-48).  Device arrays owned
+ * by the caller, read by every following tendency; NULL switches each off. */
+int cmdg_model_set_mms(cmdg_model* model, const double* d_src, const double* d_wall, int zero_enthalpy);
 
 /* Reference state at the nodes into host memory, (Np, 3, nelem):
  * rho_ref, rhoe_ref, p_ref (aux.ref_state, src/Atmos/Model/ref_state.jl:66-67). */

@@ -246,12 +246,13 @@ def test_dry_biharmonic_acts_on_horizontal_velocity():
     assert math.log2(errs[0] / errs[1]) > 0.8
 
 
-def mms_functions(gamma, mu):
+def mms_expressions(gamma, mu):
     """The manufactured solution of
     test/Numerics/DGMethods/compressible_Navier_Stokes/mms_solution.jl
-    (3D): the state q = (rho, U, V, W, E) and the source dq/dt + div F(q)
-    of the compressible Navier-Stokes flux with p = (gamma - 1)(E - |U|^2 /
-    (2 rho)) and tau = 2 mu (eps - tr(eps) I / 3), derived symbolically."""
+    (3D): the symbols (t, x, y, z), the state q = (rho, U, V, W, E) and the
+    source dq/dt + div F(q) of the compressible Navier-Stokes flux with
+    p = (gamma - 1)(E - |U|^2 / (2 rho)) and tau = 2 mu (eps - tr(eps) I / 3),
+    derived symbolically."""
     sp = pytest.importorskip("sympy")
     x, y, z, t = sp.symbols("x y z t", real=True)
     c = sp.cos(sp.pi * t)
@@ -272,8 +273,14 @@ def mms_functions(gamma, mu):
             + [vel[d] * (E + P) - sum(vel[i] * tau[d][i] for i in range(3))] for d in range(3)]
     q = (rho, U, V, W, E)
     src = [sp.diff(q[s], t) + sum(sp.diff(flux[d][s], X[d]) for d in range(3)) for s in range(5)]
-    return (sp.lambdify((t, x, y, z), q, modules="numpy", cse=True),
-            sp.lambdify((t, x, y, z), src, modules="numpy", cse=True))
+    return (t, x, y, z), q, src
+
+
+def mms_functions(gamma, mu):
+    """Numpy functions (t, x, y, z) -> q and -> source of mms_expressions."""
+    sp = pytest.importorskip("sympy")
+    args, q, src = mms_expressions(gamma, mu)
+    return (sp.lambdify(args, q, modules="numpy", cse=True), sp.lambdify(args, src, modules="numpy", cse=True))
 
 
 def test_mms_navier_stokes_golden():
