@@ -8,7 +8,9 @@ shell (arbitrary face orientations through the facing-node table).
 
 Bounds as in the other parity tests: FP64 <= 1e-10 (bricks) / 1e-9 (shell)
 of the field scale; mixed precision <= 1e-4 for one tendency and <= 1e-5
-relative L2 after steps."""
+relative L2 after steps.  Also the turbulence closures on grid arrays, and
+the manufactured-solution Navier-Stokes golden error of mms_bc_atmos.jl
+reproduced on the GPU (cmdg_model_set_mms)."""
 import numpy as np
 import pytest
 import torch
