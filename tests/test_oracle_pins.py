@@ -434,3 +434,24 @@ def test_ark2_is_second_order(split):
     errors = [m.euclidean_distance(run(dt), ref) for dt in (0.2, 0.1)]
     rate = math.log2(errors[0] / errors[1])
     assert abs(rate - 2) < 0.35, rate
+
+
+def test_mms_fixture_matches_the_derivation():
+    """tests/golden/mms_functions.py (used where sympy is absent) is the
+    symbolic derivation's code: equal values at random points and times."""
+    import importlib.util
+    import os
+    from fractions import Fraction as Fr
+
+    spec = importlib.util.spec_from_file_location(
+        "mms_functions", os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "mms_functions.py"))
+    G = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(G)
+    c = O.EARTH
+    fq, fs = mms_functions(c["cp_d"] / c["cv_d"], Fr(1, 100))
+    x, y, z = np.random.default_rng(5).uniform(0, 1, (3, 500))
+    for t in (0.0, 0.3, 1.0):
+        for f, g in ((fq, G.q), (fs, G.source)):
+            a = np.stack(np.broadcast_arrays(*f(t, x, y, z)))
+            b = np.stack(np.broadcast_arrays(*g(t, x, y, z)))
+            assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max()
