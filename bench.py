@@ -429,6 +429,83 @@ def run_cpu_reference(steps, threads=None, sample_steps=None, warmup=1, max_sec=
                 warmup=max(1, warmup))
 
 
+ACCURACY_STEPS = 100
+L2_NOTE = ("GPU arm: a 256 MiB buffer is written between timed steps (L2 is 129 MB); CPU arm: the FP64 state and "
+           "its working arrays (hundreds of MB) exceed the host caches")
+
+
+def field_errors(got, ref, M, base=None):
+    """Per-field errors of a state (nelem, 5, Np) against a reference state:
+    relative L2 weighted by the mass matrix (euclidean_distance / norm,
+    src/Arrays/MPIStateArrays.jl:583-648), max relative (max |got - ref| /
+    max |ref|), and, with a base state, the L2 error relative to the change
+    of the reference from that base (how well the evolution itself is
+    reproduced)."""
+    import numpy as np
+
+    out = {"rel_l2": [], "max_rel": []}
+    if base is not None:
+        out["rel_l2_of_change"] = []
+    for s in range(NFIELD):
+        d = got[:, s] - ref[:, s]
+        num = math.sqrt(float(np.sum(d * d * M)))
+        den = math.sqrt(float(np.sum(ref[:, s] * ref[:, s] * M)))
+        out["rel_l2"].append(num / den if den > 0 else num)
+        mx = float(np.abs(ref[:, s]).max())
+        out["max_rel"].append(float(np.abs(d).max()) / mx if mx > 0 else float(np.abs(d).max()))
+        if base is not None:
+            c = ref[:, s] - base[:, s]
+            dc = math.sqrt(float(np.sum(c * c * M)))
+            out["rel_l2_of_change"].append(num / dc if dc > 0 else None)
+    return out
+
+
+def accuracy_report(cmdg, torch, dg64, dgmx, Q0, dt, steps=ACCURACY_STEPS):
+    """Both GPU paths against the FP64 oracle (the CPU restatement of the
+    reference) on the full rising-bubble workload: per-field relative L2 and
+    max relative errors after one tendency evaluation and after `steps`
+    LSRK54 steps from the same initial state, and the drift of total mass
+    sum M rho and total energy sum M rho e (compensated sums,
+    src/Arrays/MPIStateArrays.jl:655-675) over those steps.  Runs outside
+    every timed region; independent of --steps."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+
+    O.set_threads(os.cpu_count())
+    om = O.OracleModel(N, NE, (0, 0, 0), (L, L, L), periodic=(1, 1, 0), orientation="flat", gravity=True,
+                       ref_state=True, profile="dry_adiabatic", T_surface=300.0, T_min=0.0)
+    Q0 = np.ascontiguousarray(Q0, dtype=np.float64)
+    M = dg64.grid.mass()
+    t0 = time.perf_counter()
+    ref_tend = om.tendency(Q0)
+    Qo, _ = om.lsrk54(Q0.copy(), dt, steps)
+    oracle_s = time.perf_counter() - t0
+    sums0 = [om.weightedsum(Q0, f) for f in (0, 4)]
+    sums_o = [om.weightedsum(Qo, f) for f in (0, 4)]
+    rep = {"reference": "FP64 oracle (CPU restatement of the reference DGModel + LSRK54)", "steps": steps, "dt": dt,
+           "oracle_seconds": oracle_s, "fields": ["rho", "rhou", "rhov", "rhow", "rhoe"]}
+    drift = {"oracle": {"mass": (sums_o[0] - sums0[0]) / sums0[0], "energy": (sums_o[1] - sums0[1]) / sums0[1]}}
+    for name, dg in (("mixed", dgmx), ("fp64", dg64)):
+        Q = dg.init_ode_state(Q0)
+        tend = dg.new_state(torch.float64)
+        dg(tend, Q, None, 0.0)
+        s_start = dg.weighted_sums(Q, (0, 4))
+        lsrk = cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt)
+        cmdg.dostep_(Q, lsrk, None, 0.0, nsteps=steps)
+        s_end = dg.weighted_sums(Q, (0, 4))
+        got = dg.full_state(Q).cpu().numpy()
+        rep[name] = {"after_tendency": field_errors(tend.cpu().numpy(), ref_tend, M),
+                     f"after_{steps}_steps": field_errors(got, Qo, M, base=Q0),
+                     "status_word": dg.status_word()}
+        drift[name] = {"mass": (s_end[0] - s_start[0]) / s_start[0], "energy": (s_end[1] - s_start[1]) / s_start[1]}
+    rep["drift"] = drift
+    rep["mixed_max_rel_l2"] = max(rep["mixed"][f"after_{steps}_steps"]["rel_l2"])
+    rep["target_rel_l2"] = 1e-5
+    return rep
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -436,6 +513,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="cmdg", choices=["cmdg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the accuracy report against the FP64 oracle (bubble workload)")
     ap.add_argument("--workload", default="bubble", choices=["bubble", "gcm", "les", "hyper", "ensemble", "hevi"])
     args = ap.parse_args()
 
@@ -453,7 +532,8 @@ def main():
                 "steps": r["steps"], "warmup": r["warmup"], "ms_per_step": 1e3 * r["sec"] / r["steps"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic", "impl": "reference",
-                "config": {"workload": WORKLOAD, "path": "CPU FP64 oracle port of the reference DG + LSRK54"},
+                "config": {"workload": WORKLOAD, "l2": L2_NOTE, "parallelism": f"replicas x{args.gpus}"},
+                "run": {"path": "CPU FP64 oracle port of the reference DG + LSRK54"},
                 "cpu_baseline": {"value": r["value"], "unit": "DOF-stage/s", "cores": r["threads"], "kind": "port",
                                  "sample": f"{r['steps']} timed LSRK54 steps (after {r['warmup']} warm-up) of the full 1e6-node workload"},
                 "e2e": {"value": r["value"], "unit": "DOF-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -585,6 +665,13 @@ def main():
     ach_64 = spec["bytes_fp64"] * nodes / (stage_ms_64 * 1e-3) / 1e9
     traffic = profile_traffic(spec["profile"])
 
+    accuracy = None
+    if rank == 0 and not args.no_accuracy and args.workload == "bubble":
+        try:
+            accuracy = accuracy_report(cmdg, torch, dg64, dgmx, Q0, dt)
+        except Exception as exc:  # the report must not hide the GPU line
+            accuracy = {"error": str(exc)[:300]}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and args.workload == "bubble":
         try:
@@ -600,10 +687,9 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mx / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic",
-            "config": {"workload": spec["desc"], "path": "mixed FP32 perturbation / FP64 RK register",
-                       "l2": "256 MiB buffer written between timed steps (L2 is 129 MB)",
-                       "parallelism": f"replicas x{world}", "dt": dt,
-                       "stage_kernel": {k: list(v) for k, v in kernels.items()}},
+            "config": {"workload": spec["desc"], "l2": L2_NOTE, "parallelism": f"replicas x{world}"},
+            "run": {"path": "mixed FP32 perturbation / FP64 RK register", "dt": dt,
+                    "stage_kernel": {k: list(v) for k, v in kernels.items()}},
             "fp64": {"value": v64, "ms_per_step": ms_64 / args.steps,
                      "roofline": {"bound": "hbm", "achieved": ach_64, "peak": peak, "unit": "GB/s",
                                   "frac": ach_64 / peak}},
@@ -612,6 +698,7 @@ def main():
             "mixed_vs_fp64_rel_l2": rel,
             "mixed_vs_fp64_rel_l2_rho_rhou_rhoe": rel_vec,
             "mixed_vs_fp64_steps": args.warmup + args.steps,
+            "accuracy": accuracy,
             "roofline": {"bound": "hbm", "achieved": ach_mx, "peak": peak, "unit": "GB/s", "frac": ach_mx / peak,
                          "traffic": traffic, "peak_source": peak_kind,
                          "kernel": spec["kernel"], "bytes_per_node_stage": spec["bytes_mixed"]},

@@ -32,7 +32,7 @@ EXPORTS = (
     "cmdg_batch_lsrk54_step", "cmdg_batch_autotune",
     "cmdg_filter_matrix", "cmdg_apply_filter", "cmdg_apply_tmar",
     "cmdg_linear_tendency", "cmdg_hevi_create", "cmdg_hevi_destroy", "cmdg_hevi_info", "cmdg_hevi_solve",
-    "cmdg_hevi_step", "cmdg_apply_mp_filter", "cmdg_model_set_mms",
+    "cmdg_hevi_step", "cmdg_apply_mp_filter", "cmdg_model_set_mms", "cmdg_model_set_staging_test",
 )
 
 
@@ -135,6 +135,7 @@ def load(path: str | None = None):
         "cmdg_hevi_step": [P, P, D, I, P],
         "cmdg_apply_mp_filter": [P, P, P, P, I, P, I, P],
         "cmdg_model_set_mms": [P, P, P, I],
+        "cmdg_model_set_staging_test": [P, I, I],
     }
     for name, args in proto.items():
         fn = getattr(L, name)

@@ -54,6 +54,26 @@ def isentropic_vortex(xyz: np.ndarray, t: float = 0.0, *, p_inf=1e5, T_inf=300.0
     return Q
 
 
+def c1_vortex_state(xyz: np.ndarray, *, seed=2024, strength=5.0, mach=0.5, p_inf=1e5, T_inf=300.0,
+                    consts=EARTH) -> np.ndarray:
+    """The plain CPU-runnable configuration: on the periodic brick [0, 10]^3
+    (4 x 4 x 4 elements, N = 4), an isentropic vortex of strength 5 and
+    radius 1 (a tenth of the domain) at the centre, advected diagonally (at
+    pi/4 in the x-y plane) at Mach 0.5, plus seeded uniform noise of
+    amplitude 1e-6 on all five fields.  The vortex is the Gaussian vortex of
+    isentropicvortex_setup.jl (test/Numerics/DGMethods/Euler) with its swirl
+    speed set by the strength beta as in Shu's vortex,
+    u_theta = beta e^(1/2) / (2 pi) sqrt(R_d T_inf) (r/R) exp(-r^2 / (2 R^2)),
+    which makes its temperature drop kappa beta^2 e / (8 pi^2) T_inf at the
+    centre."""
+    R_d, cp, cv = consts["R_d"], consts["cp_d"], consts["cv_d"]
+    c_inf = math.sqrt(cp / cv * R_d * T_inf)
+    vortex_speed = strength * math.exp(0.5) / (2 * math.pi) * math.sqrt(R_d * T_inf)
+    return isentropic_vortex(xyz - 5.0, 0.0, p_inf=p_inf, T_inf=T_inf, translation_speed=mach * c_inf,
+                             translation_angle=math.pi / 4, vortex_speed=vortex_speed, R=1.0, L=5.0, consts=consts,
+                             noise=1e-6, seed=seed)
+
+
 def rising_bubble(xyz: np.ndarray, *, theta0=300.0, amp=2.0, rc=250.0, center=(1250.0, 1250.0, 350.0),
                   consts=EARTH) -> np.ndarray:
     R_d, cp, cv, T0, g, p0 = (consts[k] for k in ("R_d", "cp_d", "cv_d", "T_0", "grav", "MSLP"))

@@ -77,8 +77,21 @@ static int issue_steps(Model* md, void* Q, double* dQ, double dt, int nsteps, cu
     return CMDG_OK;
 }
 
+// The fused steps run five stages with no host work between them, so a term
+// the caller refreshes at every stage time t + C_s dt cannot enter them.
+int check_fused_stepping(const Model* md) {
+    if (md->mms_src != nullptr || md->mms_wall != nullptr) {
+        set_error("the model's manufactured-solution source or wall state is refreshed by the caller at each stage "
+                  "time; step it stage by stage (cmdg_tendency at t + C_s dt), not with the fused LSRK54 steps");
+        return CMDG_ERR_STATE;
+    }
+    return CMDG_OK;
+}
+
 static int run_steps(Model* md, void* Q, double* dQ, double dt, int nsteps, cudaStream_t s) {
-    int rc = ensure_scratch(md);
+    int rc = check_fused_stepping(md);
+    if (rc) return rc;
+    rc = ensure_scratch(md);
     if (rc) return rc;
     if (s == nullptr || nsteps > 64) return issue_steps(md, Q, dQ, dt, nsteps, s);
     // capture once per (Q, dQ, dt, nsteps, stream), replay afterwards
@@ -326,6 +339,17 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
             rc = CMDG_ERR_CUDA;
         }
     }
+    if (rc == CMDG_OK) {
+        cudaError_t e = cudaGetDevice(&md.device);
+        if (e != cudaSuccess) {
+            set_error("cudaGetDevice failed: %s", cudaGetErrorString(e));
+            rc = CMDG_ERR_CUDA;
+        }
+    }
+    // set-up of the allocation-free stepping: loading the module that holds
+    // its fixed stage array reserves the array on this device now, while the
+    // library may still allocate, not at the first allocation-free call
+    if (rc == CMDG_OK) rc = noalloc_stage_address(&md.noalloc_stage);
     if (rc) {
         cmdg_model_destroy(mo);
         return rc;
@@ -531,6 +555,19 @@ int cmdg_gradient_flux(cmdg_model* model, void* d_gf, const void* d_Q, void* str
     CMDG_ARG_CHECK(model->m.mesh->kind == MESH_BRICK, "cmdg_gradient_flux exposes the brick gradient-flux layout");
     CMDG_ARG_CHECK(model->m.mesh->kind == MESH_BRICK, "the diffusive passes run on brick meshes");
     return launch_gradient(&model->m, d_Q, d_gf, (cudaStream_t)stream);
+}
+
+int cmdg_model_set_staging_test(cmdg_model* model, int skip_copies, int wait_polls) {
+    int rc = check_model(model);
+    if (rc) return rc;
+    CMDG_ARG_CHECK(wait_polls >= 0, "wait_polls must be >= 0");
+    Model& md = model->m;
+    md.staging_skip_copies = skip_copies ? 1 : 0;
+    md.wait_polls = wait_polls;
+    // captured graphs hold the old launch parameters
+    for (auto& kv : md.graphs) cudaGraphExecDestroy(kv.second);
+    md.graphs.clear();
+    return CMDG_OK;
 }
 
 int cmdg_status_word(cmdg_model* model, uint32_t* h_status, void* stream) {

@@ -207,6 +207,13 @@ struct Model {
     int grid_ctas = -1;              // stage-kernel grid: -1 = one CTA per element (the measured best
                                      // on GB300), 0 = one wave of resident CTAs, n > 0 = n CTAs
     int kernel_kind = 0;             // KERNEL_NODE or KERNEL_COLUMN
+    int device = -1;                 // CUDA device current when the model was created
+    void* noalloc_stage = nullptr;   // device address of the allocation-free stage array on that device
+    // test hook of the persistent stage kernel's bounded waits: when
+    // staging_skip_copies is set the kernel arms its staging barriers without
+    // issuing the copies, and every wait gives up after wait_polls polls
+    int staging_skip_copies = 0;
+    int wait_polls = 0;              // 0 = the default limit
 };
 
 // host-side setup (mesh.cpp, shell_mesh.cpp)
@@ -241,6 +248,12 @@ int launch_shell_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
 int launch_arrays_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
 // LSRK54CarpenterKennedy A and B coefficient arrays (5 entries each)
 void lsrk54_coefficients(const double** A, const double** B);
+// CMDG_ERR_STATE (with the message set) for a model whose tendency depends on
+// terms the caller refreshes at every stage time, which fused steps cannot honour
+int check_fused_stepping(const Model* md);
+// allocation-free stepping (noalloc.cu): device address of the fixed stage
+// array on the current device, looked up when a model is created
+int noalloc_stage_address(void** out);
 
 // diffusive passes (viscous.cu): gradient flux of Qin into md->d_gf, then the
 // stage kernel with second-order fluxes

@@ -70,6 +70,11 @@ struct KParams {
     // the FP64-computed reference jumps (rho, rhoe) per face node
     const int* fpart;
     const float* fjump;
+    // bounded waits of the persistent stage kernel: poll limit (0 = default)
+    // and the test hook that arms the staging barriers without issuing the
+    // copies, so that every wait runs out (cmdg_model_set_staging_test)
+    int wait_polls;
+    int staging_skip_copies;
 };
 
 // A run of consecutive elements [e0, e1) of ensemble member `member`, of
@@ -130,8 +135,13 @@ __device__ __forceinline__ double f32_to_f64_bits(float f) {
     return __hiloint2double((int)hi, (int)(mag << 29));
 }
 
-// FP64 -> FP32 by IEEE-754 field arithmetic on the integer pipe, rounding
-// toward zero (error below one FP32 ulp).  Magnitudes under 2^-126 flush to a
+// FP64 -> FP32 by IEEE-754 field arithmetic on the integer pipe, rounding to
+// nearest, ties to even (the IEEE default, so the stage increments carry no
+// directed bias).  The FP64 significand keeps its top 23 bits; the 29 bits
+// dropped, plus 2^28 - 1 plus the kept value's lowest bit, carry one into the
+// kept value exactly when they exceed half an FP32 ulp, or equal it with the
+// kept value odd; a carry out of the significand steps the exponent (up to an
+// infinity past the largest FP32 value).  Magnitudes under 2^-126 flush to a
 // signed zero; magnitudes beyond the FP32 range, infinities and NaNs give an
 // infinity.  Used for the stage increment only, which is small next to the
 // state it is added to.
@@ -139,7 +149,9 @@ __device__ __forceinline__ float f64_to_f32_bits(double d) {
     const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
     const unsigned sign = hi & 0x80000000u;
     const unsigned mag = hi & 0x7FFFFFFFu;
-    unsigned bits = sign | (((mag - (896u << 20)) << 3) | (lo >> 29));
+    unsigned kept = ((mag - (896u << 20)) << 3) | (lo >> 29);
+    kept += ((lo & 0x1FFFFFFFu) + 0x0FFFFFFFu + (kept & 1u)) >> 29;
+    unsigned bits = sign | kept;
     bits = (mag < (897u << 20)) ? sign : bits;
     bits = (mag >= (1151u << 20)) ? (sign | 0x7F800000u) : bits;
     return __uint_as_float(bits);
@@ -330,10 +342,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// waits for the phase of `parity` to complete; false after 2^16 polls (each
-// poll may suspend the thread for a hardware-defined interval)
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-    for (int i = 0; i < (1 << 16); ++i)
+// waits for the phase of `parity` to complete; false after `polls` polls
+// (2^16 when polls <= 0; each poll may suspend the thread for a
+// hardware-defined interval)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int polls) {
+    const int limit = polls > 0 ? polls : (1 << 16);
+    for (int i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }

@@ -5,53 +5,46 @@
 // whose memory-pool or arena allocator owns all of the device's memory (a
 // cudaMalloc from the library would fail or fragment the arena), and hosts
 // that forbid any allocation after start-up.  cmdg_lsrk54_step_noalloc serves
-// them: the two stage buffers live in one file-scope __device__ array whose
-// size is fixed when the library is loaded, so a call allocates nothing.
+// them: the two stage buffers live in one file-scope __device__ array of a
+// fixed size, so a call allocates nothing.
 //
-// The array is CMDG_NOALLOC_MAX_BYTES (48 MiB) on every GPU that loads the
-// library, held until the process exits; a state of up to half of it
-// (24 MiB) can be stepped.  Every call shares the array: the stage buffers
-// are written in full by each stage before any stage reads them, so nothing
-// in it has to start at zero, but two calls whose kernels overlap on the GPU
-// (on different streams, or from different threads) race on it.
-#include <mutex>
-
+// The array is CMDG_NOALLOC_MAX_BYTES (48 MiB) on every GPU where a model is
+// created, held until the process exits; a state of up to half of it
+// (24 MiB) can be stepped.  The CUDA runtime loads this file's module, and
+// with it reserves the array, when its symbol is first looked up; that
+// look-up is part of model creation (cmdg_model_create, which allocates
+// anyway), so the array is reserved before the host hands its memory to an
+// arena, and the allocation-free call itself reserves nothing.  Every call
+// shares the array: the stage buffers are written in full by each stage
+// before any stage reads them, so nothing in it has to start at zero, but two
+// calls whose kernels overlap on the GPU (on different streams, or from
+// different threads) race on it.
 #include "cmdg_internal.h"
 
 namespace {
 
 constexpr size_t NOALLOC_MAX_BYTES = (size_t)48 << 20;
 constexpr size_t NOALLOC_ALIGN = 256;
-constexpr int MAX_DEVICES = 64;
 
 // Both stage buffers.  In host code this name is only a handle for
 // cudaGetSymbolAddress, never a device address.
 __device__ __align__(256) unsigned char g_noalloc_stage[NOALLOC_MAX_BYTES];
 
-void* g_stage_addr[MAX_DEVICES] = {};
-std::mutex g_stage_mutex;
+}  // namespace
 
-// Device address of g_noalloc_stage on the current device, looked up once
-// per device (the first call on a device does this set-up).
-int stage_address(void** out) {
-    int dev = 0;
-    CMDG_CUDA_CHECK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= MAX_DEVICES) {
-        cmdg::set_error("device ordinal %d is beyond the %d devices the allocation-free path tracks", dev,
-                        MAX_DEVICES);
-        return CMDG_ERR_UNSUPPORTED;
-    }
-    std::lock_guard<std::mutex> lock(g_stage_mutex);
-    if (g_stage_addr[dev] == nullptr) {
-        void* p = nullptr;
-        CMDG_CUDA_CHECK(cudaGetSymbolAddress(&p, g_noalloc_stage));
-        g_stage_addr[dev] = p;
-    }
-    *out = g_stage_addr[dev];
+namespace cmdg {
+
+// Set-up, with the model's device current: the device address of the array.
+// A model created after a device reset looks it up again, so no address
+// outlives the context it belongs to longer than the models of that context.
+int noalloc_stage_address(void** out) {
+    void* p = nullptr;
+    CMDG_CUDA_CHECK(cudaGetSymbolAddress(&p, g_noalloc_stage));
+    *out = p;
     return CMDG_OK;
 }
 
-}  // namespace
+}  // namespace cmdg
 
 extern "C" int cmdg_lsrk54_step_noalloc(cmdg_model* model, void* d_Q, double* d_dQ, double t, double dt, int nsteps,
                                         void* stream) {
@@ -70,11 +63,16 @@ extern "C" int cmdg_lsrk54_step_noalloc(cmdg_model* model, void* d_Q, double* d_
                    "state of %zu bytes exceeds the allocation-free limit of %zu bytes per stage buffer "
                    "(two buffers in a fixed %zu-byte device array); use cmdg_lsrk54_step",
                    bytes, NOALLOC_MAX_BYTES / 2, NOALLOC_MAX_BYTES);
-    if (nsteps == 0) return CMDG_OK;
-    void* base = nullptr;
-    int rc = stage_address(&base);
+    int rc = check_fused_stepping(md);
     if (rc) return rc;
-    char* S1 = static_cast<char*>(base);
+    int dev = -1;
+    CMDG_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev != md->device || md->noalloc_stage == nullptr) {
+        set_error("the model was created on device %d; make it current (now %d) before stepping", md->device, dev);
+        return CMDG_ERR_STATE;
+    }
+    if (nsteps == 0) return CMDG_OK;
+    char* S1 = static_cast<char*>(md->noalloc_stage);
     char* S2 = S1 + slot;
     const double *A, *B;
     lsrk54_coefficients(&A, &B);

@@ -221,6 +221,7 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
             windows(ee, qlo, qbytes, qok, dlo, dbytes, dok);
             total = (qok ? qbytes : 0u) + (dok ? dbytes : 0u);
         }
+        if (P.staging_skip_copies) qok = dok = false;  // test hook: the armed bytes never arrive
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(&bars[b], total);
         if (qok) bulk_copy_g2s(smem_raw + ST::QB + b * ST::QBLK, reinterpret_cast<const void*>(qlo), qbytes, &bars[b]);
@@ -255,7 +256,7 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
 #pragma unroll
                 for (int s = 0; s < NSTATE; ++s) cur.qp[s] = qn[s * Np];
             }
-            if (!mbar_wait_bounded(&bars[b], (uint32_t)((it >> 1) & 1))) timed_out = true;
+            if (!mbar_wait_bounded(&bars[b], (uint32_t)((it >> 1) & 1), P.wait_polls)) timed_out = true;
             uintptr_t qlo, dlo;
             uint32_t qbytes, dbytes;
             bool qok, dok;
@@ -445,8 +446,8 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
         if (t == 0) {
             atomicOr(P.status, 2u);
             // phases complete in order: waiting for each buffer's latest armed phase covers the rest
-            if (issued0 > 0) mbar_wait_bounded(&bars[0], (uint32_t)((issued0 - 1) & 1));
-            if (issued1 > 0) mbar_wait_bounded(&bars[1], (uint32_t)((issued1 - 1) & 1));
+            if (issued0 > 0) mbar_wait_bounded(&bars[0], (uint32_t)((issued0 - 1) & 1), P.wait_polls);
+            if (issued1 > 0) mbar_wait_bounded(&bars[1], (uint32_t)((issued1 - 1) & 1), P.wait_polls);
         }
     }
 }
@@ -607,6 +608,8 @@ KParams make_params(Model* md, const LaunchArgs& a) {
     P.mms_src = md->mms_src;
     P.mms_wall = md->mms_wall;
     P.mms_zero_h = md->mms_zero_h;
+    P.wait_polls = md->wait_polls;
+    P.staging_skip_copies = md->staging_skip_copies;
     return P;
 }
 

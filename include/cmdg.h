@@ -216,7 +216,12 @@ int cmdg_tendency(cmdg_model* model, double* d_dQ, const double* d_Q, double t, 
 
 /* nsteps LSRK54CarpenterKennedy steps of size dt in FP64, in place on d_Q;
  * d_dQ is the solver's RK register (zero before the first step, as the
- * reference's `fill!(dQ, 0)`).
+ * reference's `fill!(dQ, 0)`).  The dry AtmosModel terms of the library do
+ * not depend on time, so the stage times t + C_s dt of the reference
+ * (LowStorageRungeKuttaMethod.jl:319-324) do not enter the kernels; a model
+ * whose tendency takes terms that the caller refreshes at each stage time
+ * (cmdg_model_set_mms) is refused with CMDG_ERR_STATE and is stepped stage by
+ * stage with cmdg_tendency instead.
  * Replaces dostep!(Q, lsrk::LowStorageRungeKutta2N, p, time)
  * (src/Numerics/ODESolvers/LowStorageRungeKuttaMethod.jl:102-158, 293-327). */
 int cmdg_lsrk54_step(cmdg_model* model, double* d_Q, double* d_dQ, double t, double dt, int nsteps, void* stream);
@@ -227,12 +232,15 @@ int cmdg_lsrk54_step(cmdg_model* model, double* d_Q, double* d_dQ, double t, dou
  * forbid allocation after start-up.  No counterpart in the reference.
  *   d_Q: double* for a CMDG_FP64 model, float* (the perturbation) for a
  *   CMDG_MIXED model; d_dQ: the FP64 RK register.
- *   The two stage buffers live in a fixed 48 MiB __device__ array held by
- *   every GPU that loads the library; states larger than 24 MiB are rejected
- *   with CMDG_ERR_ARG.  The call makes no cudaMalloc / cudaFree.
- *   The first call on a device looks the array's address up
- *   (cudaGetSymbolAddress); make that first call before any stream capture.
- *   Calls share the array: calls whose kernels overlap on the GPU race. */
+ *   The two stage buffers live in a fixed 48 MiB __device__ array.  It is
+ *   reserved on a device when the first model is created there
+ *   (cmdg_model_create looks its address up, which loads the module that
+ *   holds it) and is held until the process exits; create the model before
+ *   the host's arena takes the device's memory.  The call itself makes no
+ *   cudaMalloc / cudaFree and reserves nothing.  States larger than 24 MiB are
+ *   rejected with CMDG_ERR_ARG; the model's device must be current
+ *   (CMDG_ERR_STATE otherwise).  Calls share the array: calls whose kernels
+ *   overlap on the GPU race. */
 int cmdg_lsrk54_step_noalloc(cmdg_model* model, void* d_Q, double* d_dQ, double t, double dt, int nsteps,
                              void* stream);
 
@@ -410,10 +418,24 @@ int cmdg_gradient_flux(cmdg_model* model, void* d_gf, const void* d_Q, void* str
  * src/Numerics/DGMethods/DGModel.jl:132-301). */
 int cmdg_hyperdiffusive_state(cmdg_model* model, void* d_hd, const void* d_Q, void* stream);
 
-/* Device status word accumulated by the kernels since the last call
- * (bit 0: non-finite tendency seen); reading clears it.
+/* Device status word accumulated by the kernels since the last call;
+ * reading clears it.
+ *   bit 0: a kernel saw a non-finite tendency;
+ *   bit 1: a bounded wait of the persistent stage kernel (grid_ctas >= 0) for
+ *          its staging copies gave up (the CTA carried on with the shared
+ *          buffer as it was, so the stage's results are not valid, waited
+ *          again, bounded, for its copies in flight and returned; the
+ *          context stays usable).
  * Replaces checked_wait's error flag (src/Arrays/MPIStateArrays.jl:910-936). */
 int cmdg_status_word(cmdg_model* model, uint32_t* h_status, void* stream);
+
+/* Test hook of the bounded waits (bit 1 of the status word) that makes them
+ * run out without a fault: with skip_copies = 1 the persistent stage kernel
+ * arms its staging barriers with the bytes of each element's copies but
+ * issues no copy, so every wait gives up after wait_polls polls (0 = the
+ * default limit of 65536).  skip_copies = 0, wait_polls = 0 restores normal
+ * operation.  No counterpart in the reference. */
+int cmdg_model_set_staging_test(cmdg_model* model, int skip_copies, int wait_polls);
 
 #ifdef __cplusplus
 }

@@ -31,7 +31,8 @@ def test_reference_arm_line():
     assert line["cpu_baseline"]["value"] == line["value"]
     assert line["e2e"] == {"value": line["value"], "unit": "DOF-stage/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
-    assert "workload" in line["config"]
+    # the same config keys as the GPU arm, so the two lines describe one workload
+    assert set(line["config"]) == {"workload", "l2", "parallelism"}
 
 
 def test_reference_arm_other_ranks_exit_quietly():
