@@ -15,7 +15,7 @@ for sm_103a behind a C ABI, include/cmdg.h).  Names follow the reference:
 from .atmos import (EARTH, AtmosModel, HydrostaticState, DryAdiabaticProfile, IsothermalProfile, DryBiharmonic,
                     AtmosAcousticGravityLinearModel)
 from .dgmodel import (DGModel, BrickGrid, CubedShellGrid, ArraysGrid, euclidean_distance, weightedsum, norm,
-                      remainder_DGModel)
+                      remainder_DGModel, brick_element_order)
 from .odesolvers import (LSRK54CarpenterKennedy, ARK2GiraldoKellyConstantinescu, LinearBackwardEulerSolver,
                          ManyColumnLU, SingleColumnLU, LowStorageVariant, solve_, dostep_)
 from ._lib import CmdgError, load as load_library
@@ -27,5 +27,5 @@ __all__ = [
     "euclidean_distance", "weightedsum", "norm", "LSRK54CarpenterKennedy", "solve_", "dostep_", "CmdgError",
     "load_library", "Ensemble", "AtmosAcousticGravityLinearModel", "remainder_DGModel",
     "ARK2GiraldoKellyConstantinescu", "LinearBackwardEulerSolver", "ManyColumnLU", "SingleColumnLU",
-    "LowStorageVariant",
+    "LowStorageVariant", "brick_element_order",
 ]

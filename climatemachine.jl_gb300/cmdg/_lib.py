@@ -18,6 +18,7 @@ ERRORS = {1: "CMDG_ERR_ARG", 2: "CMDG_ERR_CUDA", 3: "CMDG_ERR_UNSUPPORTED", 4: "
           5: "CMDG_ERR_TIMEOUT", 6: "CMDG_ERR_ALLOC", 7: "CMDG_ERR_STATE"}
 CMDG_FP64, CMDG_MIXED = 0, 1
 CMDG_DIR_EVERY, CMDG_DIR_HORIZONTAL, CMDG_DIR_VERTICAL = 0, 1, 2
+CMDG_TOPOLOGY_LIBRARY, CMDG_TOPOLOGY_BRICK, CMDG_TOPOLOGY_STACKED_BRICK = 0, 1, 2
 
 # Every exported symbol of include/cmdg.h (checked by the CPU test suite).
 EXPORTS = (
@@ -33,6 +34,7 @@ EXPORTS = (
     "cmdg_filter_matrix", "cmdg_apply_filter", "cmdg_apply_tmar",
     "cmdg_linear_tendency", "cmdg_hevi_create", "cmdg_hevi_destroy", "cmdg_hevi_info", "cmdg_hevi_solve",
     "cmdg_hevi_step", "cmdg_apply_mp_filter", "cmdg_model_set_mms", "cmdg_model_set_staging_test",
+    "cmdg_brick_element_order", "cmdg_mesh_create_brick_ordered",
 )
 
 
@@ -136,6 +138,8 @@ def load(path: str | None = None):
         "cmdg_apply_mp_filter": [P, P, P, P, I, P, I, P],
         "cmdg_model_set_mms": [P, P, P, I],
         "cmdg_model_set_staging_test": [P, I, I],
+        "cmdg_brick_element_order": [ctypes.POINTER(BrickDesc), I, P],
+        "cmdg_mesh_create_brick_ordered": [ctypes.POINTER(BrickDesc), I, PP],
     }
     for name, args in proto.items():
         fn = getattr(L, name)

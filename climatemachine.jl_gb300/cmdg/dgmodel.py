@@ -32,28 +32,53 @@ def _dptr(t: torch.Tensor):
     return ctypes.c_void_p(t.data_ptr())
 
 
+def brick_desc(N, ne, lo, hi, periodicity=(True, True, True), boundary=((1, 2), (1, 2), (1, 2))) -> BrickDesc:
+    d = BrickDesc()
+    d.N = int(N)
+    for k in range(3):
+        d.ne[k] = int(ne[k])
+        d.lo[k] = float(lo[k])
+        d.hi[k] = float(hi[k])
+        d.periodic[k] = int(bool(periodicity[k]))
+        d.bc_lo[k] = int(boundary[k][0])
+        d.bc_hi[k] = int(boundary[k][1])
+    return d
+
+
+def brick_element_order(ne, lo, hi, topology: str) -> np.ndarray:
+    """perm[e_ref] = library (stacked x-then-y) index of the element that
+    the reference's topology ("brick": BrickTopology, "stacked_brick":
+    StackedBrickTopology) numbers e_ref; host only, needs no GPU
+    (cmdg_brick_element_order)."""
+    _lib.load()
+    d = brick_desc(2, ne, lo, hi)  # the order does not depend on N
+    perm = np.empty(int(ne[0]) * int(ne[1]) * int(ne[2]), dtype=np.int64)
+    call("cmdg_brick_element_order", ctypes.byref(d), BrickGrid.TOPOLOGIES[topology],
+         ctypes.c_void_p(perm.ctypes.data))
+    return perm
+
+
 class BrickGrid:
     """BrickTopology/StackedBrickTopology + DiscontinuousSpectralElementGrid
     (src/Numerics/Mesh/Topologies.jl:470-545,632; src/Numerics/Mesh/Grids.jl:267-414).
 
-    Elements are ordered with the vertical index fastest, then x, then y.
+    Elements are ordered with the vertical index fastest, then the columns
+    in x-then-y order (``topology="library"``) or along the 2D Hilbert curve
+    of the reference's StackedBrickTopology (``topology="stacked_brick"``).
     ``boundary`` gives the tags of the (lower, upper) faces of each
     non-periodic direction, as in the reference's ``boundary`` keyword.
     """
 
-    def __init__(self, N, ne, lo, hi, periodicity=(True, True, True), boundary=((1, 2), (1, 2), (1, 2))):
+    TOPOLOGIES = {"library": _lib.CMDG_TOPOLOGY_LIBRARY, "brick": _lib.CMDG_TOPOLOGY_BRICK,
+                  "stacked_brick": _lib.CMDG_TOPOLOGY_STACKED_BRICK}
+
+    def __init__(self, N, ne, lo, hi, periodicity=(True, True, True), boundary=((1, 2), (1, 2), (1, 2)),
+                 topology="library"):
         _lib.load()
-        d = BrickDesc()
-        d.N = int(N)
-        for k in range(3):
-            d.ne[k] = int(ne[k])
-            d.lo[k] = float(lo[k])
-            d.hi[k] = float(hi[k])
-            d.periodic[k] = int(bool(periodicity[k]))
-            d.bc_lo[k] = int(boundary[k][0])
-            d.bc_hi[k] = int(boundary[k][1])
+        d = brick_desc(N, ne, lo, hi, periodicity, boundary)
         h = ctypes.c_void_p()
-        call("cmdg_mesh_create_brick", ctypes.byref(d), ctypes.byref(h))
+        call("cmdg_mesh_create_brick_ordered", ctypes.byref(d), self.TOPOLOGIES[topology], ctypes.byref(h))
+        self.topology = topology
         self.h = h
         self.desc = d
         nelem = ctypes.c_int64()
@@ -280,11 +305,12 @@ class DGModel:
              float(dt), int(nsteps), _stream())
 
     # ------------------------------------------------------------------ launch configuration
-    KERNELS = {"node": 0, "column": 1}
+    KERNELS = {"node": 0, "column": 1, "lines": 2}
 
     def set_kernel(self, kind: str = "node", grid_ctas: int = -1):
-        """Stage-kernel family ("node" or "column") and grid: -1 = one CTA per
-        element (the default), 0 = one wave of resident CTAs, n > 0 = n CTAs."""
+        """Stage-kernel family ("node", "column" or "lines") and grid: -1 = one
+        CTA per element (the default), 0 = one wave of resident CTAs, n > 0 =
+        n CTAs (the "lines" kernel always runs one CTA per element)."""
         call("cmdg_model_set_kernel", self.h, self.KERNELS[kind], int(grid_ctas))
 
     def get_kernel(self):

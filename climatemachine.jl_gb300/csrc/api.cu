@@ -163,6 +163,30 @@ int cmdg_mesh_create_brick(const cmdg_brick_desc* desc, cmdg_mesh** out) {
     return CMDG_OK;
 }
 
+int cmdg_mesh_create_brick_ordered(const cmdg_brick_desc* desc, int topology, cmdg_mesh** out) {
+    CMDG_ARG_CHECK(out != nullptr, "output pointer is NULL");
+    *out = nullptr;
+    if (topology == CMDG_TOPOLOGY_BRICK) {
+        set_error("BrickTopology numbers the elements of a column apart, and the brick kernels' per-level tables "
+                  "need columns contiguous: build the mesh from the reference grid's arrays "
+                  "(cmdg_mesh_create_arrays), or map states with cmdg_brick_element_order");
+        return CMDG_ERR_UNSUPPORTED;
+    }
+    CMDG_ARG_CHECK(topology == CMDG_TOPOLOGY_LIBRARY || topology == CMDG_TOPOLOGY_STACKED_BRICK,
+                   "unknown topology order %d", topology);
+    cmdg_mesh* mh = new cmdg_mesh();
+    int rc = build_brick(desc, &mh->m, topology);
+    if (rc) {
+        if (mh->m.d_emetric) cudaFree(mh->m.d_emetric);
+        if (mh->m.d_nbr) cudaFree(mh->m.d_nbr);
+        if (mh->m.d_emetric32) cudaFree(mh->m.d_emetric32);
+        delete mh;
+        return rc;
+    }
+    *out = mh;
+    return CMDG_OK;
+}
+
 int cmdg_mesh_create_shell(const cmdg_shell_desc* desc, cmdg_mesh** out) {
     CMDG_ARG_CHECK(out != nullptr, "output pointer is NULL");
     *out = nullptr;
@@ -219,8 +243,9 @@ int cmdg_mesh_coordinates(const cmdg_mesh* mesh, double* h_xyz) {
     }
     for (int64_t e = 0; e < m.nelem; ++e) {
         const int64_t iz = e % m.nz;
-        const int64_t ix = (e / m.nz) % m.desc.ne[0];
-        const int64_t iy = e / ((int64_t)m.nz * m.desc.ne[0]);
+        const int64_t col = m.col_at[e / m.nz];
+        const int64_t ix = col % m.desc.ne[0];
+        const int64_t iy = col / m.desc.ne[0];
         const int64_t idx[3] = {ix, iy, iz};
         for (int d = 0; d < 3; ++d) {
             const double lo = m.desc.lo[d], hi = m.desc.hi[d];

@@ -40,8 +40,10 @@ const char* last_error();
 constexpr int NSTATE = 5;
 // neighbour table row per element: 6 face neighbours (or -tag), vertical index, spare
 constexpr int NBR_STRIDE = 8;
-// stage-kernel families: one thread per node, or one thread per vertical line of nodes
-enum { KERNEL_NODE = 0, KERNEL_COLUMN = 1 };
+// stage-kernel families: one thread per node, one thread per vertical line
+// of nodes, or one thread per node for the fluxes and one per element line
+// for the face fluxes and contractions
+enum { KERNEL_NODE = 0, KERNEL_COLUMN = 1, KERNEL_LINES = 2 };
 constexpr int MIN_N = 2;
 constexpr int MAX_N = 5;
 
@@ -129,6 +131,10 @@ struct Mesh {
     // orientation codes (4 bits per face: neighbour face 0..3, bit 2 = the
     // in-face horizontal index runs reversed)
     std::vector<double> xyz, cgeo;
+    // brick meshes: column order (col_at[h] = ix + nx iy of the h-th column)
+    // and its topology (CMDG_TOPOLOGY_LIBRARY or CMDG_TOPOLOGY_STACKED_BRICK)
+    std::vector<int> col_at;
+    int topology = CMDG_TOPOLOGY_LIBRARY;
     // grid-arrays meshes: the facing node of every face node, (Nfp, 6, nelem)
     std::vector<int> fpart;
     int* d_fpart = nullptr;
@@ -217,7 +223,13 @@ struct Model {
 };
 
 // host-side setup (mesh.cpp, shell_mesh.cpp)
-int build_brick(const cmdg_brick_desc* desc, Mesh* m);
+int build_brick(const cmdg_brick_desc* desc, Mesh* m, int topology = CMDG_TOPOLOGY_LIBRARY);
+// element orders of the reference's brick topologies (order.cpp): Hilbert
+// index of n coordinates of `bits` bits (n words, most significant first),
+// the codes of element centroids (d x nelem), and the column order of a brick
+void hilbert_code(const uint64_t* Y, int n, int bits, uint64_t* H);
+void centroid_codes(const double* centroids, int d, int64_t nelem, std::vector<uint64_t>& code);
+int brick_column_order(const cmdg_brick_desc& b, int topology, std::vector<int>& col_at);
 int build_shell(const cmdg_shell_desc* desc, Mesh* m);
 int build_arrays(const cmdg_grid_arrays* desc, Mesh* m);
 int init_arrays_tables(Model* md);

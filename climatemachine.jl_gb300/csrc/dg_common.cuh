@@ -94,6 +94,9 @@ KParams make_params(Model* md, const LaunchArgs& a);
 // Column-kernel launcher (column.cu); returns cudaErrorNotSupported when no
 // column instantiation exists for the model's N.
 cudaError_t launch_column(const KParams& P, int N, bool mixed, int mode, int grid, cudaStream_t s);
+// Line-kernel launcher (stage_lines.cu), one CTA per element; returns
+// cudaErrorNotSupported for an N without an instantiation.
+cudaError_t launch_lines(const KParams& P, int N, bool mixed, int mode, cudaStream_t s);
 
 namespace {
 

@@ -86,7 +86,7 @@ static double blend(double a, double b, int n, int i) {
     return (double)(((long double)a * (n - i) + (long double)b * i) / n);
 }
 
-int build_brick(const cmdg_brick_desc* d, Mesh* m) {
+int build_brick(const cmdg_brick_desc* d, Mesh* m, int topology) {
     CMDG_ARG_CHECK(d != nullptr, "brick descriptor is NULL");
     CMDG_ARG_CHECK(d->N >= MIN_N && d->N <= MAX_N, "polynomial order N=%d outside the built range [%d, %d]", d->N,
                    MIN_N, MAX_N);
@@ -113,7 +113,16 @@ int build_brick(const cmdg_brick_desc* d, Mesh* m) {
     m->emetric.assign(nelem * 3, 0.0);
     m->nbr.assign(nelem * NBR_STRIDE, 0);
     const int nx = d->ne[0], ny = d->ne[1], nz = d->ne[2];
-    auto eid = [&](int ix, int iy, int iz) { return (int64_t)iz + (int64_t)nz * ((int64_t)ix + (int64_t)nx * iy); };
+    // columns stay contiguous (vertical index fastest); their order is x then
+    // y, or the reference's StackedBrickTopology order
+    m->topology = topology;
+    int rc = brick_column_order(*d, topology, m->col_at);
+    if (rc) return rc;
+    std::vector<int> col_pos(m->col_at.size());
+    for (size_t h = 0; h < m->col_at.size(); ++h) col_pos[m->col_at[h]] = (int)h;
+    auto eid = [&](int ix, int iy, int iz) {
+        return (int64_t)iz + (int64_t)nz * (int64_t)col_pos[(size_t)ix + (size_t)nx * iy];
+    };
     for (int iy = 0; iy < ny; ++iy)
         for (int ix = 0; ix < nx; ++ix)
             for (int iz = 0; iz < nz; ++iz) {

@@ -630,6 +630,7 @@ int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
     const bool mixed = md->precision == CMDG_MIXED;
     cudaError_t err = cudaErrorNotSupported;
     if (md->kernel_kind == KERNEL_COLUMN) err = launch_column(P, m.N, mixed, a.mode, md->grid_ctas, s);
+    if (md->kernel_kind == KERNEL_LINES) err = launch_lines(P, m.N, mixed, a.mode, s);
     if (err == cudaErrorNotSupported) {
         switch (m.N) {
             case 2: err = launch_N<2>(P, mixed, a.mode, md->grid_ctas, s); break;

@@ -17,7 +17,8 @@ struct Candidate {
 extern "C" int cmdg_model_set_kernel(cmdg_model* model, int kernel_kind, int grid_ctas) {
     using namespace cmdg;
     CMDG_ARG_CHECK(model != nullptr, "model is NULL");
-    CMDG_ARG_CHECK(kernel_kind == KERNEL_NODE || kernel_kind == KERNEL_COLUMN, "unknown kernel kind %d", kernel_kind);
+    CMDG_ARG_CHECK(kernel_kind == KERNEL_NODE || kernel_kind == KERNEL_COLUMN || kernel_kind == KERNEL_LINES,
+                   "unknown kernel kind %d", kernel_kind);
     CMDG_ARG_CHECK(grid_ctas >= -1, "grid_ctas must be >= -1");
     model->m.kernel_kind = kernel_kind;
     model->m.grid_ctas = grid_ctas;
@@ -65,7 +66,7 @@ extern "C" int cmdg_model_autotune(cmdg_model* model, int reps, double* h_ms, in
     int rc = CMDG_OK;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     const int saved_kind = md->kernel_kind, saved_grid = md->grid_ctas;
-    std::vector<Candidate> cands = {{KERNEL_NODE, 0}, {KERNEL_NODE, -1}};
+    std::vector<Candidate> cands = {{KERNEL_NODE, 0}, {KERNEL_NODE, -1}, {KERNEL_LINES, -1}};
     // one kernel family for viscous models and for curvilinear meshes
     if (md->prm.turbulence != CMDG_TURB_NONE || md->prm.hyperdiffusion != CMDG_HYPER_NONE || m.kind != MESH_BRICK)
         cands = {{KERNEL_NODE, -1}};

@@ -25,6 +25,10 @@ const libcmdg = get(ENV, "CMDG_LIB", joinpath(@__DIR__, "..", "_build", "libcmdg
 
 const CMDG_FP64 = Cint(0)
 const CMDG_MIXED = Cint(1)
+# element orders (cmdg_mesh_create_brick_ordered / cmdg_brick_element_order)
+const CMDG_TOPOLOGY_LIBRARY = Cint(0)
+const CMDG_TOPOLOGY_BRICK = Cint(1)
+const CMDG_TOPOLOGY_STACKED_BRICK = Cint(2)
 
 struct Brick
     N::Cint
@@ -68,10 +72,15 @@ check(rc::Cint) =
 stream_handle() = CUDA.stream().handle
 
 """
-    CMDGModel(brick::Brick, params::AtmosParams; precision = CMDG_FP64)
+    CMDGModel(brick::Brick, params::AtmosParams, grid, balance_law, state_auxiliary; precision = CMDG_FP64)
 
-GPU DG model; `grid`, `balance_law` and `state_auxiliary` are kept for the
-reference's callbacks that read them.
+GPU DG model on a brick whose elements are numbered as the reference's
+`StackedBrickTopology` numbers them (columns along the 2D Hilbert curve of
+the horizontal base, each column contiguous), so `Q.data` of a grid built
+with `StackedBrickTopology` over the same ranges is passed unpermuted.  A
+`BrickTopology` grid (3D Hilbert order) goes through the grid-arrays
+constructor below.  `grid`, `balance_law` and `state_auxiliary` are kept for
+the reference's callbacks that read them.
 """
 mutable struct CMDGModel{G, BL, A} <: SpaceDiscretization
     mesh::Ptr{Cvoid}
@@ -84,7 +93,8 @@ end
 function CMDGModel(brick::Brick, params::AtmosParams, grid, balance_law, state_auxiliary;
                    precision = CMDG_FP64)
     mesh = Ref{Ptr{Cvoid}}(C_NULL)
-    check(ccall((:cmdg_mesh_create_brick, libcmdg), Cint, (Ref{Brick}, Ref{Ptr{Cvoid}}), brick, mesh))
+    check(ccall((:cmdg_mesh_create_brick_ordered, libcmdg), Cint, (Ref{Brick}, Cint, Ref{Ptr{Cvoid}}),
+                brick, CMDG_TOPOLOGY_STACKED_BRICK, mesh))
     model = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:cmdg_model_create, libcmdg), Cint, (Ptr{Cvoid}, Ref{AtmosParams}, Cint, Ref{Ptr{Cvoid}}),
                 mesh[], params, precision, model))

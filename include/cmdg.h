@@ -19,7 +19,9 @@
  *     re-entrant.
  *   - Element ordering of generated brick meshes is "stacked": the vertical
  *     element index is fastest, then x, then y (columns contiguous, as in
- *     StackedBrickTopology, src/Numerics/Mesh/Topologies.jl:632).
+ *     StackedBrickTopology, src/Numerics/Mesh/Topologies.jl:632, whose
+ *     columns follow the Hilbert curve instead; cmdg_mesh_create_brick_ordered
+ *     builds that order).
  */
 #ifndef CMDG_H
 #define CMDG_H
@@ -119,6 +121,34 @@ const char* cmdg_version(void);
  * Replaces BrickTopology/StackedBrickTopology + DiscontinuousSpectralElementGrid
  * (src/Numerics/Mesh/Topologies.jl:470-545,632; src/Numerics/Mesh/Grids.jl:267-414). */
 int cmdg_mesh_create_brick(const cmdg_brick_desc* desc, cmdg_mesh** out);
+
+/* Element orders of the reference's brick topologies.
+ *   CMDG_TOPOLOGY_LIBRARY        the library's stacked order: vertical index
+ *                                fastest, then x, then y;
+ *   CMDG_TOPOLOGY_BRICK          BrickTopology: all elements along the 3D
+ *                                Hilbert curve through their centroids
+ *                                (BrickMesh.partition, src/Numerics/Mesh/BrickMesh.jl:531-627,
+ *                                codes from centroidtocode / hilbertcode, :40-150);
+ *   CMDG_TOPOLOGY_STACKED_BRICK  StackedBrickTopology: the horizontal base
+ *                                elements along the 2D Hilbert curve, each
+ *                                column contiguous, vertical index fastest
+ *                                (src/Numerics/Mesh/Topologies.jl:632-715). */
+enum { CMDG_TOPOLOGY_LIBRARY = 0, CMDG_TOPOLOGY_BRICK = 1, CMDG_TOPOLOGY_STACKED_BRICK = 2 };
+
+/* Host-only (needs no GPU): h_perm[e_ref] = the index, in the library's
+ * stacked order, of the element that the given topology numbers e_ref
+ * (0-based), for ne[0] ne[1] ne[2] entries.  A state in the reference's
+ * order maps to the library's by moving element e_ref to h_perm[e_ref]. */
+int cmdg_brick_element_order(const cmdg_brick_desc* desc, int topology, int64_t* h_perm);
+
+/* A brick mesh whose elements are numbered in the reference's order, so
+ * states in that order need no permutation: topology CMDG_TOPOLOGY_LIBRARY
+ * (the same mesh as cmdg_mesh_create_brick) or CMDG_TOPOLOGY_STACKED_BRICK
+ * (columns along the 2D Hilbert curve; the bricks of AtmosLESConfiguration,
+ * src/Driver/driver_configs.jl:213).  CMDG_TOPOLOGY_BRICK is refused with
+ * CMDG_ERR_UNSUPPORTED: its columns are not contiguous, which the
+ * per-level tables assume; such a grid runs through cmdg_mesh_create_arrays. */
+int cmdg_mesh_create_brick_ordered(const cmdg_brick_desc* desc, int topology, cmdg_mesh** out);
 /* Builds a stacked cubed-shell mesh: curvilinear geometry with the
  * curl-invariant metric terms.  Replaces StackedCubedSphereTopology +
  * DiscontinuousSpectralElementGrid(meshwarp = equiangular_cubed_sphere_warp)

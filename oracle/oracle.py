@@ -511,3 +511,125 @@ class ScalarHyperdiffusion:
             dQ = self.state()
         self.L.om_scalar_hyper_lsrk54(self.h, _ptr(Q), _ptr(dQ), dt, nsteps)
         return Q, dQ
+
+
+# ---------------------------------------------------------------------------
+# Element orders of the reference's brick topologies, restated in plain Python
+# integers (src/Numerics/Mesh/BrickMesh.jl:40-90 hilbertcode, :112-150
+# centroidtocode, :531-627 partition's sort by code; src/Numerics/Mesh/
+# Topologies.jl:632-715 StackedBrickTopology's contiguous columns).
+
+def hilbertcode(Y, bits=64):
+    """Hilbert index of the coordinates Y (each `bits` bits wide) as
+    len(Y) words, most significant first: Skilling's axes-to-transpose
+    followed by the transposition of BrickMesh.jl:78-87."""
+    X = [int(y) for y in Y]
+    n = len(X)
+    M = 1 << (bits - 1)
+    Q = M
+    for _ in range(bits - 1):
+        P = Q - 1
+        for i in range(n):
+            if X[i] & Q:
+                X[0] ^= P
+            else:
+                t = (X[0] ^ X[i]) & P
+                X[0] ^= t
+                X[i] ^= t
+        Q >>= 1
+    for i in range(1, n):
+        X[i] ^= X[i - 1]
+    t = 0
+    Q = M
+    for _ in range(bits - 1):
+        if X[n - 1] & Q:
+            t ^= Q - 1
+        Q >>= 1
+    X = [x ^ t for x in X]
+    H = [0] * n
+    for i in range(n):
+        for j in range(bits):
+            k = i * bits + j
+            bit = (X[n - 1 - (k % n)] >> (k // n)) & 1
+            H[n - 1 - i] |= bit << j
+    return H
+
+
+def centroidtocode(elemtocorner):
+    """Codes (d, nelem) of the element centroids of elemtocorner (d, nvert,
+    nelem), as centroidtocode computes them on one rank: the centroid scaled
+    by the elements' bounding box to [0, 1], times 2^64 - 1, floored
+    exactly (BrickMesh.jl:112-150)."""
+    from fractions import Fraction
+
+    etc = np.asarray(elemtocorner, dtype=np.float64)
+    d, nvert, nelem = etc.shape
+    cent = np.zeros((d, nelem))
+    for v in range(nvert):  # the reference sums the corners in order
+        cent += etc[:, v, :]
+    cent = cent / nvert
+    lo, hi = cent.min(axis=1), cent.max(axis=1)
+    size = hi - lo
+    if np.all(size == 0):
+        size = np.ones(d)
+    else:
+        size = np.where(size == 0, size.max(), size)
+    code = np.zeros((d, nelem), dtype=np.uint64)
+    top = (1 << 64) - 1
+    for e in range(nelem):
+        c = (cent[:, e] - lo) / size
+        X = [int(Fraction(float(ci)) * top) for ci in c]  # floor of an exact product
+        code[:, e] = np.array(hilbertcode(X, 64), dtype=np.uint64)
+    return code
+
+
+def range_point(lo, hi, n, k):
+    """The k-th point of range(lo, stop=hi, length=n+1): the exact
+    (lo (n - k) + hi k) / n rounded once to the nearest double."""
+    from fractions import Fraction
+
+    if k == 0:
+        return float(lo)
+    if k == n:
+        return float(hi)
+    return float((Fraction(lo) * (n - k) + Fraction(hi) * k) / n)
+
+
+def brick_corners(ne, lo, hi):
+    """elemtocorner (d, 2^d, nelem) of brickmesh over the ranges
+    range(lo, hi, length=ne+1), elements in Cartesian order (x fastest)."""
+    d = len(ne)
+    nelem = int(np.prod(ne))
+    etc = np.zeros((d, 1 << d, nelem))
+    for e in range(nelem):
+        r = e
+        idx = []
+        for i in range(d):
+            idx.append(r % ne[i])
+            r //= ne[i]
+        for v in range(1 << d):
+            for i in range(d):
+                k = idx[i] + ((v >> i) & 1)
+                etc[i, v, e] = range_point(lo[i], hi[i], ne[i], k)
+    return etc
+
+
+def hilbert_order(ne, lo, hi):
+    """Cartesian indices of the elements of a brick in BrickTopology's
+    order (sorted by code, ties by original index)."""
+    code = centroidtocode(brick_corners(ne, lo, hi))
+    keys = [tuple(int(c) for c in code[:, e]) + (e,) for e in range(code.shape[1])]
+    return [k[-1] for k in sorted(keys)]
+
+
+def reference_element_order(ne, lo, hi, topology):
+    """perm[e_ref] = index in the library's stacked order (e = iz + nz (ix +
+    nx iy)) of the element the reference's topology numbers e_ref:
+    "brick" (3D Hilbert order) or "stacked_brick" (2D Hilbert order of the
+    base, columns contiguous)."""
+    nx, ny, nz = ne
+    lib = lambda ix, iy, iz: iz + nz * (ix + nx * iy)
+    if topology == "brick":
+        return np.array([lib(c % nx, (c // nx) % ny, c // (nx * ny)) for c in hilbert_order(ne, lo, hi)])
+    cols = hilbert_order(ne[:2], lo[:2], hi[:2])
+    return np.array([lib(c % nx, c // nx, iz) for c in cols for iz in range(nz)])

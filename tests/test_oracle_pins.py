@@ -30,6 +30,11 @@ Pins (reference paths relative to the ClimateMachine.jl project root):
   * ARK2GiraldoKellyConstantinescu order 2 +- 0.35 in both splittings —
     test/Numerics/ODESolvers/ode_tests_convergence.jl:79-116 (measured on
     the DG system below the explicit vertical acoustic limit)
+  * Hilbert codes and centroid codes of the brick topologies' element order —
+    test/Numerics/Mesh/BrickMesh.jl:15-70 (hilbertcode known answers for 1-
+    and 2-bit coordinates and the 64-bit triple (14, 3, 4); centroidtocode of
+    six 2D elements) and test/Numerics/Mesh/mpi_centroid.jl (the same codes
+    of brickmesh((2.0:5.0, 4.0:6.0)))
 Geometry checks of the cubed shell (Topologies.jl:1067-1305, Metrics.jl:431-724):
 shell volume from the mass matrix, the discrete metric identities (a uniform
 state has zero tendency) and the face-node maps (a linear density advected by
@@ -455,3 +460,39 @@ def test_mms_fixture_matches_the_derivation():
             a = np.stack(np.broadcast_arrays(*f(t, x, y, z)))
             b = np.stack(np.broadcast_arrays(*g(t, x, y, z)))
             assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max()
+
+
+# hilbertcode known answers, test/Numerics/Mesh/BrickMesh.jl:16-38
+HILBERT_KNOWN = [
+    ((0, 0), 1, (0, 0)), ((0, 1), 1, (0, 1)), ((1, 1), 1, (1, 0)), ((1, 0), 1, (1, 1)),
+    ((0, 0), 2, (0, 0)), ((1, 0), 2, (0, 1)), ((1, 1), 2, (0, 2)), ((0, 1), 2, (0, 3)),
+    ((0, 2), 2, (1, 0)), ((0, 3), 2, (1, 1)), ((1, 3), 2, (1, 2)), ((1, 2), 2, (1, 3)),
+    ((2, 2), 2, (2, 0)), ((2, 3), 2, (2, 1)), ((3, 3), 2, (2, 2)), ((3, 2), 2, (2, 3)),
+    ((3, 1), 2, (3, 0)), ((2, 1), 2, (3, 1)), ((2, 0), 2, (3, 2)), ((3, 0), 2, (3, 3)),
+    ((14, 3, 4), 64, (0x0, 0x0, 0xE25)),
+]
+# centroidtocode known answer, BrickMesh.jl:41-60 and mpi_centroid.jl:33-36
+CENTROID_CODES = [
+    [0x0000000000000000, 0x1555555555555555, 0xFFFFFFFFFFFFFFFF, 0x5555555555555555, 0x6AAAAAAAAAAAAAAA,
+     0xAAAAAAAAAAAAAAAA],
+    [0x0000000000000000, 0x5555555555555555, 0xFFFFFFFFFFFFFFFF, 0x5555555555555555, 0xAAAAAAAAAAAAAAAA,
+     0xAAAAAAAAAAAAAAAA],
+]
+
+
+@pytest.mark.parametrize("Y,bits,H", HILBERT_KNOWN)
+def test_oracle_hilbertcode_known_answers(Y, bits, H):
+    assert tuple(O.hilbertcode(Y, bits)) == H
+
+
+def test_oracle_centroidtocode_known_answers():
+    etc = np.zeros((2, 4, 6))
+    for e, (x0, y0) in enumerate([(2, 4), (3, 4), (4, 4), (2, 5), (3, 5), (4, 5)]):
+        etc[:, :, e] = [[x0, x0 + 1, x0, x0 + 1], [y0, y0, y0 + 1, y0 + 1]]
+    assert [[int(c) for c in row] for row in O.centroidtocode(etc)] == CENTROID_CODES
+    # brickmesh((2.0:5.0, 4.0:6.0), (false, true)) numbers the same six elements
+    # in the same (Cartesian) order
+    assert [[int(c) for c in row] for row in O.centroidtocode(O.brick_corners((3, 2), (2.0, 4.0), (5.0, 6.0)))] == \
+        CENTROID_CODES
+    # one element: code zero (BrickMesh.jl:62-70)
+    assert (O.centroidtocode(etc[:, :, :1]) == 0).all()

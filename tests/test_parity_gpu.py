@@ -25,7 +25,7 @@ pytestmark = pytest.mark.gpu
 TOL64 = 1e-10
 # stage-kernel configurations: one CTA per element, a resident wave walking
 # the elements, one thread per vertical line of nodes
-KERNELS = {"node": ("node", -1), "persistent": ("node", 0), "column": ("column", 0)}
+KERNELS = {"node": ("node", -1), "persistent": ("node", 0), "column": ("column", 0), "lines": ("lines", -1)}
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -70,10 +70,12 @@ def make_pair(kind, N, ne, numflux="rusanov", precision="fp64"):
     return om, dg, Q0
 
 
+@pytest.mark.parametrize("kernel", ["node", "lines"])
 @pytest.mark.parametrize("N", [2, 3, 4, 5])
 @pytest.mark.parametrize("kind", ["vortex", "bubble"])
-def test_fp64_tendency_matches_oracle(kind, N):
+def test_fp64_tendency_matches_oracle(kind, N, kernel):
     om, dg, Q0 = make_pair(kind, N, (3, 2, 4))
+    dg.set_kernel(*KERNELS[kernel])
     ref = om.tendency(Q0)
     Q = dg.init_ode_state(Q0)
     dQ = dg.new_state(torch.float64)
@@ -82,8 +84,10 @@ def test_fp64_tendency_matches_oracle(kind, N):
     assert (err < TOL64).all(), err
 
 
-def test_fp64_central_flux_and_alpha_beta():
+@pytest.mark.parametrize("kernel", ["node", "lines"])
+def test_fp64_central_flux_and_alpha_beta(kernel):
     om, dg, Q0 = make_pair("bubble", 4, (2, 3, 3), numflux="central")
+    dg.set_kernel(*KERNELS[kernel])
     prev = np.random.default_rng(3).standard_normal(Q0.shape)
     ref = om.tendency(Q0, alpha=0.7, beta=-1.3, dQ=prev.copy())
     Q = dg.init_ode_state(Q0)
@@ -93,9 +97,11 @@ def test_fp64_central_flux_and_alpha_beta():
     assert (err < TOL64).all(), err
 
 
+@pytest.mark.parametrize("kernel", ["node", "lines"])
 @pytest.mark.parametrize("kind", ["vortex", "bubble"])
-def test_fp64_lsrk54_steps_match_oracle(kind):
+def test_fp64_lsrk54_steps_match_oracle(kind, kernel):
     om, dg, Q0 = make_pair(kind, 4, (3, 3, 3))
+    dg.set_kernel(*KERNELS[kernel])
     dt = 0.5 * om.courant_dt(Q0, 0.4)
     Qo, dQo = om.lsrk54(Q0.copy(), dt, 7)
     Q = dg.init_ode_state(Q0)
@@ -154,7 +160,7 @@ def test_c1_vortex_configuration_matches_oracle():
     assert np.isfinite(Qo).all() and dg.status_word() == 0
 
 
-@pytest.mark.parametrize("kernel", ["node", "persistent", "column"])
+@pytest.mark.parametrize("kernel", ["node", "persistent", "column", "lines"])
 @pytest.mark.parametrize("N", [3, 4, 5])
 def test_mixed_tendency_close_to_oracle(kernel, N):
     om, dg, Q0 = make_pair("bubble", N, (3, 3, 4), precision="mixed")
@@ -168,7 +174,7 @@ def test_mixed_tendency_close_to_oracle(kernel, N):
     assert max(err) < 1e-4, err
 
 
-@pytest.mark.parametrize("kernel", ["node", "persistent", "column"])
+@pytest.mark.parametrize("kernel", ["node", "persistent", "column", "lines"])
 def test_mixed_bubble_100_steps_within_1e5_of_fp64_oracle(kernel):
     om, dg, Q0 = make_pair("bubble", 4, (4, 4, 4), precision="mixed")
     dg.set_kernel(*KERNELS[kernel])
@@ -243,21 +249,21 @@ def test_mixed_kernels_agree_and_autotune_keeps_results(kind):
     om, dg, Q0 = make_pair(kind, 4, (5, 4, 6), precision="mixed")
     dt = 0.5 * om.courant_dt(Q0, 0.4)
     outs = {}
-    for kernel in ("node", "persistent", "column"):
+    for kernel in ("node", "persistent", "column", "lines"):
         dg.set_kernel(*KERNELS[kernel])
         Qp = dg.init_ode_state(Q0)
         lsrk = cmdg.LSRK54CarpenterKennedy(dg, Qp, dt=dt)
         cmdg.dostep_(Qp, lsrk, None, 0.0, nsteps=5)
         outs[kernel] = dg.from_perturbation(Qp).cpu().numpy()
-    for other in ("persistent", "column"):
+    for other in ("persistent", "column", "lines"):
         err, ref = om.field_l2(outs["node"], outs[other])
         # momentum as one vector field (rho*w of the vortex is noise-sized)
         err = np.array([err[0], np.sqrt(np.sum(err[1:4] ** 2)), err[4]])
         ref = np.array([ref[0], np.sqrt(np.sum(ref[1:4] ** 2)), ref[4]])
         assert (err / ref < 1e-6).all(), (other, err / ref)
     ms, choice = dg.autotune(reps=3)
-    assert len(ms) == 3 and all(m > 0 for m in ms)
-    assert choice[0] in ("node", "column")
+    assert len(ms) == 4 and all(m > 0 for m in ms)
+    assert choice[0] in ("node", "column", "lines")
     assert dg.status_word() == 0
 
 
@@ -309,3 +315,31 @@ def test_host_state_steps_equal_device_steps():
     with pytest.raises(_lib.CmdgError, match="page-locked"):
         _lib.call("cmdg_lsrk54_step_mixed_host", dg.h, ctypes.c_void_p(pageable.ctypes.data),
                   ctypes.c_void_p(Qp2.data_ptr()), ctypes.c_void_p(dQ2.data_ptr()), 0.0, dt, 1, None)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_stacked_brick_topology_order_runs_reference_ordered_states(precision):
+    """A brick mesh numbered like the reference's StackedBrickTopology (columns
+    along the 2D Hilbert curve) takes a state in the reference's element
+    order directly: its tendency and steps are those of the library's
+    stacked order, element for element, bit for bit."""
+    ne, L = (5, 4, 3), 2500.0
+    lo, hi = (0.0, 0.0, 0.0), (L, L, L)
+    grid_ref = cmdg.BrickGrid(4, ne, lo, hi, periodicity=(True, True, False), topology="stacked_brick")
+    model = workloads.bubble_model(ne=ne, N=4, L=L, precision=precision).balance_law
+    dg_ref = cmdg.DGModel(model, grid_ref, precision=precision)
+    dg_lib = workloads.bubble_model(ne=ne, N=4, L=L, precision=precision)
+    perm = cmdg.brick_element_order(ne, lo, hi, "stacked_brick")
+    xyz = dg_lib.grid.coordinates()
+    assert np.array_equal(grid_ref.coordinates(), xyz[perm])
+    Q0 = workloads.rising_bubble(xyz, rc=900.0, center=(1100.0, 1300.0, 900.0))
+    Q0[:, 1:4] += np.random.default_rng(4).uniform(-1, 1, size=Q0[:, 1:4].shape)
+    Ql, Qr = dg_lib.init_ode_state(Q0), dg_ref.init_ode_state(Q0[perm])
+    Tl, Tr = dg_lib.new_state(torch.float64), dg_ref.new_state(torch.float64)
+    dg_lib(Tl, Ql, None, 0.0)
+    dg_ref(Tr, Qr, None, 0.0)
+    assert torch.equal(Tr, Tl[torch.from_numpy(perm).cuda()])
+    dt = dg_lib.courant_dt(Ql, 0.4)
+    for dg, Q in ((dg_lib, Ql), (dg_ref, Qr)):
+        cmdg.dostep_(Q, cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt), None, 0.0, nsteps=3)
+    assert torch.equal(Qr, Ql[torch.from_numpy(perm).cuda()])
