@@ -36,6 +36,8 @@ default, the line the benchmark contract reads, is the bubble above):
   hyper     the bubble above with DryBiharmonic hyperdiffusion (tau = 1 h):
             per stage the gradient, laplacian and gradient-of-laplacian passes
             and the stage kernel with hyperdiffusive fluxes; 308 / 536 B
+  les16     16 members of the LES above (32.8 M nodes), mixed, batched
+            (one graph per call) vs 16 sequential single-member solves
   ensemble  64 seeded rising-bubble members of 8^3..16^3 elements and
             N = 3..5, mixed; batched (one graph of per-order launches) vs
             64 sequential single-member solves
@@ -172,6 +174,75 @@ def bench_ensemble(args, cmdg, workloads, torch, barrier, stream, flush):
     return 0
 
 
+def bench_les16(args, cmdg, workloads, torch, barrier, stream, flush):
+    """The 16-member LES configuration: 16 SmagorinskyLilly members of
+    32 x 32 x 16 elements, N = 4 (2,048,000 nodes each, 32.8 M in total),
+    seeded k^-5/3 velocity fields (one seed per member) over an N_bv = 0.01
+    stratification, mixed FP32/FP64, batched (one CUDA graph per call, the
+    gradient pass and the viscous stage kernel of every member and stage)
+    against 16 sequential single-member solves."""
+    nmem = 16
+    dgs = [workloads.les_model(precision="mixed") for _ in range(nmem)]
+    xyz = dgs[0].grid.coordinates()
+    Q0s = [workloads.les_initial_state(xyz, seed=2024 + m) for m in range(nmem)]
+    Qs = [dg.init_ode_state(Q0) for dg, Q0 in zip(dgs, Q0s)]
+    dt = min(dg.courant_dt(Q, CFL) for dg, Q in zip(dgs, Qs))
+    nodes = sum(dg.grid.nelem * dg.grid.Np for dg in dgs)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        barrier()
+        ms = []
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            ms.append((a, b))
+        barrier()
+        return sum(a.elapsed_time(b) for a, b in ms)
+
+    ens = cmdg.Ensemble(dgs)
+    dQe = [torch.zeros(Q.shape, dtype=torch.float64, device="cuda") for Q in Qs]
+    Qseq = [Q.clone() for Q in Qs]
+    lsrks = [cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt) for dg, Q in zip(dgs, Qseq)]
+
+    def bat():
+        ens.lsrk54_step(Qs, dQe, [dt] * nmem, nsteps=1)
+
+    def seq():
+        for Q, lsrk in zip(Qseq, lsrks):
+            cmdg.dostep_(Q, lsrk, None, 0.0)
+
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        ms_b = timed(bat)
+    ms_s = timed(seq)
+    # both runs took the same steps from the same states: the same numbers
+    same = all(bool(torch.equal(a, b)) for a, b in zip(Qs, Qseq))
+    work = NFIELD * nodes * NSTAGE * args.steps
+    peak, peak_kind = measured_peak()
+    bytes_ns = WORKLOADS["les"]["bytes_mixed"]
+    ach = bytes_ns * nodes / (ms_b / args.steps / NSTAGE * 1e-3) / 1e9
+    line = {"metric": "DOF-stage updates/s", "value": work / (ms_b * 1e-3), "unit": "DOF-stage/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_b / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": "16-member SmagorinskyLilly LES ensemble: 32x32x16 elements, N=4 per member "
+                                   "(2,048,000 nodes each), N_bv=0.01 1/s, seeded k^-5/3 velocity rms 1 m/s, mixed",
+                       "l2": L2_NOTE, "parallelism": "replicas x1"},
+            "nodes": nodes, "dt": dt,
+            "sequential": {"value": work / (ms_s * 1e-3), "ms_per_step": ms_s / args.steps},
+            "speedup_vs_sequential": ms_s / ms_b, "batched_equals_sequential": same,
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "peak_source": peak_kind, "kernel": "gradient_kernel + viscous_stage_kernel (16 members)",
+                         "bytes_per_node_stage": bytes_ns},
+            "gpu_launches": args.steps * NSTAGE * 2 * nmem, "clocks": clk.summary()}
+    print(json.dumps(line))
+    return 0
+
+
 def bench_hevi(args, cmdg, workloads, torch, barrier, stream, flush):
     """ARK2 + column-LU (HEVI) steps of the acoustic wave on the sphere: the
     explicit tendency on the FP32 perturbation of a mixed model (value) and
@@ -192,23 +263,24 @@ def bench_hevi(args, cmdg, workloads, torch, barrier, stream, flush):
                                                   dt=dt)
         return dg, Q0, lin, Q, ark
 
-    # without the reference test's vertical filter the wave stays smooth for
-    # about half of its one-hour run: the timed steps restart from the initial
-    # state every RUN steps (the copy sits between the timed events)
-    RUN = 20
+    # a step is the reference test's step: one ARK2 step followed by the
+    # vertical ExponentialFilter(grid, 0, 18) of every field (its callback);
+    # the FP64 state is filtered by an FP64 model in both runs
+    from cmdg.filters import ExponentialFilter, apply_
 
-    def timed_steps(Q, ark):
-        Qinit = Q.clone()
-        for _ in range(args.warmup):
+    def timed_steps(Q, ark, dgf, filt):
+        def step():
             cmdg.dostep_(Q, ark, None, 0.0, 1)
+            apply_(Q, (0, 1, 2, 3, 4), dgf, filt, direction="vertical")
+
+        for _ in range(args.warmup):
+            step()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
         barrier()
         for i in range(args.steps):
-            if i % RUN == 0:
-                Q.copy_(Qinit)
             flush.fill_(i & 0xFF)
             ev[i][0].record(stream)
-            cmdg.dostep_(Q, ark, None, 0.0, 1)
+            step()
             ev[i][1].record(stream)
         barrier()
         return sum(a.elapsed_time(b) for a, b in ev)
@@ -222,9 +294,10 @@ def bench_hevi(args, cmdg, workloads, torch, barrier, stream, flush):
     bwd = sum((NB - 1 if p < 5 else p) + 1 for p in range(NB))
     solve_bytes = 8 * ark.nline * (fwd + bwd) * nz + 8 * 5 * nodes * 5  # factors + b, y (w, r), out (r, w)
 
+    filt = ExponentialFilter(dg64.grid, 0, 18)
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
-        ms = timed_steps(Q, ark)
-        ms64 = timed_steps(Q64, ark64)
+        ms = timed_steps(Q, ark, dg64, filt)
+        ms64 = timed_steps(Q64, ark64, dg64, filt)
     M = dg64.grid.mass()
     a, b = Q.cpu().numpy(), Q64.cpu().numpy()
     rel = [math.sqrt(float(np.sum((a[:, sl] - b[:, sl]) ** 2 * M[:, None, :]))) /
@@ -249,6 +322,7 @@ def bench_hevi(args, cmdg, workloads, torch, barrier, stream, flush):
     def e2e_step():
         Qd.copy_(host, non_blocking=True)
         cmdg.dostep_(Qd, ark, None, 0.0, 1)
+        apply_(Qd, (0, 1, 2, 3, 4), dg64, filt, direction="vertical")
         host.copy_(Qd, non_blocking=True)
 
     for _ in range(2):
@@ -312,8 +386,8 @@ def bench_hevi(args, cmdg, workloads, torch, barrier, stream, flush):
                        "l2": "256 MiB buffer written between timed steps"},
             "fp64": {"value": work / (ms64 * 1e-3), "ms_per_step": ms64 / args.steps},
             "mixed_vs_fp64_rel_l2_rho_rhou_rhoe": rel,
-            "mixed_vs_fp64_steps": (args.steps - 1) % RUN + 1 if args.steps else 0,
-            "restart_every_steps": RUN,
+            "mixed_vs_fp64_steps": args.warmup + args.steps,
+            "step": "ARK2 step + vertical ExponentialFilter(grid, 0, 18) of every field (acousticwave_1d_imex.jl)",
             "simulated_s_per_wall_s": dt * args.steps / (ms * 1e-3),
             "explicit_lsrk54_mixed": {"dt": dt_x, "ms_per_step": ms_x / nx,
                                       "simulated_s_per_wall_s": dt_x * nx / (ms_x * 1e-3)},
@@ -324,7 +398,7 @@ def bench_hevi(args, cmdg, workloads, torch, barrier, stream, flush):
             "cpu_baseline": cpu,
             "e2e": {"value": work / (ms_e2e * 1e-3), "unit": "DOF-stage/s", "h2d_bytes_per_step": int(host.numel() * 8),
                     "d2h_bytes_per_step": int(host.numel() * 8)},
-            "gpu_launches": args.steps * 12, "clocks": clk.summary()}
+            "gpu_launches": args.steps * 13, "clocks": clk.summary()}
     print(json.dumps(line))
     return 0
 
@@ -515,7 +589,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the accuracy report against the FP64 oracle (bubble workload)")
-    ap.add_argument("--workload", default="bubble", choices=["bubble", "gcm", "les", "hyper", "ensemble", "hevi"])
+    ap.add_argument("--workload", default="bubble",
+                    choices=["bubble", "gcm", "les", "les16", "hyper", "ensemble", "hevi"])
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -568,6 +643,8 @@ def main():
         return bench_ensemble(args, cmdg, workloads, torch, barrier, stream, flush)
     if args.workload == "hevi":
         return bench_hevi(args, cmdg, workloads, torch, barrier, stream, flush)
+    if args.workload == "les16":
+        return bench_les16(args, cmdg, workloads, torch, barrier, stream, flush)
 
     spec = WORKLOADS[args.workload]
 

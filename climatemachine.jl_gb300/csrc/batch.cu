@@ -7,6 +7,11 @@
 // the end of the call.  Tile size (elements per tile) and grid shape per order
 // are chosen by cmdg_batch_autotune.
 //
+// Members with a turbulence closure (the LES members of a viscous ensemble)
+// take the gradient pass and the viscous stage kernel at every stage; their
+// stage chains, one launch pair per member and stage, run on a fourth branch
+// of the same graph.
+//
 // There is no counterpart in the reference, which advances one DGModel per
 // solver (ensembles there are separate runs).
 #include <algorithm>
@@ -35,6 +40,10 @@ struct Batch {
     std::vector<size_t> state_bytes;
     KParams* d_params = nullptr;    // [5 stages][members]
     Group groups[BATCH_NGROUPS];
+    // members with a turbulence closure, stepped member by member on their own branch
+    std::vector<int> viscous;
+    cudaStream_t visc_stream = nullptr;
+    cudaEvent_t visc_join = nullptr;
     cudaEvent_t fork = nullptr;
     // the parameters currently on the device
     std::vector<const void*> cur_Q;
@@ -59,7 +68,7 @@ static int build_tiles(Batch* b, Group& g) {
         more = false;
         for (size_t m = 0; m < b->members.size(); ++m) {
             const Mesh& mesh = *b->members[m]->mesh;
-            if (mesh.N != g.N || pos[m] >= mesh.nelem) continue;
+            if (mesh.N != g.N || pos[m] >= mesh.nelem || b->members[m]->prm.turbulence != CMDG_TURB_NONE) continue;
             const int64_t e1 = std::min<int64_t>(mesh.nelem, pos[m] + g.tile_elems);
             tiles.push_back(BatchTile{(int)m, (int)pos[m], (int)e1, mesh.N});
             pos[m] = e1;
@@ -146,6 +155,36 @@ static int issue(Batch* b, int nsteps, cudaStream_t s) {
                 if ((e = launch_batch_stage(b->d_params + st * n, g.d_tiles, g.ntiles, g.N, grid, gs)) != cudaSuccess)
                     return launch_error(e);
     }
+    if (!b->viscous.empty()) {
+        cudaStream_t vs = first ? s : b->visc_stream;
+        if (!first && (e = cudaStreamWaitEvent(vs, b->fork, 0)) != cudaSuccess) return launch_error(e);
+        const double *A, *B;
+        lsrk54_coefficients(&A, &B);
+        for (int step = 0; step < nsteps; ++step)
+            for (int st = 0; st < 5; ++st)
+                for (int m : b->viscous) {
+                    char* S1 = static_cast<char*>(b->scratch[m]);
+                    char* S2 = S1 + b->state_bytes[m];
+                    void* Q = const_cast<void*>(b->cur_Q[m]);
+                    void* const order[6] = {Q, S1, S2, S1, S2, Q};
+                    LaunchArgs a;
+                    a.Qin = order[st];
+                    a.Qout = order[st + 1];
+                    a.dQ = const_cast<double*>(static_cast<const double*>(b->cur_dQ[m]));
+                    a.alpha = a.beta = 1.0;
+                    a.rka = A[st];
+                    a.rkb_dt = B[st] * b->cur_dt[m];
+                    a.mode = 1;
+                    a.first_stage = st == 0;
+                    a.last_stage = st == 4;
+                    const int rc = launch_stage(b->members[m], a, vs);
+                    if (rc) return rc;
+                }
+        if (!first) {
+            if ((e = cudaEventRecord(b->visc_join, vs)) != cudaSuccess) return launch_error(e);
+            if ((e = cudaStreamWaitEvent(s, b->visc_join, 0)) != cudaSuccess) return launch_error(e);
+        }
+    }
     for (Group* g : joined) {
         if ((e = cudaEventRecord(g->join, g->stream)) != cudaSuccess) return launch_error(e);
         if ((e = cudaStreamWaitEvent(s, g->join, 0)) != cudaSuccess) return launch_error(e);
@@ -162,6 +201,8 @@ static void release(Batch* b) {
         if (g.join) cudaEventDestroy(g.join);
     }
     if (b->fork) cudaEventDestroy(b->fork);
+    if (b->visc_stream) cudaStreamDestroy(b->visc_stream);
+    if (b->visc_join) cudaEventDestroy(b->visc_join);
     drop_graph(b);
     delete b;
 }
@@ -184,12 +225,15 @@ extern "C" int cmdg_batch_create(cmdg_model* const* models, int n, cmdg_batch** 
         CMDG_ARG_CHECK(md.precision == CMDG_MIXED, "member %d: ensembles run the mixed-precision path", m);
         CMDG_ARG_CHECK(md.mesh->N >= BATCH_NMIN && md.mesh->N <= BATCH_NMAX,
                        "member %d: N=%d outside the ensemble range [3, 5]", m, md.mesh->N);
-        CMDG_ARG_CHECK(md.prm.turbulence == CMDG_TURB_NONE && md.prm.hyperdiffusion == CMDG_HYPER_NONE,
-                       "member %d: ensembles are inviscid", m);
+        CMDG_ARG_CHECK(md.prm.hyperdiffusion == CMDG_HYPER_NONE, "member %d: ensembles run without hyperdiffusion",
+                       m);
         CMDG_ARG_CHECK(md.mesh->kind == MESH_BRICK, "member %d: ensembles run on brick meshes", m);
     }
     Batch* b = new Batch();
-    for (int m = 0; m < n; ++m) b->members.push_back(&models[m]->m);
+    for (int m = 0; m < n; ++m) {
+        b->members.push_back(&models[m]->m);
+        if (models[m]->m.prm.turbulence != CMDG_TURB_NONE) b->viscous.push_back(m);
+    }
     int rc = CMDG_OK;
     auto cuda_fail = [&](cudaError_t e, const char* what) {
         set_error("ensemble %s failed: %s", what, cudaGetErrorString(e));
@@ -210,6 +254,10 @@ extern "C" int cmdg_batch_create(cmdg_model* const* models, int n, cmdg_batch** 
     cudaError_t e;
     if (!rc && (e = cudaMalloc(&b->d_params, sizeof(KParams) * 5 * n)) != cudaSuccess) cuda_fail(e, "allocation");
     if (!rc && (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess) cuda_fail(e, "event");
+    if (!rc && (e = cudaStreamCreateWithFlags(&b->visc_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        cuda_fail(e, "stream");
+    if (!rc && (e = cudaEventCreateWithFlags(&b->visc_join, cudaEventDisableTiming)) != cudaSuccess)
+        cuda_fail(e, "event");
     for (int gi = 0; gi < BATCH_NGROUPS && !rc; ++gi) {
         Group& g = b->groups[gi];
         g.N = BATCH_NMIN + gi;

@@ -97,6 +97,19 @@ cudaError_t launch_column(const KParams& P, int N, bool mixed, int mode, int gri
 // Line-kernel launcher (stage_lines.cu), one CTA per element; returns
 // cudaErrorNotSupported for an N without an instantiation.
 cudaError_t launch_lines(const KParams& P, int N, bool mixed, int mode, cudaStream_t s);
+// Weak-form derivative Dhat of the orders 3, 4 and 5 in FP32, passed by value
+// to the ensemble kernel (row-major, Dhat[i][n] = D[n][i] w_n / w_i).
+struct EnsDhat {
+    float d3[16];
+    float d4[25];
+    float d5[36];
+};
+// Ensemble stage launch of the persistent line kernel over tiles of every
+// order (mixed precision, stage mode) with cta_threads = 128 or 256, and the
+// number of its CTAs resident on the device (stage_lines.cu).
+cudaError_t launch_ens_lines(const KParams* d_params, const BatchTile* d_tiles, int ntiles, int cta_threads, int grid,
+                             const EnsDhat& D, cudaStream_t s);
+int ens_lines_resident_ctas(int cta_threads);
 
 namespace {
 

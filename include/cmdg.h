@@ -274,12 +274,16 @@ int cmdg_lsrk54_step(cmdg_model* model, double* d_Q, double* d_dQ, double t, dou
 int cmdg_lsrk54_step_noalloc(cmdg_model* model, void* d_Q, double* d_dQ, double t, double dt, int nsteps,
                              void* stream);
 
-/* Ensembles.  A batch advances n mixed-precision, inviscid brick models of
- * any sizes and polynomial orders N = 3..5 together.  Members are grouped by
+/* Ensembles.  A batch advances n mixed-precision brick models of any sizes
+ * and polynomial orders N = 3..5 together.  Inviscid members are grouped by
  * order; each LSRK54 stage of a group is one launch of a tile-walking kernel
  * (a tile is a run of consecutive elements of one member), the groups' stage
  * chains run on their own streams, and the steps of a call are captured in one
- * CUDA graph (stream != NULL).  The batch owns two stage buffers per member.
+ * CUDA graph (stream != NULL).  Members with a turbulence closure (LES
+ * members: ConstantDynamicViscosity or SmagorinskyLilly) take the gradient
+ * pass and the viscous stage kernel at every stage, member by member, on a
+ * further branch of the same graph.  The batch owns two stage buffers per
+ * member; a viscous member's gradient-flux buffer is its model's.
  * No counterpart in the reference (there, ensemble members are separate
  * solver runs). */
 typedef struct cmdg_batch cmdg_batch;

@@ -100,3 +100,32 @@ def test_ensemble_member_close_to_fp64_oracle():
     err = np.array([err[0], np.sqrt(np.sum(err[1:4] ** 2)), err[4]])
     ref = np.array([ref[0], np.sqrt(np.sum(ref[1:4] ** 2)), ref[4]])
     assert (err / ref < 1e-5).all(), err / ref
+
+
+def test_les_ensemble_matches_single_models_and_stays_near_the_oracle():
+    """A batch of LES members (mixed SmagorinskyLilly, as in the 16-member LES
+    configuration, at a size the oracle steps quickly): a batched member's
+    steps equal its single-model steps bit for bit (the same gradient pass
+    and viscous stage kernel per stage), and a batched member stays within
+    1e-5 (relative L2 per field group) of the FP64 oracle after 100 steps."""
+    Lx, ne, nmem = (800.0, 800.0, 600.0), (4, 4, 3), 3
+    dgs = [workloads.les_model(ne=ne, N=4, L=Lx, precision="mixed") for _ in range(nmem)]
+    Q0s = [workloads.les_initial_state(dgs[0].grid.coordinates(), L=Lx, seed=s) for s in range(1, nmem + 1)]
+    dt = min(dg.courant_dt(dg.init_ode_state(Q0), 0.4) for dg, Q0 in zip(dgs, Q0s))
+    ens = cmdg.Ensemble(dgs)
+    Qs = [dg.init_ode_state(Q0) for dg, Q0 in zip(dgs, Q0s)]
+    dQs = [torch.zeros(Q.shape, dtype=torch.float64, device="cuda") for Q in Qs]
+    for _ in range(2):
+        ens.lsrk54_step(Qs, dQs, [dt] * nmem, nsteps=50)  # one graph, replayed
+    single = workloads.les_model(ne=ne, N=4, L=Lx, precision="mixed")
+    Q = single.init_ode_state(Q0s[0])
+    cmdg.dostep_(Q, cmdg.LSRK54CarpenterKennedy(single, Q, dt=dt), None, 0.0, nsteps=100)
+    assert torch.equal(Qs[0], Q)
+    om = O.OracleModel(4, ne, (0, 0, 0), Lx, periodic=(1, 1, 0), orientation="flat", gravity=True, ref_state=True,
+                       profile="dry_adiabatic", T_surface=300.0, T_min=0.0, turbulence="smagorinsky")
+    Qo, _ = om.lsrk54(Q0s[1].copy(), dt, 100)
+    err, refn = om.field_l2(dgs[1].from_perturbation(Qs[1]).cpu().numpy(), Qo)
+    err = np.array([err[0], np.sqrt(np.sum(err[1:4] ** 2)), err[4]])
+    refn = np.array([refn[0], np.sqrt(np.sum(refn[1:4] ** 2)), refn[4]])
+    assert (err / refn < 1e-5).all(), err / refn
+    assert all(dg.status_word() == 0 for dg in dgs)
