@@ -256,7 +256,15 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
 #pragma unroll
                 for (int s = 0; s < NSTATE; ++s) cur.qp[s] = qn[s * Np];
             }
-            if (!mbar_wait_bounded(&bars[b], (uint32_t)((it >> 1) & 1), P.wait_polls)) timed_out = true;
+            const bool arrived = mbar_wait_bounded(&bars[b], (uint32_t)((it >> 1) & 1), P.wait_polls);
+            // a staging copy that did not complete in time: every thread of
+            // the CTA stops here, before an element is computed from the
+            // unfilled buffer and before a barrier whose phase is still open
+            // would be armed again (one arrival per phase)
+            if (__syncthreads_or(!arrived)) {
+                timed_out = true;
+                break;
+            }
             uintptr_t qlo, dlo;
             uint32_t qbytes, dbytes;
             bool qok, dok;

@@ -32,8 +32,8 @@
 // Ensembles: one persistent launch per stage over a list of tiles of all
 // orders, with one CTA shape for every order: 128 threads run two N = 3
 // elements, one N = 4 element, or one N = 5 element at two nodes per thread;
-// 256 threads run four N = 3, two N = 4 or two N = 5 elements (the
-// autotuner's choice).
+// 256 threads run four N = 3, two N = 4 or one N = 5 element, a thread per
+// node (the autotuner's choice).
 //
 // Arithmetic restated from src/Numerics/DGMethods/DGModel_kernels.jl:64-548
 // (volume_tendency!), :588-901 (dgsem_interface_tendency!),
@@ -60,12 +60,14 @@ struct LDims {
 };
 
 // Work split of a CTA of NT threads over elements of order N: EPI elements
-// at a time, TPE threads per element, NPT nodes per thread.
+// at a time, TPE threads per element, NPT nodes per thread -- as many
+// elements as fit with a thread per node, else one element with several
+// nodes per thread (every line still needs a thread of its own).
 template <int N, int NT>
 struct LSplit {
     static constexpr int Np = LDims<N>::Np;
-    static constexpr int TPE_MIN = (LDims<N>::NL + 31) / 32 * 32;  // every line needs a thread
-    static constexpr int EPI = NT / TPE_MIN >= 4 ? 4 : (NT / TPE_MIN >= 2 ? 2 : 1);
+    static constexpr int TPE_NODE = (Np + 31) / 32 * 32;
+    static constexpr int EPI = NT / TPE_NODE >= 4 ? 4 : (NT / TPE_NODE >= 2 ? 2 : 1);
     static constexpr int TPE = NT / EPI;
     static constexpr int NPT = (Np + TPE - 1) / TPE;
     static_assert(TPE >= LDims<N>::NL, "a sub-block needs one thread per element line");
@@ -374,7 +376,7 @@ __device__ __forceinline__ int lines_tile(const KParams& P, const EnsDhat& D, un
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NT, NT == 128 ? 8 : 4)
+__global__ void __launch_bounds__(NT, NT == 128 ? 6 : 3)
     ens_lines_kernel(const KParams* __restrict__ params, const BatchTile* __restrict__ tiles, int ntiles,
                      const __grid_constant__ EnsDhat D) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
