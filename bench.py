@@ -145,7 +145,8 @@ def bench_ensemble(args, cmdg, workloads, torch, barrier, stream, flush):
     ens = cmdg.Ensemble(dgs)
     Qe = [Q.clone() for Q in Q0s]
     dQe = [torch.zeros(Q.shape, dtype=torch.float64, device="cuda") for Q in Qe]
-    _, tiling = ens.autotune(Qe, dQe, reps=5)
+    cand_ms, tiling = ens.autotune(Qe, dQe, reps=5)
+    persistent = tiling["kernel"][0] == "persistent"
 
     def bat():
         ens.lsrk54_step(Qe, dQe, dts, nsteps=1)
@@ -166,10 +167,14 @@ def bench_ensemble(args, cmdg, workloads, torch, barrier, stream, flush):
                        "l2": "256 MiB buffer written between timed steps"},
             "sequential": {"value": work / (ms_s * 1e-3), "ms_per_step": ms_s / args.steps},
             "speedup_vs_sequential": ms_s / ms_b,
+            "autotune_ms_per_stage": {"per_order_family": cand_ms["per_order"],
+                                      "persistent_best": min(cand_ms["persistent"])},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                         "peak_source": peak_kind, "kernel": "batch_stage_kernel<N>", "bytes_per_node_stage":
-                         BYTES_MIXED},
-            "gpu_launches": args.steps * NSTAGE * 3, "clocks": clk.summary()}
+                         "peak_source": peak_kind,
+                         "kernel": ("ens_lines_kernel (one persistent launch per stage, every order)"
+                                    if persistent else "batch_stage_kernel<N> (one launch per order and stage)"),
+                         "bytes_per_node_stage": BYTES_MIXED},
+            "gpu_launches": args.steps * NSTAGE * (1 if persistent else 3), "clocks": clk.summary()}
     print(json.dumps(line))
     return 0
 
@@ -234,7 +239,9 @@ def bench_les16(args, cmdg, workloads, torch, barrier, stream, flush):
                        "l2": L2_NOTE, "parallelism": "replicas x1"},
             "nodes": nodes, "dt": dt,
             "sequential": {"value": work / (ms_s * 1e-3), "ms_per_step": ms_s / args.steps},
-            "speedup_vs_sequential": ms_s / ms_b, "batched_equals_sequential": same,
+            "speedup_vs_sequential": ms_s / ms_b,
+            "autotune_ms_per_stage": {"per_order_family": cand_ms["per_order"],
+                                      "persistent_best": min(cand_ms["persistent"])}, "batched_equals_sequential": same,
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                          "peak_source": peak_kind, "kernel": "gradient_kernel + viscous_stage_kernel (16 members)",
                          "bytes_per_node_stage": bytes_ns},
@@ -409,6 +416,19 @@ def profile_traffic(name):
     if os.path.exists(path):
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
+                try:
+                    return float(line.split(":", 1)[1].split()[0])
+                except ValueError:
+                    return None
+    return None
+
+
+def profile_value(name, key):
+    """A `key: value` figure of a profile summary under profiles/ (None when absent)."""
+    path = os.path.join(REPO, "profiles", name)
+    if os.path.exists(path):
+        for line in open(path):
+            if line.startswith(key + ":"):
                 try:
                     return float(line.split(":", 1)[1].split()[0])
                 except ValueError:
@@ -769,7 +789,10 @@ def main():
                     "stage_kernel": {k: list(v) for k, v in kernels.items()}},
             "fp64": {"value": v64, "ms_per_step": ms_64 / args.steps,
                      "roofline": {"bound": "hbm", "achieved": ach_64, "peak": peak, "unit": "GB/s",
-                                  "frac": ach_64 / peak}},
+                                  "frac": ach_64 / peak},
+                     # the plain path is bound by the FP64 pipe (ncu capture of its stage kernel)
+                     "fp64_pipe_frac": (profile_value("stage_kernel_fp64_bubble20.md", "fp64_pipe_frac")
+                                        if args.workload == "bubble" else None)},
             "mixed_speedup_vs_fp64": value / v64,
             "mixed_step_ms": {"min": min(per_mx), "median": statistics.median(per_mx), "max": max(per_mx)},
             "mixed_vs_fp64_rel_l2": rel,

@@ -34,7 +34,7 @@ EXPORTS = (
     "cmdg_filter_matrix", "cmdg_apply_filter", "cmdg_apply_tmar",
     "cmdg_linear_tendency", "cmdg_hevi_create", "cmdg_hevi_destroy", "cmdg_hevi_info", "cmdg_hevi_solve",
     "cmdg_hevi_step", "cmdg_apply_mp_filter", "cmdg_model_set_mms", "cmdg_model_set_staging_test",
-    "cmdg_brick_element_order", "cmdg_mesh_create_brick_ordered",
+    "cmdg_brick_element_order", "cmdg_mesh_create_brick_ordered", "cmdg_batch_set_kernel", "cmdg_batch_get_kernel",
 )
 
 
@@ -140,6 +140,8 @@ def load(path: str | None = None):
         "cmdg_model_set_staging_test": [P, I, I],
         "cmdg_brick_element_order": [ctypes.POINTER(BrickDesc), I, P],
         "cmdg_mesh_create_brick_ordered": [ctypes.POINTER(BrickDesc), I, PP],
+        "cmdg_batch_set_kernel": [P, I, I, I, I],
+        "cmdg_batch_get_kernel": [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)],
     }
     for name, args in proto.items():
         fn = getattr(L, name)

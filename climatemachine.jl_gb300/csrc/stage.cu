@@ -69,14 +69,17 @@ struct Dims {
 template <int N, typename R>
 struct Smem {
     static constexpr int Nq = N + 1, Np = Nq * Nq * Nq, Nfp = Nq * Nq;
-    // planar five-field records (Planar5): node states, volume fluxes by
-    // direction, lifted face fluxes; (sound speed, 1/rho) pairs per node
+    // planar five-field records (Planar5): node states and volume fluxes by
+    // direction; (sound speed, 1/rho) pairs per node; the lifted face fluxes
+    // in node-major scalar planes, one set per face direction (a node lies
+    // on at most one face of each direction), so a node reads its face terms
+    // with consecutive 4- or 8-byte accesses
     static constexpr int P5N = planar_pad<R>(5 * Np);      // one five-field plane set over the nodes
     static constexpr int NODE = 0;
     static constexpr int CR = NODE + P5N;
     static constexpr int FLUX = CR + planar_pad<R>(2 * Np);
     static constexpr int FACE = FLUX + 3 * P5N;
-    static constexpr int DMAT = FACE + planar_pad<R>(5 * 6 * Nfp);
+    static constexpr int DMAT = FACE + planar_pad<R>(3 * 5 * Np);
     static constexpr int TOTAL = DMAT + Nq * Nq;
     static constexpr size_t BYTES = sizeof(R) * TOTAL;
 };
@@ -123,12 +126,27 @@ struct Ahead {
 // RK register blocks (contiguous in the (Np, 5, nelem) layout) into the other
 // of two shared-memory buffers, so every CTA keeps memory requests in flight
 // throughout without per-thread copy instructions.
-template <int N, typename R, bool MIXED, int MODE, bool PERSIST>
+// PARAM_D: P is the kernel's own parameter, so the weak-form derivative is
+// read from its constant bank (a constant-cache load with the thread's row
+// index) rather than from shared memory; the ensemble kernel, whose launch
+// parameters sit in global memory, stages it in shared memory.
+template <typename R>
+__device__ __forceinline__ R dhat_const(const KParams& P, int idx);
+template <>
+__device__ __forceinline__ float dhat_const<float>(const KParams& P, int idx) {
+    return P.DhatC32[idx];
+}
+template <>
+__device__ __forceinline__ double dhat_const<double>(const KParams& P, int idx) {
+    return P.DhatC64[idx];
+}
+
+template <int N, typename R, bool MIXED, int MODE, bool PERSIST, bool PARAM_D>
 __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem_raw, int e_first, int e_stride,
                                            int e_end) {
     using Dm = Dims<N>;
     using SM = Smem<N, R>;
-    constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, NFN = 6 * Nfp;
+    constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp;
     constexpr int ESTRIDE = NSTATE * Np;  // elements of R (or double) per element
     using PL = Planar5<R>;
     using CRV = typename Pair<R>::V;
@@ -171,7 +189,7 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
     };
     const R sgn = fside ? R(1) : R(-1);
 
-    if (t < Nq * Nq) s_D[t] = static_cast<const R*>(P.Dhat)[t];
+    if (!PARAM_D && t < Nq * Nq) s_D[t] = static_cast<const R*>(P.Dhat)[t];
 
     auto fetch = [&](int e, Ahead<R>& a) {
         const int* nbr = P.nbr + NBR_STRIDE * e;
@@ -368,7 +386,8 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
             R fs[NSTATE];
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) fs[s] = hl * (Fm[s] + Fp[s]) + pl * ((qm[s] - qp[s]) + jr[s]);
-            PL::st(s_fs, NFN, f * Nfp + fn, fs);
+#pragma unroll
+            for (int s = 0; s < NSTATE; ++s) s_fs[(fd * NSTATE + s) * Np + vM] = fs[s];
         }
         __syncthreads();
 
@@ -385,7 +404,9 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
                 PL::ld(s_F, Np, L1 + n * Nfp, v1);
                 PL::ld(s_F + SM::P5N, Np, L2 + n * Nfp, v2);
                 PL::ld(s_F + 2 * SM::P5N, Np, L3 + n * Nfp, v3);
-                const R d1 = s_D[ni * Nq + n], d2 = s_D[nj * Nq + n], d3 = s_D[nk * Nq + n];
+                const R d1 = PARAM_D ? dhat_const<R>(P, ni * Nq + n) : s_D[ni * Nq + n];
+                const R d2 = PARAM_D ? dhat_const<R>(P, nj * Nq + n) : s_D[nj * Nq + n];
+                const R d3 = PARAM_D ? dhat_const<R>(P, nk * Nq + n) : s_D[nk * Nq + n];
 #pragma unroll
                 for (int s = 0; s < NSTATE; ++s) {
                     acc1[s] = fma(d1, v1[s], acc1[s]);
@@ -396,19 +417,15 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
             R rhs[NSTATE];
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) rhs[s] = xi[0] * acc1[s] + xi[1] * acc2[s] + xi[2] * acc3[s];
-            // face terms (vMI sM F*, lifted in phase 2), in face order 1..6
-            auto sub_face = [&](int ff, int idx) {
-                R v[NSTATE];
-                PL::ld(s_fs, NFN, ff * Nfp + idx, v);
+            // face terms (vMI sM F*, lifted in phase 2), in face order 1..6:
+            // at most one face per direction holds the node
+            auto sub_face = [&](int dd) {
 #pragma unroll
-                for (int s = 0; s < NSTATE; ++s) rhs[s] -= v[s];
+                for (int s = 0; s < NSTATE; ++s) rhs[s] -= s_fs[(dd * NSTATE + s) * Np + t];
             };
-            if (ni == 0) sub_face(0, nj + Nq * nk);
-            if (ni == N) sub_face(1, nj + Nq * nk);
-            if (nj == 0) sub_face(2, ni + Nq * nk);
-            if (nj == N) sub_face(3, ni + Nq * nk);
-            if (nk == 0) sub_face(4, ni + Nq * nj);
-            if (nk == N) sub_face(5, ni + Nq * nj);
+            if (ni == 0 || ni == N) sub_face(0);
+            if (nj == 0 || nj == N) sub_face(1);
+            if (nk == 0 || nk == N) sub_face(2);
             rhs[3] += gsrc;
             const R rkb_dt = KConst<R>::rkb_dt(P);
 #pragma unroll
@@ -464,7 +481,7 @@ template <int N, typename R, bool MIXED, int MODE, bool PERSIST>
 __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? (PERSIST ? Dims<N>::MIN_CTAS : Dims<N>::MIN_CTAS_DIRECT)
                                                      : Dims<N>::MIN_CTAS64) stage_kernel(const KParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    stage_body<N, R, MIXED, MODE, PERSIST>(P, smem_raw, blockIdx.x, PERSIST ? gridDim.x : P.nelem, P.nelem);
+    stage_body<N, R, MIXED, MODE, PERSIST, true>(P, smem_raw, blockIdx.x, PERSIST ? gridDim.x : P.nelem, P.nelem);
 }
 
 template <int N, typename R, bool MIXED, int MODE, bool PERSIST>
@@ -521,7 +538,7 @@ __global__ void __launch_bounds__(Dims<N>::NT, Dims<N>::MIN_CTAS_DIRECT)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     for (int it = blockIdx.x; it < ntiles; it += gridDim.x) {
         const BatchTile T = tiles[it];
-        stage_body<N, float, true, 1, false>(params[T.member], smem_raw, T.e0, 1, T.e1);
+        stage_body<N, float, true, 1, false, false>(params[T.member], smem_raw, T.e0, 1, T.e1);
     }
 }
 

@@ -299,12 +299,32 @@ int cmdg_batch_get_tiling(const cmdg_batch* batch, int N, int* tile_elems, int* 
  * time steps.  Same per-member semantics as cmdg_lsrk54_step_mixed. */
 int cmdg_batch_lsrk54_step(cmdg_batch* batch, void* const* h_Q, double* const* h_dQ, const double* h_dt, int nsteps,
                            void* stream);
-/* Autotuner, per order over tile_elems {1, 2, 4, 8, 16} x grid {one CTA per
- * tile, one wave of resident CTAs}: times `reps` stage launches each on
- * copies of the members' states (the states are not changed; the RK
- * registers are overwritten, which the next step ignores), keeps each order's
- * fastest, and writes ms per stage launch to h_ms as [order 3, 4, 5][candidate]
- * (0 for an order without members). */
+/* Kernel family of the inviscid members:
+ *   CMDG_BATCH_PER_ORDER  one tile-walking launch per order and stage, the
+ *                         orders on independent branches (tiling per order:
+ *                         cmdg_batch_set_tiling);
+ *   CMDG_BATCH_PERSISTENT one launch per stage of one persistent kernel over
+ *                         tiles of every order with one CTA shape:
+ *                         cta_threads 128 (two N = 3 elements, one N = 4
+ *                         element, one N = 5 element at two nodes per thread
+ *                         per CTA pass) or 256 (four, two and one, a thread
+ *                         per node); tile_elems elements per tile; grid_ctas
+ *                         -1 = one CTA per tile, 0 = one wave of resident
+ *                         CTAs, n > 0 = n CTAs.
+ * cmdg_batch_get_kernel returns the family and the persistent tiling. */
+enum { CMDG_BATCH_PER_ORDER = 0, CMDG_BATCH_PERSISTENT = 1 };
+int cmdg_batch_set_kernel(cmdg_batch* batch, int family, int cta_threads, int tile_elems, int grid_ctas);
+int cmdg_batch_get_kernel(const cmdg_batch* batch, int* family, int* cta_threads, int* tile_elems, int* grid_ctas);
+/* Autotuner: times `reps` stage launches of every candidate on copies of the
+ * members' states (the states are not changed; the RK registers are
+ * overwritten, which the next step ignores): per order tile_elems {1, 2, 4,
+ * 8, 16} x grid {one CTA per tile, one wave of resident CTAs}, keeping each
+ * order's fastest, then the whole per-order family; and the persistent kernel
+ * over cta_threads {128, 256} x tile_elems {1, 2, 4, 8} x grid {one CTA per
+ * tile, one wave}.  Keeps the faster family with its fastest tiling.  h_ms
+ * receives ms per stage launch: [order 3, 4, 5][10 per-order candidates] (0
+ * for an order without members), the 16 persistent candidates, the whole
+ * per-order family (n_candidates = 47). */
 int cmdg_batch_autotune(cmdg_batch* batch, void* const* h_Q, double* const* h_dQ, int reps, double* h_ms,
                         int h_ms_len, int* n_candidates, void* stream);
 

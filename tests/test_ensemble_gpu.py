@@ -73,6 +73,9 @@ def test_ensemble_autotune_and_tilings_keep_results():
             for N in (3, 4, 5):
                 assert len(ms[N]) == 10 and all(m > 0 for m in ms[N])
                 assert choice[N][0] in (1, 2, 4, 8, 16) and choice[N][1] in (-1, 0)
+            assert len(ms["persistent"]) == 16 and all(m > 0 for m in ms["persistent"]) and ms["per_order"] > 0
+            assert choice["kernel"][0] in ("per_order", "persistent")
+            ens.set_kernel("per_order")  # the per-order tilings chosen above, compared bitwise below
         else:
             ens.set_tiling(*tiling)
             assert ens.get_tiling()[4] == tiling
@@ -81,6 +84,38 @@ def test_ensemble_autotune_and_tilings_keep_results():
     for other in outs[1:]:
         for a, b in zip(outs[0], other):
             assert np.array_equal(a, b)
+    assert all(dg.status_word() == 0 for dg in dgs)
+
+
+def test_persistent_ensemble_kernel_matches_per_order_launches():
+    """The persistent kernel (one launch per stage over tiles of every order,
+    one CTA shape: 128 or 256 threads, so each order runs its own number of
+    elements per CTA pass and nodes per thread) advances every member as the
+    per-order kernels do, up to FP32 reassociation (the two kernels sum the
+    same terms in different orders), for every tiling, and its results do not
+    depend on the tiling within one CTA size."""
+    specs = members(n=6, seed=5)
+    pairs = [workloads.bubble_member(s) for s in specs]
+    dgs = [p[0] for p in pairs]
+    dts = [0.5 * dg.courant_dt(dg.init_ode_state(Q0), 0.4) for dg, Q0 in pairs]
+
+    def run(kernel):
+        ens = cmdg.Ensemble(dgs)
+        ens.set_kernel(*kernel)
+        Qs = [dg.init_ode_state(Q0) for dg, Q0 in pairs]
+        dQs = [torch.zeros(Q.shape, dtype=torch.float64, device="cuda") for Q in Qs]
+        ens.lsrk54_step(Qs, dQs, dts, nsteps=3)
+        return [Q.cpu().numpy() for Q in Qs]
+
+    ref = run(("per_order",))
+    for threads in (128, 256):
+        outs = [run(("persistent", threads, tile, grid)) for tile, grid in ((1, -1), (4, 0), (8, 5))]
+        for other in outs[1:]:
+            for a, b in zip(outs[0], other):
+                assert np.array_equal(a, b)
+        for a, r in zip(outs[0], ref):
+            scale = np.abs(r).max(axis=(0, 2), keepdims=True)
+            assert (np.abs(a - r) <= 1e-6 * scale).all(), threads
     assert all(dg.status_word() == 0 for dg in dgs)
 
 
