@@ -299,8 +299,6 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
     } else if (shell) {
         CMDG_ARG_CHECK(p->orientation == CMDG_ORIENT_NONE || p->orientation == CMDG_ORIENT_SPHERE,
                        "orientation %d is not available on a cubed shell", p->orientation);
-        CMDG_ARG_CHECK(p->turbulence != CMDG_TURB_SMAGORINSKY || precision == CMDG_FP64,
-                       "SmagorinskyLilly on the cubed shell runs FP64 models");
         CMDG_ARG_CHECK(p->turbulence == CMDG_TURB_NONE || p->hyperdiffusion == CMDG_HYPER_NONE,
                        "the cubed-shell kernels run viscosity or hyperdiffusion, not both");
         CMDG_ARG_CHECK(p->orientation != CMDG_ORIENT_SPHERE || p->planet_radius > 0, "planet_radius must be positive");

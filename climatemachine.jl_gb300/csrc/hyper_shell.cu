@@ -78,7 +78,9 @@ __device__ __forceinline__ R shell_face_normal(const KParams& P, const R* g, int
 // PROJECT = false: the gradient arguments of the diffusive closures, u and
 // h_tot (AtmosModel.jl:622-650, energy.jl:20-31)
 // NA = 5 adds theta_v = T / (p / MSLP)^kappa (SmagorinskyLilly's N^2,
-// TurbulenceClosures.jl:446-454; FP64 only)
+// TurbulenceClosures.jl:446-454); in the mixed form the perturbation
+// theta_v' = theta_v_ref expm1(log1p(T'/T_ref) - kappa log1p(p'/p_ref)),
+// formed without cancelling against the reference value
 template <typename R, bool MIXED, bool PROJECT = true, int NA = 4>
 __device__ __forceinline__ void shell_hyper_args(const KParams& P, const R q[NSTATE], const Level<R>& lv, const R* g,
                                                  int Np, int n, R H[NA]) {
@@ -95,6 +97,14 @@ __device__ __forceinline__ void shell_hyper_args(const KParams& P, const R q[NST
     if (MIXED && P.ph.ref_state) {
         const R pp = gm1 * (q[4] - R(0.5) * ke2) + q[0] * lv.crho;
         H[3] = ((q[4] + pp) * lv.rho_ref - lv.href * q[0]) * (rinv / lv.rho_ref);
+        if (NA == 5) {
+            const R kappa = VConst<R>::kappa(P);
+            const R rT = (pp * lv.rho_ref - lv.p_ref * q[0]) * (rinv / lv.p_ref);  // T'/T_ref
+            const R lnr = log1p_r(rT) - kappa * log1p_r(pp / lv.p_ref);
+            const R T_ref = lv.p_ref / (lv.rho_ref * VConst<R>::R_d(P));
+            const R thv_ref = T_ref / pow_r(lv.p_ref / VConst<R>::MSLP(P), kappa);
+            H[NA - 1] = thv_ref * expm1_r(lnr);
+        }
     } else {
         const R p = gm1 * (q[4] - R(0.5) * ke2) + rho * lv.crho;
         H[3] = (q[4] + p) * rinv;
@@ -455,16 +465,19 @@ cudaError_t launch_arrays_visc(const KParams& P, int N, bool smag, const void* Q
     }
 }
 
-// grad u, grad h_tot (12 words); with smag also grad theta_v (15 words, FP64)
+// grad u, grad h_tot (12 words); with smag also grad theta_v (15 words)
 cudaError_t launch_shell_visc(const KParams& P, int N, bool mixed, bool smag, const void* Q, void* gout,
                               cudaStream_t s) {
     if (smag) {
-        if (mixed) return cudaErrorInvalidValue;
         switch (N) {
-            case 2: return launch_shell_visc_typed<2, double, false, 5>(P, Q, gout, s);
-            case 3: return launch_shell_visc_typed<3, double, false, 5>(P, Q, gout, s);
-            case 4: return launch_shell_visc_typed<4, double, false, 5>(P, Q, gout, s);
-            case 5: return launch_shell_visc_typed<5, double, false, 5>(P, Q, gout, s);
+            case 2: return mixed ? launch_shell_visc_typed<2, float, true, 5>(P, Q, gout, s)
+                                 : launch_shell_visc_typed<2, double, false, 5>(P, Q, gout, s);
+            case 3: return mixed ? launch_shell_visc_typed<3, float, true, 5>(P, Q, gout, s)
+                                 : launch_shell_visc_typed<3, double, false, 5>(P, Q, gout, s);
+            case 4: return mixed ? launch_shell_visc_typed<4, float, true, 5>(P, Q, gout, s)
+                                 : launch_shell_visc_typed<4, double, false, 5>(P, Q, gout, s);
+            case 5: return mixed ? launch_shell_visc_typed<5, float, true, 5>(P, Q, gout, s)
+                                 : launch_shell_visc_typed<5, double, false, 5>(P, Q, gout, s);
             default: return cudaErrorInvalidValue;
         }
     }
@@ -606,8 +619,10 @@ int launch_shell_hyper_passes(Model* md, const void* Qin, void* hd_out, cudaStre
 }
 
 // The gradient buffer of the viscous pass and, in mixed precision, the
-// FP64 gradient of the reference h_tot (the viscous pass on the reference
-// state at rest: u = 0, h_tot = h_ref; the pass is linear in its arguments).
+// FP64 gradients of the reference h_tot and, with SmagorinskyLilly, of the
+// reference theta_v (the viscous pass on the reference state at rest: u = 0,
+// h_tot = h_ref, theta_v = theta_v_ref; the pass is linear in its
+// arguments), per node (Np, 3 or 6, nelem).
 int init_shell_visc_tables(Model* md) {
     const Mesh& m = *md->mesh;
     const int Np = m.Np;
@@ -633,8 +648,9 @@ int init_shell_visc_tables(Model* md) {
         CMDG_CUDA_CHECK(cudaMalloc(&md->d_sdelta, nn * sizeof(double)));
         CMDG_CUDA_CHECK(cudaMemcpy(md->d_sdelta, delta.data(), nn * sizeof(double), cudaMemcpyHostToDevice));
     }
-    CMDG_CUDA_CHECK(cudaMalloc(&md->d_vgref, nn * 3 * sizeof(float)));
-    CMDG_CUDA_CHECK(cudaMemset(md->d_vgref, 0, nn * 3 * sizeof(float)));
+    const int nref = smag ? 6 : 3;
+    CMDG_CUDA_CHECK(cudaMalloc(&md->d_vgref, nn * nref * sizeof(float)));
+    CMDG_CUDA_CHECK(cudaMemset(md->d_vgref, 0, nn * nref * sizeof(float)));
     if (!mixed || !md->prm.ref_state) return CMDG_OK;
     std::vector<double> qref(nn * NSTATE, 0.0);
     for (int64_t e = 0; e < m.nelem; ++e)
@@ -644,7 +660,7 @@ int init_shell_visc_tables(Model* md) {
         }
     double *dq = nullptr, *dg = nullptr;
     cudaError_t ce = cudaMalloc(&dq, nn * NSTATE * sizeof(double));
-    if (ce == cudaSuccess) ce = cudaMalloc(&dg, nn * 12 * sizeof(double));
+    if (ce == cudaSuccess) ce = cudaMalloc(&dg, nn * ngw * sizeof(double));
     if (ce == cudaSuccess) ce = cudaMemcpy(dq, qref.data(), nn * NSTATE * sizeof(double), cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) {
         LaunchArgs a;
@@ -656,13 +672,13 @@ int init_shell_visc_tables(Model* md) {
         KParams P = make_params(md, a);
         P.Dhat = md->d_Dhat64;
         P.geo = md->d_geo64;
-        ce = launch_shell_visc(P, m.N, false, false, dq, dg, 0);
+        ce = launch_shell_visc(P, m.N, false, smag, dq, dg, 0);
         if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
     }
     std::vector<double> g64;
     if (ce == cudaSuccess) {
-        g64.resize(nn * 12);
-        ce = cudaMemcpy(g64.data(), dg, nn * 12 * sizeof(double), cudaMemcpyDeviceToHost);
+        g64.resize(nn * ngw);
+        ce = cudaMemcpy(g64.data(), dg, nn * ngw * sizeof(double), cudaMemcpyDeviceToHost);
     }
     cudaFree(dq);
     cudaFree(dg);
@@ -670,12 +686,13 @@ int init_shell_visc_tables(Model* md) {
         set_error("reference viscous gradient pass failed: %s", cudaGetErrorString(ce));
         return CMDG_ERR_CUDA;
     }
-    std::vector<float> ref32(nn * 3);
+    // words 9..11 of the pass: grad h_tot; 12..14 with SmagorinskyLilly: grad theta_v
+    std::vector<float> ref32(nn * nref);
     for (int64_t e = 0; e < m.nelem; ++e)
-        for (int j = 0; j < 3; ++j)
+        for (int j = 0; j < nref; ++j)
             for (int n = 0; n < Np; ++n)
-                ref32[((size_t)e * 3 + j) * Np + n] = (float)g64[((size_t)e * 12 + 9 + j) * Np + n];
-    CMDG_CUDA_CHECK(cudaMemcpy(md->d_vgref, ref32.data(), nn * 3 * sizeof(float), cudaMemcpyHostToDevice));
+                ref32[((size_t)e * nref + j) * Np + n] = (float)g64[((size_t)e * ngw + 9 + j) * Np + n];
+    CMDG_CUDA_CHECK(cudaMemcpy(md->d_vgref, ref32.data(), nn * nref * sizeof(float), cudaMemcpyHostToDevice));
     return CMDG_OK;
 }
 

@@ -387,17 +387,12 @@ cudaError_t launch_shell_N(const KParams& P, bool mixed, int mode, cudaStream_t 
                      : launch_shell_typed<N, double, false, 1, HYPER, VT>(P, s);
 }
 
-// hyperdiffusion and viscosity are exclusive on the shell, SmagorinskyLilly
-// is FP64 (cmdg_model_create)
+// hyperdiffusion and viscosity are exclusive on the shell (cmdg_model_create)
 template <int N>
 cudaError_t launch_shell_N(const KParams& P, bool mixed, int mode, bool hyper, int turb, cudaStream_t s) {
     if (hyper) return launch_shell_N<N, true, CMDG_TURB_NONE>(P, mixed, mode, s);
     if (turb == CMDG_TURB_CONSTANT) return launch_shell_N<N, false, CMDG_TURB_CONSTANT>(P, mixed, mode, s);
-    if (turb == CMDG_TURB_SMAGORINSKY) {
-        if (mixed) return cudaErrorInvalidValue;
-        return mode == 0 ? launch_shell_typed<N, double, false, 0, false, CMDG_TURB_SMAGORINSKY>(P, s)
-                         : launch_shell_typed<N, double, false, 1, false, CMDG_TURB_SMAGORINSKY>(P, s);
-    }
+    if (turb == CMDG_TURB_SMAGORINSKY) return launch_shell_N<N, false, CMDG_TURB_SMAGORINSKY>(P, mixed, mode, s);
     return launch_shell_N<N, false, CMDG_TURB_NONE>(P, mixed, mode, s);
 }
 

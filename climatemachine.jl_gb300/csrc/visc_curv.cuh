@@ -26,10 +26,17 @@ __device__ __forceinline__ void shell_gf(const KParams& P, int64_t e, int n, int
     for (int w = 0; w < NW; ++w) G[w] = g[w * Np];
 #pragma unroll
     for (int d = 0; d < 3; ++d) gf[d] = G[9 + d];
+    // mixed: the pass differentiated the perturbations h' (and theta_v');
+    // add the FP64-computed gradients of the reference parts
+    constexpr int NREF = VT == CMDG_TURB_SMAGORINSKY ? 6 : 3;
     if (MIXED && P.ph.ref_state) {
-        const float* r = P.vgref32 + (size_t)e * 3 * Np + n;
+        const float* r = P.vgref32 + (size_t)e * NREF * Np + n;
 #pragma unroll
         for (int d = 0; d < 3; ++d) gf[d] += (R)r[d * Np];
+        if (VT == CMDG_TURB_SMAGORINSKY) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) G[12 + (NW == 15 ? d : 0)] += (R)r[(3 + d) * Np];
+        }
     }
     gf[3] = G[0];
     gf[4] = (G[1] + G[3]) / 2;
@@ -44,7 +51,9 @@ __device__ __forceinline__ void shell_gf(const KParams& P, int64_t e, int n, int
         const R rho = MIXED ? lv.rho_ref + q[0] : q[0];
         const R rinv = R(1) / rho;
         const R ke2 = (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) * rinv;
-        const R p = KConst<R>::gm1(P) * (q[4] - R(0.5) * ke2) + rho * lv.crho;
+        // p = p_ref + p' in the mixed form (q holds the perturbation)
+        const R p = MIXED ? lv.p_ref + (KConst<R>::gm1(P) * (q[4] - R(0.5) * ke2) + q[0] * lv.crho)
+                          : KConst<R>::gm1(P) * (q[4] - R(0.5) * ke2) + rho * lv.crho;
         const R T = p * rinv / VConst<R>::R_d(P);
         const R thv = T / pow_r(p / VConst<R>::MSLP(P), VConst<R>::kappa(P));
         gf[9] = (G[12] * ge[(KG_GPHI + 0) * Np + n] + G[13] * ge[(KG_GPHI + 1) * Np + n] +
