@@ -292,8 +292,6 @@ int cmdg_model_create(cmdg_mesh* mesh, const cmdg_atmos_params* p, int precision
     const bool arrays = mesh->m.kind == MESH_ARRAYS;
     if (arrays) {
         CMDG_ARG_CHECK(p->hyperdiffusion == CMDG_HYPER_NONE, "no hyperdiffusion on grid-arrays meshes");
-        CMDG_ARG_CHECK(p->turbulence == CMDG_TURB_NONE || precision == CMDG_FP64,
-                       "turbulence closures on grid-arrays meshes run FP64 models");
         CMDG_ARG_CHECK(p->orientation >= CMDG_ORIENT_NONE && p->orientation <= CMDG_ORIENT_SPHERE,
                        "unknown orientation %d", p->orientation);
     } else if (shell) {

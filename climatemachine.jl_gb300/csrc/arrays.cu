@@ -34,7 +34,8 @@ struct ArraysSmem {
     static constexpr size_t BYTES = sizeof(R) * TOTAL;
 };
 
-// VT: the turbulence closure (FP64): the viscous fluxes of the curvilinear
+// VT: the turbulence closure (FP64 or mixed; mixed adds the FP64-computed
+// gradients of the reference h_tot and theta_v): the viscous fluxes of the curvilinear
 // gradient pass's output join the volume flux and, with the facing node's
 // state, the central second-order interface flux; walls carry the
 // first-order flux only.
@@ -307,19 +308,19 @@ cudaError_t launch_arrays_typed(const KParams& P, cudaStream_t s) {
 }
 
 // closures run FP64 on grid-arrays meshes (cmdg_model_create)
+template <int N, int VT>
+cudaError_t launch_arrays_VT(const KParams& P, bool mixed, int mode, cudaStream_t s) {
+    if (mixed)
+        return mode == 0 ? launch_arrays_typed<N, float, true, 0, VT>(P, s) : launch_arrays_typed<N, float, true, 1, VT>(P, s);
+    return mode == 0 ? launch_arrays_typed<N, double, false, 0, VT>(P, s)
+                     : launch_arrays_typed<N, double, false, 1, VT>(P, s);
+}
+
 template <int N>
 cudaError_t launch_arrays_N(const KParams& P, bool mixed, int mode, int turb, cudaStream_t s) {
-    if (turb == CMDG_TURB_CONSTANT)
-        return mode == 0 ? launch_arrays_typed<N, double, false, 0, CMDG_TURB_CONSTANT>(P, s)
-                         : launch_arrays_typed<N, double, false, 1, CMDG_TURB_CONSTANT>(P, s);
-    if (turb == CMDG_TURB_SMAGORINSKY)
-        return mode == 0 ? launch_arrays_typed<N, double, false, 0, CMDG_TURB_SMAGORINSKY>(P, s)
-                         : launch_arrays_typed<N, double, false, 1, CMDG_TURB_SMAGORINSKY>(P, s);
-    if (mixed)
-        return mode == 0 ? launch_arrays_typed<N, float, true, 0, CMDG_TURB_NONE>(P, s)
-                         : launch_arrays_typed<N, float, true, 1, CMDG_TURB_NONE>(P, s);
-    return mode == 0 ? launch_arrays_typed<N, double, false, 0, CMDG_TURB_NONE>(P, s)
-                     : launch_arrays_typed<N, double, false, 1, CMDG_TURB_NONE>(P, s);
+    if (turb == CMDG_TURB_CONSTANT) return launch_arrays_VT<N, CMDG_TURB_CONSTANT>(P, mixed, mode, s);
+    if (turb == CMDG_TURB_SMAGORINSKY) return launch_arrays_VT<N, CMDG_TURB_SMAGORINSKY>(P, mixed, mode, s);
+    return launch_arrays_VT<N, CMDG_TURB_NONE>(P, mixed, mode, s);
 }
 
 }  // namespace

@@ -218,6 +218,12 @@ int set_arrays_reference(Model* md, const double* aux7) {
     CMDG_CUDA_CHECK(cudaMemcpy(md->d_ref64, md->ref64.data(), sizeof(double) * md->ref64.size(), cudaMemcpyHostToDevice));
     CMDG_CUDA_CHECK(cudaMemcpy(md->d_fjump, jump.data(), sizeof(float) * jump.size(), cudaMemcpyHostToDevice));
     md->has_reference = true;
+    // mixed precision with a closure: the FP64 gradients of the reference
+    // h_tot (and theta_v) that the stage kernel adds to the perturbation's
+    if (md->precision == CMDG_MIXED && p.turbulence != CMDG_TURB_NONE && p.ref_state) {
+        rc = visc_reference_gradients(md);
+        if (rc) return rc;
+    }
     // the linear model's tables hold the previous reference state
     cudaFree(md->d_lin64);
     cudaFree(md->d_linface64);

@@ -285,6 +285,9 @@ int launch_shell_hyper_passes(Model* md, const void* Qin, void* hd_out, cudaStre
 // buffer (grad u, grad h_tot, (Np, 12, nelem)) and, mixed, grad h_ref; the
 // gradient pass of Qin into gout
 int init_shell_visc_tables(Model* md);
+// mixed precision: the FP64 gradients of the reference h_tot (and theta_v)
+// per node into md->d_vgref (the viscous pass on the reference state at rest)
+int visc_reference_gradients(Model* md);
 int launch_shell_visc_gradient(Model* md, const void* Qin, void* gout, cudaStream_t s);
 
 // reductions / conversions (reduce.cu)

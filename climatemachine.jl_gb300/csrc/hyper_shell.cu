@@ -450,17 +450,24 @@ cudaError_t launch_shell_visc_typed(const KParams& P, const void* Q, void* gout,
     return cudaGetLastError();
 }
 
-// grid-arrays meshes, FP64: grad u, grad h_tot (and grad theta_v with smag)
-cudaError_t launch_arrays_visc(const KParams& P, int N, bool smag, const void* Q, void* gout, cudaStream_t s) {
+// grid-arrays meshes: grad u, grad h_tot (and grad theta_v with smag); the
+// mixed form differentiates the perturbations
+template <int N>
+cudaError_t launch_arrays_visc_N(const KParams& P, bool mixed, bool smag, const void* Q, void* gout, cudaStream_t s) {
+    if (mixed)
+        return smag ? launch_shell_visc_typed<N, float, true, 5, true>(P, Q, gout, s)
+                    : launch_shell_visc_typed<N, float, true, 4, true>(P, Q, gout, s);
+    return smag ? launch_shell_visc_typed<N, double, false, 5, true>(P, Q, gout, s)
+                : launch_shell_visc_typed<N, double, false, 4, true>(P, Q, gout, s);
+}
+
+cudaError_t launch_arrays_visc(const KParams& P, int N, bool mixed, bool smag, const void* Q, void* gout,
+                               cudaStream_t s) {
     switch (N) {
-        case 2: return smag ? launch_shell_visc_typed<2, double, false, 5, true>(P, Q, gout, s)
-                            : launch_shell_visc_typed<2, double, false, 4, true>(P, Q, gout, s);
-        case 3: return smag ? launch_shell_visc_typed<3, double, false, 5, true>(P, Q, gout, s)
-                            : launch_shell_visc_typed<3, double, false, 4, true>(P, Q, gout, s);
-        case 4: return smag ? launch_shell_visc_typed<4, double, false, 5, true>(P, Q, gout, s)
-                            : launch_shell_visc_typed<4, double, false, 4, true>(P, Q, gout, s);
-        case 5: return smag ? launch_shell_visc_typed<5, double, false, 5, true>(P, Q, gout, s)
-                            : launch_shell_visc_typed<5, double, false, 4, true>(P, Q, gout, s);
+        case 2: return launch_arrays_visc_N<2>(P, mixed, smag, Q, gout, s);
+        case 3: return launch_arrays_visc_N<3>(P, mixed, smag, Q, gout, s);
+        case 4: return launch_arrays_visc_N<4>(P, mixed, smag, Q, gout, s);
+        case 5: return launch_arrays_visc_N<5>(P, mixed, smag, Q, gout, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -651,7 +658,21 @@ int init_shell_visc_tables(Model* md) {
     const int nref = smag ? 6 : 3;
     CMDG_CUDA_CHECK(cudaMalloc(&md->d_vgref, nn * nref * sizeof(float)));
     CMDG_CUDA_CHECK(cudaMemset(md->d_vgref, 0, nn * nref * sizeof(float)));
-    if (!mixed || !md->prm.ref_state) return CMDG_OK;
+    // a mesh from grid arrays takes its reference state later, from
+    // cmdg_model_set_reference, which computes these gradients then
+    if (!mixed || !md->prm.ref_state || m.kind == MESH_ARRAYS) return CMDG_OK;
+    return visc_reference_gradients(md);
+}
+
+// In mixed precision, the FP64 gradients of the reference h_tot (and
+// theta_v) per node into md->d_vgref: the FP64 viscous gradient pass on the
+// reference state at rest.
+int visc_reference_gradients(Model* md) {
+    const Mesh& m = *md->mesh;
+    const int Np = m.Np;
+    const size_t nn = (size_t)m.nelem * Np;
+    const bool smag = md->prm.turbulence == CMDG_TURB_SMAGORINSKY;
+    const int ngw = smag ? 15 : 12, nref = smag ? 6 : 3;
     std::vector<double> qref(nn * NSTATE, 0.0);
     for (int64_t e = 0; e < m.nelem; ++e)
         for (int n = 0; n < Np; ++n) {
@@ -672,7 +693,8 @@ int init_shell_visc_tables(Model* md) {
         KParams P = make_params(md, a);
         P.Dhat = md->d_Dhat64;
         P.geo = md->d_geo64;
-        ce = launch_shell_visc(P, m.N, false, smag, dq, dg, 0);
+        ce = m.kind == MESH_ARRAYS ? launch_arrays_visc(P, m.N, false, smag, dq, dg, 0)
+                                   : launch_shell_visc(P, m.N, false, smag, dq, dg, 0);
         if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
     }
     std::vector<double> g64;
@@ -707,7 +729,7 @@ int launch_shell_visc_gradient(Model* md, const void* Qin, void* gout, cudaStrea
     const KParams P = make_params(md, a);
     const bool smag = md->prm.turbulence == CMDG_TURB_SMAGORINSKY;
     const cudaError_t err = m.kind == MESH_ARRAYS
-                                ? launch_arrays_visc(P, m.N, smag, Qin, gout, s)
+                                ? launch_arrays_visc(P, m.N, md->precision == CMDG_MIXED, smag, Qin, gout, s)
                                 : launch_shell_visc(P, m.N, md->precision == CMDG_MIXED, smag, Qin, gout, s);
     if (err != cudaSuccess) {
         set_error("cubed-shell viscous gradient pass launch failed: %s", cudaGetErrorString(err));

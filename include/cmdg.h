@@ -87,7 +87,7 @@ typedef struct {
     int profile;        /* CMDG_PROFILE_* */
     double T_surface;   /* isothermal T_virt, or dry-adiabatic surface temperature */
     double T_min;       /* dry-adiabatic minimum temperature */
-    int turbulence;     /* CMDG_TURB_* (bricks and cubed shell: both closures, FP64 and mixed; grid arrays: FP64) */
+    int turbulence;     /* CMDG_TURB_* (both closures on every mesh, FP64 and mixed) */
     double rho_nu;      /* ConstantDynamicViscosity rho*nu */
     int with_divergence;/* ConstantDynamicViscosity WithDivergence */
     double C_smag;      /* SmagorinskyLilly coefficient */
