@@ -22,12 +22,23 @@ roofline   the dominant kernel (the fused mixed stage kernel) against the
            B = 2*5*4 (state r/w, FP32) + 2*5*8 (RK register r/w, FP64) = 120.
 cpu_baseline  the C++ oracle (the CPU restatement of the reference) on the
            host cores, on a bounded sample of the same workload.
+accuracy   outside the timed region: the mixed and FP64 GPU paths against the
+           FP64 oracle after one tendency and after 100 LSRK54 steps (relative
+           L2 and max relative error per field), and the mass and energy drift.
+ensemble   the batched mixed ensemble of --workload ensemble (64 members),
+           timed over the same steps (--no-ensemble skips it).
 
 --impl reference times the reference's CPU path (the oracle port, the
 reference itself is Julia and cannot run here) on the same workload.
 
 --workload selects another configuration for the same measurement (the
 default, the line the benchmark contract reads, is the bubble above):
+  bubble-arrays  the bubble above through the reference's own grid arrays
+            (vgeo, vmap+, elemtobndy in BrickTopology's Hilbert element order,
+            cmdg_mesh_create_arrays): the path a Julia caller drops in;
+            algorithmic bytes 202.4 (mixed) / 300.8 (FP64) per node-stage
+            (the per-node geometry and reference words, the facing-node and
+            reference-jump tables on top of the state and register)
   gcm       cubed-shell GCM, 6 x 12 x 12 x 6 elements, N=4 (648,000 nodes),
             30 km lid, isothermal 285 K, seeded zonal wind + 1 K anomaly;
             algorithmic bytes 224 (mixed) / 264 (FP64) per node-stage
@@ -96,6 +107,14 @@ WORKLOADS = {
                 bytes_mixed=200, bytes_fp64=320, launches_per_stage=2,
                 kernel="gradient_kernel + viscous_stage_kernel<4,float,mixed,stage,smagorinsky>",
                 profile="viscous_stage_kernel_mixed_les.md"),
+    # per node-stage: state + register 120 (mixed) / 160 (FP64), the per-node geometry and reference
+    # words 17 x 4 / 17 x 8, the facing-node table 1.2 x 4 and (mixed, Rusanov) the reference-jump
+    # table 1.2 x 8
+    "bubble-arrays": dict(desc=WORKLOAD + "; grid arrays (vgeo, vmap+, elemtobndy) in BrickTopology's Hilbert "
+                                          "element order through cmdg_mesh_create_arrays",
+                          bytes_mixed=120 + 68 + 4.8 + 9.6, bytes_fp64=160 + 136 + 4.8, launches_per_stage=1,
+                          kernel="arrays_stage_kernel<4,float,mixed,stage>",
+                          profile="arrays_stage_kernel_mixed_bubble20.md"),
     # per node-stage: stage kernel 120 + nu grad^3 read 36; gradient pass 20 + 36; laplacian 36 + 12;
     # gradient of the laplacian 12 + 36 (FP32 words; FP64 doubles all but the RK register's 80)
     "hyper": dict(desc="rising bubble of the default workload with DryBiharmonic(tau = 3600 s) hyperdiffusion: "
@@ -106,11 +125,11 @@ WORKLOADS = {
 }
 
 
-def bench_ensemble(args, cmdg, workloads, torch, barrier, stream, flush):
+def measure_ensemble(args, cmdg, workloads, torch, barrier, stream, flush):
     """64 seeded bubble members (8^3..16^3 elements, N = 3..5), mixed:
-    batched steps (one CUDA graph per call of per-order tile-walking launches)
+    batched steps (one CUDA graph per call, the tiling the autotuner picks)
     against 64 sequential single-member solves (each member autotuned, one
-    graph-captured call per member)."""
+    graph-captured call per member).  Returns the ensemble's JSON fields."""
     specs = workloads.bubble_ensemble_specs(n=64)
     pairs = [workloads.bubble_member(s) for s in specs]
     dgs = [p[0] for p in pairs]
@@ -157,14 +176,11 @@ def bench_ensemble(args, cmdg, workloads, torch, barrier, stream, flush):
     work = NFIELD * nodes * NSTAGE * args.steps
     peak, peak_kind = measured_peak()
     ach = BYTES_MIXED * nodes / (ms_b / args.steps / NSTAGE * 1e-3) / 1e9
-    line = {"metric": "DOF-stage updates/s", "value": work / (ms_b * 1e-3), "unit": "DOF-stage/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_b / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-            "data": "synthetic",
-            "config": {"workload": "64-member rising-bubble ensemble, elements U{8..16}^3, N U{3,4,5}, amplitude "
-                                   "U[0.5,3] K, radius U[150,400] m, mixed", "nodes": nodes,
-                       "tiling": {str(k): v for k, v in tiling.items()},
-                       "l2": "256 MiB buffer written between timed steps"},
+    return {"value": work / (ms_b * 1e-3), "unit": "DOF-stage/s", "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_b / args.steps,
+            "workload": "64-member rising-bubble ensemble, elements U{8..16}^3, N U{3,4,5}, amplitude "
+                        "U[0.5,3] K, radius U[150,400] m, mixed",
+            "nodes": nodes, "tiling": {str(k): v for k, v in tiling.items()},
             "sequential": {"value": work / (ms_s * 1e-3), "ms_per_step": ms_s / args.steps},
             "speedup_vs_sequential": ms_s / ms_b,
             "autotune_ms_per_stage": {"per_order_family": cand_ms["per_order"],
@@ -175,6 +191,19 @@ def bench_ensemble(args, cmdg, workloads, torch, barrier, stream, flush):
                                     if persistent else "batch_stage_kernel<N> (one launch per order and stage)"),
                          "bytes_per_node_stage": BYTES_MIXED},
             "gpu_launches": args.steps * NSTAGE * (1 if persistent else 3), "clocks": clk.summary()}
+
+
+def bench_ensemble(args, cmdg, workloads, torch, barrier, stream, flush):
+    """The ensemble of measure_ensemble as its own JSON line."""
+    r = measure_ensemble(args, cmdg, workloads, torch, barrier, stream, flush)
+    line = {"metric": "DOF-stage updates/s", "value": r["value"], "unit": "DOF-stage/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": r["workload"], "nodes": r["nodes"], "tiling": r["tiling"],
+                       "l2": "256 MiB buffer written between timed steps"}}
+    for k in ("sequential", "speedup_vs_sequential", "autotune_ms_per_stage", "roofline", "gpu_launches", "clocks"):
+        line[k] = r[k]
     print(json.dumps(line))
     return 0
 
@@ -239,9 +268,7 @@ def bench_les16(args, cmdg, workloads, torch, barrier, stream, flush):
                        "l2": L2_NOTE, "parallelism": "replicas x1"},
             "nodes": nodes, "dt": dt,
             "sequential": {"value": work / (ms_s * 1e-3), "ms_per_step": ms_s / args.steps},
-            "speedup_vs_sequential": ms_s / ms_b,
-            "autotune_ms_per_stage": {"per_order_family": cand_ms["per_order"],
-                                      "persistent_best": min(cand_ms["persistent"])}, "batched_equals_sequential": same,
+            "speedup_vs_sequential": ms_s / ms_b, "batched_equals_sequential": same,
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                          "peak_source": peak_kind, "kernel": "gradient_kernel + viscous_stage_kernel (16 members)",
                          "bytes_per_node_stage": bytes_ns},
@@ -610,7 +637,9 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the accuracy report against the FP64 oracle (bubble workload)")
     ap.add_argument("--workload", default="bubble",
-                    choices=["bubble", "gcm", "les", "les16", "hyper", "ensemble", "hevi"])
+                    choices=["bubble", "bubble-arrays", "gcm", "les", "les16", "hyper", "ensemble", "hevi"])
+    ap.add_argument("--no-ensemble", action="store_true",
+                    help="skip the batched-ensemble measurement the bubble line carries")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -675,6 +704,10 @@ def main():
         if args.workload == "les":
             dg = workloads.les_model(precision=precision)
             return dg, workloads.les_initial_state(dg.grid.coordinates())
+        if args.workload == "bubble-arrays":
+            dg, _, xyz = workloads.bubble_arrays_model(ne=NE, N=N, L=L, precision=precision)
+            Q0 = workloads.rising_bubble(xyz, theta0=300.0, amp=2.0, rc=250.0, center=(1250.0, 1250.0, 350.0))
+            return dg, Q0
         if args.workload == "hyper":
             dg = workloads.hyper_bubble_model(ne=NE, N=N, L=L, precision=precision)
         else:
@@ -769,6 +802,13 @@ def main():
         except Exception as exc:  # the report must not hide the GPU line
             accuracy = {"error": str(exc)[:300]}
 
+    ensemble = None
+    if rank == 0 and not args.no_ensemble and args.workload == "bubble":
+        try:
+            ensemble = measure_ensemble(args, cmdg, workloads, torch, barrier, stream, flush)
+        except Exception as exc:  # the ensemble leg must not hide the GPU line
+            ensemble = {"error": str(exc)[:300]}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and args.workload == "bubble":
         try:
@@ -799,6 +839,8 @@ def main():
             "mixed_vs_fp64_rel_l2_rho_rhou_rhoe": rel_vec,
             "mixed_vs_fp64_steps": args.warmup + args.steps,
             "accuracy": accuracy,
+            # the batched mixed ensemble (the --workload ensemble measurement, same steps)
+            "ensemble": ensemble,
             "roofline": {"bound": "hbm", "achieved": ach_mx, "peak": peak, "unit": "GB/s", "frac": ach_mx / peak,
                          "traffic": traffic, "peak_source": peak_kind,
                          "kernel": spec["kernel"], "bytes_per_node_stage": spec["bytes_mixed"]},

@@ -23,7 +23,7 @@ import math
 import numpy as np
 
 from .atmos import EARTH, AtmosModel, DryAdiabaticProfile, DryBiharmonic, HydrostaticState, IsothermalProfile
-from .dgmodel import BrickGrid, CubedShellGrid, DGModel
+from .dgmodel import ArraysGrid, BrickGrid, CubedShellGrid, DGModel, brick_element_order
 
 
 def isentropic_vortex(xyz: np.ndarray, t: float = 0.0, *, p_inf=1e5, T_inf=300.0, translation_speed=150.0,
@@ -100,6 +100,114 @@ def bubble_model(ne=(20, 20, 20), N=4, L=2500.0, precision="fp64", numerical_flu
     model = AtmosModel(orientation="flat", gravity=True,
                        ref_state=HydrostaticState(DryAdiabaticProfile(300.0, 0.0), subtract_off=True))
     return DGModel(model, grid, numerical_flux=numerical_flux, precision=precision)
+
+
+def lgl(N):
+    """Legendre-Gauss-Lobatto nodes and weights on [-1, 1] (N + 1 points):
+    the interior nodes are the roots of P_N', the weights 2 / (N (N+1) P_N^2)."""
+    from numpy.polynomial import legendre as leg
+
+    c = np.zeros(N + 1)
+    c[N] = 1.0
+    x = np.concatenate(([-1.0], np.sort(np.real(leg.legroots(leg.legder(c)))), [1.0]))
+    return x, 2.0 / (N * (N + 1) * leg.legval(x, c) ** 2)
+
+
+def brick_grid_arrays(N, ne, lo, hi, periodicity=(True, True, True), boundary=((1, 2), (1, 2), (1, 2)),
+                      topology="brick"):
+    """The reference's DiscontinuousSpectralElementGrid arrays of an affine
+    brick, as a Julia caller holds them for cmdg_mesh_create_arrays:
+    vgeo (nelem, 16, Np) with the fields of src/Numerics/Mesh/Grids.jl:76-92
+    (dxi_d/dx_j, M = J w_i w_j w_k, MI, MH = w_i w_j J |dxi3/dx|, x1..x3,
+    JcV = |dx/dxi3|), vmap+ (nelem, 6, Nfp; 1-based, the facing node of
+    every face node through the face masks of Grids.jl:559-638, the node
+    itself on a wall) and elemtobndy (nelem, 6), with the elements numbered
+    as the reference's topology numbers them ("brick": BrickTopology's
+    Hilbert order, "stacked_brick", or "library": columns with the vertical
+    index fastest, then x, then y).  Host only (no GPU).
+
+    Returns (vgeo, vmap_plus, elemtobndy, perm) with perm[e] the library
+    (stacked) index of the reference's element e."""
+    N, Nq = int(N), int(N) + 1
+    Np, Nfp = Nq**3, Nq * Nq
+    nx, ny, nz = (int(x) for x in ne)
+    nelem = nx * ny * nz
+    lo = np.asarray(lo, dtype=np.float64)
+    hi = np.asarray(hi, dtype=np.float64)
+    h = (hi - lo) / np.array([nx, ny, nz], dtype=np.float64)
+    perm = (np.arange(nelem, dtype=np.int64) if topology == "library"
+            else brick_element_order((nx, ny, nz), lo, hi, topology))
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(nelem, dtype=np.int64)
+    iz, ix, iy = perm % nz, (perm // nz) % nx, perm // (nz * nx)
+    cell = (ix, iy, iz)
+
+    xi, w = lgl(N)
+    p = np.arange(Np).reshape(Nq, Nq, Nq)  # p[k, j, i] = i + Nq (j + Nq k)
+    # face masks: faces 1/2 (j, k), 3/4 (i, k), 5/6 (i, j), first index fastest
+    fmask = [p[:, :, 0].ravel(), p[:, :, N].ravel(), p[:, 0, :].ravel(), p[:, N, :].ravel(),
+             p[0, :, :].ravel(), p[N, :, :].ravel()]
+    ii, jj, kk = (p % Nq), (p // Nq) % Nq, p // Nfp
+    ii, jj, kk = ii.ravel(), jj.ravel(), kk.ravel()
+
+    vgeo = np.zeros((nelem, 16, Np), dtype=np.float64)
+    for d in range(3):
+        vgeo[:, 4 * d, :] = 2.0 / h[d]
+    J = h[0] * h[1] * h[2] / 8.0
+    M = J * w[ii] * w[jj] * w[kk]
+    vgeo[:, 9, :] = M
+    vgeo[:, 10, :] = 1.0 / M
+    vgeo[:, 11, :] = w[ii] * w[jj] * h[0] * h[1] / 4.0
+    for d, (a, r) in enumerate(zip(cell, (ii, jj, kk))):
+        vgeo[:, 12 + d, :] = lo[d] + h[d] * (a[:, None] + (xi[r][None, :] + 1.0) / 2.0)
+    vgeo[:, 15, :] = h[2] / 2.0
+
+    vmap = np.empty((nelem, 6, Nfp), dtype=np.int64)
+    bndy = np.zeros((nelem, 6), dtype=np.int64)
+    own = np.arange(nelem, dtype=np.int64)
+    for f in range(6):
+        d, side = f // 2, f % 2
+        nb = [c.copy() for c in cell]
+        nb[d] = cell[d] + (1 if side else -1)
+        n_d = (nx, ny, nz)[d]
+        if periodicity[d]:
+            nb[d] %= n_d
+            wall = np.zeros(nelem, dtype=bool)
+        else:
+            wall = (nb[d] < 0) | (nb[d] >= n_d)
+            nb[d] = np.clip(nb[d], 0, n_d - 1)
+        nb_ref = inv[nb[2] + nz * (nb[0] + nx * nb[1])]
+        across = Np * nb_ref[:, None] + fmask[f ^ 1][None, :] + 1
+        itself = Np * own[:, None] + fmask[f][None, :] + 1
+        vmap[:, f, :] = np.where(wall[:, None], itself, across)
+        bndy[:, f] = np.where(wall, int(boundary[d][side]), 0)
+    return vgeo, vmap, bndy, perm
+
+
+def bubble_arrays_model(ne=(20, 20, 20), N=4, L=2500.0, precision="fp64", topology="brick"):
+    """The rising-bubble configuration of bubble_model run through the grid
+    arrays a Julia caller passes (cmdg_mesh_create_arrays +
+    cmdg_model_set_reference): the brick's arrays in the reference
+    topology's element order, Phi = g z, grad Phi = (0, 0, g), and the
+    reference state of the library's own hydrostatic solve on the same
+    brick, permuted into that order.  Returns (model, perm, xyz) with xyz
+    the node coordinates in the reference's order."""
+    per, bnd = (True, True, False), ((0, 0), (0, 0), (1, 2))
+    vgeo, vmap, bndy, perm = brick_grid_arrays(N, ne, (0.0, 0.0, 0.0), (L, L, L), per, bnd, topology)
+    model = AtmosModel(orientation="flat", gravity=True,
+                       ref_state=HydrostaticState(DryAdiabaticProfile(300.0, 0.0), subtract_off=True))
+    lib = DGModel(model, BrickGrid(N, ne, (0.0, 0.0, 0.0), (L, L, L), periodicity=per, boundary=bnd))
+    ref = lib.reference_state()[perm]
+    del lib
+    g = model.constants["grav"]
+    xyz = np.ascontiguousarray(vgeo[:, 12:15, :])
+    aux7 = np.zeros((vgeo.shape[0], 7, vgeo.shape[2]), dtype=np.float64)
+    aux7[:, 0] = g * xyz[:, 2]
+    aux7[:, 3] = g
+    aux7[:, 4:7] = ref
+    dg = DGModel(model, ArraysGrid(N, vgeo, vmap, bndy), precision=precision)
+    dg.set_reference(aux7)
+    return dg, perm, xyz
 
 
 def hyper_bubble_model(ne=(20, 20, 20), N=4, L=2500.0, precision="fp64", tau=3600.0):
