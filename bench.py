@@ -10,7 +10,11 @@ LSRK54 step (5 fused tendency + stage kernels over the whole mesh).
 value      mixed FP32/FP64 path (FP32 perturbation state, FP64 RK register),
            whole-job DOF-stage/s over all ranks, state resident in HBM; L2 is
            flushed (256 MiB write) between timed steps and each step is timed
-           with CUDA events on the launching stream.
+           with CUDA events on the launching stream.  After W warm-up steps a
+           leg times R regions of exactly K steps, each restarting from the
+           initial state outside the region, R chosen so that the regions
+           cover about a second (the clock samples then see the load); the
+           median region gives ms_per_step.
 fp64       the plain FP64 path, measured the same way.
 e2e        the same metric through the C ABI with the FP64 state in pinned
            host memory (cmdg_lsrk54_step_mixed_host): each step reads the
@@ -89,6 +93,8 @@ NSTAGE = 5
 NFIELD = 5
 BYTES_MIXED = 2 * 5 * 4 + 2 * 5 * 8   # per node-stage
 BYTES_FP64 = 2 * 5 * 8 + 2 * 5 * 8
+MIN_TIMED_S = 1.0    # each timed leg repeats its K-step region to cover about this much time
+MAX_REPEATS = 400
 WORKLOAD = ("rising bubble: 20x20x20 elements, N=4 (1e6 nodes, 5e6 DOF), [0,2500 m]^3, periodic x/y, "
             "FreeSlip walls z, dry Euler + gravity, HydrostaticState(DryAdiabatic 300 K), +2 K cos^2 bubble "
             "r=250 m at z=350 m, Rusanov, LSRK54 at CFL 0.4")
@@ -279,8 +285,10 @@ def bench_les16(args, cmdg, workloads, torch, barrier, stream, flush):
 
 def bench_hevi(args, cmdg, workloads, torch, barrier, stream, flush):
     """ARK2 + column-LU (HEVI) steps of the acoustic wave on the sphere: the
-    explicit tendency on the FP32 perturbation of a mixed model (value) and
-    in FP64 (fp64), the stage algebra and the column solve FP64 in both;
+    explicit tendency of a mixed model (value: the fused remainder f - l of
+    the vertical linear model on the FP32 perturbation plus the FP64 linear
+    tendency) and in FP64 (fp64), the stage algebra and the column solve FP64
+    in both;
     beside it the explicit LSRK54 path of the same mixed model at its own
     Courant time step, as simulated seconds per wall-clock second."""
     import numpy as np
@@ -414,7 +422,8 @@ def bench_hevi(args, cmdg, workloads, torch, barrier, stream, flush):
             "config": {"workload": "acoustic wave on the sphere (acousticwave_1d_imex.jl): cubed shell 6x10x10x5, "
                                    "N=5 (648,000 nodes), 10 km lid, isothermal 300 K, HEVI "
                                    "ARK2GiraldoKellyConstantinescu, dt = 100 s, ManyColumnLU",
-                       "path": "explicit tendency on the FP32 perturbation; ARK algebra, linear operator and "
+                       "path": "explicit tendency: the fused remainder f - l on the FP32 perturbation plus the "
+                               "FP64 linear tendency of the FP64 perturbation; ARK algebra, linear operator and "
                                "column LU FP64",
                        "dt": dt, "stages_per_step": 3, "column_lines": ark.nline, "band_half_width": ark.bandwidth,
                        "l2": "256 MiB buffer written between timed steps"},
@@ -716,21 +725,49 @@ def main():
         Q0 = workloads.rising_bubble(xyz, theta0=300.0, amp=2.0, rc=250.0, center=(1250.0, 1250.0, 350.0))
         return dg, Q0
 
+    def n_repeats(step_ms):
+        """How many times a leg repeats its timed region of exactly K steps so
+        that the clock samples cover about MIN_TIMED_S of load (the same
+        count on every rank)."""
+        r = max(1, min(MAX_REPEATS, math.ceil(MIN_TIMED_S * 1e3 / max(step_ms * args.steps, 1e-3))))
+        if dist is not None:
+            t = torch.tensor([r], dtype=torch.int64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            r = int(t.item())
+        return r
+
     def timed_run(dg, Q0, dt):
+        """W warm-up steps, then R timed regions of exactly K steps, each
+        starting from the initial state (copied in outside the timed region);
+        returns the state after the last region (K steps from the initial
+        state), the median region time, every step's time and R."""
         Q = dg.init_ode_state(Q0)
+        Qinit = Q.clone()
         lsrk = cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt)
-        for _ in range(args.warmup):
+        w0, w1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for i in range(max(args.warmup, 1)):
+            if i == max(args.warmup, 1) - 1:
+                w0.record(stream)
             cmdg.dostep_(Q, lsrk, None, 0.0)
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        barrier()
-        for i in range(args.steps):
-            flush.fill_(i & 0xFF)
-            ev[i][0].record(stream)
-            cmdg.dostep_(Q, lsrk, None, 0.0)
-            ev[i][1].record(stream)
-        barrier()
-        ms = [a.elapsed_time(b) for a, b in ev]
-        return Q, sum(ms), ms
+        w1.record(stream)
+        torch.cuda.synchronize()
+        reps = n_repeats(w0.elapsed_time(w1))
+        region_ms, per = [], []
+        for r in range(reps):
+            Q.copy_(Qinit)
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(args.steps)]
+            barrier()
+            for i in range(args.steps):
+                flush.fill_(i & 0xFF)
+                ev[i][0].record(stream)
+                cmdg.dostep_(Q, lsrk, None, 0.0)
+                ev[i][1].record(stream)
+            barrier()
+            ms = [a.elapsed_time(b) for a, b in ev]
+            region_ms.append(sum(ms))
+            per.extend(ms)
+        return Q, statistics.median(region_ms), per, reps
 
     dg64, Q0 = build("fp64")
     dgmx, _ = build("mixed")
@@ -741,10 +778,10 @@ def main():
     nodes = dg64.grid.nelem * dg64.grid.Np
 
     clk = ClockSampler(local_rank).__enter__()  # sampled across the three timed legs
-    Qmx, ms_mx, per_mx = timed_run(dgmx, Q0, dt)
-    Q64, ms_64, per_64 = timed_run(dg64, Q0, dt)
+    Qmx, ms_mx, per_mx, reps_mx = timed_run(dgmx, Q0, dt)
+    Q64, ms_64, per_64, reps_64 = timed_run(dg64, Q0, dt)
 
-    # accuracy of the mixed path against the FP64 path after warmup+steps
+    # accuracy of the mixed path against the FP64 path after the last timed region's K steps
     a = dgmx.from_perturbation(Qmx).cpu().numpy()
     b = Q64.cpu().numpy()
     M = dg64.grid.mass()
@@ -763,16 +800,26 @@ def main():
     def e2e_step():
         dgmx.lsrk54_step_host(host, Qp, dQ, 0.0, dt, 1)
 
-    for _ in range(2):
-        e2e_step()
-    barrier()
+    host0 = host.clone()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
+    for i in range(2):
+        if i == 1:
+            e0.record(stream)
         e2e_step()
     e1.record(stream)
-    barrier()
-    ms_e2e = e0.elapsed_time(e1)
+    torch.cuda.synchronize()
+    reps_e2e = n_repeats(e0.elapsed_time(e1))
+    e2e_ms = []
+    for r in range(reps_e2e):
+        host.copy_(host0)
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e1.record(stream)
+        barrier()
+        e2e_ms.append(e0.elapsed_time(e1))
+    ms_e2e = statistics.median(e2e_ms)
     clk.__exit__(None, None, None)
 
     # max over ranks
@@ -837,7 +884,10 @@ def main():
             "mixed_step_ms": {"min": min(per_mx), "median": statistics.median(per_mx), "max": max(per_mx)},
             "mixed_vs_fp64_rel_l2": rel,
             "mixed_vs_fp64_rel_l2_rho_rhou_rhoe": rel_vec,
-            "mixed_vs_fp64_steps": args.warmup + args.steps,
+            "mixed_vs_fp64_steps": args.steps,
+            # each leg times R regions of exactly K steps (restarting from the
+            # initial state) and reports the median region
+            "timed_regions": {"mixed": reps_mx, "fp64": reps_64, "e2e": reps_e2e},
             "accuracy": accuracy,
             # the batched mixed ensemble (the --workload ensemble measurement, same steps)
             "ensemble": ensemble,

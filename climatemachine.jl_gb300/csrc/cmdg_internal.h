@@ -252,10 +252,14 @@ struct LaunchArgs {
     int mode;                // 0 = tendency, 1 = RK stage
     int first_stage = 0;     // stage 1: the register is not read (A_1 = 0)
     int last_stage = 0;      // stage 5: the register is not written
+    int remainder = 0;       // tendency mode on a mixed cubed shell: f - l of the vertical linear model
 };
 int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
 // curvilinear stage kernel (shell.cu)
 int launch_shell_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
+// whether launch_shell_stage can form the remainder f - l of the vertical
+// acoustic-gravity linear model (mixed, inviscid, subtracted reference state)
+bool shell_remainder_supported(const Model* md);
 // grid-arrays stage kernel (arrays.cu)
 int launch_arrays_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
 // LSRK54CarpenterKennedy A and B coefficient arrays (5 entries each)
@@ -291,7 +295,9 @@ int visc_reference_gradients(Model* md);
 int launch_shell_visc_gradient(Model* md, const void* Qin, void* gout, cudaStream_t s);
 
 // reductions / conversions (reduce.cu)
-int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s);
+// Qp = FP32 perturbation of Q about the reference state; Qd, if given, the
+// FP64 perturbation
+int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s, double* Qd = nullptr);
 int launch_from_perturbation(Model* md, double* Q, const float* Qp, cudaStream_t s);
 int weighted_sums(Model* md, const void* Q, bool mixed, int nfields, const int* fields, double* out, cudaStream_t s);
 int courant_dt(Model* md, const double* Q, double CFL, double* dt, cudaStream_t s);

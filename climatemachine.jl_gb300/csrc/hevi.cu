@@ -622,6 +622,8 @@ struct Hevi {
     double* d_AB1 = nullptr;
     double* d_buf = nullptr;  // S1, S2, R0, R1, R2, Qhat, Y
     float* d_Sp = nullptr;    // mixed models: FP32 perturbation of the stage state
+    int rem = 0;              // mixed cubed shell: explicit part from the fused remainder f - l
+    double* d_lref = nullptr; // rem with split: l(q_ref), the linear tendency of the reference state
     unsigned* d_err = nullptr;
     double* S(int i) const { return d_buf + (size_t)(i - 1) * len; }          // i = 1, 2
     double* R(int i) const { return d_buf + (size_t)(2 + i) * len; }          // i = 0..2
@@ -689,11 +691,36 @@ int hevi_solve(Hevi* h, const double* b, double* out, int accumulate, cudaStream
     }
 }
 
+__global__ void axpy_kernel(double* __restrict__ y, double a, const double* __restrict__ x, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        y[i] = fma(a, x[i], y[i]);
+}
+
+unsigned elementwise_grid(size_t len);
+
 // rhs!: the full tendency, or the remainder f - l when split.  A mixed
 // model evaluates the explicit tendency on the FP32 perturbation of the FP64
-// stage state (FP64 output); the ARK algebra and the solve stay FP64.
+// stage state (FP64 output); the ARK algebra and the solve stay FP64.  On a
+// cubed shell the mixed tendency is split further: the fused remainder
+// kernel forms f - l on the FP32 perturbation q' (the stiff vertical
+// acoustic terms cancel before rounding) and the linear kernel adds l of the
+// FP64 perturbation Q - q_ref, so f = (f - l)(q') + l(Q - q_ref); when the
+// step is split, f - l(Q) = (f - l)(q') - l(q_ref), l(q_ref) formed once.
 int hevi_rhs(Hevi* h, double* R, const double* Q, cudaStream_t s) {
     int rc;
+    if (h->rem) {
+        double* Qd = h->Y();  // free between the solve and the next stage
+        rc = launch_to_perturbation(h->md, h->d_Sp, Q, s, Qd);
+        if (rc) return rc;
+        LaunchArgs a{h->d_Sp, nullptr, R, 1.0, 0.0, 0.0, 0.0, 0, 0, 0};
+        a.remainder = 1;
+        rc = launch_stage(h->md, a, s);
+        if (rc) return rc;
+        if (!h->split) return launch_linear_tendency(h->md, Qd, R, 1.0, 1.0, s);
+        axpy_kernel<<<elementwise_grid(h->len), 256, 0, s>>>(R, -1.0, h->d_lref, h->len);
+        CMDG_CUDA_CHECK(cudaGetLastError());
+        return CMDG_OK;
+    }
     if (h->md->precision == CMDG_MIXED) {
         rc = launch_to_perturbation(h->md, h->d_Sp, Q, s);
         if (rc) return rc;
@@ -844,6 +871,27 @@ int cmdg_hevi_create(cmdg_model* model, double dt, int split_explicit_implicit, 
         set_error("HEVI: SingleColumnLU needs identical column matrices (use ManyColumnLU on this mesh)");
         rc = CMDG_ERR_ARG;
     }
+    if (!rc && shell_remainder_supported(md)) {
+        h->rem = 1;
+        if (h->split) {
+            // l(q_ref): the reference state as a full state (zero perturbation)
+            if (cudaMalloc(&h->d_lref, sizeof(double) * h->len) != cudaSuccess) {
+                cudaGetLastError();
+                set_error("HEVI: device allocation of %zu bytes failed", sizeof(double) * h->len);
+                rc = CMDG_ERR_ALLOC;
+            }
+            if (!rc && cudaMemsetAsync(h->d_Sp, 0, sizeof(float) * h->len, s) != cudaSuccess) {
+                set_error("HEVI: cudaMemsetAsync failed");
+                rc = CMDG_ERR_CUDA;
+            }
+            if (!rc) rc = launch_from_perturbation(md, h->Y(), h->d_Sp, s);
+            if (!rc) rc = launch_linear_tendency(md, h->Y(), h->d_lref, 1.0, 0.0, s);
+            if (!rc && cudaStreamSynchronize(s) != cudaSuccess) {
+                set_error("HEVI: forming the reference state's linear tendency failed");
+                rc = CMDG_ERR_CUDA;
+            }
+        }
+    }
     if (rc) {
         cmdg_hevi_destroy(ho);
         return rc;
@@ -862,6 +910,7 @@ int cmdg_hevi_destroy(cmdg_hevi* hevi) {
     cudaFree(hevi->h.d_AB1);
     cudaFree(hevi->h.d_buf);
     cudaFree(hevi->h.d_Sp);
+    cudaFree(hevi->h.d_lref);
     cudaFree(hevi->h.d_err);
     delete hevi;
     return CMDG_OK;

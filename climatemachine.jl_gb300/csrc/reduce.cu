@@ -34,8 +34,9 @@ __device__ __forceinline__ double ref_value(const double* lvl, const double* ref
 // thread issues its five loads before converting, and no index needs a
 // division.  Q may be page-locked host memory mapped into the device's
 // address space: the kernel then reads it over the host link.
-__global__ void to_perturbation_kernel(float* __restrict__ Qp, const double* __restrict__ Q, const double* lvl,
-                                       const double* refn, int64_t nelem, int Np, int Nq, int nz) {
+// Qp = FP32 perturbation Q - q_ref; Qd (if not NULL) = the FP64 perturbation
+__global__ void to_perturbation_kernel(float* __restrict__ Qp, double* __restrict__ Qd, const double* __restrict__ Q,
+                                       const double* lvl, const double* refn, int64_t nelem, int Np, int Nq, int nz) {
     for (int64_t e = blockIdx.x; e < nelem; e += gridDim.x)
         for (int node = threadIdx.x; node < Np; node += blockDim.x) {
             const size_t base = (size_t)e * NSTATE * Np + node;
@@ -43,8 +44,11 @@ __global__ void to_perturbation_kernel(float* __restrict__ Qp, const double* __r
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) v[s] = Q[base + (size_t)s * Np];
 #pragma unroll
-            for (int s = 0; s < NSTATE; ++s)
-                Qp[base + (size_t)s * Np] = (float)(v[s] - ref_value(lvl, refn, e, node, s, Np, nz, Nq));
+            for (int s = 0; s < NSTATE; ++s) {
+                const double d = v[s] - ref_value(lvl, refn, e, node, s, Np, nz, Nq);
+                Qp[base + (size_t)s * Np] = (float)d;
+                if (Qd) Qd[base + (size_t)s * Np] = d;
+            }
         }
 }
 
@@ -222,10 +226,10 @@ void release_quad(const Model* md) {
     g_quad.erase(it);
 }
 
-int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s) {
+int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s, double* Qd) {
     const Mesh& m = *md->mesh;
     const unsigned grid = (unsigned)std::min<int64_t>(m.nelem, CONVERT_CTAS);
-    to_perturbation_kernel<<<grid, 128, 0, s>>>(Qp, Q, md->d_lvl64, md->d_ref64, m.nelem, m.Np, m.Nq, m.nz);
+    to_perturbation_kernel<<<grid, 128, 0, s>>>(Qp, Qd, Q, md->d_lvl64, md->d_ref64, m.nelem, m.Np, m.Nq, m.nz);
     CMDG_CUDA_CHECK(cudaGetLastError());
     return CMDG_OK;
 }

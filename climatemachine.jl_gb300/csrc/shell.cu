@@ -65,10 +65,26 @@ struct ShellSmem {
 // TurbulenceClosures.jl:199-225, 368-404) join the volume flux and, with
 // the neighbour's state, the central second-order interface flux; walls
 // carry the first-order flux only.
-template <int N, typename R, bool MIXED, int MODE, bool HYPER, int VT>
+//
+// REM (mixed, tendency mode, inviscid, subtract_off): the remainder f - l of
+// the vertical AtmosAcousticGravityLinearModel evaluated on the FP32
+// perturbation q' (src/Atmos/Model/linear.jl:103-190, the
+// remainder_DGModel of src/Numerics/DGMethods/remainder.jl).  The linear
+// model's terms cancel before rounding: in xi3 the volume flux is
+// J dxi3/dx . (F - F_L) with F - F_L = (0, rho u u - (R/cv) ke I,
+// rho u ((rhoe' + p') rho_ref - h_ref rho') / (rho rho_ref)) -- p' - p_L' =
+// -(R/cv) ke exactly, h_ref = rhoe_ref + p_ref -- the gravity sources cancel,
+// and the faces normal to xi3 carry the central flux of F - F_L with the
+// penalty (lambda - c_L)/2 on the perturbation jump plus lambda/2 on the
+// reference jump (c_L: the larger reference sound speed, the linear model's
+// Rusanov speed).  The stiff vertical acoustic terms are then applied in
+// FP64 by the linear kernel, so FP32 rounding no longer enters them.
+template <int N, typename R, bool MIXED, int MODE, bool HYPER, int VT, bool REM = false>
 __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER || VT != 0 ? 4 : ShellDims<N>::MIN_CTAS)
                                                           : ShellDims<N>::MIN_CTAS64)
     shell_stage_kernel(const KParams P) {
+    static_assert(!REM || (MIXED && MODE == 0 && !HYPER && VT == CMDG_TURB_NONE),
+                  "the remainder form is a mixed inviscid tendency");
     constexpr bool VISC = VT != CMDG_TURB_NONE;
     using Dm = ShellDims<N>;
     using SM = ShellSmem<N, R>;
@@ -172,14 +188,37 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER || VT != 0 ? 
                 F2[s2] += Fv[2][s2];
             }
         }
+        if (REM) {
+            // xi1, xi2: the full flux; xi3: the rows of F - F_L
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
+            for (int d = 0; d < 2; ++d) {
+                R Ft[NSTATE];
+#pragma unroll
+                for (int s = 0; s < NSTATE; ++s)
+                    Ft[s] = Jx[d * 3 + 0] * F0[s] + Jx[d * 3 + 1] * F1[s] + Jx[d * 3 + 2] * F2[s];
+                PL::st(s_F + d * SM::P5N, Np, t, Ft);
+            }
+            const R pke = KConst<R>::gm1(P) * R(0.5) * (q[1] * th.u[0] + q[2] * th.u[1] + q[3] * th.u[2]);
+            const R hrem = ((q[4] + th.pflux) * lv.rho_ref - lv.href * q[0]) * th.rinv * rcp_r(lv.rho_ref);
             R Ft[NSTATE];
+            Ft[0] = 0;
 #pragma unroll
-            for (int s = 0; s < NSTATE; ++s) Ft[s] = Jx[d * 3 + 0] * F0[s] + Jx[d * 3 + 1] * F1[s] + Jx[d * 3 + 2] * F2[s];
-            PL::st(s_F + d * SM::P5N, Np, t, Ft);
+            for (int c = 0; c < 3; ++c)
+                Ft[1 + c] = Jx[6] * (q[1] * th.u[c]) + Jx[7] * (q[2] * th.u[c]) + Jx[8] * (q[3] * th.u[c]) -
+                            Jx[6 + c] * pke;
+            Ft[4] = (Jx[6] * q[1] + Jx[7] * q[2] + Jx[8] * q[3]) * hrem;
+            PL::st(s_F + 2 * SM::P5N, Np, t, Ft);
+        } else {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                R Ft[NSTATE];
+#pragma unroll
+                for (int s = 0; s < NSTATE; ++s)
+                    Ft[s] = Jx[d * 3 + 0] * F0[s] + Jx[d * 3 + 1] * F1[s] + Jx[d * 3 + 2] * F2[s];
+                PL::st(s_F + d * SM::P5N, Np, t, Ft);
+            }
         }
-        if (ph.gravity) {
+        if (ph.gravity && !REM) {
             const R rho_s = MIXED ? ((ph.ref_state && ph.subtract_off) ? q[0] : lv.rho_ref + q[0])
                                   : ((ph.ref_state && ph.subtract_off) ? q[0] - lv.rho_ref : q[0]);
 #pragma unroll
@@ -268,6 +307,20 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER || VT != 0 ? 
 #pragma unroll
         for (int c = 0; c < 3; ++c) Fp[1 + c] = mn_p * thp.u[c] + thp.pflux * nv[c];
         Fp[4] = un_p * thp.H;
+        R cL = 0;  // REM, faces normal to xi3: the linear model's Rusanov speed
+        if (REM && fd == 2) {
+            // F - F_L of the node across the face (or of the reflected state on a wall)
+            const R pke_p = KConst<R>::gm1(P) * R(0.5) * (qp[1] * thp.u[0] + qp[2] * thp.u[1] + qp[3] * thp.u[2]);
+            const R hrem_p =
+                ((qp[4] + thp.pflux) * lvp.rho_ref - lvp.href * qp[0]) * thp.rinv * rcp_r(lvp.rho_ref);
+            Fp[0] = 0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) Fp[1 + c] = mn_p * thp.u[c] - pke_p * nv[c];
+            Fp[4] = mn_p * hrem_p;
+            const Level<R> lvm = shell_level<R, MIXED>(P, ge, Np, vM, ez * Nq + kM);
+            const R gam = KConst<R>::gamma(P);
+            cL = fmax(sqrt_r(gam * lvm.p_ref * rcp_r(lvm.rho_ref)), sqrt_r(gam * lvp.p_ref * rcp_r(lvp.rho_ref)));
+        }
         if (HYPER && nb >= 0) {
             // neighbour's hyperdiffusive flux . n
             const R* hn = static_cast<const R*>(P.hd) + (size_t)nb * 12 * Np + vP;
@@ -291,9 +344,11 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER || VT != 0 ? 
         const R lift = sJ * iJm * KConst<R>::inv_w0(P);
         const R hmw = (ph.numflux == CMDG_FLUX_RUSANOV) ? R(0.5) * fmax(lam_m, lam_p) : R(0);
         const R hl = R(0.5) * lift, pl = hmw * lift;
+        // REM: the linear model's penalty cL/2 on the perturbation jump comes off
+        const R pq = (REM && fd == 2) ? (hmw - R(0.5) * cL) * lift : pl;
         R fs[NSTATE];
 #pragma unroll
-        for (int s = 0; s < NSTATE; ++s) fs[s] = hl * (Fm[s] + Fp[s]) + pl * ((qm[s] - qp[s]) + jr[s]);
+        for (int s = 0; s < NSTATE; ++s) fs[s] = hl * (Fm[s] + Fp[s]) + (pq * (qm[s] - qp[s]) + pl * jr[s]);
         PL::st(s_fs, NFN, f * Nfp + fn, fs);
     }
     __syncthreads();
@@ -361,7 +416,7 @@ __global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER || VT != 0 ? 
     if (__any_sync(0xffffffffu, bad) && (t & 31) == 0) atomicOr(P.status, 1u);
 }
 
-template <int N, typename R, bool MIXED, int MODE, bool HYPER, int VT>
+template <int N, typename R, bool MIXED, int MODE, bool HYPER, int VT, bool REM = false>
 cudaError_t launch_shell_typed(const KParams& P, cudaStream_t s) {
     constexpr size_t bytes = ShellSmem<N, R>::BYTES;
     static unsigned long long configured = 0;
@@ -369,12 +424,12 @@ cudaError_t launch_shell_typed(const KParams& P, cudaStream_t s) {
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (!(configured & (1ull << (dev & 63)))) {
-        e = cudaFuncSetAttribute(shell_stage_kernel<N, R, MIXED, MODE, HYPER, VT>,
+        e = cudaFuncSetAttribute(shell_stage_kernel<N, R, MIXED, MODE, HYPER, VT, REM>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
         if (e != cudaSuccess) return e;
         configured |= 1ull << (dev & 63);
     }
-    shell_stage_kernel<N, R, MIXED, MODE, HYPER, VT><<<(unsigned)P.nelem, ShellDims<N>::NT, bytes, s>>>(P);
+    shell_stage_kernel<N, R, MIXED, MODE, HYPER, VT, REM><<<(unsigned)P.nelem, ShellDims<N>::NT, bytes, s>>>(P);
     return cudaGetLastError();
 }
 
@@ -398,10 +453,39 @@ cudaError_t launch_shell_N(const KParams& P, bool mixed, int mode, bool hyper, i
 
 }  // namespace
 
+bool shell_remainder_supported(const Model* md) {
+    return md->mesh->kind == MESH_SHELL && md->precision == CMDG_MIXED && md->prm.ref_state &&
+           md->prm.subtract_off && md->prm.gravity && md->prm.hyperdiffusion == CMDG_HYPER_NONE &&
+           md->prm.turbulence == CMDG_TURB_NONE && md->mms_src == nullptr;
+}
+
 int launch_shell_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
     const Mesh& m = *md->mesh;
     const bool hyper = md->prm.hyperdiffusion != CMDG_HYPER_NONE;
     const bool visc = md->prm.turbulence != CMDG_TURB_NONE;
+    if (a.remainder) {
+        if (!shell_remainder_supported(md) || a.mode != 0) {
+            set_error("the remainder tendency is built for mixed inviscid cubed-shell models with a subtracted "
+                      "hydrostatic reference state");
+            return CMDG_ERR_UNSUPPORTED;
+        }
+        const KParams P = make_params(md, a);
+        cudaError_t err;
+        switch (m.N) {
+            case 2: err = launch_shell_typed<2, float, true, 0, false, CMDG_TURB_NONE, true>(P, s); break;
+            case 3: err = launch_shell_typed<3, float, true, 0, false, CMDG_TURB_NONE, true>(P, s); break;
+            case 4: err = launch_shell_typed<4, float, true, 0, false, CMDG_TURB_NONE, true>(P, s); break;
+            case 5: err = launch_shell_typed<5, float, true, 0, false, CMDG_TURB_NONE, true>(P, s); break;
+            default:
+                set_error("no cubed-shell stage kernel for N=%d", m.N);
+                return CMDG_ERR_ARG;
+        }
+        if (err != cudaSuccess) {
+            set_error("cubed-shell remainder kernel launch failed: %s", cudaGetErrorString(err));
+            return CMDG_ERR_CUDA;
+        }
+        return CMDG_OK;
+    }
     if (hyper) {
         const int rc = launch_shell_hyper_passes(md, a.Qin, md->d_hd, s);
         if (rc) return rc;
