@@ -649,6 +649,9 @@ def main():
                     choices=["bubble", "bubble-arrays", "gcm", "les", "les16", "hyper", "ensemble", "hevi"])
     ap.add_argument("--no-ensemble", action="store_true",
                     help="skip the batched-ensemble measurement the bubble line carries")
+    ap.add_argument("--min-timed-s", type=float, default=MIN_TIMED_S,
+                    help="each timed leg repeats its K-step region until it covers about this many seconds "
+                         "(0: one region, as for a profiler run)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -729,7 +732,7 @@ def main():
         """How many times a leg repeats its timed region of exactly K steps so
         that the clock samples cover about MIN_TIMED_S of load (the same
         count on every rank)."""
-        r = max(1, min(MAX_REPEATS, math.ceil(MIN_TIMED_S * 1e3 / max(step_ms * args.steps, 1e-3))))
+        r = max(1, min(MAX_REPEATS, math.ceil(args.min_timed_s * 1e3 / max(step_ms * args.steps, 1e-3))))
         if dist is not None:
             t = torch.tensor([r], dtype=torch.int64, device="cuda")
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
