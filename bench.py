@@ -532,16 +532,41 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def run_cpu_reference(steps, threads=None, sample_steps=None, warmup=1, max_sec=None):
+def cpu_reference_case(O, workload):
+    """The oracle's model and FP64 initial state of a bench workload (the
+    same configuration and seeded state as the GPU legs)."""
+    import numpy as np
+
+    bubble = dict(periodic=(1, 1, 0), orientation="flat", gravity=True, ref_state=True, profile="dry_adiabatic",
+                  T_surface=300.0, T_min=0.0)
+    if workload in ("bubble", "bubble-arrays", "hyper"):
+        extra = dict(hyperdiffusion="dry_biharmonic", tau_hyper=3600.0) if workload == "hyper" else {}
+        om = O.OracleModel(N, NE, (0, 0, 0), (L, L, L), **bubble, **extra)
+        return om, om.init_bubble(theta0=300.0, amp=2.0, rc=250.0, xc=1250.0, yc=1250.0, zc=350.0)
+    from cmdg import workloads
+
+    if workload == "gcm":
+        R = O.EARTH["planet_radius"]
+        om = O.OracleModel(N, shell=dict(nhorz=12, nvert=6, r_inner=R, r_outer=R + 30e3), orientation="sphere",
+                           gravity=True, ref_state=True, profile="isothermal", T_surface=285.0)
+        return om, workloads.gcm_initial_state(np.ascontiguousarray(om.aux[:, 0:3]))
+    if workload == "les":
+        om = O.OracleModel(N, (32, 32, 16), (0, 0, 0), (3200.0, 3200.0, 1600.0), **bubble, turbulence="smagorinsky")
+        return om, workloads.les_initial_state(np.ascontiguousarray(om.aux[:, 0:3]))
+    raise ValueError(f"no CPU reference case for workload {workload!r}")
+
+
+def run_cpu_reference(steps, threads=None, sample_steps=None, warmup=1, max_sec=None, workload="bubble"):
     """Times the oracle (CPU restatement of the reference) on the workload."""
+    import numpy as np
+
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
 
     threads = threads or os.cpu_count()
     O.set_threads(threads)
-    om = O.OracleModel(N, NE, (0, 0, 0), (L, L, L), periodic=(1, 1, 0), orientation="flat", gravity=True,
-                       ref_state=True, profile="dry_adiabatic", T_surface=300.0, T_min=0.0)
-    Q = om.init_bubble(theta0=300.0, amp=2.0, rc=250.0, xc=1250.0, yc=1250.0, zc=350.0)
+    om, Q = cpu_reference_case(O, workload)
+    Q = np.ascontiguousarray(Q)
     dt = om.courant_dt(Q, CFL)
     dQ = om.state()
     w0 = time.perf_counter()
@@ -860,11 +885,12 @@ def main():
             ensemble = {"error": str(exc)[:300]}
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline and args.workload == "bubble":
+    if rank == 0 and not args.no_cpu_baseline:
         try:
-            r = run_cpu_reference(1, sample_steps=2)
+            r = run_cpu_reference(1, sample_steps=2, max_sec=60.0, workload=args.workload)
             cpu = {"value": r["value"], "unit": "DOF-stage/s", "cores": r["threads"], "kind": "port",
-                   "sample": f"{r['steps']} LSRK54 steps of the full 1e6-node workload, FP64 oracle"}
+                   "sample": f"{r['steps']} LSRK54 steps (after {r['warmup']} warm-up) of the full "
+                             f"{nodes:,}-node workload, FP64 oracle"}
         except Exception as exc:  # the CPU leg must not hide the GPU line
             cpu = {"value": None, "error": str(exc)[:200]}
 
@@ -872,6 +898,7 @@ def main():
         line = {
             "metric": "DOF-stage updates/s", "value": value, "unit": "DOF-stage/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mx / args.steps,
+            "node_stage_per_s": value / NFIELD,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic",
             "config": {"workload": spec["desc"], "l2": L2_NOTE, "parallelism": f"replicas x{world}"},
@@ -882,7 +909,10 @@ def main():
                                   "frac": ach_64 / peak},
                      # the plain path is bound by the FP64 pipe (ncu capture of its stage kernel)
                      "fp64_pipe_frac": (profile_value("stage_kernel_fp64_bubble20.md", "fp64_pipe_frac")
-                                        if args.workload == "bubble" else None)},
+                                        if args.workload == "bubble" else None),
+                     "flops_per_node_stage": (profile_value("stage_kernel_fp64_bubble20.md",
+                                                            "flops_per_node_stage_fp64")
+                                              if args.workload == "bubble" else None)},
             "mixed_speedup_vs_fp64": value / v64,
             "mixed_step_ms": {"min": min(per_mx), "median": statistics.median(per_mx), "max": max(per_mx)},
             "mixed_vs_fp64_rel_l2": rel,
@@ -896,7 +926,11 @@ def main():
             "ensemble": ensemble,
             "roofline": {"bound": "hbm", "achieved": ach_mx, "peak": peak, "unit": "GB/s", "frac": ach_mx / peak,
                          "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": spec["kernel"], "bytes_per_node_stage": spec["bytes_mixed"]},
+                         "kernel": spec["kernel"], "bytes_per_node_stage": spec["bytes_mixed"],
+                         # ncu FP instruction counts of the same kernel (profile summary)
+                         "flops_per_node_stage": ({"fp32": profile_value(spec["profile"], "flops_per_node_stage_fp32"),
+                                                   "fp64": profile_value(spec["profile"], "flops_per_node_stage_fp64")}
+                                                  if args.workload == "bubble" else None)},
             "cpu_baseline": cpu,
             "e2e": {"value": ve2e, "unit": "DOF-stage/s", "h2d_bytes_per_step": int(host.numel() * 8),
                     "d2h_bytes_per_step": int(host.numel() * 8)},
