@@ -40,7 +40,6 @@ __global__ void __launch_bounds__(VDims<N>::NT) gradient_kernel(const KParams P,
     R* const s_q = reinterpret_cast<R*>(smem_raw);      // planar records: states
     R* const s_G = s_q + planar_pad<R>(5 * Np);            // gradient arguments
     R* const s_dG = s_G + planar_pad<R>(5 * Np);           // face terms
-    R* const s_D = s_dG + planar_pad<R>(5 * NFN);          // strong-form D
 
     const int e = blockIdx.x, t = threadIdx.x;
     const R* __restrict__ Qin = static_cast<const R*>(Qv);
@@ -56,7 +55,6 @@ __global__ void __launch_bounds__(VDims<N>::NT) gradient_kernel(const KParams P,
     const int fa = fn % Nq, fb = fn / Nq;
     const int vM = fd == 0 ? fside * N + Nq * fn : (fd == 1 ? fa + Nq * (fside * N + Nq * fb) : fn + Nfp * (fside * N));
     const int vP = fd == 0 ? oside * N + Nq * fn : (fd == 1 ? fa + Nq * (oside * N + Nq * fb) : fn + Nfp * (oside * N));
-    if (t < Nq * Nq) s_D[t] = VConst<R>::D(P, t);
 
     R q[NSTATE], qp[NSTATE];
     if (node_thread) {
@@ -126,7 +124,9 @@ __global__ void __launch_bounds__(VDims<N>::NT) gradient_kernel(const KParams P,
             PL::ld(s_G, Np, L1 + n, v1);
             PL::ld(s_G, Np, L2 + n * Nq, v2);
             PL::ld(s_G, Np, L3 + n * Nfp, v3);
-            const R d1 = s_D[ni * Nq + n], d2 = s_D[nj * Nq + n], d3 = s_D[nk * Nq + n];
+            // strong-form D from the parameter bank (constant-cache reads)
+            const R d1 = VConst<R>::D(P, ni * Nq + n), d2 = VConst<R>::D(P, nj * Nq + n),
+                    d3 = VConst<R>::D(P, nk * Nq + n);
 #pragma unroll
             for (int g = 0; g < 5; ++g) {
                 g1[g] = fma(d1, v1[g], g1[g]);

@@ -63,9 +63,46 @@ __device__ __forceinline__ VLevel<float> load_vlevel<float>(const KParams& P, in
 __device__ __forceinline__ double pow_r(double x, double y) { return pow(x, y); }
 __device__ __forceinline__ float pow_r(float x, float y) { return powf(x, y); }
 __device__ __forceinline__ double log1p_r(double x) { return log1p(x); }
-__device__ __forceinline__ float log1p_r(float x) { return log1pf(x); }
 __device__ __forceinline__ double expm1_r(double x) { return expm1(x); }
-__device__ __forceinline__ float expm1_r(float x) { return expm1f(x); }
+// FP32 log(1 + x) and exp(y) - 1 for the mixed path's relative
+// perturbations (T'/T_ref, p'/p_ref, and their theta_v combination), which
+// are almost always below 1/32 in magnitude: there the truncated Taylor
+// series (Mercator's series x - x^2/2 + ... - x^6/6; y + y^2/2 + ... +
+// y^5/120) in Horner form, whose first omitted terms are below 2e-10 of
+// the value, far under FP32 rounding; elsewhere the library functions.
+__device__ __forceinline__ float log1p_r(float x) {
+    if (fabsf(x) < 0.03125f) {
+        float h = fmaf(-x, 1.0f / 6.0f, 0.2f);
+        h = fmaf(-x, h, 0.25f);
+        h = fmaf(-x, h, 1.0f / 3.0f);
+        h = fmaf(-x, h, 0.5f);
+        h = fmaf(-x, h, 1.0f);
+        return x * h;
+    }
+    return log1pf(x);
+}
+__device__ __forceinline__ float expm1_r(float y) {
+    if (fabsf(y) < 0.03125f) {
+        float h = fmaf(y, 1.0f / 120.0f, 1.0f / 24.0f);
+        h = fmaf(y, h, 1.0f / 6.0f);
+        h = fmaf(y, h, 0.5f);
+        h = fmaf(y, h, 1.0f);
+        return y * h;
+    }
+    return expm1f(y);
+}
+// weak-form derivative coefficient Dhat[i] from the kernel's parameter bank
+// (a constant-cache read with the thread's row index, no shared memory)
+template <typename R>
+__device__ __forceinline__ R dhat_p(const KParams& P, int i);
+template <>
+__device__ __forceinline__ float dhat_p<float>(const KParams& P, int i) {
+    return P.DhatC32[i];
+}
+template <>
+__device__ __forceinline__ double dhat_p<double>(const KParams& P, int i) {
+    return P.DhatC64[i];
+}
 // spacing to the next representable value above x >= 0 (Julia's eps(x))
 __device__ __forceinline__ double ulp_r(double x) { return __longlong_as_double(__double_as_longlong(x) + 1) - x; }
 __device__ __forceinline__ float ulp_r(float x) { return __int_as_float(__float_as_int(x) + 1) - x; }
@@ -78,7 +115,7 @@ __device__ __forceinline__ void grad_args(const KParams& P, const R q[NSTATE], c
     const Physics& ph = P.ph;
     const R gm1 = KConst<R>::gm1(P);
     const R rho = MIXED ? lv.rho_ref + q[0] : q[0];
-    const R rinv = R(1) / rho;
+    const R rinv = MIXED ? rcp_r(rho) : R(1) / rho;
     G[0] = q[1] * rinv;
     G[1] = q[2] * rinv;
     G[2] = q[3] * rinv;
@@ -87,10 +124,11 @@ __device__ __forceinline__ void grad_args(const KParams& P, const R q[NSTATE], c
     if (MIXED && ph.ref_state) {
         const R pp = gm1 * (q[4] - R(0.5) * ke2) + q[0] * lv.crho;  // p'
         const R Hp = q[4] + pp;                                       // H' = rhoe' + p'
-        G[3] = (Hp * vv.rho_ref - lv.href * q[0]) * (rinv / vv.rho_ref);
+        G[3] = (Hp * vv.rho_ref - lv.href * q[0]) * (rinv * rcp_r(vv.rho_ref));
         if (SMAG) {
-            const R rT = (pp * vv.rho_ref - vv.p_ref * q[0]) * (rinv / vv.p_ref);
-            const R lnr = log1p_r(rT) - VConst<R>::kappa(P) * log1p_r(pp / vv.p_ref);
+            const R ipr = rcp_r(vv.p_ref);
+            const R rT = (pp * vv.rho_ref - vv.p_ref * q[0]) * (rinv * ipr);
+            const R lnr = log1p_r(rT) - VConst<R>::kappa(P) * log1p_r(pp * ipr);
             G[4] = vv.thv_ref * expm1_r(lnr);
         }
     } else {
@@ -199,7 +237,6 @@ __global__ void __launch_bounds__(VDims<N>::NT, (sizeof(R) == 4 ? (HYPER ? 4 : 6
     CRV* const s_cr = reinterpret_cast<CRV*>(s_node + P5N);                 // (c, 1/rho)
     R* const s_F = s_node + P5N + planar_pad<R>(2 * Np);                    // total flux, 3 directions
     R* const s_fs = s_F + 3 * P5N;                                          // lifted face flux
-    R* const s_D = s_fs + planar_pad<R>(5 * NFN);                           // Dhat
 
     const int e = blockIdx.x, t = threadIdx.x;
     const R* __restrict__ Qin = static_cast<const R*>(P.Qin);
@@ -222,7 +259,7 @@ __global__ void __launch_bounds__(VDims<N>::NT, (sizeof(R) == 4 ? (HYPER ? 4 : 6
     const int vM = fd == 0 ? fside * N + Nq * fn : (fd == 1 ? fa + Nq * (fside * N + Nq * fb) : fn + Nfp * (fside * N));
     const int vP = fd == 0 ? oside * N + Nq * fn : (fd == 1 ? fa + Nq * (oside * N + Nq * fb) : fn + Nfp * (oside * N));
     const R sgn = fside ? R(1) : R(-1);
-    if (t < Nq * Nq) s_D[t] = static_cast<const R*>(P.Dhat)[t];
+
     // record of this node in the direction-d flux plane (contraction index slowest)
     auto dir_rec = [&](int d) {
         return d == 0 ? ni * Nfp + (nj + Nq * nk) : (d == 1 ? nj * Nfp + (ni + Nq * nk) : t);
@@ -362,7 +399,7 @@ __global__ void __launch_bounds__(VDims<N>::NT, (sizeof(R) == 4 ? (HYPER ? 4 : 6
             PL::ld(s_F, Np, L1 + n * Nfp, v1);
             PL::ld(s_F + P5N, Np, L2 + n * Nfp, v2);
             PL::ld(s_F + 2 * P5N, Np, L3 + n * Nfp, v3);
-            const R d1 = s_D[ni * Nq + n], d2 = s_D[nj * Nq + n], d3 = s_D[nk * Nq + n];
+            const R d1 = dhat_p<R>(P, ni * Nq + n), d2 = dhat_p<R>(P, nj * Nq + n), d3 = dhat_p<R>(P, nk * Nq + n);
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) {
                 acc1[s] = fma(d1, v1[s], acc1[s]);
