@@ -305,12 +305,15 @@ class DGModel:
              float(dt), int(nsteps), _stream())
 
     # ------------------------------------------------------------------ launch configuration
-    KERNELS = {"node": 0, "column": 1, "lines": 2}
+    KERNELS = {"node": 0, "column": 1, "lines": 2, "cluster": 3}
 
     def set_kernel(self, kind: str = "node", grid_ctas: int = -1):
-        """Stage-kernel family ("node", "column" or "lines") and grid: -1 = one
-        CTA per element (the default), 0 = one wave of resident CTAs, n > 0 =
-        n CTAs (the "lines" kernel always runs one CTA per element)."""
+        """Stage-kernel family ("node", "column", "lines" or "cluster") and
+        grid: -1 = one CTA per element (the default), 0 = one wave of resident
+        CTAs, n > 0 = n CTAs (the "lines" kernel always runs one CTA per
+        element); for "cluster", grid_ctas is the cluster size, 2, 4 or 8
+        adjacent elements whose shared faces read the neighbour from its
+        CTA's shared memory."""
         call("cmdg_model_set_kernel", self.h, self.KERNELS[kind], int(grid_ctas))
 
     def get_kernel(self):

@@ -390,6 +390,7 @@ int cmdg_model_destroy(cmdg_model* model) {
     cudaFree(md.d_Dhat32);
     cudaFree(md.d_status);
     cudaFree(md.d_scratch);
+    cudaFree(md.d_cl_elem);
     cudaFree(md.d_red);
     cudaFree(md.d_lvv64);
     cudaFree(md.d_lvv32);

@@ -43,7 +43,7 @@ constexpr int NBR_STRIDE = 8;
 // stage-kernel families: one thread per node, one thread per vertical line
 // of nodes, or one thread per node for the fluxes and one per element line
 // for the face fluxes and contractions
-enum { KERNEL_NODE = 0, KERNEL_COLUMN = 1, KERNEL_LINES = 2 };
+enum { KERNEL_NODE = 0, KERNEL_COLUMN = 1, KERNEL_LINES = 2, KERNEL_CLUSTER = 3 };
 constexpr int MIN_N = 2;
 constexpr int MAX_N = 5;
 
@@ -212,7 +212,9 @@ struct Model {
     int mms_zero_h = 0;
     int grid_ctas = -1;              // stage-kernel grid: -1 = one CTA per element (the measured best
                                      // on GB300), 0 = one wave of resident CTAs, n > 0 = n CTAs
-    int kernel_kind = 0;             // KERNEL_NODE or KERNEL_COLUMN
+    int kernel_kind = 0;             // KERNEL_NODE, KERNEL_COLUMN, KERNEL_LINES or KERNEL_CLUSTER
+    int* d_cl_elem = nullptr;        // KERNEL_CLUSTER: element of each CTA, clusters of cl_size adjacent elements
+    int cl_size = 0;
     int device = -1;                 // CUDA device current when the model was created
     void* noalloc_stage = nullptr;   // device address of the allocation-free stage array on that device
     // test hook of the persistent stage kernel's bounded waits: when

@@ -74,6 +74,8 @@ struct KParams {
     // and the test hook that arms the staging barriers without issuing the
     // copies, so that every wait runs out (cmdg_model_set_staging_test)
     int wait_polls;
+    // cluster kernel: the element of each CTA (clusters of adjacent elements)
+    const int* cl_elem;
     int staging_skip_copies;
 };
 

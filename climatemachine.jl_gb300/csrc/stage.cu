@@ -39,7 +39,11 @@
 // which is exact algebra for dry air (T = T0 + e_int/cv, p = rho R T), the
 // reference-state jump across vertical faces enters the Rusanov penalty
 // from an FP64-computed table, and the RK register dQ stays FP64.
+#include <cooperative_groups.h>
+
 #include "dg_common.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace cmdg {
 namespace {
@@ -141,9 +145,11 @@ __device__ __forceinline__ double dhat_const<double>(const KParams& P, int idx) 
     return P.DhatC64[idx];
 }
 
-template <int N, typename R, bool MIXED, int MODE, bool PERSIST, bool PARAM_D>
+template <int N, typename R, bool MIXED, int MODE, bool PERSIST, bool PARAM_D, int CL = 0>
 __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem_raw, int e_first, int e_stride,
                                            int e_end) {
+    static_assert(CL == 0 || CL == 2 || CL == 4 || CL == 8, "clusters of 2 (z), 4 (x, z) or 8 (x, y, z) elements");
+    static_assert(CL == 0 || !PERSIST, "a cluster CTA computes one element");
     using Dm = Dims<N>;
     using SM = Smem<N, R>;
     constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp;
@@ -170,9 +176,35 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
     const int nk = node_thread ? t / Nfp : 0;
     const int nj = node_thread ? (t - nk * Nfp) / Nq : 0;
     const int ni = node_thread ? t - nk * Nfp - nj * Nq : 0;
-    // face thread: face f (0..5 = xi1-, xi1+, xi2-, xi2+, xi3-, xi3+), in-face node fn
-    const int f = face_thread ? t / Nfp : 0;
-    const int fn = face_thread ? t - f * Nfp : 0;
+    // face thread: face f (0..5 = xi1-, xi1+, xi2-, xi2+, xi3-, xi3+), in-face node fn.
+    // CL: the CTA's rank in its cluster of 2 x 2 x 2 (CL = 8), 2 x 1 x 2 (4)
+    // or 1 x 1 x 2 (2) elements, bit 0 = upper in z, bit 1 = upper in x,
+    // bit 2 = upper in y.  The faces shared with the other elements of the
+    // cluster take the first face slots, so whole warps read their neighbour
+    // from that element's shared memory and the rest gather it from global
+    // memory (a warp that mixes the two paths runs both).
+    const int crank = CL > 0 ? (int)(blockIdx.x % (unsigned)(CL > 0 ? CL : 1)) : 0;
+    constexpr int NIN = CL == 8 ? 3 : (CL == 4 ? 2 : (CL == 2 ? 1 : 0));  // dimensions the cluster spans
+    // slot -> face: slots 0 .. NIN-1 the faces towards the other half of the
+    // cluster in z, x, y (bit b of the rank: upper half -> the minus face);
+    // NIN .. 2 NIN - 1 the opposite faces; then both faces of each direction
+    // the cluster does not span
+    auto slot_face = [&](int slot) {
+        auto dir = [](int dim) { return dim == 0 ? 2 : (dim == 1 ? 0 : 1); };  // cluster dimension z, x, y
+        if (slot < 2 * NIN) {
+            const int dim = slot < NIN ? slot : slot - NIN;
+            const int upper = (crank >> dim) & 1;
+            const int side = (slot < NIN) ? (upper ^ 1) : upper;
+            return 2 * dir(dim) + side;
+        }
+        const int rest = slot - 2 * NIN;
+        return 2 * dir(NIN + rest / 2) + (rest & 1);
+    };
+    const int fslot = face_thread ? t / Nfp : 0;
+    const int f = CL > 0 ? slot_face(fslot) : fslot;
+    const bool remote = CL > 0 && face_thread && fslot < NIN;  // neighbour inside the cluster
+    const int nrank = remote ? (crank ^ (1 << fslot)) : 0;
+    const int fn = face_thread ? t - fslot * Nfp : 0;
     const int fd = f >> 1, fside = f & 1;
     const int fa = fn % Nq, fb = fn / Nq;
     // volume node on face f at in-face (a, b), and the matching node of the neighbour on face f^1
@@ -200,7 +232,7 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
             for (int s = 0; s < NSTATE; ++s) a.q[s] = qe[s * Np];
         }
         a.nb = face_thread ? __ldg(nbr + f) : -1;
-        if (a.nb >= 0) {
+        if (a.nb >= 0 && !remote) {
             const R* qn = Qin + (size_t)a.nb * ESTRIDE + vP;
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) a.qp[s] = qn[s * Np];
@@ -340,7 +372,9 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
                 gsrc = -rho_s * lv.gphiz;
             }
         }
-        __syncthreads();
+        // CL: every element of the cluster has staged its nodes before any reads them
+        if constexpr (CL > 0) cg::this_cluster().sync();
+        else __syncthreads();
 
         // ---------------- phase 2: one numerical flux per face node
         if (face_thread) {
@@ -354,8 +388,10 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
             const R lam_m = fabs(pick3(fd, qm[1], qm[2], qm[3]) * ri_m) + c_m;
             int ezp = ez;
             if (cur.nb >= 0) {
+                if (!remote) {
 #pragma unroll
-                for (int s = 0; s < NSTATE; ++s) qp[s] = cur.qp[s];
+                    for (int s = 0; s < NSTATE; ++s) qp[s] = cur.qp[s];
+                }
                 if (fd == 2) {
                     // vertical neighbour: one element below (f = 4) or above (f = 5), periodic wrap
                     ezp = ez + (fside ? 1 : -1);
@@ -376,10 +412,23 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
                 qp[2] = (fd == 1) ? -qm[2] : qm[2];
                 qp[3] = (fd == 2) ? -qm[3] : qm[3];
             }
-            const Level<R> lvp = load_level<R>(P, ezp * Nq + (cur.nb >= 0 ? kP : kM));
-            const Thermo<R, MIXED> thp = thermo<R, MIXED>(qp, lvp, P);
-            normal_flux<R, MIXED>(qp, thp, fd, sgn, Fp);
-            const R lam_p = fabs(pick3(fd, thp.u[0], thp.u[1], thp.u[2])) + thp.c;
+            R lam_p;
+            if (CL > 0 && remote) {
+                // the neighbour inside the cluster: its staged state, (c, 1/rho)
+                // and xi_fd flux at the facing node, read from its shared memory
+                const auto cl = cg::this_cluster();
+                PL::ld(cl.map_shared_rank(s_node, (unsigned)nrank), Np, vP, qp);
+                const CRV crp = cl.map_shared_rank(s_cr, (unsigned)nrank)[vP];
+                PL::ld(cl.map_shared_rank(s_F + fd * SM::P5N, (unsigned)nrank), Np, oside * N * Nfp + fn, Fp);
+#pragma unroll
+                for (int s = 0; s < NSTATE; ++s) Fp[s] *= sgn;
+                lam_p = fabs(pick3(fd, qp[1], qp[2], qp[3]) * crp.y) + crp.x;
+            } else {
+                const Level<R> lvp = load_level<R>(P, ezp * Nq + (cur.nb >= 0 ? kP : kM));
+                const Thermo<R, MIXED> thp = thermo<R, MIXED>(qp, lvp, P);
+                normal_flux<R, MIXED>(qp, thp, fd, sgn, Fp);
+                lam_p = fabs(pick3(fd, thp.u[0], thp.u[1], thp.u[2])) + thp.c;
+            }
             const R lift = pick3(fd, xi[0], xi[1], xi[2]) * KConst<R>::inv_w0(P);
             const R hmw = (ph.numflux == CMDG_FLUX_RUSANOV) ? R(0.5) * fmax(lam_m, lam_p) : R(0);
             const R hl = R(0.5) * lift, pl = hmw * lift;
@@ -389,7 +438,10 @@ __device__ __forceinline__ void stage_body(const KParams& P, unsigned char* smem
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) s_fs[(fd * NSTATE + s) * Np + vM] = fs[s];
         }
-        __syncthreads();
+        // CL: no element of the cluster leaves (or reuses its shared memory)
+        // while another may still read it
+        if constexpr (CL > 0) cg::this_cluster().sync();
+        else __syncthreads();
 
         // ---------------- phase 3: volume contraction, face terms, source, update
         int bad = 0;
@@ -482,6 +534,65 @@ __global__ void __launch_bounds__(Dims<N>::NT, MIXED ? (PERSIST ? Dims<N>::MIN_C
                                                      : Dims<N>::MIN_CTAS64) stage_kernel(const KParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     stage_body<N, R, MIXED, MODE, PERSIST, true>(P, smem_raw, blockIdx.x, PERSIST ? gridDim.x : P.nelem, P.nelem);
+}
+
+// One CTA per element in clusters of CL CTAs that are adjacent elements
+// (2 x 2 x 2, 2 x 1 x 2 or 1 x 1 x 2 in x, y, z): the CTA of cluster rank r
+// computes element P.cl_elem[blockIdx.x], and the faces shared inside the
+// cluster read the neighbour's staged state and flux from its CTA's shared
+// memory (distributed shared memory) instead of gathering the neighbour's
+// state from global memory and recomputing its thermodynamics and flux.
+template <int N, typename R, bool MIXED, int MODE, int CL>
+__global__ void __launch_bounds__(Dims<N>::NT, MIXED ? Dims<N>::MIN_CTAS_DIRECT : Dims<N>::MIN_CTAS64)
+    stage_cluster_kernel(const KParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int e = __ldg(P.cl_elem + blockIdx.x);
+    stage_body<N, R, MIXED, MODE, false, true, CL>(P, smem_raw, e, 1, e + 1);
+}
+
+template <int N, typename R, bool MIXED, int MODE, int CL>
+cudaError_t launch_cluster_mode(const KParams& P, cudaStream_t s) {
+    constexpr size_t bytes = Smem<N, R>::BYTES;
+    static unsigned long long configured = 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (bytes > 48 * 1024 && !(configured & (1ull << (dev & 63)))) {
+        e = cudaFuncSetAttribute(stage_cluster_kernel<N, R, MIXED, MODE, CL>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e != cudaSuccess) return e;
+        configured |= 1ull << (dev & 63);
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)P.nelem, 1, 1);
+    cfg.blockDim = dim3(Dims<N>::NT, 1, 1);
+    cfg.dynamicSmemBytes = bytes;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, stage_cluster_kernel<N, R, MIXED, MODE, CL>, P);
+}
+
+template <int N, typename R, bool MIXED, int CL>
+cudaError_t launch_cluster_typed(const KParams& P, int mode, cudaStream_t s) {
+    return mode == 0 ? launch_cluster_mode<N, R, MIXED, 0, CL>(P, s) : launch_cluster_mode<N, R, MIXED, 1, CL>(P, s);
+}
+
+template <int N>
+cudaError_t launch_cluster_N(const KParams& P, bool mixed, int mode, int cl, cudaStream_t s) {
+    if (cl == 8)
+        return mixed ? launch_cluster_typed<N, float, true, 8>(P, mode, s)
+                     : launch_cluster_typed<N, double, false, 8>(P, mode, s);
+    if (cl == 4)
+        return mixed ? launch_cluster_typed<N, float, true, 4>(P, mode, s)
+                     : launch_cluster_typed<N, double, false, 4>(P, mode, s);
+    return mixed ? launch_cluster_typed<N, float, true, 2>(P, mode, s)
+                 : launch_cluster_typed<N, double, false, 2>(P, mode, s);
 }
 
 template <int N, typename R, bool MIXED, int MODE, bool PERSIST>
@@ -633,6 +744,7 @@ KParams make_params(Model* md, const LaunchArgs& a) {
     P.mms_src = md->mms_src;
     P.mms_wall = md->mms_wall;
     P.mms_zero_h = md->mms_zero_h;
+    P.cl_elem = md->d_cl_elem;
     P.wait_polls = md->wait_polls;
     P.staging_skip_copies = md->staging_skip_copies;
     return P;
@@ -656,6 +768,19 @@ int launch_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
     cudaError_t err = cudaErrorNotSupported;
     if (md->kernel_kind == KERNEL_COLUMN) err = launch_column(P, m.N, mixed, a.mode, md->grid_ctas, s);
     if (md->kernel_kind == KERNEL_LINES) err = launch_lines(P, m.N, mixed, a.mode, s);
+    if (md->kernel_kind == KERNEL_CLUSTER) {
+        if (md->d_cl_elem == nullptr || md->cl_size != md->grid_ctas) {
+            set_error("the cluster kernel needs its element map (cmdg_model_set_kernel)");
+            return CMDG_ERR_STATE;
+        }
+        switch (m.N) {
+            case 2: err = launch_cluster_N<2>(P, mixed, a.mode, md->cl_size, s); break;
+            case 3: err = launch_cluster_N<3>(P, mixed, a.mode, md->cl_size, s); break;
+            case 4: err = launch_cluster_N<4>(P, mixed, a.mode, md->cl_size, s); break;
+            case 5: err = launch_cluster_N<5>(P, mixed, a.mode, md->cl_size, s); break;
+            default: set_error("no kernel instantiated for N=%d", m.N); return CMDG_ERR_UNSUPPORTED;
+        }
+    }
     if (err == cudaErrorNotSupported) {
         switch (m.N) {
             case 2: err = launch_N<2>(P, mixed, a.mode, md->grid_ctas, s); break;

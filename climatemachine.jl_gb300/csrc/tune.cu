@@ -14,12 +14,69 @@ struct Candidate {
 
 }  // namespace
 
+namespace cmdg {
+
+// The element of every CTA of the cluster kernel: clusters of CL adjacent
+// elements of a stacked brick (2 x 2 x 2 in x, y, z for CL = 8, 2 x 1 x 2 for
+// 4, 1 x 1 x 2 for 2), cluster rank bit 0 = upper in z, bit 1 = upper in x,
+// bit 2 = upper in y; clusters ordered z fastest, then x, then y.  Needs an
+// inviscid brick in stacked order whose element counts are even in the
+// directions the cluster spans.
+int build_cluster_map(Model* md, int CL) {
+    const Mesh& m = *md->mesh;
+    CMDG_ARG_CHECK(CL == 2 || CL == 4 || CL == 8, "cluster size must be 2, 4 or 8, got %d", CL);
+    if (m.kind != MESH_BRICK || m.col_at.empty() || md->prm.turbulence != CMDG_TURB_NONE ||
+        md->prm.hyperdiffusion != CMDG_HYPER_NONE) {
+        set_error("the cluster kernel runs inviscid models on bricks in stacked (column) order");
+        return CMDG_ERR_UNSUPPORTED;
+    }
+    const int nx = m.desc.ne[0], ny = m.desc.ne[1], nz = m.desc.ne[2];
+    if (nz % 2 || (CL >= 4 && nx % 2) || (CL == 8 && ny % 2)) {
+        set_error("clusters of %d elements need even element counts in the directions they span (%d x %d x %d)", CL,
+                  nx, ny, nz);
+        return CMDG_ERR_UNSUPPORTED;
+    }
+    const int sx = CL >= 4 ? 2 : 1, sy = CL == 8 ? 2 : 1;
+    std::vector<int> col_of((size_t)nx * ny, -1);
+    for (size_t h = 0; h < m.col_at.size(); ++h) col_of[m.col_at[h]] = (int)h;
+    std::vector<int> map((size_t)m.nelem);
+    size_t b = 0;
+    for (int by = 0; by < ny / sy; ++by)
+        for (int bx = 0; bx < nx / sx; ++bx)
+            for (int bz = 0; bz < nz / 2; ++bz)
+                for (int r = 0; r < CL; ++r) {
+                    const int iz = 2 * bz + (r & 1);
+                    const int ix = sx * bx + (CL >= 4 ? (r >> 1) & 1 : 0);
+                    const int iy = sy * by + (CL == 8 ? (r >> 2) & 1 : 0);
+                    const int h = col_of[(size_t)ix + (size_t)nx * iy];
+                    if (h < 0) {
+                        set_error("cluster map: column (%d, %d) missing from the mesh", ix, iy);
+                        return CMDG_ERR_STATE;
+                    }
+                    map[b++] = iz + nz * h;
+                }
+    if (md->d_cl_elem) cudaFree(md->d_cl_elem);
+    md->d_cl_elem = nullptr;
+    md->cl_size = 0;
+    CMDG_CUDA_CHECK(cudaMalloc(&md->d_cl_elem, sizeof(int) * map.size()));
+    CMDG_CUDA_CHECK(cudaMemcpy(md->d_cl_elem, map.data(), sizeof(int) * map.size(), cudaMemcpyHostToDevice));
+    md->cl_size = CL;
+    return CMDG_OK;
+}
+
+}  // namespace cmdg
+
 extern "C" int cmdg_model_set_kernel(cmdg_model* model, int kernel_kind, int grid_ctas) {
     using namespace cmdg;
     CMDG_ARG_CHECK(model != nullptr, "model is NULL");
-    CMDG_ARG_CHECK(kernel_kind == KERNEL_NODE || kernel_kind == KERNEL_COLUMN || kernel_kind == KERNEL_LINES,
+    CMDG_ARG_CHECK(kernel_kind == KERNEL_NODE || kernel_kind == KERNEL_COLUMN || kernel_kind == KERNEL_LINES ||
+                       kernel_kind == KERNEL_CLUSTER,
                    "unknown kernel kind %d", kernel_kind);
     CMDG_ARG_CHECK(grid_ctas >= -1, "grid_ctas must be >= -1");
+    if (kernel_kind == KERNEL_CLUSTER) {
+        const int rc = build_cluster_map(&model->m, grid_ctas);
+        if (rc) return rc;
+    }
     model->m.kernel_kind = kernel_kind;
     model->m.grid_ctas = grid_ctas;
     // captured step graphs embed the old launch configuration
@@ -70,7 +127,16 @@ extern "C" int cmdg_model_autotune(cmdg_model* model, int reps, double* h_ms, in
     // one kernel family for viscous models and for curvilinear meshes
     if (md->prm.turbulence != CMDG_TURB_NONE || md->prm.hyperdiffusion != CMDG_HYPER_NONE || m.kind != MESH_BRICK)
         cands = {{KERNEL_NODE, -1}};
-    else if (mixed && m.N >= 3 && m.N <= 5) cands.push_back({KERNEL_COLUMN, 0});
+    else {
+        if (mixed && m.N >= 3 && m.N <= 5) cands.push_back({KERNEL_COLUMN, 0});
+        // thread-block clusters of adjacent elements, where the element counts allow them
+        const int nx = m.desc.ne[0], ny = m.desc.ne[1], nz = m.desc.ne[2];
+        if (nz % 2 == 0) {
+            cands.push_back({KERNEL_CLUSTER, 2});
+            if (nx % 2 == 0) cands.push_back({KERNEL_CLUSTER, 4});
+            if (nx % 2 == 0 && ny % 2 == 0) cands.push_back({KERNEL_CLUSTER, 8});
+        }
+    }
     std::vector<double> ms(cands.size(), 0.0);
     auto fail = [&](cudaError_t e, const char* what) {
         set_error("autotune: %s: %s", what, cudaGetErrorString(e));
@@ -85,6 +151,7 @@ extern "C" int cmdg_model_autotune(cmdg_model* model, int reps, double* h_ms, in
     if (!rc && (e = cudaEventCreate(&t0)) != cudaSuccess) fail(e, "event");
     if (!rc && (e = cudaEventCreate(&t1)) != cudaSuccess) fail(e, "event");
     for (size_t ci = 0; ci < cands.size() && !rc; ++ci) {
+        if (cands[ci].kind == KERNEL_CLUSTER && (rc = build_cluster_map(md, cands[ci].grid))) break;
         md->kernel_kind = cands[ci].kind;
         md->grid_ctas = cands[ci].grid;
         LaunchArgs a;
@@ -121,6 +188,11 @@ extern "C" int cmdg_model_autotune(cmdg_model* model, int reps, double* h_ms, in
     size_t best = 0;
     for (size_t ci = 1; ci < cands.size(); ++ci)
         if (ms[ci] < ms[best]) best = ci;
+    if (cands[best].kind == KERNEL_CLUSTER && (rc = build_cluster_map(md, cands[best].grid))) {
+        md->kernel_kind = saved_kind;
+        md->grid_ctas = saved_grid;
+        return rc;
+    }
     md->kernel_kind = cands[best].kind;
     md->grid_ctas = cands[best].grid;
     for (auto& kv : md->graphs) cudaGraphExecDestroy(kv.second);

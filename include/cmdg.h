@@ -216,14 +216,20 @@ int cmdg_model_set_mms(cmdg_model* model, const double* d_src, const double* d_w
 int cmdg_model_reference_state(const cmdg_model* model, double* h_ref);
 
 /* Stage-kernel family of a model: CMDG_KERNEL_NODE (one thread per node,
- * all precisions) or CMDG_KERNEL_COLUMN (one thread per vertical line of
+ * all precisions), CMDG_KERNEL_COLUMN (one thread per vertical line of
  * nodes; mixed precision, N = 3..5; other models fall back to the node
- * kernel).  For the node kernel, grid_ctas > 0 fixes the size of its
- * persistent grid, 0 = one wave of resident CTAs, -1 = no persistence (one
- * CTA per element, the default).  No counterpart in the reference (the
- * launch configuration of a KernelAbstractions kernel is fixed,
- * src/Numerics/DGMethods/SpaceDiscretization.jl:1120-1133). */
-enum { CMDG_KERNEL_NODE = 0, CMDG_KERNEL_COLUMN = 1 };
+ * kernel), CMDG_KERNEL_LINES (one thread per element line in the face and
+ * contraction phase) or CMDG_KERNEL_CLUSTER (the node kernel in thread-block
+ * clusters of grid_ctas = 2, 4 or 8 adjacent elements of an inviscid brick,
+ * 1 x 1 x 2, 2 x 1 x 2 or 2 x 2 x 2 in x, y, z, whose shared faces read the
+ * neighbour's staged state and flux from its CTA's shared memory; the
+ * element counts must be even in the directions a cluster spans, else
+ * CMDG_ERR_UNSUPPORTED).  For the node kernel, grid_ctas > 0 fixes the size
+ * of its persistent grid, 0 = one wave of resident CTAs, -1 = no
+ * persistence (one CTA per element, the default).  No counterpart in the
+ * reference (the launch configuration of a KernelAbstractions kernel is
+ * fixed, src/Numerics/DGMethods/SpaceDiscretization.jl:1120-1133). */
+enum { CMDG_KERNEL_NODE = 0, CMDG_KERNEL_COLUMN = 1, CMDG_KERNEL_LINES = 2, CMDG_KERNEL_CLUSTER = 3 };
 int cmdg_model_set_kernel(cmdg_model* model, int kernel_kind, int grid_ctas);
 int cmdg_model_get_kernel(const cmdg_model* model, int* kernel_kind, int* grid_ctas);
 

@@ -386,3 +386,52 @@ def test_degenerate_meshes_match_oracle(kind, ne, kernel):
             for sl in (slice(0, 1), slice(1, 4), slice(4, 5))]
     assert max(errs) < 1e-4, errs
     assert dgm.status_word() == 0
+
+
+@pytest.mark.parametrize("cl", [2, 4, 8])
+@pytest.mark.parametrize("N", [2, 3, 4, 5])
+@pytest.mark.parametrize("kind", ["vortex", "bubble"])
+def test_cluster_kernel_matches_oracle(kind, N, cl):
+    """The node kernel in thread-block clusters of 2, 4 or 8 adjacent
+    elements, whose shared faces read the neighbour's staged state and flux
+    from its CTA's shared memory: FP64 tendency and 3 LSRK54 steps within
+    1e-10 of the oracle; mixed tendency and 3 steps within 1e-6 (relative L2
+    per field group) of the one-CTA-per-element mixed kernel."""
+    ne = (4, 2, 4)
+    om, dg, Q0 = make_pair(kind, N, ne)
+    dg.set_kernel("cluster", cl)
+    assert dg.get_kernel() == ("cluster", cl)
+    ref = om.tendency(Q0)
+    Q = dg.init_ode_state(Q0)
+    dQ = dg.new_state(torch.float64)
+    dg(dQ, Q, None, 0.0)
+    err = rel_max(dQ.cpu().numpy(), ref)
+    assert (err < TOL64).all(), err
+    dt = 0.5 * om.courant_dt(Q0, 0.4)
+    Qo, _ = om.lsrk54(Q0.copy(), dt, 3)
+    cmdg.dostep_(Q, cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt), None, 0.0, nsteps=3)
+    err = rel_max(Q.cpu().numpy(), Qo)
+    assert (err < TOL64).all(), err
+    assert dg.status_word() == 0
+    if kind != "bubble":
+        return
+    out = {}
+    for k in ("node", "cluster"):
+        _, dgm, _ = make_pair(kind, N, ne, precision="mixed")
+        dgm.set_kernel(*(KERNELS["node"] if k == "node" else ("cluster", cl)))
+        Qm = dgm.init_ode_state(Q0)
+        T = dgm.new_state(torch.float64)
+        dgm(T, Qm, None, 0.0)
+        cmdg.dostep_(Qm, cmdg.LSRK54CarpenterKennedy(dgm, Qm, dt=dt), None, 0.0, nsteps=3)
+        out[k] = (T.cpu().numpy(), dgm.from_perturbation(Qm).cpu().numpy())
+        assert dgm.status_word() == 0
+    for a, b in zip(out["cluster"], out["node"]):
+        for sl in (slice(0, 1), slice(1, 4), slice(4, 5)):
+            assert np.linalg.norm(a[:, sl] - b[:, sl]) <= 1e-6 * np.linalg.norm(b[:, sl])
+
+
+def test_cluster_kernel_refuses_odd_counts():
+    om, dg, Q0 = make_pair("bubble", 3, (3, 2, 4))
+    with pytest.raises(cmdg.CmdgError, match="even element counts"):
+        dg.set_kernel("cluster", 4)
+    dg.set_kernel("cluster", 2)  # z only: 4 is even
