@@ -409,6 +409,8 @@ int cmdg_model_destroy(cmdg_model* model) {
     cudaFree(md.d_dxmin);
     cudaFree(md.d_ref64);
     cudaFree(md.d_filter_corr);
+    cudaFree(md.d_filter_ref64);
+    cudaFree(md.d_filter_corr_node);
     cudaFree(md.d_omega);
     cudaFree(md.d_lin64);
     cudaFree(md.d_linface64);

@@ -171,6 +171,11 @@ int init_arrays_tables(Model* md) {
 
 // The caller's geopotential, its gradient and the reference state, (Np, 7, nelem).
 int set_arrays_reference(Model* md, const double* aux7) {
+    // a filter's cached copy of the reference state belongs to the old one
+    cudaFree(md->d_filter_ref64);
+    md->d_filter_ref64 = nullptr;
+    cudaFree(md->d_filter_corr_node);
+    md->d_filter_corr_node = nullptr;
     const Mesh& m = *md->mesh;
     const cmdg_atmos_params& p = md->prm;
     const int Np = m.Np, Nfp = m.Nfp;

@@ -186,6 +186,10 @@ struct Model {
     double* d_dxmin = nullptr;       // curvilinear meshes: nearest-node distance per node
     std::vector<float> filter_corr;  // mixed precision: vertical-filter change of the reference state per level
     float* d_filter_corr = nullptr;
+    // mixed precision on other meshes: the reference state as a full FP64
+    // state, a scratch copy for its filtered values, and the per-node change
+    double* d_filter_ref64 = nullptr;
+    float* d_filter_corr_node = nullptr;
     double* d_omega = nullptr;       // LGL weights on the device (TMAR filter)
     void* d_hd = nullptr;            // hyperdiffusion: gradient, then nu grad^3, (Np, 9, nelem)
     void* d_hlap = nullptr;          // hyperdiffusion: laplacians (Np, 3, nelem)

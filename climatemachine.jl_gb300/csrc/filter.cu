@@ -9,9 +9,13 @@
 // :651-790).  One CTA per element stages the filtered fields in shared
 // memory and sweeps the three directions with a barrier between sweeps.
 // Mixed precision filters the FP32 perturbation and adds the FP64-computed
-// change of the reference state under the vertical filter, W_v q_ref - q_ref,
-// per vertical node level (a level function is left unchanged by the
-// horizontal filter, whose constant mode has Sigma_0 = 1).
+// change of the reference state under the filter, W q_ref - q_ref: on a
+// brick whose horizontal filter keeps constants, per vertical node level (a
+// level function is left unchanged by the horizontal filter, whose constant
+// mode has Sigma_0 = 1); otherwise (cubed shells and grid arrays, whose
+// reference state varies along a level, or a horizontal filter that does not
+// keep constants) per node, by the FP64 filter applied to the reference
+// state itself.
 //
 // TMAR (kernel_apply_TMAR_filter!, :794-892): per element and field,
 // r = sum(M q) / sum(M max(q, 0)) (0 when sum(M q) <= 0), q <- r q where
@@ -94,6 +98,7 @@ constexpr int FNQ = MAX_N + 1;
 struct FilterArgs {
     void* Q;
     const float* corr;        // mixed: [nlev][2] level corrections for rho, rhoe (or NULL)
+    const float* corr_node;   // mixed: [nelem][2][Np] node corrections for rho, rhoe (or NULL)
     double Wh64[FNQ * FNQ], Wv64[FNQ * FNQ];
     float Wh32[FNQ * FNQ], Wv32[FNQ * FNQ];
     int nz, horizontal, vertical;
@@ -160,6 +165,11 @@ __global__ void __launch_bounds__(((N + 1) * (N + 1) * (N + 1) + 31) / 32 * 32)
         if (A.field_mask & 1u) v[0] += (R)A.corr[2 * lev + 0];
         if (A.field_mask & 16u) v[4] += (R)A.corr[2 * lev + 1];
     }
+    if (A.corr_node) {
+        const float* c = A.corr_node + (size_t)e * 2 * Np + t;
+        if (A.field_mask & 1u) v[0] += (R)c[0];
+        if (A.field_mask & 16u) v[4] += (R)c[Np];
+    }
 #pragma unroll
     for (int s = 0; s < NSTATE; ++s)
         if ((A.field_mask >> s) & 1u) Q[s * Np + t] = v[s];
@@ -170,6 +180,28 @@ cudaError_t launch_filter_N(const FilterArgs& A, int64_t nelem, cudaStream_t s) 
     constexpr int Np = (N + 1) * (N + 1) * (N + 1);
     spectral_filter_kernel<N, R><<<(unsigned)nelem, (Np + 31) / 32 * 32, 0, s>>>(A);
     return cudaGetLastError();
+}
+
+cudaError_t launch_filter(const FilterArgs& A, int N, bool fp32, int64_t nelem, cudaStream_t s) {
+    switch (N) {
+        case 2: return fp32 ? launch_filter_N<2, float>(A, nelem, s) : launch_filter_N<2, double>(A, nelem, s);
+        case 3: return fp32 ? launch_filter_N<3, float>(A, nelem, s) : launch_filter_N<3, double>(A, nelem, s);
+        case 4: return fp32 ? launch_filter_N<4, float>(A, nelem, s) : launch_filter_N<4, double>(A, nelem, s);
+        default: return fp32 ? launch_filter_N<5, float>(A, nelem, s) : launch_filter_N<5, double>(A, nelem, s);
+    }
+}
+
+// corr[e][c][n] = W q_ref - q_ref of rho (c = 0) and rhoe (c = 1), from the
+// filtered FP64 reference state Wq and the reference state q
+__global__ void node_correction_kernel(float* __restrict__ corr, const double* __restrict__ Wq,
+                                       const double* __restrict__ q, int64_t nelem, int Np) {
+    const int64_t total = nelem * 2 * Np;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = i / (2 * Np);
+        const int c = (int)((i / Np) % 2), n = (int)(i % Np);
+        const size_t src = ((size_t)e * NSTATE + (c ? 4 : 0)) * Np + n;
+        corr[i] = (float)(Wq[src] - q[src]);
+    }
 }
 
 // TMAR: one CTA per element; sums of M q and M max(q, 0) in FP64
@@ -334,9 +366,6 @@ extern "C" int cmdg_apply_filter(cmdg_model* model, void* d_Q, const double* h_W
     CMDG_ARG_CHECK(direction >= CMDG_DIR_EVERY && direction <= CMDG_DIR_VERTICAL, "unknown direction %d", direction);
     Model* md = &model->m;
     const Mesh& m = *md->mesh;
-    // element-local line filters; the mixed path's reference-state correction is per level of a brick
-    CMDG_ARG_CHECK(m.kind == MESH_BRICK || md->precision == CMDG_FP64,
-                   "mixed-precision filters run on brick meshes");
     const bool horiz = direction != CMDG_DIR_VERTICAL, vert = direction != CMDG_DIR_HORIZONTAL;
     CMDG_ARG_CHECK(!horiz || h_Wh != nullptr, "horizontal filter matrix is NULL");
     CMDG_ARG_CHECK(!vert || h_Wv != nullptr, "vertical filter matrix is NULL");
@@ -356,16 +385,47 @@ extern "C" int cmdg_apply_filter(cmdg_model* model, void* d_Q, const double* h_W
     }
     const bool mixed = md->precision == CMDG_MIXED;
     cudaStream_t s = (cudaStream_t)stream;
-    if (mixed && md->prm.ref_state && vert && (A.field_mask & 17u)) {
-        if (horiz) {
-            // the constant mode must survive the horizontal filter (Sigma_0 = 1)
-            for (int i = 0; i < Nq; ++i) {
-                double rs = 0;
-                for (int n = 0; n < Nq; ++n) rs += h_Wh[i * Nq + n];
-                CMDG_ARG_CHECK(std::fabs(rs - 1.0) < 1e-12,
-                               "mixed precision: the horizontal filter must keep constants (Nc >= 1)");
+    // the reference state's change under the filter: per level on a brick
+    // whose horizontal filter keeps constants (Sigma_0 = 1), else per node
+    bool keeps_constants = true;
+    for (int i = 0; horiz && i < Nq; ++i) {
+        double rs = 0;
+        for (int n = 0; n < Nq; ++n) rs += h_Wh[i * Nq + n];
+        keeps_constants = keeps_constants && std::fabs(rs - 1.0) < 1e-12;
+    }
+    const bool ref_fields = mixed && md->prm.ref_state && (A.field_mask & 17u);
+    if (ref_fields && (m.kind != MESH_BRICK || !keeps_constants)) {
+        // W q_ref - q_ref per node, FP64: the filter applied to the reference
+        // state itself (zero perturbation, as a full FP64 state)
+        const size_t len = (size_t)m.nelem * NSTATE * m.Np;
+        if (!md->d_filter_ref64) {
+            float* zero = nullptr;
+            CMDG_CUDA_CHECK(cudaMalloc(&md->d_filter_ref64, sizeof(double) * 2 * len));
+            CMDG_CUDA_CHECK(cudaMalloc(&md->d_filter_corr_node, sizeof(float) * 2 * (size_t)m.nelem * m.Np));
+            CMDG_CUDA_CHECK(cudaMalloc(&zero, sizeof(float) * len));
+            cudaError_t ez = cudaMemsetAsync(zero, 0, sizeof(float) * len, s);
+            rc = ez == cudaSuccess ? launch_from_perturbation(md, md->d_filter_ref64, zero, s) : CMDG_ERR_CUDA;
+            if (cudaStreamSynchronize(s) != cudaSuccess && rc == CMDG_OK) rc = CMDG_ERR_CUDA;
+            cudaFree(zero);
+            if (rc) {
+                set_error("filter: forming the reference state failed");
+                return rc;
             }
         }
+        double* Wq = md->d_filter_ref64 + len;
+        CMDG_CUDA_CHECK(cudaMemcpyAsync(Wq, md->d_filter_ref64, sizeof(double) * len, cudaMemcpyDeviceToDevice, s));
+        FilterArgs R = A;
+        R.Q = Wq;
+        R.corr = nullptr;
+        R.corr_node = nullptr;
+        R.field_mask = A.field_mask & 17u;
+        CMDG_CUDA_CHECK(launch_filter(R, m.N, false, m.nelem, s));
+        const int64_t total = m.nelem * 2 * (int64_t)m.Np;
+        node_correction_kernel<<<(unsigned)std::min<int64_t>((total + 255) / 256, 152 * 16), 256, 0, s>>>(
+            md->d_filter_corr_node, Wq, md->d_filter_ref64, m.nelem, m.Np);
+        CMDG_CUDA_CHECK(cudaGetLastError());
+        A.corr_node = md->d_filter_corr_node;
+    } else if (ref_fields && vert) {
         // W_v q_ref - q_ref per level, FP64
         md->filter_corr.assign((size_t)m.nlev * 2, 0.0f);
         for (int ez = 0; ez < m.nz; ++ez)
@@ -382,13 +442,7 @@ extern "C" int cmdg_apply_filter(cmdg_model* model, void* d_Q, const double* h_W
                                         cudaMemcpyHostToDevice, s));
         A.corr = md->d_filter_corr;
     }
-    cudaError_t e;
-    switch (m.N) {
-        case 2: e = mixed ? launch_filter_N<2, float>(A, m.nelem, s) : launch_filter_N<2, double>(A, m.nelem, s); break;
-        case 3: e = mixed ? launch_filter_N<3, float>(A, m.nelem, s) : launch_filter_N<3, double>(A, m.nelem, s); break;
-        case 4: e = mixed ? launch_filter_N<4, float>(A, m.nelem, s) : launch_filter_N<4, double>(A, m.nelem, s); break;
-        default: e = mixed ? launch_filter_N<5, float>(A, m.nelem, s) : launch_filter_N<5, double>(A, m.nelem, s); break;
-    }
+    const cudaError_t e = launch_filter(A, m.N, mixed, m.nelem, s);
     if (e != cudaSuccess) {
         set_error("filter launch failed: %s", cudaGetErrorString(e));
         return CMDG_ERR_CUDA;

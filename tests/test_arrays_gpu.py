@@ -322,3 +322,22 @@ def test_bubble_through_reference_ordered_arrays_matches_brick_path(precision):
                for g in groups]
         assert max(err) < tol, err
     assert dga.status_word() == 0
+
+
+def test_mixed_filter_on_grid_arrays_close_to_fp64():
+    """A mixed-precision spectral filter on a mesh from grid arrays (the cubed
+    shell's arrays): the FP32 perturbation filtered plus the per-node FP64
+    change of the reference state, within 1e-6 (relative to each field
+    group's scale) of the FP64 model's filter of the full state."""
+    from cmdg import filters
+
+    om, dg64, Q0, _ = cases("shell", 4)
+    _, dgm, _, _ = cases("shell", 4, precision="mixed")
+    filt = filters.ExponentialFilter(dg64.grid, 0, 18)
+    Q = dg64.init_ode_state(Q0)
+    filters.apply_(Q, (0, 1, 2, 3, 4), dg64, filt, "every")
+    Qp = dgm.init_ode_state(Q0)
+    filters.apply_(Qp, (0, 1, 2, 3, 4), dgm, filt, "every")
+    got, ref = dgm.from_perturbation(Qp).cpu().numpy(), Q.cpu().numpy()
+    for sl in (slice(0, 1), slice(1, 4), slice(4, 5)):
+        assert np.abs(got[:, sl] - ref[:, sl]).max() <= 1e-6 * np.abs(ref[:, sl]).max()

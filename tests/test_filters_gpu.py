@@ -1,6 +1,7 @@
 """GPU filters against the oracle: spectral filters (exponential, cutoff,
 Boyd-Vandeven; every, horizontal, vertical direction; field subsets) on the
-FP64 state within 1e-13 and on the mixed-precision perturbation within 1e-6,
+FP64 state within 1e-13 and on the mixed-precision perturbation within 1e-6
+(bricks and the cubed shell),
 the CutoffFilter known answer, TMAR, and the MassPreservingCutoffFilter
 (oracle parity on bricks and on the cubed shell, mass kept per field, the
 vertical exponential filter on the shell)."""
@@ -57,7 +58,7 @@ def test_fp64_spectral_filter_matches_oracle(kind, Nc, s, direction, fields):
     assert (rel(Q.cpu().numpy(), ref) < 1e-13).all()
 
 
-@pytest.mark.parametrize("kind,Nc,s,direction,fields", [c for c in CASES if c[1][0] >= 1])
+@pytest.mark.parametrize("kind,Nc,s,direction,fields", CASES)
 def test_mixed_spectral_filter_close_to_fp64_oracle(kind, Nc, s, direction, fields):
     om, dg, Q0 = pair(precision="mixed")
     cls = {"exponential": filters.ExponentialFilter, "cutoff": filters.CutoffFilter,
@@ -148,3 +149,22 @@ def test_mass_preserving_cutoff_refuses_mixed_models():
     Qp = dgm.init_ode_state(Q0)
     with pytest.raises(cmdg.CmdgError):
         filters.apply_(Qp, (0,), dgm, filters.MassPreservingCutoffFilter(dgm.grid, 2))
+
+
+@pytest.mark.parametrize("kind,direction", [("exponential", "vertical"), ("exponential", "every"),
+                                            ("cutoff", "horizontal"), ("boyd_vandeven", "every")])
+def test_mixed_filters_on_the_shell_close_to_fp64_oracle(kind, direction):
+    """Mixed-precision filters on the cubed shell, whose reference density
+    varies along a level: the FP32 perturbation is filtered and the FP64
+    change of the reference state under the same filter, W q_ref - q_ref, is
+    added per node.  Within 1e-6 of the oracle's FP64 filter of the full state."""
+    om, _, Q0 = shell_pair()
+    dg = workloads.gcm_shell_model(nhorz=2, nvert=2, N=4, precision="mixed")
+    filt = {"exponential": lambda g: filters.ExponentialFilter(g, 0, 18),
+            "cutoff": lambda g: filters.CutoffFilter(g, 2),
+            "boyd_vandeven": lambda g: filters.BoydVandevenFilter(g, 1, 8)}[kind](dg.grid)
+    Qp = dg.init_ode_state(Q0)
+    filters.apply_(Qp, (0, 1, 2, 3, 4), dg, filt, direction)
+    ref = O.apply_filter(om, Q0.copy(), filt.filter_matrices[0], filt.filter_matrices[1], direction)
+    got = dg.from_perturbation(Qp).cpu().numpy()
+    assert (rel(got, ref) < 1e-6).all(), rel(got, ref)
