@@ -342,9 +342,10 @@ int cmdg_batch_autotune(cmdg_batch* batch, void* const* h_Q, double* const* h_dQ
  * cmdg_apply_filter: applies the horizontal matrix along xi1 and xi2 and the
  * vertical one along xi3 (direction CMDG_DIR_*) to the listed fields of a
  * model's state in place (FP64 state, or the FP32 perturbation of a mixed
- * model; mixed needs Nc >= 1 horizontally) — Filters.apply!(Q, fields, grid,
- * filter; direction) (:408-505).  Any mesh for FP64 models (the filters act
- * along the element lines); mixed-precision models on brick meshes.
+ * model, to which the FP64 change of the reference state under the filter
+ * is added) — Filters.apply!(Q, fields, grid, filter; direction)
+ * (:408-505).  Any mesh, FP64 and mixed (the filters act along the element
+ * lines).
  * cmdg_apply_tmar: TMARFilter on the listed fields (:369-407, 794-892).
  * cmdg_apply_mp_filter: MassPreservingCutoffFilter (:309-345, 542-606,
  * 895-1065) with the cutoff matrices of cmdg_filter_matrix (the identity for
