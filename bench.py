@@ -890,7 +890,8 @@ def main():
     ensemble = None
     if rank == 0 and not args.no_ensemble and args.workload == "bubble":
         try:
-            ensemble = measure_ensemble(args, cmdg, workloads, torch, barrier, stream, flush)
+            # rank 0 alone: synchronise the device only (no collective barrier)
+            ensemble = measure_ensemble(args, cmdg, workloads, torch, torch.cuda.synchronize, stream, flush)
         except Exception as exc:  # the ensemble leg must not hide the GPU line
             ensemble = {"error": str(exc)[:300]}
 
