@@ -410,6 +410,7 @@ int cmdg_model_destroy(cmdg_model* model) {
     cudaFree(md.d_ref64);
     cudaFree(md.d_filter_corr);
     cudaFree(md.d_filter_ref64);
+    cudaFree(md.d_mp_scratch);
     cudaFree(md.d_filter_corr_node);
     cudaFree(md.d_omega);
     cudaFree(md.d_lin64);

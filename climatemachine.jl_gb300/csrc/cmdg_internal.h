@@ -189,6 +189,7 @@ struct Model {
     // mixed precision on other meshes: the reference state as a full FP64
     // state, a scratch copy for its filtered values, and the per-node change
     double* d_filter_ref64 = nullptr;
+    double* d_mp_scratch = nullptr;  // mixed models: FP64 full state for the mass-preserving filter
     float* d_filter_corr_node = nullptr;
     double* d_omega = nullptr;       // LGL weights on the device (TMAR filter)
     void* d_hd = nullptr;            // hyperdiffusion: gradient, then nu grad^3, (Np, 9, nelem)

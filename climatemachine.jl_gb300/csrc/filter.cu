@@ -451,13 +451,25 @@ extern "C" int cmdg_apply_filter(cmdg_model* model, void* d_Q, const double* h_W
     return CMDG_OK;
 }
 
-extern "C" int cmdg_apply_mp_filter(cmdg_model* model, double* d_Q, const double* h_Wh, const double* h_Wv,
+extern "C" int cmdg_apply_mp_filter(cmdg_model* model, void* d_state, const double* h_Wh, const double* h_Wv,
                                     int direction, const int* h_fields, int nfields, void* stream) {
-    CMDG_ARG_CHECK(model != nullptr && d_Q != nullptr && h_fields != nullptr, "NULL argument");
+    CMDG_ARG_CHECK(model != nullptr && d_state != nullptr && h_fields != nullptr, "NULL argument");
     CMDG_ARG_CHECK(direction >= CMDG_DIR_EVERY && direction <= CMDG_DIR_VERTICAL, "unknown direction %d", direction);
     Model* md = &model->m;
     const Mesh& m = *md->mesh;
-    CMDG_ARG_CHECK(md->precision == CMDG_FP64, "the mass-preserving cutoff filter runs FP64 models");
+    cudaStream_t s = (cudaStream_t)stream;
+    // a mixed model's FP32 perturbation is filtered through an FP64 copy of
+    // the full state: the element masses are those of the full state
+    const bool mixed = md->precision == CMDG_MIXED;
+    double* d_Q = static_cast<double*>(d_state);
+    if (mixed) {
+        if (!md->d_mp_scratch) {
+            CMDG_CUDA_CHECK(cudaMalloc(&md->d_mp_scratch, sizeof(double) * (size_t)m.nelem * NSTATE * m.Np));
+        }
+        d_Q = md->d_mp_scratch;
+        const int rc0 = launch_from_perturbation(md, d_Q, static_cast<const float*>(d_state), s);
+        if (rc0) return rc0;
+    }
     const bool horiz = direction != CMDG_DIR_VERTICAL, vert = direction != CMDG_DIR_HORIZONTAL;
     CMDG_ARG_CHECK(!horiz || h_Wh != nullptr, "horizontal filter matrix is NULL");
     CMDG_ARG_CHECK(!vert || h_Wv != nullptr, "vertical filter matrix is NULL");
@@ -477,7 +489,6 @@ extern "C" int cmdg_apply_mp_filter(cmdg_model* model, double* d_Q, const double
     }
     const double* mnode = m.kind == MESH_BRICK ? nullptr : md->d_mass;
     CMDG_ARG_CHECK(m.kind == MESH_BRICK || mnode != nullptr, "no mass matrix on this mesh");
-    cudaStream_t s = (cudaStream_t)stream;
     // horizontal pass, then vertical pass, each with its own mass restoration
     for (int pass = 0; pass < 2; ++pass) {
         if ((pass == 0 && !horiz) || (pass == 1 && !vert)) continue;
@@ -491,6 +502,7 @@ extern "C" int cmdg_apply_mp_filter(cmdg_model* model, double* d_Q, const double
         }
         CMDG_CUDA_CHECK(cudaGetLastError());
     }
+    if (mixed) return launch_to_perturbation(md, static_cast<float*>(d_state), d_Q, s);
     return CMDG_OK;
 }
 

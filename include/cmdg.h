@@ -351,14 +351,15 @@ int cmdg_batch_autotune(cmdg_batch* batch, void* const* h_Q, double* const* h_dQ
  * 895-1065) with the cutoff matrices of cmdg_filter_matrix (the identity for
  * Nc > N): a horizontal pass (xi1, xi2) and/or a vertical pass (xi3), each
  * followed by the per-element shift that restores sum M q of every listed
- * field; FP64 models, any mesh. */
+ * field; any mesh; a mixed model's FP32 perturbation is filtered through an
+ * FP64 copy of its full state (the masses are those of the full state). */
 enum { CMDG_FILTER_EXPONENTIAL = 0, CMDG_FILTER_CUTOFF = 1, CMDG_FILTER_BOYD_VANDEVEN = 2 };
 enum { CMDG_DIR_EVERY = 0, CMDG_DIR_HORIZONTAL = 1, CMDG_DIR_VERTICAL = 2 };
 int cmdg_filter_matrix(int N, int kind, int Nc, int s, double alpha, double* h_W);
 int cmdg_apply_filter(cmdg_model* model, void* d_Q, const double* h_Wh, const double* h_Wv, int direction,
                       const int* h_fields, int nfields, void* stream);
 int cmdg_apply_tmar(cmdg_model* model, void* d_Q, const int* h_fields, int nfields, void* stream);
-int cmdg_apply_mp_filter(cmdg_model* model, double* d_Q, const double* h_Wh, const double* h_Wv, int direction,
+int cmdg_apply_mp_filter(cmdg_model* model, void* d_Q, const double* h_Wh, const double* h_Wv, int direction,
                          const int* h_fields, int nfields, void* stream);
 
 /* HEVI (horizontally explicit, vertically implicit) stepping of FP64 states,

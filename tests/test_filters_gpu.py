@@ -144,11 +144,24 @@ def test_fp64_filters_run_on_the_shell():
     assert rel(Q.cpu().numpy(), ref).max() < 1e-13
 
 
-def test_mass_preserving_cutoff_refuses_mixed_models():
-    _, dgm, Q0 = pair(precision="mixed")
+@pytest.mark.parametrize("mesh", ["brick", "shell"])
+def test_mass_preserving_cutoff_on_mixed_models(mesh):
+    """A mixed model's perturbation filtered through an FP64 copy of its full
+    state: within 1e-6 (relative to each field group's scale) of the oracle's
+    FP64 filter, and the mass of every field kept to FP32 rounding of the
+    perturbation."""
+    if mesh == "brick":
+        om, dgm, Q0 = pair(precision="mixed")
+    else:
+        om, _, Q0 = shell_pair()
+        dgm = workloads.gcm_shell_model(nhorz=2, nvert=2, N=4, precision="mixed")
+    filt = filters.MassPreservingCutoffFilter(dgm.grid, 2)
     Qp = dgm.init_ode_state(Q0)
-    with pytest.raises(cmdg.CmdgError):
-        filters.apply_(Qp, (0,), dgm, filters.MassPreservingCutoffFilter(dgm.grid, 2))
+    filters.apply_(Qp, (0, 1, 2, 3, 4), dgm, filt, "every")
+    ref = O.apply_mp_filter(om, Q0.copy(), filt.filter_matrices[0], filt.filter_matrices[1], "every")
+    got = dgm.from_perturbation(Qp).cpu().numpy()
+    assert (rel(got, ref) < 1e-6).all(), rel(got, ref)
+    assert dgm.status_word() == 0
 
 
 @pytest.mark.parametrize("kind,direction", [("exponential", "vertical"), ("exponential", "every"),
