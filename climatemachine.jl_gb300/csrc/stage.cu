@@ -644,7 +644,7 @@ cudaError_t launch_N(const KParams& P, bool mixed, int mode, int grid, cudaStrea
 // of one member); each tile reads its member's launch parameters from global
 // memory and runs the node-kernel body with the CTA shape of its order.
 template <int N>
-__global__ void __launch_bounds__(Dims<N>::NT, Dims<N>::MIN_CTAS_DIRECT)
+__global__ void __launch_bounds__(Dims<N>::NT, Dims<N>::MIN_CTAS)
     batch_stage_kernel(const KParams* __restrict__ params, const BatchTile* __restrict__ tiles, int ntiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     for (int it = blockIdx.x; it < ntiles; it += gridDim.x) {
