@@ -64,7 +64,9 @@ class BrickGrid:
 
     Elements are ordered with the vertical index fastest, then the columns
     in x-then-y order (``topology="library"``) or along the 2D Hilbert curve
-    of the reference's StackedBrickTopology (``topology="stacked_brick"``).
+    of the reference's StackedBrickTopology (``topology="stacked_brick"``),
+    or all along the 3D Hilbert curve of BrickTopology (``topology="brick"``;
+    HEVI refuses this order, its column solves need contiguous columns).
     ``boundary`` gives the tags of the (lower, upper) faces of each
     non-periodic direction, as in the reference's ``boundary`` keyword.
     """

@@ -166,13 +166,8 @@ int cmdg_mesh_create_brick(const cmdg_brick_desc* desc, cmdg_mesh** out) {
 int cmdg_mesh_create_brick_ordered(const cmdg_brick_desc* desc, int topology, cmdg_mesh** out) {
     CMDG_ARG_CHECK(out != nullptr, "output pointer is NULL");
     *out = nullptr;
-    if (topology == CMDG_TOPOLOGY_BRICK) {
-        set_error("BrickTopology numbers the elements of a column apart, and the brick kernels' per-level tables "
-                  "need columns contiguous: build the mesh from the reference grid's arrays "
-                  "(cmdg_mesh_create_arrays), or map states with cmdg_brick_element_order");
-        return CMDG_ERR_UNSUPPORTED;
-    }
-    CMDG_ARG_CHECK(topology == CMDG_TOPOLOGY_LIBRARY || topology == CMDG_TOPOLOGY_STACKED_BRICK,
+    CMDG_ARG_CHECK(topology == CMDG_TOPOLOGY_LIBRARY || topology == CMDG_TOPOLOGY_STACKED_BRICK ||
+                       topology == CMDG_TOPOLOGY_BRICK,
                    "unknown topology order %d", topology);
     cmdg_mesh* mh = new cmdg_mesh();
     int rc = build_brick(desc, &mh->m, topology);
@@ -242,11 +237,7 @@ int cmdg_mesh_coordinates(const cmdg_mesh* mesh, double* h_xyz) {
         return CMDG_OK;
     }
     for (int64_t e = 0; e < m.nelem; ++e) {
-        const int64_t iz = e % m.nz;
-        const int64_t col = m.col_at[e / m.nz];
-        const int64_t ix = col % m.desc.ne[0];
-        const int64_t iy = col / m.desc.ne[0];
-        const int64_t idx[3] = {ix, iy, iz};
+        const int64_t idx[3] = {m.ijk[(size_t)e * 3 + 0], m.ijk[(size_t)e * 3 + 1], m.ijk[(size_t)e * 3 + 2]};
         for (int d = 0; d < 3; ++d) {
             const double lo = m.desc.lo[d], hi = m.desc.hi[d];
             const int n = m.desc.ne[d];
@@ -429,7 +420,7 @@ int cmdg_model_reference_state(const cmdg_model* model, double* h_ref) {
     const bool pernode = !md.ref64.empty(), pernode_p = !md.pref64.empty();
     for (int64_t e = 0; e < m.nelem; ++e)
         for (int node = 0; node < m.Np; ++node) {
-            const int lev = (int)(e % m.nz) * m.Nq + node / m.Nfp;
+            const int lev = m.nbr[(size_t)e * NBR_STRIDE + 6] * m.Nq + node / m.Nfp;
             const double* L = &md.lvl64[(size_t)lev * LV_NFIELDS];
             h_ref[((size_t)e * 3 + 0) * m.Np + node] = pernode ? md.ref64[((size_t)e * 2 + 0) * m.Np + node] : L[LV_RHO_REF];
             h_ref[((size_t)e * 3 + 1) * m.Np + node] = pernode ? md.ref64[((size_t)e * 2 + 1) * m.Np + node] : L[LV_RHOE_REF];

@@ -133,7 +133,10 @@ struct Mesh {
     std::vector<double> xyz, cgeo;
     // brick meshes: column order (col_at[h] = ix + nx iy of the h-th column)
     // and its topology (CMDG_TOPOLOGY_LIBRARY or CMDG_TOPOLOGY_STACKED_BRICK)
+    // (empty in BrickTopology order, whose columns are not contiguous), and
+    // the (ix, iy, iz) of every element
     std::vector<int> col_at;
+    std::vector<int> ijk;
     int topology = CMDG_TOPOLOGY_LIBRARY;
     // grid-arrays meshes: the facing node of every face node, (Nfp, 6, nelem)
     std::vector<int> fpart;

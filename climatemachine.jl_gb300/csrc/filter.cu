@@ -101,7 +101,8 @@ struct FilterArgs {
     const float* corr_node;   // mixed: [nelem][2][Np] node corrections for rho, rhoe (or NULL)
     double Wh64[FNQ * FNQ], Wv64[FNQ * FNQ];
     float Wh32[FNQ * FNQ], Wv32[FNQ * FNQ];
-    int nz, horizontal, vertical;
+    const int* nbr;           // neighbour rows: entry 6 is the element's vertical index
+    int horizontal, vertical;
     unsigned field_mask;
 };
 
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__(((N + 1) * (N + 1) * (N + 1) + 31) / 32 * 32)
     if (A.vertical) sweep(2);
     if (!node) return;
     if (A.corr) {
-        const int lev = (e % A.nz) * Nq + k;
+        const int lev = __ldg(A.nbr + (size_t)e * NBR_STRIDE + 6) * Nq + k;
         if (A.field_mask & 1u) v[0] += (R)A.corr[2 * lev + 0];
         if (A.field_mask & 16u) v[4] += (R)A.corr[2 * lev + 1];
     }
@@ -207,7 +208,7 @@ __global__ void node_correction_kernel(float* __restrict__ corr, const double* _
 // TMAR: one CTA per element; sums of M q and M max(q, 0) in FP64
 template <int N, typename R, bool MIXED>
 __global__ void __launch_bounds__(256) tmar_kernel(void* Qv, const double* emetric, const double* mnode,
-                                                   const double* w, const double* lvl, const double* refn, int nz,
+                                                   const double* w, const double* lvl, const double* refn, const int* nbr,
                                                    unsigned field_mask) {
     constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp;
     __shared__ double red[2][256];
@@ -224,7 +225,7 @@ __global__ void __launch_bounds__(256) tmar_kernel(void* Qv, const double* emetr
             double q = (double)Q[s * Np + n];
             if (MIXED && (s == 0 || s == 4)) {
                 q += refn ? refn[((size_t)e * 2 + (s == 4)) * Np + n]
-                          : lvl[(size_t)((e % nz) * Nq + k) * LV_NFIELDS + (s == 0 ? LV_RHO_REF : LV_RHOE_REF)];
+                          : lvl[(size_t)(nbr[(size_t)e * NBR_STRIDE + 6] * Nq + k) * LV_NFIELDS + (s == 0 ? LV_RHO_REF : LV_RHOE_REF)];
             }
             a += M * q;
             b += M * (q >= 0 ? q : 0.0);
@@ -246,7 +247,7 @@ __global__ void __launch_bounds__(256) tmar_kernel(void* Qv, const double* emetr
             double ref = 0;
             if (MIXED && (s == 0 || s == 4))
                 ref = refn ? refn[((size_t)e * 2 + (s == 4)) * Np + n]
-                           : lvl[(size_t)((e % nz) * Nq + k) * LV_NFIELDS + (s == 0 ? LV_RHO_REF : LV_RHOE_REF)];
+                           : lvl[(size_t)(nbr[(size_t)e * NBR_STRIDE + 6] * Nq + k) * LV_NFIELDS + (s == 0 ? LV_RHO_REF : LV_RHOE_REF)];
             const double q = (double)Q[s * Np + n] + ref;
             Q[s * Np + n] = (R)((q >= 0 ? r * q : 0.0) - ref);
         }
@@ -374,7 +375,7 @@ extern "C" int cmdg_apply_filter(cmdg_model* model, void* d_Q, const double* h_W
     if (rc) return rc;
     const int Nq = m.Nq;
     A.Q = d_Q;
-    A.nz = m.nz;
+    A.nbr = m.d_nbr;
     A.horizontal = horiz;
     A.vertical = vert;
     for (int i = 0; i < Nq * Nq; ++i) {
@@ -478,7 +479,7 @@ extern "C" int cmdg_apply_mp_filter(cmdg_model* model, void* d_state, const doub
     if (rc) return rc;
     const int Nq = m.Nq;
     A.Q = d_Q;
-    A.nz = m.nz;
+    A.nbr = m.d_nbr;
     for (int i = 0; i < Nq * Nq; ++i) {
         A.Wh64[i] = horiz ? h_Wh[i] : 0.0;
         A.Wv64[i] = vert ? h_Wv[i] : 0.0;
@@ -525,10 +526,10 @@ extern "C" int cmdg_apply_tmar(cmdg_model* model, void* d_Q, const int* h_fields
 #define CMDG_TMAR(NN)                                                                                            \
     if (mixed)                                                                                                   \
         tmar_kernel<NN, float, true><<<(unsigned)m.nelem, 256, 0, s>>>(d_Q, m.d_emetric, md->d_mass, d_w,        \
-                                                                       md->d_lvl64, md->d_ref64, m.nz, mask);   \
+                                                                       md->d_lvl64, md->d_ref64, m.d_nbr, mask);   \
     else                                                                                                         \
         tmar_kernel<NN, double, false><<<(unsigned)m.nelem, 256, 0, s>>>(d_Q, m.d_emetric, md->d_mass, d_w,      \
-                                                                         md->d_lvl64, md->d_ref64, m.nz, mask);
+                                                                         md->d_lvl64, md->d_ref64, m.d_nbr, mask);
         switch (m.N) {
             case 2: CMDG_TMAR(2) break;
             case 3: CMDG_TMAR(3) break;

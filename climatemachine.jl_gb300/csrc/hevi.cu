@@ -455,7 +455,8 @@ int arrays_stack_height(const Mesh& m) {
 int stack_height(const Model* md) {
     const Mesh& m = *md->mesh;
     if (m.kind == MESH_SHELL) return m.nz;
-    if (m.kind == MESH_BRICK && !m.desc.periodic[2]) return m.nz;
+    // a brick in BrickTopology's Hilbert order (no column order) has no stacks
+    if (m.kind == MESH_BRICK && !m.desc.periodic[2] && !m.col_at.empty()) return m.nz;
     if (m.kind == MESH_ARRAYS) return md->lin_nz;
     return 0;
 }
@@ -804,7 +805,7 @@ int cmdg_hevi_create(cmdg_model* model, double dt, int split_explicit_implicit, 
     const Mesh& m = *md->mesh;
     const int nz = stack_height(md);
     if (nz <= 0) {
-        set_error("HEVI needs wall-bounded element stacks (a cubed shell, or a brick non-periodic in z)");
+        set_error("HEVI needs wall-bounded element stacks (a cubed shell, or a brick non-periodic in z in column order)");
         return CMDG_ERR_UNSUPPORTED;
     }
     if (m.N < 2 || m.N > 5) {

@@ -113,20 +113,39 @@ int build_brick(const cmdg_brick_desc* d, Mesh* m, int topology) {
     m->emetric.assign(nelem * 3, 0.0);
     m->nbr.assign(nelem * NBR_STRIDE, 0);
     const int nx = d->ne[0], ny = d->ne[1], nz = d->ne[2];
-    // columns stay contiguous (vertical index fastest); their order is x then
-    // y, or the reference's StackedBrickTopology order
+    // element numbering: columns contiguous (vertical index fastest) in x-then-y
+    // order or in the reference's StackedBrickTopology order, or every
+    // element along BrickTopology's Hilbert curve (no contiguous columns)
     m->topology = topology;
-    int rc = brick_column_order(*d, topology, m->col_at);
-    if (rc) return rc;
-    std::vector<int> col_pos(m->col_at.size());
-    for (size_t h = 0; h < m->col_at.size(); ++h) col_pos[m->col_at[h]] = (int)h;
+    std::vector<int64_t> eid_of((size_t)nelem);  // element id of library index iz + nz (ix + nx iy)
+    if (topology == CMDG_TOPOLOGY_BRICK) {
+        std::vector<int64_t> perm((size_t)nelem);
+        int rc = cmdg_brick_element_order(d, CMDG_TOPOLOGY_BRICK, perm.data());
+        if (rc) return rc;
+        for (int64_t p = 0; p < nelem; ++p) eid_of[(size_t)perm[p]] = p;
+        m->col_at.clear();
+    } else {
+        int rc = brick_column_order(*d, topology, m->col_at);
+        if (rc) return rc;
+        std::vector<int> col_pos(m->col_at.size());
+        for (size_t h = 0; h < m->col_at.size(); ++h) col_pos[m->col_at[h]] = (int)h;
+        for (int iy = 0; iy < ny; ++iy)
+            for (int ix = 0; ix < nx; ++ix)
+                for (int iz = 0; iz < nz; ++iz)
+                    eid_of[(size_t)iz + (size_t)nz * ((size_t)ix + (size_t)nx * iy)] =
+                        (int64_t)iz + (int64_t)nz * (int64_t)col_pos[(size_t)ix + (size_t)nx * iy];
+    }
     auto eid = [&](int ix, int iy, int iz) {
-        return (int64_t)iz + (int64_t)nz * (int64_t)col_pos[(size_t)ix + (size_t)nx * iy];
+        return eid_of[(size_t)iz + (size_t)nz * ((size_t)ix + (size_t)nx * iy)];
     };
+    m->ijk.assign((size_t)nelem * 3, 0);
     for (int iy = 0; iy < ny; ++iy)
         for (int ix = 0; ix < nx; ++ix)
             for (int iz = 0; iz < nz; ++iz) {
                 int64_t e = eid(ix, iy, iz);
+                m->ijk[(size_t)e * 3 + 0] = ix;
+                m->ijk[(size_t)e * 3 + 1] = iy;
+                m->ijk[(size_t)e * 3 + 2] = iz;
                 int idx[3] = {ix, iy, iz};
                 for (int dd = 0; dd < 3; ++dd) {
                     double a = blend(d->lo[dd], d->hi[dd], d->ne[dd], idx[dd]);

@@ -17,16 +17,18 @@
 namespace cmdg {
 namespace {
 
-__device__ __forceinline__ int node_level(int64_t e, int node, int nz, int Nq, int Nfp) {
-    return (int)(e % nz) * Nq + node / Nfp;
+// level row of a node: the element's vertical index (entry 6 of its
+// neighbour row, so any element order works) times Nq plus the node's k
+__device__ __forceinline__ int node_level(int64_t e, int node, const int* nbr, int Nq, int Nfp) {
+    return __ldg(nbr + (size_t)e * NBR_STRIDE + 6) * Nq + node / Nfp;
 }
 
 // reference value of field s at a node: per-node table (curvilinear meshes) or level row
 __device__ __forceinline__ double ref_value(const double* lvl, const double* refn, int64_t e, int node, int s,
-                                            int Np, int nz, int Nq) {
+                                            int Np, const int* nbr, int Nq) {
     if (s != 0 && s != 4) return 0.0;
     if (refn) return refn[((size_t)e * 2 + (s == 4)) * Np + node];
-    const double* L = lvl + (size_t)node_level(e, node, nz, Nq, Nq * Nq) * LV_NFIELDS;
+    const double* L = lvl + (size_t)node_level(e, node, nbr, Nq, Nq * Nq) * LV_NFIELDS;
     return (s == 0) ? L[LV_RHO_REF] : L[LV_RHOE_REF];
 }
 
@@ -36,7 +38,7 @@ __device__ __forceinline__ double ref_value(const double* lvl, const double* ref
 // address space: the kernel then reads it over the host link.
 // Qp = FP32 perturbation Q - q_ref; Qd (if not NULL) = the FP64 perturbation
 __global__ void to_perturbation_kernel(float* __restrict__ Qp, double* __restrict__ Qd, const double* __restrict__ Q,
-                                       const double* lvl, const double* refn, int64_t nelem, int Np, int Nq, int nz) {
+                                       const double* lvl, const double* refn, int64_t nelem, int Np, int Nq, const int* nbr) {
     for (int64_t e = blockIdx.x; e < nelem; e += gridDim.x)
         for (int node = threadIdx.x; node < Np; node += blockDim.x) {
             const size_t base = (size_t)e * NSTATE * Np + node;
@@ -45,7 +47,7 @@ __global__ void to_perturbation_kernel(float* __restrict__ Qp, double* __restric
             for (int s = 0; s < NSTATE; ++s) v[s] = Q[base + (size_t)s * Np];
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s) {
-                const double d = v[s] - ref_value(lvl, refn, e, node, s, Np, nz, Nq);
+                const double d = v[s] - ref_value(lvl, refn, e, node, s, Np, nbr, Nq);
                 Qp[base + (size_t)s * Np] = (float)d;
                 if (Qd) Qd[base + (size_t)s * Np] = d;
             }
@@ -53,7 +55,7 @@ __global__ void to_perturbation_kernel(float* __restrict__ Qp, double* __restric
 }
 
 __global__ void from_perturbation_kernel(double* __restrict__ Q, const float* __restrict__ Qp, const double* lvl,
-                                         const double* refn, int64_t nelem, int Np, int Nq, int nz) {
+                                         const double* refn, int64_t nelem, int Np, int Nq, const int* nbr) {
     for (int64_t e = blockIdx.x; e < nelem; e += gridDim.x)
         for (int node = threadIdx.x; node < Np; node += blockDim.x) {
             const size_t base = (size_t)e * NSTATE * Np + node;
@@ -62,7 +64,7 @@ __global__ void from_perturbation_kernel(double* __restrict__ Q, const float* __
             for (int s = 0; s < NSTATE; ++s) v[s] = Qp[base + (size_t)s * Np];
 #pragma unroll
             for (int s = 0; s < NSTATE; ++s)
-                Q[base + (size_t)s * Np] = ref_value(lvl, refn, e, node, s, Np, nz, Nq) + (double)v[s];
+                Q[base + (size_t)s * Np] = ref_value(lvl, refn, e, node, s, Np, nbr, Nq) + (double)v[s];
         }
 }
 
@@ -89,7 +91,7 @@ __device__ __forceinline__ dd two_prod(double a, double b) {
 // brick element, or the per-node M of a curvilinear mesh (mnode != NULL).
 template <bool MIXED>
 __global__ void weighted_sum_kernel(const void* Qv, int field, const double* emetric, const double* w, const double* lvl,
-                                    int64_t nelem, int Np, int Nq, int nz, const double* mnode, const double* refn,
+                                    int64_t nelem, int Np, int Nq, const int* nbr, const double* mnode, const double* refn,
                                     double* partial) {
     const int Nfp = Nq * Nq;
     dd acc{0.0, 0.0};
@@ -104,7 +106,7 @@ __global__ void weighted_sum_kernel(const void* Qv, int field, const double* eme
         const size_t qi = ((size_t)e * NSTATE + field) * Np + node;
         double qv;
         if (MIXED) {
-            const double ref = ref_value(lvl, refn, e, node, field, Np, nz, Nq);
+            const double ref = ref_value(lvl, refn, e, node, field, Np, nbr, Nq);
             // sum M*ref + M*q' as two exact products
             acc = dd_add(acc, two_prod(M, ref));
             qv = (double)static_cast<const float*>(Qv)[qi];
@@ -138,7 +140,7 @@ __global__ void weighted_sum_kernel(const void* Qv, int field, const double* eme
 // geo (grid-arrays meshes): per-node kernel geometry whose KG_DCRHO plane holds
 // the node's pressure coefficient; otherwise the level row's
 __global__ void courant_kernel(const double* __restrict__ Q, const double* emetric, const double* xi, const double* lvl,
-                               Physics ph, int64_t nelem, int Np, int Nq, int nz, const double* dxmin,
+                               Physics ph, int64_t nelem, int Np, int Nq, const int* nbr, const double* dxmin,
                                const double* geo, double* partial) {
     const int Nfp = Nq * Nq;
     double best = 0.0;
@@ -159,7 +161,7 @@ __global__ void courant_kernel(const double* __restrict__ Q, const double* emetr
                 if (a < Nq - 1) md = fmin(md, 0.5 * h * (xi[a + 1] - xi[a]));
             }
         }
-        const double* L = lvl + (size_t)node_level(e, node, nz, Nq, Nfp) * LV_NFIELDS;
+        const double* L = lvl + (size_t)node_level(e, node, nbr, Nq, Nfp) * LV_NFIELDS;
         double q[NSTATE];
         for (int s = 0; s < NSTATE; ++s) q[s] = Q[((size_t)e * NSTATE + s) * Np + node];
         const double rinv = 1.0 / q[0];
@@ -229,7 +231,7 @@ void release_quad(const Model* md) {
 int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s, double* Qd) {
     const Mesh& m = *md->mesh;
     const unsigned grid = (unsigned)std::min<int64_t>(m.nelem, CONVERT_CTAS);
-    to_perturbation_kernel<<<grid, 128, 0, s>>>(Qp, Qd, Q, md->d_lvl64, md->d_ref64, m.nelem, m.Np, m.Nq, m.nz);
+    to_perturbation_kernel<<<grid, 128, 0, s>>>(Qp, Qd, Q, md->d_lvl64, md->d_ref64, m.nelem, m.Np, m.Nq, m.d_nbr);
     CMDG_CUDA_CHECK(cudaGetLastError());
     return CMDG_OK;
 }
@@ -237,7 +239,7 @@ int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s
 int launch_from_perturbation(Model* md, double* Q, const float* Qp, cudaStream_t s) {
     const Mesh& m = *md->mesh;
     const unsigned grid = (unsigned)std::min<int64_t>(m.nelem, CONVERT_CTAS);
-    from_perturbation_kernel<<<grid, 128, 0, s>>>(Q, Qp, md->d_lvl64, md->d_ref64, m.nelem, m.Np, m.Nq, m.nz);
+    from_perturbation_kernel<<<grid, 128, 0, s>>>(Q, Qp, md->d_lvl64, md->d_ref64, m.nelem, m.Np, m.Nq, m.d_nbr);
     CMDG_CUDA_CHECK(cudaGetLastError());
     return CMDG_OK;
 }
@@ -263,11 +265,11 @@ int weighted_sums(Model* md, const void* Q, bool mixed, int nfields, const int* 
         CMDG_ARG_CHECK(fields[f] >= 0 && fields[f] < NSTATE, "field index %d out of range", fields[f]);
         if (mixed)
             weighted_sum_kernel<true><<<RED_BLOCKS, RED_THREADS, 0, s>>>(Q, fields[f], m.d_emetric, dq.w, md->d_lvl64,
-                                                                        m.nelem, m.Np, m.Nq, m.nz, md->d_mass,
+                                                                        m.nelem, m.Np, m.Nq, m.d_nbr, md->d_mass,
                                                                         md->d_ref64, md->d_red);
         else
             weighted_sum_kernel<false><<<RED_BLOCKS, RED_THREADS, 0, s>>>(Q, fields[f], m.d_emetric, dq.w, md->d_lvl64,
-                                                                         m.nelem, m.Np, m.Nq, m.nz, md->d_mass,
+                                                                         m.nelem, m.Np, m.Nq, m.d_nbr, md->d_mass,
                                                                         md->d_ref64, md->d_red);
         CMDG_CUDA_CHECK(cudaGetLastError());
         CMDG_CUDA_CHECK(cudaMemcpyAsync(h.data(), md->d_red, sizeof(double) * 2 * RED_BLOCKS, cudaMemcpyDeviceToHost, s));
@@ -286,7 +288,7 @@ int courant_dt(Model* md, const double* Q, double CFL, double* dt, cudaStream_t 
     if ((rc = quad(md, dq))) return rc;
     const Mesh& m = *md->mesh;
     courant_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(Q, m.d_emetric, dq.xi, md->d_lvl64, md->ph, m.nelem, m.Np, m.Nq,
-                                                     m.nz, md->d_dxmin,
+                                                     m.d_nbr, md->d_dxmin,
                                                      m.kind == MESH_ARRAYS ? md->d_geo64 : nullptr, md->d_red);
     CMDG_CUDA_CHECK(cudaGetLastError());
     std::vector<double> h(RED_BLOCKS);

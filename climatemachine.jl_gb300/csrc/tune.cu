@@ -17,17 +17,17 @@ struct Candidate {
 namespace cmdg {
 
 // The element of every CTA of the cluster kernel: clusters of CL adjacent
-// elements of a stacked brick (2 x 2 x 2 in x, y, z for CL = 8, 2 x 1 x 2 for
-// 4, 1 x 1 x 2 for 2), cluster rank bit 0 = upper in z, bit 1 = upper in x,
-// bit 2 = upper in y; clusters ordered z fastest, then x, then y.  Needs an
-// inviscid brick in stacked order whose element counts are even in the
-// directions the cluster spans.
+// elements of a brick (2 x 2 x 2 in x, y, z for CL = 8, 2 x 1 x 2 for 4,
+// 1 x 1 x 2 for 2), cluster rank bit 0 = upper in z, bit 1 = upper in x,
+// bit 2 = upper in y; clusters ordered z fastest, then x, then y, whatever
+// the mesh's element numbering.  Needs an inviscid brick whose element
+// counts are even in the directions the cluster spans.
 int build_cluster_map(Model* md, int CL) {
     const Mesh& m = *md->mesh;
     CMDG_ARG_CHECK(CL == 2 || CL == 4 || CL == 8, "cluster size must be 2, 4 or 8, got %d", CL);
-    if (m.kind != MESH_BRICK || m.col_at.empty() || md->prm.turbulence != CMDG_TURB_NONE ||
+    if (m.kind != MESH_BRICK || m.ijk.empty() || md->prm.turbulence != CMDG_TURB_NONE ||
         md->prm.hyperdiffusion != CMDG_HYPER_NONE) {
-        set_error("the cluster kernel runs inviscid models on bricks in stacked (column) order");
+        set_error("the cluster kernel runs inviscid models on bricks");
         return CMDG_ERR_UNSUPPORTED;
     }
     const int nx = m.desc.ne[0], ny = m.desc.ne[1], nz = m.desc.ne[2];
@@ -37,8 +37,10 @@ int build_cluster_map(Model* md, int CL) {
         return CMDG_ERR_UNSUPPORTED;
     }
     const int sx = CL >= 4 ? 2 : 1, sy = CL == 8 ? 2 : 1;
-    std::vector<int> col_of((size_t)nx * ny, -1);
-    for (size_t h = 0; h < m.col_at.size(); ++h) col_of[m.col_at[h]] = (int)h;
+    std::vector<int> elem_at((size_t)m.nelem, -1);  // element at library index iz + nz (ix + nx iy)
+    for (int64_t e = 0; e < m.nelem; ++e)
+        elem_at[(size_t)m.ijk[(size_t)e * 3 + 2] +
+                (size_t)nz * ((size_t)m.ijk[(size_t)e * 3 + 0] + (size_t)nx * m.ijk[(size_t)e * 3 + 1])] = (int)e;
     std::vector<int> map((size_t)m.nelem);
     size_t b = 0;
     for (int by = 0; by < ny / sy; ++by)
@@ -48,12 +50,7 @@ int build_cluster_map(Model* md, int CL) {
                     const int iz = 2 * bz + (r & 1);
                     const int ix = sx * bx + (CL >= 4 ? (r >> 1) & 1 : 0);
                     const int iy = sy * by + (CL == 8 ? (r >> 2) & 1 : 0);
-                    const int h = col_of[(size_t)ix + (size_t)nx * iy];
-                    if (h < 0) {
-                        set_error("cluster map: column (%d, %d) missing from the mesh", ix, iy);
-                        return CMDG_ERR_STATE;
-                    }
-                    map[b++] = iz + nz * h;
+                    map[b++] = elem_at[(size_t)iz + (size_t)nz * ((size_t)ix + (size_t)nx * iy)];
                 }
     if (md->d_cl_elem) cudaFree(md->d_cl_elem);
     md->d_cl_elem = nullptr;
@@ -111,7 +108,7 @@ extern "C" int cmdg_model_autotune(cmdg_model* model, int reps, double* h_ms, in
         double* h = reinterpret_cast<double*>(host.data());
         for (int64_t e = 0; e < m.nelem; ++e)
             for (int node = 0; node < m.Np; ++node) {
-                const int lev = (int)(e % m.nz) * m.Nq + node / m.Nfp;
+                const int lev = m.nbr[(size_t)e * NBR_STRIDE + 6] * m.Nq + node / m.Nfp;
                 const double* L = &md->lvl64[(size_t)lev * LV_NFIELDS];
                 const bool ref = md->prm.ref_state != 0;
                 h[((size_t)e * NSTATE + 0) * m.Np + node] = ref ? L[LV_RHO_REF] : 1.0;

@@ -20,8 +20,8 @@
  *   - Element ordering of generated brick meshes is "stacked": the vertical
  *     element index is fastest, then x, then y (columns contiguous, as in
  *     StackedBrickTopology, src/Numerics/Mesh/Topologies.jl:632, whose
- *     columns follow the Hilbert curve instead; cmdg_mesh_create_brick_ordered
- *     builds that order).
+ *     columns follow the Hilbert curve instead); cmdg_mesh_create_brick_ordered
+ *     builds StackedBrickTopology's or BrickTopology's order instead.
  */
 #ifndef CMDG_H
 #define CMDG_H
@@ -143,11 +143,13 @@ int cmdg_brick_element_order(const cmdg_brick_desc* desc, int topology, int64_t*
 
 /* A brick mesh whose elements are numbered in the reference's order, so
  * states in that order need no permutation: topology CMDG_TOPOLOGY_LIBRARY
- * (the same mesh as cmdg_mesh_create_brick) or CMDG_TOPOLOGY_STACKED_BRICK
+ * (the same mesh as cmdg_mesh_create_brick), CMDG_TOPOLOGY_STACKED_BRICK
  * (columns along the 2D Hilbert curve; the bricks of AtmosLESConfiguration,
- * src/Driver/driver_configs.jl:213).  CMDG_TOPOLOGY_BRICK is refused with
- * CMDG_ERR_UNSUPPORTED: its columns are not contiguous, which the
- * per-level tables assume; such a grid runs through cmdg_mesh_create_arrays. */
+ * src/Driver/driver_configs.jl:213) or CMDG_TOPOLOGY_BRICK (every element
+ * along the 3D Hilbert curve).  Every kernel reads an element's vertical
+ * index from its neighbour row, so all three orders run the same kernels
+ * with the same per-level tables; only HEVI, whose column solves need
+ * contiguous columns, refuses a CMDG_TOPOLOGY_BRICK mesh (CMDG_ERR_UNSUPPORTED). */
 int cmdg_mesh_create_brick_ordered(const cmdg_brick_desc* desc, int topology, cmdg_mesh** out);
 /* Builds a stacked cubed-shell mesh: curvilinear geometry with the
  * curl-invariant metric terms.  Replaces StackedCubedSphereTopology +
