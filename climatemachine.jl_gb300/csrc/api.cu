@@ -569,7 +569,6 @@ int cmdg_gradient_flux(cmdg_model* model, void* d_gf, const void* d_Q, void* str
     CMDG_ARG_CHECK(d_gf != nullptr && d_Q != nullptr, "NULL buffer");
     CMDG_ARG_CHECK(model->m.prm.turbulence != CMDG_TURB_NONE, "the model has no diffusive terms");
     CMDG_ARG_CHECK(model->m.mesh->kind == MESH_BRICK, "cmdg_gradient_flux exposes the brick gradient-flux layout");
-    CMDG_ARG_CHECK(model->m.mesh->kind == MESH_BRICK, "the diffusive passes run on brick meshes");
     return launch_gradient(&model->m, d_Q, d_gf, (cudaStream_t)stream);
 }
 

@@ -75,6 +75,9 @@ enum ViscLevelField {
 
 // gradient-flux words per node: grad h_tot (3), S = sym(grad u) (6), N^2 (Smagorinsky)
 constexpr int NGF = 10;
+// second-order flux words per node on bricks: F2[d][s] of fields s = 1..4 in
+// the three directions, word 4 d + s - 1
+constexpr int NF2 = 12;
 
 // Physical constants in the form the kernels use them.
 struct Physics {
@@ -281,9 +284,10 @@ int check_fused_stepping(const Model* md);
 // array on the current device, looked up when a model is created
 int noalloc_stage_address(void** out);
 
-// diffusive passes (viscous.cu): gradient flux of Qin into md->d_gf, then the
-// stage kernel with second-order fluxes
-int launch_gradient(Model* md, const void* Qin, void* gf_out, cudaStream_t s);
+// diffusive passes (viscous.cu): gradient flux of Qin (NGF words per node;
+// with flux, the second-order flux rows it gives, NF2 words) into gf_out,
+// then the stage kernel with second-order fluxes
+int launch_gradient(Model* md, const void* Qin, void* gf_out, cudaStream_t s, bool flux = false);
 int launch_viscous_stage(Model* md, const LaunchArgs& a, cudaStream_t s);
 
 // hyperdiffusion (hyper.cu): reference rows and buffers, the three passes of

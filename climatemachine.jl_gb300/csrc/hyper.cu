@@ -463,7 +463,7 @@ int launch_hyper_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
     int rc = launch_hyper_passes(md, a.Qin, md->d_hd, s);
     if (rc) return rc;
     const int turb = md->prm.turbulence;
-    if (turb != CMDG_TURB_NONE && (rc = launch_gradient(md, a.Qin, md->d_gf, s))) return rc;
+    if (turb != CMDG_TURB_NONE && (rc = launch_gradient(md, a.Qin, md->d_gf, s, true))) return rc;
     const KParams P = make_params(md, a);
     const bool mixed = md->precision == CMDG_MIXED;
     cudaError_t err;

@@ -6,6 +6,7 @@
 // such elements (up to rounding).  Reference-state, geopotential and their
 // DG derivatives depend only on the height of a node on a brick, so they are
 // tabulated per vertical node level instead of per node.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -350,8 +351,10 @@ int init_viscous_tables(Model* md) {
     CMDG_CUDA_CHECK(cudaMemcpy(md->d_lvv32, v32.data(), sizeof(float) * v32.size(), cudaMemcpyHostToDevice));
     if (p.turbulence != CMDG_TURB_NONE) {
         const size_t elt = md->precision == CMDG_MIXED ? sizeof(float) : sizeof(double);
-        CMDG_CUDA_CHECK(cudaMalloc(&md->d_gf, (size_t)m.nelem * NGF * m.Np * elt));
-        CMDG_CUDA_CHECK(cudaMemset(md->d_gf, 0, (size_t)m.nelem * NGF * m.Np * elt));
+        // the stages' gradient pass writes the NF2 second-order flux words
+        const size_t words = std::max(NGF, NF2);
+        CMDG_CUDA_CHECK(cudaMalloc(&md->d_gf, (size_t)m.nelem * words * m.Np * elt));
+        CMDG_CUDA_CHECK(cudaMemset(md->d_gf, 0, (size_t)m.nelem * words * m.Np * elt));
     }
     return CMDG_OK;
 }

@@ -30,7 +30,14 @@
 namespace cmdg {
 namespace {
 
-template <int N, typename R, bool MIXED, bool SMAG>
+// FLUX: instead of the NGF gradient-flux words, write the second-order flux
+// rows F2[d][1..4] they give at the node (NF2 words, word 4 d + s - 1), which
+// is all the viscous stage kernel needs of them: the stage then evaluates
+// the closure once per node here instead of at its nodes and again at every
+// face node for the neighbour, and gathers 4 words per neighbour face node
+// instead of NGF.  The neighbour's flux carries its own element's filter
+// width, as the reference's per-node auxiliary Delta does.
+template <int N, typename R, bool MIXED, bool SMAG, bool FLUX>
 __global__ void __launch_bounds__(VDims<N>::NT) gradient_kernel(const KParams P, const void* Qv, R* __restrict__ gf) {
     using Dm = VDims<N>;
     constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, NFN = 6 * Nfp;
@@ -175,38 +182,60 @@ __global__ void __launch_bounds__(VDims<N>::NT) gradient_kernel(const KParams P,
         out[6] = g2[1];
         out[7] = (g3[1] + g2[2]) / R(2);
         out[8] = g3[2];
-        out[9] = SMAG ? (g3[4] * load_level<R>(P, lev).gphiz) / thv : R(0);
-        R* o = gf + (size_t)e * NGF * Np + t;
+        const Level<R> lv = load_level<R>(P, lev);
+        out[9] = SMAG ? (g3[4] * lv.gphiz) / thv : R(0);
+        if (FLUX) {
+            const R rho = MIXED ? lv.rho_ref + q[0] : q[0];
+            const R ru[3] = {q[1], q[2], q[3]};
+            // Smagorinsky filter width, lengthscale = 2 / (cbrt(det dxi/dx) N) (src/Numerics/Mesh/Geometry.jl:121-122)
+            const R Delta = R(2) / (cbrt(xi[0] * xi[1] * xi[2]) * R(N));
+            R F2[3][NSTATE];
+            flux2<R, SMAG ? CMDG_TURB_SMAGORINSKY : CMDG_TURB_CONSTANT>(P, rho, rcp_r(rho), ru, out,
+                                                                      lv.gphiz / VConst<R>::grav(P), Delta, F2);
+            R* o = gf + (size_t)e * NF2 * Np + t;
 #pragma unroll
-        for (int s = 0; s < NGF; ++s) o[s * Np] = out[s];
+            for (int d = 0; d < 3; ++d)
+#pragma unroll
+                for (int s = 1; s < NSTATE; ++s) o[(4 * d + s - 1) * Np] = F2[d][s];
+        } else {
+            R* o = gf + (size_t)e * NGF * Np + t;
+#pragma unroll
+            for (int s = 0; s < NGF; ++s) o[s * Np] = out[s];
+        }
     }
 }
 
 
-template <int N, typename R, bool MIXED>
-cudaError_t launch_grad_typed(const KParams& P, const void* Q, void* gf, int turb, cudaStream_t s) {
+template <int N, typename R, bool MIXED, bool SMAG, bool FLUX>
+cudaError_t launch_grad_kernel(const KParams& P, const void* Q, void* gf, cudaStream_t s) {
     constexpr int Nq = N + 1, Nfp = Nq * Nq, Np = Nq * Nfp;
     constexpr size_t bytes = sizeof(R) * (2 * planar_pad<R>(5 * Np) + planar_pad<R>(30 * Nfp) + Nq * Nq);
+    auto k = gradient_kernel<N, R, MIXED, SMAG, FLUX>;
     cudaError_t e;
-    if (turb == CMDG_TURB_SMAGORINSKY) {
-        if ((e = opt_in(gradient_kernel<N, R, MIXED, true>, bytes)) != cudaSuccess) return e;
-        gradient_kernel<N, R, MIXED, true><<<P.nelem, VDims<N>::NT, bytes, s>>>(P, Q, static_cast<R*>(gf));
-    } else {
-        if ((e = opt_in(gradient_kernel<N, R, MIXED, false>, bytes)) != cudaSuccess) return e;
-        gradient_kernel<N, R, MIXED, false><<<P.nelem, VDims<N>::NT, bytes, s>>>(P, Q, static_cast<R*>(gf));
-    }
+    if ((e = opt_in(k, bytes)) != cudaSuccess) return e;
+    k<<<P.nelem, VDims<N>::NT, bytes, s>>>(P, Q, static_cast<R*>(gf));
     return cudaGetLastError();
 }
 
+template <int N, typename R, bool MIXED>
+cudaError_t launch_grad_typed(const KParams& P, const void* Q, void* gf, int turb, bool flux, cudaStream_t s) {
+    if (turb == CMDG_TURB_SMAGORINSKY)
+        return flux ? launch_grad_kernel<N, R, MIXED, true, true>(P, Q, gf, s)
+                    : launch_grad_kernel<N, R, MIXED, true, false>(P, Q, gf, s);
+    return flux ? launch_grad_kernel<N, R, MIXED, false, true>(P, Q, gf, s)
+                : launch_grad_kernel<N, R, MIXED, false, false>(P, Q, gf, s);
+}
+
 template <int N>
-cudaError_t launch_grad_N(const KParams& P, const void* Q, void* gf, bool mixed, int turb, cudaStream_t s) {
-    return mixed ? launch_grad_typed<N, float, true>(P, Q, gf, turb, s)
-                 : launch_grad_typed<N, double, false>(P, Q, gf, turb, s);
+cudaError_t launch_grad_N(const KParams& P, const void* Q, void* gf, bool mixed, int turb, bool flux,
+                          cudaStream_t s) {
+    return mixed ? launch_grad_typed<N, float, true>(P, Q, gf, turb, flux, s)
+                 : launch_grad_typed<N, double, false>(P, Q, gf, turb, flux, s);
 }
 
 }  // namespace
 
-int launch_gradient(Model* md, const void* Qin, void* gf_out, cudaStream_t s) {
+int launch_gradient(Model* md, const void* Qin, void* gf_out, cudaStream_t s, bool flux) {
     const Mesh& m = *md->mesh;
     LaunchArgs a;
     a.Qin = Qin;
@@ -219,10 +248,10 @@ int launch_gradient(Model* md, const void* Qin, void* gf_out, cudaStream_t s) {
     const int turb = md->prm.turbulence;
     cudaError_t err;
     switch (m.N) {
-        case 2: err = launch_grad_N<2>(P, Qin, gf_out, mixed, turb, s); break;
-        case 3: err = launch_grad_N<3>(P, Qin, gf_out, mixed, turb, s); break;
-        case 4: err = launch_grad_N<4>(P, Qin, gf_out, mixed, turb, s); break;
-        case 5: err = launch_grad_N<5>(P, Qin, gf_out, mixed, turb, s); break;
+        case 2: err = launch_grad_N<2>(P, Qin, gf_out, mixed, turb, flux, s); break;
+        case 3: err = launch_grad_N<3>(P, Qin, gf_out, mixed, turb, flux, s); break;
+        case 4: err = launch_grad_N<4>(P, Qin, gf_out, mixed, turb, flux, s); break;
+        case 5: err = launch_grad_N<5>(P, Qin, gf_out, mixed, turb, flux, s); break;
         default: set_error("no gradient kernel for N=%d", m.N); return CMDG_ERR_UNSUPPORTED;
     }
     if (err != cudaSuccess) {
@@ -234,8 +263,9 @@ int launch_gradient(Model* md, const void* Qin, void* gf_out, cudaStream_t s) {
 
 int launch_viscous_stage(Model* md, const LaunchArgs& a, cudaStream_t s) {
     const Mesh& m = *md->mesh;
-    // gradient pass of this stage's input state, then the tendency / stage update
-    int rc = launch_gradient(md, a.Qin, md->d_gf, s);
+    // gradient pass of this stage's input state (its second-order flux rows),
+    // then the tendency / stage update
+    int rc = launch_gradient(md, a.Qin, md->d_gf, s, true);
     if (rc) return rc;
     const KParams P = make_params(md, a);
     const bool mixed = md->precision == CMDG_MIXED;

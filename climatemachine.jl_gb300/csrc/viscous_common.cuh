@@ -199,12 +199,6 @@ __device__ __forceinline__ void flux2(const KParams& P, R rho, R rinv, const R r
     }
 }
 
-template <typename R>
-__device__ __forceinline__ void ld_gf(const R* gf, size_t base, int Np, R out[NGF]) {
-#pragma unroll
-    for (int s = 0; s < NGF; ++s) out[s] = gf[base + (size_t)s * Np];
-}
-
 // Hyperdiffusive flux rows (HyperdiffViscousFlux, HyperdiffEnthalpyFlux;
 // src/Atmos/Model/tendencies_momentum.jl:51-54, tendencies_energy.jl:40-48)
 // added to F: hd holds nu grad^3 of (u, v, h_tot) as words 3 c + d (the
@@ -266,12 +260,17 @@ __global__ void __launch_bounds__(VDims<N>::NT, (sizeof(R) == 4 ? (HYPER ? 4 : 6
     };
 
     const size_t ebase = (size_t)e * ESTRIDE + t;
-    R q[NSTATE], g[NGF], hd[9];
+    R q[NSTATE], f2[NF2], hd[9];
     double dq_old[NSTATE];
     if (node_thread) {
 #pragma unroll
         for (int s = 0; s < NSTATE; ++s) q[s] = Qin[ebase + s * Np];
-        if (VISC) ld_gf<R>(GF, (size_t)e * NGF * Np + t, Np, g);
+        if (VISC) {
+            // the node's second-order flux rows, formed by the gradient pass
+            const R* g = GF + (size_t)e * NF2 * Np + t;
+#pragma unroll
+            for (int w = 0; w < NF2; ++w) f2[w] = g[(size_t)w * Np];
+        }
         if (HYPER) {
 #pragma unroll
             for (int w = 0; w < 9; ++w) hd[w] = HDS[(size_t)e * 9 * Np + w * Np + t];
@@ -282,13 +281,18 @@ __global__ void __launch_bounds__(VDims<N>::NT, (sizeof(R) == 4 ? (HYPER ? 4 : 6
         }
     }
     const int nb = face_thread ? __ldg(nbr + f) : -1;
-    R qp[NSTATE], gp[NGF], hdp[3];
+    R qp[NSTATE], f2p[4], hdp[3];
     int ezp = ez;
     if (nb >= 0) {
         const R* qn = Qin + (size_t)nb * ESTRIDE + vP;
 #pragma unroll
         for (int s = 0; s < NSTATE; ++s) qp[s] = qn[s * Np];
-        if (VISC) ld_gf<R>(GF, (size_t)nb * NGF * Np + vP, Np, gp);
+        if (VISC) {
+            // the neighbour's second-order flux row normal to the face
+            const R* gn = GF + (size_t)nb * NF2 * Np + (size_t)(4 * fd) * Np + vP;
+#pragma unroll
+            for (int w = 0; w < 4; ++w) f2p[w] = gn[(size_t)w * Np];
+        }
         if (HYPER) {
             // the neighbour's nu grad^3 components normal to the face
             const R* hn = HDS + (size_t)nb * 9 * Np + (size_t)fd * Np + vP;
@@ -301,8 +305,6 @@ __global__ void __launch_bounds__(VDims<N>::NT, (sizeof(R) == 4 ? (HYPER ? 4 : 6
         }
     }
     const R xi[3] = {KConst<R>::metric(P, e, 0), KConst<R>::metric(P, e, 1), KConst<R>::metric(P, e, 2)};
-    // Smagorinsky filter width, lengthscale = 2 / (cbrt(det dxi/dx) N) (src/Numerics/Mesh/Geometry.jl:121-122)
-    const R Delta = R(2) / (cbrt(xi[0] * xi[1] * xi[2]) * R(N));
 
     // phase 1: node thermodynamics, total (first + second order) volume flux
     R gsrc = 0;
@@ -314,7 +316,12 @@ __global__ void __launch_bounds__(VDims<N>::NT, (sizeof(R) == 4 ? (HYPER ? 4 : 6
         R F2[3][NSTATE] = {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}};
         const R rho = MIXED ? lv.rho_ref + q[0] : q[0];
         const R ru[3] = {q[1], q[2], q[3]};
-        if (VISC) flux2<R, TURB>(P, rho, th.rinv, ru, g, lv.gphiz / VConst<R>::grav(P), Delta, F2);
+        if (VISC) {
+#pragma unroll
+            for (int dd = 0; dd < 3; ++dd)
+#pragma unroll
+                for (int s = 1; s < NSTATE; ++s) F2[dd][s] = f2[4 * dd + s - 1];
+        }
         if (HYPER) add_hyper_flux<R>(rho, ru, hd, F2);
 #pragma unroll
         for (int dd = 0; dd < 3; ++dd) {
@@ -366,10 +373,8 @@ __global__ void __launch_bounds__(VDims<N>::NT, (sizeof(R) == 4 ? (HYPER ? 4 : 6
             const R rho = MIXED ? lvp.rho_ref + qp[0] : qp[0];
             const R ru[3] = {qp[1], qp[2], qp[3]};
             if (VISC) {
-                R F2[3][NSTATE];
-                flux2<R, TURB>(P, rho, thp.rinv, ru, gp, lvp.gphiz / VConst<R>::grav(P), Delta, F2);
 #pragma unroll
-                for (int s = 0; s < NSTATE; ++s) Fp[s] += sgn * pick3(fd, F2[0][s], F2[1][s], F2[2][s]);
+                for (int s = 1; s < NSTATE; ++s) Fp[s] += sgn * f2p[s - 1];
             }
             if (HYPER) {
                 Fp[1] += sgn * (rho * hdp[0]);
