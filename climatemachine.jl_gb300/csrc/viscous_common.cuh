@@ -216,11 +216,24 @@ __device__ __forceinline__ void add_hyper_flux(R rho, const R ru[3], const R hd[
 // Stage kernel with second-order fluxes: TURB = the turbulence closure
 // (CMDG_TURB_NONE only together with HYPER), HYPER = DryBiharmonic
 // hyperdiffusion, whose state nu grad^3 (Np, 9, nelem) is read from P.hd.
+// Resident CTAs per SM the FP32 stage kernel is compiled for.  N = 4: 6
+// with a closure (measured on the Smagorinsky LES: 183 us per stage against
+// 195 us at the compiler's choice of 90 registers, 4 CTAs) and with
+// hyperdiffusion alone (64 registers; on the hyperdiffusion bubble 0.528 ms
+// per step against 0.547 ms at 5 CTAs and 0.587 ms at 4); 5 with both (72
+// registers, where 6 would spill).  N = 5 (224 threads): 4, 72 registers
+// (at 6 the closure kernels spilled 160-184 bytes).  FP64: the compiler's
+// choice.
+template <int N, typename R, int TURB, bool HYPER>
+constexpr int vstage_min_ctas() {
+    if (sizeof(R) != 4) return 1;
+    if (N == 5) return 4;
+    return (HYPER && TURB != CMDG_TURB_NONE) ? 5 : 6;
+}
+
 template <int N, typename R, bool MIXED, int MODE, int TURB, bool HYPER>
-// FP32: 6 resident CTAs per SM (measured on the Smagorinsky LES: 183 us per
-// stage against 195 us at the compiler's choice of 90 registers, 4 CTAs); 4 with
-// hyperdiffusion, whose nu grad^3 words would spill at 6
-__global__ void __launch_bounds__(VDims<N>::NT, (sizeof(R) == 4 ? (HYPER ? 4 : 6) : 1)) viscous_stage_kernel(const KParams P) {
+__global__ void __launch_bounds__(VDims<N>::NT, vstage_min_ctas<N, R, TURB, HYPER>())
+    viscous_stage_kernel(const KParams P) {
     using Dm = VDims<N>;
     constexpr int Nq = Dm::Nq, Np = Dm::Np, Nfp = Dm::Nfp, NFN = 6 * Nfp, P5N = planar_pad<R>(5 * Np);
     constexpr int ESTRIDE = NSTATE * Np;
