@@ -72,15 +72,17 @@ check(rc::Cint) =
 stream_handle() = CUDA.stream().handle
 
 """
-    CMDGModel(brick::Brick, params::AtmosParams, grid, balance_law, state_auxiliary; precision = CMDG_FP64)
+    CMDGModel(brick::Brick, params::AtmosParams, grid, balance_law, state_auxiliary;
+              precision = CMDG_FP64, topology = CMDG_TOPOLOGY_STACKED_BRICK)
 
 GPU DG model on a brick whose elements are numbered as the reference's
-`StackedBrickTopology` numbers them (columns along the 2D Hilbert curve of
-the horizontal base, each column contiguous), so `Q.data` of a grid built
-with `StackedBrickTopology` over the same ranges is passed unpermuted.  A
-`BrickTopology` grid (3D Hilbert order) goes through the grid-arrays
-constructor below.  `grid`, `balance_law` and `state_auxiliary` are kept for
-the reference's callbacks that read them.
+topology numbers them: `CMDG_TOPOLOGY_STACKED_BRICK` (the default) for a
+grid built with `StackedBrickTopology` (columns along the 2D Hilbert curve
+of the horizontal base, each column contiguous), `CMDG_TOPOLOGY_BRICK` for
+`BrickTopology` (every element along the 3D Hilbert curve), so `Q.data` of
+that grid over the same ranges is passed unpermuted.  HEVI needs the
+stacked order.  `grid`, `balance_law` and `state_auxiliary` are kept for the
+reference's callbacks that read them.
 """
 mutable struct CMDGModel{G, BL, A} <: SpaceDiscretization
     mesh::Ptr{Cvoid}
@@ -91,10 +93,10 @@ mutable struct CMDGModel{G, BL, A} <: SpaceDiscretization
 end
 
 function CMDGModel(brick::Brick, params::AtmosParams, grid, balance_law, state_auxiliary;
-                   precision = CMDG_FP64)
+                   precision = CMDG_FP64, topology = CMDG_TOPOLOGY_STACKED_BRICK)
     mesh = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:cmdg_mesh_create_brick_ordered, libcmdg), Cint, (Ref{Brick}, Cint, Ref{Ptr{Cvoid}}),
-                brick, CMDG_TOPOLOGY_STACKED_BRICK, mesh))
+                brick, Cint(topology), mesh))
     model = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:cmdg_model_create, libcmdg), Cint, (Ptr{Cvoid}, Ref{AtmosParams}, Cint, Ref{Ptr{Cvoid}}),
                 mesh[], params, precision, model))
