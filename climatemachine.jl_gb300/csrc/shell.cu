@@ -79,9 +79,17 @@ struct ShellSmem {
 // reference jump (c_L: the larger reference sound speed, the linear model's
 // Rusanov speed).  The stiff vertical acoustic terms are then applied in
 // FP64 by the linear kernel, so FP32 rounding no longer enters them.
+//
+// Resident CTAs per SM of the FP32 kernel: the inviscid one ShellDims'
+// MIN_CTAS; with hyperdiffusion alone at N = 4, 5 (72 registers; the mixed
+// GCM with horizontal DryBiharmonic steps in 0.595 ms against 0.612 ms at 4
+// and 0.629 ms at 6, which spills); 4 with a closure (24-56 bytes of
+// spills at 5) and with hyperdiffusion at other N.
 template <int N, typename R, bool MIXED, int MODE, bool HYPER, int VT, bool REM = false>
-__global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? (HYPER || VT != 0 ? 4 : ShellDims<N>::MIN_CTAS)
-                                                          : ShellDims<N>::MIN_CTAS64)
+__global__ void __launch_bounds__(ShellDims<N>::NT,
+                                  MIXED ? (HYPER && VT == 0 && N == 4 ? 5
+                                                                      : (HYPER || VT != 0 ? 4 : ShellDims<N>::MIN_CTAS))
+                                        : ShellDims<N>::MIN_CTAS64)
     shell_stage_kernel(const KParams P) {
     static_assert(!REM || (MIXED && MODE == 0 && !HYPER && VT == CMDG_TURB_NONE),
                   "the remainder form is a mixed inviscid tendency");
