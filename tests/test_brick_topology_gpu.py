@@ -93,6 +93,27 @@ def test_bubble_in_brick_order_matches_library_order(precision, kernel):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("N,ne", [(2, (3, 1, 5)), (3, (1, 3, 2)), (5, (2, 2, 1)), (3, (5, 4, 3))])
+def test_other_orders_and_degenerate_bricks_in_brick_order(N, ne, precision):
+    """Orders 2, 3 and 5, and bricks with one element in a direction (an
+    element that is its own periodic neighbour, a single element between
+    the two walls): tendency and steps bit for bit after the permutation."""
+    dg_lib, dg_ref, perm = pair(workloads.bubble_model, ne, N=N, precision=precision)
+    P = torch.from_numpy(perm).cuda()
+    Q0 = bubble_state(dg_lib.grid.coordinates(), seed=N)
+    Ql, Qr = dg_lib.init_ode_state(Q0), dg_ref.init_ode_state(Q0[perm])
+    Tl, Tr = dg_lib.new_state(torch.float64), dg_ref.new_state(torch.float64)
+    dg_lib(Tl, Ql, None, 0.0)
+    dg_ref(Tr, Qr, None, 0.0)
+    assert torch.equal(Tr, Tl[P])
+    dt = dg_lib.courant_dt(Ql, 0.4)
+    for dg, Q in ((dg_lib, Ql), (dg_ref, Qr)):
+        cmdg.dostep_(Q, cmdg.LSRK54CarpenterKennedy(dg, Q, dt=dt), None, 0.0, nsteps=2)
+    assert torch.equal(Qr, Ql[P])
+    assert dg_lib.status_word() == 0 and dg_ref.status_word() == 0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("case", ["les", "hyper"])
 def test_viscous_and_hyperdiffusive_models_in_brick_order(case, precision):
     """SmagorinskyLilly (gradient + viscous stage kernels) and DryBiharmonic
