@@ -645,8 +645,18 @@ cudaError_t launch_N(const KParams& P, bool mixed, int mode, int grid, cudaStrea
 // of that order.  The CTAs walk a list of tiles (runs of consecutive elements
 // of one member); each tile reads its member's launch parameters from global
 // memory and runs the node-kernel body with the CTA shape of its order.
+// Resident CTAs per SM: the persistent kernel's budget, except at N = 4,
+// where reading each tile's launch parameters from global memory costs
+// registers: 5 CTAs (72 registers, 20 bytes of spills) measured 1.203e11
+// DOF-stage/s on the 64-member ensemble against 1.159e11 at 6 (64
+// registers, 44 bytes of spills) and 1.17-1.19e11 at 4 (96, none).
 template <int N>
-__global__ void __launch_bounds__(Dims<N>::NT, Dims<N>::MIN_CTAS)
+constexpr int batch_min_ctas() {
+    return N == 4 ? 5 : Dims<N>::MIN_CTAS;
+}
+
+template <int N>
+__global__ void __launch_bounds__(Dims<N>::NT, batch_min_ctas<N>())
     batch_stage_kernel(const KParams* __restrict__ params, const BatchTile* __restrict__ tiles, int ntiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     for (int it = blockIdx.x; it < ntiles; it += gridDim.x) {
