@@ -39,8 +39,15 @@ struct ArraysSmem {
 // gradient pass's output join the volume flux and, with the facing node's
 // state, the central second-order interface flux; walls carry the
 // first-order flux only.
+//
+// Resident CTAs per SM of the FP32 kernel: ShellDims' MIN_CTAS, but 4 with a
+// closure at N = 4 (93-96 registers, no spills; at 6 the closure
+// kernels spilled 24-116 bytes; a mixed Smagorinsky LES of 24 x 24 x 12
+// elements through grid arrays steps in 0.762 ms against 0.766 ms).
 template <int N, typename R, bool MIXED, int MODE, int VT = CMDG_TURB_NONE>
-__global__ void __launch_bounds__(ShellDims<N>::NT, MIXED ? ShellDims<N>::MIN_CTAS : ShellDims<N>::MIN_CTAS64)
+__global__ void __launch_bounds__(ShellDims<N>::NT,
+                                  MIXED ? (VT != CMDG_TURB_NONE && N == 4 ? 4 : ShellDims<N>::MIN_CTAS)
+                                        : ShellDims<N>::MIN_CTAS64)
     arrays_stage_kernel(const KParams P) {
     constexpr bool VISC = VT != CMDG_TURB_NONE;
     using Dm = ShellDims<N>;
