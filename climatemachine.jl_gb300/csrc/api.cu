@@ -402,6 +402,10 @@ int cmdg_model_destroy(cmdg_model* model) {
     cudaFree(md.d_filter_corr);
     cudaFree(md.d_filter_ref64);
     cudaFree(md.d_mp_scratch);
+    cudaFree(md.d_host_stage);
+    for (cudaEvent_t e : md.host_ev)
+        if (e) cudaEventDestroy(e);
+    if (md.host_copy_stream) cudaStreamDestroy(md.host_copy_stream);
     cudaFree(md.d_filter_corr_node);
     cudaFree(md.d_omega);
     cudaFree(md.d_lin64);
@@ -501,6 +505,21 @@ int cmdg_lsrk54_step_mixed(cmdg_model* model, float* d_Qp, double* d_dQ, double 
     return run_steps(&model->m, d_Qp, d_dQ, dt, nsteps, (cudaStream_t)stream);
 }
 
+namespace cmdg {
+// FP64 device copy of a host-memory state, the copy stream and its events,
+// made on first use with the model's device current
+static int ensure_host_staging(Model* md) {
+    const Mesh& m = *md->mesh;
+    if (!md->host_copy_stream)
+        CMDG_CUDA_CHECK(cudaStreamCreateWithFlags(&md->host_copy_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : md->host_ev)
+        if (!e) CMDG_CUDA_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    if (!md->d_host_stage)
+        CMDG_CUDA_CHECK(cudaMalloc(&md->d_host_stage, sizeof(double) * NSTATE * m.Np * (size_t)m.nelem));
+    return CMDG_OK;
+}
+}  // namespace cmdg
+
 int cmdg_lsrk54_step_mixed_host(cmdg_model* model, double* h_Q, float* d_Qp, double* d_dQ, double t, double dt,
                                 int nsteps, void* stream) {
     int rc = check_model(model);
@@ -509,7 +528,7 @@ int cmdg_lsrk54_step_mixed_host(cmdg_model* model, double* h_Q, float* d_Qp, dou
     CMDG_ARG_CHECK(h_Q != nullptr && d_Qp != nullptr && d_dQ != nullptr, "NULL state");
     CMDG_ARG_CHECK(nsteps >= 0, "nsteps must be >= 0");
     CMDG_ARG_CHECK(std::isfinite(dt) && dt > 0, "dt must be positive and finite");
-    // the host state must be page-locked (mapped into the device's address space)
+    // the host state must be page-locked, so the copies run asynchronously on the copy engines
     cudaPointerAttributes attr;
     cudaError_t e = cudaPointerGetAttributes(&attr, h_Q);
     if (e != cudaSuccess) {
@@ -519,11 +538,53 @@ int cmdg_lsrk54_step_mixed_host(cmdg_model* model, double* h_Q, float* d_Qp, dou
     }
     CMDG_ARG_CHECK(attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr,
                    "h_Q must be page-locked host memory (cudaHostAlloc, cudaMallocHost or cudaHostRegister)");
-    double* dev_view = static_cast<double*>(attr.devicePointer);
-    const cudaStream_t s = (cudaStream_t)stream;
-    if ((rc = launch_to_perturbation(&model->m, d_Qp, dev_view, s))) return rc;
+    Model* md = &model->m;
+    const Mesh& m = *md->mesh;
+    if ((rc = ensure_host_staging(md))) return rc;
+    const cudaStream_t s = (cudaStream_t)stream, cs = md->host_copy_stream;
+    double* stage = md->d_host_stage;
+    cudaEvent_t* ev = md->host_ev;  // [0] fork, [1..K] copied in, [K+1..2K] converted out, [2K+1] join
+    const size_t per_elem = (size_t)NSTATE * m.Np;
+    auto chunk = [&](int k, int64_t& e0, int64_t& e1) {
+        e0 = m.nelem * k / HOST_CHUNKS;
+        e1 = m.nelem * (k + 1) / HOST_CHUNKS;
+    };
+    // host -> device on the copy stream, chunk by chunk, after the caller's earlier work;
+    // each chunk's conversion on the caller's stream overlaps the next chunk's copy
+    CMDG_CUDA_CHECK(cudaEventRecord(ev[0], s));
+    CMDG_CUDA_CHECK(cudaStreamWaitEvent(cs, ev[0], 0));
+    for (int k = 0; k < HOST_CHUNKS; ++k) {
+        int64_t e0, e1;
+        chunk(k, e0, e1);
+        if (e1 > e0)
+            CMDG_CUDA_CHECK(cudaMemcpyAsync(stage + e0 * per_elem, h_Q + e0 * per_elem,
+                                            (size_t)(e1 - e0) * per_elem * sizeof(double), cudaMemcpyHostToDevice,
+                                            cs));
+        CMDG_CUDA_CHECK(cudaEventRecord(ev[1 + k], cs));
+    }
+    for (int k = 0; k < HOST_CHUNKS; ++k) {
+        int64_t e0, e1;
+        chunk(k, e0, e1);
+        CMDG_CUDA_CHECK(cudaStreamWaitEvent(s, ev[1 + k], 0));
+        if ((rc = launch_to_perturbation(md, d_Qp, stage, s, nullptr, e0, e1))) return rc;
+    }
     if (nsteps > 0 && (rc = cmdg_lsrk54_step_mixed(model, d_Qp, d_dQ, t, dt, nsteps, stream))) return rc;
-    return launch_from_perturbation(&model->m, dev_view, d_Qp, s);
+    // device -> host: each converted chunk is copied back while the next converts
+    for (int k = 0; k < HOST_CHUNKS; ++k) {
+        int64_t e0, e1;
+        chunk(k, e0, e1);
+        if ((rc = launch_from_perturbation(md, stage, d_Qp, s, e0, e1))) return rc;
+        CMDG_CUDA_CHECK(cudaEventRecord(ev[1 + HOST_CHUNKS + k], s));
+        CMDG_CUDA_CHECK(cudaStreamWaitEvent(cs, ev[1 + HOST_CHUNKS + k], 0));
+        if (e1 > e0)
+            CMDG_CUDA_CHECK(cudaMemcpyAsync(h_Q + e0 * per_elem, stage + e0 * per_elem,
+                                            (size_t)(e1 - e0) * per_elem * sizeof(double), cudaMemcpyDeviceToHost,
+                                            cs));
+    }
+    // the caller's stream resumes after the last copy back
+    CMDG_CUDA_CHECK(cudaEventRecord(ev[1 + 2 * HOST_CHUNKS], cs));
+    CMDG_CUDA_CHECK(cudaStreamWaitEvent(s, ev[1 + 2 * HOST_CHUNKS], 0));
+    return CMDG_OK;
 }
 
 int cmdg_to_perturbation(cmdg_model* model, float* d_Qp, const double* d_Q, void* stream) {

@@ -78,6 +78,9 @@ constexpr int NGF = 10;
 // second-order flux words per node on bricks: F2[d][s] of fields s = 1..4 in
 // the three directions, word 4 d + s - 1
 constexpr int NF2 = 12;
+// element chunks of a host-memory state: each chunk's copy over the host
+// link overlaps the conversion of the one before it
+constexpr int HOST_CHUNKS = 4;
 
 // Physical constants in the form the kernels use them.
 struct Physics {
@@ -228,6 +231,13 @@ struct Model {
     int cl_size = 0;
     int device = -1;                 // CUDA device current when the model was created
     void* noalloc_stage = nullptr;   // device address of the allocation-free stage array on that device
+    // stepping a state held in host memory: its FP64 device copy, the stream
+    // of the host-link copies and the events that order them against the
+    // conversions on the caller's stream (fork, HOST_CHUNKS copies in,
+    // HOST_CHUNKS conversions out, join)
+    double* d_host_stage = nullptr;
+    cudaStream_t host_copy_stream = nullptr;
+    cudaEvent_t host_ev[2 * HOST_CHUNKS + 2] = {};
     // test hook of the persistent stage kernel's bounded waits: when
     // staging_skip_copies is set the kernel arms its staging barriers without
     // issuing the copies, and every wait gives up after wait_polls polls
@@ -311,8 +321,11 @@ int launch_shell_visc_gradient(Model* md, const void* Qin, void* gout, cudaStrea
 // reductions / conversions (reduce.cu)
 // Qp = FP32 perturbation of Q about the reference state; Qd, if given, the
 // FP64 perturbation
-int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s, double* Qd = nullptr);
-int launch_from_perturbation(Model* md, double* Q, const float* Qp, cudaStream_t s);
+// elements [e0, e1) only (e1 < 0: to the last element)
+int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s, double* Qd = nullptr,
+                           int64_t e0 = 0, int64_t e1 = -1);
+int launch_from_perturbation(Model* md, double* Q, const float* Qp, cudaStream_t s, int64_t e0 = 0,
+                             int64_t e1 = -1);
 int weighted_sums(Model* md, const void* Q, bool mixed, int nfields, const int* fields, double* out, cudaStream_t s);
 int courant_dt(Model* md, const double* Q, double CFL, double* dt, cudaStream_t s);
 void release_quad(const Model* md);

@@ -38,8 +38,9 @@ __device__ __forceinline__ double ref_value(const double* lvl, const double* ref
 // address space: the kernel then reads it over the host link.
 // Qp = FP32 perturbation Q - q_ref; Qd (if not NULL) = the FP64 perturbation
 __global__ void to_perturbation_kernel(float* __restrict__ Qp, double* __restrict__ Qd, const double* __restrict__ Q,
-                                       const double* lvl, const double* refn, int64_t nelem, int Np, int Nq, const int* nbr) {
-    for (int64_t e = blockIdx.x; e < nelem; e += gridDim.x)
+                                       const double* lvl, const double* refn, int64_t e_first, int64_t e_end, int Np,
+                                       int Nq, const int* nbr) {
+    for (int64_t e = e_first + blockIdx.x; e < e_end; e += gridDim.x)
         for (int node = threadIdx.x; node < Np; node += blockDim.x) {
             const size_t base = (size_t)e * NSTATE * Np + node;
             double v[NSTATE];
@@ -55,8 +56,9 @@ __global__ void to_perturbation_kernel(float* __restrict__ Qp, double* __restric
 }
 
 __global__ void from_perturbation_kernel(double* __restrict__ Q, const float* __restrict__ Qp, const double* lvl,
-                                         const double* refn, int64_t nelem, int Np, int Nq, const int* nbr) {
-    for (int64_t e = blockIdx.x; e < nelem; e += gridDim.x)
+                                         const double* refn, int64_t e_first, int64_t e_end, int Np, int Nq,
+                                         const int* nbr) {
+    for (int64_t e = e_first + blockIdx.x; e < e_end; e += gridDim.x)
         for (int node = threadIdx.x; node < Np; node += blockDim.x) {
             const size_t base = (size_t)e * NSTATE * Np + node;
             float v[NSTATE];
@@ -228,18 +230,23 @@ void release_quad(const Model* md) {
     g_quad.erase(it);
 }
 
-int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s, double* Qd) {
+int launch_to_perturbation(Model* md, float* Qp, const double* Q, cudaStream_t s, double* Qd, int64_t e0,
+                           int64_t e1) {
     const Mesh& m = *md->mesh;
-    const unsigned grid = (unsigned)std::min<int64_t>(m.nelem, CONVERT_CTAS);
-    to_perturbation_kernel<<<grid, 128, 0, s>>>(Qp, Qd, Q, md->d_lvl64, md->d_ref64, m.nelem, m.Np, m.Nq, m.d_nbr);
+    if (e1 < 0) e1 = m.nelem;
+    if (e1 <= e0) return CMDG_OK;
+    const unsigned grid = (unsigned)std::min<int64_t>(e1 - e0, CONVERT_CTAS);
+    to_perturbation_kernel<<<grid, 128, 0, s>>>(Qp, Qd, Q, md->d_lvl64, md->d_ref64, e0, e1, m.Np, m.Nq, m.d_nbr);
     CMDG_CUDA_CHECK(cudaGetLastError());
     return CMDG_OK;
 }
 
-int launch_from_perturbation(Model* md, double* Q, const float* Qp, cudaStream_t s) {
+int launch_from_perturbation(Model* md, double* Q, const float* Qp, cudaStream_t s, int64_t e0, int64_t e1) {
     const Mesh& m = *md->mesh;
-    const unsigned grid = (unsigned)std::min<int64_t>(m.nelem, CONVERT_CTAS);
-    from_perturbation_kernel<<<grid, 128, 0, s>>>(Q, Qp, md->d_lvl64, md->d_ref64, m.nelem, m.Np, m.Nq, m.d_nbr);
+    if (e1 < 0) e1 = m.nelem;
+    if (e1 <= e0) return CMDG_OK;
+    const unsigned grid = (unsigned)std::min<int64_t>(e1 - e0, CONVERT_CTAS);
+    from_perturbation_kernel<<<grid, 128, 0, s>>>(Q, Qp, md->d_lvl64, md->d_ref64, e0, e1, m.Np, m.Nq, m.d_nbr);
     CMDG_CUDA_CHECK(cudaGetLastError());
     return CMDG_OK;
 }

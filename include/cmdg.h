@@ -433,10 +433,14 @@ int cmdg_lsrk54_step_mixed(cmdg_model* model, float* d_Qp, double* d_dQ, double 
 
 /* Mixed-precision LSRK54 steps of an FP64 state h_Q (Np, 5, nelem) held in
  * page-locked host memory (cudaHostAlloc / cudaMallocHost /
- * cudaHostRegister; anything else is refused with CMDG_ERR_ARG): the device
- * reads h_Q over the host link into the FP32 perturbation d_Qp, advances
- * nsteps steps with the FP64 register d_dQ, and writes the FP64 result back
- * into h_Q, all ordered on `stream` (synchronize it before reading h_Q).
+ * cudaHostRegister; anything else is refused with CMDG_ERR_ARG): h_Q is
+ * copied over the host link into an FP64 device copy and converted to the
+ * FP32 perturbation d_Qp, nsteps steps advance it with the FP64 register
+ * d_dQ, and the FP64 result is copied back into h_Q.  The copies run on a
+ * stream of the model's own in element chunks, each overlapping the
+ * conversion of its neighbour, and are ordered after the earlier work of
+ * `stream` and before its later work (synchronize it before reading h_Q).
+ * The first call allocates the device copy (state-sized) and that stream.
  * The dostep! of a reference solver whose state lives in host memory
  * (src/Numerics/ODESolvers/LowStorageRungeKuttaMethod.jl:102-158). */
 int cmdg_lsrk54_step_mixed_host(cmdg_model* model, double* h_Q, float* d_Qp, double* d_dQ, double t, double dt,
