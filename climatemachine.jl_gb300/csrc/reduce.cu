@@ -32,10 +32,9 @@ __device__ __forceinline__ double ref_value(const double* lvl, const double* ref
     return (s == 0) ? L[LV_RHO_REF] : L[LV_RHOE_REF];
 }
 
-// One CTA per element (grid-stride over elements), one thread per node; each
-// thread issues its five loads before converting, and no index needs a
-// division.  Q may be page-locked host memory mapped into the device's
-// address space: the kernel then reads it over the host link.
+// One CTA per element of [e_first, e_end) (grid-stride over elements), one
+// thread per node; each thread issues its five loads before converting, and
+// no index needs a division.
 // Qp = FP32 perturbation Q - q_ref; Qd (if not NULL) = the FP64 perturbation
 __global__ void to_perturbation_kernel(float* __restrict__ Qp, double* __restrict__ Qd, const double* __restrict__ Q,
                                        const double* lvl, const double* refn, int64_t e_first, int64_t e_end, int Np,
