@@ -296,9 +296,9 @@ class DGModel:
 
     def lsrk54_step_host(self, h_Q: torch.Tensor, Qp: torch.Tensor, dQ: torch.Tensor, t, dt, nsteps=1):
         """Mixed-precision steps of an FP64 state in pinned host memory
-        (``h_Q.is_pinned()``): the device reads h_Q into the FP32
-        perturbation Qp, steps with the FP64 register dQ and writes the result
-        back into h_Q, ordered on the current stream."""
+        (``h_Q.is_pinned()``): h_Q is copied to the device and converted to
+        the FP32 perturbation Qp, stepped with the FP64 register dQ, and the
+        FP64 result copied back into h_Q, ordered on the current stream."""
         if not self.mixed:
             raise ValueError("lsrk54_step_host needs a mixed-precision model")
         if h_Q.device.type != "cpu" or not h_Q.is_pinned() or h_Q.dtype != torch.float64 or not h_Q.is_contiguous():

@@ -293,15 +293,25 @@ def test_persistent_kernel_bitwise_equals_one_cta_per_element(precision, grid):
     assert dg.status_word() == 0
 
 
-def test_host_state_steps_equal_device_steps():
-    """cmdg_lsrk54_step_mixed_host (the state in pinned host memory, read and
-    written by the device over the host link) gives the same bits as
-    converting on the device and stepping; pageable memory is refused."""
+@pytest.mark.parametrize("ne", [(3, 3, 3), (1, 1, 3), (1, 1, 1), (5, 1, 1)])
+def test_host_state_steps_equal_device_steps(ne):
+    """cmdg_lsrk54_step_mixed_host (the state in pinned host memory, copied
+    over the host link in element chunks that overlap the conversions)
+    gives the same bits as converting on the device and stepping, also on
+    meshes with fewer elements than chunks or a count the chunks do not
+    divide; pageable memory is refused; a step count of zero converts and
+    copies back only."""
     import ctypes
 
     from cmdg import _lib
 
-    om, dg, Q0 = make_pair("bubble", 4, (3, 3, 3), precision="mixed")
+    om, dg, Q0 = make_pair("bubble", 4, ne, precision="mixed")
+    h0 = torch.from_numpy(Q0.copy()).pin_memory()
+    Qz = dg.new_state(torch.float32)
+    dQz = torch.zeros(h0.shape, dtype=torch.float64, device="cuda")
+    dg.lsrk54_step_host(h0, Qz, dQz, 0.0, 0.05, 0)
+    torch.cuda.synchronize()
+    assert torch.equal(h0, dg.from_perturbation(dg.init_ode_state(Q0)).cpu())
     dt = 0.05
     Qp = dg.init_ode_state(Q0)
     dQ = torch.zeros(Qp.shape, dtype=torch.float64, device=Qp.device)
